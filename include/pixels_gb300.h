@@ -1,0 +1,125 @@
+/*
+ * pixels_gb300 — C ABI of the GB300 scene voxeliser.
+ *
+ * Drop-in for the reference's world-building path (paths relative to the
+ * reference project):
+ *   - the sparse voxel store          src/world/VoxelWorld.ts:15-187
+ *   - the rasteriser and its Builder  src/world/shapes.ts:334-414, :417-431
+ *   - the derived upload buffers      src/gpu/GpuWorld.ts:52-113
+ * A host binding (Python ctypes in this repository; an N-API addon for the
+ * TypeScript host) records Builder.add/carve/paint calls as
+ * a PXIR op list, submits it, and builds on the GPU.  All device memory is
+ * owned by the world handle.  Functions return a PX_* status; no C++ exception
+ * crosses this boundary; px_last_error() describes the last failure.
+ * One host thread per handle.
+ */
+#ifndef PIXELS_GB300_H
+#define PIXELS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define PX_OK 0
+#define PX_E_INVALID_ARG 1    /* bad handle, size or mode */
+#define PX_E_INVALID_IR 2     /* malformed op list (bounds, bytecode, NaN/inf parameters) */
+#define PX_E_OOM 3            /* device allocation failed */
+#define PX_E_QUEUE_OVERFLOW 4 /* a device work list ran out of room */
+#define PX_E_TIMEOUT 5        /* a bounded device wait gave up */
+#define PX_E_CUDA 6           /* CUDA runtime error */
+#define PX_E_RANGE 7          /* a paint function got an argument outside its supported range */
+#define PX_E_NO_DEVICE 8      /* no CUDA device */
+
+/* build modes */
+#define PX_MODE_FP64 0   /* every decision in float64, as JavaScript numbers */
+#define PX_MODE_MIXED 1  /* float32 evaluation, float64 rescue within a certified error bound */
+
+#define PX_UNIFORM 0x80000000u /* grid flag of a uniform brick (VoxelWorld.ts:13) */
+
+typedef struct px_world px_world;
+
+typedef struct px_stats {
+  uint64_t ops_applied;      /* ops built into this world so far */
+  uint64_t pairs;            /* (op, brick) pairs of the last build */
+  uint64_t brick_evals;      /* SDF evaluations at brick centres (last build) */
+  uint64_t sub_evals;        /* ... at 4^3 sub-block centres */
+  uint64_t voxel_evals;      /* ... at voxel centres */
+  uint64_t paint_evals;      /* paint-function calls */
+  uint64_t rescued;          /* float32 evaluations re-done in float64 (mixed mode) */
+  uint64_t alloc_events;     /* pool allocations replayed */
+  uint64_t free_events;      /* pool frees replayed */
+  uint32_t pool_used;        /* VoxelWorld.poolUsed */
+  uint32_t n_holes;          /* VoxelWorld.freeList.length */
+  uint32_t pool_capacity;    /* bricks the device pool can hold */
+  uint32_t status;           /* device status bits of the last build */
+  double max_abs_err32;      /* max |d32 - d64| seen by rescued evaluations (mixed mode) */
+  float build_ms;            /* device time of the last build */
+  float fold_ms;             /* device time of its fold kernel */
+  uint32_t kernel_launches;  /* kernels the last build launched */
+  uint32_t pad;
+} px_stats;
+
+/* Device addresses of the world's buffers (valid until the next build or destroy). */
+typedef struct px_device_view {
+  const uint32_t* grid;      /* bx*by*bz */
+  const uint16_t* pool;      /* pool_used * 512 */
+  const uint32_t* holes;     /* n_holes, push order */
+  const uint32_t* super_counts; /* ceil(bx/4)*ceil(by/4)*ceil(bz/4), after px_derive */
+  const uint8_t* density;    /* bx*by*bz, after px_derive */
+} px_device_view;
+
+/* new VoxelWorld(dx, dy, dz, initialPoolBricks) at a voxel density (VoxelWorld.ts:35-45;
+   VOXEL_SIZE = 1/vpm, config.ts:12-13).  dx, dy, dz: positive multiples of 8. */
+int px_world_create(int dx, int dy, int dz, double vpm, uint32_t initial_pool_bricks, px_world** out);
+void px_world_destroy(px_world* w);
+
+/* Queue ops (PXIR bytes, pixels_gb300/ir.py) — Builder.add/carve/paint (shapes.ts:417-431). */
+int px_submit_ops(px_world* w, const void* ir, size_t bytes);
+
+/* Run every queued op, in order, as apply() would (shapes.ts:334-414), on `stream`
+   (a cudaStream_t, NULL = default stream).  px_build waits for the result;
+   px_build_enqueue only launches, px_build_finish waits and reports. */
+int px_build(px_world* w, int mode, void* stream);
+int px_build_enqueue(px_world* w, int mode, void* stream);
+int px_build_finish(px_world* w);
+
+/* Empty the world (all air, poolUsed = 0, no holes), like a fresh VoxelWorld of the
+   same dims.  requeue_last_ops = 1 queues the ops of the last build again, reusing
+   their device copies (rebuilding a scene without re-uploading it). */
+int px_world_reset(px_world* w, int requeue_last_ops, void* stream);
+
+/* Reads into caller memory (grid: VoxelWorld.grid; pool: pool[0 .. poolUsed*512);
+   holes: freeBricks(), VoxelWorld.ts:173-175). n = capacity of dst in elements. */
+int px_read_grid(px_world* w, uint32_t* dst, size_t n);
+int px_read_pool(px_world* w, uint16_t* dst, size_t n);
+int px_read_holes(px_world* w, uint32_t* dst, size_t n);
+
+/* Derived upload buffers (GpuWorld.ts:52-113): super-grid counts, density
+   (red channel of the density texture) and the GPU free list for a pool of
+   capacity min(max_bricks, max(used + 98304, 2 used)). */
+int px_derive(px_world* w);
+int px_read_super(px_world* w, uint32_t* dst, size_t n);
+int px_read_density(px_world* w, uint8_t* dst, size_t n);
+int px_read_free_list(px_world* w, uint32_t max_bricks, uint32_t* dst, size_t n, uint32_t* out_len);
+
+/* Material tables for the density pass: opaque[id] (OPAQUE, VoxelWorld.ts:190-196) and the
+   density of a uniform brick of material id (VoxelWorld.ts:162).  256 bytes each. */
+int px_set_material_tables(px_world* w, const uint8_t* opaque256, const uint8_t* uniform_density256);
+
+int px_get_stats(px_world* w, px_stats* out);
+int px_device_view_get(px_world* w, px_device_view* out);
+const char* px_last_error(px_world* w);
+
+/* Measurement utility (no counterpart in the reference): dependent-FMA
+   throughput of this GPU's CUDA cores in TFLOP/s, float64 (fp64 = 1) or
+   float32 (fp64 = 0) — the denominators of the voxeliser's ALU roofline. */
+int px_probe_peak(int fp64, float* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PIXELS_GB300_H */

@@ -13,10 +13,10 @@
 // constants the reference's closures capture.  Compiled with
 // -ffp-contract=off and no fast-math so every operation rounds like JS.
 //
-// Transcendentals: Math.sin/Math.atan2 are the C library's sin/atan2 here;
-// Math.hypot is the engine method (scale by the largest magnitude, Kahan-sum
-// the squares, sqrt, rescale).  Last-ulp parity with V8 is unpinned (no
-// JavaScript runtime is available to pin it).
+// Transcendentals: Math.sin/Math.atan2 are correctly rounded double-double
+// routines (jsmath_ref.h); Math.hypot is the engine method (scale by the
+// largest magnitude, Kahan-sum the squares, sqrt, rescale).  Last-ulp parity
+// with a JavaScript engine is unpinned (no JavaScript runtime is available).
 
 #include <cmath>
 #include <cstdio>
@@ -28,6 +28,8 @@
 #include <thread>
 #include <vector>
 #include <algorithm>
+
+#include "jsmath_ref.h"
 
 namespace {
 
@@ -402,7 +404,7 @@ uint32_t paint_eval(int kind, const double* p, double x, double y, double z) {
   switch (kind) {
     case PK_CHIP: {  // penthouse.ts:371-377
       L(20, 2, 1, 1);
-      double a = std::atan2(z - p[2], x - p[0]);
+      double a = ref::ref_atan2(z - p[2], x - p[0]);
       bool edge = js_hypot2(x - p[0], z - p[2]) > p[3];
       bool stripe = std::fmod(std::floor(((a + PI) / (2 * PI)) * 8), 2) == 0;
       double layer = std::fmod(std::floor((y - p[1]) / 0.0045), 2);
@@ -437,10 +439,10 @@ uint32_t paint_eval(int kind, const double* p, double x, double y, double z) {
     }
     case PK_VASE: {  // penthouse.ts:810-816
       L(16, 1, 0, 3);
-      double a = std::atan2(z - p[2], x - p[0]);
+      double a = ref::ref_atan2(z - p[2], x - p[0]);
       double h = (y - p[1]) / p[3];
       bool band = (h > 0.04 && h < 0.06) || (h > 0.36 && h < 0.38) || (h > 0.47 && h < 0.49);
-      bool motif = h > 0.08 && h < 0.33 && std::sin(a * 5 + std::sin(h * 30) * 2) > 0.55;
+      bool motif = h > 0.08 && h < 0.33 && ref::ref_sin(a * 5 + ref::ref_sin(h * 30) * 2) > 0.55;
       return vox(p[4], band || motif ? 255 : 0);
     }
     case PK_PAINTING: {  // penthouse.ts:840-845
@@ -450,7 +452,7 @@ uint32_t paint_eval(int kind, const double* p, double x, double y, double z) {
         const double* b = p + 1 + 4 * i;
         if (js_hypot2(x - b[0], (y - b[1]) * 1.3) < b[2]) shade = b[3];
       }
-      bool stripe = std::fabs(std::sin(x * 9 + y * 3)) < 0.06;
+      bool stripe = std::fabs(ref::ref_sin(x * 9 + y * 3)) < 0.06;
       return vox(p[0], stripe ? 255 : shade);
     }
     case PK_NOISE: {  // synthetic scenes

@@ -64,7 +64,7 @@ class OracleWorld:
     """The world the reference would build from an op list, plus derived buffers."""
 
     def __init__(self, ir_bytes: bytes, vpm: float, dims, initial_pool_bricks: int = 1 << 15,
-                 count_flops: bool = False):
+                 count_flops: bool = False, threads: int = 1):
         from pixels_gb300.materials import opaque_table, uniform_density_table
         L = lib()
         res = OracleResult()

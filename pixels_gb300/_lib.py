@@ -1,0 +1,165 @@
+"""ctypes binding of ``libpixels_gb300.so`` (include/pixels_gb300.h).
+
+The library is the only compute path: if it is missing or cannot find a GPU,
+every call raises.  There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpixels_gb300.so")
+
+PX_OK = 0
+ERRORS = {1: "PX_E_INVALID_ARG", 2: "PX_E_INVALID_IR", 3: "PX_E_OOM", 4: "PX_E_QUEUE_OVERFLOW",
+          5: "PX_E_TIMEOUT", 6: "PX_E_CUDA", 7: "PX_E_RANGE", 8: "PX_E_NO_DEVICE"}
+
+# Every symbol include/pixels_gb300.h declares.
+EXPORTS = [
+    "px_world_create", "px_world_destroy", "px_world_reset", "px_submit_ops", "px_build", "px_build_enqueue",
+    "px_build_finish", "px_read_grid", "px_read_pool", "px_read_holes", "px_derive", "px_read_super",
+    "px_read_density", "px_read_free_list", "px_set_material_tables", "px_get_stats",
+    "px_device_view_get", "px_last_error", "px_probe_peak",
+]
+
+
+class PxError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("ops_applied", ctypes.c_uint64), ("pairs", ctypes.c_uint64), ("brick_evals", ctypes.c_uint64),
+        ("sub_evals", ctypes.c_uint64), ("voxel_evals", ctypes.c_uint64), ("paint_evals", ctypes.c_uint64),
+        ("rescued", ctypes.c_uint64), ("alloc_events", ctypes.c_uint64), ("free_events", ctypes.c_uint64),
+        ("pool_used", ctypes.c_uint32), ("n_holes", ctypes.c_uint32), ("pool_capacity", ctypes.c_uint32),
+        ("status", ctypes.c_uint32), ("max_abs_err32", ctypes.c_double), ("build_ms", ctypes.c_float),
+        ("fold_ms", ctypes.c_float), ("kernel_launches", ctypes.c_uint32), ("pad", ctypes.c_uint32),
+    ]
+
+
+_L = None
+
+
+def load(path: str = LIB_PATH):
+    """Load the library (raises if it was not built)."""
+    global _L
+    if _L is not None:
+        return _L
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with `python -m pixels_gb300.build`")
+    L = ctypes.CDLL(path)
+    vp, sz, u32 = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint32
+    L.px_world_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, u32, ctypes.POINTER(vp)]
+    L.px_world_destroy.argtypes = [vp]
+    L.px_world_reset.argtypes = [vp, ctypes.c_int, vp]
+    L.px_world_destroy.restype = None
+    L.px_submit_ops.argtypes = [vp, vp, sz]
+    L.px_build.argtypes = [vp, ctypes.c_int, vp]
+    L.px_build_enqueue.argtypes = [vp, ctypes.c_int, vp]
+    L.px_build_finish.argtypes = [vp]
+    for f in ("px_read_grid", "px_read_pool", "px_read_holes", "px_read_super", "px_read_density"):
+        getattr(L, f).argtypes = [vp, vp, sz]
+    L.px_derive.argtypes = [vp]
+    L.px_read_free_list.argtypes = [vp, u32, vp, sz, ctypes.POINTER(u32)]
+    L.px_set_material_tables.argtypes = [vp, vp, vp]
+    L.px_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+    L.px_device_view_get.argtypes = [vp, vp]
+    L.px_last_error.argtypes = [vp]
+    L.px_last_error.restype = ctypes.c_char_p
+    L.px_probe_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
+    _L = L
+    return L
+
+
+def _check(h, rc: int):
+    if rc != PX_OK:
+        msg = load().px_last_error(h) if h else b""
+        raise PxError(rc, (msg or b"").decode())
+
+
+def world_create(dx, dy, dz, vpm, initial_pool_bricks):
+    from .materials import opaque_table, uniform_density_table
+    L = load()
+    h = ctypes.c_void_p()
+    _check(None, L.px_world_create(dx, dy, dz, vpm, initial_pool_bricks, ctypes.byref(h)))
+    op = np.array(opaque_table(), np.uint8)
+    ud = np.array(uniform_density_table(), np.uint8)
+    _check(h, L.px_set_material_tables(h, op.ctypes.data, ud.ctypes.data))
+    return h
+
+
+def world_destroy(h):
+    load().px_world_destroy(h)
+
+
+def submit_ops(h, ir: bytes):
+    buf = ctypes.create_string_buffer(ir, len(ir))
+    _check(h, load().px_submit_ops(h, buf, len(ir)))
+
+
+def build(h, mode: int, stream: int = 0):
+    _check(h, load().px_build(h, mode, ctypes.c_void_p(stream)))
+
+
+def build_enqueue(h, mode: int, stream: int = 0):
+    _check(h, load().px_build_enqueue(h, mode, ctypes.c_void_p(stream)))
+
+
+def build_finish(h):
+    _check(h, load().px_build_finish(h))
+
+
+def world_reset(h, requeue_last_ops: bool = False, stream: int = 0):
+    _check(h, load().px_world_reset(h, int(requeue_last_ops), ctypes.c_void_p(stream)))
+
+
+def stats(h) -> dict:
+    s = Stats()
+    _check(h, load().px_get_stats(h, ctypes.byref(s)))
+    return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+
+def read_grid(h, n: int) -> np.ndarray:
+    out = np.empty(n, np.uint32)
+    _check(h, load().px_read_grid(h, out.ctypes.data, n))
+    return out
+
+
+def read_pool(h) -> np.ndarray:
+    used = stats(h)["pool_used"]
+    out = np.empty(used * 512, np.uint16)
+    _check(h, load().px_read_pool(h, out.ctypes.data if used else None, out.size))
+    return out
+
+
+def read_holes(h) -> np.ndarray:
+    n = stats(h)["n_holes"]
+    out = np.empty(n, np.uint32)
+    _check(h, load().px_read_holes(h, out.ctypes.data if n else None, n))
+    return out
+
+
+def read_derived(h, max_bricks: int, n_cells: int, n_super: int) -> dict:
+    L = load()
+    sup = np.empty(n_super, np.uint32)
+    den = np.empty(n_cells, np.uint8)
+    _check(h, L.px_read_super(h, sup.ctypes.data, n_super))
+    _check(h, L.px_read_density(h, den.ctypes.data, n_cells))
+    ln = ctypes.c_uint32()
+    _check(h, L.px_read_free_list(h, max_bricks, None, 0, ctypes.byref(ln)))
+    fl = np.empty(ln.value, np.uint32)
+    _check(h, L.px_read_free_list(h, max_bricks, fl.ctypes.data, fl.size, ctypes.byref(ln)))
+    return {"super": sup, "density": den, "free_list": fl}
+
+
+def probe_peak(fp64: bool) -> float:
+    """Measured FMA throughput of the CUDA cores (TFLOP/s)."""
+    v = ctypes.c_float()
+    _check(None, load().px_probe_peak(int(fp64), ctypes.byref(v)))
+    return float(v.value)

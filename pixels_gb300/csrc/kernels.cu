@@ -1,0 +1,845 @@
+// Voxeliser kernels for sm_103a (GB300).
+//
+// Pipeline of one build (all on one stream, no host round trip):
+//   cull      one warp per 4^3-brick tile scans the op list (ballot) and keeps
+//             the ops whose brick box overlaps the tile, in op order.
+//   fold      persistent warps, one brick at a time: the brick's 512 voxels live
+//             in registers (two voxels per lane per z slice); the warp applies
+//             the brick's ops in order exactly as apply() does (shapes.ts:353-412):
+//             brick classify, 4^3 sub-block classify, boundary voxels, paint,
+//             uniform shortcuts, compaction.  Pool alloc/free events are
+//             recorded per (op, brick) pair; bricks that end non-uniform are
+//             written to a staging area.
+//   replay    parallel replay of the LIFO pool allocator (VoxelWorld.ts:112-127)
+//             over the events in (op, cell) order: clamped depth scan, match
+//             of each pop to its push (previous-smaller-value search on a
+//             32-ary min tree), pointer chasing of recycled indices.
+//   finalize  staging -> pool at the replayed indices (16-byte vector copies),
+//             grid entries.
+//   derive    super-grid counts and density bytes (GpuWorld.ts:90-101).
+#include <cstdio>
+#include "px_internal.cuh"
+#include "sdf64.cuh"
+#include "paint.cuh"
+
+namespace px {
+
+#define FULLMASK 0xffffffffu
+
+// kernel launches issued by the host wrappers (reported per build)
+static unsigned long long g_launches = 0;
+unsigned long long launch_count() { return g_launches; }
+
+// ---------------------------------------------------------------------------
+// cull
+
+__device__ __forceinline__ bool box_overlaps_tile(uint2 b, int tx, int ty, int tz) {
+  int x0 = b.x & 1023, y0 = (b.x >> 10) & 1023, z0 = (b.x >> 20) & 1023;
+  int x1 = b.y & 1023, y1 = (b.y >> 10) & 1023, z1 = (b.y >> 20) & 1023;
+  if (b.x >> 30) return false;  // op with an empty voxel range
+  return x0 <= tx * 4 + 3 && x1 >= tx * 4 && y0 <= ty * 4 + 3 && y1 >= ty * 4 && z0 <= tz * 4 + 3 && z1 >= tz * 4;
+}
+
+__global__ void __launch_bounds__(256) cull_count_kernel(const uint2* __restrict__ boxes, int n_ops, int TX, int TY, int TZ,
+                                                         uint32_t* tile_cnt, uint32_t* tiles_nonempty, BuildResult* res) {
+  const int lane = threadIdx.x & 31;
+  const int n_tiles = TX * TY * TZ;
+  for (int tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; tile < n_tiles; tile += (gridDim.x * blockDim.x) >> 5) {
+    int tz = tile / (TX * TY), r = tile - tz * TX * TY, ty = r / TX, tx = r - ty * TX;
+    uint32_t cnt = 0;
+    for (int c0 = 0; c0 < n_ops; c0 += 32) {
+      int i = c0 + lane;
+      bool ov = i < n_ops && box_overlaps_tile(__ldg(boxes + i), tx, ty, tz);
+      cnt += __popc(__ballot_sync(FULLMASK, ov));
+    }
+    if (lane == 0) {
+      tile_cnt[tile] = cnt;
+      if (cnt) tiles_nonempty[atomicAdd(&res->n_nonempty, 1u)] = (uint32_t)tile;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) cull_fill_kernel(const uint2* __restrict__ boxes, int n_ops, int TX, int TY, int TZ,
+                                                        const uint32_t* __restrict__ tile_off, uint32_t* tile_ops) {
+  const int lane = threadIdx.x & 31;
+  const int n_tiles = TX * TY * TZ;
+  for (int tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; tile < n_tiles; tile += (gridDim.x * blockDim.x) >> 5) {
+    int tz = tile / (TX * TY), r = tile - tz * TX * TY, ty = r / TX, tx = r - ty * TX;
+    uint32_t pos = tile_off[tile];
+    for (int c0 = 0; c0 < n_ops; c0 += 32) {
+      int i = c0 + lane;
+      bool ov = i < n_ops && box_overlaps_tile(__ldg(boxes + i), tx, ty, tz);
+      uint32_t m = __ballot_sync(FULLMASK, ov);
+      if (ov) tile_ops[pos + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
+      pos += __popc(m);
+    }
+  }
+}
+
+void launch_cull_count(const uint2* boxes, int n_ops, int TX, int TY, int TZ, uint32_t* tile_cnt,
+                       uint32_t* tiles_nonempty, BuildResult* res, cudaStream_t s) {
+  int n_tiles = TX * TY * TZ;
+  int blocks = (n_tiles * 32 + 255) / 256;
+  ++g_launches; cull_count_kernel<<<blocks, 256, 0, s>>>(boxes, n_ops, TX, TY, TZ, tile_cnt, tiles_nonempty, res);
+}
+void launch_cull_fill(const uint2* boxes, int n_ops, int TX, int TY, int TZ, const uint32_t* tile_off,
+                      uint32_t* tile_ops, cudaStream_t s) {
+  int n_tiles = TX * TY * TZ;
+  int blocks = (n_tiles * 32 + 255) / 256;
+  ++g_launches; cull_fill_kernel<<<blocks, 256, 0, s>>>(boxes, n_ops, TX, TY, TZ, tile_off, tile_ops);
+}
+
+// ---------------------------------------------------------------------------
+// fold
+
+enum { ST_EMPTY = 0, ST_UNIF = 1, ST_MIXED = 2 };
+
+struct WarpCounters {
+  unsigned long long brick, sub, vox, paint, resc, alloc, free_;
+};
+
+// Lane layout of a brick in registers: lane owns the voxel pair
+// (x0, y, z) / (x0 + 1, y, z) with x0 = 2 (lane & 3), y = lane >> 2, in
+// register j = z.  Voxel index li = x | y << 3 | z << 6 (VoxelWorld.ts:60), so
+// register j of the warp is the contiguous 128-byte slice pool[64 j .. 64 j + 63].
+template <int MODE>
+__global__ void __launch_bounds__(256, 2) fold_kernel(FoldArgs a) {
+  __shared__ unsigned long long smask[8][8];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int lx0 = (lane & 3) * 2, ly = lane >> 2;
+  const double vs = a.vs;
+  WarpCounters wc = {0, 0, 0, 0, 0, 0, 0};
+  uint32_t st_local = 0;
+  const uint32_t n_work = __ldg(&a.res->n_nonempty) * 64u;
+
+  for (;;) {
+    uint32_t item = 0;
+    if (lane == 0) item = atomicAdd(a.work_counter, 1u);
+    item = __shfl_sync(FULLMASK, item, 0);
+    if (item >= n_work) break;
+    const uint32_t tile = __ldg(a.tiles_nonempty + (item >> 6));
+    const int local = item & 63;
+    const int tz = tile / (a.TX * a.TY), rr = tile - tz * a.TX * a.TY, ty = rr / a.TX, tx = rr - ty * a.TX;
+    const int bx = tx * 4 + (local & 3), by = ty * 4 + ((local >> 2) & 3), bz = tz * 4 + (local >> 4);
+    if (bx >= a.BX || by >= a.BY || bz >= a.BZ) continue;
+    const size_t ci = (size_t)bx + (size_t)a.BX * ((size_t)by + (size_t)a.BY * bz);
+    const int ox = bx * 8, oy = by * 8, oz = bz * 8;
+
+    // current brick contents (VoxelWorld.ts:55-61)
+    const uint32_t g = a.grid[ci];
+    int state;
+    uint32_t uval = 0;
+    uint32_t vox[8];
+    long long src;  // pool identity: >= 0 pair of the last alloc, < 0 -(old index + 1)
+    if (g == 0) {
+      state = ST_EMPTY; src = -1;
+#pragma unroll
+      for (int j = 0; j < 8; j++) vox[j] = 0;
+    } else if (g & UNIFORM) {
+      state = ST_UNIF; uval = g & 0xffffu; src = -1;
+#pragma unroll
+      for (int j = 0; j < 8; j++) vox[j] = uval | (uval << 16);
+    } else {
+      state = ST_MIXED; src = -(long long)(g - 1) - 1;
+      const uint32_t* pb = a.pool32 + (size_t)(g - 1) * 256;
+#pragma unroll
+      for (int j = 0; j < 8; j++) vox[j] = pb[32 * j + lane];
+    }
+    bool dirty = false;
+
+    const uint32_t toff = __ldg(a.tile_off + tile), tcnt = __ldg(a.tile_cnt + tile);
+    for (uint32_t c0 = 0; c0 < tcnt; c0 += 32) {
+      uint32_t oi = 0;
+      bool cov = false;
+      if (c0 + lane < tcnt) {
+        oi = __ldg(a.tile_ops + toff + c0 + lane);
+        const OpDev* o = a.ops + oi;
+        cov = bx >= o->bx0 && bx <= o->bx1 && by >= o->by0 && by <= o->by1 && bz >= o->bz0 && bz <= o->bz1;
+      }
+      uint32_t m = __ballot_sync(FULLMASK, cov);
+      while (m) {
+        const int b = __ffs(m) - 1;
+        m &= m - 1;
+        const uint32_t o_idx = __shfl_sync(FULLMASK, oi, b);
+        const OpDev* O = a.ops + o_idx;
+        const int kind = O->kind, flags = O->flags;
+        const uint32_t pk = O->paint_kind, pv = O->paint_value;
+        const bool constPaint = pk == PK_CONST;
+        const uint2* code = a.code + O->code_off;
+        const int clen = (int)O->code_len;
+        const unsigned long long pair = O->pair_base +
+            (unsigned long long)(((bz - O->bz0) * O->ny + (by - O->by0)) * O->nx + (bx - O->bx0));
+
+        // brick classification (shapes.ts:358-366)
+        bool full = false;
+        if (flags & OPF_CONTAINS) {
+          double x0 = (ox + 0.5) * vs, y0 = (oy + 0.5) * vs, z0 = (oz + 0.5) * vs;
+          double x1 = (ox + 7.5) * vs, y1 = (oy + 7.5) * vs, z1 = (oz + 7.5) * vs;
+          full = x0 >= O->mn[0] && x1 <= O->mx[0] && y0 >= O->mn[1] && y1 <= O->mx[1] && z0 >= O->mn[2] && z1 <= O->mx[2];
+        }
+        if (!full) {
+          double d = sdf64(code, clen, a.params, (ox + 4) * vs, (oy + 4) * vs, (oz + 4) * vs);
+          wc.brick++;
+          const double bhd = O->bhd;
+          if (d > bhd) continue;
+          full = d < -bhd;
+        }
+        // uniform shortcuts (shapes.ts:367-374)
+        int set_u = -1;
+        if (full) {
+          if (kind == KIND_ADD && constPaint) set_u = (int)pv;
+          else if (kind == KIND_CARVE) set_u = 0;
+          else if (kind == KIND_PAINT && state == ST_EMPTY) continue;
+          else if (kind == KIND_PAINT && constPaint && state == ST_UNIF) set_u = (int)pv;
+        }
+        if (set_u >= 0) {  // setBrickUniform (VoxelWorld.ts:89-97)
+          if (state == ST_MIXED) {
+            if (lane == 0) { a.evt[pair] = 2; a.fsrc[pair] = src; }
+            wc.free_++;
+          }
+          uint32_t v = (uint32_t)set_u;
+          state = v == 0 ? ST_EMPTY : ST_UNIF;
+          uval = v; src = -1;
+#pragma unroll
+          for (int j = 0; j < 8; j++) vox[j] = v | (v << 16);
+          dirty = true;
+          continue;
+        }
+        if (kind == KIND_PAINT && state == ST_EMPTY) continue;
+
+        // sub-block classification (shapes.ts:382-389)
+        uint32_t sub_full = full ? 0xffu : 0u, sub_part = 0u;
+        if (!full) {
+          bool in8 = lane < 8;
+          double d = 0.0;
+          if (in8) {
+            int sx = ox + (lane & 1) * 4, sy = oy + ((lane >> 1) & 1) * 4, sz = oz + ((lane >> 2) & 1) * 4;
+            d = sdf64(code, clen, a.params, (sx + 2) * vs, (sy + 2) * vs, (sz + 2) * vs);
+          }
+          wc.sub += 8;
+          const double shd = O->shd;
+          uint32_t bf = __ballot_sync(FULLMASK, in8 && d < -shd);
+          uint32_t bs = __ballot_sync(FULLMASK, in8 && d > shd);
+          sub_full = bf & 0xffu;
+          sub_part = ~(bf | bs) & 0xffu;
+        }
+        // boundary voxels of partial sub-blocks (shapes.ts:390-394)
+        if (lane < 8) smask[wib][lane] = ((sub_full >> lane) & 1u) ? ~0ull : 0ull;
+        __syncwarp();
+        for (uint32_t sp = sub_part; sp; sp &= sp - 1) {
+          const int s = __ffs(sp) - 1;
+          const int sx = ox + (s & 1) * 4, sy = oy + ((s >> 1) & 1) * 4, sz = oz + ((s >> 2) & 1) * 4;
+          uint32_t bal[2];
+#pragma unroll
+          for (int r = 0; r < 2; r++) {
+            const int e = r * 32 + lane;
+            const int X = sx + (e & 3), Y = sy + ((e >> 2) & 3), Z = sz + (e >> 4);
+            double d = sdf64(code, clen, a.params, (X + 0.5) * vs, (Y + 0.5) * vs, (Z + 0.5) * vs);
+            bal[r] = __ballot_sync(FULLMASK, !(d > 0.0));
+          }
+          if (lane == 0) smask[wib][s] = (unsigned long long)bal[0] | ((unsigned long long)bal[1] << 32);
+          wc.vox += 64;
+        }
+        __syncwarp();
+
+        // write voxels (shapes.ts:395-405)
+        bool changed = false;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          const int s = (lx0 >> 2) | ((ly >> 2) << 1) | ((j >> 2) << 2);
+          const int e0 = (lx0 & 3) | ((ly & 3) << 2) | ((j & 3) << 4);
+          const unsigned long long ms = smask[wib][s];
+#pragma unroll
+          for (int h = 0; h < 2; h++) {
+            if (!((ms >> (e0 + h)) & 1ull)) continue;
+            const uint32_t cur = (vox[j] >> (16 * h)) & 0xffffu;
+            uint32_t next;
+            if (kind == KIND_CARVE) next = 0;
+            else if (kind == KIND_PAINT && cur == 0) continue;
+            else if (!constPaint) {
+              double PX = (ox + lx0 + h + 0.5) * vs, PY = (oy + ly + 0.5) * vs, PZ = (oz + j + 0.5) * vs;
+              if (flags & OPF_PAINT_FRAME) {  // localPaint (penthouse.ts:88-91)
+                const double fpx = O->frame[0], fpz = O->frame[1], c = O->frame[2], sn = O->frame[3];
+                double dx = PX - fpx, dz = PZ - fpz;
+                PX = fpx + c * dx + sn * dz;
+                PZ = fpz - sn * dx + c * dz;
+              }
+              next = paint_eval(pk, a.params + O->paint_off, PX, PY, PZ, st_local);
+              wc.paint++;
+            } else next = pv;
+            if (next != cur) {  // Uint16Array store; the comparison uses the unstored value
+              vox[j] = (vox[j] & ~(0xffffu << (16 * h))) | ((next & 0xffffu) << (16 * h));
+              changed = true;
+            }
+          }
+        }
+        __syncwarp();
+        if (!__any_sync(FULLMASK, changed)) continue;
+        dirty = true;
+        uint8_t ev = 0;
+        if (state != ST_MIXED) {  // editableBrick -> allocBrick (VoxelWorld.ts:103-122)
+          ev = 1; src = (long long)pair; state = ST_MIXED;
+          wc.alloc++;
+        }
+        // compactCell (VoxelWorld.ts:147-156)
+        const uint32_t v0 = __shfl_sync(FULLMASK, vox[0] & 0xffffu, 0);
+        const uint32_t vv = v0 | (v0 << 16);
+        bool eq = true;
+#pragma unroll
+        for (int j = 0; j < 8; j++) eq = eq && vox[j] == vv;
+        if (__all_sync(FULLMASK, eq)) {
+          if (lane == 0) a.fsrc[pair] = src;
+          ev |= 2;
+          wc.free_++;
+          state = v0 == 0 ? ST_EMPTY : ST_UNIF;
+          uval = v0; src = -1;
+        }
+        if (lane == 0) a.evt[pair] = ev;
+      }
+    }
+
+    if (!dirty) continue;
+    if (state == ST_EMPTY) {
+      if (lane == 0) a.grid[ci] = 0;
+    } else if (state == ST_UNIF) {
+      if (lane == 0) a.grid[ci] = UNIFORM | uval;
+    } else {
+      uint32_t slot = 0;
+      if (lane == 0) slot = atomicAdd(&a.res->stage_count, 1u);
+      slot = __shfl_sync(FULLMASK, slot, 0);
+      if (slot >= a.stage_cap) {
+        st_local |= ST_STAGE_OVERFLOW;
+      } else {
+        uint32_t* dst = a.staging32 + (size_t)slot * 256;
+#pragma unroll
+        for (int j = 0; j < 8; j++) dst[32 * j + lane] = vox[j];
+        if (lane == 0) { a.stage_cell[slot] = (uint32_t)ci; a.stage_src[slot] = src; }
+      }
+    }
+  }
+  if (lane == 0) {
+    if (wc.brick) atomicAdd(&a.res->c.brick_evals, wc.brick);
+    if (wc.sub) atomicAdd(&a.res->c.sub_evals, wc.sub);
+    if (wc.vox) atomicAdd(&a.res->c.voxel_evals, wc.vox);
+    if (wc.alloc) atomicAdd(&a.res->c.alloc_events, wc.alloc);
+    if (wc.free_) atomicAdd(&a.res->c.free_events, wc.free_);
+  }
+  unsigned long long pc = wc.paint;
+#pragma unroll
+  for (int o = 16; o; o >>= 1) pc += __shfl_xor_sync(FULLMASK, pc, o);
+  uint32_t stw = st_local;
+#pragma unroll
+  for (int o = 16; o; o >>= 1) stw |= __shfl_xor_sync(FULLMASK, stw, o);
+  if (lane == 0) {
+    if (pc) atomicAdd(&a.res->c.paint_evals, pc);
+    if (stw) atomicOr(&a.res->status, stw);
+  }
+}
+
+void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s) {
+  (void)mode;
+  int blocks = n_sms * 2;
+  ++g_launches; fold_kernel<0><<<blocks, 256, 0, s>>>(a);
+}
+
+// ---------------------------------------------------------------------------
+// scans (block-wise, three passes; sizes may live on the device)
+
+constexpr int SCAN_THREADS = 512;
+constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+size_t scan_items_per_block() { return SCAN_TILE; }
+
+__device__ __forceinline__ uint32_t shfl_up_any(uint32_t v, int o) { return __shfl_up_sync(FULLMASK, v, o); }
+__device__ __forceinline__ int32_t shfl_up_any(int32_t v, int o) { return __shfl_up_sync(FULLMASK, v, o); }
+__device__ __forceinline__ int2 shfl_up_any(int2 v, int o) {
+  return make_int2(__shfl_up_sync(FULLMASK, v.x, o), __shfl_up_sync(FULLMASK, v.y, o));
+}
+
+struct SumOp {
+  typedef uint32_t T;
+  __device__ static T identity() { return 0u; }
+  __device__ static T combine(T a, T b) { return a + b; }
+};
+// Clamped stack depth: after an event the depth is max(c, d + a).  Applying x
+// then y gives (x.a + y.a, max(y.c, x.c + y.a)).  A push is (1, -inf); a pop
+// that finds the stack empty allocates a fresh brick instead: (-1, 0).
+struct DepthOp {
+  typedef int2 T;
+  __device__ static T identity() { return make_int2(0, -(1 << 30)); }
+  __device__ static T combine(T x, T y) { return make_int2(x.x + y.x, max(y.y, x.y + y.x)); }
+};
+struct MinOp {
+  typedef int32_t T;
+  __device__ static T identity() { return 0x7fffffff; }
+  __device__ static T combine(T a, T b) { return min(a, b); }
+};
+
+// Exclusive scan of one value per thread across the block; returns the
+// thread's exclusive prefix and the block total.
+template <class Op>
+__device__ typename Op::T block_exclusive(typename Op::T v, typename Op::T* sh, typename Op::T& total) {
+  typedef typename Op::T T;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  T x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T y = shfl_up_any(x, o);
+    if (lane >= o) x = Op::combine(y, x);
+  }
+  if (lane == 31) sh[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    T s = lane < nw ? sh[lane] : Op::identity();
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      T y = shfl_up_any(s, o);
+      if (lane >= o) s = Op::combine(y, s);
+    }
+    if (lane < nw) sh[lane] = s;
+  }
+  __syncthreads();
+  T wp = w ? sh[w - 1] : Op::identity();
+  total = sh[nw - 1];
+  T ex = shfl_up_any(x, 1);
+  if (lane == 0) ex = Op::identity();
+  __syncthreads();
+  return Op::combine(wp, ex);
+}
+
+__device__ __forceinline__ size_t scan_n(size_t n_max, const uint32_t* n_dev) {
+  if (!n_dev) return n_max;
+  size_t n = *n_dev;
+  return n < n_max ? n : n_max;
+}
+// scan position k -> array index (reverse scans run from the end)
+template <bool REV>
+__device__ __forceinline__ size_t scan_idx(size_t k, size_t n) { return REV ? n - 1 - k : k; }
+
+template <class Op, bool REV>
+__global__ void __launch_bounds__(SCAN_THREADS) scan_pass1(const typename Op::T* in, size_t n_max, const uint32_t* n_dev,
+                                                            typename Op::T* agg) {
+  typedef typename Op::T T;
+  __shared__ T sh[32];
+  const size_t n = scan_n(n_max, n_dev);
+  const size_t k0 = (size_t)blockIdx.x * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
+  T acc = Op::identity();
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; i++) {
+    size_t k = k0 + i;
+    if (k < n) acc = Op::combine(acc, in[scan_idx<REV>(k, n)]);
+  }
+  T total;
+  block_exclusive<Op>(acc, sh, total);
+  if (threadIdx.x == 0) agg[blockIdx.x] = total;
+}
+
+template <class Op>
+__global__ void __launch_bounds__(1024) scan_pass2(typename Op::T* agg, int nb) {
+  typedef typename Op::T T;
+  __shared__ T sh[32];
+  const int per = (nb + blockDim.x - 1) / blockDim.x;
+  const int b0 = threadIdx.x * per;
+  T acc = Op::identity();
+  for (int i = 0; i < per; i++)
+    if (b0 + i < nb) acc = Op::combine(acc, agg[b0 + i]);
+  T total;
+  T pre = block_exclusive<Op>(acc, sh, total);
+  for (int i = 0; i < per; i++)
+    if (b0 + i < nb) {
+      T v = agg[b0 + i];
+      agg[b0 + i] = pre;
+      pre = Op::combine(pre, v);
+    }
+}
+
+template <class Op, bool REV>
+__global__ void __launch_bounds__(SCAN_THREADS) scan_pass3(const typename Op::T* in, typename Op::T* out, size_t n_max,
+                                                            const uint32_t* n_dev, const typename Op::T* agg,
+                                                            bool inclusive, typename Op::T* total_out) {
+  typedef typename Op::T T;
+  __shared__ T sh[32];
+  const size_t n = scan_n(n_max, n_dev);
+  const size_t k0 = (size_t)blockIdx.x * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
+  T v[SCAN_ITEMS];
+  T acc = Op::identity();
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; i++) {
+    size_t k = k0 + i;
+    v[i] = k < n ? in[scan_idx<REV>(k, n)] : Op::identity();
+    acc = Op::combine(acc, v[i]);
+  }
+  T total;
+  T pre = Op::combine(agg[blockIdx.x], block_exclusive<Op>(acc, sh, total));
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; i++) {
+    size_t k = k0 + i;
+    T nxt = Op::combine(pre, v[i]);
+    if (k < n) out[scan_idx<REV>(k, n)] = inclusive ? nxt : pre;
+    if (total_out && k + 1 == n) *total_out = nxt;
+    pre = nxt;
+  }
+}
+
+template <class Op, bool REV>
+void scan_any(const typename Op::T* in, typename Op::T* out, size_t n_max, const uint32_t* n_dev, bool inclusive,
+              typename Op::T* total_out, ScanTemp& t, cudaStream_t s) {
+  if (n_max == 0) return;
+  int nb = (int)((n_max + SCAN_TILE - 1) / SCAN_TILE);
+  typename Op::T* agg = (typename Op::T*)t.block_agg;
+  ++g_launches; scan_pass1<Op, REV><<<nb, SCAN_THREADS, 0, s>>>(in, n_max, n_dev, agg);
+  ++g_launches; scan_pass2<Op><<<1, 1024, 0, s>>>(agg, nb);
+  ++g_launches; scan_pass3<Op, REV><<<nb, SCAN_THREADS, 0, s>>>(in, out, n_max, n_dev, agg, inclusive, total_out);
+}
+
+void launch_scan_u32(const uint32_t* in, uint32_t* out, size_t n, const uint32_t* n_dev, bool inclusive,
+                     uint32_t* total_out, ScanTemp& t, cudaStream_t s) {
+  scan_any<SumOp, false>(in, out, n, n_dev, inclusive, total_out, t, s);
+}
+
+// ---------------------------------------------------------------------------
+// replay of the LIFO pool allocator (VoxelWorld.ts:112-127) over the build's
+// alloc/free events in (op, cell) order.
+
+constexpr unsigned long long KNOWN = 1ull << 63;
+enum : uint8_t { EV_PUSH = 0, EV_POP = 1 };
+
+__global__ void evt_count_kernel(const uint8_t* __restrict__ evt, size_t P, uint32_t* cnt) {
+  for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < P; p += (size_t)gridDim.x * blockDim.x)
+    cnt[p] = __popc(evt[p] & 3u);
+}
+
+__global__ void n_events_kernel(const uint32_t* pos, const uint32_t* cnt, size_t P, uint32_t H, BuildResult* res) {
+  res->n_events = H + (P ? pos[P - 1] + cnt[P - 1] : 0u);
+}
+
+__global__ void events_build_kernel(ReplayArgs a) {
+  const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = tid; i < a.H; i += stride) {
+    a.etype[i] = EV_PUSH;
+    a.depth_fn[i] = make_int2(1, -(1 << 30));
+    a.ew[i] = KNOWN | a.holes_in[i];
+  }
+  for (size_t p = tid; p < a.P; p += stride) {
+    const uint32_t e = a.evt[p];
+    if (!e) continue;
+    const size_t base = a.H + a.pos[p];
+    if (e & 1u) {
+      a.etype[base] = EV_POP;
+      a.depth_fn[base] = make_int2(-1, 0);
+      a.ew[base] = 0;
+    }
+    if (e & 2u) {
+      const size_t k = base + (e & 1u);
+      a.etype[k] = EV_PUSH;
+      a.depth_fn[k] = make_int2(1, -(1 << 30));
+      const long long src = a.fsrc[p];
+      a.ew[k] = src >= 0 ? (unsigned long long)(a.H + a.pos[src]) : (KNOWN | (unsigned long long)(-(src + 1)));
+    }
+  }
+}
+
+__global__ void depth_apply_kernel(const int2* __restrict__ fn, int32_t* depth, const BuildResult* res) {
+  const size_t E = res->n_events;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (size_t)gridDim.x * blockDim.x) {
+    int2 f = fn[e];
+    depth[e] = max(f.y, f.x);  // applied to the empty stack (depth 0)
+  }
+}
+
+__global__ void fresh_flags_kernel(const uint8_t* __restrict__ etype, const int32_t* __restrict__ depth, uint32_t* fresh,
+                                   const BuildResult* res) {
+  const size_t E = res->n_events;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (size_t)gridDim.x * blockDim.x) {
+    int dprev = e ? depth[e - 1] : 0;
+    fresh[e] = (etype[e] == EV_POP && dprev == 0) ? 1u : 0u;
+  }
+}
+
+struct TreeLevels {
+  size_t off[8];  // offsets (in int32) of levels 1.. in the tree buffer
+  int n;          // levels above the depth array
+};
+
+__device__ __forceinline__ size_t level_size(size_t E, int l) {
+  size_t n = E;
+  for (int i = 0; i < l; i++) n = (n + 31) >> 5;
+  return n;
+}
+
+__global__ void tree_level_kernel(const int32_t* __restrict__ below, int32_t* level, int l, const BuildResult* res) {
+  const size_t n_below = level_size(res->n_events, l - 1);
+  const size_t n = (n_below + 31) >> 5;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    int32_t m = 0x7fffffff;
+    size_t c0 = k * 32, c1 = min(c0 + 32, n_below);
+    for (size_t c = c0; c < c1; c++) m = min(m, below[c]);
+    level[k] = m;
+  }
+}
+
+// Largest i < e with depth[i] < D (or -1): climb the min tree to the nearest
+// block holding a smaller value, then descend to its last such leaf.
+__device__ long long prev_less(const int32_t* depth, const int32_t* tree, const TreeLevels& tl, size_t E, size_t e, int D) {
+  long long i = (long long)e - 1;
+  int lev = 0;
+  long long found = -1;
+  while (i >= 0) {
+    const int32_t* L = lev == 0 ? depth : tree + tl.off[lev - 1];
+    long long start = i & ~31ll;
+    for (long long k = i; k >= start; k--)
+      if (L[k] < D) { found = k; break; }
+    if (found >= 0) break;
+    if (start == 0 || lev == tl.n) return -1;
+    i = (start >> 5) - 1;
+    lev++;
+  }
+  if (found < 0) return -1;
+  while (lev > 0) {
+    lev--;
+    const int32_t* L = lev == 0 ? depth : tree + tl.off[lev - 1];
+    const size_t n = level_size(E, lev);
+    long long c0 = found * 32, c1 = min((long long)n - 1, c0 + 31);
+    long long nf = -1;
+    for (long long c = c1; c >= c0; c--)
+      if (L[c] < D) { nf = c; break; }
+    found = nf;
+    if (found < 0) return -1;  // cannot happen: the parent's minimum is below D
+  }
+  return found;
+}
+
+__global__ void match_kernel(ReplayArgs a, TreeLevels tl) {
+  const size_t E = a.res->n_events;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (size_t)gridDim.x * blockDim.x) {
+    if (a.etype[e] != EV_POP) continue;
+    const int dprev = e ? a.depth[e - 1] : 0;
+    if (dprev == 0) {
+      a.ew[e] = KNOWN | (unsigned long long)(a.U0 + a.fresh_rank[e]);
+    } else {
+      long long i = prev_less(a.depth, a.tree, tl, E, e, dprev);
+      a.ew[e] = (unsigned long long)(i + 1);  // the push that filled slot dprev
+    }
+  }
+}
+
+__global__ void resolve_kernel(unsigned long long* ew, BuildResult* res) {
+  const size_t E = res->n_events;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (size_t)gridDim.x * blockDim.x) {
+    unsigned long long w = ew[e];
+    if (w & KNOWN) continue;
+    size_t p = (size_t)w;
+    size_t steps = 0;
+    // pointers always lead to an earlier event, so the walk ends within E steps
+    for (;;) {
+      unsigned long long q = *((volatile unsigned long long*)ew + p);
+      if (q & KNOWN) { w = q; break; }
+      if ((size_t)q >= p || ++steps > E) { atomicOr(&res->status, (uint32_t)ST_CHAIN); w = KNOWN; break; }
+      p = (size_t)q;
+    }
+    ew[e] = w;
+  }
+}
+
+__global__ void holes_out_kernel(const uint8_t* __restrict__ etype, const int32_t* __restrict__ depth,
+                                 const int32_t* __restrict__ sufmin, const unsigned long long* __restrict__ ew,
+                                 uint32_t* holes_out, BuildResult* res, uint32_t U0) {
+  const size_t E = res->n_events;
+  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (size_t)gridDim.x * blockDim.x) {
+    if (etype[e] != EV_PUSH) continue;
+    const int d = depth[e];
+    if (sufmin[e] >= d) holes_out[d - 1] = (uint32_t)(ew[e] & 0xffffffffull);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    res->n_holes = E ? (uint32_t)depth[E - 1] : 0u;
+    res->pool_used = U0 + res->n_fresh;
+  }
+}
+
+static size_t level_size_host(size_t E, int l) {
+  size_t n = E;
+  for (int i = 0; i < l; i++) n = (n + 31) / 32;
+  return n;
+}
+
+void launch_replay(const ReplayArgs& a, cudaStream_t s) {
+  const int T = 256;
+  auto blocks = [&](size_t n) { size_t b = (n + T - 1) / T; return (int)(b < 4096 ? (b ? b : 1) : 4096); };
+  ++g_launches; evt_count_kernel<<<blocks(a.P), T, 0, s>>>(a.evt, a.P, a.cnt);
+  scan_any<SumOp, false>(a.cnt, a.pos, a.P, nullptr, false, nullptr, *a.scan, s);
+  ++g_launches; n_events_kernel<<<1, 1, 0, s>>>(a.pos, a.cnt, a.P, a.H, a.res);
+  ++g_launches; events_build_kernel<<<blocks(a.P > a.H ? a.P : a.H), T, 0, s>>>(a);
+  const uint32_t* nE = &a.res->n_events;
+  scan_any<DepthOp, false>(a.depth_fn, a.depth_fn, a.E_max, nE, true, nullptr, *a.scan, s);
+  ++g_launches; depth_apply_kernel<<<blocks(a.E_max), T, 0, s>>>(a.depth_fn, a.depth, a.res);
+  ++g_launches; fresh_flags_kernel<<<blocks(a.E_max), T, 0, s>>>(a.etype, a.depth, a.fresh, a.res);
+  scan_any<SumOp, false>(a.fresh, a.fresh_rank, a.E_max, nE, false, &a.res->n_fresh, *a.scan, s);
+  // min tree over the depths
+  TreeLevels tl;
+  tl.n = 0;
+  size_t n = a.E_max, off = 0;
+  while (n > 32 && tl.n < 8) {
+    n = (n + 31) / 32;
+    tl.off[tl.n++] = off;
+    off += n;
+  }
+  for (int l = 1; l <= tl.n; l++) {
+    const int32_t* below = l == 1 ? a.depth : a.tree + tl.off[l - 2];
+    ++g_launches; tree_level_kernel<<<blocks(level_size_host(a.E_max, l)), T, 0, s>>>(below, a.tree + tl.off[l - 1], l, a.res);
+  }
+  ++g_launches; match_kernel<<<blocks(a.E_max), T, 0, s>>>(a, tl);
+  ++g_launches; resolve_kernel<<<blocks(a.E_max), T, 0, s>>>(a.ew, a.res);
+  // suffix minimum of the depths (stored after the tree levels)
+  int32_t* sufmin = a.tree + off;
+  scan_any<MinOp, true>(a.depth, sufmin, a.E_max, nE, true, nullptr, *a.scan, s);
+  ++g_launches; holes_out_kernel<<<blocks(a.E_max), T, 0, s>>>(a.etype, a.depth, sufmin, a.ew, a.holes_out, a.res, a.U0);
+}
+
+// ---------------------------------------------------------------------------
+// finalize: staging -> pool at the replayed indices, grid entries
+
+__global__ void __launch_bounds__(256) finalize_kernel(FinalizeArgs a) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t n = min(a.res->stage_count, 0xffffffffu);
+  for (uint32_t slot = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; slot < n; slot += (gridDim.x * blockDim.x) >> 5) {
+    const long long src = a.stage_src[slot];
+    uint32_t idx;
+    if (src >= 0) {
+      unsigned long long w = a.ew[a.H + a.pos[src]];
+      if (!(w & KNOWN)) { if (lane == 0) atomicOr(&a.res->status, (uint32_t)ST_CHAIN); continue; }
+      idx = (uint32_t)(w & 0xffffffffull);
+    } else {
+      idx = (uint32_t)(-(src + 1));
+    }
+    if (lane == 0) atomicMax(&a.res->max_pool_index, idx);
+    if (idx >= a.pool_cap) {
+      if (lane == 0) atomicOr(&a.res->status, (uint32_t)ST_POOL_OVERFLOW);
+      continue;
+    }
+    const uint4* s4 = reinterpret_cast<const uint4*>(a.staging32 + (size_t)slot * 256);
+    uint4* d4 = reinterpret_cast<uint4*>(a.pool32 + (size_t)idx * 256);
+    d4[lane] = s4[lane];
+    d4[lane + 32] = s4[lane + 32];
+    if (lane == 0) a.grid[a.stage_cell[slot]] = idx + 1;
+  }
+}
+
+void launch_finalize(const FinalizeArgs& a, uint32_t stage_cap, cudaStream_t s) {
+  size_t warps = stage_cap ? stage_cap : 1;
+  size_t b = (warps * 32 + 255) / 256;
+  int blocks = (int)(b < 8192 ? b : 8192);
+  ++g_launches; finalize_kernel<<<blocks, 256, 0, s>>>(a);
+}
+
+// ---------------------------------------------------------------------------
+// derive: super-grid counts and density (GpuWorld.ts:90-101, VoxelWorld.ts:159-170)
+
+__global__ void __launch_bounds__(256) derive_kernel(const uint32_t* __restrict__ grid, const uint32_t* __restrict__ pool32,
+                                                     int BX, int BY, int BZ, const uint8_t* __restrict__ opaque,
+                                                     const uint8_t* __restrict__ udens, uint32_t* super_counts, uint8_t* density) {
+  __shared__ uint8_t op_s[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) op_s[i] = opaque[i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int SX = (BX + 3) / 4, SY = (BY + 3) / 4, SZ = (BZ + 3) / 4;
+  const int n_super = SX * SY * SZ;
+  for (int sc = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; sc < n_super; sc += (gridDim.x * blockDim.x) >> 5) {
+    const int sz = sc / (SX * SY), r = sc - sz * SX * SY, sy = r / SX, sx = r - sy * SX;
+    uint32_t nz = 0;
+    uint32_t mixed_g[2] = {0, 0};
+    size_t mixed_ci[2] = {0, 0};
+    bool is_mixed[2] = {false, false};
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int k = lane + 32 * h;
+      const int bx = sx * 4 + (k & 3), by = sy * 4 + ((k >> 2) & 3), bz = sz * 4 + (k >> 4);
+      if (bx < BX && by < BY && bz < BZ) {
+        const size_t ci = (size_t)bx + (size_t)BX * ((size_t)by + (size_t)BY * bz);
+        const uint32_t g = grid[ci];
+        nz += g != 0;
+        if (g == 0) density[ci] = 0;
+        else if (g & UNIFORM) density[ci] = udens[g & 0xffu];
+        else { is_mixed[h] = true; mixed_g[h] = g; mixed_ci[h] = ci; }
+      }
+    }
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      uint32_t mm = __ballot_sync(FULLMASK, is_mixed[h]);
+      while (mm) {
+        const int src = __ffs(mm) - 1;
+        mm &= mm - 1;
+        const uint32_t g = __shfl_sync(FULLMASK, mixed_g[h], src);
+        const unsigned long long ci = __shfl_sync(FULLMASK, (unsigned long long)mixed_ci[h], src);
+        const uint32_t* b = pool32 + (size_t)(g - 1) * 256;
+        uint32_t cnt = 0;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          uint32_t w = b[32 * j + lane];
+          uint32_t v0 = w & 0xffffu, v1 = w >> 16;
+          cnt += (v0 != 0 && op_s[v0 & 0xffu]) + (v1 != 0 && op_s[v1 & 0xffu]);
+        }
+#pragma unroll
+        for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(FULLMASK, cnt, o);
+        if (lane == 0) density[ci] = (uint8_t)px_round(((double)cnt / 512.0) * 255.0);
+      }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) nz += __shfl_xor_sync(FULLMASK, nz, o);
+    if (lane == 0) super_counts[sc] = nz;
+  }
+}
+
+void launch_derive(const uint32_t* grid, const uint32_t* pool32, int BX, int BY, int BZ, const uint8_t* opaque,
+                   const uint8_t* udens, uint32_t* super_counts, uint8_t* density, cudaStream_t s) {
+  int n_super = ((BX + 3) / 4) * ((BY + 3) / 4) * ((BZ + 3) / 4);
+  size_t b = ((size_t)n_super * 32 + 255) / 256;
+  ++g_launches; derive_kernel<<<(int)(b < 65535 ? b : 65535), 256, 0, s>>>(grid, pool32, BX, BY, BZ, opaque, udens, super_counts, density);
+}
+
+// ---------------------------------------------------------------------------
+// peak probe: dependent FMA chains on every SM (roofline denominators)
+
+template <typename T>
+__global__ void __launch_bounds__(256) fma_probe_kernel(T* out, int iters, T a, T b) {
+  T x0 = (T)threadIdx.x, x1 = x0 + (T)1, x2 = x0 + (T)2, x3 = x0 + (T)3, x4 = x0 + (T)4, x5 = x0 + (T)5,
+    x6 = x0 + (T)6, x7 = x0 + (T)7;
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int k = 0; k < 16; k++) {
+      x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+      x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+  }
+  T r = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+  if (r == (T)-1.2345) out[threadIdx.x] = r;  // keeps the chains alive
+}
+
+float probe_fma_tflops(int fp64, int n_sms) {
+  void* out = nullptr;
+  cudaMalloc(&out, 1024 * 8);
+  const int blocks = n_sms * 8, threads = 256;
+  const int iters = fp64 ? 64 : 4096;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 0.f;
+  for (int rep = 0; rep < 4; rep++) {
+    cudaEventRecord(e0);
+    if (fp64) fma_probe_kernel<double><<<blocks, threads>>>((double*)out, iters, 0.999999, 1e-7);
+    else fma_probe_kernel<float><<<blocks, threads>>>((float*)out, iters, 0.999999f, 1e-7f);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    double flops = 2.0 * 8 * 16 * (double)iters * blocks * threads;
+    float tf = (float)(flops / (ms * 1e-3) / 1e12);
+    if (rep > 0 && tf > best) best = tf;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  return best;
+}
+
+}  // namespace px

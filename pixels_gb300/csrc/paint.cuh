@@ -1,0 +1,108 @@
+// Device counterparts of the scene's paint closures, evaluated in float64 in
+// every build mode (their floors, rounds and thresholds are discontinuous, so
+// they are always computed exactly as the reference computes them).
+#pragma once
+#include "jsmath.cuh"
+#include "px_internal.cuh"
+
+namespace px {
+
+__device__ __forceinline__ uint32_t vox_of(double mat, double shade) {  // materials.ts:108-110
+  return ((uint32_t)(long long)mat & 0xffu) | (((uint32_t)(long long)shade & 0xffu) << 8);
+}
+
+__device__ __forceinline__ uint32_t noise_hash(uint32_t ix, uint32_t iy, uint32_t iz, uint32_t seed) {
+  uint32_t h = seed ^ (ix * 0x8DA6B343u) ^ (iy * 0xD8163841u) ^ (iz * 0xCB1AB31Fu);
+  h ^= h >> 16; h *= 0x7FEB352Du; h ^= h >> 15; h *= 0x846CA68Bu; h ^= h >> 16;
+  return h;
+}
+
+// float32 triangle-wave sine of the synthetic noise paint; explicit
+// round-to-nearest intrinsics keep every step a separate float32 operation.
+__device__ __forceinline__ float sin_poly_f32(float t) {
+  float u = __fsub_rn(t, floorf(t));
+  float v = __fsub_rn(__fmul_rn(u, 4.0f), 2.0f);
+  float w = __fsub_rn(fabsf(v), 1.0f);
+  float w2 = __fmul_rn(w, w);
+  float p = __fsub_rn(__fmul_rn(w2, 0.0751f), 0.6432f);
+  p = __fadd_rn(__fmul_rn(p, w2), 1.5708f);
+  float r = __fmul_rn(p, w);
+  return v >= 0.0f ? r : -r;
+}
+
+__device__ __forceinline__ double sin_checked(double x, uint32_t& st) {
+  double r = px_sin(x);
+  if (r != r && x == x) st |= ST_RANGE;
+  return r;
+}
+
+// One paint call at a voxel centre (metres, after the optional frame).
+__device__ __noinline__ uint32_t paint_eval(uint32_t kind, const double* __restrict__ p, double x, double y, double z,
+                                            uint32_t& st) {
+  const double PI = 3.141592653589793;
+  switch (kind) {
+    case PK_CHIP: {  // penthouse.ts:371-377
+      double a = px_atan2(z - __ldg(p + 2), x - __ldg(p));
+      bool edge = px_hypot2(x - __ldg(p), z - __ldg(p + 2)) > __ldg(p + 3);
+      bool stripe = fmod(floor(((a + PI) / (2 * PI)) * 8), 2.0) == 0;
+      double layer = fmod(floor((y - __ldg(p + 1)) / 0.0045), 2.0);
+      return vox_of(__ldg(p + 4), edge && stripe && layer == 0 ? 255 : 0);
+    }
+    case PK_TUFTED: {  // penthouse.ts:495-501
+      double u = (z - __ldg(p)) / 0.16, v = (y - __ldg(p + 1)) / 0.16;
+      double ru = px_round(u), rv = px_round(v);
+      double du = u - ru, dv = v - rv;
+      bool odd = fmod(ru + rv, 2.0) == 0;
+      return vox_of(__ldg(p + 2), odd && px_hypot2(du, dv) < 0.12 ? 200 : 0);
+    }
+    case PK_CARD: {  // penthouse.ts:597-600
+      bool edge = fabs(x - __ldg(p) - __ldg(p + 2)) > 0.022 || fabs(z - __ldg(p + 1)) > 0.034;
+      return vox_of(__ldg(p + 3), edge ? 0 : 255);
+    }
+    case PK_WHITE: {  // penthouse.ts:744-748
+      double k = floor((x - __ldg(p)) / 0.0254);
+      double f = (x - __ldg(p)) / 0.0254 - k;
+      return vox_of(__ldg(p + 1), f < 0.12 ? 120 : 0);
+    }
+    case PK_BLACK: {  // penthouse.ts:749-756
+      double u = (x - __ldg(p)) / 0.0254;
+      double k = floor(u + 0.5);
+      double f = u + 0.5 - k;
+      double n = fmod(fmod(k - 1, 7.0) + 7, 7.0);
+      bool has = n == 0 || n == 1 || n == 3 || n == 4 || n == 5;
+      return has && fabs(f - 0.5) < 0.3 ? vox_of(__ldg(p + 1), 0) : 0u;
+    }
+    case PK_VASE: {  // penthouse.ts:810-816
+      double a = px_atan2(z - __ldg(p + 2), x - __ldg(p));
+      double h = (y - __ldg(p + 1)) / __ldg(p + 3);
+      bool band = (h > 0.04 && h < 0.06) || (h > 0.36 && h < 0.38) || (h > 0.47 && h < 0.49);
+      bool motif = h > 0.08 && h < 0.33 && sin_checked(a * 5 + sin_checked(h * 30, st) * 2, st) > 0.55;
+      return vox_of(__ldg(p + 4), band || motif ? 255 : 0);
+    }
+    case PK_PAINTING: {  // penthouse.ts:840-845
+      double shade = 0;
+      for (int i = 0; i < 9; i++) {
+        const double* b = p + 1 + 4 * i;
+        if (px_hypot2(x - __ldg(b), (y - __ldg(b + 1)) * 1.3) < __ldg(b + 2)) shade = __ldg(b + 3);
+      }
+      bool stripe = fabs(sin_checked(x * 9 + y * 3, st)) < 0.06;
+      return vox_of(__ldg(p), stripe ? 255 : shade);
+    }
+    case PK_NOISE: {  // synthetic scenes: integer hash + float32 sine
+      double sc = __ldg(p + 1);
+      double ix = floor(x * sc), iy = floor(y * sc), iz = floor(z * sc);
+      uint32_t h = noise_hash((uint32_t)(long long)ix, (uint32_t)(long long)iy, (uint32_t)(long long)iz,
+                              (uint32_t)(long long)__ldg(p));
+      float jitter = __fmul_rn((float)(h & 0xffffu), 1.0f / 65536.0f);
+      float a = __fmul_rn(__double2float_rn(x), __double2float_rn(__ldg(p + 2)));
+      float b = __fmul_rn(__double2float_rn(y), __double2float_rn(__ldg(p + 3)));
+      float c = __fmul_rn(__double2float_rn(z), __double2float_rn(__ldg(p + 4)));
+      float t = __fadd_rn(__fadd_rn(__fadd_rn(a, b), c), jitter);
+      float s = sin_poly_f32(t);
+      return s > __double2float_rn(__ldg(p + 5)) ? (uint32_t)__ldg(p + 6) : (uint32_t)__ldg(p + 7);
+    }
+  }
+  return 0;
+}
+
+}  // namespace px

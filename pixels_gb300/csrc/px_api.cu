@@ -1,0 +1,654 @@
+// Host runtime of the C ABI (include/pixels_gb300.h): world state, PXIR
+// validation, per-op derived data, device buffers and the launch sequence of
+// one build.  Compiled with -ffp-contract=off: the per-op float64 constants
+// (voxel ranges, classify thresholds) must round exactly as the reference's
+// JavaScript does (shapes.ts:341-350).
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/pixels_gb300.h"
+#include "px_internal.cuh"
+
+using namespace px;
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace
+
+struct px_world {
+  int dx, dy, dz, BX, BY, BZ, TX, TY, TZ;
+  double vpm, vs;
+  size_t ncells, ntiles;
+  int n_sms = 0;
+
+  // world state on the device
+  uint32_t* d_grid = nullptr;
+  uint32_t* d_pool32 = nullptr;   // pool as voxel pairs (capacity * 256 words)
+  uint32_t pool_cap = 0;
+  uint32_t pool_used = 0;
+  uint32_t n_holes = 0;
+  DevBuf holes_a, holes_b;        // current free list (holes), double-buffered across builds
+  bool holes_in_a = true;
+
+  // ops queued by px_submit_ops (and the ops of the last committed build)
+  std::vector<OpDev> ops, last_ops;
+  std::vector<uint2> last_boxes, last_code;
+  std::vector<double> last_params;
+  bool ops_resident = false;   // the device op tables already hold `ops`
+  std::vector<uint2> boxes;
+  std::vector<uint2> code;
+  std::vector<double> params;
+  uint64_t ops_applied = 0;
+
+  // per-build device scratch
+  DevBuf d_ops, d_boxes, d_code, d_params;
+  DevBuf tile_cnt, tile_off, tiles_nonempty, tile_ops;
+  DevBuf evt, fsrc, cnt, pos, etype, ew, depth_fn, depth, tree, fresh, fresh_rank;
+  DevBuf staging, stage_cell, stage_src;
+  DevBuf scan_agg;
+  DevBuf work_counter;
+  DevBuf res;
+  DevBuf opaque, udens, super_counts, density;
+  BuildResult* h_res = nullptr;   // pinned
+  std::vector<unsigned char> h_upload;
+
+  // in-flight build
+  bool in_flight = false;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_fold0 = nullptr, ev_fold1 = nullptr;
+  size_t last_P = 0;
+  uint32_t last_stage_cap = 0;
+  uint32_t last_H = 0, last_U0 = 0;
+  FinalizeArgs fin{};
+  bool derived_valid = false;
+
+  px_stats stats{};
+  std::string err;
+};
+
+namespace {
+
+int fail(px_world* w, int code, const char* fmt, ...) {
+  if (w) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    w->err = buf;
+  }
+  return code;
+}
+
+#define CU(call)                                                                           \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) return fail(w, PX_E_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+int ensure(px_world* w, DevBuf& b, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (b.bytes >= bytes) return PX_OK;
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+  size_t want = bytes + bytes / 4;
+  if (cudaMalloc(&b.p, want) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(w, PX_E_OOM, "cudaMalloc of %zu bytes failed", want);
+  }
+  b.bytes = want;
+  return PX_OK;
+}
+void release(DevBuf& b) {
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+}
+
+inline double js_max(double a, double b) { return a > b ? a : b; }  // finite inputs (validated)
+inline double js_min(double a, double b) { return a < b ? a : b; }
+
+// Validate one op's SDF bytecode: opcodes, parameter ranges, finite values,
+// stack and rotation depths the device evaluator holds.
+bool check_code(const uint32_t* code, uint32_t n, const double* P, size_t np, std::string& why) {
+  int depth = 0, rot = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    uint32_t w0 = code[2 * i], off = code[2 * i + 1];
+    uint32_t op = w0 & 0xffu, cnt = w0 >> 8;
+    size_t need = 0;
+    switch (op) {
+      case OP_BOX: need = 6; break;
+      case OP_ROUNDBOX: need = 7; break;
+      case OP_SPHERE: need = 4; break;
+      case OP_ELLIPSOID: need = 7; break;
+      case OP_CYL_X: case OP_CYL_Y: case OP_CYL_Z: need = 5; break;
+      case OP_CAPSULE: need = 8; break;
+      case OP_TORUS_X: case OP_TORUS_Y: case OP_TORUS_Z: need = 5; break;
+      case OP_STADIUM: need = 6; break;
+      case OP_LATHE_SOLID:
+        if (cnt < 2) { why = "lathe polygon needs 2+ points"; return false; }
+        need = 3 + 2 * (size_t)cnt; break;
+      case OP_LATHE_SHELL:
+        if (cnt < 2) { why = "lathe profile needs 2+ points"; return false; }
+        need = 4 + 2 * (size_t)cnt; break;
+      case OP_PRISM:
+        if (cnt < 3) { why = "prism needs 3+ points"; return false; }
+        need = 4 + 2 * (size_t)cnt; break;
+      case OP_ROT_X: case OP_ROT_Y: case OP_ROT_Z:
+        need = 4;
+        if (++rot > MAX_ROT) { why = "rotations nested deeper than 3"; return false; }
+        break;
+      case OP_ROT_END:
+        if (--rot < 0) { why = "unmatched rotation end"; return false; }
+        break;
+      case OP_OFFSET: need = 1; if (depth < 1) { why = "offset of nothing"; return false; } break;
+      case OP_NEGMAX: case OP_MAX: case OP_MIN:
+        if (depth < 2) { why = "combinator needs two operands"; return false; }
+        depth--; break;
+      default: why = "unknown opcode"; return false;
+    }
+    if (need) {
+      if ((size_t)off + need > np) { why = "parameters out of range"; return false; }
+      for (size_t k = 0; k < need; k++)
+        if (!std::isfinite(P[off + k])) { why = "non-finite parameter"; return false; }
+    }
+    if (op < OP_ROT_X) {
+      if (++depth > MAX_STACK) { why = "SDF stack deeper than 4"; return false; }
+    }
+  }
+  if (depth != 1 || rot != 0) { why = "bytecode does not leave exactly one distance"; return false; }
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int px_world_create(int dx, int dy, int dz, double vpm, uint32_t initial_pool_bricks, px_world** out) {
+  if (!out) return PX_E_INVALID_ARG;
+  *out = nullptr;
+  if (dx <= 0 || dy <= 0 || dz <= 0 || dx % 8 || dy % 8 || dz % 8) return PX_E_INVALID_ARG;
+  if (dx / 8 > MAX_AXIS_BRICKS || dy / 8 > MAX_AXIS_BRICKS || dz / 8 > MAX_AXIS_BRICKS) return PX_E_INVALID_ARG;
+  if (!(vpm > 0) || !std::isfinite(vpm)) return PX_E_INVALID_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return PX_E_NO_DEVICE;
+  }
+  px_world* w = new px_world();
+  w->dx = dx; w->dy = dy; w->dz = dz;
+  w->BX = dx / 8; w->BY = dy / 8; w->BZ = dz / 8;
+  w->TX = (w->BX + 3) / 4; w->TY = (w->BY + 3) / 4; w->TZ = (w->BZ + 3) / 4;
+  w->vpm = vpm;
+  w->vs = 1 / vpm;  // config.ts:13
+  w->ncells = (size_t)w->BX * w->BY * w->BZ;
+  w->ntiles = (size_t)w->TX * w->TY * w->TZ;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&w->n_sms, cudaDevAttrMultiProcessorCount, dev);
+  int rc;
+  DevBuf g;
+  if ((rc = ensure(w, g, w->ncells * 4)) != PX_OK) { delete w; return rc; }
+  w->d_grid = (uint32_t*)g.p;
+  if (cudaMemset(w->d_grid, 0, w->ncells * 4) != cudaSuccess) { delete w; return PX_E_CUDA; }
+  uint32_t cap = initial_pool_bricks ? initial_pool_bricks : 1;
+  if (cudaMalloc((void**)&w->d_pool32, (size_t)cap * 1024) != cudaSuccess) { cudaFree(w->d_grid); delete w; return PX_E_OOM; }
+  w->pool_cap = cap;
+  if (cudaMallocHost((void**)&w->h_res, sizeof(BuildResult)) != cudaSuccess) { delete w; return PX_E_OOM; }
+  cudaEventCreate(&w->ev0);
+  cudaEventCreate(&w->ev1);
+  cudaEventCreate(&w->ev_fold0);
+  cudaEventCreate(&w->ev_fold1);
+  // material tables (VoxelWorld.ts:159-170,190-196): filled by px_set_tables or the defaults
+  uint8_t op_tab[256], ud_tab[256];
+  for (int i = 0; i < 256; i++) { op_tab[i] = i ? 1 : 0; ud_tab[i] = 255; }
+  ensure(w, w->opaque, 256);
+  ensure(w, w->udens, 256);
+  cudaMemcpy(w->opaque.p, op_tab, 256, cudaMemcpyHostToDevice);
+  cudaMemcpy(w->udens.p, ud_tab, 256, cudaMemcpyHostToDevice);
+  *out = w;
+  return PX_OK;
+}
+
+// Opacity (OPAQUE, VoxelWorld.ts:190-196) and uniform-brick density per material id.
+int px_set_material_tables(px_world* w, const uint8_t* opaque256, const uint8_t* uniform_density256) {
+  if (!w || !opaque256 || !uniform_density256) return PX_E_INVALID_ARG;
+  CU(cudaMemcpy(w->opaque.p, opaque256, 256, cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(w->udens.p, uniform_density256, 256, cudaMemcpyHostToDevice));
+  w->derived_valid = false;
+  return PX_OK;
+}
+
+void px_world_destroy(px_world* w) {
+  if (!w) return;
+  if (w->in_flight) cudaStreamSynchronize(w->stream);
+  cudaFree(w->d_grid);
+  cudaFree(w->d_pool32);
+  DevBuf* bufs[] = {&w->holes_a, &w->holes_b, &w->d_ops, &w->d_boxes, &w->d_code, &w->d_params, &w->tile_cnt,
+                    &w->tile_off, &w->tiles_nonempty, &w->tile_ops, &w->evt, &w->fsrc, &w->cnt, &w->pos, &w->etype,
+                    &w->ew, &w->depth_fn, &w->depth, &w->tree, &w->fresh, &w->fresh_rank, &w->staging,
+                    &w->stage_cell, &w->stage_src, &w->scan_agg, &w->work_counter, &w->res, &w->opaque,
+                    &w->udens, &w->super_counts, &w->density};
+  for (DevBuf* b : bufs) release(*b);
+  if (w->h_res) cudaFreeHost(w->h_res);
+  if (w->ev0) cudaEventDestroy(w->ev0);
+  if (w->ev1) cudaEventDestroy(w->ev1);
+  if (w->ev_fold0) cudaEventDestroy(w->ev_fold0);
+  if (w->ev_fold1) cudaEventDestroy(w->ev_fold1);
+  delete w;
+}
+
+int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
+  if (!w || (!ir && bytes)) return PX_E_INVALID_ARG;
+  if (w->in_flight) return fail(w, PX_E_INVALID_ARG, "a build is in flight");
+  w->ops_resident = false;
+  if (bytes < 32) return fail(w, PX_E_INVALID_IR, "IR shorter than its header");
+  const uint32_t* h = (const uint32_t*)ir;
+  if (h[0] != 0x52495850u || h[1] != 1u) return fail(w, PX_E_INVALID_IR, "not a PXIR v1 buffer");
+  const size_t n_ops = h[2], n_code = h[3], n_params = h[4];
+  const size_t need = 32 + n_ops * sizeof(IrOp) + n_code * 8 + n_params * 8;
+  if (bytes < need) return fail(w, PX_E_INVALID_IR, "IR truncated (%zu < %zu bytes)", bytes, need);
+  const IrOp* iops = (const IrOp*)((const char*)ir + 32);
+  const uint32_t* code = (const uint32_t*)((const char*)ir + 32 + n_ops * sizeof(IrOp));
+  std::vector<double> P(n_params);
+  std::memcpy(P.data(), (const char*)ir + 32 + n_ops * sizeof(IrOp) + n_code * 8, n_params * 8);
+
+  const size_t code_base = w->code.size(), param_base = w->params.size();
+  std::vector<OpDev> nops;
+  std::vector<uint2> nboxes;
+  nops.reserve(n_ops);
+  const double vs = w->vs;
+  for (size_t i = 0; i < n_ops; i++) {
+    const IrOp& o = iops[i];
+    std::string why;
+    if (o.kind > 2) return fail(w, PX_E_INVALID_IR, "op %zu: bad kind", i);
+    if (o.paint_kind >= PK_COUNT) return fail(w, PX_E_INVALID_IR, "op %zu: unknown paint kind", i);
+    if (o.paint_kind == PK_CONST && o.paint_value > 0xffffu) return fail(w, PX_E_INVALID_IR, "op %zu: paint is not a u16", i);
+    if (o.paint_kind != PK_CONST) {
+      size_t np = (size_t)PAINT_NPARAMS[o.paint_kind];
+      if ((size_t)o.paint_param + np > n_params) return fail(w, PX_E_INVALID_IR, "op %zu: paint parameters out of range", i);
+      for (size_t k = 0; k < np; k++)
+        if (!std::isfinite(P[o.paint_param + k])) return fail(w, PX_E_INVALID_IR, "op %zu: non-finite paint parameter", i);
+    }
+    for (int k = 0; k < 3; k++)
+      if (!std::isfinite(o.mn[k]) || !std::isfinite(o.mx[k])) return fail(w, PX_E_INVALID_IR, "op %zu: non-finite bounds", i);
+    if (!std::isfinite(o.slack)) return fail(w, PX_E_INVALID_IR, "op %zu: non-finite slack", i);
+    for (int k = 0; k < 4; k++)
+      if (!std::isfinite(o.frame[k])) return fail(w, PX_E_INVALID_IR, "op %zu: non-finite paint frame", i);
+    if (o.code_len == 0 || (size_t)o.code_begin + o.code_len > n_code) return fail(w, PX_E_INVALID_IR, "op %zu: code range", i);
+    if (!check_code(code + 2 * (size_t)o.code_begin, o.code_len, P.data(), n_params, why))
+      return fail(w, PX_E_INVALID_IR, "op %zu: %s", i, why.c_str());
+
+    OpDev d{};
+    d.kind = o.kind;
+    d.flags = o.flags;
+    d.paint_kind = o.paint_kind;
+    d.paint_value = o.paint_value;
+    d.code_off = (uint32_t)(code_base + o.code_begin);
+    d.code_len = o.code_len;
+    d.paint_off = (uint32_t)(param_base + o.paint_param);
+    for (int k = 0; k < 3; k++) { d.mn[k] = o.mn[k]; d.mx[k] = o.mx[k]; }
+    for (int k = 0; k < 4; k++) d.frame[k] = o.frame[k];
+    // shapes.ts:341-347: voxel range of the op, clamped to the world
+    double vx0 = js_max(0, std::floor(o.mn[0] / vs - 0.5)), vy0 = js_max(0, std::floor(o.mn[1] / vs - 0.5)),
+           vz0 = js_max(0, std::floor(o.mn[2] / vs - 0.5));
+    double vx1 = js_min(w->dx - 1, std::ceil(o.mx[0] / vs + 0.5)), vy1 = js_min(w->dy - 1, std::ceil(o.mx[1] / vs + 0.5)),
+           vz1 = js_min(w->dz - 1, std::ceil(o.mx[2] / vs + 0.5));
+    uint2 box;
+    if (vx0 > vx1 || vy0 > vy1 || vz0 > vz1) {
+      d.bx0 = d.by0 = d.bz0 = 1; d.bx1 = d.by1 = d.bz1 = 0; d.nx = d.ny = 0;
+      box = make_uint2(3u << 30, 0u);
+    } else {
+      d.bx0 = (int)vx0 >> 3; d.by0 = (int)vy0 >> 3; d.bz0 = (int)vz0 >> 3;
+      d.bx1 = (int)vx1 >> 3; d.by1 = (int)vy1 >> 3; d.bz1 = (int)vz1 >> 3;
+      d.nx = d.bx1 - d.bx0 + 1; d.ny = d.by1 - d.by0 + 1;
+      box = make_uint2((uint32_t)d.bx0 | ((uint32_t)d.by0 << 10) | ((uint32_t)d.bz0 << 20),
+                       (uint32_t)d.bx1 | ((uint32_t)d.by1 << 10) | ((uint32_t)d.bz1 << 20));
+    }
+    // shapes.ts:349-350
+    d.bhd = 4 * std::sqrt(3.0) * vs * o.slack + vs * 0.01;
+    d.shd = 2 * std::sqrt(3.0) * vs * o.slack + vs * 0.01;
+    nops.push_back(d);
+    nboxes.push_back(box);
+  }
+  w->code.resize(code_base + n_code);
+  std::memcpy(w->code.data() + code_base, code, n_code * 8);
+  // parameter offsets in the code are relative to this IR's parameter block
+  for (size_t i = 0; i < n_code; i++) w->code[code_base + i].y += (uint32_t)param_base;
+  w->params.insert(w->params.end(), P.begin(), P.end());
+  w->ops.insert(w->ops.end(), nops.begin(), nops.end());
+  w->boxes.insert(w->boxes.end(), nboxes.begin(), nboxes.end());
+  return PX_OK;
+}
+
+int px_build_enqueue(px_world* w, int mode, void* stream) {
+  if (!w) return PX_E_INVALID_ARG;
+  if (w->in_flight) return fail(w, PX_E_INVALID_ARG, "a build is already in flight");
+  if (mode != PX_MODE_FP64 && mode != PX_MODE_MIXED) return fail(w, PX_E_INVALID_ARG, "unknown mode %d", mode);
+  cudaStream_t s = (cudaStream_t)stream;
+  w->stream = s;
+  const int n_ops = (int)w->ops.size();
+  int rc;
+
+  // (op, brick) pair bases and the tile-list bound
+  uint64_t P = 0, tile_pairs = 0;
+  for (int i = 0; i < n_ops; i++) {
+    OpDev& o = w->ops[i];
+    o.pair_base = P;
+    if (o.bx0 > o.bx1) continue;
+    uint64_t nz = (uint64_t)(o.bz1 - o.bz0 + 1);
+    P += (uint64_t)o.nx * o.ny * nz;
+    uint64_t tx = (uint64_t)(o.bx1 / 4 - o.bx0 / 4 + 1), ty = (uint64_t)(o.by1 / 4 - o.by0 / 4 + 1),
+             tz = (uint64_t)(o.bz1 / 4 - o.bz0 / 4 + 1);
+    tile_pairs += tx * ty * tz;
+  }
+  if (P > 0x7fffffffull) return fail(w, PX_E_QUEUE_OVERFLOW, "too many (op, brick) pairs in one build: %llu", (unsigned long long)P);
+  const uint64_t touched_bound = P < w->ncells ? P : w->ncells;
+  const uint32_t H = w->n_holes, U0 = w->pool_used;
+  const size_t E_max = (size_t)H + 2 * P;
+
+  // pool capacity: poolUsed can grow by at most the number of touched bricks
+  uint64_t need_cap = (uint64_t)U0 + touched_bound;
+  if (need_cap > w->pool_cap) {
+    uint64_t cap = w->pool_cap;
+    while (cap < need_cap) cap = (uint64_t)std::ceil(cap * 1.5) + 1;  // growPool (VoxelWorld.ts:129-136)
+    if (cap > 0xffffffffull / 2) return fail(w, PX_E_OOM, "pool too large");
+    uint32_t* np_ = nullptr;
+    if (cudaMalloc((void**)&np_, (size_t)cap * 1024) != cudaSuccess) { cudaGetLastError(); return fail(w, PX_E_OOM, "pool of %llu bricks", (unsigned long long)cap); }
+    if (U0) CU(cudaMemcpyAsync(np_, w->d_pool32, (size_t)U0 * 1024, cudaMemcpyDeviceToDevice, s));
+    CU(cudaStreamSynchronize(s));
+    cudaFree(w->d_pool32);
+    w->d_pool32 = np_;
+    w->pool_cap = (uint32_t)cap;
+  }
+
+  // scratch
+  if ((rc = ensure(w, w->d_ops, sizeof(OpDev) * (size_t)n_ops)) ||
+      (rc = ensure(w, w->d_boxes, sizeof(uint2) * (size_t)n_ops)) ||
+      (rc = ensure(w, w->d_code, sizeof(uint2) * w->code.size())) ||
+      (rc = ensure(w, w->d_params, sizeof(double) * w->params.size())) ||
+      (rc = ensure(w, w->tile_cnt, 4 * w->ntiles)) || (rc = ensure(w, w->tile_off, 4 * w->ntiles)) ||
+      (rc = ensure(w, w->tiles_nonempty, 4 * w->ntiles)) || (rc = ensure(w, w->tile_ops, 4 * tile_pairs)) ||
+      (rc = ensure(w, w->evt, P)) || (rc = ensure(w, w->fsrc, 8 * P)) || (rc = ensure(w, w->cnt, 4 * P)) ||
+      (rc = ensure(w, w->pos, 4 * P)) || (rc = ensure(w, w->etype, E_max)) || (rc = ensure(w, w->ew, 8 * E_max)) ||
+      (rc = ensure(w, w->depth_fn, 8 * E_max)) || (rc = ensure(w, w->depth, 4 * E_max)) ||
+      (rc = ensure(w, w->tree, 4 * (E_max / 16 + 64 + E_max))) || (rc = ensure(w, w->fresh, 4 * E_max)) ||
+      (rc = ensure(w, w->fresh_rank, 4 * E_max)) || (rc = ensure(w, w->staging, 1024 * touched_bound)) ||
+      (rc = ensure(w, w->stage_cell, 4 * touched_bound)) || (rc = ensure(w, w->stage_src, 8 * touched_bound)) ||
+      (rc = ensure(w, w->work_counter, 16)) || (rc = ensure(w, w->res, sizeof(BuildResult))))
+    return rc;
+  {
+    size_t items = w->ntiles > E_max ? w->ntiles : E_max;
+    if (P > items) items = P;
+    size_t nb = items / scan_items_per_block() + 2;
+    if ((rc = ensure(w, w->scan_agg, 8 * nb))) return rc;
+  }
+  DevBuf& holes_in = w->holes_in_a ? w->holes_a : w->holes_b;
+  DevBuf& holes_out = w->holes_in_a ? w->holes_b : w->holes_a;
+  if ((rc = ensure(w, holes_in, 4 * (size_t)H + 4)) || (rc = ensure(w, holes_out, 4 * E_max + 4))) return rc;
+
+  // upload the ops (one pinned staging copy per array)
+  for (int i = 0; i < n_ops; i++) {
+    OpDev& o = w->ops[i];
+    o.bhd32 = (float)o.bhd; o.shd32 = (float)o.shd; o.err32 = 0.f;
+  }
+  const unsigned long long launches0 = launch_count();
+  CU(cudaEventRecord(w->ev0, s));
+  if (!w->ops_resident) {
+    CU(cudaMemcpyAsync(w->d_ops.p, w->ops.data(), sizeof(OpDev) * (size_t)n_ops, cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(w->d_boxes.p, w->boxes.data(), sizeof(uint2) * (size_t)n_ops, cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(w->d_code.p, w->code.data(), sizeof(uint2) * w->code.size(), cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(w->d_params.p, w->params.data(), sizeof(double) * w->params.size(), cudaMemcpyHostToDevice, s));
+  }
+  CU(cudaMemsetAsync(w->res.p, 0, sizeof(BuildResult), s));
+  CU(cudaMemsetAsync(w->work_counter.p, 0, 16, s));
+  if (P) CU(cudaMemsetAsync(w->evt.p, 0, P, s));
+
+  BuildResult* res = (BuildResult*)w->res.p;
+  ScanTemp st{w->scan_agg.p, w->scan_agg.bytes / 8};
+  launch_cull_count((const uint2*)w->d_boxes.p, n_ops, w->TX, w->TY, w->TZ, (uint32_t*)w->tile_cnt.p,
+                    (uint32_t*)w->tiles_nonempty.p, res, s);
+  launch_scan_u32((const uint32_t*)w->tile_cnt.p, (uint32_t*)w->tile_off.p, w->ntiles, nullptr, false, nullptr, st, s);
+  launch_cull_fill((const uint2*)w->d_boxes.p, n_ops, w->TX, w->TY, w->TZ, (const uint32_t*)w->tile_off.p,
+                   (uint32_t*)w->tile_ops.p, s);
+  FoldArgs fa{};
+  fa.ops = (const OpDev*)w->d_ops.p;
+  fa.code = (const uint2*)w->d_code.p;
+  fa.params = (const double*)w->d_params.p;
+  fa.tile_off = (const uint32_t*)w->tile_off.p;
+  fa.tile_cnt = (const uint32_t*)w->tile_cnt.p;
+  fa.tile_ops = (const uint32_t*)w->tile_ops.p;
+  fa.tiles_nonempty = (const uint32_t*)w->tiles_nonempty.p;
+  fa.BX = w->BX; fa.BY = w->BY; fa.BZ = w->BZ; fa.TX = w->TX; fa.TY = w->TY;
+  fa.vs = w->vs;
+  fa.grid = w->d_grid;
+  fa.pool32 = w->d_pool32;
+  fa.evt = (uint8_t*)w->evt.p;
+  fa.fsrc = (int64_t*)w->fsrc.p;
+  fa.staging32 = (uint32_t*)w->staging.p;
+  fa.stage_cap = (uint32_t)touched_bound;
+  fa.stage_cell = (uint32_t*)w->stage_cell.p;
+  fa.stage_src = (int64_t*)w->stage_src.p;
+  fa.work_counter = (uint32_t*)w->work_counter.p;
+  fa.res = res;
+  CU(cudaEventRecord(w->ev_fold0, s));
+  launch_fold(fa, mode, w->n_sms, s);
+  CU(cudaEventRecord(w->ev_fold1, s));
+
+  ReplayArgs ra{};
+  ra.P = P; ra.E_max = E_max; ra.H = H; ra.U0 = U0;
+  ra.evt = (const uint8_t*)w->evt.p;
+  ra.fsrc = (const int64_t*)w->fsrc.p;
+  ra.holes_in = (const uint32_t*)holes_in.p;
+  ra.cnt = (uint32_t*)w->cnt.p;
+  ra.pos = (uint32_t*)w->pos.p;
+  ra.etype = (uint8_t*)w->etype.p;
+  ra.ew = (unsigned long long*)w->ew.p;
+  ra.depth_fn = (int2*)w->depth_fn.p;
+  ra.depth = (int32_t*)w->depth.p;
+  ra.tree = (int32_t*)w->tree.p;
+  ra.tree_words = w->tree.bytes / 4;
+  ra.fresh = (uint32_t*)w->fresh.p;
+  ra.fresh_rank = (uint32_t*)w->fresh_rank.p;
+  ra.holes_out = (uint32_t*)holes_out.p;
+  ra.res = res;
+  ra.scan = &st;
+  launch_replay(ra, s);
+
+  FinalizeArgs& fn = w->fin;
+  fn.staging32 = (const uint32_t*)w->staging.p;
+  fn.stage_cell = (const uint32_t*)w->stage_cell.p;
+  fn.stage_src = (const int64_t*)w->stage_src.p;
+  fn.pos = (const uint32_t*)w->pos.p;
+  fn.ew = (const unsigned long long*)w->ew.p;
+  fn.H = H;
+  fn.grid = w->d_grid;
+  fn.pool32 = w->d_pool32;
+  fn.pool_cap = w->pool_cap;
+  fn.res = res;
+  launch_finalize(fn, (uint32_t)touched_bound, s);
+  CU(cudaGetLastError());
+  w->stats.kernel_launches = (uint32_t)(launch_count() - launches0);
+  CU(cudaEventRecord(w->ev1, s));
+  CU(cudaMemcpyAsync(w->h_res, res, sizeof(BuildResult), cudaMemcpyDeviceToHost, s));
+  w->in_flight = true;
+  w->last_P = P;
+  w->last_stage_cap = (uint32_t)touched_bound;
+  w->last_H = H;
+  w->last_U0 = U0;
+  return PX_OK;
+}
+
+int px_build_finish(px_world* w) {
+  if (!w) return PX_E_INVALID_ARG;
+  if (!w->in_flight) return PX_OK;
+  w->in_flight = false;
+  CU(cudaStreamSynchronize(w->stream));
+  const BuildResult& r = *w->h_res;
+  float ms = 0.f, fold_ms = 0.f;
+  cudaEventElapsedTime(&ms, w->ev0, w->ev1);
+  cudaEventElapsedTime(&fold_ms, w->ev_fold0, w->ev_fold1);
+  w->stats.fold_ms = fold_ms;
+  w->stats.pairs = w->last_P;
+  w->stats.brick_evals = r.c.brick_evals;
+  w->stats.sub_evals = r.c.sub_evals;
+  w->stats.voxel_evals = r.c.voxel_evals;
+  w->stats.paint_evals = r.c.paint_evals;
+  w->stats.rescued = r.c.rescued;
+  w->stats.alloc_events = r.c.alloc_events;
+  w->stats.free_events = r.c.free_events;
+  w->stats.max_abs_err32 = r.max_err;
+  w->stats.build_ms = ms;
+  w->stats.status = r.status;
+  if (r.status & (ST_STAGE_OVERFLOW | ST_POOL_OVERFLOW | ST_CHAIN))
+    return fail(w, PX_E_QUEUE_OVERFLOW, "device status 0x%x (stage %u of %u, max pool index %u of %u)", r.status,
+                r.stage_count, w->last_stage_cap, r.max_pool_index, w->pool_cap);
+  // the build is committed: holes/pool counters move to the new state
+  w->pool_used = r.pool_used;
+  w->n_holes = r.n_holes;
+  w->holes_in_a = !w->holes_in_a;
+  w->ops_applied += w->ops.size();
+  w->last_ops.swap(w->ops);
+  w->last_boxes.swap(w->boxes);
+  w->last_code.swap(w->code);
+  w->last_params.swap(w->params);
+  w->ops.clear();
+  w->boxes.clear();
+  w->code.clear();
+  w->params.clear();
+  w->derived_valid = false;
+  w->stats.ops_applied = w->ops_applied;
+  w->stats.pool_used = w->pool_used;
+  w->stats.n_holes = w->n_holes;
+  w->stats.pool_capacity = w->pool_cap;
+  if (r.status & ST_RANGE) return fail(w, PX_E_RANGE, "a paint function received an argument outside its supported range");
+  return PX_OK;
+}
+
+int px_build(px_world* w, int mode, void* stream) {
+  int rc = px_build_enqueue(w, mode, stream);
+  if (rc) return rc;
+  return px_build_finish(w);
+}
+
+int px_world_reset(px_world* w, int requeue_last_ops, void* stream) {
+  if (!w) return PX_E_INVALID_ARG;
+  if (w->in_flight) return fail(w, PX_E_INVALID_ARG, "a build is in flight");
+  CU(cudaMemsetAsync(w->d_grid, 0, w->ncells * 4, (cudaStream_t)stream));
+  w->pool_used = 0;
+  w->n_holes = 0;
+  w->derived_valid = false;
+  if (requeue_last_ops) {
+    if (!w->ops.empty()) return fail(w, PX_E_INVALID_ARG, "ops are already queued");
+    w->ops = w->last_ops;
+    w->boxes = w->last_boxes;
+    w->code = w->last_code;
+    w->params = w->last_params;
+    w->ops_resident = true;  // the device tables of the last build still hold them
+  }
+  return PX_OK;
+}
+
+int px_read_grid(px_world* w, uint32_t* dst, size_t n) {
+  if (!w || !dst || n < w->ncells) return PX_E_INVALID_ARG;
+  CU(cudaMemcpy(dst, w->d_grid, w->ncells * 4, cudaMemcpyDeviceToHost));
+  return PX_OK;
+}
+int px_read_pool(px_world* w, uint16_t* dst, size_t n) {
+  if (!w || (!dst && w->pool_used) || n < (size_t)w->pool_used * 512) return PX_E_INVALID_ARG;
+  if (w->pool_used) CU(cudaMemcpy(dst, w->d_pool32, (size_t)w->pool_used * 1024, cudaMemcpyDeviceToHost));
+  return PX_OK;
+}
+int px_read_holes(px_world* w, uint32_t* dst, size_t n) {
+  if (!w || n < w->n_holes) return PX_E_INVALID_ARG;
+  DevBuf& cur = w->holes_in_a ? w->holes_a : w->holes_b;
+  if (w->n_holes) CU(cudaMemcpy(dst, cur.p, (size_t)w->n_holes * 4, cudaMemcpyDeviceToHost));
+  return PX_OK;
+}
+
+int px_derive(px_world* w) {
+  if (!w) return PX_E_INVALID_ARG;
+  int rc;
+  size_t nsup = w->ntiles;
+  if ((rc = ensure(w, w->super_counts, 4 * nsup)) || (rc = ensure(w, w->density, w->ncells))) return rc;
+  launch_derive(w->d_grid, w->d_pool32, w->BX, w->BY, w->BZ, (const uint8_t*)w->opaque.p, (const uint8_t*)w->udens.p,
+                (uint32_t*)w->super_counts.p, (uint8_t*)w->density.p, 0);
+  CU(cudaGetLastError());
+  CU(cudaDeviceSynchronize());
+  w->derived_valid = true;
+  return PX_OK;
+}
+int px_read_super(px_world* w, uint32_t* dst, size_t n) {
+  if (!w || !dst || n < w->ntiles) return PX_E_INVALID_ARG;
+  if (!w->derived_valid) { int rc = px_derive(w); if (rc) return rc; }
+  CU(cudaMemcpy(dst, w->super_counts.p, w->ntiles * 4, cudaMemcpyDeviceToHost));
+  return PX_OK;
+}
+int px_read_density(px_world* w, uint8_t* dst, size_t n) {
+  if (!w || !dst || n < w->ncells) return PX_E_INVALID_ARG;
+  if (!w->derived_valid) { int rc = px_derive(w); if (rc) return rc; }
+  CU(cudaMemcpy(dst, w->density.p, w->ncells, cudaMemcpyDeviceToHost));
+  return PX_OK;
+}
+// GpuWorld.ts:55-60, 103-109
+int px_read_free_list(px_world* w, uint32_t max_bricks, uint32_t* dst, size_t n, uint32_t* out_len) {
+  if (!w) return PX_E_INVALID_ARG;
+  uint64_t used = w->pool_used;
+  uint64_t cap = used + 98304 > used * 2 ? used + 98304 : used * 2;
+  if (cap > max_bricks) cap = max_bricks;
+  if (used > cap) return fail(w, PX_E_OOM, "the scene needs %llu bricks but the pool holds %llu", (unsigned long long)used, (unsigned long long)cap);
+  uint64_t len = w->n_holes + (cap - used);
+  if (out_len) *out_len = (uint32_t)len;
+  if (!dst) return PX_OK;
+  if (n < len) return PX_E_INVALID_ARG;
+  int rc = px_read_holes(w, dst, n);
+  if (rc) return rc;
+  for (uint64_t i = 0; i < cap - used; i++) dst[w->n_holes + i] = (uint32_t)(cap - 1 - i);
+  return PX_OK;
+}
+
+int px_get_stats(px_world* w, px_stats* out) {
+  if (!w || !out) return PX_E_INVALID_ARG;
+  *out = w->stats;
+  out->pool_used = w->pool_used;
+  out->n_holes = w->n_holes;
+  out->pool_capacity = w->pool_cap;
+  out->ops_applied = w->ops_applied;
+  return PX_OK;
+}
+
+int px_device_view_get(px_world* w, px_device_view* out) {
+  if (!w || !out) return PX_E_INVALID_ARG;
+  out->grid = w->d_grid;
+  out->pool = (const uint16_t*)w->d_pool32;
+  DevBuf& cur = w->holes_in_a ? w->holes_a : w->holes_b;
+  out->holes = (const uint32_t*)cur.p;
+  out->super_counts = w->derived_valid ? (const uint32_t*)w->super_counts.p : nullptr;
+  out->density = w->derived_valid ? (const uint8_t*)w->density.p : nullptr;
+  return PX_OK;
+}
+
+const char* px_last_error(px_world* w) { return w ? w->err.c_str() : "null world"; }
+
+int px_probe_peak(int fp64, float* tflops) {
+  if (!tflops) return PX_E_INVALID_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { cudaGetLastError(); return PX_E_NO_DEVICE; }
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  *tflops = probe_fma_tflops(fp64, sms);
+  return cudaGetLastError() == cudaSuccess ? PX_OK : PX_E_CUDA;
+}
+
+}  // extern "C"

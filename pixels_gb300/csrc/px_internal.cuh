@@ -1,0 +1,173 @@
+// Shared definitions of the voxeliser's host runtime and kernels.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace px {
+
+constexpr uint32_t UNIFORM = 0x80000000u;  // VoxelWorld.ts:13
+constexpr int BRICK = 8;
+constexpr int BRICK_VOXELS = 512;
+constexpr int TILE = 4;                    // tiles are the 4^3-brick super cells (GpuWorld.ts:52)
+constexpr int MAX_STACK = 4;               // SDF value-stack depth the device evaluator holds
+constexpr int MAX_ROT = 3;                 // nested rotation frames
+constexpr int MAX_AXIS_BRICKS = 1023;      // op brick boxes pack 10 bits per axis
+
+// op kinds (shapes.ts:325-330)
+enum : uint8_t { KIND_ADD = 0, KIND_CARVE = 1, KIND_PAINT = 2 };
+
+// SDF bytecode opcodes (pixels_gb300/ir.py)
+enum : uint32_t {
+  OP_BOX = 1, OP_ROUNDBOX = 2, OP_SPHERE = 3, OP_ELLIPSOID = 4,
+  OP_CYL_X = 5, OP_CYL_Y = 6, OP_CYL_Z = 7, OP_CAPSULE = 8,
+  OP_TORUS_X = 9, OP_TORUS_Y = 10, OP_TORUS_Z = 11,
+  OP_LATHE_SOLID = 12, OP_LATHE_SHELL = 13, OP_PRISM = 14, OP_STADIUM = 15,
+  OP_ROT_X = 20, OP_ROT_Y = 21, OP_ROT_Z = 22, OP_ROT_END = 23,
+  OP_OFFSET = 24, OP_NEGMAX = 25, OP_MAX = 26, OP_MIN = 27,
+};
+
+// paint kinds
+enum : uint16_t {
+  PK_CONST = 0, PK_CHIP = 1, PK_TUFTED = 2, PK_CARD = 3, PK_WHITE = 4, PK_BLACK = 5,
+  PK_VASE = 6, PK_PAINTING = 7, PK_NOISE = 8, PK_COUNT = 9,
+};
+constexpr int PAINT_NPARAMS[PK_COUNT] = {0, 5, 3, 4, 2, 2, 5, 37, 8};
+
+enum : uint8_t { OPF_CONTAINS = 1, OPF_HAS_SLACK = 2, OPF_PAINT_FRAME = 4 };
+
+// device status bits (first error wins for the reported code)
+enum : uint32_t {
+  ST_OK = 0, ST_STAGE_OVERFLOW = 1, ST_POOL_OVERFLOW = 2, ST_RANGE = 4, ST_CHAIN = 8,
+};
+
+// PXIR op record (128 bytes, pixels_gb300/ir.py OP_DTYPE)
+struct IrOp {
+  uint8_t kind, flags;
+  uint16_t paint_kind;
+  uint32_t paint_value, paint_param, code_begin, code_len, pad0;
+  double mn[3], mx[3], slack;
+  double frame[4];
+  double pad1[2];
+};
+static_assert(sizeof(IrOp) == 128, "PXIR op is 128 bytes");
+
+// An op as the kernels see it.
+struct OpDev {
+  int32_t bx0, by0, bz0, bx1, by1, bz1;  // brick box (inclusive), from apply()'s voxel range
+  int32_t nx, ny;                        // box extent in bricks (x, y)
+  uint64_t pair_base;                    // index of the op's first (op, brick) pair
+  uint32_t code_off, code_len;           // SDF bytecode (uint2 records)
+  uint32_t paint_off;                    // paint parameters (doubles)
+  uint8_t kind, flags;
+  uint16_t paint_kind;
+  uint32_t paint_value;
+  uint32_t pad;
+  double bhd, shd;                       // brickHalfDiag, subHalfDiag (shapes.ts:349-350)
+  double mn[3], mx[3];                   // contains box (boxes only)
+  double frame[4];                       // paint frame px, pz, cos, sin
+  float bhd32, shd32, err32, pad32;      // mixed mode thresholds and error bound
+};
+
+struct BuildCounters {
+  unsigned long long brick_evals, sub_evals, voxel_evals, paint_evals, rescued;
+  unsigned long long alloc_events, free_events;
+  unsigned long long pad;
+};
+
+// Small device block read back after every build.
+struct BuildResult {
+  uint32_t status;
+  uint32_t n_events;     // H + N
+  uint32_t pool_used;    // after the build
+  uint32_t n_holes;      // after the build
+  uint32_t stage_count;  // bricks that end as pool bricks and were touched
+  uint32_t n_nonempty;   // tiles with at least one op
+  uint32_t n_fresh;
+  uint32_t max_pool_index;
+  BuildCounters c;
+  double max_err;        // max |d32 - d64| over rescued evaluations
+};
+
+struct FoldArgs {
+  const OpDev* ops;
+  const uint2* code;
+  const double* params;
+  const uint32_t* tile_off;
+  const uint32_t* tile_cnt;
+  const uint32_t* tile_ops;
+  const uint32_t* tiles_nonempty;
+  int BX, BY, BZ, TX, TY;
+  double vs;
+  uint32_t* grid;
+  const uint32_t* pool32;     // pool viewed as voxel pairs
+  uint8_t* evt;               // per pair: 1 = alloc, 2 = free
+  int64_t* fsrc;              // per pair with a free: pair of the brick's last alloc, or -(old index + 1)
+  uint32_t* staging32;
+  uint32_t stage_cap;
+  uint32_t* stage_cell;
+  int64_t* stage_src;
+  uint32_t* work_counter;
+  BuildResult* res;
+};
+
+// Host-side launch wrappers (kernels.cu)
+void launch_cull_count(const uint2* boxes, int n_ops, int TX, int TY, int TZ, uint32_t* tile_cnt,
+                       uint32_t* tiles_nonempty, BuildResult* res, cudaStream_t s);
+void launch_cull_fill(const uint2* boxes, int n_ops, int TX, int TY, int TZ, const uint32_t* tile_off,
+                      uint32_t* tile_ops, cudaStream_t s);
+void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s);
+
+struct ScanTemp {
+  void* block_agg;
+  size_t max_blocks;
+};
+size_t scan_items_per_block();
+void launch_scan_u32(const uint32_t* in, uint32_t* out, size_t n, const uint32_t* n_dev, bool inclusive,
+                     uint32_t* total_out, ScanTemp& t, cudaStream_t s);
+
+struct ReplayArgs {
+  size_t P;                 // pairs
+  size_t E_max;             // H + 2P
+  uint32_t H;               // holes before the build
+  uint32_t U0;              // poolUsed before the build
+  const uint8_t* evt;
+  const int64_t* fsrc;
+  const uint32_t* holes_in;
+  uint32_t* cnt;            // P
+  uint32_t* pos;            // P
+  uint8_t* etype;           // E_max
+  unsigned long long* ew;   // E_max
+  int2* depth_fn;           // E_max
+  int32_t* depth;           // E_max (+ tree levels)
+  int32_t* tree;            // levels above depth
+  size_t tree_words;
+  uint32_t* fresh;          // E_max
+  uint32_t* fresh_rank;     // E_max
+  uint32_t* holes_out;      // >= E_max
+  BuildResult* res;
+  ScanTemp* scan;
+};
+void launch_replay(const ReplayArgs& a, cudaStream_t s);
+
+struct FinalizeArgs {
+  const uint32_t* staging32;
+  const uint32_t* stage_cell;
+  const int64_t* stage_src;
+  const uint32_t* pos;
+  const unsigned long long* ew;
+  uint32_t H;
+  uint32_t* grid;
+  uint32_t* pool32;
+  uint32_t pool_cap;
+  BuildResult* res;
+};
+void launch_finalize(const FinalizeArgs& a, uint32_t stage_cap, cudaStream_t s);
+
+void launch_derive(const uint32_t* grid, const uint32_t* pool32, int BX, int BY, int BZ,
+                   const uint8_t* opaque, const uint8_t* udens, uint32_t* super_counts,
+                   uint8_t* density, cudaStream_t s);
+
+float probe_fma_tflops(int fp64, int n_sms);
+unsigned long long launch_count();
+
+}  // namespace px

@@ -68,7 +68,7 @@ class VoxelWorld:
         self._lib.build(self._h, self.mode, stream)
 
     def _ensure(self):
-        if len(self._pending) or self._lib.has_pending(self._h):
+        if len(self._pending):
             self.build()
 
     # -- reads ------------------------------------------------------------
@@ -79,7 +79,8 @@ class VoxelWorld:
 
     @property
     def liveBricks(self) -> int:
-        s = self._lib.stats(self._h) if not self._ensure() else None
+        """``poolUsed - freeList.length`` (VoxelWorld.ts:139-141)."""
+        self._ensure()
         s = self._lib.stats(self._h)
         return s["pool_used"] - s["n_holes"]
 
@@ -115,7 +116,8 @@ class VoxelWorld:
     def derived(self) -> dict:
         """The upload products of GpuWorld.ts:90-113 (super counts, density, free list)."""
         self._ensure()
-        return self._lib.read_derived(self._h, self.max_bricks)
+        n_super = ((self.bx + 3) // 4) * ((self.by + 3) // 4) * ((self.bz + 3) // 4)
+        return self._lib.read_derived(self._h, self.max_bricks, self.bx * self.by * self.bz, n_super)
 
     def stats(self) -> dict:
         return self._lib.stats(self._h)
