@@ -477,8 +477,17 @@ uint32_t paint_eval(int kind, const double* p, double x, double y, double z) {
 const uint32_t UNIFORM = 0x80000000u;  // VoxelWorld.ts:13
 const int BRICK = 8, BRICK_VOXELS = 512;
 
+struct AllocEvent {
+  uint32_t op, ci;
+  uint8_t seq, free_;  // seq: 0 alloc / 1 free within one (op, cell); free_: 1 = free
+  uint32_t local;      // pool index in the thread-local world
+};
+
 struct World {
   int dx, dy, dz, bx, by, bz;
+  std::vector<AllocEvent>* log = nullptr;  // set when bricks are split across threads
+  uint32_t cur_op = 0;
+  size_t cur_ci = 0;
   std::vector<uint32_t> grid;
   std::vector<uint16_t> pool;
   uint32_t poolCapacity, poolUsed = 0;
@@ -514,9 +523,14 @@ struct World {
       p = poolUsed++;
     }
     std::fill(pool.begin() + (size_t)p * BRICK_VOXELS, pool.begin() + (size_t)(p + 1) * BRICK_VOXELS, fill);
+    if (log) log->push_back({cur_op, (uint32_t)cur_ci, 0, 0, p});
     return p;
   }
-  void freeBrick(uint32_t p) { frees++; freeList.push_back(p); }  // :124-127
+  void freeBrick(uint32_t p) {  // :124-127
+    frees++;
+    freeList.push_back(p);
+    if (log) log->push_back({cur_op, (uint32_t)cur_ci, 1, 1, p});
+  }
   void growPool() {  // :129-136
     uint32_t cap = (uint32_t)std::ceil(poolCapacity * 1.5);
     pool.resize((size_t)cap * BRICK_VOXELS, 0);
@@ -549,7 +563,7 @@ struct OpCtx {
   const double* paint_params;
 };
 
-void apply(World& world, const OpCtx& oc, double vs, Stats& st, int bz_lo, int bz_hi) {
+void apply(World& world, const OpCtx& oc, double vs, Stats& st, int bz_mod, int bz_count) {
   const IrOp& op = *oc.op;
   const Node& shape = *oc.shape;
   const double slack = op.slack;
@@ -568,13 +582,13 @@ void apply(World& world, const OpCtx& oc, double vs, Stats& st, int bz_lo, int b
   uint16_t scratch[BRICK_VOXELS];
 
   int bz0 = (int)vz0 >> 3, bz1 = (int)vz1 >> 3;
-  if (bz0 < bz_lo) bz0 = bz_lo;
-  if (bz1 > bz_hi - 1) bz1 = bz_hi - 1;
-  for (int bz = bz0; bz <= bz1; bz++)
+  for (int bz = bz0; bz <= bz1; bz++) {
+    if (bz_count > 1 && bz % bz_count != bz_mod) continue;  // this thread's slabs only
     for (int by = (int)vy0 >> 3; by <= ((int)vy1 >> 3); by++)
       for (int bx = (int)vx0 >> 3; bx <= ((int)vx1 >> 3); bx++) {
         st.pairs++;
         size_t ci = world.cellIndex(bx, by, bz);
+        world.cur_ci = ci;
         int ox = bx * BRICK, oy = by * BRICK, oz = bz * BRICK;
         bool full = false;
         if (op.flags & OPF_CONTAINS) {  // :359-361 (box contains, shapes.ts:47-48)
@@ -649,6 +663,7 @@ void apply(World& world, const OpCtx& oc, double vs, Stats& st, int bz_lo, int b
         std::memcpy(world.pool.data() + (size_t)p * BRICK_VOXELS, scratch, sizeof scratch);
         world.compactCell(ci);
       }
+  }
 }
 
 struct Program {
@@ -725,7 +740,8 @@ int oracle_build(const void* ir, size_t bytes, double vpm, int dx, int dy, int d
   if (count_flops) g_ledger = &led;
   for (size_t i = 0; i < prog.ops.size(); i++) {
     OpCtx oc{&prog.ops[i], prog.shapes[i].get(), prog.params + prog.ops[i].paint_param};
-    apply(w, oc, vs, st, 0, w.bz);
+    w.cur_op = (uint32_t)i;
+    apply(w, oc, vs, st, 0, 1);
   }
   g_ledger = nullptr;
   out->dx = dx; out->dy = dy; out->dz = dz; out->bx = w.bx; out->by = w.by; out->bz = w.bz;
@@ -741,6 +757,91 @@ int oracle_build(const void* ir, size_t bytes, double vpm, int dx, int dy, int d
   out->sub_evals = st.sub_evals; out->voxel_evals = st.voxel_evals; out->paint_evals = st.paint_evals;
   out->flops = led.flops; out->divs = led.divs; out->sqrts = led.sqrts; out->trans = led.trans;
   out->allocs = w.allocs; out->frees = w.frees;
+  return 0;
+}
+
+// The same build with bricks split across host threads: thread t owns the
+// brick slabs bz = t (mod threads) and runs every op on them in order (a
+// brick's result depends only on the ops that touch it).  The threads' pool
+// alloc/free events are then merged in (op, cell) order -- the order of the
+// single-threaded loop (shapes.ts:353-355) -- and the LIFO allocator
+// (VoxelWorld.ts:112-127) is replayed once to give the same pool indices.
+int oracle_build_mt(const void* ir, size_t bytes, double vpm, int dx, int dy, int dz, int threads,
+                    oracle_result* out) {
+  std::memset(out, 0, sizeof *out);
+  Program prog;
+  std::string err;
+  if (!load_program(ir, bytes, prog, err)) { std::snprintf(out->error, sizeof out->error, "%s", err.c_str()); return 1; }
+  if (dx <= 0 || dy <= 0 || dz <= 0 || dx % 8 || dy % 8 || dz % 8) { std::snprintf(out->error, sizeof out->error, "dims must be positive multiples of 8"); return 1; }
+  if (threads < 1) threads = 1;
+  const double vs = 1 / vpm;
+  std::vector<std::unique_ptr<World>> worlds;
+  std::vector<std::vector<AllocEvent>> logs(threads);
+  std::vector<Stats> stats(threads);
+  for (int t = 0; t < threads; t++) {
+    worlds.emplace_back(new World(dx, dy, dz, 1024));
+    worlds.back()->log = &logs[t];
+  }
+  std::vector<std::thread> pool_threads;
+  for (int t = 0; t < threads; t++)
+    pool_threads.emplace_back([&, t] {
+      World& w = *worlds[t];
+      for (size_t i = 0; i < prog.ops.size(); i++) {
+        OpCtx oc{&prog.ops[i], prog.shapes[i].get(), prog.params + prog.ops[i].paint_param};
+        w.cur_op = (uint32_t)i;
+        apply(w, oc, vs, stats[t], t, threads);
+      }
+    });
+  for (auto& th : pool_threads) th.join();
+  struct Tagged { AllocEvent e; int t; };
+  std::vector<Tagged> all;
+  for (int t = 0; t < threads; t++)
+    for (auto& e : logs[t]) all.push_back({e, t});
+  std::sort(all.begin(), all.end(), [](const Tagged& a, const Tagged& b) {
+    if (a.e.op != b.e.op) return a.e.op < b.e.op;
+    if (a.e.ci != b.e.ci) return a.e.ci < b.e.ci;
+    return a.e.seq < b.e.seq;
+  });
+  std::vector<std::vector<uint32_t>> local_to_global(threads);
+  for (int t = 0; t < threads; t++) local_to_global[t].assign(worlds[t]->poolUsed, 0xffffffffu);
+  std::vector<uint32_t> stack;
+  uint32_t used = 0;
+  for (auto& x : all) {
+    if (!x.e.free_) {
+      uint32_t g;
+      if (!stack.empty()) { g = stack.back(); stack.pop_back(); }
+      else g = used++;
+      local_to_global[x.t][x.e.local] = g;
+    } else {
+      stack.push_back(local_to_global[x.t][x.e.local]);
+    }
+  }
+  World& w0 = *worlds[0];
+  const size_t ncells = w0.grid.size();
+  out->dx = dx; out->dy = dy; out->dz = dz; out->bx = w0.bx; out->by = w0.by; out->bz = w0.bz;
+  out->pool_used = used;
+  out->n_free = (uint32_t)stack.size();
+  out->grid = (uint32_t*)std::malloc(ncells * 4);
+  out->pool = (uint16_t*)std::calloc((size_t)used * BRICK_VOXELS + 1, 2);
+  for (size_t ci = 0; ci < ncells; ci++) {
+    int bz = (int)(ci / ((size_t)w0.bx * w0.by));
+    const World& wt = *worlds[bz % threads];
+    uint32_t g = wt.grid[ci];
+    if (g != 0 && !(g & UNIFORM)) {
+      uint32_t gl = local_to_global[bz % threads][g - 1];
+      std::memcpy(out->pool + (size_t)gl * BRICK_VOXELS, wt.pool.data() + (size_t)(g - 1) * BRICK_VOXELS, BRICK_VOXELS * 2);
+      g = gl + 1;
+    }
+    out->grid[ci] = g;
+  }
+  out->free_list = (uint32_t*)std::malloc(stack.size() * 4 + 4);
+  std::memcpy(out->free_list, stack.data(), stack.size() * 4);
+  for (int t = 0; t < threads; t++) {
+    out->pairs += stats[t].pairs; out->contains_tests += stats[t].contains_tests;
+    out->brick_evals += stats[t].brick_evals; out->sub_evals += stats[t].sub_evals;
+    out->voxel_evals += stats[t].voxel_evals; out->paint_evals += stats[t].paint_evals;
+    out->allocs += worlds[t]->allocs; out->frees += worlds[t]->frees;
+  }
   return 0;
 }
 

@@ -53,6 +53,9 @@ def lib():
                                    ctypes.c_int, ctypes.c_int, ctypes.c_uint32, ctypes.c_int,
                                    ctypes.POINTER(OracleResult)]
         L.oracle_build.restype = ctypes.c_int
+        L.oracle_build_mt.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_double, ctypes.c_int,
+                                      ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(OracleResult)]
+        L.oracle_build_mt.restype = ctypes.c_int
         L.oracle_free.argtypes = [ctypes.POINTER(OracleResult)]
         L.oracle_derive.argtypes = [ctypes.POINTER(OracleResult), ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.c_void_p, ctypes.c_void_p]
@@ -69,8 +72,12 @@ class OracleWorld:
         L = lib()
         res = OracleResult()
         buf = ctypes.create_string_buffer(ir_bytes, len(ir_bytes))
-        rc = L.oracle_build(buf, len(ir_bytes), float(vpm), int(dims[0]), int(dims[1]), int(dims[2]),
-                            int(initial_pool_bricks), int(count_flops), ctypes.byref(res))
+        if threads > 1:
+            rc = L.oracle_build_mt(buf, len(ir_bytes), float(vpm), int(dims[0]), int(dims[1]), int(dims[2]),
+                                   int(threads), ctypes.byref(res))
+        else:
+            rc = L.oracle_build(buf, len(ir_bytes), float(vpm), int(dims[0]), int(dims[1]), int(dims[2]),
+                                int(initial_pool_bricks), int(count_flops), ctypes.byref(res))
         if rc != 0:
             raise ValueError(res.error.decode())
         try:
