@@ -61,6 +61,7 @@ typedef struct px_stats {
   float fold_ms;             /* device time of its fold kernel */
   uint32_t kernel_launches;  /* kernels the last build launched */
   uint32_t pad;
+  uint64_t violations;       /* validation mode: float64 results outside their float32 enclosure */
 } px_stats;
 
 /* Device addresses of the world's buffers (valid until the next build or destroy). */
@@ -109,6 +110,11 @@ int px_read_free_list(px_world* w, uint32_t max_bricks, uint32_t* dst, size_t n,
 /* Material tables for the density pass: opaque[id] (OPAQUE, VoxelWorld.ts:190-196) and the
    density of a uniform brick of material id (VoxelWorld.ts:162).  256 bytes each. */
 int px_set_material_tables(px_world* w, const uint8_t* opaque256, const uint8_t* uniform_density256);
+
+/* Validation mode for the mixed form (testing aid, slow): every float32
+   evaluation is also done in float64 and checked against its enclosure;
+   stats.violations counts failures (must stay 0). */
+int px_set_validation(px_world* w, int on);
 
 int px_get_stats(px_world* w, px_stats* out);
 int px_device_view_get(px_world* w, px_device_view* out);

@@ -21,7 +21,7 @@ ERRORS = {1: "PX_E_INVALID_ARG", 2: "PX_E_INVALID_IR", 3: "PX_E_OOM", 4: "PX_E_Q
 EXPORTS = [
     "px_world_create", "px_world_destroy", "px_world_reset", "px_submit_ops", "px_build", "px_build_enqueue",
     "px_build_finish", "px_read_grid", "px_read_pool", "px_read_holes", "px_derive", "px_read_super",
-    "px_read_density", "px_read_free_list", "px_set_material_tables", "px_get_stats",
+    "px_read_density", "px_read_free_list", "px_set_material_tables", "px_set_validation", "px_get_stats",
     "px_device_view_get", "px_last_error", "px_probe_peak",
 ]
 
@@ -40,6 +40,7 @@ class Stats(ctypes.Structure):
         ("pool_used", ctypes.c_uint32), ("n_holes", ctypes.c_uint32), ("pool_capacity", ctypes.c_uint32),
         ("status", ctypes.c_uint32), ("max_abs_err32", ctypes.c_double), ("build_ms", ctypes.c_float),
         ("fold_ms", ctypes.c_float), ("kernel_launches", ctypes.c_uint32), ("pad", ctypes.c_uint32),
+        ("violations", ctypes.c_uint64),
     ]
 
 
@@ -68,6 +69,7 @@ def load(path: str = LIB_PATH):
     L.px_derive.argtypes = [vp]
     L.px_read_free_list.argtypes = [vp, u32, vp, sz, ctypes.POINTER(u32)]
     L.px_set_material_tables.argtypes = [vp, vp, vp]
+    L.px_set_validation.argtypes = [vp, ctypes.c_int]
     L.px_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
     L.px_device_view_get.argtypes = [vp, vp]
     L.px_last_error.argtypes = [vp]
@@ -92,6 +94,10 @@ def world_create(dx, dy, dz, vpm, initial_pool_bricks):
     ud = np.array(uniform_density_table(), np.uint8)
     _check(h, L.px_set_material_tables(h, op.ctypes.data, ud.ctypes.data))
     return h
+
+
+def set_validation(h, on: bool):
+    _check(h, load().px_set_validation(h, int(on)))
 
 
 def world_destroy(h):

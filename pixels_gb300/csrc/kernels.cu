@@ -20,6 +20,7 @@
 #include <cstdio>
 #include "px_internal.cuh"
 #include "sdf64.cuh"
+#include "sdf32.cuh"
 #include "paint.cuh"
 
 namespace px {
@@ -95,8 +96,66 @@ void launch_cull_fill(const uint2* boxes, int n_ops, int TX, int TY, int TZ, con
 enum { ST_EMPTY = 0, ST_UNIF = 1, ST_MIXED = 2 };
 
 struct WarpCounters {
-  unsigned long long brick, sub, vox, paint, resc, alloc, free_;
+  unsigned long long brick, sub, vox, alloc, free_;
 };
+
+// Per-lane statistics of the float32 path.
+struct LaneStats {
+  unsigned long long paint, resc, viol;
+  double max_err;
+};
+
+// Decisions of apply() from a float32 interval (thresholds certified on the host):
+// brick/sub-block: 0 = outside (skip), 1 = partial, 2 = full, 3 = undecided.
+__device__ __forceinline__ int classify32(Iv d, const float* thr, int base) {
+  if (d.lo > thr[base + 0]) return 0;
+  if (!(d.hi <= thr[base + 1])) return 3;
+  if (d.hi < thr[base + 2]) return 2;
+  if (d.lo >= thr[base + 3]) return 1;
+  return 3;
+}
+__device__ __forceinline__ int classify64(double d, double half_diag) {
+  if (d > half_diag) return 0;
+  return d < -half_diag ? 2 : 1;
+}
+
+// The float32 point (relative to the op anchor) of voxel-space offset k * vs
+// from the brick's first voxel centre, enclosing the reference's float64 point.
+__device__ __forceinline__ Iv koff(float k, float vs_lo, float vs_hi) { return {__fmul_rd(k, vs_lo), __fmul_ru(k, vs_hi)}; }
+
+// Evaluate one shape at one point: float64 directly, or float32 interval with
+// a float64 rescue when the interval cannot decide.  `kind`: 0 voxel (returns
+// inside), 1 brick, 2 sub-block (return the classification).
+template <int MODE>
+__device__ __forceinline__ int eval_decide(const FoldArgs& a, const OpDev* O, const uint2* code, int clen, bool use32,
+                                           const Iv* bo, float kx, float ky, float kz, double X, double Y, double Z,
+                                           int what, LaneStats& ls) {
+  const int base = what == 1 ? T_BSK_HI : T_SSK_HI;
+  if (MODE == 1 && use32) {
+    bool amb = false;
+    Iv px_ = iadd(bo[0], koff(kx, a.vs_lo, a.vs_hi)), py_ = iadd(bo[1], koff(ky, a.vs_lo, a.vs_hi)),
+       pz_ = iadd(bo[2], koff(kz, a.vs_lo, a.vs_hi));
+    Iv d = sdf32i(code, a.code32 + O->code_off, clen, reinterpret_cast<const Iv*>(a.p32), px_, py_, pz_, O->thr[T_M], amb);
+    int r;
+    if (what == 0) r = amb ? 3 : (d.lo > O->thr[T_V_HI] ? 0 : (d.hi <= O->thr[T_V_LO] ? 1 : 3));
+    else r = amb ? 3 : classify32(d, O->thr, base);
+    if (r != 3 && !a.validate) return r;
+    double d64 = sdf64(code, clen, a.params, X, Y, Z);
+    const double M = MIXED_MARGIN;
+    if (a.validate && !amb && !((double)d.lo - M <= d64 && d64 <= (double)d.hi + M)) ls.viol++;
+    if (r == 3) {
+      ls.resc++;
+      double mid = 0.5 * ((double)d.lo + (double)d.hi);
+      double e = fabs(mid - d64);
+      if (e == e && e > ls.max_err && !amb) ls.max_err = e;
+    }
+    if (what == 0) return d64 > 0.0 ? 0 : 1;
+    return classify64(d64, what == 1 ? O->bhd : O->shd);
+  }
+  double d = sdf64(code, clen, a.params, X, Y, Z);
+  if (what == 0) return d > 0.0 ? 0 : 1;
+  return classify64(d, what == 1 ? O->bhd : O->shd);
+}
 
 // Lane layout of a brick in registers: lane owns the voxel pair
 // (x0, y, z) / (x0 + 1, y, z) with x0 = 2 (lane & 3), y = lane >> 2, in
@@ -109,7 +168,8 @@ __global__ void __launch_bounds__(256, 2) fold_kernel(FoldArgs a) {
   const int wib = threadIdx.x >> 5;
   const int lx0 = (lane & 3) * 2, ly = lane >> 2;
   const double vs = a.vs;
-  WarpCounters wc = {0, 0, 0, 0, 0, 0, 0};
+  WarpCounters wc = {0, 0, 0, 0, 0};
+  LaneStats ls = {0, 0, 0, 0.0};
   uint32_t st_local = 0;
   const uint32_t n_work = __ldg(&a.res->n_nonempty) * 64u;
 
@@ -170,6 +230,16 @@ __global__ void __launch_bounds__(256, 2) fold_kernel(FoldArgs a) {
         const int clen = (int)O->code_len;
         const unsigned long long pair = O->pair_base +
             (unsigned long long)(((bz - O->bz0) * O->ny + (by - O->by0)) * O->nx + (bx - O->bx0));
+        const bool use32 = MODE == 1 && !(flags & OPF_FP64_ONLY);
+        // float32 enclosure of the first voxel centre relative to the op anchor
+        Iv bo[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+        if (MODE == 1 && use32) {
+          const double pad = 0x1p-38;
+          double b0 = (ox + 0.5) * vs - O->anchor[0], b1 = (oy + 0.5) * vs - O->anchor[1], b2 = (oz + 0.5) * vs - O->anchor[2];
+          bo[0] = {__double2float_rd(b0 - pad), __double2float_ru(b0 + pad)};
+          bo[1] = {__double2float_rd(b1 - pad), __double2float_ru(b1 + pad)};
+          bo[2] = {__double2float_rd(b2 - pad), __double2float_ru(b2 + pad)};
+        }
 
         // brick classification (shapes.ts:358-366)
         bool full = false;
@@ -179,11 +249,11 @@ __global__ void __launch_bounds__(256, 2) fold_kernel(FoldArgs a) {
           full = x0 >= O->mn[0] && x1 <= O->mx[0] && y0 >= O->mn[1] && y1 <= O->mx[1] && z0 >= O->mn[2] && z1 <= O->mx[2];
         }
         if (!full) {
-          double d = sdf64(code, clen, a.params, (ox + 4) * vs, (oy + 4) * vs, (oz + 4) * vs);
+          int cls = eval_decide<MODE>(a, O, code, clen, use32, bo, 3.5f, 3.5f, 3.5f, (ox + 4) * vs, (oy + 4) * vs,
+                                      (oz + 4) * vs, 1, ls);
           wc.brick++;
-          const double bhd = O->bhd;
-          if (d > bhd) continue;
-          full = d < -bhd;
+          if (cls == 0) continue;
+          full = cls == 2;
         }
         // uniform shortcuts (shapes.ts:367-374)
         int set_u = -1;
@@ -212,15 +282,16 @@ __global__ void __launch_bounds__(256, 2) fold_kernel(FoldArgs a) {
         uint32_t sub_full = full ? 0xffu : 0u, sub_part = 0u;
         if (!full) {
           bool in8 = lane < 8;
-          double d = 0.0;
+          int cls = 0;
           if (in8) {
-            int sx = ox + (lane & 1) * 4, sy = oy + ((lane >> 1) & 1) * 4, sz = oz + ((lane >> 2) & 1) * 4;
-            d = sdf64(code, clen, a.params, (sx + 2) * vs, (sy + 2) * vs, (sz + 2) * vs);
+            const int sxb = lane & 1, syb = (lane >> 1) & 1, szb = (lane >> 2) & 1;
+            const int sx = ox + sxb * 4, sy = oy + syb * 4, sz = oz + szb * 4;
+            cls = eval_decide<MODE>(a, O, code, clen, use32, bo, 4.f * sxb + 1.5f, 4.f * syb + 1.5f, 4.f * szb + 1.5f,
+                                    (sx + 2) * vs, (sy + 2) * vs, (sz + 2) * vs, 2, ls);
           }
           wc.sub += 8;
-          const double shd = O->shd;
-          uint32_t bf = __ballot_sync(FULLMASK, in8 && d < -shd);
-          uint32_t bs = __ballot_sync(FULLMASK, in8 && d > shd);
+          uint32_t bf = __ballot_sync(FULLMASK, in8 && cls == 2);
+          uint32_t bs = __ballot_sync(FULLMASK, in8 && cls == 0);
           sub_full = bf & 0xffu;
           sub_part = ~(bf | bs) & 0xffu;
         }
@@ -229,14 +300,15 @@ __global__ void __launch_bounds__(256, 2) fold_kernel(FoldArgs a) {
         __syncwarp();
         for (uint32_t sp = sub_part; sp; sp &= sp - 1) {
           const int s = __ffs(sp) - 1;
-          const int sx = ox + (s & 1) * 4, sy = oy + ((s >> 1) & 1) * 4, sz = oz + ((s >> 2) & 1) * 4;
+          const int sxo = (s & 1) * 4, syo = ((s >> 1) & 1) * 4, szo = ((s >> 2) & 1) * 4;
           uint32_t bal[2];
 #pragma unroll
           for (int r = 0; r < 2; r++) {
             const int e = r * 32 + lane;
-            const int X = sx + (e & 3), Y = sy + ((e >> 2) & 3), Z = sz + (e >> 4);
-            double d = sdf64(code, clen, a.params, (X + 0.5) * vs, (Y + 0.5) * vs, (Z + 0.5) * vs);
-            bal[r] = __ballot_sync(FULLMASK, !(d > 0.0));
+            const int lx = sxo + (e & 3), lyv = syo + ((e >> 2) & 3), lz = szo + (e >> 4);
+            int inside = eval_decide<MODE>(a, O, code, clen, use32, bo, (float)lx, (float)lyv, (float)lz,
+                                           (ox + lx + 0.5) * vs, (oy + lyv + 0.5) * vs, (oz + lz + 0.5) * vs, 0, ls);
+            bal[r] = __ballot_sync(FULLMASK, inside == 1);
           }
           if (lane == 0) smask[wib][s] = (unsigned long long)bal[0] | ((unsigned long long)bal[1] << 32);
           wc.vox += 64;
@@ -266,7 +338,7 @@ __global__ void __launch_bounds__(256, 2) fold_kernel(FoldArgs a) {
                 PZ = fpz - sn * dx + c * dz;
               }
               next = paint_eval(pk, a.params + O->paint_off, PX, PY, PZ, st_local);
-              wc.paint++;
+              ls.paint++;
             } else next = pv;
             if (next != cur) {  // Uint16Array store; the comparison uses the unstored value
               vox[j] = (vox[j] & ~(0xffffu << (16 * h))) | ((next & 0xffffu) << (16 * h));
@@ -325,22 +397,33 @@ __global__ void __launch_bounds__(256, 2) fold_kernel(FoldArgs a) {
     if (wc.alloc) atomicAdd(&a.res->c.alloc_events, wc.alloc);
     if (wc.free_) atomicAdd(&a.res->c.free_events, wc.free_);
   }
-  unsigned long long pc = wc.paint;
-#pragma unroll
-  for (int o = 16; o; o >>= 1) pc += __shfl_xor_sync(FULLMASK, pc, o);
+  unsigned long long pc = ls.paint, rc = ls.resc, vc = ls.viol;
+  double me = ls.max_err;
   uint32_t stw = st_local;
 #pragma unroll
-  for (int o = 16; o; o >>= 1) stw |= __shfl_xor_sync(FULLMASK, stw, o);
+  for (int o = 16; o; o >>= 1) {
+    pc += __shfl_xor_sync(FULLMASK, pc, o);
+    rc += __shfl_xor_sync(FULLMASK, rc, o);
+    vc += __shfl_xor_sync(FULLMASK, vc, o);
+    me = fmax(me, __shfl_xor_sync(FULLMASK, me, o));
+    stw |= __shfl_xor_sync(FULLMASK, stw, o);
+  }
   if (lane == 0) {
     if (pc) atomicAdd(&a.res->c.paint_evals, pc);
+    if (rc) atomicAdd(&a.res->c.rescued, rc);
+    if (vc) atomicAdd(&a.res->c.violations, vc);
+    if (me > 0.0) atomicMax(&a.res->max_err_bits, (unsigned long long)__double_as_longlong(me));
     if (stw) atomicOr(&a.res->status, stw);
   }
 }
 
 void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s) {
-  (void)mode;
   int blocks = n_sms * 2;
-  ++g_launches; fold_kernel<0><<<blocks, 256, 0, s>>>(a);
+  if (mode == 1) {
+    ++g_launches; fold_kernel<1><<<blocks, 256, 0, s>>>(a);
+  } else {
+    ++g_launches; fold_kernel<0><<<blocks, 256, 0, s>>>(a);
+  }
 }
 
 // ---------------------------------------------------------------------------

@@ -47,10 +47,13 @@ struct px_world {
   std::vector<uint2> boxes;
   std::vector<uint2> code;
   std::vector<double> params;
+  std::vector<uint32_t> code32, last_code32;   // per instruction: float32 parameter offset
+  std::vector<float2> p32, last_p32;           // float32 interval parameters
+  int validate = 0;
   uint64_t ops_applied = 0;
 
   // per-build device scratch
-  DevBuf d_ops, d_boxes, d_code, d_params;
+  DevBuf d_ops, d_boxes, d_code, d_params, d_code32, d_p32;
   DevBuf tile_cnt, tile_off, tiles_nonempty, tile_ops;
   DevBuf evt, fsrc, cnt, pos, etype, ew, depth_fn, depth, tree, fresh, fresh_rank;
   DevBuf staging, stage_cell, stage_src;
@@ -117,6 +120,104 @@ void release(DevBuf& b) {
 
 inline double js_max(double a, double b) { return a > b ? a : b; }  // finite inputs (validated)
 inline double js_min(double a, double b) { return a < b ? a : b; }
+
+// float32 enclosures of float64 values (mixed mode)
+inline float rd32(double v) {
+  float f = (float)v;
+  if ((double)f > v) f = std::nextafterf(f, -INFINITY);
+  return f;
+}
+inline float ru32(double v) {
+  float f = (float)v;
+  if ((double)f < v) f = std::nextafterf(f, INFINITY);
+  return f;
+}
+inline float2 enc(double v, double pad = 0.0) { return make_float2(rd32(v - pad), ru32(v + pad)); }
+
+// Convert one op's SDF parameters to float32 intervals relative to the op's
+// anchor.  Positions are shifted by the anchor; reciprocals (1/r, 1/|e|^2)
+// replace the divisions; polygon edges are expanded to per-vertex records.
+// Returns false when a value falls outside the range the float32 path
+// certifies (the op then runs in float64 only).
+bool convert32(const uint32_t* code, uint32_t n, const double* P, const double A[3], std::vector<uint32_t>& code32,
+               std::vector<float2>& p32) {
+  bool ok = true;
+  auto put = [&](double v, double pad) {
+    float2 e = enc(v, pad);
+    if (!std::isfinite(e.x) || !std::isfinite(e.y) || std::fabs(v) > MIXED_MAX_COORD) ok = false;
+    p32.push_back(e);
+  };
+  auto val = [&](double v) { put(v, 0.0); };
+  auto pos = [&](double v, int axis) { double r = v - A[axis]; put(r, (std::fabs(v) + std::fabs(A[axis])) * 0x1p-52); };
+  auto inv = [&](double v) {
+    double r = 1.0 / v;
+    float2 e = enc(r, std::fabs(r) * 0x1p-51);
+    if (!std::isfinite(e.x) || !std::isfinite(e.y) || std::fabs(r) > 0x1p60 || v == 0.0) ok = false;
+    p32.push_back(e);
+  };
+  auto edge = [&](double vjx, double vjy, double vix, double viy, bool with_vjy, bool polyline) {
+    double ex = vjx - vix, ey = vjy - viy;  // polygon: from i to j = i - 1; polyline: from a to b
+    if (polyline) { val(vix); val(viy); }
+    else { val(vix); val(viy); if (with_vjy) val(vjy); }
+    put(ex, (std::fabs(vjx) + std::fabs(vix)) * 0x1p-52);
+    put(ey, (std::fabs(vjy) + std::fabs(viy)) * 0x1p-52);
+    double den = ex * ex + ey * ey;
+    if (den == 0.0) {  // the reference's `|| 1e-12`; e is exactly zero then
+      p32.push_back(make_float2(rd32(1e12), ru32(1e12)));
+    } else {
+      double r = 1.0 / den;
+      float2 e = enc(r, std::fabs(r) * 0x1p-46);
+      if (!std::isfinite(e.x) || !std::isfinite(e.y) || std::fabs(r) > 0x1p60) ok = false;
+      p32.push_back(e);
+    }
+  };
+  for (uint32_t i = 0; i < n; i++) {
+    uint32_t op = code[2 * i] & 0xffu, cnt = code[2 * i] >> 8;
+    const double* p = P + code[2 * i + 1];
+    code32.push_back((uint32_t)p32.size());
+    switch (op) {
+      case OP_BOX: pos(p[0], 0); pos(p[1], 1); pos(p[2], 2); val(p[3]); val(p[4]); val(p[5]); break;
+      case OP_ROUNDBOX: pos(p[0], 0); pos(p[1], 1); pos(p[2], 2); val(p[3]); val(p[4]); val(p[5]); val(p[6]); break;
+      case OP_SPHERE: pos(p[0], 0); pos(p[1], 1); pos(p[2], 2); val(p[3]); break;
+      case OP_ELLIPSOID: pos(p[0], 0); pos(p[1], 1); pos(p[2], 2); inv(p[3]); inv(p[4]); inv(p[5]); val(p[6]); break;
+      case OP_CYL_X: case OP_CYL_Y: case OP_CYL_Z:
+      case OP_TORUS_X: case OP_TORUS_Y: case OP_TORUS_Z:
+        pos(p[0], 0); pos(p[1], 1); pos(p[2], 2); val(p[3]); val(p[4]); break;
+      case OP_CAPSULE: pos(p[0], 0); pos(p[1], 1); pos(p[2], 2); val(p[3]); val(p[4]); val(p[5]); inv(p[6]); val(p[7]); break;
+      case OP_LATHE_SOLID: {
+        pos(p[0], 0); pos(p[1], 1); pos(p[2], 2);
+        const double* v = p + 3;
+        for (uint32_t k = 0; k < cnt; k++) {
+          uint32_t j = k ? k - 1 : cnt - 1;
+          edge(v[2 * j], v[2 * j + 1], v[2 * k], v[2 * k + 1], true, false);
+        }
+        break;
+      }
+      case OP_LATHE_SHELL: {
+        pos(p[0], 0); pos(p[1], 1); pos(p[2], 2); val(p[3]);
+        const double* v = p + 4;
+        for (uint32_t k = 0; k + 1 < cnt; k++) edge(v[2 * k + 2], v[2 * k + 3], v[2 * k], v[2 * k + 1], false, true);
+        break;
+      }
+      case OP_PRISM: {
+        pos(p[0], 0); pos(p[1], 2); pos(p[2], 1); val(p[3]);
+        const double* v = p + 4;
+        for (uint32_t k = 0; k < cnt; k++) {
+          uint32_t j = k ? k - 1 : cnt - 1;
+          edge(v[2 * j], v[2 * j + 1], v[2 * k], v[2 * k + 1], true, false);
+        }
+        break;
+      }
+      case OP_STADIUM: pos(p[0], 0); pos(p[1], 2); val(p[2]); val(p[3]); pos(p[4], 1); val(p[5]); break;
+      case OP_ROT_X: pos(p[0], 1); pos(p[1], 2); val(p[2]); val(p[3]); break;
+      case OP_ROT_Y: pos(p[0], 0); pos(p[1], 2); val(p[2]); val(p[3]); break;
+      case OP_ROT_Z: pos(p[0], 0); pos(p[1], 1); val(p[2]); val(p[3]); break;
+      case OP_OFFSET: val(p[0]); break;
+      default: break;
+    }
+  }
+  return ok;
+}
 
 // Validate one op's SDF bytecode: opcodes, parameter ranges, finite values,
 // stack and rotation depths the device evaluator holds.
@@ -234,7 +335,8 @@ void px_world_destroy(px_world* w) {
   if (w->in_flight) cudaStreamSynchronize(w->stream);
   cudaFree(w->d_grid);
   cudaFree(w->d_pool32);
-  DevBuf* bufs[] = {&w->holes_a, &w->holes_b, &w->d_ops, &w->d_boxes, &w->d_code, &w->d_params, &w->tile_cnt,
+  DevBuf* bufs[] = {&w->holes_a, &w->holes_b, &w->d_ops, &w->d_boxes, &w->d_code, &w->d_params, &w->d_code32,
+                    &w->d_p32, &w->tile_cnt,
                     &w->tile_off, &w->tiles_nonempty, &w->tile_ops, &w->evt, &w->fsrc, &w->cnt, &w->pos, &w->etype,
                     &w->ew, &w->depth_fn, &w->depth, &w->tree, &w->fresh, &w->fresh_rank, &w->staging,
                     &w->stage_cell, &w->stage_src, &w->scan_agg, &w->work_counter, &w->res, &w->opaque,
@@ -266,6 +368,9 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
   const size_t code_base = w->code.size(), param_base = w->params.size();
   std::vector<OpDev> nops;
   std::vector<uint2> nboxes;
+  std::vector<uint2> ncode;         // the new ops' instructions, one copy per op
+  std::vector<uint32_t> n32_code;   // their float32 parameter offsets
+  std::vector<float2> n32_p;
   nops.reserve(n_ops);
   const double vs = w->vs;
   for (size_t i = 0; i < n_ops; i++) {
@@ -294,7 +399,11 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
     d.flags = o.flags;
     d.paint_kind = o.paint_kind;
     d.paint_value = o.paint_value;
-    d.code_off = (uint32_t)(code_base + o.code_begin);
+    d.code_off = (uint32_t)(code_base + ncode.size());
+    for (uint32_t k = 0; k < o.code_len; k++) {
+      const uint32_t* ins = code + 2 * ((size_t)o.code_begin + k);
+      ncode.push_back(make_uint2(ins[0], ins[1] + (uint32_t)param_base));
+    }
     d.code_len = o.code_len;
     d.paint_off = (uint32_t)(param_base + o.paint_param);
     for (int k = 0; k < 3; k++) { d.mn[k] = o.mn[k]; d.mx[k] = o.mx[k]; }
@@ -318,13 +427,32 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
     // shapes.ts:349-350
     d.bhd = 4 * std::sqrt(3.0) * vs * o.slack + vs * 0.01;
     d.shd = 2 * std::sqrt(3.0) * vs * o.slack + vs * 0.01;
+    // mixed mode: anchor, float32 parameters, certified thresholds
+    for (int k = 0; k < 3; k++) d.anchor[k] = 0.5 * (o.mn[k] + o.mx[k]);
+    {
+      const double M = MIXED_MARGIN;
+      d.thr[T_BSK_HI] = ru32(d.bhd + M); d.thr[T_BSK_LO] = rd32(d.bhd - M);
+      d.thr[T_BFU_HI] = rd32(-d.bhd - M); d.thr[T_BFU_LO] = ru32(-d.bhd + M);
+      d.thr[T_SSK_HI] = ru32(d.shd + M); d.thr[T_SSK_LO] = rd32(d.shd - M);
+      d.thr[T_SFU_HI] = rd32(-d.shd - M); d.thr[T_SFU_LO] = ru32(-d.shd + M);
+      d.thr[T_V_HI] = ru32(M); d.thr[T_V_LO] = rd32(-M);
+      d.thr[T_M] = ru32(M);
+      size_t c32_before = n32_code.size(), p32_before = n32_p.size();
+      bool ok32 = convert32(code + 2 * (size_t)o.code_begin, o.code_len, P.data(), d.anchor, n32_code, n32_p);
+      double ext = (double)w->dx * vs;
+      if ((double)w->dy * vs > ext) ext = (double)w->dy * vs;
+      if ((double)w->dz * vs > ext) ext = (double)w->dz * vs;
+      if (!ok32 || ext > MIXED_MAX_COORD) d.flags |= OPF_FP64_ONLY;
+      // code32 entries are relative to this op's code; rebase onto the world's arrays
+      for (size_t k = c32_before; k < n32_code.size(); k++) n32_code[k] += (uint32_t)(w->p32.size());
+      (void)p32_before;
+    }
     nops.push_back(d);
     nboxes.push_back(box);
   }
-  w->code.resize(code_base + n_code);
-  std::memcpy(w->code.data() + code_base, code, n_code * 8);
-  // parameter offsets in the code are relative to this IR's parameter block
-  for (size_t i = 0; i < n_code; i++) w->code[code_base + i].y += (uint32_t)param_base;
+  w->code.insert(w->code.end(), ncode.begin(), ncode.end());
+  w->code32.insert(w->code32.end(), n32_code.begin(), n32_code.end());
+  w->p32.insert(w->p32.end(), n32_p.begin(), n32_p.end());
   w->params.insert(w->params.end(), P.begin(), P.end());
   w->ops.insert(w->ops.end(), nops.begin(), nops.end());
   w->boxes.insert(w->boxes.end(), nboxes.begin(), nboxes.end());
@@ -372,11 +500,14 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
     w->pool_cap = (uint32_t)cap;
   }
 
-  // scratch
+  // scratch (a reallocated op table loses its resident copy)
+  const void* op_bufs_before[6] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p, w->d_p32.p};
   if ((rc = ensure(w, w->d_ops, sizeof(OpDev) * (size_t)n_ops)) ||
       (rc = ensure(w, w->d_boxes, sizeof(uint2) * (size_t)n_ops)) ||
       (rc = ensure(w, w->d_code, sizeof(uint2) * w->code.size())) ||
       (rc = ensure(w, w->d_params, sizeof(double) * w->params.size())) ||
+      (rc = ensure(w, w->d_code32, sizeof(uint32_t) * w->code32.size())) ||
+      (rc = ensure(w, w->d_p32, sizeof(float2) * w->p32.size())) ||
       (rc = ensure(w, w->tile_cnt, 4 * w->ntiles)) || (rc = ensure(w, w->tile_off, 4 * w->ntiles)) ||
       (rc = ensure(w, w->tiles_nonempty, 4 * w->ntiles)) || (rc = ensure(w, w->tile_ops, 4 * tile_pairs)) ||
       (rc = ensure(w, w->evt, P)) || (rc = ensure(w, w->fsrc, 8 * P)) || (rc = ensure(w, w->cnt, 4 * P)) ||
@@ -393,15 +524,16 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
     size_t nb = items / scan_items_per_block() + 2;
     if ((rc = ensure(w, w->scan_agg, 8 * nb))) return rc;
   }
+  {
+    const void* after[6] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p, w->d_p32.p};
+    for (int k = 0; k < 6; k++)
+      if (after[k] != op_bufs_before[k]) w->ops_resident = false;
+  }
   DevBuf& holes_in = w->holes_in_a ? w->holes_a : w->holes_b;
   DevBuf& holes_out = w->holes_in_a ? w->holes_b : w->holes_a;
   if ((rc = ensure(w, holes_in, 4 * (size_t)H + 4)) || (rc = ensure(w, holes_out, 4 * E_max + 4))) return rc;
 
   // upload the ops (one pinned staging copy per array)
-  for (int i = 0; i < n_ops; i++) {
-    OpDev& o = w->ops[i];
-    o.bhd32 = (float)o.bhd; o.shd32 = (float)o.shd; o.err32 = 0.f;
-  }
   const unsigned long long launches0 = launch_count();
   CU(cudaEventRecord(w->ev0, s));
   if (!w->ops_resident) {
@@ -409,6 +541,10 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
     CU(cudaMemcpyAsync(w->d_boxes.p, w->boxes.data(), sizeof(uint2) * (size_t)n_ops, cudaMemcpyHostToDevice, s));
     CU(cudaMemcpyAsync(w->d_code.p, w->code.data(), sizeof(uint2) * w->code.size(), cudaMemcpyHostToDevice, s));
     CU(cudaMemcpyAsync(w->d_params.p, w->params.data(), sizeof(double) * w->params.size(), cudaMemcpyHostToDevice, s));
+    if (!w->code32.empty()) {
+      CU(cudaMemcpyAsync(w->d_code32.p, w->code32.data(), sizeof(uint32_t) * w->code32.size(), cudaMemcpyHostToDevice, s));
+      CU(cudaMemcpyAsync(w->d_p32.p, w->p32.data(), sizeof(float2) * w->p32.size(), cudaMemcpyHostToDevice, s));
+    }
   }
   CU(cudaMemsetAsync(w->res.p, 0, sizeof(BuildResult), s));
   CU(cudaMemsetAsync(w->work_counter.p, 0, 16, s));
@@ -425,6 +561,11 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   fa.ops = (const OpDev*)w->d_ops.p;
   fa.code = (const uint2*)w->d_code.p;
   fa.params = (const double*)w->d_params.p;
+  fa.code32 = (const uint32_t*)w->d_code32.p;
+  fa.p32 = (const float2*)w->d_p32.p;
+  fa.vs_lo = rd32(w->vs);
+  fa.vs_hi = ru32(w->vs);
+  fa.validate = w->validate;
   fa.tile_off = (const uint32_t*)w->tile_off.p;
   fa.tile_cnt = (const uint32_t*)w->tile_cnt.p;
   fa.tile_ops = (const uint32_t*)w->tile_ops.p;
@@ -507,7 +648,13 @@ int px_build_finish(px_world* w) {
   w->stats.rescued = r.c.rescued;
   w->stats.alloc_events = r.c.alloc_events;
   w->stats.free_events = r.c.free_events;
-  w->stats.max_abs_err32 = r.max_err;
+  {
+    double me;
+    unsigned long long bits = r.max_err_bits;
+    std::memcpy(&me, &bits, 8);
+    w->stats.max_abs_err32 = me;
+  }
+  w->stats.violations = r.c.violations;
   w->stats.build_ms = ms;
   w->stats.status = r.status;
   if (r.status & (ST_STAGE_OVERFLOW | ST_POOL_OVERFLOW | ST_CHAIN))
@@ -522,6 +669,10 @@ int px_build_finish(px_world* w) {
   w->last_boxes.swap(w->boxes);
   w->last_code.swap(w->code);
   w->last_params.swap(w->params);
+  w->last_code32.swap(w->code32);
+  w->last_p32.swap(w->p32);
+  w->code32.clear();
+  w->p32.clear();
   w->ops.clear();
   w->boxes.clear();
   w->code.clear();
@@ -541,6 +692,12 @@ int px_build(px_world* w, int mode, void* stream) {
   return px_build_finish(w);
 }
 
+int px_set_validation(px_world* w, int on) {
+  if (!w) return PX_E_INVALID_ARG;
+  w->validate = on ? 1 : 0;
+  return PX_OK;
+}
+
 int px_world_reset(px_world* w, int requeue_last_ops, void* stream) {
   if (!w) return PX_E_INVALID_ARG;
   if (w->in_flight) return fail(w, PX_E_INVALID_ARG, "a build is in flight");
@@ -554,6 +711,8 @@ int px_world_reset(px_world* w, int requeue_last_ops, void* stream) {
     w->boxes = w->last_boxes;
     w->code = w->last_code;
     w->params = w->last_params;
+    w->code32 = w->last_code32;
+    w->p32 = w->last_p32;
     w->ops_resident = true;  // the device tables of the last build still hold them
   }
   return PX_OK;

@@ -33,7 +33,15 @@ enum : uint16_t {
 };
 constexpr int PAINT_NPARAMS[PK_COUNT] = {0, 5, 3, 4, 2, 2, 5, 37, 8};
 
-enum : uint8_t { OPF_CONTAINS = 1, OPF_HAS_SLACK = 2, OPF_PAINT_FRAME = 4 };
+enum : uint8_t { OPF_CONTAINS = 1, OPF_HAS_SLACK = 2, OPF_PAINT_FRAME = 4, OPF_FP64_ONLY = 0x80 };
+
+// Mixed mode: margin between the exact value of an expression on the float64
+// inputs and the reference's float64 result (valid for |values| <= 2^10 m).
+constexpr double MIXED_MARGIN = 0x1p-30;
+constexpr double MIXED_MAX_COORD = 1024.0;
+
+// per-op float32 thresholds of the mixed mode (certified comparisons)
+enum { T_BSK_HI, T_BSK_LO, T_BFU_HI, T_BFU_LO, T_SSK_HI, T_SSK_LO, T_SFU_HI, T_SFU_LO, T_V_HI, T_V_LO, T_M, T_COUNT };
 
 // device status bits (first error wins for the reported code)
 enum : uint32_t {
@@ -65,13 +73,14 @@ struct OpDev {
   double bhd, shd;                       // brickHalfDiag, subHalfDiag (shapes.ts:349-350)
   double mn[3], mx[3];                   // contains box (boxes only)
   double frame[4];                       // paint frame px, pz, cos, sin
-  float bhd32, shd32, err32, pad32;      // mixed mode thresholds and error bound
+  double anchor[3];                      // mixed mode: origin of the op's float32 coordinates
+  float thr[12];                         // mixed mode thresholds (T_*)
 };
 
 struct BuildCounters {
   unsigned long long brick_evals, sub_evals, voxel_evals, paint_evals, rescued;
   unsigned long long alloc_events, free_events;
-  unsigned long long pad;
+  unsigned long long violations;  // validation mode: float64 results outside the float32 enclosure
 };
 
 // Small device block read back after every build.
@@ -85,13 +94,17 @@ struct BuildResult {
   uint32_t n_fresh;
   uint32_t max_pool_index;
   BuildCounters c;
-  double max_err;        // max |d32 - d64| over rescued evaluations
+  unsigned long long max_err_bits;  // max |mid(d32) - d64| over rescued evaluations (double bits, >= 0)
 };
 
 struct FoldArgs {
   const OpDev* ops;
   const uint2* code;
   const double* params;
+  const uint32_t* code32;     // per instruction: offset of its float32 interval parameters
+  const float2* p32;          // float32 interval parameters (lo, hi)
+  float vs_lo, vs_hi;         // float32 enclosure of the voxel size
+  int validate;               // mixed mode: also evaluate float64 everywhere and count violations
   const uint32_t* tile_off;
   const uint32_t* tile_cnt;
   const uint32_t* tile_ops;

@@ -1,0 +1,197 @@
+// Float32 interval evaluator of the SDF bytecode (the mixed build mode).
+//
+// Every quantity is an interval [lo, hi] of float32 computed with directed
+// rounding (__f*_rd / __f*_ru), so it encloses the exact real value of the
+// reference expression evaluated on the exact float64 inputs.  Coordinates
+// are relative to a per-op anchor (the centre of the op's bounds), which
+// keeps magnitudes at the op's extent instead of the world's.  The reference's
+// float64 result differs from that exact value by far less than the margin M
+// (2^-30 m for |coordinates| <= 2^10 m), so a decision whose threshold lies
+// outside [lo - M, hi + M] is the reference's decision; anything else — and
+// any polygon crossing test that the intervals cannot settle — is re-done in
+// float64 (sdf64.cuh).  Only multiplications by constant intervals and squares
+// occur, so no general interval product is needed.
+#pragma once
+#include "px_internal.cuh"
+
+namespace px {
+
+struct Iv {
+  float lo, hi;
+};
+
+__device__ __forceinline__ Iv iv(float a) { return {a, a}; }
+__device__ __forceinline__ Iv iadd(Iv a, Iv b) { return {__fadd_rd(a.lo, b.lo), __fadd_ru(a.hi, b.hi)}; }
+__device__ __forceinline__ Iv isub(Iv a, Iv b) { return {__fsub_rd(a.lo, b.hi), __fsub_ru(a.hi, b.lo)}; }
+__device__ __forceinline__ Iv ineg(Iv a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ Iv iabs(Iv a) {
+  if (a.lo >= 0.f) return a;
+  if (a.hi <= 0.f) return {-a.hi, -a.lo};
+  return {0.f, fmaxf(-a.lo, a.hi)};
+}
+__device__ __forceinline__ Iv imax0(Iv a) { return {fmaxf(a.lo, 0.f), fmaxf(a.hi, 0.f)}; }
+__device__ __forceinline__ Iv imin0(Iv a) { return {fminf(a.lo, 0.f), fminf(a.hi, 0.f)}; }
+__device__ __forceinline__ Iv imax(Iv a, Iv b) { return {fmaxf(a.lo, b.lo), fmaxf(a.hi, b.hi)}; }
+__device__ __forceinline__ Iv imin(Iv a, Iv b) { return {fminf(a.lo, b.lo), fminf(a.hi, b.hi)}; }
+__device__ __forceinline__ Iv iclamp01(Iv a) { return {fminf(fmaxf(a.lo, 0.f), 1.f), fminf(fmaxf(a.hi, 0.f), 1.f)}; }
+__device__ __forceinline__ Iv isqr(Iv a) {
+  float l = fabsf(a.lo), h = fabsf(a.hi);
+  float mn = (a.lo <= 0.f && a.hi >= 0.f) ? 0.f : fminf(l, h);
+  float mx = fmaxf(l, h);
+  return {__fmul_rd(mn, mn), __fmul_ru(mx, mx)};
+}
+__device__ __forceinline__ Iv isqrt(Iv a) { return {__fsqrt_rd(fmaxf(a.lo, 0.f)), __fsqrt_ru(fmaxf(a.hi, 0.f))}; }
+// x * c for a constant interval c that does not straddle zero (or is [0, 0])
+__device__ __forceinline__ Iv icmul(Iv x, Iv c) {
+  if (c.lo >= 0.f) return {__fmul_rd(x.lo, x.lo >= 0.f ? c.lo : c.hi), __fmul_ru(x.hi, x.hi >= 0.f ? c.hi : c.lo)};
+  return {__fmul_rd(x.hi, x.hi >= 0.f ? c.lo : c.hi), __fmul_ru(x.lo, x.lo >= 0.f ? c.hi : c.lo)};
+}
+__device__ __forceinline__ Iv ilen2(Iv a, Iv b) { return isqrt(iadd(isqr(a), isqr(b))); }
+__device__ __forceinline__ Iv ilen3(Iv a, Iv b, Iv c) { return isqrt(iadd(iadd(isqr(a), isqr(b)), isqr(c))); }
+__device__ __forceinline__ Iv ldp(const Iv* p, int k) {
+  float2 v = __ldg(reinterpret_cast<const float2*>(p) + k);
+  return {v.x, v.y};
+}
+
+// shapes.ts:146-161 on intervals.  Records per vertex i: vix, viy, vjy, ex, ey, 1/den.
+__device__ __forceinline__ Iv sd_polygon32(Iv px_, Iv py_, const Iv* __restrict__ r, int n, float M, bool& amb) {
+  Iv d = iadd(isqr(isub(px_, ldp(r, 0))), isqr(isub(py_, ldp(r, 1))));
+  bool flip_all = false;
+  for (int i = 0; i < n; i++) {
+    const Iv* e = r + 6 * i;
+    Iv vix = ldp(e, 0), viy = ldp(e, 1), vjy = ldp(e, 2), ex = ldp(e, 3), ey = ldp(e, 4), inv = ldp(e, 5);
+    Iv wx = isub(px_, vix), wy = isub(py_, viy);
+    Iv t = iclamp01(icmul(iadd(icmul(wx, ex), icmul(wy, ey)), inv));
+    Iv bx = isub(wx, icmul(t, ex)), by = isub(wy, icmul(t, ey));
+    d = imin(d, iadd(isqr(bx), isqr(by)));
+    // crossing test (c1 && c2 && c3) || (!c1 && !c2 && !c3), decided only when certain
+    bool c1t = py_.lo >= __fadd_ru(viy.hi, M), c1f = py_.hi < __fsub_rd(viy.lo, M);
+    bool c2t = py_.hi < __fsub_rd(vjy.lo, M), c2f = py_.lo >= __fadd_ru(vjy.hi, M);
+    if (!(c1t || c1f) || !(c2t || c2f)) { amb = true; continue; }
+    if (c1t != c2t) continue;  // no flip whatever c3 is
+    Iv L = icmul(wy, ex), R = icmul(wx, ey);
+    float m3 = __fadd_ru(__fmul_ru(__fadd_ru(fmaxf(fabsf(L.lo), fabsf(L.hi)), fmaxf(fabsf(R.lo), fabsf(R.hi))), 0x1p-40f), 0x1p-60f);
+    bool c3t = L.lo > __fadd_ru(R.hi, m3), c3f = L.hi < __fsub_rd(R.lo, m3);
+    if (!(c3t || c3f)) { amb = true; continue; }
+    if (c1t ? c3t : !c3t) flip_all = !flip_all;
+  }
+  Iv s = isqrt(d);
+  return flip_all ? ineg(s) : s;
+}
+
+// shapes.ts:164-173 on intervals.  Records per segment: ax, ay, ex, ey, 1/den.
+__device__ __forceinline__ Iv sd_polyline32(Iv px_, Iv py_, const Iv* __restrict__ r, int nseg) {
+  Iv d = {INFINITY, INFINITY};
+  for (int i = 0; i < nseg; i++) {
+    const Iv* e = r + 5 * i;
+    Iv ex = ldp(e, 2), ey = ldp(e, 3), inv = ldp(e, 4);
+    Iv wx = isub(px_, ldp(e, 0)), wy = isub(py_, ldp(e, 1));
+    Iv t = iclamp01(icmul(iadd(icmul(wx, ex), icmul(wy, ey)), inv));
+    d = imin(d, iadd(isqr(isub(wx, icmul(t, ex))), isqr(isub(wy, icmul(t, ey)))));
+  }
+  return isqrt(d);
+}
+
+__device__ __forceinline__ Iv prim32(uint32_t op, int cnt, const Iv* __restrict__ p, Iv x, Iv y, Iv z, float M, bool& amb) {
+  switch (op) {
+    case OP_BOX: case OP_ROUNDBOX: {
+      Iv qx = isub(iabs(isub(x, ldp(p, 0))), ldp(p, 3)), qy = isub(iabs(isub(y, ldp(p, 1))), ldp(p, 4)),
+         qz = isub(iabs(isub(z, ldp(p, 2))), ldp(p, 5));
+      Iv r = iadd(ilen3(imax0(qx), imax0(qy), imax0(qz)), imin0(imax(imax(qx, qy), qz)));
+      return op == OP_BOX ? r : isub(r, ldp(p, 6));
+    }
+    case OP_SPHERE:
+      return isub(ilen3(isub(x, ldp(p, 0)), isub(y, ldp(p, 1)), isub(z, ldp(p, 2))), ldp(p, 3));
+    case OP_ELLIPSOID: {  // params hold 1/rx, 1/ry, 1/rz
+      Iv l = ilen3(icmul(isub(x, ldp(p, 0)), ldp(p, 3)), icmul(isub(y, ldp(p, 1)), ldp(p, 4)),
+                   icmul(isub(z, ldp(p, 2)), ldp(p, 5)));
+      return icmul(isub(l, iv(1.f)), ldp(p, 6));
+    }
+    case OP_CYL_X: case OP_CYL_Y: case OP_CYL_Z: {
+      Iv a, b, h;
+      if (op == OP_CYL_Y) { a = isub(x, ldp(p, 0)); b = isub(z, ldp(p, 2)); h = isub(y, ldp(p, 1)); }
+      else if (op == OP_CYL_X) { a = isub(y, ldp(p, 1)); b = isub(z, ldp(p, 2)); h = isub(x, ldp(p, 0)); }
+      else { a = isub(x, ldp(p, 0)); b = isub(y, ldp(p, 1)); h = isub(z, ldp(p, 2)); }
+      Iv dr = isub(ilen2(a, b), ldp(p, 3)), dh = isub(iabs(h), ldp(p, 4));
+      return iadd(imin0(imax(dr, dh)), ilen2(imax0(dr), imax0(dh)));
+    }
+    case OP_CAPSULE: {  // params: a, ba, 1/bb, r
+      Iv px_ = isub(x, ldp(p, 0)), py_ = isub(y, ldp(p, 1)), pz_ = isub(z, ldp(p, 2));
+      Iv bax = ldp(p, 3), bay = ldp(p, 4), baz = ldp(p, 5);
+      Iv h = iclamp01(icmul(iadd(iadd(icmul(px_, bax), icmul(py_, bay)), icmul(pz_, baz)), ldp(p, 6)));
+      return isub(ilen3(isub(px_, icmul(h, bax)), isub(py_, icmul(h, bay)), isub(pz_, icmul(h, baz))), ldp(p, 7));
+    }
+    case OP_TORUS_X: case OP_TORUS_Y: case OP_TORUS_Z: {
+      Iv a, b, h;
+      if (op == OP_TORUS_Y) { a = isub(x, ldp(p, 0)); b = isub(z, ldp(p, 2)); h = isub(y, ldp(p, 1)); }
+      else if (op == OP_TORUS_X) { a = isub(y, ldp(p, 1)); b = isub(z, ldp(p, 2)); h = isub(x, ldp(p, 0)); }
+      else { a = isub(x, ldp(p, 0)); b = isub(y, ldp(p, 1)); h = isub(z, ldp(p, 2)); }
+      return isub(ilen2(isub(ilen2(a, b), ldp(p, 3)), h), ldp(p, 4));
+    }
+    case OP_LATHE_SOLID:
+      return sd_polygon32(ilen2(isub(x, ldp(p, 0)), isub(z, ldp(p, 2))), isub(y, ldp(p, 1)), p + 3, cnt, M, amb);
+    case OP_LATHE_SHELL:
+      return isub(sd_polyline32(ilen2(isub(x, ldp(p, 0)), isub(z, ldp(p, 2))), isub(y, ldp(p, 1)), p + 4, cnt - 1),
+                  ldp(p, 3));
+    case OP_PRISM: {
+      Iv d2 = sd_polygon32(isub(x, ldp(p, 0)), isub(z, ldp(p, 1)), p + 4, cnt, M, amb);
+      Iv dy = isub(iabs(isub(y, ldp(p, 2))), ldp(p, 3));
+      return iadd(imin0(imax(d2, dy)), ilen2(imax0(d2), imax0(dy)));
+    }
+    case OP_STADIUM: {  // Math.hypot encloses like len2
+      Iv dx = imax0(isub(iabs(isub(x, ldp(p, 0))), ldp(p, 2)));
+      Iv d2 = isub(ilen2(dx, isub(z, ldp(p, 1))), ldp(p, 3));
+      Iv dy = isub(iabs(isub(y, ldp(p, 4))), ldp(p, 5));
+      return iadd(imin0(imax(d2, dy)), ilen2(imax0(d2), imax0(dy)));
+    }
+  }
+  return {-INFINITY, INFINITY};
+}
+
+// code32[i] is the offset of instruction i's float32 parameters.
+__device__ __noinline__ Iv sdf32i(const uint2* __restrict__ code, const uint32_t* __restrict__ code32, int n,
+                                  const Iv* __restrict__ P, Iv x, Iv y, Iv z, float M, bool& amb) {
+  Iv s0 = {0.f, 0.f}, s1 = s0, s2 = s0, s3 = s0;
+  Iv ax0 = s0, ay0 = s0, az0 = s0, ax1 = s0, ay1 = s0, az1 = s0, ax2 = s0, ay2 = s0, az2 = s0;
+  for (int i = 0; i < n; i++) {
+    const uint32_t w0 = __ldg(&code[i].x);
+    const uint32_t op = w0 & 0xffu;
+    const int cnt = (int)(w0 >> 8);
+    const Iv* p = P + __ldg(code32 + i);
+    if (op < OP_ROT_X) {
+      Iv v = prim32(op, cnt, p, x, y, z, M, amb);
+      s3 = s2; s2 = s1; s1 = s0; s0 = v;
+      continue;
+    }
+    switch (op) {
+      case OP_ROT_X: case OP_ROT_Y: case OP_ROT_Z: {
+        ax2 = ax1; ay2 = ay1; az2 = az1; ax1 = ax0; ay1 = ay0; az1 = az0; ax0 = x; ay0 = y; az0 = z;
+        Iv p0 = ldp(p, 0), p1 = ldp(p, 1), c = ldp(p, 2), sn = ldp(p, 3);
+        if (op == OP_ROT_Y) {
+          Iv dx = isub(x, p0), dz = isub(z, p1);
+          x = iadd(iadd(p0, icmul(dx, c)), icmul(dz, sn));
+          z = iadd(isub(p1, icmul(dx, sn)), icmul(dz, c));
+        } else if (op == OP_ROT_X) {
+          Iv dy = isub(y, p0), dz = isub(z, p1);
+          y = iadd(iadd(p0, icmul(dy, c)), icmul(dz, sn));
+          z = iadd(isub(p1, icmul(dy, sn)), icmul(dz, c));
+        } else {
+          Iv dx = isub(x, p0), dy = isub(y, p1);
+          x = iadd(iadd(p0, icmul(dx, c)), icmul(dy, sn));
+          y = iadd(isub(p1, icmul(dx, sn)), icmul(dy, c));
+        }
+        break;
+      }
+      case OP_ROT_END:
+        x = ax0; y = ay0; z = az0; ax0 = ax1; ay0 = ay1; az0 = az1; ax1 = ax2; ay1 = ay2; az1 = az2;
+        break;
+      case OP_OFFSET: s0 = iadd(s0, ldp(p, 0)); break;
+      case OP_NEGMAX: { Iv b = s0; s0 = s1; s1 = s2; s2 = s3; s0 = imax(s0, ineg(b)); break; }
+      case OP_MAX: { Iv b = s0; s0 = s1; s1 = s2; s2 = s3; s0 = imax(s0, b); break; }
+      case OP_MIN: { Iv b = s0; s0 = s1; s1 = s2; s2 = s3; s0 = imin(s0, b); break; }
+    }
+  }
+  return s0;
+}
+
+}  // namespace px

@@ -43,7 +43,7 @@ def assert_same_world(w, o):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("mode", [MODE_FP64])
+@pytest.mark.parametrize("mode", [MODE_FP64, MODE_MIXED])
 def test_penthouse_vpm20_bit_exact(built_lib, mode):
     prog, _ = penthouse_program(20.0)
     o = pyoracle.OracleWorld(prog.to_bytes(), 20.0, config.Config(20.0).dims)
@@ -52,3 +52,32 @@ def test_penthouse_vpm20_bit_exact(built_lib, mode):
     s = w.stats()
     assert s["voxel_evals"] == o.stats["voxel_evals"]
     assert s["brick_evals"] == o.stats["brick_evals"]
+
+
+@pytest.mark.gpu
+def test_mixed_enclosures_hold_everywhere(built_lib):
+    """Validation mode: every float32 interval must enclose the float64 value
+    (within the certified margin); the build must still be bit-exact."""
+    from pixels_gb300 import _lib
+    vpm = 20.0
+    prog, _ = penthouse_program(vpm)
+    o = pyoracle.OracleWorld(prog.to_bytes(), vpm, config.Config(vpm).dims)
+    cfg = config.Config(vpm)
+    w = VoxelWorld(*cfg.dims, vpm=vpm, mode=MODE_MIXED)
+    _lib.set_validation(w._h, True)
+    w._pending = prog
+    w.build()
+    s = w.stats()
+    assert s["violations"] == 0
+    assert_same_world(w, o)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("vpm", [40.0])
+def test_penthouse_vpm40_mixed_bit_exact(built_lib, vpm):
+    prog, _ = penthouse_program(vpm)
+    o = pyoracle.OracleWorld(prog.to_bytes(), vpm, config.Config(vpm).dims)
+    w = build_gpu(vpm, MODE_MIXED, program=prog)
+    assert_same_world(w, o)
+    s = w.stats()
+    assert s["rescued"] < 0.01 * s["voxel_evals"]
