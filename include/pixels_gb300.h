@@ -62,6 +62,8 @@ typedef struct px_stats {
   uint32_t kernel_launches;  /* kernels the last build launched */
   uint32_t pad;
   uint64_t violations;       /* validation mode: float64 results outside their float32 enclosure */
+  uint64_t rescued_brick, rescued_sub, rescued_voxel;  /* rescues by level (mixed mode) */
+  uint64_t rescued_polygon;  /* ... of which a polygon crossing test was undecided */
 } px_stats;
 
 /* Device addresses of the world's buffers (valid until the next build or destroy). */

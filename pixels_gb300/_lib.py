@@ -40,7 +40,8 @@ class Stats(ctypes.Structure):
         ("pool_used", ctypes.c_uint32), ("n_holes", ctypes.c_uint32), ("pool_capacity", ctypes.c_uint32),
         ("status", ctypes.c_uint32), ("max_abs_err32", ctypes.c_double), ("build_ms", ctypes.c_float),
         ("fold_ms", ctypes.c_float), ("kernel_launches", ctypes.c_uint32), ("pad", ctypes.c_uint32),
-        ("violations", ctypes.c_uint64),
+        ("violations", ctypes.c_uint64), ("rescued_brick", ctypes.c_uint64), ("rescued_sub", ctypes.c_uint64),
+        ("rescued_voxel", ctypes.c_uint64), ("rescued_polygon", ctypes.c_uint64),
     ]
 
 

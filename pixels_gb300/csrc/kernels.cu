@@ -103,6 +103,7 @@ struct WarpCounters {
 struct LaneStats {
   unsigned long long paint, resc, viol;
   double max_err;
+  unsigned long long rb, rs, rv, rp;
 };
 
 // Decisions of apply() from a float32 interval (thresholds certified on the host):
@@ -129,7 +130,7 @@ __device__ __forceinline__ Iv koff(float k, float vs_lo, float vs_hi) { return {
 template <int MODE>
 __device__ __forceinline__ int eval_decide(const FoldArgs& a, const OpDev* O, const uint2* code, int clen, bool use32,
                                            const Iv* bo, float kx, float ky, float kz, double X, double Y, double Z,
-                                           int what, LaneStats& ls) {
+                                           int what, LaneStats& ls, bool count = true) {
   const int base = what == 1 ? T_BSK_HI : T_SSK_HI;
   if (MODE == 1 && use32) {
     bool amb = false;
@@ -142,9 +143,11 @@ __device__ __forceinline__ int eval_decide(const FoldArgs& a, const OpDev* O, co
     if (r != 3 && !a.validate) return r;
     double d64 = sdf64(code, clen, a.params, X, Y, Z);
     const double M = MIXED_MARGIN;
-    if (a.validate && !amb && !((double)d.lo - M <= d64 && d64 <= (double)d.hi + M)) ls.viol++;
-    if (r == 3) {
+    if (a.validate && !amb && !((double)d.lo - M <= d64 && d64 <= (double)d.hi + M) && count) ls.viol++;
+    if (r == 3 && count) {
       ls.resc++;
+      if (what == 1) ls.rb++; else if (what == 2) ls.rs++; else ls.rv++;  // brick: counted by lane 0 only
+      if (amb) ls.rp++;
       double mid = 0.5 * ((double)d.lo + (double)d.hi);
       double e = fabs(mid - d64);
       if (e == e && e > ls.max_err && !amb) ls.max_err = e;
@@ -169,7 +172,7 @@ __global__ void __launch_bounds__(256, 2) fold_kernel(FoldArgs a) {
   const int lx0 = (lane & 3) * 2, ly = lane >> 2;
   const double vs = a.vs;
   WarpCounters wc = {0, 0, 0, 0, 0};
-  LaneStats ls = {0, 0, 0, 0.0};
+  LaneStats ls = {0, 0, 0, 0.0, 0, 0, 0, 0};
   uint32_t st_local = 0;
   const uint32_t n_work = __ldg(&a.res->n_nonempty) * 64u;
 
@@ -250,7 +253,7 @@ __global__ void __launch_bounds__(256, 2) fold_kernel(FoldArgs a) {
         }
         if (!full) {
           int cls = eval_decide<MODE>(a, O, code, clen, use32, bo, 3.5f, 3.5f, 3.5f, (ox + 4) * vs, (oy + 4) * vs,
-                                      (oz + 4) * vs, 1, ls);
+                                      (oz + 4) * vs, 1, ls, lane == 0);
           wc.brick++;
           if (cls == 0) continue;
           full = cls == 2;
@@ -397,7 +400,7 @@ __global__ void __launch_bounds__(256, 2) fold_kernel(FoldArgs a) {
     if (wc.alloc) atomicAdd(&a.res->c.alloc_events, wc.alloc);
     if (wc.free_) atomicAdd(&a.res->c.free_events, wc.free_);
   }
-  unsigned long long pc = ls.paint, rc = ls.resc, vc = ls.viol;
+  unsigned long long pc = ls.paint, rc = ls.resc, vc = ls.viol, rb = ls.rb, rs = ls.rs, rv = ls.rv, rp = ls.rp;
   double me = ls.max_err;
   uint32_t stw = st_local;
 #pragma unroll
@@ -405,6 +408,10 @@ __global__ void __launch_bounds__(256, 2) fold_kernel(FoldArgs a) {
     pc += __shfl_xor_sync(FULLMASK, pc, o);
     rc += __shfl_xor_sync(FULLMASK, rc, o);
     vc += __shfl_xor_sync(FULLMASK, vc, o);
+    rb += __shfl_xor_sync(FULLMASK, rb, o);
+    rs += __shfl_xor_sync(FULLMASK, rs, o);
+    rv += __shfl_xor_sync(FULLMASK, rv, o);
+    rp += __shfl_xor_sync(FULLMASK, rp, o);
     me = fmax(me, __shfl_xor_sync(FULLMASK, me, o));
     stw |= __shfl_xor_sync(FULLMASK, stw, o);
   }
@@ -412,6 +419,10 @@ __global__ void __launch_bounds__(256, 2) fold_kernel(FoldArgs a) {
     if (pc) atomicAdd(&a.res->c.paint_evals, pc);
     if (rc) atomicAdd(&a.res->c.rescued, rc);
     if (vc) atomicAdd(&a.res->c.violations, vc);
+    if (rb) atomicAdd(&a.res->c.resc_brick, rb);
+    if (rs) atomicAdd(&a.res->c.resc_sub, rs);
+    if (rv) atomicAdd(&a.res->c.resc_vox, rv);
+    if (rp) atomicAdd(&a.res->c.resc_poly, rp);
     if (me > 0.0) atomicMax(&a.res->max_err_bits, (unsigned long long)__double_as_longlong(me));
     if (stw) atomicOr(&a.res->status, stw);
   }

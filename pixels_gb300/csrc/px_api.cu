@@ -655,6 +655,10 @@ int px_build_finish(px_world* w) {
     w->stats.max_abs_err32 = me;
   }
   w->stats.violations = r.c.violations;
+  w->stats.rescued_brick = r.c.resc_brick;
+  w->stats.rescued_sub = r.c.resc_sub;
+  w->stats.rescued_voxel = r.c.resc_vox;
+  w->stats.rescued_polygon = r.c.resc_poly;
   w->stats.build_ms = ms;
   w->stats.status = r.status;
   if (r.status & (ST_STAGE_OVERFLOW | ST_POOL_OVERFLOW | ST_CHAIN))

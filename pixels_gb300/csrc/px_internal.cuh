@@ -81,6 +81,7 @@ struct BuildCounters {
   unsigned long long brick_evals, sub_evals, voxel_evals, paint_evals, rescued;
   unsigned long long alloc_events, free_events;
   unsigned long long violations;  // validation mode: float64 results outside the float32 enclosure
+  unsigned long long resc_brick, resc_sub, resc_vox, resc_poly;  // rescues by level; polygon-test ambiguity
 };
 
 // Small device block read back after every build.
