@@ -11,7 +11,8 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libpixels_gb300.so")
+# PIXELS_GB300_LIB selects another in-tree build of the library (kernel variants)
+LIB_PATH = os.environ.get("PIXELS_GB300_LIB", os.path.join(HERE, "libpixels_gb300.so"))
 
 PX_OK = 0
 ERRORS = {1: "PX_E_INVALID_ARG", 2: "PX_E_INVALID_IR", 3: "PX_E_OOM", 4: "PX_E_QUEUE_OVERFLOW",

@@ -38,17 +38,20 @@ def _stale(target: str, deps) -> bool:
     return any(os.path.exists(d) and os.path.getmtime(d) > t for d in deps)
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
+def build(force: bool = False, verbose: bool = False, defines=(), out: str = OUT) -> str:
+    """Compile and link the library; ``defines`` (``NAME=VALUE``) select kernel
+    variants (register budgets) and ``out`` an alternative output path."""
     os.makedirs(BUILD_DIR, exist_ok=True)
+    tag = "_".join(d.replace("=", "") for d in defines)
     hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(HERE, "..", "include", "pixels_gb300.h")]
     objs = []
     jobs = []
     for u in UNITS:
         src = os.path.join(CSRC, u)
-        obj = os.path.join(BUILD_DIR, u.replace(".cu", ".o"))
+        obj = os.path.join(BUILD_DIR, u.replace(".cu", f"{tag}.o"))
         objs.append(obj)
         if force or _stale(obj, [src, *hdrs, __file__]):
-            jobs.append([_nvcc(), *ARCH, *NVCC_FLAGS, "-c", src, "-o", obj])
+            jobs.append([_nvcc(), *ARCH, *NVCC_FLAGS, *[f"-D{d}" for d in defines], "-c", src, "-o", obj])
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -57,12 +60,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
             sys.stderr.write(r.stdout + r.stderr)
     with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         list(ex.map(run, jobs))
-    if force or jobs or _stale(OUT, objs):
-        run([_nvcc(), *ARCH, "-shared", "-o", OUT, *objs, "-lcudart"])
+    if force or jobs or _stale(out, objs):
+        run([_nvcc(), *ARCH, "-shared", "-o", out, *objs, "-lcudart"])
     jsrc = os.path.join(CSRC, "jsmath_host.cpp")
     if force or _stale(JSM_OUT, [jsrc, os.path.join(CSRC, "jsmath.cuh"), os.path.join(CSRC, "jsmath_tables.h")]):
         run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-o", JSM_OUT, jsrc])
-    return OUT
+    return out
 
 
 if __name__ == "__main__":

@@ -27,6 +27,14 @@ namespace px {
 
 #define FULLMASK 0xffffffffu
 
+// CTAs per SM the two build kernels are compiled for (register budget)
+#ifndef PX_CLASSIFY_MINB
+#define PX_CLASSIFY_MINB 3
+#endif
+#ifndef PX_FOLD_MINB
+#define PX_FOLD_MINB 2
+#endif
+
 // kernel launches issued by the host wrappers (reported per build)
 static unsigned long long g_launches = 0;
 unsigned long long launch_count() { return g_launches; }
@@ -96,14 +104,14 @@ void launch_cull_fill(const uint2* boxes, int n_ops, int TX, int TY, int TZ, con
 enum { ST_EMPTY = 0, ST_UNIF = 1, ST_MIXED = 2 };
 
 struct WarpCounters {
-  unsigned long long brick, sub, vox, alloc, free_;
+  uint32_t brick, sub, vox, alloc, free_;
 };
 
 // Per-lane statistics of the float32 path.
 struct LaneStats {
-  unsigned long long paint, resc, viol;
-  double max_err;
-  unsigned long long rb, rs, rv, rp;
+  uint32_t paint, resc, viol;
+  float max_err;
+  uint32_t rb, rs, rv, rp;
 };
 
 // Decisions of apply() from a float32 interval (thresholds certified on the host):
@@ -125,11 +133,14 @@ __device__ __forceinline__ int classify64(double d, double half_diag) {
 __device__ __forceinline__ Iv koff(float k, float vs_lo, float vs_hi) { return {__fmul_rd(k, vs_lo), __fmul_ru(k, vs_hi)}; }
 
 // Evaluate one shape at one point: float64 directly, or float32 interval with
-// a float64 rescue when the interval cannot decide.  `kind`: 0 voxel (returns
-// inside), 1 brick, 2 sub-block (return the classification).
+// a float64 rescue when the interval cannot decide.  (tx, ty, tz) are the
+// reference's point in voxel units (ox + 4, sx + 2 or x + 0.5, exact in
+// float32); the float64 point (t * vs) is only formed when float64 runs.
+// `what`: 0 voxel (returns 1 = inside), 1 brick, 2 sub-block (return the
+// classification: 0 outside, 1 partial, 2 full).
 template <int MODE>
 __device__ __forceinline__ int eval_decide(const FoldArgs& a, const OpDev* O, const uint2* code, int clen, bool use32,
-                                           const Iv* bo, float kx, float ky, float kz, double X, double Y, double Z,
+                                           const Iv* bo, float kx, float ky, float kz, float tx, float ty, float tz,
                                            int what, LaneStats& ls, bool count = true) {
   const int base = what == 1 ? T_BSK_HI : T_SSK_HI;
   if (MODE == 1 && use32) {
@@ -141,7 +152,8 @@ __device__ __forceinline__ int eval_decide(const FoldArgs& a, const OpDev* O, co
     if (what == 0) r = amb ? 3 : (d.lo > O->thr[T_V_HI] ? 0 : (d.hi <= O->thr[T_V_LO] ? 1 : 3));
     else r = amb ? 3 : classify32(d, O->thr, base);
     if (r != 3 && !a.validate) return r;
-    double d64 = sdf64(code, clen, a.params, X, Y, Z);
+    const double vs = a.vs;
+    double d64 = sdf64(code, clen, a.params, (double)tx * vs, (double)ty * vs, (double)tz * vs);
     const double M = MIXED_MARGIN;
     if (a.validate && !amb && !((double)d.lo - M <= d64 && d64 <= (double)d.hi + M) && count) ls.viol++;
     if (r == 3 && count) {
@@ -150,29 +162,174 @@ __device__ __forceinline__ int eval_decide(const FoldArgs& a, const OpDev* O, co
       if (amb) ls.rp++;
       double mid = 0.5 * ((double)d.lo + (double)d.hi);
       double e = fabs(mid - d64);
-      if (e == e && e > ls.max_err && !amb) ls.max_err = e;
+      if (e == e && (float)e > ls.max_err && !amb) ls.max_err = (float)e;
     }
     if (what == 0) return d64 > 0.0 ? 0 : 1;
     return classify64(d64, what == 1 ? O->bhd : O->shd);
   }
-  double d = sdf64(code, clen, a.params, X, Y, Z);
+  const double vs = a.vs;
+  double d = sdf64(code, clen, a.params, (double)tx * vs, (double)ty * vs, (double)tz * vs);
   if (what == 0) return d > 0.0 ? 0 : 1;
   return classify64(d, what == 1 ? O->bhd : O->shd);
+}
+
+__device__ __forceinline__ void brick_of_pair(const OpDev* O, unsigned long long p, int& bx, int& by, int& bz) {
+  const uint32_t local = (uint32_t)(p - O->pair_base);
+  const uint32_t nxy = (uint32_t)(O->nx * O->ny);
+  const uint32_t zq = local / nxy, r = local - zq * nxy;
+  const uint32_t yq = r / (uint32_t)O->nx;
+  bz = O->bz0 + (int)zq;
+  by = O->by0 + (int)yq;
+  bx = O->bx0 + (int)(r - yq * (uint32_t)O->nx);
+}
+
+__device__ __forceinline__ void brick_bases(const FoldArgs& a, const OpDev* O, int bx, int by, int bz, Iv* bo) {
+  const float2* bt = a.bases + O->base_off;
+  float2 b0 = __ldg(bt + (bx - O->bx0)), b1 = __ldg(bt + O->nx + (by - O->by0)),
+         b2 = __ldg(bt + O->nx + O->ny + (bz - O->bz0));
+  bo[0] = {b0.x, b0.y};
+  bo[1] = {b1.x, b1.y};
+  bo[2] = {b2.x, b2.y};
+}
+
+// Classification of every (op, brick) pair — apply()'s SDF tests, which do not
+// depend on the world's state (shapes.ts:358-366, 382-394):
+//   brick level: one pair per lane (32 consecutive pairs, mostly one op);
+//   sub-block level: 4 partial pairs x 8 sub-blocks per pass;
+//   voxel level: one partial sub-block per pass, 64 voxels on 32 lanes.
+template <int MODE>
+__global__ void __launch_bounds__(256, PX_CLASSIFY_MINB) classify_kernel(FoldArgs a) {
+  const int lane = threadIdx.x & 31;
+  LaneStats ls = {0, 0, 0, 0.f, 0, 0, 0, 0};
+  uint32_t n_brick = 0;
+  const unsigned long long P = a.n_pairs;
+  const uint32_t n_chunks = (uint32_t)((P + 31) / 32);
+  for (;;) {
+    uint32_t chunk = 0;
+    if (lane == 0) chunk = atomicAdd(a.chunk_counter, 1u);
+    chunk = __shfl_sync(FULLMASK, chunk, 0);
+    if (chunk >= n_chunks) break;
+    const unsigned long long p = (unsigned long long)chunk * 32 + lane;
+    const bool valid = p < P;
+    uint32_t o = __ldg(a.chunk_op + chunk);
+    if (valid)
+      while (o + 1 < a.n_ops && a.ops[o + 1].pair_base <= p) o++;
+    const OpDev* O = a.ops + o;
+    int bx = 0, by = 0, bz = 0, cls = PC_SKIP;
+    if (valid) {
+      brick_of_pair(O, p, bx, by, bz);
+      const int flags = O->flags;
+      const bool contained = (flags & OPF_CONTAINS) && bx >= O->cbx0 && bx <= O->cbx1 && by >= O->cby0 &&
+                             by <= O->cby1 && bz >= O->cbz0 && bz <= O->cbz1;
+      if (contained) {
+        cls = PC_FULL;
+      } else {
+        const bool use32 = MODE == 1 && !(flags & OPF_FP64_ONLY);
+        Iv bo[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+        if (use32) brick_bases(a, O, bx, by, bz, bo);
+        cls = eval_decide<MODE>(a, O, a.code + O->code_off, (int)O->code_len, use32, bo, 3.5f, 3.5f, 3.5f,
+                                (float)(bx * 8 + 4), (float)(by * 8 + 4), (float)(bz * 8 + 4), 1, ls);
+        n_brick++;
+      }
+      a.pcode[p] = (uint8_t)cls;
+    }
+    uint32_t part = __ballot_sync(FULLMASK, valid && cls == PC_PARTIAL);
+    while (part) {
+      int src0 = -1, src1 = -1, src2 = -1, src3 = -1;
+      if (part) { src0 = __ffs(part) - 1; part &= part - 1; }
+      if (part) { src1 = __ffs(part) - 1; part &= part - 1; }
+      if (part) { src2 = __ffs(part) - 1; part &= part - 1; }
+      if (part) { src3 = __ffs(part) - 1; part &= part - 1; }
+      const int k = lane >> 3, s = lane & 7;
+      const int sl = k == 0 ? src0 : k == 1 ? src1 : k == 2 ? src2 : src3;
+      const int sll = sl < 0 ? 0 : sl;
+      const unsigned long long pp = __shfl_sync(FULLMASK, p, sll);
+      const uint32_t oo = __shfl_sync(FULLMASK, o, sll);
+      const int pbx = __shfl_sync(FULLMASK, bx, sll), pby = __shfl_sync(FULLMASK, by, sll),
+                pbz = __shfl_sync(FULLMASK, bz, sll);
+      int scls = PC_SKIP;
+      if (sl >= 0) {
+        const OpDev* Q = a.ops + oo;
+        const bool use32 = MODE == 1 && !(Q->flags & OPF_FP64_ONLY);
+        Iv bo[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+        if (use32) brick_bases(a, Q, pbx, pby, pbz, bo);
+        const int sxb = s & 1, syb = (s >> 1) & 1, szb = (s >> 2) & 1;
+        scls = eval_decide<MODE>(a, Q, a.code + Q->code_off, (int)Q->code_len, use32, bo, 4.f * sxb + 1.5f,
+                                 4.f * syb + 1.5f, 4.f * szb + 1.5f, (float)(pbx * 8 + sxb * 4 + 2),
+                                 (float)(pby * 8 + syb * 4 + 2), (float)(pbz * 8 + szb * 4 + 2), 2, ls);
+      }
+      uint32_t code16 = (uint32_t)scls << (2 * s);
+      code16 |= __shfl_xor_sync(FULLMASK, code16, 1);
+      code16 |= __shfl_xor_sync(FULLMASK, code16, 2);
+      code16 |= __shfl_xor_sync(FULLMASK, code16, 4);
+      if (s == 0 && sl >= 0) a.psub[pp] = (uint16_t)code16;
+      uint32_t vm = __ballot_sync(FULLMASK, sl >= 0 && scls == PC_PARTIAL);
+      while (vm) {
+        const int l = __ffs(vm) - 1;
+        vm &= vm - 1;
+        const int ss = l & 7;
+        const unsigned long long vp = __shfl_sync(FULLMASK, pp, l);
+        const uint32_t vo = __shfl_sync(FULLMASK, oo, l);
+        const int vbx = __shfl_sync(FULLMASK, pbx, l), vby = __shfl_sync(FULLMASK, pby, l),
+                  vbz = __shfl_sync(FULLMASK, pbz, l);
+        const OpDev* V = a.ops + vo;
+        const bool use32 = MODE == 1 && !(V->flags & OPF_FP64_ONLY);
+        Iv bo[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+        if (use32) brick_bases(a, V, vbx, vby, vbz, bo);
+        const int sxo = (ss & 1) * 4, syo = ((ss >> 1) & 1) * 4, szo = ((ss >> 2) & 1) * 4;
+        uint32_t bal[2];
+#pragma unroll
+        for (int r = 0; r < 2; r++) {
+          const int e = r * 32 + lane;
+          const int lx = sxo + (e & 3), lyv = syo + ((e >> 2) & 3), lz = szo + (e >> 4);
+          int inside = eval_decide<MODE>(a, V, a.code + V->code_off, (int)V->code_len, use32, bo, (float)lx,
+                                         (float)lyv, (float)lz, (float)(vbx * 8 + lx) + 0.5f,
+                                         (float)(vby * 8 + lyv) + 0.5f, (float)(vbz * 8 + lz) + 0.5f, 0, ls);
+          bal[r] = __ballot_sync(FULLMASK, inside == 1);
+        }
+        if (lane == 0) a.pmask[vp * 8 + ss] = (unsigned long long)bal[0] | ((unsigned long long)bal[1] << 32);
+      }
+    }
+  }
+  uint32_t nb = n_brick, rc = ls.resc, vc = ls.viol, rb = ls.rb, rs = ls.rs, rv = ls.rv, rp = ls.rp;
+  float me = ls.max_err;
+#pragma unroll
+  for (int o2 = 16; o2; o2 >>= 1) {
+    nb += __shfl_xor_sync(FULLMASK, nb, o2);
+    rc += __shfl_xor_sync(FULLMASK, rc, o2);
+    vc += __shfl_xor_sync(FULLMASK, vc, o2);
+    rb += __shfl_xor_sync(FULLMASK, rb, o2);
+    rs += __shfl_xor_sync(FULLMASK, rs, o2);
+    rv += __shfl_xor_sync(FULLMASK, rv, o2);
+    rp += __shfl_xor_sync(FULLMASK, rp, o2);
+    me = fmaxf(me, __shfl_xor_sync(FULLMASK, me, o2));
+  }
+  if (lane == 0) {
+    if (nb) atomicAdd(&a.res->c.brick_evals, (unsigned long long)nb);
+    if (rc) atomicAdd(&a.res->c.rescued, (unsigned long long)rc);
+    if (vc) atomicAdd(&a.res->c.violations, (unsigned long long)vc);
+    if (rb) atomicAdd(&a.res->c.resc_brick, (unsigned long long)rb);
+    if (rs) atomicAdd(&a.res->c.resc_sub, (unsigned long long)rs);
+    if (rv) atomicAdd(&a.res->c.resc_vox, (unsigned long long)rv);
+    if (rp) atomicAdd(&a.res->c.resc_poly, (unsigned long long)rp);
+    if (me > 0.f) atomicMax(&a.res->max_err_bits, (unsigned long long)__double_as_longlong((double)me));
+  }
 }
 
 // Lane layout of a brick in registers: lane owns the voxel pair
 // (x0, y, z) / (x0 + 1, y, z) with x0 = 2 (lane & 3), y = lane >> 2, in
 // register j = z.  Voxel index li = x | y << 3 | z << 6 (VoxelWorld.ts:60), so
 // register j of the warp is the contiguous 128-byte slice pool[64 j .. 64 j + 63].
-template <int MODE>
-__global__ void __launch_bounds__(256, 2) fold_kernel(FoldArgs a) {
+// The warp applies its brick's ops in order, as apply() does (shapes.ts:367-412),
+// using the pair classifications.
+__global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
   __shared__ unsigned long long smask[8][8];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const int lx0 = (lane & 3) * 2, ly = lane >> 2;
   const double vs = a.vs;
   WarpCounters wc = {0, 0, 0, 0, 0};
-  LaneStats ls = {0, 0, 0, 0.0, 0, 0, 0, 0};
+  uint32_t paint_calls = 0;
   uint32_t st_local = 0;
   const uint32_t n_work = __ldg(&a.res->n_nonempty) * 64u;
 
@@ -226,38 +383,14 @@ __global__ void __launch_bounds__(256, 2) fold_kernel(FoldArgs a) {
         m &= m - 1;
         const uint32_t o_idx = __shfl_sync(FULLMASK, oi, b);
         const OpDev* O = a.ops + o_idx;
+        const unsigned long long pair = O->pair_base +
+            (unsigned long long)(((bz - O->bz0) * O->ny + (by - O->by0)) * O->nx + (bx - O->bx0));
+        const int cls = __ldg(a.pcode + pair);
+        if (cls == PC_SKIP) continue;  // shapes.ts:364
+        const bool full = cls == PC_FULL;
         const int kind = O->kind, flags = O->flags;
         const uint32_t pk = O->paint_kind, pv = O->paint_value;
         const bool constPaint = pk == PK_CONST;
-        const uint2* code = a.code + O->code_off;
-        const int clen = (int)O->code_len;
-        const unsigned long long pair = O->pair_base +
-            (unsigned long long)(((bz - O->bz0) * O->ny + (by - O->by0)) * O->nx + (bx - O->bx0));
-        const bool use32 = MODE == 1 && !(flags & OPF_FP64_ONLY);
-        // float32 enclosure of the first voxel centre relative to the op anchor
-        Iv bo[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-        if (MODE == 1 && use32) {
-          const double pad = 0x1p-38;
-          double b0 = (ox + 0.5) * vs - O->anchor[0], b1 = (oy + 0.5) * vs - O->anchor[1], b2 = (oz + 0.5) * vs - O->anchor[2];
-          bo[0] = {__double2float_rd(b0 - pad), __double2float_ru(b0 + pad)};
-          bo[1] = {__double2float_rd(b1 - pad), __double2float_ru(b1 + pad)};
-          bo[2] = {__double2float_rd(b2 - pad), __double2float_ru(b2 + pad)};
-        }
-
-        // brick classification (shapes.ts:358-366)
-        bool full = false;
-        if (flags & OPF_CONTAINS) {
-          double x0 = (ox + 0.5) * vs, y0 = (oy + 0.5) * vs, z0 = (oz + 0.5) * vs;
-          double x1 = (ox + 7.5) * vs, y1 = (oy + 7.5) * vs, z1 = (oz + 7.5) * vs;
-          full = x0 >= O->mn[0] && x1 <= O->mx[0] && y0 >= O->mn[1] && y1 <= O->mx[1] && z0 >= O->mn[2] && z1 <= O->mx[2];
-        }
-        if (!full) {
-          int cls = eval_decide<MODE>(a, O, code, clen, use32, bo, 3.5f, 3.5f, 3.5f, (ox + 4) * vs, (oy + 4) * vs,
-                                      (oz + 4) * vs, 1, ls, lane == 0);
-          wc.brick++;
-          if (cls == 0) continue;
-          full = cls == 2;
-        }
         // uniform shortcuts (shapes.ts:367-374)
         int set_u = -1;
         if (full) {
@@ -281,40 +414,20 @@ __global__ void __launch_bounds__(256, 2) fold_kernel(FoldArgs a) {
         }
         if (kind == KIND_PAINT && state == ST_EMPTY) continue;
 
-        // sub-block classification (shapes.ts:382-389)
-        uint32_t sub_full = full ? 0xffu : 0u, sub_part = 0u;
+        // sub-block and voxel classes (shapes.ts:382-394), computed by classify_kernel
         if (!full) {
-          bool in8 = lane < 8;
-          int cls = 0;
-          if (in8) {
-            const int sxb = lane & 1, syb = (lane >> 1) & 1, szb = (lane >> 2) & 1;
-            const int sx = ox + sxb * 4, sy = oy + syb * 4, sz = oz + szb * 4;
-            cls = eval_decide<MODE>(a, O, code, clen, use32, bo, 4.f * sxb + 1.5f, 4.f * syb + 1.5f, 4.f * szb + 1.5f,
-                                    (sx + 2) * vs, (sy + 2) * vs, (sz + 2) * vs, 2, ls);
+          const uint32_t sc = __ldg(a.psub + pair);
+          if (lane < 8) {
+            const uint32_t c = (sc >> (2 * lane)) & 3u;
+            smask[wib][lane] = c == PC_FULL ? ~0ull : c == PC_PARTIAL ? __ldg(a.pmask + pair * 8 + lane) : 0ull;
           }
           wc.sub += 8;
-          uint32_t bf = __ballot_sync(FULLMASK, in8 && cls == 2);
-          uint32_t bs = __ballot_sync(FULLMASK, in8 && cls == 0);
-          sub_full = bf & 0xffu;
-          sub_part = ~(bf | bs) & 0xffu;
-        }
-        // boundary voxels of partial sub-blocks (shapes.ts:390-394)
-        if (lane < 8) smask[wib][lane] = ((sub_full >> lane) & 1u) ? ~0ull : 0ull;
-        __syncwarp();
-        for (uint32_t sp = sub_part; sp; sp &= sp - 1) {
-          const int s = __ffs(sp) - 1;
-          const int sxo = (s & 1) * 4, syo = ((s >> 1) & 1) * 4, szo = ((s >> 2) & 1) * 4;
-          uint32_t bal[2];
+          uint32_t np_ = 0;
 #pragma unroll
-          for (int r = 0; r < 2; r++) {
-            const int e = r * 32 + lane;
-            const int lx = sxo + (e & 3), lyv = syo + ((e >> 2) & 3), lz = szo + (e >> 4);
-            int inside = eval_decide<MODE>(a, O, code, clen, use32, bo, (float)lx, (float)lyv, (float)lz,
-                                           (ox + lx + 0.5) * vs, (oy + lyv + 0.5) * vs, (oz + lz + 0.5) * vs, 0, ls);
-            bal[r] = __ballot_sync(FULLMASK, inside == 1);
-          }
-          if (lane == 0) smask[wib][s] = (unsigned long long)bal[0] | ((unsigned long long)bal[1] << 32);
-          wc.vox += 64;
+          for (int s2 = 0; s2 < 8; s2++) np_ += ((sc >> (2 * s2)) & 3u) == PC_PARTIAL;
+          wc.vox += 64 * np_;
+        } else if (lane < 8) {
+          smask[wib][lane] = ~0ull;
         }
         __syncwarp();
 
@@ -341,7 +454,7 @@ __global__ void __launch_bounds__(256, 2) fold_kernel(FoldArgs a) {
                 PZ = fpz - sn * dx + c * dz;
               }
               next = paint_eval(pk, a.params + O->paint_off, PX, PY, PZ, st_local);
-              ls.paint++;
+              paint_calls++;
             } else next = pv;
             if (next != cur) {  // Uint16Array store; the comparison uses the unstored value
               vox[j] = (vox[j] & ~(0xffffu << (16 * h))) | ((next & 0xffffu) << (16 * h));
@@ -394,47 +507,31 @@ __global__ void __launch_bounds__(256, 2) fold_kernel(FoldArgs a) {
     }
   }
   if (lane == 0) {
-    if (wc.brick) atomicAdd(&a.res->c.brick_evals, wc.brick);
-    if (wc.sub) atomicAdd(&a.res->c.sub_evals, wc.sub);
-    if (wc.vox) atomicAdd(&a.res->c.voxel_evals, wc.vox);
-    if (wc.alloc) atomicAdd(&a.res->c.alloc_events, wc.alloc);
-    if (wc.free_) atomicAdd(&a.res->c.free_events, wc.free_);
+    if (wc.sub) atomicAdd(&a.res->c.sub_evals, (unsigned long long)wc.sub);
+    if (wc.vox) atomicAdd(&a.res->c.voxel_evals, (unsigned long long)wc.vox);
+    if (wc.alloc) atomicAdd(&a.res->c.alloc_events, (unsigned long long)wc.alloc);
+    if (wc.free_) atomicAdd(&a.res->c.free_events, (unsigned long long)wc.free_);
   }
-  unsigned long long pc = ls.paint, rc = ls.resc, vc = ls.viol, rb = ls.rb, rs = ls.rs, rv = ls.rv, rp = ls.rp;
-  double me = ls.max_err;
-  uint32_t stw = st_local;
+  uint32_t pc = paint_calls, stw = st_local;
 #pragma unroll
-  for (int o = 16; o; o >>= 1) {
-    pc += __shfl_xor_sync(FULLMASK, pc, o);
-    rc += __shfl_xor_sync(FULLMASK, rc, o);
-    vc += __shfl_xor_sync(FULLMASK, vc, o);
-    rb += __shfl_xor_sync(FULLMASK, rb, o);
-    rs += __shfl_xor_sync(FULLMASK, rs, o);
-    rv += __shfl_xor_sync(FULLMASK, rv, o);
-    rp += __shfl_xor_sync(FULLMASK, rp, o);
-    me = fmax(me, __shfl_xor_sync(FULLMASK, me, o));
-    stw |= __shfl_xor_sync(FULLMASK, stw, o);
+  for (int o2 = 16; o2; o2 >>= 1) {
+    pc += __shfl_xor_sync(FULLMASK, pc, o2);
+    stw |= __shfl_xor_sync(FULLMASK, stw, o2);
   }
   if (lane == 0) {
-    if (pc) atomicAdd(&a.res->c.paint_evals, pc);
-    if (rc) atomicAdd(&a.res->c.rescued, rc);
-    if (vc) atomicAdd(&a.res->c.violations, vc);
-    if (rb) atomicAdd(&a.res->c.resc_brick, rb);
-    if (rs) atomicAdd(&a.res->c.resc_sub, rs);
-    if (rv) atomicAdd(&a.res->c.resc_vox, rv);
-    if (rp) atomicAdd(&a.res->c.resc_poly, rp);
-    if (me > 0.0) atomicMax(&a.res->max_err_bits, (unsigned long long)__double_as_longlong(me));
+    if (pc) atomicAdd(&a.res->c.paint_evals, (unsigned long long)pc);
     if (stw) atomicOr(&a.res->status, stw);
   }
 }
 
 void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s) {
-  int blocks = n_sms * 2;
+  const int blocks = n_sms * PX_CLASSIFY_MINB;
   if (mode == 1) {
-    ++g_launches; fold_kernel<1><<<blocks, 256, 0, s>>>(a);
+    ++g_launches; classify_kernel<1><<<blocks, 256, 0, s>>>(a);
   } else {
-    ++g_launches; fold_kernel<0><<<blocks, 256, 0, s>>>(a);
+    ++g_launches; classify_kernel<0><<<blocks, 256, 0, s>>>(a);
   }
+  ++g_launches; fold_kernel<<<n_sms * PX_FOLD_MINB, 256, 0, s>>>(a);
 }
 
 // ---------------------------------------------------------------------------

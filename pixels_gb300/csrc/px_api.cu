@@ -49,14 +49,17 @@ struct px_world {
   std::vector<double> params;
   std::vector<uint32_t> code32, last_code32;   // per instruction: float32 parameter offset
   std::vector<float2> p32, last_p32;           // float32 interval parameters
+  std::vector<float2> bases, last_bases;       // per-op brick-row offsets (mixed mode)
   int validate = 0;
   uint64_t ops_applied = 0;
 
   // per-build device scratch
-  DevBuf d_ops, d_boxes, d_code, d_params, d_code32, d_p32;
+  DevBuf d_ops, d_boxes, d_code, d_params, d_code32, d_p32, d_bases;
   DevBuf tile_cnt, tile_off, tiles_nonempty, tile_ops;
   DevBuf evt, fsrc, cnt, pos, etype, ew, depth_fn, depth, tree, fresh, fresh_rank;
   DevBuf staging, stage_cell, stage_src;
+  DevBuf chunk_op, pcode, psub, pmask, chunk_counter;
+  std::vector<uint32_t> h_chunk_op;
   DevBuf scan_agg;
   DevBuf work_counter;
   DevBuf res;
@@ -336,10 +339,11 @@ void px_world_destroy(px_world* w) {
   cudaFree(w->d_grid);
   cudaFree(w->d_pool32);
   DevBuf* bufs[] = {&w->holes_a, &w->holes_b, &w->d_ops, &w->d_boxes, &w->d_code, &w->d_params, &w->d_code32,
-                    &w->d_p32, &w->tile_cnt,
+                    &w->d_p32, &w->d_bases, &w->tile_cnt,
                     &w->tile_off, &w->tiles_nonempty, &w->tile_ops, &w->evt, &w->fsrc, &w->cnt, &w->pos, &w->etype,
                     &w->ew, &w->depth_fn, &w->depth, &w->tree, &w->fresh, &w->fresh_rank, &w->staging,
-                    &w->stage_cell, &w->stage_src, &w->scan_agg, &w->work_counter, &w->res, &w->opaque,
+                    &w->stage_cell, &w->stage_src, &w->chunk_op, &w->pcode, &w->psub, &w->pmask,
+                    &w->chunk_counter, &w->scan_agg, &w->work_counter, &w->res, &w->opaque,
                     &w->udens, &w->super_counts, &w->density};
   for (DevBuf* b : bufs) release(*b);
   if (w->h_res) cudaFreeHost(w->h_res);
@@ -370,6 +374,7 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
   std::vector<uint2> nboxes;
   std::vector<uint2> ncode;         // the new ops' instructions, one copy per op
   std::vector<uint32_t> n32_code;   // their float32 parameter offsets
+  std::vector<float2> nbases;
   std::vector<float2> n32_p;
   nops.reserve(n_ops);
   const double vs = w->vs;
@@ -424,6 +429,25 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
       box = make_uint2((uint32_t)d.bx0 | ((uint32_t)d.by0 << 10) | ((uint32_t)d.bz0 << 20),
                        (uint32_t)d.bx1 | ((uint32_t)d.by1 << 10) | ((uint32_t)d.bz1 << 20));
     }
+    // contains() per axis (shapes.ts:47-48,360): monotone in the brick index, so a range
+    d.cbx0 = d.cby0 = d.cbz0 = 1;
+    d.cbx1 = d.cby1 = d.cbz1 = 0;
+    if ((o.flags & OPF_CONTAINS) && d.bx0 <= d.bx1) {
+      int32_t* lo[3] = {&d.cbx0, &d.cby0, &d.cbz0};
+      int32_t* hi[3] = {&d.cbx1, &d.cby1, &d.cbz1};
+      const int b0[3] = {d.bx0, d.by0, d.bz0}, b1[3] = {d.bx1, d.by1, d.bz1};
+      for (int k = 0; k < 3; k++) {
+        int first = -1, last = -2;
+        for (int b = b0[k]; b <= b1[k]; b++) {
+          int ob = b * 8;
+          if ((ob + 0.5) * vs >= o.mn[k] && (ob + 7.5) * vs <= o.mx[k]) {
+            if (first < 0) first = b;
+            last = b;
+          }
+        }
+        if (first < 0) { *lo[k] = 1; *hi[k] = 0; } else { *lo[k] = first; *hi[k] = last; }
+      }
+    }
     // shapes.ts:349-350
     d.bhd = 4 * std::sqrt(3.0) * vs * o.slack + vs * 0.01;
     d.shd = 2 * std::sqrt(3.0) * vs * o.slack + vs * 0.01;
@@ -437,6 +461,14 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
       d.thr[T_SFU_HI] = rd32(-d.shd - M); d.thr[T_SFU_LO] = ru32(-d.shd + M);
       d.thr[T_V_HI] = ru32(M); d.thr[T_V_LO] = rd32(-M);
       d.thr[T_M] = ru32(M);
+      // (b*8 + 0.5)*vs - anchor per brick row, padded for the float64 rounding of the
+      // reference's voxel centres ((x + 0.5)*vs, |x*vs| <= 2^10 m)
+      d.base_off = (uint32_t)(w->bases.size() + nbases.size());
+      if (d.bx0 <= d.bx1) {
+        const int b0[3] = {d.bx0, d.by0, d.bz0}, b1[3] = {d.bx1, d.by1, d.bz1};
+        for (int k = 0; k < 3; k++)
+          for (int b = b0[k]; b <= b1[k]; b++) nbases.push_back(enc((b * 8 + 0.5) * vs - d.anchor[k], 0x1p-38));
+      }
       size_t c32_before = n32_code.size(), p32_before = n32_p.size();
       bool ok32 = convert32(code + 2 * (size_t)o.code_begin, o.code_len, P.data(), d.anchor, n32_code, n32_p);
       double ext = (double)w->dx * vs;
@@ -453,6 +485,7 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
   w->code.insert(w->code.end(), ncode.begin(), ncode.end());
   w->code32.insert(w->code32.end(), n32_code.begin(), n32_code.end());
   w->p32.insert(w->p32.end(), n32_p.begin(), n32_p.end());
+  w->bases.insert(w->bases.end(), nbases.begin(), nbases.end());
   w->params.insert(w->params.end(), P.begin(), P.end());
   w->ops.insert(w->ops.end(), nops.begin(), nops.end());
   w->boxes.insert(w->boxes.end(), nboxes.begin(), nboxes.end());
@@ -501,13 +534,14 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   }
 
   // scratch (a reallocated op table loses its resident copy)
-  const void* op_bufs_before[6] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p, w->d_p32.p};
+  const void* op_bufs_before[7] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p, w->d_p32.p, w->d_bases.p};
   if ((rc = ensure(w, w->d_ops, sizeof(OpDev) * (size_t)n_ops)) ||
       (rc = ensure(w, w->d_boxes, sizeof(uint2) * (size_t)n_ops)) ||
       (rc = ensure(w, w->d_code, sizeof(uint2) * w->code.size())) ||
       (rc = ensure(w, w->d_params, sizeof(double) * w->params.size())) ||
       (rc = ensure(w, w->d_code32, sizeof(uint32_t) * w->code32.size())) ||
       (rc = ensure(w, w->d_p32, sizeof(float2) * w->p32.size())) ||
+      (rc = ensure(w, w->d_bases, sizeof(float2) * w->bases.size())) ||
       (rc = ensure(w, w->tile_cnt, 4 * w->ntiles)) || (rc = ensure(w, w->tile_off, 4 * w->ntiles)) ||
       (rc = ensure(w, w->tiles_nonempty, 4 * w->ntiles)) || (rc = ensure(w, w->tile_ops, 4 * tile_pairs)) ||
       (rc = ensure(w, w->evt, P)) || (rc = ensure(w, w->fsrc, 8 * P)) || (rc = ensure(w, w->cnt, 4 * P)) ||
@@ -516,7 +550,9 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
       (rc = ensure(w, w->tree, 4 * (E_max / 16 + 64 + E_max))) || (rc = ensure(w, w->fresh, 4 * E_max)) ||
       (rc = ensure(w, w->fresh_rank, 4 * E_max)) || (rc = ensure(w, w->staging, 1024 * touched_bound)) ||
       (rc = ensure(w, w->stage_cell, 4 * touched_bound)) || (rc = ensure(w, w->stage_src, 8 * touched_bound)) ||
-      (rc = ensure(w, w->work_counter, 16)) || (rc = ensure(w, w->res, sizeof(BuildResult))))
+      (rc = ensure(w, w->work_counter, 16)) || (rc = ensure(w, w->res, sizeof(BuildResult))) ||
+      (rc = ensure(w, w->chunk_op, 4 * ((P + 31) / 32))) || (rc = ensure(w, w->pcode, P)) ||
+      (rc = ensure(w, w->psub, 2 * P)) || (rc = ensure(w, w->pmask, 64 * P)) || (rc = ensure(w, w->chunk_counter, 16)))
     return rc;
   {
     size_t items = w->ntiles > E_max ? w->ntiles : E_max;
@@ -525,8 +561,8 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
     if ((rc = ensure(w, w->scan_agg, 8 * nb))) return rc;
   }
   {
-    const void* after[6] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p, w->d_p32.p};
-    for (int k = 0; k < 6; k++)
+    const void* after[7] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p, w->d_p32.p, w->d_bases.p};
+    for (int k = 0; k < 7; k++)
       if (after[k] != op_bufs_before[k]) w->ops_resident = false;
   }
   DevBuf& holes_in = w->holes_in_a ? w->holes_a : w->holes_b;
@@ -545,9 +581,23 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
       CU(cudaMemcpyAsync(w->d_code32.p, w->code32.data(), sizeof(uint32_t) * w->code32.size(), cudaMemcpyHostToDevice, s));
       CU(cudaMemcpyAsync(w->d_p32.p, w->p32.data(), sizeof(float2) * w->p32.size(), cudaMemcpyHostToDevice, s));
     }
+    if (!w->bases.empty())
+      CU(cudaMemcpyAsync(w->d_bases.p, w->bases.data(), sizeof(float2) * w->bases.size(), cudaMemcpyHostToDevice, s));
   }
   CU(cudaMemsetAsync(w->res.p, 0, sizeof(BuildResult), s));
   CU(cudaMemsetAsync(w->work_counter.p, 0, 16, s));
+  CU(cudaMemsetAsync(w->chunk_counter.p, 0, 16, s));
+  {  // op of the first pair of every 32-pair chunk
+    const size_t n_chunks = (P + 31) / 32;
+    w->h_chunk_op.resize(n_chunks);
+    uint32_t o = 0;
+    for (size_t c = 0; c < n_chunks; c++) {
+      const uint64_t p0 = (uint64_t)c * 32;
+      while (o + 1 < (uint32_t)n_ops && w->ops[o + 1].pair_base <= p0) o++;
+      w->h_chunk_op[c] = o;
+    }
+    if (n_chunks) CU(cudaMemcpyAsync(w->chunk_op.p, w->h_chunk_op.data(), 4 * n_chunks, cudaMemcpyHostToDevice, s));
+  }
   if (P) CU(cudaMemsetAsync(w->evt.p, 0, P, s));
 
   BuildResult* res = (BuildResult*)w->res.p;
@@ -558,11 +608,19 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   launch_cull_fill((const uint2*)w->d_boxes.p, n_ops, w->TX, w->TY, w->TZ, (const uint32_t*)w->tile_off.p,
                    (uint32_t*)w->tile_ops.p, s);
   FoldArgs fa{};
+  fa.chunk_op = (const uint32_t*)w->chunk_op.p;
+  fa.n_ops = (uint32_t)n_ops;
+  fa.n_pairs = P;
+  fa.pcode = (uint8_t*)w->pcode.p;
+  fa.psub = (uint16_t*)w->psub.p;
+  fa.pmask = (unsigned long long*)w->pmask.p;
+  fa.chunk_counter = (uint32_t*)w->chunk_counter.p;
   fa.ops = (const OpDev*)w->d_ops.p;
   fa.code = (const uint2*)w->d_code.p;
   fa.params = (const double*)w->d_params.p;
   fa.code32 = (const uint32_t*)w->d_code32.p;
   fa.p32 = (const float2*)w->d_p32.p;
+  fa.bases = (const float2*)w->d_bases.p;
   fa.vs_lo = rd32(w->vs);
   fa.vs_hi = ru32(w->vs);
   fa.validate = w->validate;
@@ -675,8 +733,10 @@ int px_build_finish(px_world* w) {
   w->last_params.swap(w->params);
   w->last_code32.swap(w->code32);
   w->last_p32.swap(w->p32);
+  w->last_bases.swap(w->bases);
   w->code32.clear();
   w->p32.clear();
+  w->bases.clear();
   w->ops.clear();
   w->boxes.clear();
   w->code.clear();
@@ -717,6 +777,7 @@ int px_world_reset(px_world* w, int requeue_last_ops, void* stream) {
     w->params = w->last_params;
     w->code32 = w->last_code32;
     w->p32 = w->last_p32;
+    w->bases = w->last_bases;
     w->ops_resident = true;  // the device tables of the last build still hold them
   }
   return PX_OK;

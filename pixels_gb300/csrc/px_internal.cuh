@@ -75,6 +75,9 @@ struct OpDev {
   double frame[4];                       // paint frame px, pz, cos, sin
   double anchor[3];                      // mixed mode: origin of the op's float32 coordinates
   float thr[12];                         // mixed mode thresholds (T_*)
+  int32_t cbx0, cby0, cbz0, cbx1, cby1, cbz1;  // bricks the box fully contains (contains(), shapes.ts:47-48,360)
+  uint32_t base_off;                     // mixed mode: float32 first-voxel-centre offsets per brick row
+  uint32_t pad2;
 };
 
 struct BuildCounters {
@@ -98,12 +101,24 @@ struct BuildResult {
   unsigned long long max_err_bits;  // max |mid(d32) - d64| over rescued evaluations (double bits, >= 0)
 };
 
+// Pair classification (state independent): class per (op, brick) pair, the 8
+// sub-block classes of partial pairs, and voxel inside-masks of partial sub-blocks.
+enum : uint8_t { PC_SKIP = 0, PC_PARTIAL = 1, PC_FULL = 2 };
+
 struct FoldArgs {
+  const uint32_t* chunk_op;   // op containing pair 32 * chunk
+  uint32_t n_ops;
+  unsigned long long n_pairs;
+  uint8_t* pcode;             // per pair: PC_*
+  uint16_t* psub;             // per partial pair: 2 bits per sub-block (PC_*)
+  unsigned long long* pmask;  // per partial pair: 8 inside-masks (bit = x&3 | (y&3)<<2 | (z&3)<<4)
+  uint32_t* chunk_counter;
   const OpDev* ops;
   const uint2* code;
   const double* params;
   const uint32_t* code32;     // per instruction: offset of its float32 interval parameters
   const float2* p32;          // float32 interval parameters (lo, hi)
+  const float2* bases;        // per op and axis: (b*8 + 0.5)*vs - anchor as a float32 interval
   float vs_lo, vs_hi;         // float32 enclosure of the voxel size
   int validate;               // mixed mode: also evaluate float64 everywhere and count violations
   const uint32_t* tile_off;
