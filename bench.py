@@ -93,6 +93,21 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(values, dist=None, device=None):
+    """Element-wise maximum of per-rank timings (the slowest rank sets the job time)."""
+    if dist is None:
+        return list(values)
+    import torch
+    t = torch.tensor(list(values), dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
+def job_value(world_size: int, cells_per_rank: int, seconds: float) -> float:
+    """Whole-job Gvoxels/s: every rank builds its own replica (weak scaling)."""
+    return world_size * cells_per_rank / seconds / 1e9
+
+
 def reference_arm(args):
     """The reference's CPU algorithm (float64 oracle restatement) on the host cores."""
     rank = _env_int("RANK", 0)
@@ -212,15 +227,10 @@ def main():
     st = _lib.stats(h)
 
     # max over ranks
-    t_mx = statistics.mean(ms_mx)
-    t_64 = statistics.mean(ms64)
-    if dist is not None:
-        tt = torch.tensor([t_mx, t_64], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_mx, t_64 = float(tt[0]), float(tt[1])
+    t_mx, t_64 = max_over_ranks([statistics.mean(ms_mx), statistics.mean(ms64)], dist, dev)
     cells = cfg.cells
-    value = world * cells / (t_mx * 1e-3) / 1e9
-    value64 = world * cells / (t_64 * 1e-3) / 1e9
+    value = job_value(world, cells, t_mx * 1e-3)
+    value64 = job_value(world, cells, t_64 * 1e-3)
 
     # end to end through the C ABI: op list from host memory, grid + pool back to pinned host memory
     grid_h = torch.empty(cfg.bricks[0] * cfg.bricks[1] * cfg.bricks[2], dtype=torch.int32, pin_memory=True)
@@ -247,12 +257,8 @@ def main():
         pool_h = torch.empty(max(used, 1) * 512, dtype=torch.int16, pin_memory=True)
         assert L.px_read_pool(h, pool_h.data_ptr(), pool_h.numel()) == 0
         e2e = [float("nan")]
-    t_e2e = statistics.mean(e2e)
-    if dist is not None:
-        tt = torch.tensor([t_e2e], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_e2e = float(tt[0])
-    e2e_value = world * cells / t_e2e / 1e9
+    t_e2e = max_over_ranks([statistics.mean(e2e)], dist, dev)[0]
+    e2e_value = job_value(world, cells, t_e2e)
 
     if rank != 0:
         if dist is not None:

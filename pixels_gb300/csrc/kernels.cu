@@ -32,7 +32,7 @@ namespace px {
 #define PX_CLASSIFY_MINB 3
 #endif
 #ifndef PX_FOLD_MINB
-#define PX_FOLD_MINB 2
+#define PX_FOLD_MINB 3
 #endif
 
 // kernel launches issued by the host wrappers (reported per build)
