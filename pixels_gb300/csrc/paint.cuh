@@ -30,10 +30,31 @@ __device__ __forceinline__ float sin_poly_f32(float t) {
   return v >= 0.0f ? r : -r;
 }
 
-__device__ __forceinline__ double sin_checked(double x, uint32_t& st) {
+__device__ __noinline__ double sin_cr(double x, uint32_t& st) {
   double r = px_sin(x);
   if (r != r && x == x) st |= ST_RANGE;
   return r;
+}
+__device__ __noinline__ double atan2_cr(double y, double x) { return px_atan2(y, x); }
+
+// Fast-path transcendentals: CUDA's own double sin/atan2 (documented maximum
+// error 2 ulp) decide a paint threshold when the result is farther than
+// FAST_ULPS ulps (8x the documented bound) from it; otherwise the correctly
+// rounded routines above decide.  Either way the decision equals the one the
+// correctly rounded value gives.
+constexpr double FAST_ULPS = 16.0;
+__device__ __forceinline__ double ulp_of(double v) { return fabs(v) * 0x1p-52 + 0x1p-1074; }
+
+// floor(((a + PI) / (2 PI)) * 8) for the chip-stack stripes, where a = atan2(y, x).
+// The map a -> q is monotone, so q at a -/+ the error bound brackets the exact q.
+__device__ __forceinline__ double stripe_index(double y, double x, uint32_t& st) {
+  const double PI = 3.141592653589793;
+  double a = atan2(y, x);
+  double e = FAST_ULPS * ulp_of(a);
+  double qlo = floor((((a - e) + PI) / (2 * PI)) * 8), qhi = floor((((a + e) + PI) / (2 * PI)) * 8);
+  if (qlo == qhi) return qlo;
+  double ac = atan2_cr(y, x);
+  return floor(((ac + PI) / (2 * PI)) * 8);
 }
 
 // One paint call at a voxel centre (metres, after the optional frame).
@@ -41,11 +62,11 @@ __device__ __noinline__ uint32_t paint_eval(uint32_t kind, const double* __restr
                                             uint32_t& st) {
   const double PI = 3.141592653589793;
   switch (kind) {
-    case PK_CHIP: {  // penthouse.ts:371-377
-      double a = px_atan2(z - __ldg(p + 2), x - __ldg(p));
+    case PK_CHIP: {  // penthouse.ts:371-377 (stripe only matters on the edge of even layers)
       bool edge = px_hypot2(x - __ldg(p), z - __ldg(p + 2)) > __ldg(p + 3);
-      bool stripe = fmod(floor(((a + PI) / (2 * PI)) * 8), 2.0) == 0;
       double layer = fmod(floor((y - __ldg(p + 1)) / 0.0045), 2.0);
+      bool stripe = false;
+      if (edge && layer == 0) stripe = fmod(stripe_index(z - __ldg(p + 2), x - __ldg(p), st), 2.0) == 0;
       return vox_of(__ldg(p + 4), edge && stripe && layer == 0 ? 255 : 0);
     }
     case PK_TUFTED: {  // penthouse.ts:495-501
@@ -72,11 +93,25 @@ __device__ __noinline__ uint32_t paint_eval(uint32_t kind, const double* __restr
       bool has = n == 0 || n == 1 || n == 3 || n == 4 || n == 5;
       return has && fabs(f - 0.5) < 0.3 ? vox_of(__ldg(p + 1), 0) : 0u;
     }
-    case PK_VASE: {  // penthouse.ts:810-816
-      double a = px_atan2(z - __ldg(p + 2), x - __ldg(p));
+    case PK_VASE: {  // penthouse.ts:810-816 (the motif only matters off the bands)
       double h = (y - __ldg(p + 1)) / __ldg(p + 3);
       bool band = (h > 0.04 && h < 0.06) || (h > 0.36 && h < 0.38) || (h > 0.47 && h < 0.49);
-      bool motif = h > 0.08 && h < 0.33 && sin_checked(a * 5 + sin_checked(h * 30, st) * 2, st) > 0.55;
+      bool motif = false;
+      if (!band && h > 0.08 && h < 0.33) {
+        const double yy = z - __ldg(p + 2), xx = x - __ldg(p);
+        double a = atan2(yy, xx);
+        double inner = sin(h * 30);
+        double arg = a * 5 + inner * 2;
+        double s = sin(arg);
+        // |arg - arg_ref| <= 5 |a - a_ref| + 2 |inner - inner_ref| + rounding; sin is 1-Lipschitz
+        double e = 5 * FAST_ULPS * ulp_of(a) + 2 * FAST_ULPS * ulp_of(1.0) + 8 * ulp_of(arg) + FAST_ULPS * ulp_of(1.0);
+        if (s - 0.55 > e) motif = true;
+        else if (0.55 - s > e) motif = false;
+        else {
+          double ac = atan2_cr(yy, xx);
+          motif = sin_cr(ac * 5 + sin_cr(h * 30, st) * 2, st) > 0.55;
+        }
+      }
       return vox_of(__ldg(p + 4), band || motif ? 255 : 0);
     }
     case PK_PAINTING: {  // penthouse.ts:840-845
@@ -85,7 +120,13 @@ __device__ __noinline__ uint32_t paint_eval(uint32_t kind, const double* __restr
         const double* b = p + 1 + 4 * i;
         if (px_hypot2(x - __ldg(b), (y - __ldg(b + 1)) * 1.3) < __ldg(b + 2)) shade = __ldg(b + 3);
       }
-      bool stripe = fabs(sin_checked(x * 9 + y * 3, st)) < 0.06;
+      double arg = x * 9 + y * 3;
+      double s = fabs(sin(arg));
+      double e = FAST_ULPS * ulp_of(1.0);
+      bool stripe;
+      if (s < 0.06 - e) stripe = true;
+      else if (s > 0.06 + e) stripe = false;
+      else stripe = fabs(sin_cr(arg, st)) < 0.06;
       return vox_of(__ldg(p), stripe ? 255 : shade);
     }
     case PK_NOISE: {  // synthetic scenes: integer hash + float32 sine
@@ -103,6 +144,38 @@ __device__ __noinline__ uint32_t paint_eval(uint32_t kind, const double* __restr
     }
   }
   return 0;
+}
+
+// The correctly rounded decisions of the same paints (validation mode compares).
+__device__ __noinline__ uint32_t paint_eval_cr(uint32_t kind, const double* __restrict__ p, double x, double y, double z,
+                                               uint32_t& st) {
+  const double PI = 3.141592653589793;
+  switch (kind) {
+    case PK_CHIP: {
+      double a = atan2_cr(z - __ldg(p + 2), x - __ldg(p));
+      bool edge = px_hypot2(x - __ldg(p), z - __ldg(p + 2)) > __ldg(p + 3);
+      bool stripe = fmod(floor(((a + PI) / (2 * PI)) * 8), 2.0) == 0;
+      double layer = fmod(floor((y - __ldg(p + 1)) / 0.0045), 2.0);
+      return vox_of(__ldg(p + 4), edge && stripe && layer == 0 ? 255 : 0);
+    }
+    case PK_VASE: {
+      double a = atan2_cr(z - __ldg(p + 2), x - __ldg(p));
+      double h = (y - __ldg(p + 1)) / __ldg(p + 3);
+      bool band = (h > 0.04 && h < 0.06) || (h > 0.36 && h < 0.38) || (h > 0.47 && h < 0.49);
+      bool motif = h > 0.08 && h < 0.33 && sin_cr(a * 5 + sin_cr(h * 30, st) * 2, st) > 0.55;
+      return vox_of(__ldg(p + 4), band || motif ? 255 : 0);
+    }
+    case PK_PAINTING: {
+      double shade = 0;
+      for (int i = 0; i < 9; i++) {
+        const double* b = p + 1 + 4 * i;
+        if (px_hypot2(x - __ldg(b), (y - __ldg(b + 1)) * 1.3) < __ldg(b + 2)) shade = __ldg(b + 3);
+      }
+      bool stripe = fabs(sin_cr(x * 9 + y * 3, st)) < 0.06;
+      return vox_of(__ldg(p), stripe ? 255 : shade);
+    }
+  }
+  return paint_eval(kind, p, x, y, z, st);
 }
 
 }  // namespace px

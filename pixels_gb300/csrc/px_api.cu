@@ -373,6 +373,7 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
   std::vector<OpDev> nops;
   std::vector<uint2> nboxes;
   std::vector<uint2> ncode;         // the new ops' instructions, one copy per op
+  std::vector<double> xparams;      // expanded polygon records (device float64 layout)
   std::vector<uint32_t> n32_code;   // their float32 parameter offsets
   std::vector<float2> nbases;
   std::vector<float2> n32_p;
@@ -407,7 +408,33 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
     d.code_off = (uint32_t)(code_base + ncode.size());
     for (uint32_t k = 0; k < o.code_len; k++) {
       const uint32_t* ins = code + 2 * ((size_t)o.code_begin + k);
-      ncode.push_back(make_uint2(ins[0], ins[1] + (uint32_t)param_base));
+      const uint32_t opc = ins[0] & 0xffu, cnt = ins[0] >> 8;
+      if (opc == OP_LATHE_SOLID || opc == OP_LATHE_SHELL || opc == OP_PRISM) {
+        // device polygon records with the per-edge constants (same float64 values
+        // as every reference call computes), appended after the IR's parameters
+        const double* pp = P.data() + ins[1];
+        const uint32_t off = (uint32_t)(param_base + n_params + xparams.size());
+        const int head = opc == OP_LATHE_SOLID ? 3 : 4;
+        for (int h = 0; h < head; h++) xparams.push_back(pp[h]);
+        const double* v = pp + head;
+        auto den_of = [](double ex, double ey) { double dd = ex * ex + ey * ey; return dd == 0.0 ? 1e-12 : dd; };
+        if (opc == OP_LATHE_SHELL) {
+          for (uint32_t q = 0; q + 1 < cnt; q++) {
+            double ax = v[2 * q], ay = v[2 * q + 1], ex = v[2 * q + 2] - ax, ey = v[2 * q + 3] - ay;
+            xparams.insert(xparams.end(), {ax, ay, ex, ey, den_of(ex, ey)});
+          }
+        } else {
+          for (uint32_t q = 0; q < cnt; q++) {
+            uint32_t j = q ? q - 1 : cnt - 1;
+            double vix = v[2 * q], viy = v[2 * q + 1], vjx = v[2 * j], vjy = v[2 * j + 1];
+            double ex = vjx - vix, ey = vjy - viy;
+            xparams.insert(xparams.end(), {vix, viy, vjy, ex, ey, den_of(ex, ey)});
+          }
+        }
+        ncode.push_back(make_uint2(ins[0], off));
+      } else {
+        ncode.push_back(make_uint2(ins[0], ins[1] + (uint32_t)param_base));
+      }
     }
     d.code_len = o.code_len;
     d.paint_off = (uint32_t)(param_base + o.paint_param);
@@ -487,6 +514,7 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
   w->p32.insert(w->p32.end(), n32_p.begin(), n32_p.end());
   w->bases.insert(w->bases.end(), nbases.begin(), nbases.end());
   w->params.insert(w->params.end(), P.begin(), P.end());
+  w->params.insert(w->params.end(), xparams.begin(), xparams.end());
   w->ops.insert(w->ops.end(), nops.begin(), nops.end());
   w->boxes.insert(w->boxes.end(), nboxes.begin(), nboxes.end());
   return PX_OK;

@@ -13,44 +13,37 @@ namespace px {
 __device__ __forceinline__ double len2d(double x, double y) { return sqrt(x * x + y * y); }
 __device__ __forceinline__ double len3d(double x, double y, double z) { return sqrt(x * x + y * y + z * z); }
 
-// shapes.ts:146-161
-__device__ __forceinline__ double sd_polygon64(double px_, double py_, const double* __restrict__ pts, int n) {
-  double d0x = px_ - __ldg(pts), d0y = py_ - __ldg(pts + 1);
+// shapes.ts:146-161.  The host expands the polygon into per-vertex records
+// (vix, viy, vjy, ex, ey, den) with ex = vjx - vix, ey = vjy - viy and
+// den = ex*ex + ey*ey || 1e-12 computed once in float64 exactly as every call
+// of the reference computes them, so the results are the same bits.
+__device__ __forceinline__ double sd_polygon64(double px_, double py_, const double* __restrict__ r, int n) {
+  double d0x = px_ - __ldg(r), d0y = py_ - __ldg(r + 1);
   double d = d0x * d0x + d0y * d0y;
   double s = 1.0;
-  double vjx = __ldg(pts + 2 * (n - 1)), vjy = __ldg(pts + 2 * (n - 1) + 1);
   for (int i = 0; i < n; i++) {
-    double vix = __ldg(pts + 2 * i), viy = __ldg(pts + 2 * i + 1);
-    double ex = vjx - vix, ey = vjy - viy;
+    const double* e = r + 6 * i;
+    double vix = __ldg(e), viy = __ldg(e + 1), vjy = __ldg(e + 2), ex = __ldg(e + 3), ey = __ldg(e + 4);
     double wx = px_ - vix, wy = py_ - viy;
-    double den = ex * ex + ey * ey;
-    if (den == 0.0) den = 1e-12;
-    double t = fmin(1.0, fmax(0.0, (wx * ex + wy * ey) / den));
+    double t = fmin(1.0, fmax(0.0, (wx * ex + wy * ey) / __ldg(e + 5)));
     double bx = wx - ex * t, by = wy - ey * t;
     d = fmin(d, bx * bx + by * by);
     bool c1 = py_ >= viy, c2 = py_ < vjy, c3 = ex * wy > ey * wx;
     if ((c1 && c2 && c3) || (!c1 && !c2 && !c3)) s = -s;
-    vjx = vix;
-    vjy = viy;
   }
   return s * sqrt(d);
 }
 
-// shapes.ts:164-173
-__device__ __forceinline__ double sd_polyline64(double px_, double py_, const double* __restrict__ pts, int n) {
+// shapes.ts:164-173, records per segment (ax, ay, ex, ey, den).
+__device__ __forceinline__ double sd_polyline64(double px_, double py_, const double* __restrict__ r, int nseg) {
   double d = INFINITY;
-  double ax = __ldg(pts), ay = __ldg(pts + 1);
-  for (int i = 1; i < n; i++) {
-    double bxp = __ldg(pts + 2 * i), byp = __ldg(pts + 2 * i + 1);
-    double ex = bxp - ax, ey = byp - ay;
-    double wx = px_ - ax, wy = py_ - ay;
-    double den = ex * ex + ey * ey;
-    if (den == 0.0) den = 1e-12;
-    double t = fmin(1.0, fmax(0.0, (wx * ex + wy * ey) / den));
+  for (int i = 0; i < nseg; i++) {
+    const double* e = r + 5 * i;
+    double ex = __ldg(e + 2), ey = __ldg(e + 3);
+    double wx = px_ - __ldg(e), wy = py_ - __ldg(e + 1);
+    double t = fmin(1.0, fmax(0.0, (wx * ex + wy * ey) / __ldg(e + 4)));
     double qx = wx - ex * t, qy = wy - ey * t;
     d = fmin(d, qx * qx + qy * qy);
-    ax = bxp;
-    ay = byp;
   }
   return sqrt(d);
 }
@@ -97,7 +90,7 @@ __device__ __forceinline__ double prim64(uint32_t op, int cnt, const double* __r
     case OP_LATHE_SOLID:  // shapes.ts:194-195
       return sd_polygon64(len2d(x - __ldg(p), z - __ldg(p + 2)), y - __ldg(p + 1), p + 3, cnt);
     case OP_LATHE_SHELL:  // shapes.ts:192
-      return sd_polyline64(len2d(x - __ldg(p), z - __ldg(p + 2)), y - __ldg(p + 1), p + 4, cnt) - __ldg(p + 3);
+      return sd_polyline64(len2d(x - __ldg(p), z - __ldg(p + 2)), y - __ldg(p + 1), p + 4, cnt - 1) - __ldg(p + 3);
     case OP_PRISM: {  // shapes.ts:214-218
       double d2 = sd_polygon64(x - __ldg(p), z - __ldg(p + 1), p + 4, cnt);
       double dy = fabs(y - __ldg(p + 2)) - __ldg(p + 3);
