@@ -194,7 +194,7 @@ def main():
         for _ in range(warmup):
             _lib.world_reset(h, True, s_ptr)
             _lib.build(h, mode, s_ptr)
-        ms, fold_ms = [], []
+        ms, fold_ms, cls_ms = [], [], []
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
         barrier()
         torch.cuda.synchronize()
@@ -205,20 +205,26 @@ def main():
             _lib.build_enqueue(h, mode, s_ptr)
             ev[i][1].record(stream)
             _lib.build_finish(h)
-            fold_ms.append(_lib.stats(h)["fold_ms"])
+            st_ = _lib.stats(h)
+            fold_ms.append(st_["fold_ms"])
+            cls_ms.append(st_["classify_ms"])
         torch.cuda.synchronize()
         barrier()
         ms = [a.elapsed_time(b) for a, b in ev]
+        timed_builds.cls = statistics.mean(cls_ms)
         return ms, fold_ms
 
     sampler = ClockSampler(local) if rank == 0 else None
     if sampler:
         sampler.start()
     ms64 = fold64 = ms_mx = fold_mx = None
+    cls64 = cls_mx = None
     if args.mode in ("both", "fp64"):
         ms64, fold64 = timed_builds(MODE_FP64, args.steps, args.warmup)
+        cls64 = timed_builds.cls
     if args.mode in ("both", "mixed"):
         ms_mx, fold_mx = timed_builds(MODE_MIXED, args.steps, args.warmup)
+        cls_mx = timed_builds.cls
     if ms_mx is None:
         ms_mx, fold_mx = ms64, fold64
     if ms64 is None:
@@ -307,7 +313,8 @@ def main():
                    "cells": cells, "ops": len(prog), "l2": "flushed between timed steps (256 MB write)",
                    "parallelism": f"replicas x{world}"},
         "fp64_form": {"value": round(value64, 4), "ms_per_step": round(t_64, 4),
-                      "fold_ms": round(fold64_s * 1e3, 4)},
+                      "fold_ms": round(fold64_s * 1e3, 4), "classify_ms": cls64},
+        "classify_ms": cls_mx,
         "speedup_mixed_vs_fp64": round(t_64 / t_mx, 3),
         "mismatches": {"grid_cells": mism_grid, "pool_voxels": mism_vox, "pool_used": int(used) - int(o.pool_used)},
         "rescued": {"total": st["rescued"], "brick": st["rescued_brick"], "sub": st["rescued_sub"],

@@ -58,12 +58,14 @@ typedef struct px_stats {
   uint32_t status;           /* device status bits of the last build */
   double max_abs_err32;      /* max |d32 - d64| seen by rescued evaluations (mixed mode) */
   float build_ms;            /* device time of the last build */
-  float fold_ms;             /* device time of its fold kernel */
+  float fold_ms;             /* device time of its classify + apply kernels */
   uint32_t kernel_launches;  /* kernels the last build launched */
   uint32_t pad;
   uint64_t violations;       /* validation mode: float64 results outside their float32 enclosure */
   uint64_t rescued_brick, rescued_sub, rescued_voxel;  /* rescues by level (mixed mode) */
   uint64_t rescued_polygon;  /* ... of which a polygon crossing test was undecided */
+  float classify_ms;         /* device time of the classify kernel alone */
+  float pad2;
 } px_stats;
 
 /* Device addresses of the world's buffers (valid until the next build or destroy). */
@@ -120,6 +122,37 @@ int px_set_validation(px_world* w, int on);
 
 int px_get_stats(px_world* w, px_stats* out);
 int px_device_view_get(px_world* w, px_device_view* out);
+/* Dims (voxels) and voxel density of a world. */
+int px_world_info(px_world* w, int dims[3], double* vpm);
+
+/* ---- serving: subtract-edits on a resident world (continuous batching) ----
+   The game's carve as the rasteriser sees it: Builder.carve of a sphere
+   (shapes.ts:65-72) or capsule (shapes.ts:114-128), appended to the world's
+   op history (shapes.ts:423-426). */
+#define PX_EDIT_SPHERE 0
+#define PX_EDIT_CAPSULE 1
+typedef struct px_edit {
+  uint32_t shape;      /* PX_EDIT_SPHERE (centre a) or PX_EDIT_CAPSULE (segment a-b) */
+  uint32_t pad;
+  double a[3], b[3];
+  double r;            /* radius in metres (capsules clamp to 0.9 voxel, shapes.ts:115) */
+} px_edit;
+typedef struct px_edit_result {
+  uint64_t id;         /* index into the edits array */
+  uint32_t status;     /* PX_OK, or PX_E_OOM when the edit cannot fit the pool budget */
+  uint32_t batch;      /* build step that applied it */
+  double arrival_s, start_s, done_s;  /* seconds since the run started */
+} px_edit_result;
+/* Serve `n` edits arriving at arrival_s[i] (seconds from now): a producer
+   releases them in real time; each build step takes every released edit, in
+   arrival order, up to max_batch, whose worst-case pool growth (bricks in its
+   box) fits pool_budget_bricks minus the live bricks, and builds them together
+   on the resident world.  applied_order (n entries, may be NULL) receives the
+   edit indices in the order applied.  Blocks until every edit is applied or
+   rejected. */
+int px_serve_run(px_world* w, const px_edit* edits, const double* arrival_s, size_t n, uint32_t max_batch,
+                 uint64_t pool_budget_bricks, int mode, void* stream, px_edit_result* results,
+                 uint64_t* applied_order, size_t* n_applied);
 const char* px_last_error(px_world* w);
 
 /* Measurement utility (no counterpart in the reference): dependent-FMA

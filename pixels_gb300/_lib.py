@@ -23,7 +23,7 @@ EXPORTS = [
     "px_world_create", "px_world_destroy", "px_world_reset", "px_submit_ops", "px_build", "px_build_enqueue",
     "px_build_finish", "px_read_grid", "px_read_pool", "px_read_holes", "px_derive", "px_read_super",
     "px_read_density", "px_read_free_list", "px_set_material_tables", "px_set_validation", "px_get_stats",
-    "px_device_view_get", "px_last_error", "px_probe_peak",
+    "px_device_view_get", "px_last_error", "px_probe_peak", "px_world_info", "px_serve_run",
 ]
 
 
@@ -31,6 +31,16 @@ class PxError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"{ERRORS.get(code, code)}: {msg}")
         self.code = code
+
+
+class Edit(ctypes.Structure):
+    _fields_ = [("shape", ctypes.c_uint32), ("pad", ctypes.c_uint32), ("a", ctypes.c_double * 3),
+                ("b", ctypes.c_double * 3), ("r", ctypes.c_double)]
+
+
+class EditResult(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_uint64), ("status", ctypes.c_uint32), ("batch", ctypes.c_uint32),
+                ("arrival_s", ctypes.c_double), ("start_s", ctypes.c_double), ("done_s", ctypes.c_double)]
 
 
 class Stats(ctypes.Structure):
@@ -43,6 +53,7 @@ class Stats(ctypes.Structure):
         ("fold_ms", ctypes.c_float), ("kernel_launches", ctypes.c_uint32), ("pad", ctypes.c_uint32),
         ("violations", ctypes.c_uint64), ("rescued_brick", ctypes.c_uint64), ("rescued_sub", ctypes.c_uint64),
         ("rescued_voxel", ctypes.c_uint64), ("rescued_polygon", ctypes.c_uint64),
+        ("classify_ms", ctypes.c_float), ("pad2", ctypes.c_float),
     ]
 
 
@@ -77,6 +88,10 @@ def load(path: str = LIB_PATH):
     L.px_last_error.argtypes = [vp]
     L.px_last_error.restype = ctypes.c_char_p
     L.px_probe_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
+    L.px_world_info.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
+    L.px_serve_run.argtypes = [vp, ctypes.POINTER(Edit), ctypes.POINTER(ctypes.c_double), sz, u32, ctypes.c_uint64,
+                               ctypes.c_int, vp, ctypes.POINTER(EditResult), ctypes.POINTER(ctypes.c_uint64),
+                               ctypes.POINTER(sz)]
     _L = L
     return L
 
@@ -171,3 +186,27 @@ def probe_peak(fp64: bool) -> float:
     v = ctypes.c_float()
     _check(None, load().px_probe_peak(int(fp64), ctypes.byref(v)))
     return float(v.value)
+
+
+def serve_run(h, edits, arrivals, max_batch: int, pool_budget: int, mode: int, stream: int = 0):
+    """Run the continuous-batching edit server; returns (results array, applied order).
+
+    ``edits``: sequence of (shape, a, b, r) with shape 0 sphere / 1 capsule.
+    """
+    n = len(edits)
+    arr = (Edit * max(n, 1))()
+    for i, (shape, a, b, r) in enumerate(edits):
+        arr[i].shape = int(shape)
+        arr[i].a[:] = [float(v) for v in a]
+        arr[i].b[:] = [float(v) for v in b]
+        arr[i].r = float(r)
+    t = (ctypes.c_double * max(n, 1))(*[float(v) for v in arrivals])
+    res = (EditResult * max(n, 1))()
+    order = (ctypes.c_uint64 * max(n, 1))()
+    n_app = ctypes.c_size_t()
+    _check(h, load().px_serve_run(h, arr, t, n, max_batch, pool_budget, mode, ctypes.c_void_p(stream), res, order,
+                                  ctypes.byref(n_app)))
+    out = np.array([(r.id, r.status, r.batch, r.arrival_s, r.start_s, r.done_s) for r in res[:n]],
+                   dtype=[("id", "u8"), ("status", "u4"), ("batch", "u4"), ("arrival_s", "f8"), ("start_s", "f8"),
+                          ("done_s", "f8")])
+    return out, np.array(order[:n_app.value], dtype=np.int64)

@@ -197,10 +197,9 @@ __device__ __forceinline__ void brick_bases(const FoldArgs& a, const OpDev* O, i
 
 // Classification of every (op, brick) pair — apply()'s SDF tests, which do not
 // depend on the world's state (shapes.ts:358-366, 382-394):
-//   phase 0, bricks: one pair per lane (32 consecutive pairs, mostly one op);
-//   phase 1, sub-blocks: 4 partial pairs x 8 sub-blocks per pass;
-//   phase 2, voxels: one partial sub-block per two passes, 32 voxels per pass.
-// All phases share one evaluation call site (one copy of the evaluators).
+//   brick level: one pair per lane (32 consecutive pairs, mostly one op);
+//   sub-block level: 4 partial pairs x 8 sub-blocks per pass;
+//   voxel level: one partial sub-block per pass, 64 voxels on 32 lanes.
 template <int MODE>
 __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIFY64_MINB) classify_kernel(FoldArgs a) {
   const int lane = threadIdx.x & 31;
@@ -218,116 +217,80 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
     uint32_t o = __ldg(a.chunk_op + chunk);
     if (valid)
       while (o + 1 < a.n_ops && a.ops[o + 1].pair_base <= p) o++;
-    int bx = 0, by = 0, bz = 0;
-    bool contained = false;
+    const OpDev* O = a.ops + o;
+    int bx = 0, by = 0, bz = 0, cls = PC_SKIP;
     if (valid) {
-      const OpDev* O = a.ops + o;
       brick_of_pair(O, p, bx, by, bz);
-      contained = (O->flags & OPF_CONTAINS) && bx >= O->cbx0 && bx <= O->cbx1 && by >= O->cby0 && by <= O->cby1 &&
-                  bz >= O->cbz0 && bz <= O->cbz1;
-    }
-    // sub pass state (per lane: the pair of its 8-lane group)
-    uint32_t part = 0, vm = 0, bal0 = 0;
-    unsigned long long gp = 0;   // pair of this lane's group
-    uint32_t go = 0;
-    int gbx = 0, gby = 0, gbz = 0, gsl = -1;
-    int cur_l = 0, vr = 0;
-    int phase = 0;
-    for (;;) {
-      // --- this lane's item ---
-      bool active;
-      uint32_t qo;
-      int qbx, qby, qbz, what;
-      float kx, ky, kz, tx, ty, tz;
-      if (phase == 0) {
-        active = valid && !contained;
-        qo = o; qbx = bx; qby = by; qbz = bz; what = 1;
-        kx = ky = kz = 3.5f;
-        tx = (float)(bx * 8 + 4); ty = (float)(by * 8 + 4); tz = (float)(bz * 8 + 4);
-      } else if (phase == 1) {
-        const int s = lane & 7, sxb = s & 1, syb = (s >> 1) & 1, szb = (s >> 2) & 1;
-        active = gsl >= 0;
-        qo = go; qbx = gbx; qby = gby; qbz = gbz; what = 2;
-        kx = 4.f * sxb + 1.5f; ky = 4.f * syb + 1.5f; kz = 4.f * szb + 1.5f;
-        tx = (float)(gbx * 8 + sxb * 4 + 2); ty = (float)(gby * 8 + syb * 4 + 2); tz = (float)(gbz * 8 + szb * 4 + 2);
+      const int flags = O->flags;
+      const bool contained = (flags & OPF_CONTAINS) && bx >= O->cbx0 && bx <= O->cbx1 && by >= O->cby0 &&
+                             by <= O->cby1 && bz >= O->cbz0 && bz <= O->cbz1;
+      if (contained) {
+        cls = PC_FULL;
       } else {
-        const int ss = cur_l & 7;
-        qo = __shfl_sync(FULLMASK, go, cur_l);
-        qbx = __shfl_sync(FULLMASK, gbx, cur_l); qby = __shfl_sync(FULLMASK, gby, cur_l);
-        qbz = __shfl_sync(FULLMASK, gbz, cur_l);
-        const int e = vr * 32 + lane;
-        const int lx = (ss & 1) * 4 + (e & 3), lyv = ((ss >> 1) & 1) * 4 + ((e >> 2) & 3), lz = ((ss >> 2) & 1) * 4 + (e >> 4);
-        active = true; what = 0;
-        kx = (float)lx; ky = (float)lyv; kz = (float)lz;
-        tx = (float)(qbx * 8 + lx) + 0.5f; ty = (float)(qby * 8 + lyv) + 0.5f; tz = (float)(qbz * 8 + lz) + 0.5f;
+        const bool use32 = MODE == 1 && !(flags & OPF_FP64_ONLY);
+        Iv bo[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+        if (use32) brick_bases(a, O, bx, by, bz, bo);
+        cls = eval_decide<MODE>(a, O, a.code + O->code_off, (int)O->code_len, use32, bo, 3.5f, 3.5f, 3.5f,
+                                (float)(bx * 8 + 4), (float)(by * 8 + 4), (float)(bz * 8 + 4), 1, ls);
+        n_brick++;
       }
-      int r = 0;
-      if (active) {
-        const OpDev* Q = a.ops + qo;
+      a.pcode[p] = (uint8_t)cls;
+    }
+    uint32_t part = __ballot_sync(FULLMASK, valid && cls == PC_PARTIAL);
+    while (part) {
+      int src0 = -1, src1 = -1, src2 = -1, src3 = -1;
+      if (part) { src0 = __ffs(part) - 1; part &= part - 1; }
+      if (part) { src1 = __ffs(part) - 1; part &= part - 1; }
+      if (part) { src2 = __ffs(part) - 1; part &= part - 1; }
+      if (part) { src3 = __ffs(part) - 1; part &= part - 1; }
+      const int k = lane >> 3, s = lane & 7;
+      const int sl = k == 0 ? src0 : k == 1 ? src1 : k == 2 ? src2 : src3;
+      const int sll = sl < 0 ? 0 : sl;
+      const unsigned long long pp = __shfl_sync(FULLMASK, p, sll);
+      const uint32_t oo = __shfl_sync(FULLMASK, o, sll);
+      const int pbx = __shfl_sync(FULLMASK, bx, sll), pby = __shfl_sync(FULLMASK, by, sll),
+                pbz = __shfl_sync(FULLMASK, bz, sll);
+      int scls = PC_SKIP;
+      if (sl >= 0) {
+        const OpDev* Q = a.ops + oo;
         const bool use32 = MODE == 1 && !(Q->flags & OPF_FP64_ONLY);
         Iv bo[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-        if (use32) brick_bases(a, Q, qbx, qby, qbz, bo);
-        r = eval_decide<MODE>(a, Q, a.code + Q->code_off, (int)Q->code_len, use32, bo, kx, ky, kz, tx, ty, tz, what, ls);
+        if (use32) brick_bases(a, Q, pbx, pby, pbz, bo);
+        const int sxb = s & 1, syb = (s >> 1) & 1, szb = (s >> 2) & 1;
+        scls = eval_decide<MODE>(a, Q, a.code + Q->code_off, (int)Q->code_len, use32, bo, 4.f * sxb + 1.5f,
+                                 4.f * syb + 1.5f, 4.f * szb + 1.5f, (float)(pbx * 8 + sxb * 4 + 2),
+                                 (float)(pby * 8 + syb * 4 + 2), (float)(pbz * 8 + szb * 4 + 2), 2, ls);
       }
-      // --- consume ---
-      bool next_subs = false;
-      if (phase == 0) {
-        const int cls = contained ? PC_FULL : r;
-        if (valid) {
-          a.pcode[p] = (uint8_t)cls;
-          n_brick += contained ? 0 : 1;
+      uint32_t code16 = (uint32_t)scls << (2 * s);
+      code16 |= __shfl_xor_sync(FULLMASK, code16, 1);
+      code16 |= __shfl_xor_sync(FULLMASK, code16, 2);
+      code16 |= __shfl_xor_sync(FULLMASK, code16, 4);
+      if (s == 0 && sl >= 0) a.psub[pp] = (uint16_t)code16;
+      uint32_t vm = __ballot_sync(FULLMASK, sl >= 0 && scls == PC_PARTIAL);
+      while (vm) {
+        const int l = __ffs(vm) - 1;
+        vm &= vm - 1;
+        const int ss = l & 7;
+        const unsigned long long vp = __shfl_sync(FULLMASK, pp, l);
+        const uint32_t vo = __shfl_sync(FULLMASK, oo, l);
+        const int vbx = __shfl_sync(FULLMASK, pbx, l), vby = __shfl_sync(FULLMASK, pby, l),
+                  vbz = __shfl_sync(FULLMASK, pbz, l);
+        const OpDev* V = a.ops + vo;
+        const bool use32 = MODE == 1 && !(V->flags & OPF_FP64_ONLY);
+        Iv bo[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+        if (use32) brick_bases(a, V, vbx, vby, vbz, bo);
+        const int sxo = (ss & 1) * 4, syo = ((ss >> 1) & 1) * 4, szo = ((ss >> 2) & 1) * 4;
+        uint32_t bal[2];
+#pragma unroll
+        for (int r = 0; r < 2; r++) {
+          const int e = r * 32 + lane;
+          const int lx = sxo + (e & 3), lyv = syo + ((e >> 2) & 3), lz = szo + (e >> 4);
+          int inside = eval_decide<MODE>(a, V, a.code + V->code_off, (int)V->code_len, use32, bo, (float)lx,
+                                         (float)lyv, (float)lz, (float)(vbx * 8 + lx) + 0.5f,
+                                         (float)(vby * 8 + lyv) + 0.5f, (float)(vbz * 8 + lz) + 0.5f, 0, ls);
+          bal[r] = __ballot_sync(FULLMASK, inside == 1);
         }
-        part = __ballot_sync(FULLMASK, valid && cls == PC_PARTIAL);
-        next_subs = true;
-      } else if (phase == 1) {
-        uint32_t code16 = (uint32_t)r << (2 * (lane & 7));
-        code16 |= __shfl_xor_sync(FULLMASK, code16, 1);
-        code16 |= __shfl_xor_sync(FULLMASK, code16, 2);
-        code16 |= __shfl_xor_sync(FULLMASK, code16, 4);
-        if ((lane & 7) == 0 && gsl >= 0) a.psub[gp] = (uint16_t)code16;
-        vm = __ballot_sync(FULLMASK, active && r == PC_PARTIAL);
-        if (vm) {
-          cur_l = __ffs(vm) - 1;
-          vm &= vm - 1;
-          vr = 0;
-          phase = 2;
-        } else {
-          next_subs = true;
-        }
-      } else {
-        const uint32_t bal = __ballot_sync(FULLMASK, r == 1);
-        if (vr == 0) {
-          bal0 = bal;
-          vr = 1;
-        } else {
-          const unsigned long long vp = __shfl_sync(FULLMASK, gp, cur_l);
-          if (lane == 0) a.pmask[vp * 8 + (cur_l & 7)] = (unsigned long long)bal0 | ((unsigned long long)bal << 32);
-          if (vm) {
-            cur_l = __ffs(vm) - 1;
-            vm &= vm - 1;
-            vr = 0;
-          } else {
-            next_subs = true;
-          }
-        }
-      }
-      if (next_subs) {
-        if (!part) break;
-        // next sub pass: up to 4 partial pairs, 8 lanes each
-        int src0 = -1, src1 = -1, src2 = -1, src3 = -1;
-        if (part) { src0 = __ffs(part) - 1; part &= part - 1; }
-        if (part) { src1 = __ffs(part) - 1; part &= part - 1; }
-        if (part) { src2 = __ffs(part) - 1; part &= part - 1; }
-        if (part) { src3 = __ffs(part) - 1; part &= part - 1; }
-        const int k = lane >> 3;
-        gsl = k == 0 ? src0 : k == 1 ? src1 : k == 2 ? src2 : src3;
-        const int sll = gsl < 0 ? 0 : gsl;
-        gp = __shfl_sync(FULLMASK, p, sll);
-        go = __shfl_sync(FULLMASK, o, sll);
-        gbx = __shfl_sync(FULLMASK, bx, sll);
-        gby = __shfl_sync(FULLMASK, by, sll);
-        gbz = __shfl_sync(FULLMASK, bz, sll);
-        phase = 1;
+        if (lane == 0) a.pmask[vp * 8 + ss] = (unsigned long long)bal[0] | ((unsigned long long)bal[1] << 32);
       }
     }
   }
@@ -567,12 +530,13 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
   }
 }
 
-void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s) {
+void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEvent_t mid) {
   if (mode == 1) {
     ++g_launches; classify_kernel<1><<<n_sms * PX_CLASSIFY_MINB, 256, 0, s>>>(a);
   } else {
     ++g_launches; classify_kernel<0><<<n_sms * PX_CLASSIFY64_MINB, 256, 0, s>>>(a);
   }
+  if (mid) cudaEventRecord(mid, s);
   ++g_launches; fold_kernel<<<n_sms * PX_FOLD_MINB, 256, 0, s>>>(a);
 }
 

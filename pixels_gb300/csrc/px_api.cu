@@ -70,7 +70,7 @@ struct px_world {
   // in-flight build
   bool in_flight = false;
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_fold0 = nullptr, ev_fold1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_fold0 = nullptr, ev_fold1 = nullptr, ev_mid = nullptr;
   size_t last_P = 0;
   uint32_t last_stage_cap = 0;
   uint32_t last_H = 0, last_U0 = 0;
@@ -313,6 +313,7 @@ int px_world_create(int dx, int dy, int dz, double vpm, uint32_t initial_pool_br
   cudaEventCreate(&w->ev1);
   cudaEventCreate(&w->ev_fold0);
   cudaEventCreate(&w->ev_fold1);
+  cudaEventCreate(&w->ev_mid);
   // material tables (VoxelWorld.ts:159-170,190-196): filled by px_set_tables or the defaults
   uint8_t op_tab[256], ud_tab[256];
   for (int i = 0; i < 256; i++) { op_tab[i] = i ? 1 : 0; ud_tab[i] = 255; }
@@ -351,6 +352,7 @@ void px_world_destroy(px_world* w) {
   if (w->ev1) cudaEventDestroy(w->ev1);
   if (w->ev_fold0) cudaEventDestroy(w->ev_fold0);
   if (w->ev_fold1) cudaEventDestroy(w->ev_fold1);
+  if (w->ev_mid) cudaEventDestroy(w->ev_mid);
   delete w;
 }
 
@@ -669,7 +671,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   fa.work_counter = (uint32_t*)w->work_counter.p;
   fa.res = res;
   CU(cudaEventRecord(w->ev_fold0, s));
-  launch_fold(fa, mode, w->n_sms, s);
+  launch_fold(fa, mode, w->n_sms, s, w->ev_mid);
   CU(cudaEventRecord(w->ev_fold1, s));
 
   ReplayArgs ra{};
@@ -726,6 +728,9 @@ int px_build_finish(px_world* w) {
   cudaEventElapsedTime(&ms, w->ev0, w->ev1);
   cudaEventElapsedTime(&fold_ms, w->ev_fold0, w->ev_fold1);
   w->stats.fold_ms = fold_ms;
+  float cls_ms = 0.f;
+  cudaEventElapsedTime(&cls_ms, w->ev_fold0, w->ev_mid);
+  w->stats.classify_ms = cls_ms;
   w->stats.pairs = w->last_P;
   w->stats.brick_evals = r.c.brick_evals;
   w->stats.sub_evals = r.c.sub_evals;
@@ -876,6 +881,13 @@ int px_get_stats(px_world* w, px_stats* out) {
   out->n_holes = w->n_holes;
   out->pool_capacity = w->pool_cap;
   out->ops_applied = w->ops_applied;
+  return PX_OK;
+}
+
+int px_world_info(px_world* w, int dims[3], double* vpm) {
+  if (!w) return PX_E_INVALID_ARG;
+  if (dims) { dims[0] = w->dx; dims[1] = w->dy; dims[2] = w->dz; }
+  if (vpm) *vpm = w->vpm;
   return PX_OK;
 }
 

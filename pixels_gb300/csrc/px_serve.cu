@@ -1,0 +1,208 @@
+// Serving: continuous batching of subtract-edits on a resident world.
+//
+// The game's carve is a Carve op of a sphere or capsule (shapes.ts:65-72,
+// 114-128, 423-426).  A producer thread releases requests at their arrival
+// times; the serving loop takes every released request (in arrival order, up
+// to max_batch) whose worst-case pool growth fits the free pool, builds them in
+// one incremental build on the resident world (the same kernels as a scene
+// build, starting from the world's current grid, pool and free list), and
+// stamps their completion.  Requests that arrive while a batch is on the GPU
+// join the next batch.  The world after any sequence of batches equals the
+// reference applying the same carves one after another in admission order.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "../../include/pixels_gb300.h"
+#include "px_internal.cuh"
+
+using namespace px;
+
+namespace {
+
+using clock_t_ = std::chrono::steady_clock;
+
+double secs(clock_t_::time_point t0, clock_t_::time_point t) { return std::chrono::duration<double>(t - t0).count(); }
+
+// PXIR encoding of one carve (the constructors of shapes.ts, float64 as in JS)
+void encode_carve(const px_edit& e, double vs, std::vector<IrOp>& ops, std::vector<uint32_t>& code,
+                  std::vector<double>& params) {
+  IrOp o;
+  std::memset(&o, 0, sizeof o);
+  o.kind = KIND_CARVE;
+  o.flags = 0;
+  o.paint_kind = PK_CONST;
+  o.paint_value = 0;
+  o.code_begin = (uint32_t)(code.size() / 2);
+  o.code_len = 1;
+  o.slack = 1.0;
+  o.frame[2] = 1.0;
+  const uint32_t off = (uint32_t)params.size();
+  if (e.shape == PX_EDIT_SPHERE) {  // shapes.ts:65-72
+    const double cx = e.a[0], cy = e.a[1], cz = e.a[2], r = e.r;
+    params.insert(params.end(), {cx, cy, cz, r});
+    code.push_back(OP_SPHERE);
+    code.push_back(off);
+    o.mn[0] = cx - r; o.mn[1] = cy - r; o.mn[2] = cz - r;
+    o.mx[0] = cx + r; o.mx[1] = cy + r; o.mx[2] = cz + r;
+  } else {  // shapes.ts:114-128
+    const double min_line_r = 0.9 * vs;
+    const double r = e.r > min_line_r ? e.r : min_line_r;
+    const double ax = e.a[0], ay = e.a[1], az = e.a[2];
+    const double bax = e.b[0] - ax, bay = e.b[1] - ay, baz = e.b[2] - az;
+    double bb = bax * bax + bay * bay + baz * baz;
+    if (bb == 0 || bb != bb) bb = 1e-12;
+    params.insert(params.end(), {ax, ay, az, bax, bay, baz, bb, r});
+    code.push_back(OP_CAPSULE);
+    code.push_back(off);
+    const double* b = e.b;
+    o.mn[0] = std::min(ax, b[0]) - r; o.mn[1] = std::min(ay, b[1]) - r; o.mn[2] = std::min(az, b[2]) - r;
+    o.mx[0] = std::max(ax, b[0]) + r; o.mx[1] = std::max(ay, b[1]) + r; o.mx[2] = std::max(az, b[2]) + r;
+  }
+  ops.push_back(o);
+}
+
+// Bricks an edit can touch (the brick box of apply(), shapes.ts:341-347): the
+// most pool bricks it can add.
+uint64_t brick_bound(const px_edit& e, double vs, int dx, int dy, int dz) {
+  double lo[3], hi[3];
+  double r = e.r;
+  if (e.shape == PX_EDIT_SPHERE) {
+    for (int k = 0; k < 3; k++) { lo[k] = e.a[k] - r; hi[k] = e.a[k] + r; }
+  } else {
+    r = std::max(r, 0.9 * vs);
+    for (int k = 0; k < 3; k++) { lo[k] = std::min(e.a[k], e.b[k]) - r; hi[k] = std::max(e.a[k], e.b[k]) + r; }
+  }
+  const int dims[3] = {dx, dy, dz};
+  uint64_t n = 1;
+  for (int k = 0; k < 3; k++) {
+    double v0 = std::max(0.0, std::floor(lo[k] / vs - 0.5)), v1 = std::min((double)dims[k] - 1, std::ceil(hi[k] / vs + 0.5));
+    if (v0 > v1) return 0;
+    n *= (uint64_t)(((int)v1 >> 3) - ((int)v0 >> 3) + 1);
+  }
+  return n;
+}
+
+}  // namespace
+
+extern "C" {
+
+int px_serve_run(px_world* w, const px_edit* edits, const double* arrival_s, size_t n, uint32_t max_batch,
+                 uint64_t pool_budget_bricks, int mode, void* stream, px_edit_result* results, uint64_t* applied_order,
+                 size_t* n_applied) {
+  if (!w || (!edits && n) || (!arrival_s && n) || (!results && n) || max_batch == 0) return PX_E_INVALID_ARG;
+  int dims[3];
+  double vpm;
+  px_world_info(w, dims, &vpm);
+  const double vs = 1 / vpm;
+  px_stats st;
+  px_get_stats(w, &st);
+  uint64_t live = (uint64_t)st.pool_used - st.n_holes;
+
+  // arrival order
+  std::vector<size_t> order(n);
+  for (size_t i = 0; i < n; i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return arrival_s[x] < arrival_s[y]; });
+  for (size_t i = 0; i < n; i++) {
+    results[i].id = i;
+    results[i].status = PX_OK;
+    results[i].batch = 0;
+    results[i].arrival_s = arrival_s[i];
+    results[i].start_s = results[i].done_s = -1;
+  }
+
+  // producer: releases requests at their arrival times
+  std::mutex mu;
+  std::condition_variable cv;
+  size_t released = 0;
+  bool stop = false;
+  const auto t0 = clock_t_::now();
+  std::thread producer([&] {
+    for (size_t k = 0; k < n; k++) {
+      const double t = arrival_s[order[k]];
+      std::this_thread::sleep_until(t0 + std::chrono::duration_cast<clock_t_::duration>(std::chrono::duration<double>(t)));
+      {
+        std::lock_guard<std::mutex> g(mu);
+        released = k + 1;
+        if (stop) return;
+      }
+      cv.notify_one();
+    }
+  });
+
+  size_t next = 0, applied = 0;
+  uint32_t batch_id = 0;
+  int rc = PX_OK;
+  std::vector<IrOp> ops;
+  std::vector<uint32_t> code;
+  std::vector<double> params;
+  std::vector<size_t> batch;
+  while (next < n && rc == PX_OK) {
+    size_t avail;
+    {
+      std::unique_lock<std::mutex> g(mu);
+      cv.wait(g, [&] { return released > next; });
+      avail = released;
+    }
+    // admit in arrival order while the free pool holds the worst case
+    batch.clear();
+    ops.clear();
+    code.clear();
+    params.clear();
+    uint64_t bound = 0;
+    while (next < avail && batch.size() < max_batch) {
+      const size_t i = order[next];
+      const uint64_t b = brick_bound(edits[i], vs, dims[0], dims[1], dims[2]);
+      if (live + bound + b > pool_budget_bricks) {
+        if (batch.empty()) {  // cannot fit even alone: reject
+          results[i].status = PX_E_OOM;
+          results[i].done_s = secs(t0, clock_t_::now());
+          next++;
+          continue;
+        }
+        break;  // wait for the next batch
+      }
+      bound += b;
+      batch.push_back(i);
+      encode_carve(edits[i], vs, ops, code, params);
+      next++;
+    }
+    if (batch.empty()) continue;
+    const double start = secs(t0, clock_t_::now());
+    // PXIR buffer
+    std::vector<unsigned char> ir(32 + ops.size() * sizeof(IrOp) + code.size() * 4 + params.size() * 8);
+    uint32_t hdr[8] = {0x52495850u, 1u, (uint32_t)ops.size(), (uint32_t)(code.size() / 2), (uint32_t)params.size(), 0, 0, 0};
+    std::memcpy(ir.data(), hdr, 32);
+    std::memcpy(ir.data() + 32, ops.data(), ops.size() * sizeof(IrOp));
+    std::memcpy(ir.data() + 32 + ops.size() * sizeof(IrOp), code.data(), code.size() * 4);
+    std::memcpy(ir.data() + 32 + ops.size() * sizeof(IrOp) + code.size() * 4, params.data(), params.size() * 8);
+    rc = px_submit_ops(w, ir.data(), ir.size());
+    if (rc == PX_OK) rc = px_build(w, mode, stream);
+    const double done = secs(t0, clock_t_::now());
+    px_get_stats(w, &st);
+    live = (uint64_t)st.pool_used - st.n_holes;
+    for (size_t i : batch) {
+      results[i].start_s = start;
+      results[i].done_s = done;
+      results[i].batch = batch_id;
+      results[i].status = (uint32_t)rc;
+      if (applied_order && rc == PX_OK) applied_order[applied] = i;
+      if (rc == PX_OK) applied++;
+    }
+    batch_id++;
+  }
+  {
+    std::lock_guard<std::mutex> g(mu);
+    stop = true;
+  }
+  producer.join();
+  if (n_applied) *n_applied = applied;
+  return rc;
+}
+
+}  // extern "C"
