@@ -197,14 +197,16 @@ __device__ __forceinline__ void brick_bases(const FoldArgs& a, const OpDev* O, i
 
 // Classification of every (op, brick) pair — apply()'s SDF tests, which do not
 // depend on the world's state (shapes.ts:358-366, 382-394):
-//   brick level: one pair per lane (32 consecutive pairs, mostly one op);
-//   sub-block level: 4 partial pairs x 8 sub-blocks per pass;
-//   voxel level: one partial sub-block per pass, 64 voxels on 32 lanes.
+//   bricks: one pair per lane (32 consecutive pairs, mostly one op);
+//   sub-blocks: 4 partial pairs x 8 sub-blocks per pass;
+// partial sub-blocks go to a queue that voxel_kernel drains one at a time
+// (64 voxels on 32 lanes), which keeps the heavy voxel work evenly spread.
 template <int MODE>
 __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIFY64_MINB) classify_kernel(FoldArgs a) {
   const int lane = threadIdx.x & 31;
   LaneStats ls = {0, 0, 0, 0.f, 0, 0, 0, 0};
   uint32_t n_brick = 0;
+  uint32_t st_local = 0;
   const unsigned long long P = a.n_pairs;
   const uint32_t n_chunks = (uint32_t)((P + 31) / 32);
   for (;;) {
@@ -266,35 +268,20 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
       code16 |= __shfl_xor_sync(FULLMASK, code16, 2);
       code16 |= __shfl_xor_sync(FULLMASK, code16, 4);
       if (s == 0 && sl >= 0) a.psub[pp] = (uint16_t)code16;
-      uint32_t vm = __ballot_sync(FULLMASK, sl >= 0 && scls == PC_PARTIAL);
-      while (vm) {
-        const int l = __ffs(vm) - 1;
-        vm &= vm - 1;
-        const int ss = l & 7;
-        const unsigned long long vp = __shfl_sync(FULLMASK, pp, l);
-        const uint32_t vo = __shfl_sync(FULLMASK, oo, l);
-        const int vbx = __shfl_sync(FULLMASK, pbx, l), vby = __shfl_sync(FULLMASK, pby, l),
-                  vbz = __shfl_sync(FULLMASK, pbz, l);
-        const OpDev* V = a.ops + vo;
-        const bool use32 = MODE == 1 && !(V->flags & OPF_FP64_ONLY);
-        Iv bo[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-        if (use32) brick_bases(a, V, vbx, vby, vbz, bo);
-        const int sxo = (ss & 1) * 4, syo = ((ss >> 1) & 1) * 4, szo = ((ss >> 2) & 1) * 4;
-        uint32_t bal[2];
-#pragma unroll
-        for (int r = 0; r < 2; r++) {
-          const int e = r * 32 + lane;
-          const int lx = sxo + (e & 3), lyv = syo + ((e >> 2) & 3), lz = szo + (e >> 4);
-          int inside = eval_decide<MODE>(a, V, a.code + V->code_off, (int)V->code_len, use32, bo, (float)lx,
-                                         (float)lyv, (float)lz, (float)(vbx * 8 + lx) + 0.5f,
-                                         (float)(vby * 8 + lyv) + 0.5f, (float)(vbz * 8 + lz) + 0.5f, 0, ls);
-          bal[r] = __ballot_sync(FULLMASK, inside == 1);
-        }
-        if (lane == 0) a.pmask[vp * 8 + ss] = (unsigned long long)bal[0] | ((unsigned long long)bal[1] << 32);
+      // queue the partial sub-blocks (one warp-aggregated append)
+      const bool push = sl >= 0 && scls == PC_PARTIAL;
+      const uint32_t vm = __ballot_sync(FULLMASK, push);
+      uint32_t base = 0;
+      if (lane == 0 && vm) base = atomicAdd(&a.vitem_counter[0], (uint32_t)__popc(vm));
+      base = __shfl_sync(FULLMASK, base, 0);
+      if (push) {
+        const uint32_t slot = base + __popc(vm & ((1u << lane) - 1u));
+        if (slot < a.vitems_cap) a.vitems[slot] = make_uint2(oo, (uint32_t)(pp << 3) | (uint32_t)s);
+        else st_local |= ST_STAGE_OVERFLOW;
       }
     }
   }
-  uint32_t nb = n_brick, rc = ls.resc, vc = ls.viol, rb = ls.rb, rs = ls.rs, rv = ls.rv, rp = ls.rp;
+  uint32_t nb = n_brick, rc = ls.resc, vc = ls.viol, rb = ls.rb, rs = ls.rs, rv = ls.rv, rp = ls.rp, stw = st_local;
   float me = ls.max_err;
 #pragma unroll
   for (int o2 = 16; o2; o2 >>= 1) {
@@ -305,6 +292,7 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
     rs += __shfl_xor_sync(FULLMASK, rs, o2);
     rv += __shfl_xor_sync(FULLMASK, rv, o2);
     rp += __shfl_xor_sync(FULLMASK, rp, o2);
+    stw |= __shfl_xor_sync(FULLMASK, stw, o2);
     me = fmaxf(me, __shfl_xor_sync(FULLMASK, me, o2));
   }
   if (lane == 0) {
@@ -313,6 +301,62 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
     if (vc) atomicAdd(&a.res->c.violations, (unsigned long long)vc);
     if (rb) atomicAdd(&a.res->c.resc_brick, (unsigned long long)rb);
     if (rs) atomicAdd(&a.res->c.resc_sub, (unsigned long long)rs);
+    if (rv) atomicAdd(&a.res->c.resc_vox, (unsigned long long)rv);
+    if (rp) atomicAdd(&a.res->c.resc_poly, (unsigned long long)rp);
+    if (stw) atomicOr(&a.res->status, stw);
+    if (me > 0.f) atomicMax(&a.res->max_err_bits, (unsigned long long)__double_as_longlong((double)me));
+  }
+}
+
+// Voxel inside-masks of the queued partial sub-blocks: one sub-block per warp
+// pass, 64 voxel SDFs on 32 lanes, two ballots (shapes.ts:390-394).
+template <int MODE>
+__global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIFY64_MINB) voxel_kernel(FoldArgs a) {
+  const int lane = threadIdx.x & 31;
+  LaneStats ls = {0, 0, 0, 0.f, 0, 0, 0, 0};
+  const uint32_t n_items = min(__ldg(&a.vitem_counter[0]), a.vitems_cap);
+  for (;;) {
+    uint32_t it = 0;
+    if (lane == 0) it = atomicAdd(&a.vitem_counter[1], 1u);
+    it = __shfl_sync(FULLMASK, it, 0);
+    if (it >= n_items) break;
+    const uint2 item = __ldg(a.vitems + it);
+    const OpDev* V = a.ops + item.x;
+    const unsigned long long vp = item.y >> 3;
+    const int ss = item.y & 7;
+    int vbx, vby, vbz;
+    brick_of_pair(V, vp, vbx, vby, vbz);
+    const bool use32 = MODE == 1 && !(V->flags & OPF_FP64_ONLY);
+    Iv bo[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    if (use32) brick_bases(a, V, vbx, vby, vbz, bo);
+    const int sxo = (ss & 1) * 4, syo = ((ss >> 1) & 1) * 4, szo = ((ss >> 2) & 1) * 4;
+    const uint2* code = a.code + V->code_off;
+    const int clen = (int)V->code_len;
+    uint32_t bal[2];
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+      const int e = r * 32 + lane;
+      const int lx = sxo + (e & 3), lyv = syo + ((e >> 2) & 3), lz = szo + (e >> 4);
+      int inside = eval_decide<MODE>(a, V, code, clen, use32, bo, (float)lx, (float)lyv, (float)lz,
+                                     (float)(vbx * 8 + lx) + 0.5f, (float)(vby * 8 + lyv) + 0.5f,
+                                     (float)(vbz * 8 + lz) + 0.5f, 0, ls);
+      bal[r] = __ballot_sync(FULLMASK, inside == 1);
+    }
+    if (lane == 0) a.pmask[vp * 8 + ss] = (unsigned long long)bal[0] | ((unsigned long long)bal[1] << 32);
+  }
+  uint32_t rc = ls.resc, vc = ls.viol, rv = ls.rv, rp = ls.rp;
+  float me = ls.max_err;
+#pragma unroll
+  for (int o2 = 16; o2; o2 >>= 1) {
+    rc += __shfl_xor_sync(FULLMASK, rc, o2);
+    vc += __shfl_xor_sync(FULLMASK, vc, o2);
+    rv += __shfl_xor_sync(FULLMASK, rv, o2);
+    rp += __shfl_xor_sync(FULLMASK, rp, o2);
+    me = fmaxf(me, __shfl_xor_sync(FULLMASK, me, o2));
+  }
+  if (lane == 0) {
+    if (rc) atomicAdd(&a.res->c.rescued, (unsigned long long)rc);
+    if (vc) atomicAdd(&a.res->c.violations, (unsigned long long)vc);
     if (rv) atomicAdd(&a.res->c.resc_vox, (unsigned long long)rv);
     if (rp) atomicAdd(&a.res->c.resc_poly, (unsigned long long)rp);
     if (me > 0.f) atomicMax(&a.res->max_err_bits, (unsigned long long)__double_as_longlong((double)me));
@@ -492,10 +536,12 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
     }
 
     if (!dirty) continue;
+    // the grid entry is committed by finalize, so a failed build leaves the world intact
+    uint32_t tag;
     if (state == ST_EMPTY) {
-      if (lane == 0) a.grid[ci] = 0;
+      tag = 0;
     } else if (state == ST_UNIF) {
-      if (lane == 0) a.grid[ci] = UNIFORM | uval;
+      tag = UNIFORM | uval;
     } else {
       uint32_t slot = 0;
       if (lane == 0) slot = atomicAdd(&a.res->stage_count, 1u);
@@ -508,6 +554,12 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
         for (int j = 0; j < 8; j++) dst[32 * j + lane] = vox[j];
         if (lane == 0) { a.stage_cell[slot] = (uint32_t)ci; a.stage_src[slot] = src; }
       }
+      tag = TAG_STAGED | (slot & 0x3fffffffu);
+    }
+    if (lane == 0) {
+      const uint32_t t = atomicAdd(&a.res->touched_count, 1u);
+      if (t < a.touched_cap) a.touched[t] = make_uint2((uint32_t)ci, tag);
+      else st_local |= ST_STAGE_OVERFLOW;
     }
   }
   if (lane == 0) {
@@ -533,8 +585,10 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
 void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEvent_t mid) {
   if (mode == 1) {
     ++g_launches; classify_kernel<1><<<n_sms * PX_CLASSIFY_MINB, 256, 0, s>>>(a);
+    ++g_launches; voxel_kernel<1><<<n_sms * PX_CLASSIFY_MINB, 256, 0, s>>>(a);
   } else {
     ++g_launches; classify_kernel<0><<<n_sms * PX_CLASSIFY64_MINB, 256, 0, s>>>(a);
+    ++g_launches; voxel_kernel<0><<<n_sms * PX_CLASSIFY64_MINB, 256, 0, s>>>(a);
   }
   if (mid) cudaEventRecord(mid, s);
   ++g_launches; fold_kernel<<<n_sms * PX_FOLD_MINB, 256, 0, s>>>(a);
@@ -897,9 +951,21 @@ void launch_replay(const ReplayArgs& a, cudaStream_t s) {
 // finalize: staging -> pool at the replayed indices, grid entries
 
 __global__ void __launch_bounds__(256) finalize_kernel(FinalizeArgs a) {
+  // commit only a complete build: every staging slot written, every pool index within the pool
+  if (a.res->status & (ST_STAGE_OVERFLOW | ST_CHAIN)) return;
+  if (a.res->pool_used > a.pool_cap) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.res->status, (uint32_t)ST_POOL_OVERFLOW);
+    return;
+  }
   const int lane = threadIdx.x & 31;
-  const uint32_t n = min(a.res->stage_count, 0xffffffffu);
-  for (uint32_t slot = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; slot < n; slot += (gridDim.x * blockDim.x) >> 5) {
+  const uint32_t n = a.res->touched_count;
+  for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < n; t += (gridDim.x * blockDim.x) >> 5) {
+    const uint2 e = a.touched[t];
+    if (!(e.y & TAG_STAGED) || (e.y & UNIFORM)) {
+      if (lane == 0) a.grid[e.x] = e.y;
+      continue;
+    }
+    const uint32_t slot = e.y & 0x3fffffffu;
     const long long src = a.stage_src[slot];
     uint32_t idx;
     if (src >= 0) {
@@ -910,20 +976,16 @@ __global__ void __launch_bounds__(256) finalize_kernel(FinalizeArgs a) {
       idx = (uint32_t)(-(src + 1));
     }
     if (lane == 0) atomicMax(&a.res->max_pool_index, idx);
-    if (idx >= a.pool_cap) {
-      if (lane == 0) atomicOr(&a.res->status, (uint32_t)ST_POOL_OVERFLOW);
-      continue;
-    }
     const uint4* s4 = reinterpret_cast<const uint4*>(a.staging32 + (size_t)slot * 256);
     uint4* d4 = reinterpret_cast<uint4*>(a.pool32 + (size_t)idx * 256);
     d4[lane] = s4[lane];
     d4[lane + 32] = s4[lane + 32];
-    if (lane == 0) a.grid[a.stage_cell[slot]] = idx + 1;
+    if (lane == 0) a.grid[e.x] = idx + 1;
   }
 }
 
-void launch_finalize(const FinalizeArgs& a, uint32_t stage_cap, cudaStream_t s) {
-  size_t warps = stage_cap ? stage_cap : 1;
+void launch_finalize(const FinalizeArgs& a, uint32_t touched_cap, cudaStream_t s) {
+  size_t warps = touched_cap ? touched_cap : 1;
   size_t b = (warps * 32 + 255) / 256;
   int blocks = (int)(b < 8192 ? b : 8192);
   ++g_launches; finalize_kernel<<<blocks, 256, 0, s>>>(a);

@@ -3,6 +3,7 @@
 // one build.  Compiled with -ffp-contract=off: the per-op float64 constants
 // (voxel ranges, classify thresholds) must round exactly as the reference's
 // JavaScript does (shapes.ts:341-350).
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -57,8 +58,9 @@ struct px_world {
   DevBuf d_ops, d_boxes, d_code, d_params, d_code32, d_p32, d_bases;
   DevBuf tile_cnt, tile_off, tiles_nonempty, tile_ops;
   DevBuf evt, fsrc, cnt, pos, etype, ew, depth_fn, depth, tree, fresh, fresh_rank;
-  DevBuf staging, stage_cell, stage_src;
-  DevBuf chunk_op, pcode, psub, pmask, chunk_counter;
+  DevBuf staging, stage_cell, stage_src, touched;
+  uint64_t stage_hint = 0;      // staging slots the next build reserves (grown on overflow)
+  DevBuf chunk_op, pcode, psub, pmask, chunk_counter, vitems;
   std::vector<uint32_t> h_chunk_op;
   DevBuf scan_agg;
   DevBuf work_counter;
@@ -72,7 +74,9 @@ struct px_world {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_fold0 = nullptr, ev_fold1 = nullptr, ev_mid = nullptr;
   size_t last_P = 0;
-  uint32_t last_stage_cap = 0;
+  uint32_t last_stage_cap = 0, last_touched_cap = 0;
+  int last_mode = 0;
+  int retries = 0;
   uint32_t last_H = 0, last_U0 = 0;
   FinalizeArgs fin{};
   bool derived_valid = false;
@@ -274,6 +278,26 @@ bool check_code(const uint32_t* code, uint32_t n, const double* P, size_t np, st
   return true;
 }
 
+// Grow the device pool to at least `need` bricks, keeping the first `keep`
+// bricks (growPool, VoxelWorld.ts:129-136, grows by 1.5x).
+int grow_pool(px_world* w, uint64_t need, uint32_t keep, cudaStream_t s) {
+  if (need <= w->pool_cap) return PX_OK;
+  uint64_t cap = w->pool_cap ? w->pool_cap : 1;
+  while (cap < need) cap = (uint64_t)std::ceil(cap * 1.5) + 1;
+  if (cap > 0x3fffffffull) return fail(w, PX_E_OOM, "pool of %llu bricks exceeds the index range", (unsigned long long)cap);
+  uint32_t* np_ = nullptr;
+  if (cudaMalloc((void**)&np_, (size_t)cap * 1024) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(w, PX_E_OOM, "pool of %llu bricks", (unsigned long long)cap);
+  }
+  if (keep) CU(cudaMemcpyAsync(np_, w->d_pool32, (size_t)keep * 1024, cudaMemcpyDeviceToDevice, s));
+  CU(cudaStreamSynchronize(s));
+  cudaFree(w->d_pool32);
+  w->d_pool32 = np_;
+  w->pool_cap = (uint32_t)cap;
+  return PX_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -342,9 +366,9 @@ void px_world_destroy(px_world* w) {
   DevBuf* bufs[] = {&w->holes_a, &w->holes_b, &w->d_ops, &w->d_boxes, &w->d_code, &w->d_params, &w->d_code32,
                     &w->d_p32, &w->d_bases, &w->tile_cnt,
                     &w->tile_off, &w->tiles_nonempty, &w->tile_ops, &w->evt, &w->fsrc, &w->cnt, &w->pos, &w->etype,
-                    &w->ew, &w->depth_fn, &w->depth, &w->tree, &w->fresh, &w->fresh_rank, &w->staging,
+                    &w->ew, &w->depth_fn, &w->depth, &w->tree, &w->fresh, &w->fresh_rank, &w->staging, &w->touched,
                     &w->stage_cell, &w->stage_src, &w->chunk_op, &w->pcode, &w->psub, &w->pmask,
-                    &w->chunk_counter, &w->scan_agg, &w->work_counter, &w->res, &w->opaque,
+                    &w->chunk_counter, &w->vitems, &w->scan_agg, &w->work_counter, &w->res, &w->opaque,
                     &w->udens, &w->super_counts, &w->density};
   for (DevBuf* b : bufs) release(*b);
   if (w->h_res) cudaFreeHost(w->h_res);
@@ -543,25 +567,16 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
              tz = (uint64_t)(o.bz1 / 4 - o.bz0 / 4 + 1);
     tile_pairs += tx * ty * tz;
   }
-  if (P > 0x7fffffffull) return fail(w, PX_E_QUEUE_OVERFLOW, "too many (op, brick) pairs in one build: %llu", (unsigned long long)P);
+  if (P > 0x1fffffffull) return fail(w, PX_E_QUEUE_OVERFLOW, "too many (op, brick) pairs in one build: %llu", (unsigned long long)P);
   const uint64_t touched_bound = P < w->ncells ? P : w->ncells;
   const uint32_t H = w->n_holes, U0 = w->pool_used;
   const size_t E_max = (size_t)H + 2 * P;
 
-  // pool capacity: poolUsed can grow by at most the number of touched bricks
-  uint64_t need_cap = (uint64_t)U0 + touched_bound;
-  if (need_cap > w->pool_cap) {
-    uint64_t cap = w->pool_cap;
-    while (cap < need_cap) cap = (uint64_t)std::ceil(cap * 1.5) + 1;  // growPool (VoxelWorld.ts:129-136)
-    if (cap > 0xffffffffull / 2) return fail(w, PX_E_OOM, "pool too large");
-    uint32_t* np_ = nullptr;
-    if (cudaMalloc((void**)&np_, (size_t)cap * 1024) != cudaSuccess) { cudaGetLastError(); return fail(w, PX_E_OOM, "pool of %llu bricks", (unsigned long long)cap); }
-    if (U0) CU(cudaMemcpyAsync(np_, w->d_pool32, (size_t)U0 * 1024, cudaMemcpyDeviceToDevice, s));
-    CU(cudaStreamSynchronize(s));
-    cudaFree(w->d_pool32);
-    w->d_pool32 = np_;
-    w->pool_cap = (uint32_t)cap;
-  }
+  // staging slots and pool bricks are reserved from a guess; a build that needs
+  // more commits nothing and is retried with larger buffers (px_build_finish)
+  uint64_t stage_cap = std::max(std::max((uint64_t)4096, w->stage_hint), (uint64_t)(P / 4));
+  if (stage_cap > touched_bound) stage_cap = touched_bound ? touched_bound : 1;
+  if ((rc = grow_pool(w, (uint64_t)U0 + stage_cap, U0, s))) return rc;
 
   // scratch (a reallocated op table loses its resident copy)
   const void* op_bufs_before[7] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p, w->d_p32.p, w->d_bases.p};
@@ -578,11 +593,13 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
       (rc = ensure(w, w->pos, 4 * P)) || (rc = ensure(w, w->etype, E_max)) || (rc = ensure(w, w->ew, 8 * E_max)) ||
       (rc = ensure(w, w->depth_fn, 8 * E_max)) || (rc = ensure(w, w->depth, 4 * E_max)) ||
       (rc = ensure(w, w->tree, 4 * (E_max / 16 + 64 + E_max))) || (rc = ensure(w, w->fresh, 4 * E_max)) ||
-      (rc = ensure(w, w->fresh_rank, 4 * E_max)) || (rc = ensure(w, w->staging, 1024 * touched_bound)) ||
-      (rc = ensure(w, w->stage_cell, 4 * touched_bound)) || (rc = ensure(w, w->stage_src, 8 * touched_bound)) ||
+      (rc = ensure(w, w->fresh_rank, 4 * E_max)) || (rc = ensure(w, w->staging, 1024 * stage_cap)) ||
+      (rc = ensure(w, w->stage_cell, 4 * stage_cap)) || (rc = ensure(w, w->stage_src, 8 * stage_cap)) ||
+      (rc = ensure(w, w->touched, 8 * touched_bound)) ||
       (rc = ensure(w, w->work_counter, 16)) || (rc = ensure(w, w->res, sizeof(BuildResult))) ||
       (rc = ensure(w, w->chunk_op, 4 * ((P + 31) / 32))) || (rc = ensure(w, w->pcode, P)) ||
-      (rc = ensure(w, w->psub, 2 * P)) || (rc = ensure(w, w->pmask, 64 * P)) || (rc = ensure(w, w->chunk_counter, 16)))
+      (rc = ensure(w, w->psub, 2 * P)) || (rc = ensure(w, w->pmask, 64 * P)) || (rc = ensure(w, w->chunk_counter, 16)) ||
+      (rc = ensure(w, w->vitems, 8 * 8 * P)))
     return rc;
   {
     size_t items = w->ntiles > E_max ? w->ntiles : E_max;
@@ -645,6 +662,9 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   fa.psub = (uint16_t*)w->psub.p;
   fa.pmask = (unsigned long long*)w->pmask.p;
   fa.chunk_counter = (uint32_t*)w->chunk_counter.p;
+  fa.vitems = (uint2*)w->vitems.p;
+  fa.vitems_cap = (uint32_t)(8 * P < 0xffffffffull ? 8 * P : 0xffffffffull);
+  fa.vitem_counter = (uint32_t*)w->chunk_counter.p + 2;
   fa.ops = (const OpDev*)w->d_ops.p;
   fa.code = (const uint2*)w->d_code.p;
   fa.params = (const double*)w->d_params.p;
@@ -665,7 +685,9 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   fa.evt = (uint8_t*)w->evt.p;
   fa.fsrc = (int64_t*)w->fsrc.p;
   fa.staging32 = (uint32_t*)w->staging.p;
-  fa.stage_cap = (uint32_t)touched_bound;
+  fa.stage_cap = (uint32_t)stage_cap;
+  fa.touched = (uint2*)w->touched.p;
+  fa.touched_cap = (uint32_t)touched_bound;
   fa.stage_cell = (uint32_t*)w->stage_cell.p;
   fa.stage_src = (int64_t*)w->stage_src.p;
   fa.work_counter = (uint32_t*)w->work_counter.p;
@@ -695,6 +717,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   launch_replay(ra, s);
 
   FinalizeArgs& fn = w->fin;
+  fn.touched = (const uint2*)w->touched.p;
   fn.staging32 = (const uint32_t*)w->staging.p;
   fn.stage_cell = (const uint32_t*)w->stage_cell.p;
   fn.stage_src = (const int64_t*)w->stage_src.p;
@@ -712,7 +735,9 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   CU(cudaMemcpyAsync(w->h_res, res, sizeof(BuildResult), cudaMemcpyDeviceToHost, s));
   w->in_flight = true;
   w->last_P = P;
-  w->last_stage_cap = (uint32_t)touched_bound;
+  w->last_stage_cap = (uint32_t)stage_cap;
+  w->last_touched_cap = (uint32_t)touched_bound;
+  w->last_mode = mode;
   w->last_H = H;
   w->last_U0 = U0;
   return PX_OK;
@@ -752,6 +777,34 @@ int px_build_finish(px_world* w) {
   w->stats.rescued_polygon = r.c.resc_poly;
   w->stats.build_ms = ms;
   w->stats.status = r.status;
+  // transactional retries: nothing was committed
+  if ((r.status & ST_STAGE_OVERFLOW) && r.stage_count > w->last_stage_cap && w->retries < 2) {
+    w->stage_hint = (uint64_t)r.stage_count + r.stage_count / 4 + 64;
+    w->retries++;
+    w->ops_resident = true;  // the op tables uploaded by this attempt are still on the device
+    int rc = px_build_enqueue(w, w->last_mode, w->stream);
+    if (rc == PX_OK) rc = px_build_finish(w);
+    w->retries = 0;
+    return rc;
+  }
+  if ((r.status & ST_POOL_OVERFLOW) && !(r.status & (ST_STAGE_OVERFLOW | ST_CHAIN)) && w->retries < 2) {
+    w->retries++;
+    int rc = grow_pool(w, (uint64_t)r.pool_used + r.pool_used / 4 + 64, w->last_U0, w->stream);
+    if (rc) { w->retries = 0; return rc; }
+    BuildResult* dres = (BuildResult*)w->res.p;
+    const uint32_t st2 = r.status & ~(uint32_t)ST_POOL_OVERFLOW;
+    CU(cudaMemcpyAsync(&dres->status, &st2, 4, cudaMemcpyHostToDevice, w->stream));
+    w->fin.pool32 = w->d_pool32;
+    w->fin.pool_cap = w->pool_cap;
+    launch_finalize(w->fin, w->last_touched_cap, w->stream);
+    CU(cudaGetLastError());
+    CU(cudaMemcpyAsync(w->h_res, dres, sizeof(BuildResult), cudaMemcpyDeviceToHost, w->stream));
+    w->in_flight = true;
+    rc = px_build_finish(w);
+    w->retries = 0;
+    return rc;
+  }
+  w->retries = 0;
   if (r.status & (ST_STAGE_OVERFLOW | ST_POOL_OVERFLOW | ST_CHAIN))
     return fail(w, PX_E_QUEUE_OVERFLOW, "device status 0x%x (stage %u of %u, max pool index %u of %u)", r.status,
                 r.stage_count, w->last_stage_cap, r.max_pool_index, w->pool_cap);

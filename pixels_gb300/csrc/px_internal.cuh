@@ -93,7 +93,8 @@ struct BuildResult {
   uint32_t n_events;     // H + N
   uint32_t pool_used;    // after the build
   uint32_t n_holes;      // after the build
-  uint32_t stage_count;  // bricks that end as pool bricks and were touched
+  uint32_t stage_count;  // bricks that end as pool bricks and were touched (staging slots wanted)
+  uint32_t touched_count;  // bricks whose grid entry the build rewrites
   uint32_t n_nonempty;   // tiles with at least one op
   uint32_t n_fresh;
   uint32_t max_pool_index;
@@ -113,6 +114,9 @@ struct FoldArgs {
   uint16_t* psub;             // per partial pair: 2 bits per sub-block (PC_*)
   unsigned long long* pmask;  // per partial pair: 8 inside-masks (bit = x&3 | (y&3)<<2 | (z&3)<<4)
   uint32_t* chunk_counter;
+  uint2* vitems;              // partial sub-blocks to classify voxel by voxel: (op, pair << 3 | sub)
+  uint32_t vitems_cap;
+  uint32_t* vitem_counter;    // [0] items pushed, [1] items taken
   const OpDev* ops;
   const uint2* code;
   const double* params;
@@ -135,9 +139,14 @@ struct FoldArgs {
   uint32_t stage_cap;
   uint32_t* stage_cell;
   int64_t* stage_src;
+  uint2* touched;             // (cell, final tag): 0, UNIFORM|v, or STAGED|slot
+  uint32_t touched_cap;
   uint32_t* work_counter;
   BuildResult* res;
 };
+
+// touched-list tag of a brick that ends as a pool brick: its staging slot
+constexpr uint32_t TAG_STAGED = 0x40000000u;
 
 // Host-side launch wrappers (kernels.cu)
 void launch_cull_count(const uint2* boxes, int n_ops, int TX, int TY, int TZ, uint32_t* tile_cnt,
@@ -179,6 +188,7 @@ struct ReplayArgs {
 void launch_replay(const ReplayArgs& a, cudaStream_t s);
 
 struct FinalizeArgs {
+  const uint2* touched;
   const uint32_t* staging32;
   const uint32_t* stage_cell;
   const int64_t* stage_src;
@@ -190,7 +200,7 @@ struct FinalizeArgs {
   uint32_t pool_cap;
   BuildResult* res;
 };
-void launch_finalize(const FinalizeArgs& a, uint32_t stage_cap, cudaStream_t s);
+void launch_finalize(const FinalizeArgs& a, uint32_t touched_cap, cudaStream_t s);
 
 void launch_derive(const uint32_t* grid, const uint32_t* pool32, int BX, int BY, int BZ,
                    const uint8_t* opaque, const uint8_t* udens, uint32_t* super_counts,

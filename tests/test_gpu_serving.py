@@ -81,6 +81,6 @@ def test_pool_budget_admission(built_lib):
     cfg = config.Config(vpm)
     live = w.liveBricks
     edits, _ = serving.edit_stream(w.grid, cfg.bricks, vpm, 50, rate=0, seed=9, r_min=0.3, r_max=0.4)
-    res, order = serving.serve(w, edits, np.zeros(len(edits)), max_batch=50, pool_budget=live + 64)
-    # a 30-40 cm edit spans more than 64 bricks at 2.5 cm voxels: none fits
+    res, order = serving.serve(w, edits, np.zeros(len(edits)), max_batch=50, pool_budget=live + 8)
+    # a 30-40 cm edit spans at least 3 x 3 x 3 bricks of 20 cm: none fits in 8
     assert (res["status"] == 3).all() and len(order) == 0
