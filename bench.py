@@ -143,6 +143,94 @@ def reference_arm(args):
     }))
 
 
+def _device_ms(build_fn, steps, warmup):
+    import torch
+    for _ in range(warmup):
+        build_fn()
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        build_fn()
+        b.record()
+        torch.cuda.synchronize()
+        ms.append(a.elapsed_time(b))
+    return statistics.mean(ms)
+
+
+def synthetic_section(args, pyoracle):
+    """Seeded synthetic scene: 4,096 primitives (box, rounded box, cylinder, capsule,
+    torus, 8-point lathe, extruded hexagon; 30% subtract, 10% intersect; 25% noise
+    paint) in the 16 x 4.4 x 12 m volume at vpm=80, both forms, checked against the oracle."""
+    import numpy as np
+    from pixels_gb300 import _lib, config
+    from pixels_gb300.scenes.synthetic import synthetic_program
+    from pixels_gb300.world import MODE_FP64, MODE_MIXED
+    vpm = 80.0
+    cfg = config.Config(vpm)
+    prog = synthetic_program(1, 4096, vpm)
+    ir = prog.to_bytes()
+    h = _lib.world_create(*cfg.dims, vpm, 1 << 15)
+    _lib.submit_ops(h, ir)
+    _lib.build(h, MODE_MIXED)
+    res = {"workload": "synthetic seed 1, 4096 primitives, vpm=80", "ops": len(prog), "cells": cfg.cells}
+    for name, mode in (("mixed", MODE_MIXED), ("fp64", MODE_FP64)):
+        def one():
+            _lib.world_reset(h, True)
+            _lib.build(h, mode)
+        t = _device_ms(one, max(2, args.steps // 2), 2)
+        res[name] = {"ms_per_step": round(t, 4), "value": round(cfg.cells / (t * 1e-3) / 1e9, 3)}
+    st = _lib.stats(h)
+    grid = _lib.read_grid(h, cfg.bricks[0] * cfg.bricks[1] * cfg.bricks[2])
+    pool = _lib.read_pool(h)
+    o = pyoracle.OracleWorld(ir, vpm, cfg.dims, threads=os.cpu_count() or 1)
+    live = np.nonzero((o.grid != 0) & ((o.grid & 0x80000000) == 0))[0]
+    idx = o.grid[live].astype(np.int64) - 1
+    res["mismatches"] = {"grid_cells": int(np.count_nonzero(grid != o.grid)),
+                         "pool_voxels": int(np.count_nonzero(pool.reshape(-1, 512)[idx] != o.pool.reshape(-1, 512)[idx]))
+                         if st["pool_used"] == o.pool_used else -1,
+                         "pool_used": int(st["pool_used"]) - int(o.pool_used)}
+    res["rescued_voxels"] = st["rescued_voxel"]
+    res["voxel_evals"] = st["voxel_evals"]
+    _lib.world_destroy(h)
+    return res
+
+
+def serving_section(args, pyoracle):
+    """Subtract-edits (70% spheres, 30% capsules, radii 1-40 cm, centres on occupied
+    bricks, Poisson arrivals) served on a resident synthetic map at vpm=160
+    (2560x704x1920 = 3.46 G cells), continuous batching up to 512 edits per step."""
+    import numpy as np
+    from pixels_gb300 import config, serving
+    from pixels_gb300.scenes.synthetic import synthetic_program
+    from pixels_gb300.world import MODE_MIXED, VoxelWorld
+    vpm = 160.0
+    cfg = config.Config(vpm)
+    prog = synthetic_program(1, 4096, vpm)
+    w = VoxelWorld(*cfg.dims, initialPoolBricks=1 << 20, vpm=vpm, mode=MODE_MIXED)
+    w._pending = prog
+    w.build()
+    grid = w.grid
+    out = {"workload": "resident synthetic map (seed 1, 4096 primitives) at vpm=160", "cells": cfg.cells,
+           "max_batch": 512, "rates": []}
+    for rate in (1000.0, 20000.0, 100000.0, 200000.0):
+        edits, arr = serving.edit_stream(grid, cfg.bricks, vpm, 2000, rate=rate, seed=int(rate))
+        res, order = serving.serve(w, edits, arr, max_batch=512)
+        st = serving.latency_stats(res)
+        st["rate_offered"] = rate
+        out["rates"].append(st)
+    # 256 concurrent requests: bursts of 256 edits arriving together, 4 ms apart
+    edits, _ = serving.edit_stream(grid, cfg.bricks, vpm, 256 * 16, rate=0, seed=7)
+    arr = np.repeat(np.arange(16) * 0.004, 256)
+    res, order = serving.serve(w, edits, arr, max_batch=512)
+    st = serving.latency_stats(res)
+    st["burst"] = 256
+    out["concurrent_256"] = st
+    w.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -154,6 +242,8 @@ def main():
     ap.add_argument("--mode", choices=("both", "mixed", "fp64"), default="both",
                     help="forms to time (profiling runs time one)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the synthetic-scene and serving sections")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -335,6 +425,10 @@ def main():
         "clocks": clocks,
         "gpu_launches": int(st["kernel_launches"]) * args.steps,
     }
+    if not args.no_extra:
+        _lib.world_destroy(h)
+        out["synthetic"] = synthetic_section(args, pyoracle)
+        out["serving"] = serving_section(args, pyoracle)
     print(json.dumps(out))
     if dist is not None:
         dist.destroy_process_group()
