@@ -33,6 +33,7 @@ extern "C" {
 #define PX_E_CUDA 6           /* CUDA runtime error */
 #define PX_E_RANGE 7          /* a paint function got an argument outside its supported range */
 #define PX_E_NO_DEVICE 8      /* no CUDA device */
+#define PX_E_TOO_LARGE 9      /* input larger than a fixed-size buffer of the library allows */
 
 /* build modes */
 #define PX_MODE_FP64 0   /* every decision in float64, as JavaScript numbers */
@@ -110,6 +111,26 @@ int px_derive(px_world* w);
 int px_read_super(px_world* w, uint32_t* dst, size_t n);
 int px_read_density(px_world* w, uint8_t* dst, size_t n);
 int px_read_free_list(px_world* w, uint32_t max_bricks, uint32_t* dst, size_t n, uint32_t* out_len);
+
+/* The same super-grid counts and density bytes as px_derive, from a grid (bx*by*bz
+   entries, bricks) and a pool (n_pool_bricks * 512 voxels) that the caller holds
+   on the current device, written into caller-held device buffers super_counts
+   (ceil(bx/4)*ceil(by/4)*ceil(bz/4)) and density (bx*by*bz); the material tables
+   are host arrays of 256 bytes (as px_set_material_tables).  No counterpart in
+   the reference (GpuWorld.ts:90-101 computes these with its world); this entry
+   point exists for callers that must not allocate device memory once they run
+   (fixed device budgets, frame loops): it allocates nothing and uses a fixed
+   scratch area of 2 MiB + 256 bytes inside the library, which limits
+   n_pool_bricks to PX_NOALLOC_MAX_POOL_BRICKS (larger: PX_E_TOO_LARGE, no GPU
+   work).  The first call on each device looks up that area, with the device
+   current; make it before any stream capture on that device.  All calls share
+   the area, so calls that overlap in time race: serialise them.  Returns after
+   the work on `stream` has finished; PX_E_INVALID_ARG also when the grid names
+   a pool brick >= n_pool_bricks (that cell's density is written as 0). */
+#define PX_NOALLOC_MAX_POOL_BRICKS 1048576u
+int px_derive_noalloc(const uint32_t* grid, const uint16_t* pool, int bx, int by, int bz, uint32_t n_pool_bricks,
+                      const uint8_t* opaque256, const uint8_t* uniform_density256, uint32_t* super_counts,
+                      uint8_t* density, void* stream);
 
 /* Material tables for the density pass: opaque[id] (OPAQUE, VoxelWorld.ts:190-196) and the
    density of a uniform brick of material id (VoxelWorld.ts:162).  256 bytes each. */

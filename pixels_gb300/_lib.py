@@ -16,14 +16,15 @@ LIB_PATH = os.environ.get("PIXELS_GB300_LIB", os.path.join(HERE, "libpixels_gb30
 
 PX_OK = 0
 ERRORS = {1: "PX_E_INVALID_ARG", 2: "PX_E_INVALID_IR", 3: "PX_E_OOM", 4: "PX_E_QUEUE_OVERFLOW",
-          5: "PX_E_TIMEOUT", 6: "PX_E_CUDA", 7: "PX_E_RANGE", 8: "PX_E_NO_DEVICE"}
+          5: "PX_E_TIMEOUT", 6: "PX_E_CUDA", 7: "PX_E_RANGE", 8: "PX_E_NO_DEVICE", 9: "PX_E_TOO_LARGE"}
+PX_NOALLOC_MAX_POOL_BRICKS = 1 << 20
 
 # Every symbol include/pixels_gb300.h declares.
 EXPORTS = [
     "px_world_create", "px_world_destroy", "px_world_reset", "px_submit_ops", "px_build", "px_build_enqueue",
     "px_build_finish", "px_read_grid", "px_read_pool", "px_read_holes", "px_derive", "px_read_super",
     "px_read_density", "px_read_free_list", "px_set_material_tables", "px_set_validation", "px_get_stats",
-    "px_device_view_get", "px_last_error", "px_probe_peak", "px_world_info", "px_serve_run",
+    "px_device_view_get", "px_last_error", "px_probe_peak", "px_world_info", "px_serve_run", "px_derive_noalloc",
 ]
 
 
@@ -31,6 +32,11 @@ class PxError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"{ERRORS.get(code, code)}: {msg}")
         self.code = code
+
+
+class DeviceView(ctypes.Structure):
+    _fields_ = [("grid", ctypes.c_void_p), ("pool", ctypes.c_void_p), ("holes", ctypes.c_void_p),
+                ("super_counts", ctypes.c_void_p), ("density", ctypes.c_void_p)]
 
 
 class Edit(ctypes.Structure):
@@ -92,6 +98,7 @@ def load(path: str = LIB_PATH):
     L.px_serve_run.argtypes = [vp, ctypes.POINTER(Edit), ctypes.POINTER(ctypes.c_double), sz, u32, ctypes.c_uint64,
                                ctypes.c_int, vp, ctypes.POINTER(EditResult), ctypes.POINTER(ctypes.c_uint64),
                                ctypes.POINTER(sz)]
+    L.px_derive_noalloc.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, u32, vp, vp, vp, vp, vp]
     _L = L
     return L
 
@@ -210,3 +217,29 @@ def serve_run(h, edits, arrivals, max_batch: int, pool_budget: int, mode: int, s
                    dtype=[("id", "u8"), ("status", "u4"), ("batch", "u4"), ("arrival_s", "f8"), ("start_s", "f8"),
                           ("done_s", "f8")])
     return out, np.array(order[:n_app.value], dtype=np.int64)
+
+
+def device_view(h) -> DeviceView:
+    """Device addresses of a world's buffers (valid until its next build)."""
+    v = DeviceView()
+    _check(h, load().px_device_view_get(h, ctypes.byref(v)))
+    return v
+
+
+def derive_noalloc(grid_ptr: int, pool_ptr: int, bricks, n_pool_bricks: int, super_ptr: int, density_ptr: int,
+                   stream: int = 0) -> None:
+    """px_derive_noalloc on caller-held device buffers (addresses as ints)."""
+    from .materials import opaque_table, uniform_density_table
+    op = np.array(opaque_table(), np.uint8)
+    ud = np.array(uniform_density_table(), np.uint8)
+    bx, by, bz = bricks
+    rc = load().px_derive_noalloc(ctypes.c_void_p(grid_ptr), ctypes.c_void_p(pool_ptr), int(bx), int(by), int(bz),
+                                  int(n_pool_bricks), op.ctypes.data, ud.ctypes.data, ctypes.c_void_p(super_ptr),
+                                  ctypes.c_void_p(density_ptr), ctypes.c_void_p(stream))
+    if rc == 9:
+        raise PxError(rc, f"a pool of {n_pool_bricks} bricks exceeds the fixed scratch of px_derive_noalloc "
+                          f"({PX_NOALLOC_MAX_POOL_BRICKS} bricks)")
+    if rc == 1:
+        raise PxError(rc, "bad argument, or the grid names a pool brick beyond n_pool_bricks")
+    if rc != PX_OK:
+        raise PxError(rc, "px_derive_noalloc failed")
