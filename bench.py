@@ -315,6 +315,7 @@ def main():
     if args.mode in ("both", "mixed"):
         ms_mx, fold_mx = timed_builds(MODE_MIXED, args.steps, args.warmup)
         cls_mx = timed_builds.cls
+    have64 = ms64 is not None
     if ms_mx is None:
         ms_mx, fold_mx = ms64, fold64
     if ms64 is None:
@@ -402,10 +403,10 @@ def main():
                                "one full world build per step",
                    "cells": cells, "ops": len(prog), "l2": "flushed between timed steps (256 MB write)",
                    "parallelism": f"replicas x{world}"},
-        "fp64_form": {"value": round(value64, 4), "ms_per_step": round(t_64, 4),
-                      "fold_ms": round(fold64_s * 1e3, 4), "classify_ms": cls64},
+        "fp64_form": ({"value": round(value64, 4), "ms_per_step": round(t_64, 4),
+                       "fold_ms": round(fold64_s * 1e3, 4), "classify_ms": cls64} if have64 else None),
         "classify_ms": cls_mx,
-        "speedup_mixed_vs_fp64": round(t_64 / t_mx, 3),
+        "speedup_mixed_vs_fp64": round(t_64 / t_mx, 3) if have64 else None,
         "mismatches": {"grid_cells": mism_grid, "pool_voxels": mism_vox, "pool_used": int(used) - int(o.pool_used)},
         "rescued": {"total": st["rescued"], "brick": st["rescued_brick"], "sub": st["rescued_sub"],
                     "voxel": st["rescued_voxel"], "polygon_test": st["rescued_polygon"],
@@ -416,11 +417,12 @@ def main():
                 "ms_per_step": round(t_e2e * 1e3, 3)},
         "roofline": {"bound": "fp32-alu", "achieved": round(achieved, 4), "peak": round(peak32, 2),
                      "unit": "TFLOP/s", "frac": round(achieved / peak32, 5), "traffic": None,
-                     "kernel": "fold_kernel", "alg_ops_per_launch": int(alg_ops),
+                     "kernel": "classify_kernel + voxel_kernel + fold_kernel (every SDF and paint evaluation)",
+                     "alg_ops_per_launch": int(alg_ops),
                      "fold_ms": round(fold_s * 1e3, 4),
                      "peak_source": "measured here: dependent FFMA chains on all SMs (px_probe_peak)",
-                     "fp64": {"achieved": round(alg_ops / fold64_s / 1e12, 5), "peak": round(peak64, 3),
-                              "frac": round(alg_ops / fold64_s / 1e12 / peak64, 5)}},
+                     "fp64": ({"achieved": round(alg_ops / fold64_s / 1e12, 5), "peak": round(peak64, 3),
+                               "frac": round(alg_ops / fold64_s / 1e12 / peak64, 5)} if have64 else None)},
         "cpu_baseline": cpu,
         "clocks": clocks,
         "gpu_launches": int(st["kernel_launches"]) * args.steps,

@@ -176,6 +176,23 @@ __device__ __forceinline__ int eval_decide(const FoldArgs& a, const OpDev* O, co
   return classify64(d, what == 1 ? O->bhd : O->shd);
 }
 
+// Bits i (0..3) of a 4-voxel row starting at voxel s that lie in the run [lo, hi].
+__device__ __forceinline__ uint32_t run4(int s, int lo, int hi) {
+  const int a0 = max(lo - s, 0), b0 = min(hi - s, 3);
+  return a0 > b0 ? 0u : (2u << b0) - (1u << a0);
+}
+// Inside-mask of a lone box's 4^3 sub-block at voxel (sx, sy, sz) from its
+// per-axis runs (OPF_BOX_RANGES): bit lx | ly << 2 | lz << 4.
+__device__ __forceinline__ unsigned long long box_mask(const OpDev* O, int sx, int sy, int sz) {
+  const uint32_t xb = run4(sx, O->vr[0], O->vr[1]), yb = run4(sy, O->vr[2], O->vr[3]),
+                 zb = run4(sz, O->vr[4], O->vr[5]);
+  const uint32_t ys = (yb & 1u) | ((yb & 2u) << 3) | ((yb & 4u) << 6) | ((yb & 8u) << 9);  // bit ly -> 4 ly
+  const unsigned long long zs =
+      (zb & 1ull) | ((unsigned long long)(zb & 2u) << 15) | ((unsigned long long)(zb & 4u) << 30) |
+      ((unsigned long long)(zb & 8u) << 45);  // bit lz -> 16 lz
+  return (unsigned long long)(xb * ys) * zs;
+}
+
 __device__ __forceinline__ void brick_of_pair(const OpDev* O, unsigned long long p, int& bx, int& by, int& bz) {
   const uint32_t local = (uint32_t)(p - O->pair_base);
   const uint32_t nxy = (uint32_t)(O->nx * O->ny);
@@ -253,8 +270,10 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
       const int pbx = __shfl_sync(FULLMASK, bx, sll), pby = __shfl_sync(FULLMASK, by, sll),
                 pbz = __shfl_sync(FULLMASK, bz, sll);
       int scls = PC_SKIP;
+      bool boxr = false;
       if (sl >= 0) {
         const OpDev* Q = a.ops + oo;
+        boxr = (Q->flags & OPF_BOX_RANGES) && !a.validate;
         const bool use32 = MODE == 1 && !(Q->flags & OPF_FP64_ONLY);
         Iv bo[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
         if (use32) brick_bases(a, Q, pbx, pby, pbz, bo);
@@ -268,8 +287,12 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
       code16 |= __shfl_xor_sync(FULLMASK, code16, 2);
       code16 |= __shfl_xor_sync(FULLMASK, code16, 4);
       if (s == 0 && sl >= 0) a.psub[pp] = (uint16_t)code16;
-      // queue the partial sub-blocks (one warp-aggregated append)
-      const bool push = sl >= 0 && scls == PC_PARTIAL;
+      // queue the partial sub-blocks (one warp-aggregated append); a lone box's
+      // voxel mask comes from its per-axis runs instead
+      if (boxr && scls == PC_PARTIAL)
+        a.pmask[pp * 8 + s] = box_mask(a.ops + oo, pbx * 8 + (s & 1) * 4, pby * 8 + ((s >> 1) & 1) * 4,
+                                       pbz * 8 + ((s >> 2) & 1) * 4);
+      const bool push = sl >= 0 && scls == PC_PARTIAL && !boxr;
       const uint32_t vm = __ballot_sync(FULLMASK, push);
       uint32_t base = 0;
       if (lane == 0 && vm) base = atomicAdd(&a.vitem_counter[0], (uint32_t)__popc(vm));
@@ -342,7 +365,11 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
                                      (float)(vbz * 8 + lz) + 0.5f, 0, ls);
       bal[r] = __ballot_sync(FULLMASK, inside == 1);
     }
-    if (lane == 0) a.pmask[vp * 8 + ss] = (unsigned long long)bal[0] | ((unsigned long long)bal[1] << 32);
+    const unsigned long long m = (unsigned long long)bal[0] | ((unsigned long long)bal[1] << 32);
+    // a lone box's sub-block is queued only in validation mode: check its runs
+    if ((V->flags & OPF_BOX_RANGES) && lane == 0 && box_mask(V, vbx * 8 + sxo, vby * 8 + syo, vbz * 8 + szo) != m)
+      ls.viol++;
+    if (lane == 0) a.pmask[vp * 8 + ss] = m;
   }
   uint32_t rc = ls.resc, vc = ls.viol, rv = ls.rv, rp = ls.rp;
   float me = ls.max_err;

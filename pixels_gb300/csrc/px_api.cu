@@ -428,7 +428,7 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
 
     OpDev d{};
     d.kind = o.kind;
-    d.flags = o.flags;
+    d.flags = o.flags & OPF_FROM_IR;
     d.paint_kind = o.paint_kind;
     d.paint_value = o.paint_value;
     d.code_off = (uint32_t)(code_base + ncode.size());
@@ -500,6 +500,37 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
         }
         if (first < 0) { *lo[k] = 1; *hi[k] = 0; } else { *lo[k] = first; *hi[k] = last; }
       }
+    }
+    // A lone box (shapes.ts:40-44): d = |max(q, 0)| + min(max(qx, qy, qz), 0) with
+    // q = |p - c| - h is > 0 exactly when some q_k > 0 (a positive q_k >= 2^-60
+    // squares without underflow, so the length is positive; otherwise the length
+    // is 0 and d = max q_k <= 0).  In float64, q_k <= 0 iff |fl(p_k - c_k)| <= h_k,
+    // and fl(p_k - c_k) is monotone in the voxel index, so the voxels inside on
+    // each axis form one run: evaluate the reference's expression once per voxel
+    // row of the op's bricks and keep the run.  A voxel is inside iff it is in
+    // all three runs (the same decision as evaluating the SDF at its centre).
+    d.vr[0] = d.vr[2] = d.vr[4] = 1;
+    d.vr[1] = d.vr[3] = d.vr[5] = 0;
+    if (o.code_len == 1 && (code[2 * (size_t)o.code_begin] & 0xffu) == OP_BOX && d.bx0 <= d.bx1) {
+      const double* bp = P.data() + code[2 * (size_t)o.code_begin + 1];
+      const int b0[3] = {d.bx0, d.by0, d.bz0}, b1[3] = {d.bx1, d.by1, d.bz1};
+      bool runs = true;
+      for (int k = 0; k < 3; k++) {
+        int first = 1, last = 0, n_in = 0;
+        for (int v = b0[k] * 8; v <= b1[k] * 8 + 7; v++) {
+          const double t = ((double)v + 0.5) * vs;
+          const double q = std::fabs(t - bp[k]) - bp[3 + k];
+          if (q <= 0) {
+            if (n_in == 0) first = v;
+            last = v;
+            n_in++;
+          }
+        }
+        if (n_in && n_in != last - first + 1) runs = false;  // not one run: evaluate per voxel
+        d.vr[2 * k] = n_in ? first : 1;
+        d.vr[2 * k + 1] = n_in ? last : 0;
+      }
+      if (runs) d.flags |= OPF_BOX_RANGES;
     }
     // shapes.ts:349-350
     d.bhd = 4 * std::sqrt(3.0) * vs * o.slack + vs * 0.01;

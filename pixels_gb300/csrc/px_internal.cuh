@@ -33,7 +33,8 @@ enum : uint16_t {
 };
 constexpr int PAINT_NPARAMS[PK_COUNT] = {0, 5, 3, 4, 2, 2, 5, 37, 8};
 
-enum : uint8_t { OPF_CONTAINS = 1, OPF_HAS_SLACK = 2, OPF_PAINT_FRAME = 4, OPF_FP64_ONLY = 0x80 };
+enum : uint8_t { OPF_CONTAINS = 1, OPF_HAS_SLACK = 2, OPF_PAINT_FRAME = 4, OPF_BOX_RANGES = 0x40, OPF_FP64_ONLY = 0x80 };
+constexpr uint8_t OPF_FROM_IR = OPF_CONTAINS | OPF_HAS_SLACK | OPF_PAINT_FRAME;  // flags an op list may set
 
 // Mixed mode: margin between the exact value of an expression on the float64
 // inputs and the reference's float64 result (valid for |values| <= 2^10 m).
@@ -78,6 +79,10 @@ struct OpDev {
   int32_t cbx0, cby0, cbz0, cbx1, cby1, cbz1;  // bricks the box fully contains (contains(), shapes.ts:47-48,360)
   uint32_t base_off;                     // mixed mode: float32 first-voxel-centre offsets per brick row
   uint32_t pad2;
+  // OPF_BOX_RANGES (a lone axis-aligned box): per axis, the first and last voxel
+  // whose centre the reference's float64 box SDF puts inside on that axis
+  int32_t vr[6];                         // x lo, x hi, y lo, y hi, z lo, z hi (empty: lo > hi)
+  int32_t pad3[2];
 };
 
 struct BuildCounters {
