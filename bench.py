@@ -231,6 +231,21 @@ def serving_section(args, pyoracle):
     return out
 
 
+def hbm_line(cfg, pool_used, ir_bytes, ms):
+    """Algorithmic HBM bytes of one build (outputs written + the op list read
+    once) over the build time, against the measured copy bandwidth."""
+    peak = None
+    try:
+        peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
+    except (OSError, KeyError, ValueError):
+        pass
+    n_bricks = cfg.bricks[0] * cfg.bricks[1] * cfg.bricks[2]
+    alg = 4 * n_bricks + 1024 * int(pool_used) + int(ir_bytes)
+    gbs = alg / (ms * 1e-3) / 1e9
+    return {"alg_bytes_per_build": alg, "achieved_gbs": round(gbs, 2), "peak_gbs": peak,
+            "frac": round(gbs / peak, 5) if peak else None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -266,8 +281,10 @@ def main():
     L = _lib.load()
     vpm = args.vpm
     cfg = config.Config(vpm)
+    t_flat = time.perf_counter()
     prog, _ = penthouse_program(vpm)
     ir = prog.to_bytes()
+    t_flat = time.perf_counter() - t_flat  # host: run the scene program and flatten it to PXIR
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
     s_ptr = stream.cuda_stream
@@ -410,6 +427,7 @@ def main():
         "mismatches": {"grid_cells": mism_grid, "pool_voxels": mism_vox, "pool_used": int(used) - int(o.pool_used)},
         "rescued": {"total": st["rescued"], "brick": st["rescued_brick"], "sub": st["rescued_sub"],
                     "voxel": st["rescued_voxel"], "polygon_test": st["rescued_polygon"],
+                    "paint": st["rescued_paint"],
                     "fraction_of_voxel_evals": round(st["rescued_voxel"] / max(st["voxel_evals"], 1), 6)},
         "max_abs_d32_minus_d64": st["max_abs_err32"],
         "e2e": {"value": round(e2e_value, 4), "unit": UNIT, "h2d_bytes_per_step": len(ir),
@@ -423,6 +441,8 @@ def main():
                      "peak_source": "measured here: dependent FFMA chains on all SMs (px_probe_peak)",
                      "fp64": ({"achieved": round(alg_ops / fold64_s / 1e12, 5), "peak": round(peak64, 3),
                                "frac": round(alg_ops / fold64_s / 1e12 / peak64, 5)} if have64 else None)},
+        "hbm": hbm_line(cfg, used, len(ir), t_mx),
+        "host_flatten_ms": round(t_flat * 1e3, 2),
         "cpu_baseline": cpu,
         "clocks": clocks,
         "gpu_launches": int(st["kernel_launches"]) * args.steps,

@@ -65,8 +65,8 @@ typedef struct px_stats {
   uint64_t violations;       /* validation mode: float64 results outside their float32 enclosure */
   uint64_t rescued_brick, rescued_sub, rescued_voxel;  /* rescues by level (mixed mode) */
   uint64_t rescued_polygon;  /* ... of which a polygon crossing test was undecided */
-  float classify_ms;         /* device time of the classify kernel alone */
-  float pad2;
+  float classify_ms;         /* device time of the classify and voxel kernels */
+  uint32_t rescued_paint;    /* mixed mode: paint calls the float32 path left to float64 */
 } px_stats;
 
 /* Device addresses of the world's buffers (valid until the next build or destroy). */

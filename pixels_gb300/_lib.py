@@ -59,7 +59,7 @@ class Stats(ctypes.Structure):
         ("fold_ms", ctypes.c_float), ("kernel_launches", ctypes.c_uint32), ("pad", ctypes.c_uint32),
         ("violations", ctypes.c_uint64), ("rescued_brick", ctypes.c_uint64), ("rescued_sub", ctypes.c_uint64),
         ("rescued_voxel", ctypes.c_uint64), ("rescued_polygon", ctypes.c_uint64),
-        ("classify_ms", ctypes.c_float), ("pad2", ctypes.c_float),
+        ("classify_ms", ctypes.c_float), ("rescued_paint", ctypes.c_uint32),
     ]
 
 

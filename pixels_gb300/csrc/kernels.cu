@@ -22,6 +22,7 @@
 #include "sdf64.cuh"
 #include "sdf32.cuh"
 #include "paint.cuh"
+#include "paint32.cuh"
 
 namespace px {
 
@@ -52,17 +53,28 @@ __device__ __forceinline__ bool box_overlaps_tile(uint2 b, int tx, int ty, int t
   return x0 <= tx * 4 + 3 && x1 >= tx * 4 && y0 <= ty * 4 + 3 && y1 >= ty * 4 && z0 <= tz * 4 + 3 && z1 >= tz * 4;
 }
 
+// The op boxes are followed by one union box per 32 consecutive ops: a warp
+// tests the 32-op groups first and only the ops of groups that overlap its
+// tile (a two-level culling hierarchy; scene ops come object by object, so
+// groups are compact).
 __global__ void __launch_bounds__(256) cull_count_kernel(const uint2* __restrict__ boxes, int n_ops, int TX, int TY, int TZ,
                                                          uint32_t* tile_cnt, uint32_t* tiles_nonempty, BuildResult* res) {
   const int lane = threadIdx.x & 31;
   const int n_tiles = TX * TY * TZ;
+  const int n_groups = (n_ops + 31) / 32;
+  const uint2* __restrict__ gboxes = boxes + n_ops;
   for (int tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; tile < n_tiles; tile += (gridDim.x * blockDim.x) >> 5) {
     int tz = tile / (TX * TY), r = tile - tz * TX * TY, ty = r / TX, tx = r - ty * TX;
     uint32_t cnt = 0;
-    for (int c0 = 0; c0 < n_ops; c0 += 32) {
-      int i = c0 + lane;
-      bool ov = i < n_ops && box_overlaps_tile(__ldg(boxes + i), tx, ty, tz);
-      cnt += __popc(__ballot_sync(FULLMASK, ov));
+    for (int g0 = 0; g0 < n_groups; g0 += 32) {
+      const int gi = g0 + lane;
+      uint32_t gm = __ballot_sync(FULLMASK, gi < n_groups && box_overlaps_tile(__ldg(gboxes + gi), tx, ty, tz));
+      while (gm) {
+        const int i = (g0 + __ffs(gm) - 1) * 32 + lane;
+        gm &= gm - 1;
+        bool ov = i < n_ops && box_overlaps_tile(__ldg(boxes + i), tx, ty, tz);
+        cnt += __popc(__ballot_sync(FULLMASK, ov));
+      }
     }
     if (lane == 0) {
       tile_cnt[tile] = cnt;
@@ -75,15 +87,22 @@ __global__ void __launch_bounds__(256) cull_fill_kernel(const uint2* __restrict_
                                                         const uint32_t* __restrict__ tile_off, uint32_t* tile_ops) {
   const int lane = threadIdx.x & 31;
   const int n_tiles = TX * TY * TZ;
+  const int n_groups = (n_ops + 31) / 32;
+  const uint2* __restrict__ gboxes = boxes + n_ops;
   for (int tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; tile < n_tiles; tile += (gridDim.x * blockDim.x) >> 5) {
     int tz = tile / (TX * TY), r = tile - tz * TX * TY, ty = r / TX, tx = r - ty * TX;
     uint32_t pos = tile_off[tile];
-    for (int c0 = 0; c0 < n_ops; c0 += 32) {
-      int i = c0 + lane;
-      bool ov = i < n_ops && box_overlaps_tile(__ldg(boxes + i), tx, ty, tz);
-      uint32_t m = __ballot_sync(FULLMASK, ov);
-      if (ov) tile_ops[pos + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
-      pos += __popc(m);
+    for (int g0 = 0; g0 < n_groups; g0 += 32) {
+      const int gi = g0 + lane;
+      uint32_t gm = __ballot_sync(FULLMASK, gi < n_groups && box_overlaps_tile(__ldg(gboxes + gi), tx, ty, tz));
+      while (gm) {
+        const int i = (g0 + __ffs(gm) - 1) * 32 + lane;
+        gm &= gm - 1;
+        bool ov = i < n_ops && box_overlaps_tile(__ldg(boxes + i), tx, ty, tz);
+        uint32_t m = __ballot_sync(FULLMASK, ov);
+        if (ov) tile_ops[pos + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
+        pos += __popc(m);
+      }
     }
   }
 }
@@ -390,18 +409,118 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
   }
 }
 
+// Paint calls of the heavy paint kinds, ahead of the apply pass: one 4^3
+// sub-block of one (op, brick) pair per warp pass, two voxels per lane, every
+// voxel the op's shape covers (whether the reference then paints it depends on
+// the world's state, which fold_kernel knows).  Values go to the pair's slot in
+// voxel index order.  Spreading these calls over the whole GPU keeps one
+// warp from evaluating a painted brick's 512 calls alone.  Mixed mode tries the
+// certified float32 evaluation first (paint32.cuh).
+template <int MODE>
+__global__ void __launch_bounds__(256) paint_kernel(FoldArgs a) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t n_items = a.n_paint_slots * 8u;
+  uint32_t resc = 0, viol = 0;
+  for (;;) {
+    uint32_t it = 0;
+    if (lane == 0) it = atomicAdd(a.paint_counter, 1u);
+    it = __shfl_sync(FULLMASK, it, 0);
+    if (it >= n_items) break;
+    const uint32_t slot = it >> 3;
+    const int s = (int)(it & 7u);
+    int lo = 0, hi = (int)a.n_heavy - 1;  // last heavy op whose first slot <= slot
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(a.heavy_slot + mid) <= slot) lo = mid; else hi = mid - 1;
+    }
+    const OpDev* O = a.ops + __ldg(a.heavy_op + lo);
+    const unsigned long long pair = O->pair_base + (slot - O->paint_slot);
+    const int cls = __ldg(a.pcode + pair);
+    if (cls == PC_SKIP) continue;
+    unsigned long long m = ~0ull;
+    if (cls != PC_FULL) {
+      const uint32_t c = (__ldg(a.psub + pair) >> (2 * s)) & 3u;
+      m = c == PC_FULL ? ~0ull : c == PC_PARTIAL ? __ldg(a.pmask + pair * 8 + s) : 0ull;
+    }
+    if (!m) continue;
+    int bx, by, bz;
+    brick_of_pair(O, pair, bx, by, bz);
+    const uint32_t pk = O->paint_kind;
+    const double* pp = a.params + O->paint_off;
+    const bool try32 = MODE == 1 && O->paint32_off != NO_SLOT;
+    Iv bo[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    if (try32) brick_bases(a, O, bx, by, bz, bo);
+#pragma unroll 1
+    for (int r = 0; r < 2; r++) {
+      const int e = r * 32 + lane;
+      if (!((m >> e) & 1ull)) continue;
+      const int lx = (s & 1) * 4 + (e & 3), ly = ((s >> 1) & 1) * 4 + ((e >> 2) & 3), lz = ((s >> 2) & 1) * 4 + (e >> 4);
+      uint32_t v = 0, st = 0;
+      bool done = false;
+      if (try32) {
+        done = paint32(pk, a.p32 + O->paint32_off, iadd(bo[0], koff((float)lx, a.vs_lo, a.vs_hi)),
+                       iadd(bo[1], koff((float)ly, a.vs_lo, a.vs_hi)), iadd(bo[2], koff((float)lz, a.vs_lo, a.vs_hi)), v);
+        if (!done) resc++;
+      }
+      if (!done || a.validate) {
+        double PX = (bx * 8 + lx + 0.5) * a.vs, PY = (by * 8 + ly + 0.5) * a.vs, PZ = (bz * 8 + lz + 0.5) * a.vs;
+        if (O->flags & OPF_PAINT_FRAME) {  // localPaint (penthouse.ts:88-91)
+          const double fpx = O->frame[0], fpz = O->frame[1], c = O->frame[2], sn = O->frame[3];
+          const double dx = PX - fpx, dz = PZ - fpz;
+          PX = fpx + c * dx + sn * dz;
+          PZ = fpz - sn * dx + c * dz;
+        }
+        if (!done) v = paint_eval(pk, pp, PX, PY, PZ, st);
+        if (a.validate && v != paint_eval_cr(pk, pp, PX, PY, PZ, st)) viol++;
+      }
+      a.pvals[(size_t)slot * 512 + (uint32_t)(lx | (ly << 3) | (lz << 6))] = (v & 0xffffu) | (st & ST_RANGE ? PV_RANGE : 0u);
+    }
+  }
+#pragma unroll
+  for (int o2 = 16; o2; o2 >>= 1) {
+    resc += __shfl_xor_sync(FULLMASK, resc, o2);
+    viol += __shfl_xor_sync(FULLMASK, viol, o2);
+  }
+  if (lane == 0) {
+    if (resc) atomicAdd(&a.res->c.resc_paint, (unsigned long long)resc);
+    if (viol) atomicAdd(&a.res->c.violations, (unsigned long long)viol);
+  }
+}
+
+// One paint call at voxel (x, y, z) of the world, in float64 (the paint kinds
+// that paint_kernel does not evaluate ahead).  Out of line, so that the apply
+// loop holds no float64 values.  Returns the value (a u16 for these kinds) with
+// PV_RANGE for a range error and PV_VIOL for a validation mismatch.
+constexpr uint32_t PV_VIOL = 0x40000000u;
+__device__ __noinline__ uint32_t paint_at_voxel(const double* __restrict__ params, double vs, int validate,
+                                                const OpDev* O, int x, int y, int z) {
+  double PX = (x + 0.5) * vs, PY = (y + 0.5) * vs, PZ = (z + 0.5) * vs;
+  if (O->flags & OPF_PAINT_FRAME) {  // localPaint (penthouse.ts:88-91)
+    const double fpx = O->frame[0], fpz = O->frame[1], c = O->frame[2], sn = O->frame[3];
+    const double dx = PX - fpx, dz = PZ - fpz;
+    PX = fpx + c * dx + sn * dz;
+    PZ = fpz - sn * dx + c * dz;
+  }
+  uint32_t st = 0;
+  const uint32_t v = paint_eval(O->paint_kind, params + O->paint_off, PX, PY, PZ, st);
+  const bool viol = validate && v != paint_eval_cr(O->paint_kind, params + O->paint_off, PX, PY, PZ, st);
+  return (v & 0xffffu) | (st & ST_RANGE ? PV_RANGE : 0u) | (viol ? PV_VIOL : 0u);
+}
+
 // Lane layout of a brick in registers: lane owns the voxel pair
 // (x0, y, z) / (x0 + 1, y, z) with x0 = 2 (lane & 3), y = lane >> 2, in
 // register j = z.  Voxel index li = x | y << 3 | z << 6 (VoxelWorld.ts:60), so
 // register j of the warp is the contiguous 128-byte slice pool[64 j .. 64 j + 63].
 // The warp applies its brick's ops in order, as apply() does (shapes.ts:367-412),
 // using the pair classifications.
+// INLINE: some painted op has no paint slot (paint values past the slot
+// budget), so paint calls happen here too; otherwise the apply loop calls nothing.
+template <bool INLINE>
 __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
   __shared__ unsigned long long smask[8][8];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const int lx0 = (lane & 3) * 2, ly = lane >> 2;
-  const double vs = a.vs;
   WarpCounters wc = {0, 0, 0, 0, 0};
   uint32_t paint_calls = 0, paint_viol = 0;
   uint32_t st_local = 0;
@@ -519,17 +638,23 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
             uint32_t next;
             if (kind == KIND_CARVE) next = 0;
             else if (kind == KIND_PAINT && cur == 0) continue;
-            else if (!constPaint) {
-              double PX = (ox + lx0 + h + 0.5) * vs, PY = (oy + ly + 0.5) * vs, PZ = (oz + j + 0.5) * vs;
-              if (flags & OPF_PAINT_FRAME) {  // localPaint (penthouse.ts:88-91)
-                const double fpx = O->frame[0], fpz = O->frame[1], c = O->frame[2], sn = O->frame[3];
-                double dx = PX - fpx, dz = PZ - fpz;
-                PX = fpx + c * dx + sn * dz;
-                PZ = fpz - sn * dx + c * dz;
-              }
-              next = paint_eval(pk, a.params + O->paint_off, PX, PY, PZ, st_local);
-              if (a.validate && next != paint_eval_cr(pk, a.params + O->paint_off, PX, PY, PZ, st_local)) paint_viol++;
+            else if (!constPaint && O->paint_slot != NO_SLOT) {  // evaluated by paint_kernel
+              const uint32_t pvv = __ldg(a.pvals + (size_t)(O->paint_slot + (uint32_t)(pair - O->pair_base)) * 512 +
+                                         (uint32_t)((lx0 + h) | (ly << 3) | (j << 6)));
+              if (pvv & PV_RANGE) st_local |= ST_RANGE;
+              next = pvv & 0xffffu;
               paint_calls++;
+            } else if (!constPaint) {
+              if constexpr (INLINE) {
+                const uint32_t pv2 = paint_at_voxel(a.params, a.vs, a.validate, O, ox + lx0 + h, oy + ly, oz + j);
+                if (pv2 & PV_RANGE) st_local |= ST_RANGE;
+                if (pv2 & PV_VIOL) paint_viol++;
+                next = pv2 & 0xffffu;
+                paint_calls++;
+              } else {  // every painted op has a slot in this build
+                st_local |= ST_CHAIN;
+                next = cur;
+              }
             } else next = pv;
             if (next != cur) {  // Uint16Array store; the comparison uses the unstored value
               vox[j] = (vox[j] & ~(0xffffu << (16 * h))) | ((next & 0xffffu) << (16 * h));
@@ -617,8 +742,13 @@ void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEve
     ++g_launches; classify_kernel<0><<<n_sms * PX_CLASSIFY64_MINB, 256, 0, s>>>(a);
     ++g_launches; voxel_kernel<0><<<n_sms * PX_CLASSIFY64_MINB, 256, 0, s>>>(a);
   }
+  if (a.n_paint_slots) {
+    if (mode == 1) { ++g_launches; paint_kernel<1><<<n_sms * 4, 256, 0, s>>>(a); }
+    else { ++g_launches; paint_kernel<0><<<n_sms * 4, 256, 0, s>>>(a); }
+  }
   if (mid) cudaEventRecord(mid, s);
-  ++g_launches; fold_kernel<<<n_sms * PX_FOLD_MINB, 256, 0, s>>>(a);
+  if (a.inline_paints) { ++g_launches; fold_kernel<true><<<n_sms * PX_FOLD_MINB, 256, 0, s>>>(a); }
+  else { ++g_launches; fold_kernel<false><<<n_sms * PX_FOLD_MINB, 256, 0, s>>>(a); }
 }
 
 // ---------------------------------------------------------------------------
@@ -986,33 +1116,68 @@ __global__ void __launch_bounds__(256) finalize_kernel(FinalizeArgs a) {
   }
   const int lane = threadIdx.x & 31;
   const uint32_t n = a.res->touched_count;
-  for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < n; t += (gridDim.x * blockDim.x) >> 5) {
-    const uint2 e = a.touched[t];
-    if (!(e.y & TAG_STAGED) || (e.y & UNIFORM)) {
-      if (lane == 0) a.grid[e.x] = e.y;
-      continue;
+  // 32 touched bricks per warp pass: each lane resolves one brick's pool index
+  // (a chain of dependent loads, so 32 chains in flight), then the warp copies
+  // the staged bricks four at a time (eight 16-byte loads in flight per lane)
+  const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; base < n; base += n_warps * 32) {
+    const uint32_t t = base + lane;
+    uint32_t cell = 0, slot = 0, idx = 0;
+    bool staged = false;
+    if (t < n) {
+      const uint2 e = a.touched[t];
+      cell = e.x;
+      if (!(e.y & TAG_STAGED) || (e.y & UNIFORM)) {
+        a.grid[e.x] = e.y;
+      } else {
+        slot = e.y & 0x3fffffffu;
+        const long long src = a.stage_src[slot];
+        if (src >= 0) {
+          const unsigned long long w = a.ew[a.H + a.pos[src]];
+          if (!(w & KNOWN)) atomicOr(&a.res->status, (uint32_t)ST_CHAIN);
+          else { idx = (uint32_t)(w & 0xffffffffull); staged = true; }
+        } else {
+          idx = (uint32_t)(-(src + 1));
+          staged = true;
+        }
+      }
     }
-    const uint32_t slot = e.y & 0x3fffffffu;
-    const long long src = a.stage_src[slot];
-    uint32_t idx;
-    if (src >= 0) {
-      unsigned long long w = a.ew[a.H + a.pos[src]];
-      if (!(w & KNOWN)) { if (lane == 0) atomicOr(&a.res->status, (uint32_t)ST_CHAIN); continue; }
-      idx = (uint32_t)(w & 0xffffffffull);
-    } else {
-      idx = (uint32_t)(-(src + 1));
+    uint32_t mx = staged ? idx : 0u;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) mx = max(mx, __shfl_xor_sync(FULLMASK, mx, o));
+    if (lane == 0 && mx) atomicMax(&a.res->max_pool_index, mx);
+    if (staged) a.grid[cell] = idx + 1;
+    uint32_t sm = __ballot_sync(FULLMASK, staged);
+    while (sm) {
+      int src_l[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        src_l[q] = -1;
+        if (sm) { src_l[q] = __ffs(sm) - 1; sm &= sm - 1; }
+      }
+      uint4 v[4][2];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        if (src_l[q] < 0) continue;
+        const uint32_t sl = __shfl_sync(FULLMASK, slot, src_l[q]);
+        const uint4* s4 = reinterpret_cast<const uint4*>(a.staging32 + (size_t)sl * 256);
+        v[q][0] = s4[lane];
+        v[q][1] = s4[lane + 32];
+      }
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        if (src_l[q] < 0) continue;
+        const uint32_t di = __shfl_sync(FULLMASK, idx, src_l[q]);
+        uint4* d4 = reinterpret_cast<uint4*>(a.pool32 + (size_t)di * 256);
+        d4[lane] = v[q][0];
+        d4[lane + 32] = v[q][1];
+      }
     }
-    if (lane == 0) atomicMax(&a.res->max_pool_index, idx);
-    const uint4* s4 = reinterpret_cast<const uint4*>(a.staging32 + (size_t)slot * 256);
-    uint4* d4 = reinterpret_cast<uint4*>(a.pool32 + (size_t)idx * 256);
-    d4[lane] = s4[lane];
-    d4[lane + 32] = s4[lane + 32];
-    if (lane == 0) a.grid[e.x] = idx + 1;
   }
 }
 
 void launch_finalize(const FinalizeArgs& a, uint32_t touched_cap, cudaStream_t s) {
-  size_t warps = touched_cap ? touched_cap : 1;
+  size_t warps = touched_cap ? (touched_cap + 31) / 32 : 1;
   size_t b = (warps * 32 + 255) / 256;
   int blocks = (int)(b < 8192 ? b : 8192);
   ++g_launches; finalize_kernel<<<blocks, 256, 0, s>>>(a);

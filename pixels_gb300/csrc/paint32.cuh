@@ -1,0 +1,101 @@
+// Mixed mode: certified float32 evaluation of the two paints with the most
+// calls in the penthouse, tufted leather (penthouse.ts:495-501) and the
+// painting (penthouse.ts:840-845).  Every float64 value the reference forms is
+// enclosed in a float32 interval with directed rounding; an interval is widened
+// by 2^-23 of its magnitude for each float64 rounding the reference applies
+// (at most 2^-53 relative).  A decision (Math.round, a parity, a threshold) is
+// taken from the intervals only when it cannot differ from the reference's;
+// otherwise the call returns false and the float64 evaluation decides.
+//
+// Math.hypot(a, b) is computed by the engine from m = max(|a|, |b|) as
+// sqrt(1 + (min/m)^2) * m with one division, one square, one compensated sum,
+// one square root and one product: at most 4 roundings of 2^-53, so within
+// 2^-50 relative of sqrt(a^2 + b^2); the intervals use 2^-22.
+// Math.sin(t) is enclosed from sinf at a point m of t's interval: CUDA's
+// sinf has a documented maximum error of 2 ulp (at most 2^-22 for results in
+// [-1, 1]) and sin is 1-Lipschitz, so |sin(t) - sinf(m)| <= |t - m| + 2^-22;
+// the enclosure uses the interval's full width plus 2^-21.
+#pragma once
+#include "px_internal.cuh"
+#include "sdf32.cuh"
+
+namespace px {
+
+// one float64 rounding of a value in the interval (relative 2^-53 <= 2^-23)
+__device__ __forceinline__ Iv r64(Iv v) {
+  return {__fsub_rd(v.lo, __fmul_ru(fabsf(v.lo), 0x1p-23f)), __fadd_ru(v.hi, __fmul_ru(fabsf(v.hi), 0x1p-23f))};
+}
+__device__ __forceinline__ Iv ivf(float2 f) { return {f.x, f.y}; }
+
+// Math.hypot(a, b) < thr, thr enclosed as [thr.x, thr.y]: 1 true, 0 false, 2 undecided
+__device__ __forceinline__ int hypot_lt32(Iv a, Iv b, float2 thr) {
+  const Iv t = ilen2(a, b);
+  const float hi = __fmul_ru(t.hi, 1.0f + 0x1p-22f), lo = __fmul_rd(t.lo, 1.0f - 0x1p-22f);
+  if (hi < thr.x) return 1;
+  if (lo >= thr.y) return 0;
+  return 2;
+}
+
+// Math.round of a value in u: the integer, or NAN when undecided
+__device__ __forceinline__ float round32(Iv u) {
+  const float a = floorf(__fadd_rd(u.lo, 0.5f)), b = floorf(__fadd_ru(u.hi, 0.5f));
+  return a == b ? a : __int_as_float(0x7fc00000);
+}
+
+__device__ __forceinline__ uint32_t vox32(float mat, float shade) {
+  return ((uint32_t)(int)mat & 0xffu) | (((uint32_t)(int)shade & 0xffu) << 8);
+}
+
+// Float32 parameter blocks (written by the host, paint_params32 in px_api.cu),
+// positions relative to the op's anchor:
+//   tufted:   [0] z0, [1] floor, [2] 1/0.16, [3] 0.12, [4] (material, 0)
+//   painting: [0] (9 ax + 3 ay) mod 2 pi, [1] 1.3, [2] 0.06, [3] (material, 0),
+//             [4 + 4i] blob x, [5 + 4i] blob y, [6 + 4i] blob r, [7 + 4i] (shade, 0)
+// (rx, ry, rz): the voxel centre relative to the anchor.
+__device__ __forceinline__ bool paint32(uint32_t kind, const float2* __restrict__ q, Iv rx, Iv ry, Iv rz,
+                                        uint32_t& out) {
+  if (kind == PK_TUFTED) {
+    const Iv inv = ivf(__ldg(q + 2));
+    const Iv u = r64(icmul(r64(isub(rz, ivf(__ldg(q + 0)))), inv));  // (z - z0) / 0.16
+    const Iv v = r64(icmul(r64(isub(ry, ivf(__ldg(q + 1)))), inv));  // (y - floor) / 0.16
+    const float nu = round32(u), nv = round32(v);
+    if (nu != nu || nv != nv) return false;
+    const float mat = __ldg(q + 4).x;
+    if (((int)nu + (int)nv) & 1) { out = vox32(mat, 0.f); return true; }  // (ru + rv) % 2 != 0
+    const Iv du = {__fsub_rd(u.lo, nu), __fsub_ru(u.hi, nu)}, dv = {__fsub_rd(v.lo, nv), __fsub_ru(v.hi, nv)};
+    const int h = hypot_lt32(du, dv, __ldg(q + 3));
+    if (h == 2) return false;
+    out = vox32(mat, h ? 200.f : 0.f);
+    return true;
+  }
+  if (kind == PK_PAINTING) {
+    const Iv k13 = ivf(__ldg(q + 1));
+    float shade = 0.f;
+#pragma unroll 1
+    for (int i = 0; i < 9; i++) {
+      const float2* b = q + 4 + 4 * i;
+      const Iv a = r64(isub(rx, ivf(__ldg(b))));                    // x - bx
+      const Iv c = r64(icmul(r64(isub(ry, ivf(__ldg(b + 1)))), k13));  // (y - by) * 1.3
+      const int h = hypot_lt32(a, c, __ldg(b + 2));
+      if (h == 2) return false;
+      if (h) shade = __ldg(b + 3).x;
+    }
+    // x * 9 + y * 3, reduced by a multiple of 2 pi (exact for the real value)
+    Iv t = iadd(ivf(__ldg(q + 0)), iadd(icmul(rx, iv(9.f)), icmul(ry, iv(3.f))));
+    t = {__fsub_rd(t.lo, 0x1p-40f), __fadd_ru(t.hi, 0x1p-40f)};  // the reference's roundings of x*9 + y*3
+    const float m = fminf(fmaxf(0.5f * (t.lo + t.hi), t.lo), t.hi);
+    const float sm = sinf(m);
+    const float r = __fadd_ru(__fsub_ru(t.hi, t.lo), 0x1p-21f);
+    const Iv s = iabs(Iv{__fsub_rd(sm, r), __fadd_ru(sm, r)});
+    const float2 thr = __ldg(q + 2);
+    bool stripe;
+    if (s.hi < thr.x) stripe = true;
+    else if (s.lo >= thr.y) stripe = false;
+    else return false;
+    out = vox32(__ldg(q + 3).x, stripe ? 255.f : shade);
+    return true;
+  }
+  return false;
+}
+
+}  // namespace px

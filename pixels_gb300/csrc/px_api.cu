@@ -45,7 +45,7 @@ struct px_world {
   std::vector<uint2> last_boxes, last_code;
   std::vector<double> last_params;
   bool ops_resident = false;   // the device op tables already hold `ops`
-  std::vector<uint2> boxes;
+  std::vector<uint2> boxes, h_boxes;  // h_boxes: boxes + 32-op group boxes as uploaded
   std::vector<uint2> code;
   std::vector<double> params;
   std::vector<uint32_t> code32, last_code32;   // per instruction: float32 parameter offset
@@ -62,6 +62,8 @@ struct px_world {
   uint64_t stage_hint = 0;      // staging slots the next build reserves (grown on overflow)
   DevBuf chunk_op, pcode, psub, pmask, chunk_counter, vitems;
   std::vector<uint32_t> h_chunk_op;
+  DevBuf heavy, pvals;          // heavy-paint ops (op index, first slot) and their paint values
+  std::vector<uint32_t> h_heavy;
   DevBuf scan_agg;
   DevBuf work_counter;
   DevBuf res;
@@ -369,7 +371,7 @@ void px_world_destroy(px_world* w) {
                     &w->ew, &w->depth_fn, &w->depth, &w->tree, &w->fresh, &w->fresh_rank, &w->staging, &w->touched,
                     &w->stage_cell, &w->stage_src, &w->chunk_op, &w->pcode, &w->psub, &w->pmask,
                     &w->chunk_counter, &w->vitems, &w->scan_agg, &w->work_counter, &w->res, &w->opaque,
-                    &w->udens, &w->super_counts, &w->density};
+                    &w->udens, &w->super_counts, &w->density, &w->heavy, &w->pvals};
   for (DevBuf* b : bufs) release(*b);
   if (w->h_res) cudaFreeHost(w->h_res);
   if (w->ev0) cudaEventDestroy(w->ev0);
@@ -378,6 +380,51 @@ void px_world_destroy(px_world* w) {
   if (w->ev_fold1) cudaEventDestroy(w->ev_fold1);
   if (w->ev_mid) cudaEventDestroy(w->ev_mid);
   delete w;
+}
+
+// Float32 parameters of the certified paint evaluation (paint32.cuh) for one
+// op, relative to its anchor A.  Returns false (float64 only) for a paint
+// frame or values outside the certified range.
+bool paint_params32(uint32_t kind, bool framed, const double* p, const double A[3], std::vector<float2>& out) {
+  if (framed || (kind != PK_TUFTED && kind != PK_PAINTING)) return false;
+  bool ok = true;
+  auto put = [&](float2 e, double v) {
+    if (!std::isfinite(e.x) || !std::isfinite(e.y) || std::fabs(v) > MIXED_MAX_COORD) ok = false;
+    out.push_back(e);
+  };
+  auto pos = [&](double v, int axis) {  // v - A[axis], enclosing the real difference
+    const double r = v - A[axis];
+    put(enc(r, (std::fabs(v) + std::fabs(A[axis])) * 0x1p-52), v);
+  };
+  auto thr = [&](double v) { put(make_float2(rd32(v), ru32(v)), v); };
+  auto intv = [&](double v) {  // a value the reference converts with (x & 0xff) after truncation
+    put(make_float2((float)((long long)v & 0xff), 0.f), 0.0);
+  };
+  if (kind == PK_TUFTED) {  // penthouse.ts:495-501
+    pos(p[0], 2);
+    pos(p[1], 1);
+    const double r = 1.0 / 0.16;  // the real 1/0.16 (float64 0.16) lies within 2^-53 of r
+    put(enc(r, r * 0x1p-52), r);
+    thr(0.12);
+    intv(p[2]);
+  } else {  // penthouse.ts:840-845
+    const long double K = 9.0L * (long double)A[0] + 3.0L * (long double)A[1];
+    const long double k = std::floor(K / (2.0L * 3.14159265358979323846264338327950288L) + 0.5L);
+    const long double Kr = K - k * (2.0L * 3.14159265358979323846264338327950288L);
+    put(enc((double)Kr, 0x1p-40), 0.0);  // generous pad for the reduction's rounding
+    const double k13 = 1.3;
+    put(enc(k13, 0.0), k13);
+    thr(0.06);
+    intv(p[0]);
+    for (int i = 0; i < 9; i++) {
+      const double* b = p + 1 + 4 * i;
+      pos(b[0], 0);
+      pos(b[1], 1);
+      thr(b[2]);
+      intv(b[3]);
+    }
+  }
+  return ok;
 }
 
 int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
@@ -416,6 +463,12 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
       if ((size_t)o.paint_param + np > n_params) return fail(w, PX_E_INVALID_IR, "op %zu: paint parameters out of range", i);
       for (size_t k = 0; k < np; k++)
         if (!std::isfinite(P[o.paint_param + k])) return fail(w, PX_E_INVALID_IR, "op %zu: non-finite paint parameter", i);
+      if (o.paint_kind == PK_NOISE)  // its two results are voxel values (u16), like every other paint's
+        for (int k = 6; k < 8; k++) {
+          const double v = P[o.paint_param + k];
+          if (!(v >= 0 && v <= 65535 && v == std::floor(v)))
+            return fail(w, PX_E_INVALID_IR, "op %zu: noise paint values must be integers in [0, 65535]", i);
+        }
     }
     for (int k = 0; k < 3; k++)
       if (!std::isfinite(o.mn[k]) || !std::isfinite(o.mx[k])) return fail(w, PX_E_INVALID_IR, "op %zu: non-finite bounds", i);
@@ -559,6 +612,15 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
       if ((double)w->dy * vs > ext) ext = (double)w->dy * vs;
       if ((double)w->dz * vs > ext) ext = (double)w->dz * vs;
       if (!ok32 || ext > MIXED_MAX_COORD) d.flags |= OPF_FP64_ONLY;
+      d.paint_slot = NO_SLOT;
+      d.paint32_off = NO_SLOT;
+      if (!(d.flags & OPF_FP64_ONLY) && o.kind != KIND_CARVE && paint_is_heavy(o.paint_kind)) {
+        const size_t at = n32_p.size();
+        if (paint_params32(o.paint_kind, (o.flags & OPF_PAINT_FRAME) != 0, P.data() + o.paint_param, d.anchor, n32_p))
+          d.paint32_off = (uint32_t)(w->p32.size() + at);
+        else
+          n32_p.resize(at);
+      }
       // code32 entries are relative to this op's code; rebase onto the world's arrays
       for (size_t k = c32_before; k < n32_code.size(); k++) n32_code[k] += (uint32_t)(w->p32.size());
       (void)p32_before;
@@ -599,6 +661,34 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
     tile_pairs += tx * ty * tz;
   }
   if (P > 0x1fffffffull) return fail(w, PX_E_QUEUE_OVERFLOW, "too many (op, brick) pairs in one build: %llu", (unsigned long long)P);
+  // paint slots (one per (op, brick) pair of a painted op, 2 KiB each): every
+  // painted op when they fit in 512 MiB, else the heavy kinds alone when they
+  // fit, else none; ops without a slot have their paints called by the apply pass
+  uint64_t n_slots = 0;
+  bool inline_paints = false;
+  for (int tier = 0; tier < 3; tier++) {
+    n_slots = 0;
+    inline_paints = false;
+    w->h_heavy.clear();
+    for (int i = 0; i < n_ops; i++) {
+      OpDev& o = w->ops[i];
+      o.paint_slot = NO_SLOT;
+      if (o.bx0 > o.bx1 || o.kind == KIND_CARVE || o.paint_kind == PK_CONST) continue;
+      if (tier == 2 || (tier == 1 && !paint_is_heavy(o.paint_kind))) { inline_paints = true; continue; }
+      const uint64_t np = (uint64_t)o.nx * o.ny * (uint64_t)(o.bz1 - o.bz0 + 1);
+      o.paint_slot = (uint32_t)n_slots;
+      w->h_heavy.push_back((uint32_t)i);
+      w->h_heavy.push_back((uint32_t)n_slots);
+      n_slots += np;
+    }
+    if (n_slots * 2048 <= (512ull << 20)) break;
+  }
+  const uint32_t n_heavy = (uint32_t)(w->h_heavy.size() / 2);
+  {  // (op indices, then first slots) as two arrays
+    std::vector<uint32_t> t(w->h_heavy.size());
+    for (uint32_t k = 0; k < n_heavy; k++) { t[k] = w->h_heavy[2 * k]; t[n_heavy + k] = w->h_heavy[2 * k + 1]; }
+    w->h_heavy.swap(t);
+  }
   const uint64_t touched_bound = P < w->ncells ? P : w->ncells;
   const uint32_t H = w->n_holes, U0 = w->pool_used;
   const size_t E_max = (size_t)H + 2 * P;
@@ -612,7 +702,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   // scratch (a reallocated op table loses its resident copy)
   const void* op_bufs_before[7] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p, w->d_p32.p, w->d_bases.p};
   if ((rc = ensure(w, w->d_ops, sizeof(OpDev) * (size_t)n_ops)) ||
-      (rc = ensure(w, w->d_boxes, sizeof(uint2) * (size_t)n_ops)) ||
+      (rc = ensure(w, w->d_boxes, sizeof(uint2) * ((size_t)n_ops + (n_ops + 31) / 32))) ||
       (rc = ensure(w, w->d_code, sizeof(uint2) * w->code.size())) ||
       (rc = ensure(w, w->d_params, sizeof(double) * w->params.size())) ||
       (rc = ensure(w, w->d_code32, sizeof(uint32_t) * w->code32.size())) ||
@@ -630,7 +720,8 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
       (rc = ensure(w, w->work_counter, 16)) || (rc = ensure(w, w->res, sizeof(BuildResult))) ||
       (rc = ensure(w, w->chunk_op, 4 * ((P + 31) / 32))) || (rc = ensure(w, w->pcode, P)) ||
       (rc = ensure(w, w->psub, 2 * P)) || (rc = ensure(w, w->pmask, 64 * P)) || (rc = ensure(w, w->chunk_counter, 16)) ||
-      (rc = ensure(w, w->vitems, 8 * 8 * P)))
+      (rc = ensure(w, w->vitems, 8 * 8 * P)) || (rc = ensure(w, w->heavy, 4 * w->h_heavy.size() + 4)) ||
+      (rc = ensure(w, w->pvals, 2048 * n_slots + 4)))
     return rc;
   {
     size_t items = w->ntiles > E_max ? w->ntiles : E_max;
@@ -652,7 +743,26 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   CU(cudaEventRecord(w->ev0, s));
   if (!w->ops_resident) {
     CU(cudaMemcpyAsync(w->d_ops.p, w->ops.data(), sizeof(OpDev) * (size_t)n_ops, cudaMemcpyHostToDevice, s));
-    CU(cudaMemcpyAsync(w->d_boxes.p, w->boxes.data(), sizeof(uint2) * (size_t)n_ops, cudaMemcpyHostToDevice, s));
+    {  // op boxes, then the union box of every 32 consecutive ops (cull_count_kernel)
+      const int n_groups = (n_ops + 31) / 32;
+      w->h_boxes.assign(w->boxes.begin(), w->boxes.end());
+      for (int g = 0; g < n_groups; g++) {
+        uint32_t lo[3] = {1023, 1023, 1023}, hi[3] = {0, 0, 0};
+        bool any = false;
+        for (int i = g * 32; i < n_ops && i < g * 32 + 32; i++) {
+          const uint2 b = w->boxes[i];
+          if (b.x >> 30) continue;
+          any = true;
+          for (int k = 0; k < 3; k++) {
+            lo[k] = std::min(lo[k], (b.x >> (10 * k)) & 1023u);
+            hi[k] = std::max(hi[k], (b.y >> (10 * k)) & 1023u);
+          }
+        }
+        w->h_boxes.push_back(any ? make_uint2(lo[0] | (lo[1] << 10) | (lo[2] << 20), hi[0] | (hi[1] << 10) | (hi[2] << 20))
+                                 : make_uint2(3u << 30, 0u));
+      }
+      CU(cudaMemcpyAsync(w->d_boxes.p, w->h_boxes.data(), sizeof(uint2) * w->h_boxes.size(), cudaMemcpyHostToDevice, s));
+    }
     CU(cudaMemcpyAsync(w->d_code.p, w->code.data(), sizeof(uint2) * w->code.size(), cudaMemcpyHostToDevice, s));
     CU(cudaMemcpyAsync(w->d_params.p, w->params.data(), sizeof(double) * w->params.size(), cudaMemcpyHostToDevice, s));
     if (!w->code32.empty()) {
@@ -677,6 +787,8 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
     if (n_chunks) CU(cudaMemcpyAsync(w->chunk_op.p, w->h_chunk_op.data(), 4 * n_chunks, cudaMemcpyHostToDevice, s));
   }
   if (P) CU(cudaMemsetAsync(w->evt.p, 0, P, s));
+  if (n_heavy)
+    CU(cudaMemcpyAsync(w->heavy.p, w->h_heavy.data(), 4 * w->h_heavy.size(), cudaMemcpyHostToDevice, s));
 
   BuildResult* res = (BuildResult*)w->res.p;
   ScanTemp st{w->scan_agg.p, w->scan_agg.bytes / 8};
@@ -696,6 +808,13 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   fa.vitems = (uint2*)w->vitems.p;
   fa.vitems_cap = (uint32_t)(8 * P < 0xffffffffull ? 8 * P : 0xffffffffull);
   fa.vitem_counter = (uint32_t*)w->chunk_counter.p + 2;
+  fa.paint_counter = (uint32_t*)w->chunk_counter.p + 1;
+  fa.n_paint_slots = (uint32_t)n_slots;
+  fa.n_heavy = n_heavy;
+  fa.heavy_op = (const uint32_t*)w->heavy.p;
+  fa.heavy_slot = (const uint32_t*)w->heavy.p + n_heavy;
+  fa.pvals = (uint32_t*)w->pvals.p;
+  fa.inline_paints = inline_paints ? 1 : 0;
   fa.ops = (const OpDev*)w->d_ops.p;
   fa.code = (const uint2*)w->d_code.p;
   fa.params = (const double*)w->d_params.p;
@@ -806,6 +925,7 @@ int px_build_finish(px_world* w) {
   w->stats.rescued_sub = r.c.resc_sub;
   w->stats.rescued_voxel = r.c.resc_vox;
   w->stats.rescued_polygon = r.c.resc_poly;
+  w->stats.rescued_paint = (uint32_t)r.c.resc_paint;
   w->stats.build_ms = ms;
   w->stats.status = r.status;
   // transactional retries: nothing was committed

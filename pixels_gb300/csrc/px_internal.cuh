@@ -82,14 +82,28 @@ struct OpDev {
   // OPF_BOX_RANGES (a lone axis-aligned box): per axis, the first and last voxel
   // whose centre the reference's float64 box SDF puts inside on that axis
   int32_t vr[6];                         // x lo, x hi, y lo, y hi, z lo, z hi (empty: lo > hi)
-  int32_t pad3[2];
+  // paints evaluated ahead of the apply pass (paint_kernel): the op's first
+  // paint slot (one slot of 512 values per (op, brick) pair), or NO_SLOT
+  uint32_t paint_slot;
+  // mixed mode: float32 parameters of the certified paint evaluation (p32 index), or NO_SLOT
+  uint32_t paint32_off;
 };
+constexpr uint32_t NO_SLOT = 0xffffffffu;
+// paint kinds whose calls are the most expensive (transcendentals, Math.hypot):
+// chip stack, tufted, vase, painting.  Their calls are evaluated ahead of the
+// apply pass whenever the slots fit; the other kinds when all painted ops fit.
+__host__ __device__ constexpr bool paint_is_heavy(uint32_t k) {
+  return k == PK_CHIP || k == PK_TUFTED || k == PK_VASE || k == PK_PAINTING;
+}
+// a precomputed paint value with a paint argument out of range (ST_RANGE)
+constexpr uint32_t PV_RANGE = 0x80000000u;
 
 struct BuildCounters {
   unsigned long long brick_evals, sub_evals, voxel_evals, paint_evals, rescued;
   unsigned long long alloc_events, free_events;
   unsigned long long violations;  // validation mode: float64 results outside the float32 enclosure
   unsigned long long resc_brick, resc_sub, resc_vox, resc_poly;  // rescues by level; polygon-test ambiguity
+  unsigned long long resc_paint;  // mixed mode: paint calls the float32 path could not decide
 };
 
 // Small device block read back after every build.
@@ -122,6 +136,13 @@ struct FoldArgs {
   uint2* vitems;              // partial sub-blocks to classify voxel by voxel: (op, pair << 3 | sub)
   uint32_t vitems_cap;
   uint32_t* vitem_counter;    // [0] items pushed, [1] items taken
+  uint32_t* paint_counter;    // paint_kernel items taken
+  uint32_t n_paint_slots;     // (op, brick) pairs of heavy-paint ops
+  uint32_t n_heavy;           // heavy-paint ops, ascending slots
+  const uint32_t* heavy_op;   // their op indices
+  const uint32_t* heavy_slot; // their first slots
+  uint32_t* pvals;            // 512 paint values per slot (voxel index order); PV_RANGE flags
+  int inline_paints;          // some painted op has no slot: fold_kernel calls its paints itself
   const OpDev* ops;
   const uint2* code;
   const double* params;
