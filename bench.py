@@ -197,6 +197,69 @@ def synthetic_section(args, pyoracle):
     return res
 
 
+def batched_section(args, pyoracle, n_scenes: int = 256, check: int = 8):
+    """256 independent seeded scenes of uneven size (volumes log-uniform 0.5-64 m^3,
+    aspect up to 4:1, 16-2048 primitives, vpm 40/80/160) rebuilt by one CUDA graph
+    launch; the autotuner picks the launch shape; `check` scenes (every n/check-th)
+    are compared with the oracle bit for bit."""
+    import numpy as np
+    from pixels_gb300.batch import Batch, tune
+    from pixels_gb300.scenes.synthetic import batch_specs, synthetic_program
+    from pixels_gb300.world import MODE_FP64, MODE_MIXED, VoxelWorld
+    specs = batch_specs(seed=7, n=n_scenes)
+    t0 = time.perf_counter()
+    progs = [synthetic_program(s["seed"], s["n_prims"], s["vpm"], s["volume"]) for s in specs]
+    t_gen = time.perf_counter() - t0
+    worlds = []
+    for s, prog in zip(specs, progs):
+        w = VoxelWorld(*s["dims"], initialPoolBricks=256, vpm=s["vpm"], mode=MODE_MIXED)
+        w._pending = prog
+        w.build()
+        worlds.append(w)
+    cells = int(sum(s["dims"][0] * s["dims"][1] * s["dims"][2] for s in specs))
+    shape, ms, table = tune(worlds, MODE_MIXED)
+    out = {"workload": f"{n_scenes} synthetic scenes (batch seed 7), one graph launch per step",
+           "cells": cells, "prims": int(sum(s["n_prims"] for s in specs)), "host_generation_s": round(t_gen, 2),
+           "autotune": table, "shape": {"streams": shape[0], "pairs_per_block": shape[1]}}
+    with Batch(worlds, MODE_MIXED, *shape) as b:
+        for _ in range(2):
+            b.run()
+        ts = [b.run() for _ in range(max(3, args.steps))]
+    t = statistics.median(ts)
+    out["mixed"] = {"ms_per_launch": round(t, 4), "value": round(cells / (t * 1e-3) / 1e9, 3),
+                    "scenes_per_s": round(n_scenes / (t * 1e-3), 1)}
+    with Batch(worlds, MODE_FP64, *shape) as b:
+        b.run()
+        ts = [b.run() for _ in range(3)]
+    t64 = statistics.median(ts)
+    out["fp64"] = {"ms_per_launch": round(t64, 4), "value": round(cells / (t64 * 1e-3) / 1e9, 3)}
+    # sequential builds of the same scenes, one after another on one stream (no graph)
+    from pixels_gb300 import _lib
+    t0 = time.perf_counter()
+    for w in worlds:
+        _lib.world_reset(w._h, True)
+        _lib.build(w._h, MODE_MIXED)
+    out["sequential_ms"] = round((time.perf_counter() - t0) * 1e3, 3)
+    mism = 0
+    checked = []
+    for i in range(0, n_scenes, max(1, n_scenes // check)):
+        s, w = specs[i], worlds[i]
+        o = pyoracle.OracleWorld(progs[i].to_bytes(), s["vpm"], s["dims"], threads=os.cpu_count() or 1)
+        grid = w.grid
+        bad = int(np.count_nonzero(grid != o.grid)) + abs(w.poolUsed - o.pool_used)
+        if not bad:
+            live = np.nonzero((o.grid != 0) & ((o.grid & 0x80000000) == 0))[0]
+            idx = o.grid[live].astype(np.int64) - 1
+            bad = int(np.count_nonzero(w.pool.reshape(-1, 512)[idx] != o.pool.reshape(-1, 512)[idx]))
+        mism += bad
+        checked.append(i)
+    out["oracle_checked_scenes"] = checked
+    out["mismatches"] = mism
+    for w in worlds:
+        w.close()
+    return out
+
+
 def serving_section(args, pyoracle):
     """Subtract-edits (70% spheres, 30% capsules, radii 1-40 cm, centres on occupied
     bricks, Poisson arrivals) served on a resident synthetic map at vpm=160
@@ -451,6 +514,7 @@ def main():
         _lib.world_destroy(h)
         out["synthetic"] = synthetic_section(args, pyoracle)
         out["serving"] = serving_section(args, pyoracle)
+        out["batched"] = batched_section(args, pyoracle)
     print(json.dumps(out))
     if dist is not None:
         dist.destroy_process_group()

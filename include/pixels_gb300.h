@@ -176,6 +176,25 @@ int px_serve_run(px_world* w, const px_edit* edits, const double* arrival_s, siz
                  uint64_t* applied_order, size_t* n_applied);
 const char* px_last_error(px_world* w);
 
+/* ---- batched builds: many scenes in one CUDA graph ----
+   No counterpart in the reference (it builds one world); the per-scene result
+   is the reference's apply() loop over that scene's ops (shapes.ts:334-431).
+   px_batch_create takes worlds that each hold a built scene (px_build done,
+   no ops queued), rebuilds each once from its last op list to size every
+   buffer, then captures the rebuild of all of them (reset + the same ops) into
+   one graph over n_streams streams, largest scenes first; pairs_per_block
+   sizes each scene's persistent grids to its (op, brick) pairs (0: whole GPU
+   per kernel).  px_batch_run launches the graph on `stream`, waits, and
+   updates every world (reads work as after px_build); device_ms (may be NULL)
+   receives the graph's device time.  While a batch exists its worlds cannot
+   be rebuilt, reset or destroyed (PX_E_INVALID_ARG; destroy is ignored). */
+typedef struct px_batch px_batch;
+int px_batch_create(px_world* const* worlds, size_t n, int mode, uint32_t n_streams, uint32_t pairs_per_block,
+                    px_batch** out);
+int px_batch_run(px_batch* b, void* stream, float* device_ms);
+void px_batch_destroy(px_batch* b);
+const char* px_batch_last_error(px_batch* b);
+
 /* Measurement utility (no counterpart in the reference): dependent-FMA
    throughput of this GPU's CUDA cores in TFLOP/s, float64 (fp64 = 1) or
    float32 (fp64 = 0) — the denominators of the voxeliser's ALU roofline. */

@@ -25,6 +25,7 @@ EXPORTS = [
     "px_build_finish", "px_read_grid", "px_read_pool", "px_read_holes", "px_derive", "px_read_super",
     "px_read_density", "px_read_free_list", "px_set_material_tables", "px_set_validation", "px_get_stats",
     "px_device_view_get", "px_last_error", "px_probe_peak", "px_world_info", "px_serve_run", "px_derive_noalloc",
+    "px_batch_create", "px_batch_run", "px_batch_destroy", "px_batch_last_error",
 ]
 
 
@@ -98,6 +99,12 @@ def load(path: str = LIB_PATH):
     L.px_serve_run.argtypes = [vp, ctypes.POINTER(Edit), ctypes.POINTER(ctypes.c_double), sz, u32, ctypes.c_uint64,
                                ctypes.c_int, vp, ctypes.POINTER(EditResult), ctypes.POINTER(ctypes.c_uint64),
                                ctypes.POINTER(sz)]
+    L.px_batch_create.argtypes = [ctypes.POINTER(vp), sz, ctypes.c_int, u32, u32, ctypes.POINTER(vp)]
+    L.px_batch_run.argtypes = [vp, vp, ctypes.POINTER(ctypes.c_float)]
+    L.px_batch_destroy.argtypes = [vp]
+    L.px_batch_destroy.restype = None
+    L.px_batch_last_error.argtypes = [vp]
+    L.px_batch_last_error.restype = ctypes.c_char_p
     L.px_derive_noalloc.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, u32, vp, vp, vp, vp, vp]
     _L = L
     return L
@@ -243,3 +250,29 @@ def derive_noalloc(grid_ptr: int, pool_ptr: int, bricks, n_pool_bricks: int, sup
         raise PxError(rc, "bad argument, or the grid names a pool brick beyond n_pool_bricks")
     if rc != PX_OK:
         raise PxError(rc, "px_derive_noalloc failed")
+
+
+def batch_create(handles, mode: int, n_streams: int, pairs_per_block: int):
+    """px_batch_create over world handles; returns the batch handle."""
+    L = load()
+    arr = (ctypes.c_void_p * len(handles))(*[h.value if isinstance(h, ctypes.c_void_p) else h for h in handles])
+    b = ctypes.c_void_p()
+    rc = L.px_batch_create(arr, len(handles), mode, n_streams, pairs_per_block, ctypes.byref(b))
+    if rc != PX_OK:
+        msgs = [(L.px_last_error(h) or b"").decode() for h in handles]
+        raise PxError(rc, "; ".join(m for m in msgs if m) or "px_batch_create failed")
+    return b
+
+
+def batch_run(b, stream: int = 0) -> float:
+    """Launch the batch's graph and wait; returns its device time in ms."""
+    L = load()
+    ms = ctypes.c_float()
+    rc = L.px_batch_run(b, ctypes.c_void_p(stream), ctypes.byref(ms))
+    if rc != PX_OK:
+        raise PxError(rc, (L.px_batch_last_error(b) or b"").decode())
+    return float(ms.value)
+
+
+def batch_destroy(b):
+    load().px_batch_destroy(b)

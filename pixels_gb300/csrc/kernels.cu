@@ -734,21 +734,22 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
   }
 }
 
-void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEvent_t mid) {
+void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEvent_t mid, int max_blocks) {
+  auto grid = [&](int per_sm) { return max_blocks > 0 && max_blocks < n_sms * per_sm ? max_blocks : n_sms * per_sm; };
   if (mode == 1) {
-    ++g_launches; classify_kernel<1><<<n_sms * PX_CLASSIFY_MINB, 256, 0, s>>>(a);
-    ++g_launches; voxel_kernel<1><<<n_sms * PX_CLASSIFY_MINB, 256, 0, s>>>(a);
+    ++g_launches; classify_kernel<1><<<grid(PX_CLASSIFY_MINB), 256, 0, s>>>(a);
+    ++g_launches; voxel_kernel<1><<<grid(PX_CLASSIFY_MINB), 256, 0, s>>>(a);
   } else {
-    ++g_launches; classify_kernel<0><<<n_sms * PX_CLASSIFY64_MINB, 256, 0, s>>>(a);
-    ++g_launches; voxel_kernel<0><<<n_sms * PX_CLASSIFY64_MINB, 256, 0, s>>>(a);
+    ++g_launches; classify_kernel<0><<<grid(PX_CLASSIFY64_MINB), 256, 0, s>>>(a);
+    ++g_launches; voxel_kernel<0><<<grid(PX_CLASSIFY64_MINB), 256, 0, s>>>(a);
   }
   if (a.n_paint_slots) {
-    if (mode == 1) { ++g_launches; paint_kernel<1><<<n_sms * 4, 256, 0, s>>>(a); }
-    else { ++g_launches; paint_kernel<0><<<n_sms * 4, 256, 0, s>>>(a); }
+    if (mode == 1) { ++g_launches; paint_kernel<1><<<grid(4), 256, 0, s>>>(a); }
+    else { ++g_launches; paint_kernel<0><<<grid(4), 256, 0, s>>>(a); }
   }
   if (mid) cudaEventRecord(mid, s);
-  if (a.inline_paints) { ++g_launches; fold_kernel<true><<<n_sms * PX_FOLD_MINB, 256, 0, s>>>(a); }
-  else { ++g_launches; fold_kernel<false><<<n_sms * PX_FOLD_MINB, 256, 0, s>>>(a); }
+  if (a.inline_paints) { ++g_launches; fold_kernel<true><<<grid(PX_FOLD_MINB), 256, 0, s>>>(a); }
+  else { ++g_launches; fold_kernel<false><<<grid(PX_FOLD_MINB), 256, 0, s>>>(a); }
 }
 
 // ---------------------------------------------------------------------------

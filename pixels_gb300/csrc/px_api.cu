@@ -83,6 +83,12 @@ struct px_world {
   FinalizeArgs fin{};
   bool derived_valid = false;
 
+  // batched builds (px_batch_*): the world's last build is captured in a graph
+  bool capturing = false;        // enqueue records no timing events
+  bool batch_locked = false;     // buffers are referenced by a graph: no rebuild, reset or destroy
+  bool batch_holes_in_a = true;  // holes_in_a of the captured build
+  uint32_t pairs_per_block = 0;  // launch shape: persistent grids sized to the build (0: whole GPU)
+
   px_stats stats{};
   std::string err;
 };
@@ -361,7 +367,7 @@ int px_set_material_tables(px_world* w, const uint8_t* opaque256, const uint8_t*
 }
 
 void px_world_destroy(px_world* w) {
-  if (!w) return;
+  if (!w || w->batch_locked) return;  // a batch's world outlives the batch
   if (w->in_flight) cudaStreamSynchronize(w->stream);
   cudaFree(w->d_grid);
   cudaFree(w->d_pool32);
@@ -429,6 +435,7 @@ bool paint_params32(uint32_t kind, bool framed, const double* p, const double A[
 
 int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
   if (!w || (!ir && bytes)) return PX_E_INVALID_ARG;
+  if (w->batch_locked) return fail(w, PX_E_INVALID_ARG, "the world belongs to a batch");
   if (w->in_flight) return fail(w, PX_E_INVALID_ARG, "a build is in flight");
   w->ops_resident = false;
   if (bytes < 32) return fail(w, PX_E_INVALID_IR, "IR shorter than its header");
@@ -641,6 +648,7 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
 
 int px_build_enqueue(px_world* w, int mode, void* stream) {
   if (!w) return PX_E_INVALID_ARG;
+  if (w->batch_locked && !w->capturing) return fail(w, PX_E_INVALID_ARG, "the world belongs to a batch");
   if (w->in_flight) return fail(w, PX_E_INVALID_ARG, "a build is already in flight");
   if (mode != PX_MODE_FP64 && mode != PX_MODE_MIXED) return fail(w, PX_E_INVALID_ARG, "unknown mode %d", mode);
   cudaStream_t s = (cudaStream_t)stream;
@@ -700,7 +708,8 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   if ((rc = grow_pool(w, (uint64_t)U0 + stage_cap, U0, s))) return rc;
 
   // scratch (a reallocated op table loses its resident copy)
-  const void* op_bufs_before[7] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p, w->d_p32.p, w->d_bases.p};
+  const void* op_bufs_before[9] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p,
+                                   w->d_p32.p, w->d_bases.p, w->chunk_op.p, w->heavy.p};
   if ((rc = ensure(w, w->d_ops, sizeof(OpDev) * (size_t)n_ops)) ||
       (rc = ensure(w, w->d_boxes, sizeof(uint2) * ((size_t)n_ops + (n_ops + 31) / 32))) ||
       (rc = ensure(w, w->d_code, sizeof(uint2) * w->code.size())) ||
@@ -730,8 +739,9 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
     if ((rc = ensure(w, w->scan_agg, 8 * nb))) return rc;
   }
   {
-    const void* after[7] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p, w->d_p32.p, w->d_bases.p};
-    for (int k = 0; k < 7; k++)
+    const void* after[9] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p,
+                            w->d_p32.p, w->d_bases.p, w->chunk_op.p, w->heavy.p};
+    for (int k = 0; k < 9; k++)
       if (after[k] != op_bufs_before[k]) w->ops_resident = false;
   }
   DevBuf& holes_in = w->holes_in_a ? w->holes_a : w->holes_b;
@@ -740,8 +750,9 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
 
   // upload the ops (one pinned staging copy per array)
   const unsigned long long launches0 = launch_count();
-  CU(cudaEventRecord(w->ev0, s));
-  if (!w->ops_resident) {
+  if (!w->capturing) CU(cudaEventRecord(w->ev0, s));
+  const bool upload = !w->ops_resident;
+  if (upload) {
     CU(cudaMemcpyAsync(w->d_ops.p, w->ops.data(), sizeof(OpDev) * (size_t)n_ops, cudaMemcpyHostToDevice, s));
     {  // op boxes, then the union box of every 32 consecutive ops (cull_count_kernel)
       const int n_groups = (n_ops + 31) / 32;
@@ -775,7 +786,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   CU(cudaMemsetAsync(w->res.p, 0, sizeof(BuildResult), s));
   CU(cudaMemsetAsync(w->work_counter.p, 0, 16, s));
   CU(cudaMemsetAsync(w->chunk_counter.p, 0, 16, s));
-  {  // op of the first pair of every 32-pair chunk
+  if (upload) {  // op of the first pair of every 32-pair chunk
     const size_t n_chunks = (P + 31) / 32;
     w->h_chunk_op.resize(n_chunks);
     uint32_t o = 0;
@@ -787,7 +798,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
     if (n_chunks) CU(cudaMemcpyAsync(w->chunk_op.p, w->h_chunk_op.data(), 4 * n_chunks, cudaMemcpyHostToDevice, s));
   }
   if (P) CU(cudaMemsetAsync(w->evt.p, 0, P, s));
-  if (n_heavy)
+  if (n_heavy && upload)
     CU(cudaMemcpyAsync(w->heavy.p, w->h_heavy.data(), 4 * w->h_heavy.size(), cudaMemcpyHostToDevice, s));
 
   BuildResult* res = (BuildResult*)w->res.p;
@@ -842,9 +853,11 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   fa.stage_src = (int64_t*)w->stage_src.p;
   fa.work_counter = (uint32_t*)w->work_counter.p;
   fa.res = res;
-  CU(cudaEventRecord(w->ev_fold0, s));
-  launch_fold(fa, mode, w->n_sms, s, w->ev_mid);
-  CU(cudaEventRecord(w->ev_fold1, s));
+  int max_blocks = 0;  // persistent grids sized to the build (batched builds share the GPU)
+  if (w->pairs_per_block) max_blocks = (int)std::max<uint64_t>(1, (P + w->pairs_per_block - 1) / w->pairs_per_block);
+  if (!w->capturing) CU(cudaEventRecord(w->ev_fold0, s));
+  launch_fold(fa, mode, w->n_sms, s, w->capturing ? nullptr : w->ev_mid, max_blocks);
+  if (!w->capturing) CU(cudaEventRecord(w->ev_fold1, s));
 
   ReplayArgs ra{};
   ra.P = P; ra.E_max = E_max; ra.H = H; ra.U0 = U0;
@@ -881,7 +894,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   launch_finalize(fn, (uint32_t)touched_bound, s);
   CU(cudaGetLastError());
   w->stats.kernel_launches = (uint32_t)(launch_count() - launches0);
-  CU(cudaEventRecord(w->ev1, s));
+  if (!w->capturing) CU(cudaEventRecord(w->ev1, s));
   CU(cudaMemcpyAsync(w->h_res, res, sizeof(BuildResult), cudaMemcpyDeviceToHost, s));
   w->in_flight = true;
   w->last_P = P;
@@ -893,19 +906,11 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   return PX_OK;
 }
 
-int px_build_finish(px_world* w) {
-  if (!w) return PX_E_INVALID_ARG;
-  if (!w->in_flight) return PX_OK;
-  w->in_flight = false;
-  CU(cudaStreamSynchronize(w->stream));
-  const BuildResult& r = *w->h_res;
-  float ms = 0.f, fold_ms = 0.f;
-  cudaEventElapsedTime(&ms, w->ev0, w->ev1);
-  cudaEventElapsedTime(&fold_ms, w->ev_fold0, w->ev_fold1);
-  w->stats.fold_ms = fold_ms;
-  float cls_ms = 0.f;
-  cudaEventElapsedTime(&cls_ms, w->ev_fold0, w->ev_mid);
-  w->stats.classify_ms = cls_ms;
+}  // extern "C"
+
+namespace {
+// Counters of a finished build (device result block) into the world's stats.
+void fill_stats(px_world* w, const BuildResult& r) {
   w->stats.pairs = w->last_P;
   w->stats.brick_evals = r.c.brick_evals;
   w->stats.sub_evals = r.c.sub_evals;
@@ -926,8 +931,28 @@ int px_build_finish(px_world* w) {
   w->stats.rescued_voxel = r.c.resc_vox;
   w->stats.rescued_polygon = r.c.resc_poly;
   w->stats.rescued_paint = (uint32_t)r.c.resc_paint;
-  w->stats.build_ms = ms;
   w->stats.status = r.status;
+}
+
+}  // namespace
+
+extern "C" {
+
+int px_build_finish(px_world* w) {
+  if (!w) return PX_E_INVALID_ARG;
+  if (!w->in_flight) return PX_OK;
+  w->in_flight = false;
+  CU(cudaStreamSynchronize(w->stream));
+  const BuildResult& r = *w->h_res;
+  float ms = 0.f, fold_ms = 0.f;
+  cudaEventElapsedTime(&ms, w->ev0, w->ev1);
+  cudaEventElapsedTime(&fold_ms, w->ev_fold0, w->ev_fold1);
+  w->stats.fold_ms = fold_ms;
+  float cls_ms = 0.f;
+  cudaEventElapsedTime(&cls_ms, w->ev_fold0, w->ev_mid);
+  w->stats.classify_ms = cls_ms;
+  w->stats.build_ms = ms;
+  fill_stats(w, r);
   // transactional retries: nothing was committed
   if ((r.status & ST_STAGE_OVERFLOW) && r.stage_count > w->last_stage_cap && w->retries < 2) {
     w->stage_hint = (uint64_t)r.stage_count + r.stage_count / 4 + 64;
@@ -1001,6 +1026,7 @@ int px_set_validation(px_world* w, int on) {
 
 int px_world_reset(px_world* w, int requeue_last_ops, void* stream) {
   if (!w) return PX_E_INVALID_ARG;
+  if (w->batch_locked && !w->capturing) return fail(w, PX_E_INVALID_ARG, "the world belongs to a batch");
   if (w->in_flight) return fail(w, PX_E_INVALID_ARG, "a build is in flight");
   CU(cudaMemsetAsync(w->d_grid, 0, w->ncells * 4, (cudaStream_t)stream));
   w->pool_used = 0;
@@ -1118,5 +1144,197 @@ int px_probe_peak(int fp64, float* tflops) {
   *tflops = probe_fma_tflops(fp64, sms);
   return cudaGetLastError() == cudaSuccess ? PX_OK : PX_E_CUDA;
 }
+
+// ---------------------------------------------------------------------------
+// Batched builds: the rebuild of many worlds (each from its last op list)
+// captured once into one CUDA graph over several streams and relaunched as a
+// single graph.  Small scenes run side by side on the GPU; each scene's
+// persistent grids are sized to its pairs (pairs_per_block).
+
+struct px_batch {
+  std::vector<px_world*> worlds;
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> joins;
+  cudaEvent_t fork = nullptr, t0 = nullptr, t1 = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int mode = 0;
+  std::string err;
+};
+
+namespace {
+
+int batch_fail(px_batch* b, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  b->err = buf;
+  return code;
+}
+
+void batch_free(px_batch* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  for (cudaStream_t s : b->streams) cudaStreamDestroy(s);
+  for (cudaEvent_t e : b->joins) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->t0) cudaEventDestroy(b->t0);
+  if (b->t1) cudaEventDestroy(b->t1);
+  for (px_world* w : b->worlds) w->batch_locked = false;
+  delete b;
+}
+
+// Host state of a world across the capture (capture runs nothing).
+struct WorldSaved {
+  uint32_t pool_used, n_holes;
+  bool holes_in_a, derived_valid;
+  uint32_t ppb;
+};
+
+}  // namespace
+
+int px_batch_create(px_world* const* worlds, size_t n, int mode, uint32_t n_streams, uint32_t pairs_per_block,
+                    px_batch** out) {
+  if (!out) return PX_E_INVALID_ARG;
+  *out = nullptr;
+  if (!worlds || n == 0 || n_streams == 0 || n_streams > 64 || (mode != PX_MODE_FP64 && mode != PX_MODE_MIXED))
+    return PX_E_INVALID_ARG;
+  for (size_t i = 0; i < n; i++) {
+    px_world* w = worlds[i];
+    if (!w || w->batch_locked || w->in_flight || !w->ops.empty() || w->last_ops.empty()) return PX_E_INVALID_ARG;
+    for (size_t j = 0; j < i; j++)
+      if (worlds[j] == w) return PX_E_INVALID_ARG;
+  }
+  px_batch* b = new px_batch;
+  b->worlds.assign(worlds, worlds + n);
+  b->mode = mode;
+  // largest builds first, dealt round-robin over the streams
+  std::vector<size_t> order(n);
+  for (size_t i = 0; i < n; i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) {
+    return b->worlds[x]->last_ops.size() * b->worlds[x]->ncells > b->worlds[y]->last_ops.size() * b->worlds[y]->ncells;
+  });
+  // one real rebuild per world first, so that every buffer the captured
+  // rebuild touches already has its size (nothing allocates while capturing)
+  for (size_t i = 0; i < n; i++) {
+    px_world* w = b->worlds[i];
+    const uint32_t keep = w->pairs_per_block;
+    w->pairs_per_block = pairs_per_block;
+    int rc = px_world_reset(w, 1, nullptr);
+    if (rc == PX_OK) rc = px_build(w, mode, nullptr);
+    w->pairs_per_block = keep;
+    if (rc != PX_OK) {  // px_last_error(w) tells why
+      delete b;
+      return rc;
+    }
+  }
+  if (cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreate(&b->t0) != cudaSuccess || cudaEventCreate(&b->t1) != cudaSuccess) {
+    cudaGetLastError();
+    batch_free(b);
+    return PX_E_CUDA;
+  }
+  for (uint32_t k = 0; k < n_streams; k++) {
+    cudaStream_t st;
+    cudaEvent_t ev;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) { cudaGetLastError(); batch_free(b); return PX_E_CUDA; }
+    b->streams.push_back(st);
+    if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) { cudaGetLastError(); batch_free(b); return PX_E_CUDA; }
+    b->joins.push_back(ev);
+  }
+  std::vector<WorldSaved> saved(n);
+  for (size_t i = 0; i < n; i++) {
+    px_world* w = b->worlds[i];
+    saved[i] = {w->pool_used, w->n_holes, w->holes_in_a, w->derived_valid, w->pairs_per_block};
+  }
+  cudaStream_t origin = b->streams[0];
+  int rc = PX_OK;
+  if (cudaStreamBeginCapture(origin, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { cudaGetLastError(); batch_free(b); return PX_E_CUDA; }
+  cudaEventRecord(b->fork, origin);
+  for (uint32_t k = 1; k < n_streams; k++) cudaStreamWaitEvent(b->streams[k], b->fork, 0);
+  for (size_t q = 0; q < n && rc == PX_OK; q++) {
+    px_world* w = b->worlds[order[q]];
+    cudaStream_t st = b->streams[q % n_streams];
+    w->capturing = true;
+    w->batch_locked = true;
+    w->pairs_per_block = pairs_per_block;
+    w->batch_holes_in_a = w->holes_in_a;
+    rc = px_world_reset(w, 1, st);
+    if (rc == PX_OK) rc = px_build_enqueue(w, mode, st);
+    w->capturing = false;
+    w->in_flight = false;  // captured, not launched
+    if (rc != PX_OK) batch_fail(b, rc, "world %zu: %s", order[q], w->err.c_str());
+  }
+  for (uint32_t k = 1; k < n_streams; k++) {
+    cudaEventRecord(b->joins[k], b->streams[k]);
+    cudaStreamWaitEvent(origin, b->joins[k], 0);
+  }
+  const cudaError_t ce = cudaStreamEndCapture(origin, &b->graph);
+  // the worlds keep their built state until the graph runs
+  for (size_t i = 0; i < n; i++) {
+    px_world* w = b->worlds[i];
+    w->pool_used = saved[i].pool_used;
+    w->n_holes = saved[i].n_holes;
+    w->holes_in_a = saved[i].holes_in_a;
+    w->derived_valid = saved[i].derived_valid;
+    w->pairs_per_block = saved[i].ppb;
+    w->ops.clear(); w->boxes.clear(); w->code.clear(); w->params.clear();
+    w->code32.clear(); w->p32.clear(); w->bases.clear();
+  }
+  if (rc == PX_OK && ce != cudaSuccess) rc = batch_fail(b, PX_E_CUDA, "capture: %s", cudaGetErrorString(ce));
+  if (rc == PX_OK && cudaGraphInstantiate(&b->exec, b->graph, 0) != cudaSuccess)
+    rc = batch_fail(b, PX_E_CUDA, "graph instantiation failed");
+  if (rc != PX_OK) {
+    cudaGetLastError();
+    batch_free(b);
+    return rc;
+  }
+  *out = b;
+  return PX_OK;
+}
+
+int px_batch_run(px_batch* b, void* stream, float* device_ms) {
+  if (!b) return PX_E_INVALID_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaEventRecord(b->t0, s) != cudaSuccess || cudaGraphLaunch(b->exec, s) != cudaSuccess ||
+      cudaEventRecord(b->t1, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) {
+    const cudaError_t e = cudaGetLastError();
+    return batch_fail(b, PX_E_CUDA, "graph launch: %s", cudaGetErrorString(e));
+  }
+  if (device_ms) cudaEventElapsedTime(device_ms, b->t0, b->t1);
+  int first = PX_OK;
+  for (size_t i = 0; i < b->worlds.size(); i++) {
+    px_world* w = b->worlds[i];
+    const BuildResult& r = *w->h_res;
+    fill_stats(w, r);
+    w->stats.build_ms = 0.f;
+    if (r.status & (ST_STAGE_OVERFLOW | ST_POOL_OVERFLOW | ST_CHAIN)) {
+      if (first == PX_OK) first = batch_fail(b, PX_E_QUEUE_OVERFLOW, "world %zu: device status 0x%x", i, r.status);
+      continue;
+    }
+    w->pool_used = r.pool_used;
+    w->n_holes = r.n_holes;
+    w->holes_in_a = !w->batch_holes_in_a;  // the captured build wrote the other holes buffer
+    w->derived_valid = false;
+    w->ops_applied += w->last_ops.size();
+    w->stats.ops_applied = w->ops_applied;
+    w->stats.pool_used = w->pool_used;
+    w->stats.n_holes = w->n_holes;
+    w->stats.pool_capacity = w->pool_cap;
+    if ((r.status & ST_RANGE) && first == PX_OK)
+      first = batch_fail(b, PX_E_RANGE, "world %zu: a paint function received an argument outside its supported range", i);
+  }
+  return first;
+}
+
+void px_batch_destroy(px_batch* b) {
+  if (!b) return;
+  if (b->streams.size()) cudaStreamSynchronize(b->streams[0]);
+  batch_free(b);
+}
+
+const char* px_batch_last_error(px_batch* b) { return b ? b->err.c_str() : "null batch"; }
 
 }  // extern "C"

@@ -179,7 +179,8 @@ void launch_cull_count(const uint2* boxes, int n_ops, int TX, int TY, int TZ, ui
                        uint32_t* tiles_nonempty, BuildResult* res, cudaStream_t s);
 void launch_cull_fill(const uint2* boxes, int n_ops, int TX, int TY, int TZ, const uint32_t* tile_off,
                       uint32_t* tile_ops, cudaStream_t s);
-void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEvent_t mid);
+// max_blocks > 0 caps the persistent grids (builds sharing the GPU)
+void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEvent_t mid, int max_blocks);
 
 struct ScanTemp {
   void* block_agg;

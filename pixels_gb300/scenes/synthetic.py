@@ -38,9 +38,9 @@ def _f32(v) -> float:
     return float(np.float32(v))
 
 
-def _prim(rng: np.random.Generator):
+def _prim(rng: np.random.Generator, volume=VOLUME):
     kind = KINDS[int(rng.integers(len(KINDS)))]
-    c = tuple(_f32(rng.uniform(0, VOLUME[i])) for i in range(3))
+    c = tuple(_f32(rng.uniform(0, volume[i])) for i in range(3))
     size = _f32(math.exp(rng.uniform(math.log(0.02), math.log(1.5))))
     half = size / 2
     ext = tuple(_f32(half * rng.uniform(0.3, 1.0)) for _ in range(3))
@@ -96,8 +96,9 @@ def _paint(rng: np.random.Generator):
     return v
 
 
-def build_synthetic(world, seed: int = 1, n_prims: int = 4096) -> int:
-    """Queue a seeded synthetic scene on ``world``; returns the number of ops."""
+def build_synthetic(world, seed: int = 1, n_prims: int = 4096, volume=VOLUME) -> int:
+    """Queue a seeded synthetic scene on ``world`` (centres uniform in
+    ``volume``, metres); returns the number of ops."""
     rng = np.random.default_rng(seed)
     B = Builder(world)
     ops = 0
@@ -106,15 +107,15 @@ def build_synthetic(world, seed: int = 1, n_prims: int = 4096) -> int:
         while i < n_prims:
             u = rng.random()
             if u < 0.3 and i + 1 < n_prims:
-                s = subtract(_prim(rng), _prim(rng))
+                s = subtract(_prim(rng, volume), _prim(rng, volume))
                 i += 2
                 B.add(s, _paint(rng))
             elif u < 0.4 and i + 1 < n_prims:
-                s = intersect(_prim(rng), _prim(rng))
+                s = intersect(_prim(rng, volume), _prim(rng, volume))
                 i += 2
                 B.add(s, _paint(rng))
             else:
-                s = _prim(rng)
+                s = _prim(rng, volume)
                 i += 1
                 if rng.random() < 0.1:
                     B.carve(s)
@@ -124,8 +125,36 @@ def build_synthetic(world, seed: int = 1, n_prims: int = 4096) -> int:
     return ops
 
 
-def synthetic_program(seed: int = 1, n_prims: int = 4096, vpm: float = 80.0):
+def synthetic_program(seed: int = 1, n_prims: int = 4096, vpm: float = 80.0, volume=VOLUME):
     from ..world import OpRecorder
     rec = OpRecorder(vpm)
-    build_synthetic(rec, seed, n_prims)
+    build_synthetic(rec, seed, n_prims, volume)
     return rec.program
+
+
+def dims_for(volume, vpm: float):
+    """World dims (voxels) of a volume: ceil(m * vpm / 8) * 8 per axis, as config.ts sizes the world."""
+    return tuple(int(math.ceil(m * vpm / 8)) * 8 for m in volume)
+
+
+def batch_specs(seed: int = 7, n: int = 256):
+    """The batched workload: ``n`` independent scenes of uneven size.
+
+    Volumes log-uniform 0.5-64 m^3 with aspect ratios up to 4:1 (two axes
+    1-4x the third, in random order), primitive counts log-uniform 16-2048,
+    voxel density uniform over {40, 80, 160} per metre; each scene is a
+    synthetic scene (same distributions as above) with its own seed.
+    """
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(n):
+        vol = math.exp(rng.uniform(math.log(0.5), math.log(64.0)))
+        ratios = [1.0, float(rng.uniform(1.0, 4.0)), float(rng.uniform(1.0, 4.0))]
+        rng.shuffle(ratios)
+        k = (vol / (ratios[0] * ratios[1] * ratios[2])) ** (1.0 / 3.0)
+        volume = tuple(_f32(k * r) for r in ratios)
+        n_prims = int(round(math.exp(rng.uniform(math.log(16), math.log(2048)))))
+        vpm = float((40, 80, 160)[int(rng.integers(3))])
+        specs.append({"seed": seed * 100003 + i, "volume": volume, "n_prims": n_prims, "vpm": vpm,
+                      "dims": dims_for(volume, vpm)})
+    return specs
