@@ -132,6 +132,15 @@ int px_derive_noalloc(const uint32_t* grid, const uint16_t* pool, int bx, int by
                       const uint8_t* opaque256, const uint8_t* uniform_density256, uint32_t* super_counts,
                       uint8_t* density, void* stream);
 
+/* snapToEmissive (GpuWorld.ts:165-174) for n light anchors of the built world in
+   one launch: xyz / out_xyz hold n voxel coordinates (x, y, z) each; every anchor
+   moves to the first voxel of the cubes of radius 0, 1, 2 around it (z, then y,
+   then x outermost first, each from -r to r) whose material emits, else stays.
+   emission256[id]: 0 no emission, 1 emits, 2 no such material (the reference
+   throws there: PX_E_INVALID_ARG).  packLights (GpuWorld.ts:141-162) lays the
+   result out on the host. */
+int px_snap_anchors(px_world* w, const int32_t* xyz, size_t n, const uint8_t* emission256, int32_t* out_xyz);
+
 /* Material tables for the density pass: opaque[id] (OPAQUE, VoxelWorld.ts:190-196) and the
    density of a uniform brick of material id (VoxelWorld.ts:162).  256 bytes each. */
 int px_set_material_tables(px_world* w, const uint8_t* opaque256, const uint8_t* uniform_density256);

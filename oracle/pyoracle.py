@@ -120,6 +120,32 @@ class OracleWorld:
         tail = np.arange(cap - 1, self.pool_used - 1, -1, dtype=np.int64).astype(np.uint32)
         return np.concatenate([self.free_holes.astype(np.uint32), tail])
 
+    def get(self, x: int, y: int, z: int) -> int:
+        """VoxelWorld.get (VoxelWorld.ts:55-61)."""
+        dx, dy, dz = self.dims
+        if x < 0 or y < 0 or z < 0 or x >= dx or y >= dy or z >= dz:
+            return 0
+        bx, by, _ = self.bricks
+        g = int(self.grid[(x >> 3) + bx * ((y >> 3) + by * (z >> 3))])
+        if g == 0:
+            return 0
+        if g & 0x80000000:
+            return g & 0xFFFF
+        return int(self.pool[(g - 1) * 512 + ((x & 7) | ((y & 7) << 3) | ((z & 7) << 6))])
+
+    def snap_to_emissive(self, emits, x: int, y: int, z: int):
+        """snapToEmissive (GpuWorld.ts:165-174): the first emissive voxel of the
+        cubes of radius 0..2 around (x, y, z), z then y then x outermost first.
+        ``emits(material_byte)`` is True/False, or raises for an unknown material."""
+        for r in range(3):
+            for oz in range(-r, r + 1):
+                for oy in range(-r, r + 1):
+                    for ox in range(-r, r + 1):
+                        v = self.get(x + ox, y + oy, z + oz)
+                        if v and emits(v & 0xFF):
+                            return (x + ox, y + oy, z + oz)
+        return (x, y, z)
+
     def live_pool_bricks(self) -> dict:
         """{cell index: brick voxels} for every cell that references the pool."""
         g = self.grid

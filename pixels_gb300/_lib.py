@@ -25,7 +25,7 @@ EXPORTS = [
     "px_build_finish", "px_read_grid", "px_read_pool", "px_read_holes", "px_derive", "px_read_super",
     "px_read_density", "px_read_free_list", "px_set_material_tables", "px_set_validation", "px_get_stats",
     "px_device_view_get", "px_last_error", "px_probe_peak", "px_world_info", "px_serve_run", "px_derive_noalloc",
-    "px_batch_create", "px_batch_run", "px_batch_destroy", "px_batch_last_error",
+    "px_batch_create", "px_batch_run", "px_batch_destroy", "px_batch_last_error", "px_snap_anchors",
 ]
 
 
@@ -105,6 +105,7 @@ def load(path: str = LIB_PATH):
     L.px_batch_destroy.restype = None
     L.px_batch_last_error.argtypes = [vp]
     L.px_batch_last_error.restype = ctypes.c_char_p
+    L.px_snap_anchors.argtypes = [vp, vp, sz, vp, vp]
     L.px_derive_noalloc.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, u32, vp, vp, vp, vp, vp]
     _L = L
     return L
@@ -276,3 +277,14 @@ def batch_run(b, stream: int = 0) -> float:
 
 def batch_destroy(b):
     load().px_batch_destroy(b)
+
+
+def snap_anchors(h, xyz: np.ndarray, emission: np.ndarray) -> np.ndarray:
+    """px_snap_anchors: (n, 3) int32 voxel coordinates -> snapped coordinates."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.int32).reshape(-1, 3)
+    out = np.empty_like(xyz)
+    em = np.ascontiguousarray(emission, dtype=np.uint8)
+    if em.size != 256:
+        raise ValueError("emission table must have 256 entries")
+    _check(h, load().px_snap_anchors(h, xyz.ctypes.data, xyz.shape[0], em.ctypes.data, out.ctypes.data))
+    return out

@@ -31,6 +31,8 @@ _PALETTE = [
 ]
 
 GLASS = {i + 1: g for i, (_, g) in enumerate(_PALETTE)}
+# emission (materials.ts:34,80; nonzero only for these, :171-177)
+EMISSION = {"neonPink": 6, "neonCyan": 6, "neonGold": 6, "bulb": 8, "lampshade": 1.3, "screen": 2.5, "tv": 1.6}
 NUM_MATERIALS = len(_PALETTE)
 
 
@@ -73,4 +75,13 @@ def uniform_density_table() -> list[int]:
         g = GLASS.get(i)
         if g is not None and g > 0:
             t[i] = 0
+    return t
+
+
+def emission_table() -> list:
+    """Per material byte: 1 if the material emits (mat(id).emission > 0), 0 if not,
+    2 if no material has that id (mat(id) is undefined in the reference)."""
+    t = [2] * 256
+    for i, (name, _) in enumerate(_PALETTE):
+        t[i + 1] = 1 if EMISSION.get(name, 0) > 0 else 0
     return t
