@@ -154,6 +154,13 @@ __device__ __forceinline__ int classify64(double d, double half_diag) {
 // from the brick's first voxel centre, enclosing the reference's float64 point.
 __device__ __forceinline__ Iv koff(float k, float vs_lo, float vs_hi) { return {__fmul_rd(k, vs_lo), __fmul_ru(k, vs_hi)}; }
 
+// The shape at the reference's point (t * vs per axis, t in voxel units).  Out
+// of line so that no float64 product is hoisted into the float32 path.
+__device__ __noinline__ double sdf64_at(const uint2* __restrict__ code, int clen, const double* __restrict__ params,
+                                        double vs, float tx, float ty, float tz) {
+  return sdf64(code, clen, params, (double)tx * vs, (double)ty * vs, (double)tz * vs);
+}
+
 // Evaluate one shape at one point: float64 directly, or float32 interval with
 // a float64 rescue when the interval cannot decide.  (tx, ty, tz) are the
 // reference's point in voxel units (ox + 4, sx + 2 or x + 0.5, exact in
@@ -174,8 +181,7 @@ __device__ __forceinline__ int eval_decide(const FoldArgs& a, const OpDev* O, co
     if (what == 0) r = amb ? 3 : (d.lo > O->thr[T_V_HI] ? 0 : (d.hi <= O->thr[T_V_LO] ? 1 : 3));
     else r = amb ? 3 : classify32(d, O->thr, base);
     if (r != 3 && !a.validate) return r;
-    const double vs = a.vs;
-    double d64 = sdf64(code, clen, a.params, (double)tx * vs, (double)ty * vs, (double)tz * vs);
+    double d64 = sdf64_at(code, clen, a.params, a.vs, tx, ty, tz);
     const double M = MIXED_MARGIN;
     if (a.validate && !amb && !((double)d.lo - M <= d64 && d64 <= (double)d.hi + M) && count) ls.viol++;
     if (r == 3 && count) {
@@ -409,6 +415,26 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
   }
 }
 
+// One paint call at voxel (x, y, z) of the world, in float64 (the paint kinds
+// that paint_kernel does not evaluate ahead).  Out of line, so that the apply
+// loop holds no float64 values.  Returns the value (a u16 for these kinds) with
+// PV_RANGE for a range error and PV_VIOL for a validation mismatch.
+constexpr uint32_t PV_VIOL = 0x40000000u;
+__device__ __noinline__ uint32_t paint_at_voxel(const double* __restrict__ params, double vs, int validate,
+                                                const OpDev* O, int x, int y, int z) {
+  double PX = (x + 0.5) * vs, PY = (y + 0.5) * vs, PZ = (z + 0.5) * vs;
+  if (O->flags & OPF_PAINT_FRAME) {  // localPaint (penthouse.ts:88-91)
+    const double fpx = O->frame[0], fpz = O->frame[1], c = O->frame[2], sn = O->frame[3];
+    const double dx = PX - fpx, dz = PZ - fpz;
+    PX = fpx + c * dx + sn * dz;
+    PZ = fpz - sn * dx + c * dz;
+  }
+  uint32_t st = 0;
+  const uint32_t v = paint_eval(O->paint_kind, params + O->paint_off, PX, PY, PZ, st);
+  const bool viol = validate && v != paint_eval_cr(O->paint_kind, params + O->paint_off, PX, PY, PZ, st);
+  return (v & 0xffffu) | (st & ST_RANGE ? PV_RANGE : 0u) | (viol ? PV_VIOL : 0u);
+}
+
 // Paint calls of the heavy paint kinds, ahead of the apply pass: one 4^3
 // sub-block of one (op, brick) pair per warp pass, two voxels per lane, every
 // voxel the op's shape covers (whether the reference then paints it depends on
@@ -446,7 +472,6 @@ __global__ void __launch_bounds__(256) paint_kernel(FoldArgs a) {
     int bx, by, bz;
     brick_of_pair(O, pair, bx, by, bz);
     const uint32_t pk = O->paint_kind;
-    const double* pp = a.params + O->paint_off;
     const bool try32 = MODE == 1 && O->paint32_off != NO_SLOT;
     Iv bo[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
     if (try32) brick_bases(a, O, bx, by, bz, bo);
@@ -462,16 +487,15 @@ __global__ void __launch_bounds__(256) paint_kernel(FoldArgs a) {
                        iadd(bo[1], koff((float)ly, a.vs_lo, a.vs_hi)), iadd(bo[2], koff((float)lz, a.vs_lo, a.vs_hi)), v);
         if (!done) resc++;
       }
-      if (!done || a.validate) {
-        double PX = (bx * 8 + lx + 0.5) * a.vs, PY = (by * 8 + ly + 0.5) * a.vs, PZ = (bz * 8 + lz + 0.5) * a.vs;
-        if (O->flags & OPF_PAINT_FRAME) {  // localPaint (penthouse.ts:88-91)
-          const double fpx = O->frame[0], fpz = O->frame[1], c = O->frame[2], sn = O->frame[3];
-          const double dx = PX - fpx, dz = PZ - fpz;
-          PX = fpx + c * dx + sn * dz;
-          PZ = fpz - sn * dx + c * dz;
+      if (!done || a.validate) {  // float64 (validation: also the correctly rounded decision)
+        const uint32_t pr = paint_at_voxel(a.params, a.vs, a.validate, O, bx * 8 + lx, by * 8 + ly, bz * 8 + lz);
+        if (pr & PV_VIOL) viol++;
+        if (!done) {
+          v = pr & 0xffffu;
+          if (pr & PV_RANGE) st |= ST_RANGE;
+        } else if (v != (pr & 0xffffu)) {
+          viol++;
         }
-        if (!done) v = paint_eval(pk, pp, PX, PY, PZ, st);
-        if (a.validate && v != paint_eval_cr(pk, pp, PX, PY, PZ, st)) viol++;
       }
       a.pvals[(size_t)slot * 512 + (uint32_t)(lx | (ly << 3) | (lz << 6))] = (v & 0xffffu) | (st & ST_RANGE ? PV_RANGE : 0u);
     }
@@ -485,26 +509,6 @@ __global__ void __launch_bounds__(256) paint_kernel(FoldArgs a) {
     if (resc) atomicAdd(&a.res->c.resc_paint, (unsigned long long)resc);
     if (viol) atomicAdd(&a.res->c.violations, (unsigned long long)viol);
   }
-}
-
-// One paint call at voxel (x, y, z) of the world, in float64 (the paint kinds
-// that paint_kernel does not evaluate ahead).  Out of line, so that the apply
-// loop holds no float64 values.  Returns the value (a u16 for these kinds) with
-// PV_RANGE for a range error and PV_VIOL for a validation mismatch.
-constexpr uint32_t PV_VIOL = 0x40000000u;
-__device__ __noinline__ uint32_t paint_at_voxel(const double* __restrict__ params, double vs, int validate,
-                                                const OpDev* O, int x, int y, int z) {
-  double PX = (x + 0.5) * vs, PY = (y + 0.5) * vs, PZ = (z + 0.5) * vs;
-  if (O->flags & OPF_PAINT_FRAME) {  // localPaint (penthouse.ts:88-91)
-    const double fpx = O->frame[0], fpz = O->frame[1], c = O->frame[2], sn = O->frame[3];
-    const double dx = PX - fpx, dz = PZ - fpz;
-    PX = fpx + c * dx + sn * dz;
-    PZ = fpz - sn * dx + c * dz;
-  }
-  uint32_t st = 0;
-  const uint32_t v = paint_eval(O->paint_kind, params + O->paint_off, PX, PY, PZ, st);
-  const bool viol = validate && v != paint_eval_cr(O->paint_kind, params + O->paint_off, PX, PY, PZ, st);
-  return (v & 0xffffu) | (st & ST_RANGE ? PV_RANGE : 0u) | (viol ? PV_VIOL : 0u);
 }
 
 // Lane layout of a brick in registers: lane owns the voxel pair

@@ -678,17 +678,21 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
     n_slots = 0;
     inline_paints = false;
     w->h_heavy.clear();
-    for (int i = 0; i < n_ops; i++) {
-      OpDev& o = w->ops[i];
-      o.paint_slot = NO_SLOT;
-      if (o.bx0 > o.bx1 || o.kind == KIND_CARVE || o.paint_kind == PK_CONST) continue;
-      if (tier == 2 || (tier == 1 && !paint_is_heavy(o.paint_kind))) { inline_paints = true; continue; }
-      const uint64_t np = (uint64_t)o.nx * o.ny * (uint64_t)(o.bz1 - o.bz0 + 1);
-      o.paint_slot = (uint32_t)n_slots;
-      w->h_heavy.push_back((uint32_t)i);
-      w->h_heavy.push_back((uint32_t)n_slots);
-      n_slots += np;
-    }
+    // float64-only paints first: paint_kernel takes items in slot order, so the
+    // slowest calls start earliest
+    for (int pass = 0; pass < 2; pass++)
+      for (int i = 0; i < n_ops; i++) {
+        OpDev& o = w->ops[i];
+        if (pass == 0) o.paint_slot = NO_SLOT;
+        if (o.bx0 > o.bx1 || o.kind == KIND_CARVE || o.paint_kind == PK_CONST) continue;
+        if ((o.paint32_off != NO_SLOT) != (pass == 1)) continue;
+        if (tier == 2 || (tier == 1 && !paint_is_heavy(o.paint_kind))) { inline_paints = true; continue; }
+        const uint64_t np = (uint64_t)o.nx * o.ny * (uint64_t)(o.bz1 - o.bz0 + 1);
+        o.paint_slot = (uint32_t)n_slots;
+        w->h_heavy.push_back((uint32_t)i);
+        w->h_heavy.push_back((uint32_t)n_slots);
+        n_slots += np;
+      }
     if (n_slots * 2048 <= (512ull << 20)) break;
   }
   const uint32_t n_heavy = (uint32_t)(w->h_heavy.size() / 2);
