@@ -279,6 +279,10 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
         n_brick++;
       }
       a.pcode[p] = (uint8_t)cls;
+      if (cls != PC_SKIP) {  // the apply pass visits this brick
+        const size_t ci = (size_t)bx + (size_t)a.BX * ((size_t)by + (size_t)a.BY * (size_t)bz);
+        atomicOr(a.bmark + (ci >> 5), 1u << (ci & 31));
+      }
     }
     uint32_t part = __ballot_sync(FULLMASK, valid && cls == PC_PARTIAL);
     while (part) {
@@ -517,6 +521,35 @@ __global__ void __launch_bounds__(256) paint_kernel(FoldArgs a) {
 // register j of the warp is the contiguous 128-byte slice pool[64 j .. 64 j + 63].
 // The warp applies its brick's ops in order, as apply() does (shapes.ts:367-412),
 // using the pair classifications.
+// The bricks the apply pass visits: those with a marked bit (one warp per 32
+// words of the bitmap, a warp-aggregated append).
+__global__ void __launch_bounds__(256) mark_compact_kernel(const uint32_t* __restrict__ bmark, uint32_t n_words,
+                                                           uint32_t* work, BuildResult* res) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t w0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; w0 < n_words; w0 += warps * 32) {
+    const uint32_t wi = w0 + lane;
+    const uint32_t bits = wi < n_words ? __ldg(bmark + wi) : 0u;
+    const uint32_t cnt = __popc(bits);
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(FULLMASK, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const uint32_t total = __shfl_sync(FULLMASK, incl, 31);
+    uint32_t base = 0;
+    if (lane == 31 && total) base = atomicAdd(&res->n_work, total);
+    base = __shfl_sync(FULLMASK, base, 31) + incl - cnt;
+    uint32_t b = bits;
+    while (b) {
+      const int k = __ffs(b) - 1;
+      b &= b - 1;
+      work[base++] = wi * 32u + (uint32_t)k;
+    }
+  }
+}
+
 // INLINE: some painted op has no paint slot (paint values past the slot
 // budget), so paint calls happen here too; otherwise the apply loop calls nothing.
 template <bool INLINE>
@@ -528,65 +561,74 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
   WarpCounters wc = {0, 0, 0, 0, 0};
   uint32_t paint_calls = 0, paint_viol = 0;
   uint32_t st_local = 0;
-  const uint32_t n_work = __ldg(&a.res->n_nonempty) * 64u;
+  const uint32_t n_work = __ldg(&a.res->n_work);
 
   for (;;) {
     uint32_t item = 0;
     if (lane == 0) item = atomicAdd(a.work_counter, 1u);
     item = __shfl_sync(FULLMASK, item, 0);
     if (item >= n_work) break;
-    const uint32_t tile = __ldg(a.tiles_nonempty + (item >> 6));
-    const int local = item & 63;
-    const int tz = tile / (a.TX * a.TY), rr = tile - tz * a.TX * a.TY, ty = rr / a.TX, tx = rr - ty * a.TX;
-    const int bx = tx * 4 + (local & 3), by = ty * 4 + ((local >> 2) & 3), bz = tz * 4 + (local >> 4);
-    if (bx >= a.BX || by >= a.BY || bz >= a.BZ) continue;
-    const size_t ci = (size_t)bx + (size_t)a.BX * ((size_t)by + (size_t)a.BY * bz);
+    const size_t ci = __ldg(a.work + item);
+    const int bx = (int)(ci % (size_t)a.BX), byz = (int)(ci / (size_t)a.BX), by = byz % a.BY, bz = byz / a.BY;
+    const uint32_t tile = (uint32_t)((bx >> 2) + a.TX * ((by >> 2) + a.TY * (bz >> 2)));
     const int ox = bx * 8, oy = by * 8, oz = bz * 8;
 
-    // current brick contents (VoxelWorld.ts:55-61)
-    const uint32_t g = a.grid[ci];
-    int state;
+    // current brick contents (VoxelWorld.ts:55-61), loaded when the first op applies
+    int state = ST_EMPTY;
     uint32_t uval = 0;
     uint32_t vox[8];
-    long long src;  // pool identity: >= 0 pair of the last alloc, < 0 -(old index + 1)
-    if (g == 0) {
-      state = ST_EMPTY; src = -1;
-#pragma unroll
-      for (int j = 0; j < 8; j++) vox[j] = 0;
-    } else if (g & UNIFORM) {
-      state = ST_UNIF; uval = g & 0xffffu; src = -1;
-#pragma unroll
-      for (int j = 0; j < 8; j++) vox[j] = uval | (uval << 16);
-    } else {
-      state = ST_MIXED; src = -(long long)(g - 1) - 1;
-      const uint32_t* pb = a.pool32 + (size_t)(g - 1) * 256;
-#pragma unroll
-      for (int j = 0; j < 8; j++) vox[j] = pb[32 * j + lane];
-    }
-    bool dirty = false;
+    long long src = -1;  // pool identity: >= 0 pair of the last alloc, < 0 -(old index + 1)
+    bool loaded = false, dirty = false;
 
     const uint32_t toff = __ldg(a.tile_off + tile), tcnt = __ldg(a.tile_cnt + tile);
     for (uint32_t c0 = 0; c0 < tcnt; c0 += 32) {
-      uint32_t oi = 0;
-      bool cov = false;
+      // each lane looks up one op of the tile: does it cover the brick, the
+      // pair's classes, and the op fields the apply loop needs (all loads in parallel)
+      uint32_t oi = 0, meta = 0, pval = 0, pslot = NO_SLOT, sc = 0;
+      unsigned long long pr = 0;
+      int ocls = PC_SKIP;
       if (c0 + lane < tcnt) {
         oi = __ldg(a.tile_ops + toff + c0 + lane);
         const OpDev* o = a.ops + oi;
-        cov = bx >= o->bx0 && bx <= o->bx1 && by >= o->by0 && by <= o->by1 && bz >= o->bz0 && bz <= o->bz1;
+        if (bx >= o->bx0 && bx <= o->bx1 && by >= o->by0 && by <= o->by1 && bz >= o->bz0 && bz <= o->bz1) {
+          pr = o->pair_base + (unsigned long long)(((bz - o->bz0) * o->ny + (by - o->by0)) * o->nx + (bx - o->bx0));
+          ocls = __ldg(a.pcode + pr);
+          sc = __ldg(a.psub + pr);  // meaningful for partial pairs only
+          meta = (uint32_t)o->kind | ((uint32_t)o->flags << 8) | ((uint32_t)o->paint_kind << 16);
+          pval = o->paint_value;
+          pslot = o->paint_slot == NO_SLOT ? NO_SLOT : o->paint_slot + (uint32_t)(pr - o->pair_base);
+        }
       }
-      uint32_t m = __ballot_sync(FULLMASK, cov);
+      uint32_t m = __ballot_sync(FULLMASK, ocls != PC_SKIP);  // shapes.ts:364 skips the rest
+      if (m && !loaded) {
+        loaded = true;
+        const uint32_t g = a.grid[ci];
+        if (g == 0) {
+#pragma unroll
+          for (int j = 0; j < 8; j++) vox[j] = 0;
+        } else if (g & UNIFORM) {
+          state = ST_UNIF; uval = g & 0xffffu;
+#pragma unroll
+          for (int j = 0; j < 8; j++) vox[j] = uval | (uval << 16);
+        } else {
+          state = ST_MIXED; src = -(long long)(g - 1) - 1;
+          const uint32_t* pb = a.pool32 + (size_t)(g - 1) * 256;
+#pragma unroll
+          for (int j = 0; j < 8; j++) vox[j] = pb[32 * j + lane];
+        }
+      }
       while (m) {
         const int b = __ffs(m) - 1;
         m &= m - 1;
+        const unsigned long long pair = __shfl_sync(FULLMASK, pr, b);
+        const int cls = __shfl_sync(FULLMASK, ocls, b);
+        const uint32_t mt = __shfl_sync(FULLMASK, meta, b);
+        const uint32_t pv = __shfl_sync(FULLMASK, pval, b);
+        const uint32_t slot = __shfl_sync(FULLMASK, pslot, b);
         const uint32_t o_idx = __shfl_sync(FULLMASK, oi, b);
-        const OpDev* O = a.ops + o_idx;
-        const unsigned long long pair = O->pair_base +
-            (unsigned long long)(((bz - O->bz0) * O->ny + (by - O->by0)) * O->nx + (bx - O->bx0));
-        const int cls = __ldg(a.pcode + pair);
-        if (cls == PC_SKIP) continue;  // shapes.ts:364
         const bool full = cls == PC_FULL;
-        const int kind = O->kind, flags = O->flags;
-        const uint32_t pk = O->paint_kind, pv = O->paint_value;
+        const int kind = (int)(mt & 0xffu);
+        const uint32_t pk = mt >> 16;
         const bool constPaint = pk == PK_CONST;
         // uniform shortcuts (shapes.ts:367-374)
         int set_u = -1;
@@ -613,15 +655,15 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
 
         // sub-block and voxel classes (shapes.ts:382-394), computed by classify_kernel
         if (!full) {
-          const uint32_t sc = __ldg(a.psub + pair);
+          const uint32_t psc = __shfl_sync(FULLMASK, sc, b);
           if (lane < 8) {
-            const uint32_t c = (sc >> (2 * lane)) & 3u;
+            const uint32_t c = (psc >> (2 * lane)) & 3u;
             smask[wib][lane] = c == PC_FULL ? ~0ull : c == PC_PARTIAL ? __ldg(a.pmask + pair * 8 + lane) : 0ull;
           }
           wc.sub += 8;
           uint32_t np_ = 0;
 #pragma unroll
-          for (int s2 = 0; s2 < 8; s2++) np_ += ((sc >> (2 * s2)) & 3u) == PC_PARTIAL;
+          for (int s2 = 0; s2 < 8; s2++) np_ += ((psc >> (2 * s2)) & 3u) == PC_PARTIAL;
           wc.vox += 64 * np_;
         } else if (lane < 8) {
           smask[wib][lane] = ~0ull;
@@ -642,15 +684,14 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
             uint32_t next;
             if (kind == KIND_CARVE) next = 0;
             else if (kind == KIND_PAINT && cur == 0) continue;
-            else if (!constPaint && O->paint_slot != NO_SLOT) {  // evaluated by paint_kernel
-              const uint32_t pvv = __ldg(a.pvals + (size_t)(O->paint_slot + (uint32_t)(pair - O->pair_base)) * 512 +
-                                         (uint32_t)((lx0 + h) | (ly << 3) | (j << 6)));
+            else if (!constPaint && slot != NO_SLOT) {  // evaluated by paint_kernel
+              const uint32_t pvv = __ldg(a.pvals + (size_t)slot * 512 + (uint32_t)((lx0 + h) | (ly << 3) | (j << 6)));
               if (pvv & PV_RANGE) st_local |= ST_RANGE;
               next = pvv & 0xffffu;
               paint_calls++;
             } else if (!constPaint) {
               if constexpr (INLINE) {
-                const uint32_t pv2 = paint_at_voxel(a.params, a.vs, a.validate, O, ox + lx0 + h, oy + ly, oz + j);
+                const uint32_t pv2 = paint_at_voxel(a.params, a.vs, a.validate, a.ops + o_idx, ox + lx0 + h, oy + ly, oz + j);
                 if (pv2 & PV_RANGE) st_local |= ST_RANGE;
                 if (pv2 & PV_VIOL) paint_viol++;
                 next = pv2 & 0xffffu;
@@ -752,6 +793,11 @@ void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEve
     else { ++g_launches; paint_kernel<0><<<grid(4), 256, 0, s>>>(a); }
   }
   if (mid) cudaEventRecord(mid, s);
+  {
+    const uint32_t n_words = (uint32_t)(((size_t)a.BX * a.BY * a.BZ + 31) / 32);
+    const uint32_t blocks = (n_words + 255) / 256;  // 8 warps per block, 32 words per warp
+    ++g_launches; mark_compact_kernel<<<blocks < 4096 ? blocks : 4096, 256, 0, s>>>(a.bmark, n_words, a.work, a.res);
+  }
   if (a.inline_paints) { ++g_launches; fold_kernel<true><<<grid(PX_FOLD_MINB), 256, 0, s>>>(a); }
   else { ++g_launches; fold_kernel<false><<<grid(PX_FOLD_MINB), 256, 0, s>>>(a); }
 }

@@ -63,6 +63,7 @@ struct px_world {
   DevBuf chunk_op, pcode, psub, pmask, chunk_counter, vitems;
   std::vector<uint32_t> h_chunk_op;
   DevBuf heavy, pvals;          // heavy-paint ops (op index, first slot) and their paint values
+  DevBuf bmark, work;           // bricks the apply pass visits (bitmap, list)
   std::vector<uint32_t> h_heavy;
   DevBuf scan_agg;
   DevBuf work_counter;
@@ -377,7 +378,7 @@ void px_world_destroy(px_world* w) {
                     &w->ew, &w->depth_fn, &w->depth, &w->tree, &w->fresh, &w->fresh_rank, &w->staging, &w->touched,
                     &w->stage_cell, &w->stage_src, &w->chunk_op, &w->pcode, &w->psub, &w->pmask,
                     &w->chunk_counter, &w->vitems, &w->scan_agg, &w->work_counter, &w->res, &w->opaque,
-                    &w->udens, &w->super_counts, &w->density, &w->heavy, &w->pvals};
+                    &w->udens, &w->super_counts, &w->density, &w->heavy, &w->pvals, &w->bmark, &w->work};
   for (DevBuf* b : bufs) release(*b);
   if (w->h_res) cudaFreeHost(w->h_res);
   if (w->ev0) cudaEventDestroy(w->ev0);
@@ -734,7 +735,8 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
       (rc = ensure(w, w->chunk_op, 4 * ((P + 31) / 32))) || (rc = ensure(w, w->pcode, P)) ||
       (rc = ensure(w, w->psub, 2 * P)) || (rc = ensure(w, w->pmask, 64 * P)) || (rc = ensure(w, w->chunk_counter, 16)) ||
       (rc = ensure(w, w->vitems, 8 * 8 * P)) || (rc = ensure(w, w->heavy, 4 * w->h_heavy.size() + 4)) ||
-      (rc = ensure(w, w->pvals, 2048 * n_slots + 4)))
+      (rc = ensure(w, w->pvals, 2048 * n_slots + 4)) || (rc = ensure(w, w->bmark, 4 * ((w->ncells + 31) / 32))) ||
+      (rc = ensure(w, w->work, 4 * touched_bound + 4)))
     return rc;
   {
     size_t items = w->ntiles > E_max ? w->ntiles : E_max;
@@ -802,6 +804,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
     if (n_chunks) CU(cudaMemcpyAsync(w->chunk_op.p, w->h_chunk_op.data(), 4 * n_chunks, cudaMemcpyHostToDevice, s));
   }
   if (P) CU(cudaMemsetAsync(w->evt.p, 0, P, s));
+  CU(cudaMemsetAsync(w->bmark.p, 0, 4 * ((w->ncells + 31) / 32), s));
   if (n_heavy && upload)
     CU(cudaMemcpyAsync(w->heavy.p, w->h_heavy.data(), 4 * w->h_heavy.size(), cudaMemcpyHostToDevice, s));
 
@@ -830,6 +833,8 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   fa.heavy_slot = (const uint32_t*)w->heavy.p + n_heavy;
   fa.pvals = (uint32_t*)w->pvals.p;
   fa.inline_paints = inline_paints ? 1 : 0;
+  fa.bmark = (uint32_t*)w->bmark.p;
+  fa.work = (uint32_t*)w->work.p;
   fa.ops = (const OpDev*)w->d_ops.p;
   fa.code = (const uint2*)w->d_code.p;
   fa.params = (const double*)w->d_params.p;

@@ -115,6 +115,7 @@ struct BuildResult {
   uint32_t stage_count;  // bricks that end as pool bricks and were touched (staging slots wanted)
   uint32_t touched_count;  // bricks whose grid entry the build rewrites
   uint32_t n_nonempty;   // tiles with at least one op
+  uint32_t n_work;       // bricks with at least one (op, brick) pair that is not skipped
   uint32_t n_fresh;
   uint32_t max_pool_index;
   BuildCounters c;
@@ -143,6 +144,8 @@ struct FoldArgs {
   const uint32_t* heavy_slot; // their first slots
   uint32_t* pvals;            // 512 paint values per slot (voxel index order); PV_RANGE flags
   int inline_paints;          // some painted op has no slot: fold_kernel calls its paints itself
+  uint32_t* bmark;            // one bit per brick: some pair of it is not skipped (classify_kernel)
+  uint32_t* work;             // those bricks (cell indices), listed by mark_compact_kernel
   const OpDev* ops;
   const uint2* code;
   const double* params;
