@@ -323,12 +323,15 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
                                        pbz * 8 + ((s >> 2) & 1) * 4);
       const bool push = sl >= 0 && scls == PC_PARTIAL && !boxr;
       const uint32_t vm = __ballot_sync(FULLMASK, push);
-      uint32_t base = 0;
-      if (lane == 0 && vm) base = atomicAdd(&a.vitem_counter[0], (uint32_t)__popc(vm));
-      base = __shfl_sync(FULLMASK, base, 0);
-      if (push) {
-        const uint32_t slot = base + __popc(vm & ((1u << lane) - 1u));
-        if (slot < a.vitems_cap) a.vitems[slot] = make_uint2(oo, (uint32_t)(pp << 3) | (uint32_t)s);
+      if (push) {  // one append per shape class present among the pushing lanes
+        const uint32_t k = a.ops[oo].vclass & (VCLASSES - 1);
+        const uint32_t grp = __match_any_sync(vm, k);
+        const int leader = __ffs(grp) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(&a.vitem_counter[1 + k], (uint32_t)__popc(grp));
+        base = __shfl_sync(grp, base, leader);
+        const uint32_t slot = base + __popc(grp & ((1u << lane) - 1u));
+        if (slot < a.vq_cap[k]) a.vitems[a.vq_base[k] + slot] = make_uint2(oo, (uint32_t)(pp << 3) | (uint32_t)s);
         else st_local |= ST_STAGE_OVERFLOW;
       }
     }
@@ -366,13 +369,23 @@ template <int MODE>
 __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIFY64_MINB) voxel_kernel(FoldArgs a) {
   const int lane = threadIdx.x & 31;
   LaneStats ls = {0, 0, 0, 0.f, 0, 0, 0, 0};
-  const uint32_t n_items = min(__ldg(&a.vitem_counter[0]), a.vitems_cap);
+  // the classes' item counts, as an inclusive prefix over lanes 0..VCLASSES-1
+  uint32_t incl = lane < VCLASSES ? min(__ldg(&a.vitem_counter[1 + lane]), a.vq_cap[lane]) : 0u;
+  const uint32_t own = incl;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(FULLMASK, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const uint32_t n_items = __shfl_sync(FULLMASK, incl, 31);
   for (;;) {
     uint32_t it = 0;
-    if (lane == 0) it = atomicAdd(&a.vitem_counter[1], 1u);
+    if (lane == 0) it = atomicAdd(&a.vitem_counter[0], 1u);
     it = __shfl_sync(FULLMASK, it, 0);
     if (it >= n_items) break;
-    const uint2 item = __ldg(a.vitems + it);
+    const int k = __popc(__ballot_sync(FULLMASK, lane < VCLASSES && incl <= it));  // class of item `it`
+    const uint32_t first = __shfl_sync(FULLMASK, incl - own, k);
+    const uint2 item = __ldg(a.vitems + a.vq_base[k] + (it - first));
     const OpDev* V = a.ops + item.x;
     const unsigned long long vp = item.y >> 3;
     const int ss = item.y & 7;
@@ -573,12 +586,29 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
     const uint32_t tile = (uint32_t)((bx >> 2) + a.TX * ((by >> 2) + a.TY * (bz >> 2)));
     const int ox = bx * 8, oy = by * 8, oz = bz * 8;
 
-    // current brick contents (VoxelWorld.ts:55-61), loaded when the first op applies
+    // current brick contents (VoxelWorld.ts:55-61); every listed brick has an op
+    // that applies, so they are loaded up front, overlapping the op lookups
     int state = ST_EMPTY;
     uint32_t uval = 0;
     uint32_t vox[8];
     long long src = -1;  // pool identity: >= 0 pair of the last alloc, < 0 -(old index + 1)
-    bool loaded = false, dirty = false;
+    bool dirty = false;
+    {
+      const uint32_t g = a.grid[ci];
+      if (g == 0) {
+#pragma unroll
+        for (int j = 0; j < 8; j++) vox[j] = 0;
+      } else if (g & UNIFORM) {
+        state = ST_UNIF; uval = g & 0xffffu;
+#pragma unroll
+        for (int j = 0; j < 8; j++) vox[j] = uval | (uval << 16);
+      } else {
+        state = ST_MIXED; src = -(long long)(g - 1) - 1;
+        const uint32_t* pb = a.pool32 + (size_t)(g - 1) * 256;
+#pragma unroll
+        for (int j = 0; j < 8; j++) vox[j] = pb[32 * j + lane];
+      }
+    }
 
     const uint32_t toff = __ldg(a.tile_off + tile), tcnt = __ldg(a.tile_cnt + tile);
     for (uint32_t c0 = 0; c0 < tcnt; c0 += 32) {
@@ -600,23 +630,6 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
         }
       }
       uint32_t m = __ballot_sync(FULLMASK, ocls != PC_SKIP);  // shapes.ts:364 skips the rest
-      if (m && !loaded) {
-        loaded = true;
-        const uint32_t g = a.grid[ci];
-        if (g == 0) {
-#pragma unroll
-          for (int j = 0; j < 8; j++) vox[j] = 0;
-        } else if (g & UNIFORM) {
-          state = ST_UNIF; uval = g & 0xffffu;
-#pragma unroll
-          for (int j = 0; j < 8; j++) vox[j] = uval | (uval << 16);
-        } else {
-          state = ST_MIXED; src = -(long long)(g - 1) - 1;
-          const uint32_t* pb = a.pool32 + (size_t)(g - 1) * 256;
-#pragma unroll
-          for (int j = 0; j < 8; j++) vox[j] = pb[32 * j + lane];
-        }
-      }
       while (m) {
         const int b = __ffs(m) - 1;
         m &= m - 1;

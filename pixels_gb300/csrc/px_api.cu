@@ -524,6 +524,12 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
       }
     }
     d.code_len = o.code_len;
+    {  // voxel work class: the primitive of a one-primitive shape (an offset may follow)
+      const uint32_t op0 = code[2 * (size_t)o.code_begin] & 0xffu;
+      const bool lone = o.code_len == 1 ||
+                        (o.code_len == 2 && (code[2 * ((size_t)o.code_begin + 1)] & 0xffu) == OP_OFFSET);
+      d.vclass = lone && op0 < (uint32_t)VCLASSES ? op0 : 0u;
+    }
     d.paint_off = (uint32_t)(param_base + o.paint_param);
     for (int k = 0; k < 3; k++) { d.mn[k] = o.mn[k]; d.mx[k] = o.mx[k]; }
     for (int k = 0; k < 4; k++) d.frame[k] = o.frame[k];
@@ -733,7 +739,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
       (rc = ensure(w, w->touched, 8 * touched_bound)) ||
       (rc = ensure(w, w->work_counter, 16)) || (rc = ensure(w, w->res, sizeof(BuildResult))) ||
       (rc = ensure(w, w->chunk_op, 4 * ((P + 31) / 32))) || (rc = ensure(w, w->pcode, P)) ||
-      (rc = ensure(w, w->psub, 2 * P)) || (rc = ensure(w, w->pmask, 64 * P)) || (rc = ensure(w, w->chunk_counter, 16)) ||
+      (rc = ensure(w, w->psub, 2 * P)) || (rc = ensure(w, w->pmask, 64 * P)) || (rc = ensure(w, w->chunk_counter, 16 + 4 * (VCLASSES + 2))) ||
       (rc = ensure(w, w->vitems, 8 * 8 * P)) || (rc = ensure(w, w->heavy, 4 * w->h_heavy.size() + 4)) ||
       (rc = ensure(w, w->pvals, 2048 * n_slots + 4)) || (rc = ensure(w, w->bmark, 4 * ((w->ncells + 31) / 32))) ||
       (rc = ensure(w, w->work, 4 * touched_bound + 4)))
@@ -791,7 +797,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   }
   CU(cudaMemsetAsync(w->res.p, 0, sizeof(BuildResult), s));
   CU(cudaMemsetAsync(w->work_counter.p, 0, 16, s));
-  CU(cudaMemsetAsync(w->chunk_counter.p, 0, 16, s));
+  CU(cudaMemsetAsync(w->chunk_counter.p, 0, 16 + 4 * (VCLASSES + 2), s));
   if (upload) {  // op of the first pair of every 32-pair chunk
     const size_t n_chunks = (P + 31) / 32;
     w->h_chunk_op.resize(n_chunks);
@@ -826,6 +832,20 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   fa.vitems = (uint2*)w->vitems.p;
   fa.vitems_cap = (uint32_t)(8 * P < 0xffffffffull ? 8 * P : 0xffffffffull);
   fa.vitem_counter = (uint32_t*)w->chunk_counter.p + 2;
+  {  // per-class regions: 8 sub-blocks per pair of the class's ops
+    uint64_t per[VCLASSES] = {0};
+    for (int i = 0; i < n_ops; i++) {
+      const OpDev& o = w->ops[i];
+      if (o.bx0 > o.bx1) continue;
+      per[o.vclass & (VCLASSES - 1)] += 8ull * o.nx * o.ny * (uint64_t)(o.bz1 - o.bz0 + 1);
+    }
+    uint64_t at = 0;
+    for (int k = 0; k < VCLASSES; k++) {
+      fa.vq_base[k] = (uint32_t)std::min<uint64_t>(at, 0xffffffffull);
+      fa.vq_cap[k] = (uint32_t)std::min<uint64_t>(per[k], 0xffffffffull - fa.vq_base[k]);
+      at += per[k];
+    }
+  }
   fa.paint_counter = (uint32_t*)w->chunk_counter.p + 1;
   fa.n_paint_slots = (uint32_t)n_slots;
   fa.n_heavy = n_heavy;

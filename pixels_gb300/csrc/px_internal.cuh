@@ -70,7 +70,7 @@ struct OpDev {
   uint8_t kind, flags;
   uint16_t paint_kind;
   uint32_t paint_value;
-  uint32_t pad;
+  uint32_t vclass;                       // voxel work class (VCLASSES)
   double bhd, shd;                       // brickHalfDiag, subHalfDiag (shapes.ts:349-350)
   double mn[3], mx[3];                   // contains box (boxes only)
   double frame[4];                       // paint frame px, pz, cos, sin
@@ -126,6 +126,11 @@ struct BuildResult {
 // sub-block classes of partial pairs, and voxel inside-masks of partial sub-blocks.
 enum : uint8_t { PC_SKIP = 0, PC_PARTIAL = 1, PC_FULL = 2 };
 
+// Voxel work items are grouped by the op's shape (its primitive when the code
+// is one primitive, optionally followed by an offset; class 0 otherwise), so
+// that warps draining the queue at the same time run the same code.
+constexpr int VCLASSES = 16;
+
 struct FoldArgs {
   const uint32_t* chunk_op;   // op containing pair 32 * chunk
   uint32_t n_ops;
@@ -136,7 +141,8 @@ struct FoldArgs {
   uint32_t* chunk_counter;
   uint2* vitems;              // partial sub-blocks to classify voxel by voxel: (op, pair << 3 | sub)
   uint32_t vitems_cap;
-  uint32_t* vitem_counter;    // [0] items pushed, [1] items taken
+  uint32_t* vitem_counter;    // [0] items taken, [1 + k] items pushed to class k
+  uint32_t vq_base[VCLASSES], vq_cap[VCLASSES];  // per-class regions of vitems
   uint32_t* paint_counter;    // paint_kernel items taken
   uint32_t n_paint_slots;     // (op, brick) pairs of heavy-paint ops
   uint32_t n_heavy;           // heavy-paint ops, ascending slots
