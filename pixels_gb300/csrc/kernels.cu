@@ -136,6 +136,21 @@ struct LaneStats {
   uint32_t rb, rs, rv, rp;
 };
 
+// Work items taken by a warp from a shared counter, several per atomic (one
+// counter for the whole grid: fewer same-address atomics).
+struct WorkBatch {
+  uint32_t at = 0, end = 0;
+  __device__ __forceinline__ uint32_t next(uint32_t* counter, uint32_t batch, int lane) {
+    if (at == end) {
+      uint32_t b = 0;
+      if (lane == 0) b = atomicAdd(counter, batch);
+      at = __shfl_sync(FULLMASK, b, 0);
+      end = at + batch;
+    }
+    return at++;
+  }
+};
+
 // Decisions of apply() from a float32 interval (thresholds certified on the host):
 // brick/sub-block: 0 = outside (skip), 1 = partial, 2 = full, 3 = undecided.
 __device__ __forceinline__ int classify32(Iv d, const float* thr, int base) {
@@ -378,10 +393,9 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
     if (lane >= o) incl += t;
   }
   const uint32_t n_items = __shfl_sync(FULLMASK, incl, 31);
+  WorkBatch wb;
   for (;;) {
-    uint32_t it = 0;
-    if (lane == 0) it = atomicAdd(&a.vitem_counter[0], 1u);
-    it = __shfl_sync(FULLMASK, it, 0);
+    const uint32_t it = wb.next(&a.vitem_counter[0], 1, lane);
     if (it >= n_items) break;
     const int k = __popc(__ballot_sync(FULLMASK, lane < VCLASSES && incl <= it));  // class of item `it`
     const uint32_t first = __shfl_sync(FULLMASK, incl - own, k);
@@ -464,10 +478,9 @@ __global__ void __launch_bounds__(256) paint_kernel(FoldArgs a) {
   const int lane = threadIdx.x & 31;
   const uint32_t n_items = a.n_paint_slots * 8u;
   uint32_t resc = 0, viol = 0;
+  WorkBatch wb;
   for (;;) {
-    uint32_t it = 0;
-    if (lane == 0) it = atomicAdd(a.paint_counter, 1u);
-    it = __shfl_sync(FULLMASK, it, 0);
+    const uint32_t it = wb.next(a.paint_counter, 2, lane);
     if (it >= n_items) break;
     const uint32_t slot = it >> 3;
     const int s = (int)(it & 7u);
@@ -576,10 +589,9 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
   uint32_t st_local = 0;
   const uint32_t n_work = __ldg(&a.res->n_work);
 
+  WorkBatch wb;
   for (;;) {
-    uint32_t item = 0;
-    if (lane == 0) item = atomicAdd(a.work_counter, 1u);
-    item = __shfl_sync(FULLMASK, item, 0);
+    const uint32_t item = wb.next(a.work_counter, 4, lane);
     if (item >= n_work) break;
     const size_t ci = __ldg(a.work + item);
     const int bx = (int)(ci % (size_t)a.BX), byz = (int)(ci / (size_t)a.BX), by = byz % a.BY, bz = byz / a.BY;
