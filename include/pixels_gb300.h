@@ -151,6 +151,10 @@ int px_set_material_tables(px_world* w, const uint8_t* opaque256, const uint8_t*
 int px_set_validation(px_world* w, int on);
 
 int px_get_stats(px_world* w, px_stats* out);
+/* Grow the device pool to at least `bricks` bricks now (the contents are kept),
+   so that later builds do not stop to grow it; GpuWorld.ts:57 sizes the GPU
+   pool to max(used + 98304, 2 used) at upload in the same spirit. */
+int px_reserve_pool(px_world* w, uint64_t bricks);
 int px_device_view_get(px_world* w, px_device_view* out);
 /* Dims (voxels) and voxel density of a world. */
 int px_world_info(px_world* w, int dims[3], double* vpm);
@@ -177,7 +181,8 @@ typedef struct px_edit_result {
    releases them in real time; each build step takes every released edit, in
    arrival order, up to max_batch, whose worst-case pool growth (bricks in its
    box) fits pool_budget_bricks minus the live bricks, and builds them together
-   on the resident world.  applied_order (n entries, may be NULL) receives the
+   on the resident world.  Before the first edit the pool is reserved to
+   min(pool_budget_bricks, max(used + 98304, 2 used)) bricks (GpuWorld.ts:57).  applied_order (n entries, may be NULL) receives the
    edit indices in the order applied.  Blocks until every edit is applied or
    rejected. */
 int px_serve_run(px_world* w, const px_edit* edits, const double* arrival_s, size_t n, uint32_t max_batch,

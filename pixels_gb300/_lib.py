@@ -26,6 +26,7 @@ EXPORTS = [
     "px_read_density", "px_read_free_list", "px_set_material_tables", "px_set_validation", "px_get_stats",
     "px_device_view_get", "px_last_error", "px_probe_peak", "px_world_info", "px_serve_run", "px_derive_noalloc",
     "px_batch_create", "px_batch_run", "px_batch_destroy", "px_batch_last_error", "px_snap_anchors",
+    "px_reserve_pool",
 ]
 
 
@@ -106,6 +107,7 @@ def load(path: str = LIB_PATH):
     L.px_batch_last_error.argtypes = [vp]
     L.px_batch_last_error.restype = ctypes.c_char_p
     L.px_snap_anchors.argtypes = [vp, vp, sz, vp, vp]
+    L.px_reserve_pool.argtypes = [vp, ctypes.c_uint64]
     L.px_derive_noalloc.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, u32, vp, vp, vp, vp, vp]
     _L = L
     return L

@@ -1161,6 +1161,12 @@ int px_device_view_get(px_world* w, px_device_view* out) {
   return PX_OK;
 }
 
+int px_reserve_pool(px_world* w, uint64_t bricks) {
+  if (!w) return PX_E_INVALID_ARG;
+  if (w->in_flight || w->batch_locked) return fail(w, PX_E_INVALID_ARG, "the world is busy");
+  return grow_pool(w, bricks, w->pool_used, nullptr);
+}
+
 const char* px_last_error(px_world* w) { return w ? w->err.c_str() : "null world"; }
 
 int px_probe_peak(int fp64, float* tflops) {

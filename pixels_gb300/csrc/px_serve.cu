@@ -103,6 +103,13 @@ int px_serve_run(px_world* w, const px_edit* edits, const double* arrival_s, siz
   px_stats st;
   px_get_stats(w, &st);
   uint64_t live = (uint64_t)st.pool_used - st.n_holes;
+  {  // the pool the serving loop works in, allocated before the clock starts (GpuWorld.ts:57)
+    const uint64_t used = st.pool_used;
+    uint64_t cap = std::max<uint64_t>(used + 98304, 2 * used);
+    if (cap > pool_budget_bricks) cap = pool_budget_bricks;
+    const int rc0 = px_reserve_pool(w, cap);
+    if (rc0 != PX_OK) return rc0;
+  }
 
   // arrival order
   std::vector<size_t> order(n);

@@ -79,5 +79,6 @@ def latency_stats(results) -> dict:
         "max_ms": float(lat.max()) if len(ok) else None,
         "edits_per_s": float(len(ok) / span) if span > 0 else None,
         "batches": int(len(np.unique(ok["batch"]))) if len(ok) else 0,
+        "max_step_ms": float(((ok["done_s"] - ok["start_s"]) * 1e3).max()) if len(ok) else None,
         "mean_batch": float(len(ok) / max(len(np.unique(ok["batch"])), 1)) if len(ok) else 0.0,
     }
