@@ -294,6 +294,11 @@ def serving_section(args, pyoracle):
     return out
 
 
+# DRAM bytes per build of the evaluation kernels, from one ncu capture of each
+# (profiles/build_kernels_penthouse_vpm80.md); the bench cannot run ncu itself
+EVAL_TRAFFIC_BYTES = 29_622_784
+
+
 def hbm_line(cfg, pool_used, ir_bytes, ms):
     """Algorithmic HBM bytes of one build (outputs written + the op list read
     once) over the build time, against the measured copy bandwidth."""
@@ -497,7 +502,9 @@ def main():
                 "d2h_bytes_per_step": int(grid_h.numel() * 4 + used * 1024),
                 "ms_per_step": round(t_e2e * 1e3, 3)},
         "roofline": {"bound": "fp32-alu", "achieved": round(achieved, 4), "peak": round(peak32, 2),
-                     "unit": "TFLOP/s", "frac": round(achieved / peak32, 5), "traffic": None,
+                     "unit": "TFLOP/s", "frac": round(achieved / peak32, 5), "traffic": EVAL_TRAFFIC_BYTES,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the classify, voxel, "
+                                       "paint and apply kernels of one build (profiles/build_kernels_penthouse_vpm80.md)",
                      "kernel": "classify_kernel + voxel_kernel + fold_kernel (every SDF and paint evaluation)",
                      "alg_ops_per_launch": int(alg_ops),
                      "fold_ms": round(fold_s * 1e3, 4),
