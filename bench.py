@@ -419,6 +419,7 @@ def main():
     pool_h = torch.empty(max(st["pool_used"], 1) * 512, dtype=torch.int16, pin_memory=True)
     ir_buf = __import__("ctypes").create_string_buffer(ir, len(ir))
     e2e = []
+    e2e_parts = []
     for i in range(0 if args.no_e2e else args.warmup + args.steps):
         torch.cuda.synchronize()
         barrier()
@@ -426,13 +427,16 @@ def main():
         _lib.world_reset(h, False, s_ptr)
         rc = L.px_submit_ops(h, ir_buf, len(ir))
         assert rc == 0
+        ta = time.perf_counter()
         _lib.build(h, MODE_MIXED, s_ptr)
         used = _lib.stats(h)["pool_used"]
+        tb = time.perf_counter()
         assert L.px_read_grid(h, grid_h.data_ptr(), grid_h.numel()) == 0
         assert L.px_read_pool(h, pool_h.data_ptr(), pool_h.numel()) == 0
         t1 = time.perf_counter()
         if i >= args.warmup:
             e2e.append(t1 - t0)
+            e2e_parts.append((ta - t0, tb - ta, t1 - tb))
     if not e2e:  # profiling run: one readback for the mismatch check
         assert L.px_read_grid(h, grid_h.data_ptr(), grid_h.numel()) == 0
         used = _lib.stats(h)["pool_used"]
@@ -500,7 +504,10 @@ def main():
         "max_abs_d32_minus_d64": st["max_abs_err32"],
         "e2e": {"value": round(e2e_value, 4), "unit": UNIT, "h2d_bytes_per_step": len(ir),
                 "d2h_bytes_per_step": int(grid_h.numel() * 4 + used * 1024),
-                "ms_per_step": round(t_e2e * 1e3, 3)},
+                "ms_per_step": round(t_e2e * 1e3, 3),
+                "split_ms": ({k: round(statistics.mean(p[j] for p in e2e_parts) * 1e3, 3)
+                              for j, k in enumerate(("reset_and_submit", "build", "read_grid_and_pool"))}
+                             if e2e_parts else None)},
         "roofline": {"bound": "fp32-alu", "achieved": round(achieved, 4), "peak": round(peak32, 2),
                      "unit": "TFLOP/s", "frac": round(achieved / peak32, 5), "traffic": EVAL_TRAFFIC_BYTES,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the classify, voxel, "

@@ -299,56 +299,19 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
         atomicOr(a.bmark + (ci >> 5), 1u << (ci & 31));
       }
     }
-    uint32_t part = __ballot_sync(FULLMASK, valid && cls == PC_PARTIAL);
-    while (part) {
-      int src0 = -1, src1 = -1, src2 = -1, src3 = -1;
-      if (part) { src0 = __ffs(part) - 1; part &= part - 1; }
-      if (part) { src1 = __ffs(part) - 1; part &= part - 1; }
-      if (part) { src2 = __ffs(part) - 1; part &= part - 1; }
-      if (part) { src3 = __ffs(part) - 1; part &= part - 1; }
-      const int k = lane >> 3, s = lane & 7;
-      const int sl = k == 0 ? src0 : k == 1 ? src1 : k == 2 ? src2 : src3;
-      const int sll = sl < 0 ? 0 : sl;
-      const unsigned long long pp = __shfl_sync(FULLMASK, p, sll);
-      const uint32_t oo = __shfl_sync(FULLMASK, o, sll);
-      const int pbx = __shfl_sync(FULLMASK, bx, sll), pby = __shfl_sync(FULLMASK, by, sll),
-                pbz = __shfl_sync(FULLMASK, bz, sll);
-      int scls = PC_SKIP;
-      bool boxr = false;
-      if (sl >= 0) {
-        const OpDev* Q = a.ops + oo;
-        boxr = (Q->flags & OPF_BOX_RANGES) && !a.validate;
-        const bool use32 = MODE == 1 && !(Q->flags & OPF_FP64_ONLY);
-        Iv bo[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-        if (use32) brick_bases(a, Q, pbx, pby, pbz, bo);
-        const int sxb = s & 1, syb = (s >> 1) & 1, szb = (s >> 2) & 1;
-        scls = eval_decide<MODE>(a, Q, a.code + Q->code_off, (int)Q->code_len, use32, bo, 4.f * sxb + 1.5f,
-                                 4.f * syb + 1.5f, 4.f * szb + 1.5f, (float)(pbx * 8 + sxb * 4 + 2),
-                                 (float)(pby * 8 + syb * 4 + 2), (float)(pbz * 8 + szb * 4 + 2), 2, ls);
-      }
-      uint32_t code16 = (uint32_t)scls << (2 * s);
-      code16 |= __shfl_xor_sync(FULLMASK, code16, 1);
-      code16 |= __shfl_xor_sync(FULLMASK, code16, 2);
-      code16 |= __shfl_xor_sync(FULLMASK, code16, 4);
-      if (s == 0 && sl >= 0) a.psub[pp] = (uint16_t)code16;
-      // queue the partial sub-blocks (one warp-aggregated append); a lone box's
-      // voxel mask comes from its per-axis runs instead
-      if (boxr && scls == PC_PARTIAL)
-        a.pmask[pp * 8 + s] = box_mask(a.ops + oo, pbx * 8 + (s & 1) * 4, pby * 8 + ((s >> 1) & 1) * 4,
-                                       pbz * 8 + ((s >> 2) & 1) * 4);
-      const bool push = sl >= 0 && scls == PC_PARTIAL && !boxr;
-      const uint32_t vm = __ballot_sync(FULLMASK, push);
-      if (push) {  // one append per shape class present among the pushing lanes
-        const uint32_t k = a.ops[oo].vclass & (VCLASSES - 1);
-        const uint32_t grp = __match_any_sync(vm, k);
-        const int leader = __ffs(grp) - 1;
-        uint32_t base = 0;
-        if (lane == leader) base = atomicAdd(&a.vitem_counter[1 + k], (uint32_t)__popc(grp));
-        base = __shfl_sync(grp, base, leader);
-        const uint32_t slot = base + __popc(grp & ((1u << lane) - 1u));
-        if (slot < a.vq_cap[k]) a.vitems[a.vq_base[k] + slot] = make_uint2(oo, (uint32_t)(pp << 3) | (uint32_t)s);
-        else st_local |= ST_STAGE_OVERFLOW;
-      }
+    // partial pairs go to the sub-block pass, one queue region per shape class
+    const bool part = valid && cls == PC_PARTIAL;
+    const uint32_t pm = __ballot_sync(FULLMASK, part);
+    if (part) {
+      const uint32_t k = O->vclass & (VCLASSES - 1);
+      const uint32_t grp = __match_any_sync(pm, k);
+      const int leader = __ffs(grp) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(&a.pitem_counter[1 + k], (uint32_t)__popc(grp));
+      base = __shfl_sync(grp, base, leader);
+      const uint32_t slot = base + __popc(grp & ((1u << lane) - 1u));
+      if (slot < a.pq_cap[k]) a.pitems[a.pq_base[k] + slot] = make_uint2(o, (uint32_t)p);
+      else st_local |= ST_STAGE_OVERFLOW;
     }
   }
   uint32_t nb = n_brick, rc = ls.resc, vc = ls.viol, rb = ls.rb, rs = ls.rs, rv = ls.rv, rp = ls.rp, stw = st_local;
@@ -372,6 +335,102 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
     if (rb) atomicAdd(&a.res->c.resc_brick, (unsigned long long)rb);
     if (rs) atomicAdd(&a.res->c.resc_sub, (unsigned long long)rs);
     if (rv) atomicAdd(&a.res->c.resc_vox, (unsigned long long)rv);
+    if (rp) atomicAdd(&a.res->c.resc_poly, (unsigned long long)rp);
+    if (stw) atomicOr(&a.res->status, stw);
+    if (me > 0.f) atomicMax(&a.res->max_err_bits, (unsigned long long)__double_as_longlong((double)me));
+  }
+}
+
+// Sub-block classes of the partial pairs (shapes.ts:382-389): four pairs per
+// warp pass (8 lanes each, one sub-block per lane), pairs taken in shape-class
+// order like the voxel work.  Writes the pair's 2-bit sub-block classes, the
+// voxel masks of lone boxes (per-axis runs), and queues the partial sub-blocks.
+template <int MODE>
+__global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIFY64_MINB) sub_kernel(FoldArgs a) {
+  const int lane = threadIdx.x & 31;
+  LaneStats ls = {0, 0, 0, 0.f, 0, 0, 0, 0};
+  uint32_t st_local = 0;
+  uint32_t incl = lane < VCLASSES ? min(__ldg(&a.pitem_counter[1 + lane]), a.pq_cap[lane]) : 0u;
+  const uint32_t own = incl;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(FULLMASK, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const uint32_t n_items = __shfl_sync(FULLMASK, incl, 31);
+  const int g = lane >> 3, s = lane & 7;
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(&a.pitem_counter[0], 4u);
+    base = __shfl_sync(FULLMASK, base, 0);
+    if (base >= n_items) break;
+    // the class and queue position of each of the pass's four items
+    uint32_t my_k = 0, my_first = 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int kq = __popc(__ballot_sync(FULLMASK, lane < VCLASSES && incl <= base + q));
+      const uint32_t fq = __shfl_sync(FULLMASK, incl - own, kq & 31);
+      if (g == q) { my_k = (uint32_t)kq; my_first = fq; }
+    }
+    const uint32_t it = base + (uint32_t)g;
+    const bool have = it < n_items;
+    uint32_t oo = 0;
+    unsigned long long pp = 0;
+    int pbx = 0, pby = 0, pbz = 0, scls = PC_SKIP;
+    bool boxr = false;
+    if (have) {
+      const uint2 item = __ldg(a.pitems + a.pq_base[my_k] + (it - my_first));
+      oo = item.x;
+      pp = item.y;
+      const OpDev* Q = a.ops + oo;
+      brick_of_pair(Q, pp, pbx, pby, pbz);
+      boxr = (Q->flags & OPF_BOX_RANGES) && !a.validate;
+      const bool use32 = MODE == 1 && !(Q->flags & OPF_FP64_ONLY);
+      Iv bo[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+      if (use32) brick_bases(a, Q, pbx, pby, pbz, bo);
+      const int sxb = s & 1, syb = (s >> 1) & 1, szb = (s >> 2) & 1;
+      scls = eval_decide<MODE>(a, Q, a.code + Q->code_off, (int)Q->code_len, use32, bo, 4.f * sxb + 1.5f,
+                               4.f * syb + 1.5f, 4.f * szb + 1.5f, (float)(pbx * 8 + sxb * 4 + 2),
+                               (float)(pby * 8 + syb * 4 + 2), (float)(pbz * 8 + szb * 4 + 2), 2, ls);
+    }
+    uint32_t code16 = (uint32_t)scls << (2 * s);
+    code16 |= __shfl_xor_sync(FULLMASK, code16, 1);
+    code16 |= __shfl_xor_sync(FULLMASK, code16, 2);
+    code16 |= __shfl_xor_sync(FULLMASK, code16, 4);
+    if (s == 0 && have) a.psub[pp] = (uint16_t)code16;
+    // a lone box's voxel mask comes from its per-axis runs; other partial sub-blocks are queued
+    if (boxr && scls == PC_PARTIAL)
+      a.pmask[pp * 8 + s] = box_mask(a.ops + oo, pbx * 8 + (s & 1) * 4, pby * 8 + ((s >> 1) & 1) * 4,
+                                     pbz * 8 + ((s >> 2) & 1) * 4);
+    const bool push = have && scls == PC_PARTIAL && !boxr;
+    const uint32_t vm = __ballot_sync(FULLMASK, push);
+    if (push) {  // one append per shape class present among the pushing lanes
+      const uint32_t k = a.ops[oo].vclass & (VCLASSES - 1);
+      const uint32_t grp = __match_any_sync(vm, k);
+      const int leader = __ffs(grp) - 1;
+      uint32_t vb = 0;
+      if (lane == leader) vb = atomicAdd(&a.vitem_counter[1 + k], (uint32_t)__popc(grp));
+      vb = __shfl_sync(grp, vb, leader);
+      const uint32_t slot = vb + __popc(grp & ((1u << lane) - 1u));
+      if (slot < a.vq_cap[k]) a.vitems[a.vq_base[k] + slot] = make_uint2(oo, (uint32_t)(pp << 3) | (uint32_t)s);
+      else st_local |= ST_STAGE_OVERFLOW;
+    }
+  }
+  uint32_t rc = ls.resc, vc = ls.viol, rs = ls.rs, rp = ls.rp, stw = st_local;
+  float me = ls.max_err;
+#pragma unroll
+  for (int o2 = 16; o2; o2 >>= 1) {
+    rc += __shfl_xor_sync(FULLMASK, rc, o2);
+    vc += __shfl_xor_sync(FULLMASK, vc, o2);
+    rs += __shfl_xor_sync(FULLMASK, rs, o2);
+    rp += __shfl_xor_sync(FULLMASK, rp, o2);
+    stw |= __shfl_xor_sync(FULLMASK, stw, o2);
+    me = fmaxf(me, __shfl_xor_sync(FULLMASK, me, o2));
+  }
+  if (lane == 0) {
+    if (rc) atomicAdd(&a.res->c.rescued, (unsigned long long)rc);
+    if (vc) atomicAdd(&a.res->c.violations, (unsigned long long)vc);
+    if (rs) atomicAdd(&a.res->c.resc_sub, (unsigned long long)rs);
     if (rp) atomicAdd(&a.res->c.resc_poly, (unsigned long long)rp);
     if (stw) atomicOr(&a.res->status, stw);
     if (me > 0.f) atomicMax(&a.res->max_err_bits, (unsigned long long)__double_as_longlong((double)me));
@@ -808,9 +867,11 @@ void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEve
   auto grid = [&](int per_sm) { return max_blocks > 0 && max_blocks < n_sms * per_sm ? max_blocks : n_sms * per_sm; };
   if (mode == 1) {
     ++g_launches; classify_kernel<1><<<grid(PX_CLASSIFY_MINB), 256, 0, s>>>(a);
+    ++g_launches; sub_kernel<1><<<grid(PX_CLASSIFY_MINB), 256, 0, s>>>(a);
     ++g_launches; voxel_kernel<1><<<grid(PX_CLASSIFY_MINB), 256, 0, s>>>(a);
   } else {
     ++g_launches; classify_kernel<0><<<grid(PX_CLASSIFY64_MINB), 256, 0, s>>>(a);
+    ++g_launches; sub_kernel<0><<<grid(PX_CLASSIFY64_MINB), 256, 0, s>>>(a);
     ++g_launches; voxel_kernel<0><<<grid(PX_CLASSIFY64_MINB), 256, 0, s>>>(a);
   }
   if (a.n_paint_slots) {

@@ -60,7 +60,7 @@ struct px_world {
   DevBuf evt, fsrc, cnt, pos, etype, ew, depth_fn, depth, tree, fresh, fresh_rank;
   DevBuf staging, stage_cell, stage_src, touched;
   uint64_t stage_hint = 0;      // staging slots the next build reserves (grown on overflow)
-  DevBuf chunk_op, pcode, psub, pmask, chunk_counter, vitems;
+  DevBuf chunk_op, pcode, psub, pmask, chunk_counter, vitems, pitems;
   std::vector<uint32_t> h_chunk_op;
   DevBuf heavy, pvals;          // heavy-paint ops (op index, first slot) and their paint values
   DevBuf bmark, work;           // bricks the apply pass visits (bitmap, list)
@@ -378,7 +378,7 @@ void px_world_destroy(px_world* w) {
                     &w->ew, &w->depth_fn, &w->depth, &w->tree, &w->fresh, &w->fresh_rank, &w->staging, &w->touched,
                     &w->stage_cell, &w->stage_src, &w->chunk_op, &w->pcode, &w->psub, &w->pmask,
                     &w->chunk_counter, &w->vitems, &w->scan_agg, &w->work_counter, &w->res, &w->opaque,
-                    &w->udens, &w->super_counts, &w->density, &w->heavy, &w->pvals, &w->bmark, &w->work};
+                    &w->udens, &w->super_counts, &w->density, &w->heavy, &w->pvals, &w->bmark, &w->work, &w->pitems};
   for (DevBuf* b : bufs) release(*b);
   if (w->h_res) cudaFreeHost(w->h_res);
   if (w->ev0) cudaEventDestroy(w->ev0);
@@ -739,7 +739,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
       (rc = ensure(w, w->touched, 8 * touched_bound)) ||
       (rc = ensure(w, w->work_counter, 16)) || (rc = ensure(w, w->res, sizeof(BuildResult))) ||
       (rc = ensure(w, w->chunk_op, 4 * ((P + 31) / 32))) || (rc = ensure(w, w->pcode, P)) ||
-      (rc = ensure(w, w->psub, 2 * P)) || (rc = ensure(w, w->pmask, 64 * P)) || (rc = ensure(w, w->chunk_counter, 16 + 4 * (VCLASSES + 2))) ||
+      (rc = ensure(w, w->psub, 2 * P)) || (rc = ensure(w, w->pmask, 64 * P)) || (rc = ensure(w, w->chunk_counter, 256)) || (rc = ensure(w, w->pitems, 8 * P)) ||
       (rc = ensure(w, w->vitems, 8 * 8 * P)) || (rc = ensure(w, w->heavy, 4 * w->h_heavy.size() + 4)) ||
       (rc = ensure(w, w->pvals, 2048 * n_slots + 4)) || (rc = ensure(w, w->bmark, 4 * ((w->ncells + 31) / 32))) ||
       (rc = ensure(w, w->work, 4 * touched_bound + 4)))
@@ -797,7 +797,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   }
   CU(cudaMemsetAsync(w->res.p, 0, sizeof(BuildResult), s));
   CU(cudaMemsetAsync(w->work_counter.p, 0, 16, s));
-  CU(cudaMemsetAsync(w->chunk_counter.p, 0, 16 + 4 * (VCLASSES + 2), s));
+  CU(cudaMemsetAsync(w->chunk_counter.p, 0, 256, s));
   if (upload) {  // op of the first pair of every 32-pair chunk
     const size_t n_chunks = (P + 31) / 32;
     w->h_chunk_op.resize(n_chunks);
@@ -832,20 +832,24 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   fa.vitems = (uint2*)w->vitems.p;
   fa.vitems_cap = (uint32_t)(8 * P < 0xffffffffull ? 8 * P : 0xffffffffull);
   fa.vitem_counter = (uint32_t*)w->chunk_counter.p + 2;
-  {  // per-class regions: 8 sub-blocks per pair of the class's ops
+  {  // per-class regions: the class's pairs (sub-block pass), 8 sub-blocks per pair (voxel pass)
     uint64_t per[VCLASSES] = {0};
     for (int i = 0; i < n_ops; i++) {
       const OpDev& o = w->ops[i];
       if (o.bx0 > o.bx1) continue;
-      per[o.vclass & (VCLASSES - 1)] += 8ull * o.nx * o.ny * (uint64_t)(o.bz1 - o.bz0 + 1);
+      per[o.vclass & (VCLASSES - 1)] += (uint64_t)o.nx * o.ny * (uint64_t)(o.bz1 - o.bz0 + 1);
     }
     uint64_t at = 0;
     for (int k = 0; k < VCLASSES; k++) {
-      fa.vq_base[k] = (uint32_t)std::min<uint64_t>(at, 0xffffffffull);
-      fa.vq_cap[k] = (uint32_t)std::min<uint64_t>(per[k], 0xffffffffull - fa.vq_base[k]);
+      fa.pq_base[k] = (uint32_t)at;
+      fa.pq_cap[k] = (uint32_t)per[k];
+      fa.vq_base[k] = (uint32_t)std::min<uint64_t>(8 * at, 0xffffffffull);
+      fa.vq_cap[k] = (uint32_t)std::min<uint64_t>(8 * per[k], 0xffffffffull - fa.vq_base[k]);
       at += per[k];
     }
   }
+  fa.pitems = (uint2*)w->pitems.p;
+  fa.pitem_counter = (uint32_t*)w->chunk_counter.p + 20;
   fa.paint_counter = (uint32_t*)w->chunk_counter.p + 1;
   fa.n_paint_slots = (uint32_t)n_slots;
   fa.n_heavy = n_heavy;

@@ -143,6 +143,9 @@ struct FoldArgs {
   uint32_t vitems_cap;
   uint32_t* vitem_counter;    // [0] items taken, [1 + k] items pushed to class k
   uint32_t vq_base[VCLASSES], vq_cap[VCLASSES];  // per-class regions of vitems
+  uint2* pitems;              // partial pairs for the sub-block pass: (op, pair)
+  uint32_t* pitem_counter;    // [0] items taken, [1 + k] items pushed to class k
+  uint32_t pq_base[VCLASSES], pq_cap[VCLASSES];  // per-class regions of pitems
   uint32_t* paint_counter;    // paint_kernel items taken
   uint32_t n_paint_slots;     // (op, brick) pairs of heavy-paint ops
   uint32_t n_heavy;           // heavy-paint ops, ascending slots
