@@ -4,6 +4,12 @@
 // (voxel ranges, classify thresholds) must round exactly as the reference's
 // JavaScript does (shapes.ts:341-350).
 #include <algorithm>
+#include <atomic>
+#include <condition_variable>
+#include <functional>
+#include <limits>
+#include <mutex>
+#include <thread>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -138,14 +144,32 @@ inline double js_max(double a, double b) { return a > b ? a : b; }  // finite in
 inline double js_min(double a, double b) { return a < b ? a : b; }
 
 // float32 enclosures of float64 values (mixed mode)
+// the neighbouring floats of a float (by its bit pattern; inlined, unlike nextafterf)
+inline float float_below(float f) {
+  if (f == 0.0f) return -std::numeric_limits<float>::denorm_min();
+  uint32_t b;
+  std::memcpy(&b, &f, 4);
+  b = f > 0.0f ? b - 1 : b + 1;
+  std::memcpy(&f, &b, 4);
+  return f;
+}
+inline float float_above(float f) {
+  if (f == 0.0f) return std::numeric_limits<float>::denorm_min();
+  uint32_t b;
+  std::memcpy(&b, &f, 4);
+  b = f > 0.0f ? b + 1 : b - 1;
+  std::memcpy(&f, &b, 4);
+  return f;
+}
+// float32 bounds of a float64 value: the largest float <= v, the smallest float >= v
 inline float rd32(double v) {
   float f = (float)v;
-  if ((double)f > v) f = std::nextafterf(f, -INFINITY);
+  if ((double)f > v) f = float_below(f);
   return f;
 }
 inline float ru32(double v) {
   float f = (float)v;
-  if ((double)f < v) f = std::nextafterf(f, INFINITY);
+  if ((double)f < v) f = float_above(f);
   return f;
 }
 inline float2 enc(double v, double pad = 0.0) { return make_float2(rd32(v - pad), ru32(v + pad)); }
@@ -434,93 +458,105 @@ bool paint_params32(uint32_t kind, bool framed, const double* p, const double A[
   return ok;
 }
 
-int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
-  if (!w || (!ir && bytes)) return PX_E_INVALID_ARG;
-  if (w->batch_locked) return fail(w, PX_E_INVALID_ARG, "the world belongs to a batch");
-  if (w->in_flight) return fail(w, PX_E_INVALID_ARG, "a build is in flight");
-  w->ops_resident = false;
-  if (bytes < 32) return fail(w, PX_E_INVALID_IR, "IR shorter than its header");
-  const uint32_t* h = (const uint32_t*)ir;
-  if (h[0] != 0x52495850u || h[1] != 1u) return fail(w, PX_E_INVALID_IR, "not a PXIR v1 buffer");
-  const size_t n_ops = h[2], n_code = h[3], n_params = h[4];
-  const size_t need = 32 + n_ops * sizeof(IrOp) + n_code * 8 + n_params * 8;
-  if (bytes < need) return fail(w, PX_E_INVALID_IR, "IR truncated (%zu < %zu bytes)", bytes, need);
-  const IrOp* iops = (const IrOp*)((const char*)ir + 32);
-  const uint32_t* code = (const uint32_t*)((const char*)ir + 32 + n_ops * sizeof(IrOp));
-  std::vector<double> P(n_params);
-  std::memcpy(P.data(), (const char*)ir + 32 + n_ops * sizeof(IrOp) + n_code * 8, n_params * 8);
+}  // extern "C"
 
-  const size_t code_base = w->code.size(), param_base = w->params.size();
-  std::vector<OpDev> nops;
-  std::vector<uint2> nboxes;
-  std::vector<uint2> ncode;         // the new ops' instructions, one copy per op
-  std::vector<double> xparams;      // expanded polygon records (device float64 layout)
-  std::vector<uint32_t> n32_code;   // their float32 parameter offsets
-  std::vector<float2> nbases;
-  std::vector<float2> n32_p;
-  nops.reserve(n_ops);
+namespace {
+
+// One contiguous range of a submitted op list, converted by one host thread:
+// offsets into its own arrays, rebased when the ranges are merged in order.
+struct SubmitChunk {
+  std::vector<OpDev> ops;
+  std::vector<uint2> boxes, code;
+  std::vector<double> xparams;     // expanded polygon records (device float64 layout)
+  std::vector<uint32_t> code32;    // float32 parameter offset per instruction
+  std::vector<float2> bases, p32;
+  std::vector<uint32_t> xfix;      // instructions whose parameter offset is a polygon record
+  int rc = PX_OK;
+  std::string err;
+};
+
+int chunk_fail(SubmitChunk& out, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  out.rc = code;
+  out.err = buf;
+  return code;
+}
+
+int convert_ops(const px_world* w, const IrOp* iops, size_t i0, size_t i1, const uint32_t* code, size_t n_code,
+                const double* P, size_t n_params, size_t param_base, SubmitChunk& out) {
   const double vs = w->vs;
-  for (size_t i = 0; i < n_ops; i++) {
+  out.ops.reserve(i1 - i0);
+  out.boxes.reserve(i1 - i0);
+  out.code.reserve(4 * (i1 - i0));
+  out.code32.reserve(4 * (i1 - i0));
+  out.p32.reserve(32 * (i1 - i0));
+  out.bases.reserve(16 * (i1 - i0));
+  for (size_t i = i0; i < i1; i++) {
     const IrOp& o = iops[i];
     std::string why;
-    if (o.kind > 2) return fail(w, PX_E_INVALID_IR, "op %zu: bad kind", i);
-    if (o.paint_kind >= PK_COUNT) return fail(w, PX_E_INVALID_IR, "op %zu: unknown paint kind", i);
-    if (o.paint_kind == PK_CONST && o.paint_value > 0xffffu) return fail(w, PX_E_INVALID_IR, "op %zu: paint is not a u16", i);
+    if (o.kind > 2) return chunk_fail(out, PX_E_INVALID_IR, "op %zu: bad kind", i);
+    if (o.paint_kind >= PK_COUNT) return chunk_fail(out, PX_E_INVALID_IR, "op %zu: unknown paint kind", i);
+    if (o.paint_kind == PK_CONST && o.paint_value > 0xffffu) return chunk_fail(out, PX_E_INVALID_IR, "op %zu: paint is not a u16", i);
     if (o.paint_kind != PK_CONST) {
       size_t np = (size_t)PAINT_NPARAMS[o.paint_kind];
-      if ((size_t)o.paint_param + np > n_params) return fail(w, PX_E_INVALID_IR, "op %zu: paint parameters out of range", i);
+      if ((size_t)o.paint_param + np > n_params) return chunk_fail(out, PX_E_INVALID_IR, "op %zu: paint parameters out of range", i);
       for (size_t k = 0; k < np; k++)
-        if (!std::isfinite(P[o.paint_param + k])) return fail(w, PX_E_INVALID_IR, "op %zu: non-finite paint parameter", i);
+        if (!std::isfinite(P[o.paint_param + k])) return chunk_fail(out, PX_E_INVALID_IR, "op %zu: non-finite paint parameter", i);
       if (o.paint_kind == PK_NOISE)  // its two results are voxel values (u16), like every other paint's
         for (int k = 6; k < 8; k++) {
           const double v = P[o.paint_param + k];
           if (!(v >= 0 && v <= 65535 && v == std::floor(v)))
-            return fail(w, PX_E_INVALID_IR, "op %zu: noise paint values must be integers in [0, 65535]", i);
+            return chunk_fail(out, PX_E_INVALID_IR, "op %zu: noise paint values must be integers in [0, 65535]", i);
         }
     }
     for (int k = 0; k < 3; k++)
-      if (!std::isfinite(o.mn[k]) || !std::isfinite(o.mx[k])) return fail(w, PX_E_INVALID_IR, "op %zu: non-finite bounds", i);
-    if (!std::isfinite(o.slack)) return fail(w, PX_E_INVALID_IR, "op %zu: non-finite slack", i);
+      if (!std::isfinite(o.mn[k]) || !std::isfinite(o.mx[k])) return chunk_fail(out, PX_E_INVALID_IR, "op %zu: non-finite bounds", i);
+    if (!std::isfinite(o.slack)) return chunk_fail(out, PX_E_INVALID_IR, "op %zu: non-finite slack", i);
     for (int k = 0; k < 4; k++)
-      if (!std::isfinite(o.frame[k])) return fail(w, PX_E_INVALID_IR, "op %zu: non-finite paint frame", i);
-    if (o.code_len == 0 || (size_t)o.code_begin + o.code_len > n_code) return fail(w, PX_E_INVALID_IR, "op %zu: code range", i);
-    if (!check_code(code + 2 * (size_t)o.code_begin, o.code_len, P.data(), n_params, why))
-      return fail(w, PX_E_INVALID_IR, "op %zu: %s", i, why.c_str());
+      if (!std::isfinite(o.frame[k])) return chunk_fail(out, PX_E_INVALID_IR, "op %zu: non-finite paint frame", i);
+    if (o.code_len == 0 || (size_t)o.code_begin + o.code_len > n_code) return chunk_fail(out, PX_E_INVALID_IR, "op %zu: code range", i);
+    if (!check_code(code + 2 * (size_t)o.code_begin, o.code_len, P, n_params, why))
+      return chunk_fail(out, PX_E_INVALID_IR, "op %zu: %s", i, why.c_str());
 
     OpDev d{};
     d.kind = o.kind;
     d.flags = o.flags & OPF_FROM_IR;
     d.paint_kind = o.paint_kind;
     d.paint_value = o.paint_value;
-    d.code_off = (uint32_t)(code_base + ncode.size());
+    d.code_off = (uint32_t)out.code.size();  // + the chunk's code base (merge)
     for (uint32_t k = 0; k < o.code_len; k++) {
       const uint32_t* ins = code + 2 * ((size_t)o.code_begin + k);
       const uint32_t opc = ins[0] & 0xffu, cnt = ins[0] >> 8;
       if (opc == OP_LATHE_SOLID || opc == OP_LATHE_SHELL || opc == OP_PRISM) {
         // device polygon records with the per-edge constants (same float64 values
         // as every reference call computes), appended after the IR's parameters
-        const double* pp = P.data() + ins[1];
-        const uint32_t off = (uint32_t)(param_base + n_params + xparams.size());
+        const double* pp = P + ins[1];
+        const uint32_t off = (uint32_t)out.xparams.size();  // + the chunk's record base (merge)
+        out.xfix.push_back((uint32_t)out.code.size());
         const int head = opc == OP_LATHE_SOLID ? 3 : 4;
-        for (int h = 0; h < head; h++) xparams.push_back(pp[h]);
+        for (int h = 0; h < head; h++) out.xparams.push_back(pp[h]);
         const double* v = pp + head;
         auto den_of = [](double ex, double ey) { double dd = ex * ex + ey * ey; return dd == 0.0 ? 1e-12 : dd; };
         if (opc == OP_LATHE_SHELL) {
           for (uint32_t q = 0; q + 1 < cnt; q++) {
             double ax = v[2 * q], ay = v[2 * q + 1], ex = v[2 * q + 2] - ax, ey = v[2 * q + 3] - ay;
-            xparams.insert(xparams.end(), {ax, ay, ex, ey, den_of(ex, ey)});
+            out.xparams.insert(out.xparams.end(), {ax, ay, ex, ey, den_of(ex, ey)});
           }
         } else {
           for (uint32_t q = 0; q < cnt; q++) {
             uint32_t j = q ? q - 1 : cnt - 1;
             double vix = v[2 * q], viy = v[2 * q + 1], vjx = v[2 * j], vjy = v[2 * j + 1];
             double ex = vjx - vix, ey = vjy - viy;
-            xparams.insert(xparams.end(), {vix, viy, vjy, ex, ey, den_of(ex, ey)});
+            out.xparams.insert(out.xparams.end(), {vix, viy, vjy, ex, ey, den_of(ex, ey)});
           }
         }
-        ncode.push_back(make_uint2(ins[0], off));
+        out.code.push_back(make_uint2(ins[0], off));
       } else {
-        ncode.push_back(make_uint2(ins[0], ins[1] + (uint32_t)param_base));
+        out.code.push_back(make_uint2(ins[0], ins[1] + (uint32_t)param_base));
       }
     }
     d.code_len = o.code_len;
@@ -579,7 +615,7 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
     d.vr[0] = d.vr[2] = d.vr[4] = 1;
     d.vr[1] = d.vr[3] = d.vr[5] = 0;
     if (o.code_len == 1 && (code[2 * (size_t)o.code_begin] & 0xffu) == OP_BOX && d.bx0 <= d.bx1) {
-      const double* bp = P.data() + code[2 * (size_t)o.code_begin + 1];
+      const double* bp = P + code[2 * (size_t)o.code_begin + 1];
       const int b0[3] = {d.bx0, d.by0, d.bz0}, b1[3] = {d.bx1, d.by1, d.bz1};
       bool runs = true;
       for (int k = 0; k < 3; k++) {
@@ -614,14 +650,14 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
       d.thr[T_M] = ru32(M);
       // (b*8 + 0.5)*vs - anchor per brick row, padded for the float64 rounding of the
       // reference's voxel centres ((x + 0.5)*vs, |x*vs| <= 2^10 m)
-      d.base_off = (uint32_t)(w->bases.size() + nbases.size());
+      d.base_off = (uint32_t)out.bases.size();  // + the chunk's base offset (merge)
       if (d.bx0 <= d.bx1) {
         const int b0[3] = {d.bx0, d.by0, d.bz0}, b1[3] = {d.bx1, d.by1, d.bz1};
         for (int k = 0; k < 3; k++)
-          for (int b = b0[k]; b <= b1[k]; b++) nbases.push_back(enc((b * 8 + 0.5) * vs - d.anchor[k], 0x1p-38));
+          for (int b = b0[k]; b <= b1[k]; b++) out.bases.push_back(enc((b * 8 + 0.5) * vs - d.anchor[k], 0x1p-38));
       }
-      size_t c32_before = n32_code.size(), p32_before = n32_p.size();
-      bool ok32 = convert32(code + 2 * (size_t)o.code_begin, o.code_len, P.data(), d.anchor, n32_code, n32_p);
+      size_t c32_before = out.code32.size(), p32_before = out.p32.size();
+      bool ok32 = convert32(code + 2 * (size_t)o.code_begin, o.code_len, P, d.anchor, out.code32, out.p32);
       double ext = (double)w->dx * vs;
       if ((double)w->dy * vs > ext) ext = (double)w->dy * vs;
       if ((double)w->dz * vs > ext) ext = (double)w->dz * vs;
@@ -629,27 +665,160 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
       d.paint_slot = NO_SLOT;
       d.paint32_off = NO_SLOT;
       if (!(d.flags & OPF_FP64_ONLY) && o.kind != KIND_CARVE && paint_is_heavy(o.paint_kind)) {
-        const size_t at = n32_p.size();
-        if (paint_params32(o.paint_kind, (o.flags & OPF_PAINT_FRAME) != 0, P.data() + o.paint_param, d.anchor, n32_p))
-          d.paint32_off = (uint32_t)(w->p32.size() + at);
+        const size_t at = out.p32.size();
+        if (paint_params32(o.paint_kind, (o.flags & OPF_PAINT_FRAME) != 0, P + o.paint_param, d.anchor, out.p32))
+          d.paint32_off = (uint32_t)at;  // + the chunk's float32 base (merge)
         else
-          n32_p.resize(at);
+          out.p32.resize(at);
       }
-      // code32 entries are relative to this op's code; rebase onto the world's arrays
-      for (size_t k = c32_before; k < n32_code.size(); k++) n32_code[k] += (uint32_t)(w->p32.size());
+      (void)c32_before;
       (void)p32_before;
     }
-    nops.push_back(d);
-    nboxes.push_back(box);
+    out.ops.push_back(d);
+    out.boxes.push_back(box);
   }
-  w->code.insert(w->code.end(), ncode.begin(), ncode.end());
-  w->code32.insert(w->code32.end(), n32_code.begin(), n32_code.end());
-  w->p32.insert(w->p32.end(), n32_p.begin(), n32_p.end());
-  w->bases.insert(w->bases.end(), nbases.begin(), nbases.end());
-  w->params.insert(w->params.end(), P.begin(), P.end());
-  w->params.insert(w->params.end(), xparams.begin(), xparams.end());
-  w->ops.insert(w->ops.end(), nops.begin(), nops.end());
-  w->boxes.insert(w->boxes.end(), nboxes.begin(), nboxes.end());
+  return PX_OK;
+}
+
+// A small pool of host threads for op conversion (started on first use).
+class HostPool {
+ public:
+  static HostPool& get() {
+    static HostPool* p = new HostPool();  // never destroyed: its threads live as long as the process
+    return *p;
+  }
+  int size() const { return (int)workers_.size() + 1; }
+  // run f(k) for k in [0, n) on the pool and the calling thread
+  void run(int n, const std::function<void(int)>& f) {
+    if (n <= 1 || workers_.empty()) {
+      for (int k = 0; k < n; k++) f(k);
+      return;
+    }
+    std::lock_guard<std::mutex> one_job(run_mu_);  // callers on other threads wait their turn
+    std::unique_lock<std::mutex> g(mu_);
+    job_ = &f;
+    n_ = n;
+    next_.store(0);
+    done_ = 0;
+    gen_++;
+    cv_.notify_all();
+    g.unlock();
+    work();
+    g.lock();
+    done_cv_.wait(g, [&] { return done_ == (int)workers_.size(); });
+    job_ = nullptr;
+  }
+
+ private:
+  HostPool() {
+    unsigned hc = std::thread::hardware_concurrency();
+    int n = (int)std::min<unsigned>(hc > 1 ? hc - 1 : 0, 15);
+    for (int i = 0; i < n; i++) workers_.emplace_back([this] { loop(); });
+    for (auto& t : workers_) t.detach();
+  }
+  void work() {
+    for (;;) {
+      const int k = next_.fetch_add(1);
+      if (k >= n_) break;
+      (*job_)(k);
+    }
+  }
+  void loop() {
+    uint64_t seen = 0;
+    for (;;) {
+      std::unique_lock<std::mutex> g(mu_);
+      cv_.wait(g, [&] { return gen_ != seen; });
+      seen = gen_;
+      g.unlock();
+      work();
+      g.lock();
+      done_++;
+      done_cv_.notify_one();
+    }
+  }
+  std::vector<std::thread> workers_;
+  std::mutex run_mu_, mu_;
+  std::condition_variable cv_, done_cv_;
+  const std::function<void(int)>* job_ = nullptr;
+  int n_ = 0, done_ = 0;
+  std::atomic<int> next_{0};
+  uint64_t gen_ = 0;
+};
+
+}  // namespace
+
+extern "C" {
+
+int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
+  if (!w || (!ir && bytes)) return PX_E_INVALID_ARG;
+  if (w->batch_locked) return fail(w, PX_E_INVALID_ARG, "the world belongs to a batch");
+  if (w->in_flight) return fail(w, PX_E_INVALID_ARG, "a build is in flight");
+  w->ops_resident = false;
+  if (bytes < 32) return fail(w, PX_E_INVALID_IR, "IR shorter than its header");
+  const uint32_t* h = (const uint32_t*)ir;
+  if (h[0] != 0x52495850u || h[1] != 1u) return fail(w, PX_E_INVALID_IR, "not a PXIR v1 buffer");
+  const size_t n_ops = h[2], n_code = h[3], n_params = h[4];
+  const size_t need = 32 + n_ops * sizeof(IrOp) + n_code * 8 + n_params * 8;
+  if (bytes < need) return fail(w, PX_E_INVALID_IR, "IR truncated (%zu < %zu bytes)", bytes, need);
+  const IrOp* iops = (const IrOp*)((const char*)ir + 32);
+  const uint32_t* code = (const uint32_t*)((const char*)ir + 32 + n_ops * sizeof(IrOp));
+  // the parameters, read in place when the buffer is aligned (copied otherwise)
+  const char* praw = (const char*)ir + 32 + n_ops * sizeof(IrOp) + n_code * 8;
+  std::vector<double> Pcopy;
+  const double* Pp = (const double*)praw;
+  if ((uintptr_t)praw % alignof(double)) {
+    Pcopy.resize(n_params);
+    std::memcpy(Pcopy.data(), praw, n_params * 8);
+    Pp = Pcopy.data();
+  }
+
+  const size_t param_base = w->params.size();
+  // convert the ops in contiguous ranges on the host pool, then append the
+  // ranges in order (offsets rebased)
+  HostPool& pool = HostPool::get();
+  const int n_chunks = n_ops < 512 ? 1 : (int)std::min<size_t>((size_t)pool.size() * 2, n_ops / 128);
+  std::vector<SubmitChunk> chunks(n_chunks);
+  pool.run(n_chunks, [&](int k) {
+    const size_t i0 = n_ops * k / n_chunks, i1 = n_ops * (k + 1) / n_chunks;
+    convert_ops(w, iops, i0, i1, code, n_code, Pp, n_params, param_base, chunks[k]);
+  });
+  for (auto& c : chunks)
+    if (c.rc != PX_OK) return fail(w, c.rc, "%s", c.err.c_str());
+  size_t n_code_new = 0, n_p32_new = 0, n_bases_new = 0, n_xp = 0;
+  for (const auto& c : chunks) {
+    n_code_new += c.code.size();
+    n_p32_new += c.p32.size();
+    n_bases_new += c.bases.size();
+    n_xp += c.xparams.size();
+  }
+  w->code.reserve(w->code.size() + n_code_new);
+  w->code32.reserve(w->code32.size() + n_code_new);
+  w->p32.reserve(w->p32.size() + n_p32_new);
+  w->bases.reserve(w->bases.size() + n_bases_new);
+  w->ops.reserve(w->ops.size() + n_ops);
+  w->boxes.reserve(w->boxes.size() + n_ops);
+  w->params.reserve(param_base + n_params + n_xp);
+  w->params.insert(w->params.end(), Pp, Pp + n_params);
+  size_t xbase = param_base + n_params;
+  for (auto& c : chunks) {  // in order: rebase each range's offsets, append it
+    const uint32_t code_at = (uint32_t)w->code.size(), p32_at = (uint32_t)w->p32.size(),
+                   bases_at = (uint32_t)w->bases.size();
+    for (uint32_t i : c.xfix) c.code[i].y += (uint32_t)xbase;
+    for (uint32_t& v : c.code32) v += p32_at;
+    for (OpDev& d : c.ops) {
+      d.code_off += code_at;
+      d.base_off += bases_at;
+      if (d.paint32_off != NO_SLOT) d.paint32_off += p32_at;
+    }
+    w->code.insert(w->code.end(), c.code.begin(), c.code.end());
+    w->code32.insert(w->code32.end(), c.code32.begin(), c.code32.end());
+    w->p32.insert(w->p32.end(), c.p32.begin(), c.p32.end());
+    w->bases.insert(w->bases.end(), c.bases.begin(), c.bases.end());
+    w->ops.insert(w->ops.end(), c.ops.begin(), c.ops.end());
+    w->boxes.insert(w->boxes.end(), c.boxes.begin(), c.boxes.end());
+    xbase += c.xparams.size();
+  }
+  for (const auto& c : chunks) w->params.insert(w->params.end(), c.xparams.begin(), c.xparams.end());
   return PX_OK;
 }
 
