@@ -32,6 +32,9 @@ namespace px {
 #ifndef PX_CLASSIFY_MINB
 #define PX_CLASSIFY_MINB 3
 #endif
+#ifndef PX_VOXEL_MINB
+#define PX_VOXEL_MINB 3
+#endif
 #ifndef PX_CLASSIFY64_MINB
 #define PX_CLASSIFY64_MINB 2
 #endif
@@ -440,7 +443,7 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
 // Voxel inside-masks of the queued partial sub-blocks: one sub-block per warp
 // pass, 64 voxel SDFs on 32 lanes, two ballots (shapes.ts:390-394).
 template <int MODE>
-__global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIFY64_MINB) voxel_kernel(FoldArgs a) {
+__global__ void __launch_bounds__(256, MODE == 1 ? PX_VOXEL_MINB : PX_CLASSIFY64_MINB) voxel_kernel(FoldArgs a) {
   const int lane = threadIdx.x & 31;
   LaneStats ls = {0, 0, 0, 0.f, 0, 0, 0, 0};
   // the classes' item counts, as an inclusive prefix over lanes 0..VCLASSES-1
@@ -868,7 +871,7 @@ void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEve
   if (mode == 1) {
     ++g_launches; classify_kernel<1><<<grid(PX_CLASSIFY_MINB), 256, 0, s>>>(a);
     ++g_launches; sub_kernel<1><<<grid(PX_CLASSIFY_MINB), 256, 0, s>>>(a);
-    ++g_launches; voxel_kernel<1><<<grid(PX_CLASSIFY_MINB), 256, 0, s>>>(a);
+    ++g_launches; voxel_kernel<1><<<grid(PX_VOXEL_MINB), 256, 0, s>>>(a);
   } else {
     ++g_launches; classify_kernel<0><<<grid(PX_CLASSIFY64_MINB), 256, 0, s>>>(a);
     ++g_launches; sub_kernel<0><<<grid(PX_CLASSIFY64_MINB), 256, 0, s>>>(a);

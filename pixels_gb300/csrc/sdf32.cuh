@@ -14,6 +14,10 @@
 #pragma once
 #include "px_internal.cuh"
 
+#ifndef PX_SDF32I_INLINE
+#define PX_SDF32I_INLINE __forceinline__
+#endif
+
 namespace px {
 
 struct Iv {
@@ -149,7 +153,7 @@ __device__ __forceinline__ Iv prim32(uint32_t op, int cnt, const Iv* __restrict_
 }
 
 // code32[i] is the offset of instruction i's float32 parameters.
-__device__ __noinline__ Iv sdf32i(const uint2* __restrict__ code, const uint32_t* __restrict__ code32, int n,
+__device__ PX_SDF32I_INLINE Iv sdf32i(const uint2* __restrict__ code, const uint32_t* __restrict__ code32, int n,
                                   const Iv* __restrict__ P, Iv x, Iv y, Iv z, float M, bool& amb) {
   Iv s0 = {0.f, 0.f}, s1 = s0, s2 = s0, s3 = s0;
   Iv ax0 = s0, ay0 = s0, az0 = s0, ax1 = s0, ay1 = s0, az1 = s0, ax2 = s0, ay2 = s0, az2 = s0;
