@@ -302,6 +302,19 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
         atomicOr(a.bmark + (ci >> 5), 1u << (ci & 31));
       }
     }
+    // a full pair of a painted op: its 8 sub-blocks go to the paint pass
+    const bool fullp = valid && cls == PC_FULL && O->paint_slot != NO_SLOT;
+    const uint32_t fm = __ballot_sync(FULLMASK, fullp);
+    if (fm) {
+      uint32_t pb = 0;
+      if (lane == 0) pb = atomicAdd(a.paint_item_counter, 8u * __popc(fm));
+      pb = __shfl_sync(FULLMASK, pb, 0);
+      if (fullp) {
+        const uint32_t at = pb + 8u * __popc(fm & ((1u << lane) - 1u));
+        for (uint32_t q = 0; q < 8; q++)
+          if (at + q < a.paint_items_cap) a.paint_items[at + q] = make_uint2(o, (uint32_t)(p << 3) | q);
+      }
+    }
     // partial pairs go to the sub-block pass, one queue region per shape class
     const bool part = valid && cls == PC_PARTIAL;
     const uint32_t pm = __ballot_sync(FULLMASK, part);
@@ -405,6 +418,15 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
     if (boxr && scls == PC_PARTIAL)
       a.pmask[pp * 8 + s] = box_mask(a.ops + oo, pbx * 8 + (s & 1) * 4, pby * 8 + ((s >> 1) & 1) * 4,
                                      pbz * 8 + ((s >> 2) & 1) * 4);
+    const bool paint = have && scls != PC_SKIP && a.ops[oo].paint_slot != NO_SLOT;
+    const uint32_t qm = __ballot_sync(FULLMASK, paint);
+    if (qm) {  // the covered sub-blocks of a painted op go to the paint pass
+      uint32_t pb = 0;
+      if (lane == 0) pb = atomicAdd(a.paint_item_counter, (uint32_t)__popc(qm));
+      pb = __shfl_sync(FULLMASK, pb, 0);
+      const uint32_t at = pb + __popc(qm & ((1u << lane) - 1u));
+      if (paint && at < a.paint_items_cap) a.paint_items[at] = make_uint2(oo, (uint32_t)(pp << 3) | (uint32_t)s);
+    }
     const bool push = have && scls == PC_PARTIAL && !boxr;
     const uint32_t vm = __ballot_sync(FULLMASK, push);
     if (push) {  // one append per shape class present among the pushing lanes
@@ -528,33 +550,29 @@ __device__ __noinline__ uint32_t paint_at_voxel(const double* __restrict__ param
   return (v & 0xffffu) | (st & ST_RANGE ? PV_RANGE : 0u) | (viol ? PV_VIOL : 0u);
 }
 
-// Paint calls of the heavy paint kinds, ahead of the apply pass: one 4^3
-// sub-block of one (op, brick) pair per warp pass, two voxels per lane, every
-// voxel the op's shape covers (whether the reference then paints it depends on
-// the world's state, which fold_kernel knows).  Values go to the pair's slot in
+// Paint calls ahead of the apply pass: the covered sub-blocks of the painted
+// ops' pairs (queued by the classify and sub-block passes), one 4^3 sub-block
+// per warp pass, two voxels per lane, every voxel the op's shape covers (whether
+// the reference then paints it depends on the world's state, which fold_kernel
+// knows).  Values go to the pair's slot in
 // voxel index order.  Spreading these calls over the whole GPU keeps one
 // warp from evaluating a painted brick's 512 calls alone.  Mixed mode tries the
 // certified float32 evaluation first (paint32.cuh).
 template <int MODE>
 __global__ void __launch_bounds__(256) paint_kernel(FoldArgs a) {
   const int lane = threadIdx.x & 31;
-  const uint32_t n_items = a.n_paint_slots * 8u;
+  const uint32_t n_items = min(__ldg(a.paint_item_counter), a.paint_items_cap);
   uint32_t resc = 0, viol = 0;
   WorkBatch wb;
   for (;;) {
     const uint32_t it = wb.next(a.paint_counter, 2, lane);
     if (it >= n_items) break;
-    const uint32_t slot = it >> 3;
-    const int s = (int)(it & 7u);
-    int lo = 0, hi = (int)a.n_heavy - 1;  // last heavy op whose first slot <= slot
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (__ldg(a.heavy_slot + mid) <= slot) lo = mid; else hi = mid - 1;
-    }
-    const OpDev* O = a.ops + __ldg(a.heavy_op + lo);
-    const unsigned long long pair = O->pair_base + (slot - O->paint_slot);
+    const uint2 item = __ldg(a.paint_items + it);
+    const OpDev* O = a.ops + item.x;
+    const unsigned long long pair = item.y >> 3;
+    const int s = (int)(item.y & 7u);
+    const uint32_t slot = O->paint_slot + (uint32_t)(pair - O->pair_base);
     const int cls = __ldg(a.pcode + pair);
-    if (cls == PC_SKIP) continue;
     unsigned long long m = ~0ull;
     if (cls != PC_FULL) {
       const uint32_t c = (__ldg(a.psub + pair) >> (2 * s)) & 3u;

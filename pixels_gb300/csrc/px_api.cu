@@ -68,9 +68,8 @@ struct px_world {
   uint64_t stage_hint = 0;      // staging slots the next build reserves (grown on overflow)
   DevBuf chunk_op, pcode, psub, pmask, chunk_counter, vitems, pitems;
   std::vector<uint32_t> h_chunk_op;
-  DevBuf heavy, pvals;          // heavy-paint ops (op index, first slot) and their paint values
+  DevBuf paint_items, pvals;    // sub-blocks to paint and the paint values
   DevBuf bmark, work;           // bricks the apply pass visits (bitmap, list)
-  std::vector<uint32_t> h_heavy;
   DevBuf scan_agg;
   DevBuf work_counter;
   DevBuf res;
@@ -402,7 +401,7 @@ void px_world_destroy(px_world* w) {
                     &w->ew, &w->depth_fn, &w->depth, &w->tree, &w->fresh, &w->fresh_rank, &w->staging, &w->touched,
                     &w->stage_cell, &w->stage_src, &w->chunk_op, &w->pcode, &w->psub, &w->pmask,
                     &w->chunk_counter, &w->vitems, &w->scan_agg, &w->work_counter, &w->res, &w->opaque,
-                    &w->udens, &w->super_counts, &w->density, &w->heavy, &w->pvals, &w->bmark, &w->work, &w->pitems};
+                    &w->udens, &w->super_counts, &w->density, &w->paint_items, &w->pvals, &w->bmark, &w->work, &w->pitems};
   for (DevBuf* b : bufs) release(*b);
   if (w->h_res) cudaFreeHost(w->h_res);
   if (w->ev0) cudaEventDestroy(w->ev0);
@@ -853,7 +852,6 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   for (int tier = 0; tier < 3; tier++) {
     n_slots = 0;
     inline_paints = false;
-    w->h_heavy.clear();
     // float64-only paints first: paint_kernel takes items in slot order, so the
     // slowest calls start earliest
     for (int pass = 0; pass < 2; pass++)
@@ -865,17 +863,9 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
         if (tier == 2 || (tier == 1 && !paint_is_heavy(o.paint_kind))) { inline_paints = true; continue; }
         const uint64_t np = (uint64_t)o.nx * o.ny * (uint64_t)(o.bz1 - o.bz0 + 1);
         o.paint_slot = (uint32_t)n_slots;
-        w->h_heavy.push_back((uint32_t)i);
-        w->h_heavy.push_back((uint32_t)n_slots);
         n_slots += np;
       }
     if (n_slots * 2048 <= (512ull << 20)) break;
-  }
-  const uint32_t n_heavy = (uint32_t)(w->h_heavy.size() / 2);
-  {  // (op indices, then first slots) as two arrays
-    std::vector<uint32_t> t(w->h_heavy.size());
-    for (uint32_t k = 0; k < n_heavy; k++) { t[k] = w->h_heavy[2 * k]; t[n_heavy + k] = w->h_heavy[2 * k + 1]; }
-    w->h_heavy.swap(t);
   }
   const uint64_t touched_bound = P < w->ncells ? P : w->ncells;
   const uint32_t H = w->n_holes, U0 = w->pool_used;
@@ -889,7 +879,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
 
   // scratch (a reallocated op table loses its resident copy)
   const void* op_bufs_before[9] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p,
-                                   w->d_p32.p, w->d_bases.p, w->chunk_op.p, w->heavy.p};
+                                   w->d_p32.p, w->d_bases.p, w->chunk_op.p, w->chunk_op.p};
   if ((rc = ensure(w, w->d_ops, sizeof(OpDev) * (size_t)n_ops)) ||
       (rc = ensure(w, w->d_boxes, sizeof(uint2) * ((size_t)n_ops + (n_ops + 31) / 32))) ||
       (rc = ensure(w, w->d_code, sizeof(uint2) * w->code.size())) ||
@@ -909,7 +899,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
       (rc = ensure(w, w->work_counter, 16)) || (rc = ensure(w, w->res, sizeof(BuildResult))) ||
       (rc = ensure(w, w->chunk_op, 4 * ((P + 31) / 32))) || (rc = ensure(w, w->pcode, P)) ||
       (rc = ensure(w, w->psub, 2 * P)) || (rc = ensure(w, w->pmask, 64 * P)) || (rc = ensure(w, w->chunk_counter, 256)) || (rc = ensure(w, w->pitems, 8 * P)) ||
-      (rc = ensure(w, w->vitems, 8 * 8 * P)) || (rc = ensure(w, w->heavy, 4 * w->h_heavy.size() + 4)) ||
+      (rc = ensure(w, w->vitems, 8 * 8 * P)) || (rc = ensure(w, w->paint_items, 8 * 8 * n_slots + 8)) ||
       (rc = ensure(w, w->pvals, 2048 * n_slots + 4)) || (rc = ensure(w, w->bmark, 4 * ((w->ncells + 31) / 32))) ||
       (rc = ensure(w, w->work, 4 * touched_bound + 4)))
     return rc;
@@ -921,7 +911,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   }
   {
     const void* after[9] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p,
-                            w->d_p32.p, w->d_bases.p, w->chunk_op.p, w->heavy.p};
+                            w->d_p32.p, w->d_bases.p, w->chunk_op.p, w->chunk_op.p};
     for (int k = 0; k < 9; k++)
       if (after[k] != op_bufs_before[k]) w->ops_resident = false;
   }
@@ -980,8 +970,6 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   }
   if (P) CU(cudaMemsetAsync(w->evt.p, 0, P, s));
   CU(cudaMemsetAsync(w->bmark.p, 0, 4 * ((w->ncells + 31) / 32), s));
-  if (n_heavy && upload)
-    CU(cudaMemcpyAsync(w->heavy.p, w->h_heavy.data(), 4 * w->h_heavy.size(), cudaMemcpyHostToDevice, s));
 
   BuildResult* res = (BuildResult*)w->res.p;
   ScanTemp st{w->scan_agg.p, w->scan_agg.bytes / 8};
@@ -1021,9 +1009,9 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   fa.pitem_counter = (uint32_t*)w->chunk_counter.p + 20;
   fa.paint_counter = (uint32_t*)w->chunk_counter.p + 1;
   fa.n_paint_slots = (uint32_t)n_slots;
-  fa.n_heavy = n_heavy;
-  fa.heavy_op = (const uint32_t*)w->heavy.p;
-  fa.heavy_slot = (const uint32_t*)w->heavy.p + n_heavy;
+  fa.paint_items = (uint2*)w->paint_items.p;
+  fa.paint_items_cap = (uint32_t)std::min<uint64_t>(8 * n_slots, 0xffffffffull);
+  fa.paint_item_counter = (uint32_t*)w->chunk_counter.p + 38;
   fa.pvals = (uint32_t*)w->pvals.p;
   fa.inline_paints = inline_paints ? 1 : 0;
   fa.bmark = (uint32_t*)w->bmark.p;

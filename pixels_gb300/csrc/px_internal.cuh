@@ -147,10 +147,10 @@ struct FoldArgs {
   uint32_t* pitem_counter;    // [0] items taken, [1 + k] items pushed to class k
   uint32_t pq_base[VCLASSES], pq_cap[VCLASSES];  // per-class regions of pitems
   uint32_t* paint_counter;    // paint_kernel items taken
-  uint32_t n_paint_slots;     // (op, brick) pairs of heavy-paint ops
-  uint32_t n_heavy;           // heavy-paint ops, ascending slots
-  const uint32_t* heavy_op;   // their op indices
-  const uint32_t* heavy_slot; // their first slots
+  uint32_t n_paint_slots;     // (op, brick) pairs of painted ops with a slot
+  uint2* paint_items;         // sub-blocks to paint: (op, pair << 3 | sub-block), from classify and sub
+  uint32_t paint_items_cap;
+  uint32_t* paint_item_counter;  // items pushed
   uint32_t* pvals;            // 512 paint values per slot (voxel index order); PV_RANGE flags
   int inline_paints;          // some painted op has no slot: fold_kernel calls its paints itself
   uint32_t* bmark;            // one bit per brick: some pair of it is not skipped (classify_kernel)
