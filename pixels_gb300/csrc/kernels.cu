@@ -236,6 +236,31 @@ __device__ __forceinline__ unsigned long long box_mask(const OpDev* O, int sx, i
   return (unsigned long long)(xb * ys) * zs;
 }
 
+// The float64 side of a mixed-mode voxel decision taken from the interval d
+// (r: 0 outside, 1 inside, 3 undecided; amb: a polygon crossing test was
+// undecided): the rescue, or in validation mode the enclosure check.
+// Returns the decision, whether the enclosure failed, and |mid(d) - d64|
+// (-1 when not a rescue, or for an undecided crossing test).
+struct VoxelF64 {
+  int inside, viol;
+  float err;
+};
+__device__ __noinline__ VoxelF64 voxel_f64(const double* __restrict__ params, double vs, int validate,
+                                           const uint2* code, int clen, Iv d, bool amb, int r, float tx, float ty,
+                                           float tz) {
+  const double d64 = sdf64_at(code, clen, params, vs, tx, ty, tz);
+  const double M = MIXED_MARGIN;
+  VoxelF64 out;
+  out.inside = d64 > 0.0 ? 0 : 1;
+  out.viol = validate && !amb && !((double)d.lo - M <= d64 && d64 <= (double)d.hi + M);
+  out.err = -1.f;
+  if (r == 3 && !amb) {
+    const double e = fabs(0.5 * ((double)d.lo + (double)d.hi) - d64);
+    out.err = e == e ? (float)e : 0.f;
+  }
+  return out;
+}
+
 __device__ __forceinline__ void brick_of_pair(const OpDev* O, unsigned long long p, int& bx, int& by, int& bz) {
   const uint32_t local = (uint32_t)(p - O->pair_base);
   const uint32_t nxy = (uint32_t)(O->nx * O->ny);
@@ -495,17 +520,54 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_VOXEL_MINB : PX_CLASSIFY64
     const int sxo = (ss & 1) * 4, syo = ((ss >> 1) & 1) * 4, szo = ((ss >> 2) & 1) * 4;
     const uint2* code = a.code + V->code_off;
     const int clen = (int)V->code_len;
-    uint32_t bal[2];
+    unsigned long long m;
+    if (MODE == 1 && use32 && (V->flags & OPF_Y_SEPARABLE)) {
+      // lane = column (x, z) of the sub-block and a pair of y rows: one pass, the x/z work once
+      const int col = lane & 15, yh = lane >> 4;
+      const int lx = sxo + (col & 3), lz = szo + (col >> 2), ly0 = syo + 2 * yh;
+      bool amb = false;
+      const Iv X = iadd(bo[0], koff((float)lx, a.vs_lo, a.vs_hi)), Z = iadd(bo[2], koff((float)lz, a.vs_lo, a.vs_hi));
+      const Iv Y0 = iadd(bo[1], koff((float)ly0, a.vs_lo, a.vs_hi)), Y1 = iadd(bo[1], koff((float)(ly0 + 1), a.vs_lo, a.vs_hi));
+      const Iv2 d = sdf32i_y2(code, a.code32 + V->code_off, clen, reinterpret_cast<const Iv*>(a.p32), X, Y0, Y1, Z,
+                              V->thr[T_M], amb);
+      uint32_t lo = 0, hi = 0;
 #pragma unroll
-    for (int r = 0; r < 2; r++) {
-      const int e = r * 32 + lane;
-      const int lx = sxo + (e & 3), lyv = syo + ((e >> 2) & 3), lz = szo + (e >> 4);
-      int inside = eval_decide<MODE>(a, V, code, clen, use32, bo, (float)lx, (float)lyv, (float)lz,
-                                     (float)(vbx * 8 + lx) + 0.5f, (float)(vby * 8 + lyv) + 0.5f,
-                                     (float)(vbz * 8 + lz) + 0.5f, 0, ls);
-      bal[r] = __ballot_sync(FULLMASK, inside == 1);
+      for (int k = 0; k < 2; k++) {
+        const Iv dk = k ? d.b : d.a;
+        int inside = amb ? 3 : (dk.lo > V->thr[T_V_HI] ? 0 : (dk.hi <= V->thr[T_V_LO] ? 1 : 3));
+        if (inside == 3 || a.validate) {
+          const VoxelF64 f = voxel_f64(a.params, a.vs, a.validate, code, clen, dk, amb, inside,
+                                       (float)(vbx * 8 + lx) + 0.5f, (float)(vby * 8 + ly0 + k) + 0.5f,
+                                       (float)(vbz * 8 + lz) + 0.5f);
+          ls.viol += f.viol;
+          if (inside == 3) {
+            ls.resc++;
+            ls.rv++;
+            if (amb) ls.rp++;
+            ls.max_err = fmaxf(ls.max_err, f.err);
+          }
+          inside = f.inside;
+        }
+        const int bit = (col & 3) | ((2 * yh + k) << 2) | ((col >> 2) << 4);  // voxel index in the sub-block
+        if (inside == 1) {
+          if (bit < 32) lo |= 1u << bit;
+          else hi |= 1u << (bit - 32);
+        }
+      }
+      m = (unsigned long long)__reduce_or_sync(FULLMASK, lo) | ((unsigned long long)__reduce_or_sync(FULLMASK, hi) << 32);
+    } else {
+      uint32_t bal[2];
+#pragma unroll
+      for (int r = 0; r < 2; r++) {
+        const int e = r * 32 + lane;
+        const int lx = sxo + (e & 3), lyv = syo + ((e >> 2) & 3), lz = szo + (e >> 4);
+        int inside = eval_decide<MODE>(a, V, code, clen, use32, bo, (float)lx, (float)lyv, (float)lz,
+                                       (float)(vbx * 8 + lx) + 0.5f, (float)(vby * 8 + lyv) + 0.5f,
+                                       (float)(vbz * 8 + lz) + 0.5f, 0, ls);
+        bal[r] = __ballot_sync(FULLMASK, inside == 1);
+      }
+      m = (unsigned long long)bal[0] | ((unsigned long long)bal[1] << 32);
     }
-    const unsigned long long m = (unsigned long long)bal[0] | ((unsigned long long)bal[1] << 32);
     // a lone box's sub-block is queued only in validation mode: check its runs
     if ((V->flags & OPF_BOX_RANGES) && lane == 0 && box_mask(V, vbx * 8 + sxo, vby * 8 + syo, vbz * 8 + szo) != m)
       ls.viol++;

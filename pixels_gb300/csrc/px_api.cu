@@ -19,6 +19,7 @@
 
 #include "../../include/pixels_gb300.h"
 #include "px_internal.cuh"
+#include "sdf32.cuh"
 
 using namespace px;
 
@@ -661,6 +662,12 @@ int convert_ops(const px_world* w, const IrOp* iops, size_t i0, size_t i1, const
       if ((double)w->dy * vs > ext) ext = (double)w->dy * vs;
       if ((double)w->dz * vs > ext) ext = (double)w->dz * vs;
       if (!ok32 || ext > MIXED_MAX_COORD) d.flags |= OPF_FP64_ONLY;
+      {  // shapes extruded along y: two voxels of a column share the x/z work (sdf32i_y2)
+        bool ysep = true;
+        for (uint32_t k = 0; k < o.code_len; k++)
+          ysep = ysep && op_is_y_separable(code[2 * ((size_t)o.code_begin + k)] & 0xffu);
+        if (ysep) d.flags |= OPF_Y_SEPARABLE;
+      }
       d.paint_slot = NO_SLOT;
       d.paint32_off = NO_SLOT;
       if (!(d.flags & OPF_FP64_ONLY) && o.kind != KIND_CARVE && paint_is_heavy(o.paint_kind)) {

@@ -33,7 +33,8 @@ enum : uint16_t {
 };
 constexpr int PAINT_NPARAMS[PK_COUNT] = {0, 5, 3, 4, 2, 2, 5, 37, 8};
 
-enum : uint8_t { OPF_CONTAINS = 1, OPF_HAS_SLACK = 2, OPF_PAINT_FRAME = 4, OPF_BOX_RANGES = 0x40, OPF_FP64_ONLY = 0x80 };
+enum : uint8_t { OPF_CONTAINS = 1, OPF_HAS_SLACK = 2, OPF_PAINT_FRAME = 4, OPF_Y_SEPARABLE = 0x20, OPF_BOX_RANGES = 0x40,
+                 OPF_FP64_ONLY = 0x80 };
 constexpr uint8_t OPF_FROM_IR = OPF_CONTAINS | OPF_HAS_SLACK | OPF_PAINT_FRAME;  // flags an op list may set
 
 // Mixed mode: margin between the exact value of an expression on the float64

@@ -198,4 +198,130 @@ __device__ PX_SDF32I_INLINE Iv sdf32i(const uint2* __restrict__ code, const uint
   return s0;
 }
 
+
+// Shapes whose code uses only primitives extruded along y (box, rounded box,
+// cylinder and torus about y, stadium, prism), rotations about y and the
+// combinators: the x/z part of every primitive is the same for all voxels of a
+// column, so two voxels of one column (same x, z; y0, y1) are evaluated in one
+// pass, sharing that part (a prism's polygon distance, a cylinder's radius...).
+// Each result encloses the same expression as sdf32i's, in the same order of
+// operations on every value.
+__host__ __device__ constexpr bool op_is_y_separable(uint32_t op) {
+  return op == OP_BOX || op == OP_ROUNDBOX || op == OP_CYL_Y || op == OP_TORUS_Y || op == OP_STADIUM ||
+         op == OP_PRISM || op == OP_ROT_Y || op == OP_ROT_END || op == OP_OFFSET || op == OP_NEGMAX ||
+         op == OP_MAX || op == OP_MIN;
+}
+
+struct Iv2 {
+  Iv a, b;  // the values at y0 and y1
+};
+
+__device__ __forceinline__ Iv2 prim32_y2(uint32_t op, int cnt, const Iv* __restrict__ p, Iv x, Iv y0, Iv y1, Iv z,
+                                         float M, bool& amb) {
+  switch (op) {
+    case OP_BOX: case OP_ROUNDBOX: {
+      const Iv qx = isub(iabs(isub(x, ldp(p, 0))), ldp(p, 3)), qz = isub(iabs(isub(z, ldp(p, 2))), ldp(p, 5));
+      const Iv sx = isqr(imax0(qx)), sz = isqr(imax0(qz)), mxz = qx;
+      const Iv cy = ldp(p, 1), hy = ldp(p, 4);
+      Iv out[2];
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        const Iv qy = isub(iabs(isub(k ? y1 : y0, cy)), hy);
+        out[k] = iadd(isqrt(iadd(iadd(sx, isqr(imax0(qy))), sz)), imin0(imax(imax(mxz, qy), qz)));
+      }
+      if (op == OP_ROUNDBOX) {
+        const Iv r = ldp(p, 6);
+        out[0] = isub(out[0], r);
+        out[1] = isub(out[1], r);
+      }
+      return {out[0], out[1]};
+    }
+    case OP_CYL_Y: {
+      const Iv dr = isub(ilen2(isub(x, ldp(p, 0)), isub(z, ldp(p, 2))), ldp(p, 3));
+      const Iv cy = ldp(p, 1), hh = ldp(p, 4);
+      Iv out[2];
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        const Iv dh = isub(iabs(isub(k ? y1 : y0, cy)), hh);
+        out[k] = iadd(imin0(imax(dr, dh)), ilen2(imax0(dr), imax0(dh)));
+      }
+      return {out[0], out[1]};
+    }
+    case OP_TORUS_Y: {
+      const Iv t = isub(ilen2(isub(x, ldp(p, 0)), isub(z, ldp(p, 2))), ldp(p, 3));
+      const Iv cy = ldp(p, 1), r = ldp(p, 4);
+      return {isub(ilen2(t, isub(y0, cy)), r), isub(ilen2(t, isub(y1, cy)), r)};
+    }
+    case OP_STADIUM: {
+      const Iv dx = imax0(isub(iabs(isub(x, ldp(p, 0))), ldp(p, 2)));
+      const Iv d2 = isub(ilen2(dx, isub(z, ldp(p, 1))), ldp(p, 3));
+      const Iv cy = ldp(p, 4), hh = ldp(p, 5);
+      Iv out[2];
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        const Iv dy = isub(iabs(isub(k ? y1 : y0, cy)), hh);
+        out[k] = iadd(imin0(imax(d2, dy)), ilen2(imax0(d2), imax0(dy)));
+      }
+      return {out[0], out[1]};
+    }
+    case OP_PRISM: {
+      const Iv d2 = sd_polygon32(isub(x, ldp(p, 0)), isub(z, ldp(p, 1)), p + 4, cnt, M, amb);
+      const Iv cy = ldp(p, 2), hh = ldp(p, 3);
+      Iv out[2];
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        const Iv dy = isub(iabs(isub(k ? y1 : y0, cy)), hh);
+        out[k] = iadd(imin0(imax(d2, dy)), ilen2(imax0(d2), imax0(dy)));
+      }
+      return {out[0], out[1]};
+    }
+  }
+  return {{-INFINITY, INFINITY}, {-INFINITY, INFINITY}};
+}
+
+// sdf32i for a y-separable shape at (x, y0, z) and (x, y1, z).
+__device__ __forceinline__ Iv2 sdf32i_y2(const uint2* __restrict__ code, const uint32_t* __restrict__ code32, int n,
+                                         const Iv* __restrict__ P, Iv x, Iv y0, Iv y1, Iv z, float M, bool& amb) {
+  const Iv zero = {0.f, 0.f};
+  Iv2 s0 = {zero, zero}, s1 = s0, s2 = s0, s3 = s0;
+  Iv ax0 = zero, az0 = zero, ax1 = zero, az1 = zero, ax2 = zero, az2 = zero;
+  for (int i = 0; i < n; i++) {
+    const uint32_t w0 = __ldg(&code[i].x);
+    const uint32_t op = w0 & 0xffu;
+    const int cnt = (int)(w0 >> 8);
+    const Iv* p = P + __ldg(code32 + i);
+    switch (op) {
+      case OP_ROT_Y: {  // rotations about y keep y: x and z only
+        ax2 = ax1; az2 = az1; ax1 = ax0; az1 = az0; ax0 = x; az0 = z;
+        const Iv p0 = ldp(p, 0), p1 = ldp(p, 1), c = ldp(p, 2), sn = ldp(p, 3);
+        const Iv dx = isub(x, p0), dz = isub(z, p1);
+        x = iadd(iadd(p0, icmul(dx, c)), icmul(dz, sn));
+        z = iadd(isub(p1, icmul(dx, sn)), icmul(dz, c));
+        break;
+      }
+      case OP_ROT_END:
+        x = ax0; z = az0; ax0 = ax1; az0 = az1; ax1 = ax2; az1 = az2;
+        break;
+      case OP_OFFSET: {
+        const Iv o = ldp(p, 0);
+        s0 = {iadd(s0.a, o), iadd(s0.b, o)};
+        break;
+      }
+      case OP_NEGMAX: case OP_MAX: case OP_MIN: {
+        const Iv2 b = s0;
+        s0 = s1; s1 = s2; s2 = s3;
+        if (op == OP_NEGMAX) s0 = {imax(s0.a, ineg(b.a)), imax(s0.b, ineg(b.b))};
+        else if (op == OP_MAX) s0 = {imax(s0.a, b.a), imax(s0.b, b.b)};
+        else s0 = {imin(s0.a, b.a), imin(s0.b, b.b)};
+        break;
+      }
+      default: {
+        const Iv2 v = prim32_y2(op, cnt, p, x, y0, y1, z, M, amb);
+        s3 = s2; s2 = s1; s1 = s0; s0 = v;
+      }
+    }
+  }
+  return s0;
+}
+
 }  // namespace px
