@@ -1,0 +1,114 @@
+"""Edge cases of the rasteriser against the oracle, bit for bit, in both forms.
+
+Empty op lists, ops wholly outside the world, degenerate shapes (zero-size
+boxes, capsules with equal ends, lathe profiles with repeated points,
+collinear prisms), paints on air and paints that return air, carve/re-add
+sequences that reuse freed pool bricks in LIFO order, and a world wider than
+the float32 path certifies (every op then runs in float64).
+"""
+import numpy as np
+import pytest
+
+from pixels_gb300 import config
+from pixels_gb300.ir import Program
+from pixels_gb300.materials import M, vox
+from pixels_gb300.paints import black_keys, tufted
+from pixels_gb300.shapes import (box, boxMinMax, capsule, cylinder, lathe, prism, rotateY, roundBox, sphere,
+                                 subtract, torus)
+from pixels_gb300.world import MODE_FP64, MODE_MIXED, VoxelWorld
+
+import pyoracle
+
+
+def run_both(prog: Program, vpm: float, dims):
+    """Build the op list on the GPU in both forms (and in validation mode) and the oracle."""
+    o = pyoracle.OracleWorld(prog.to_bytes(), vpm, dims)
+    out = []
+    for mode, validate in ((MODE_FP64, False), (MODE_MIXED, False), (MODE_MIXED, True)):
+        w = VoxelWorld(*dims, initialPoolBricks=4, vpm=vpm, mode=mode)
+        if validate:
+            from pixels_gb300 import _lib
+            _lib.set_validation(w._h, True)
+        w._pending = prog
+        w.build()
+        grid = w.grid
+        np.testing.assert_array_equal(grid, o.grid, err_msg=f"grid, mode {mode} validate {validate}")
+        assert w.poolUsed == o.pool_used
+        np.testing.assert_array_equal(w.freeBricks(), o.free_holes)
+        live = np.nonzero((o.grid != 0) & ((o.grid & 0x80000000) == 0))[0]
+        idx = o.grid[live].astype(np.int64) - 1
+        np.testing.assert_array_equal(w.pool.reshape(-1, 512)[idx], o.pool.reshape(-1, 512)[idx])
+        d = w.derived()
+        np.testing.assert_array_equal(d["super"], o.super)
+        np.testing.assert_array_equal(d["density"], o.density)
+        if validate:
+            assert w.stats()["violations"] == 0
+        out.append(w.stats())
+        w.close()
+    return o, out
+
+
+def program(vpm, ops):
+    prog = Program()
+    with config.using(vpm):
+        for kind, shape, paint in ops():
+            prog.add_op(kind, shape, paint)
+    return prog
+
+
+@pytest.mark.gpu
+def test_empty_op_list(built_lib):
+    o, _ = run_both(Program(), 40.0, (64, 32, 48))
+    assert o.pool_used == 0 and not o.grid.any()
+
+
+@pytest.mark.gpu
+def test_ops_outside_the_world_and_degenerate_shapes(built_lib):
+    vpm = 40.0
+    vs = 1 / vpm
+
+    def ops():
+        yield 0, box((-5.0, -5.0, -5.0), (0.5, 0.5, 0.5)), vox(M.wall)           # wholly outside
+        yield 0, box((0.5, 0.4, 0.5), (0.0, 0.0, 0.0)), vox(M.marble)            # zero-size box
+        yield 0, capsule((0.3, 0.3, 0.3), (0.3, 0.3, 0.3), 0.1), vox(M.gold)      # equal ends: bb || 1e-12
+        yield 0, lathe((0.8, 0.2, 0.8), [0.1, 0.0, 0.1, 0.0, 0.15, 0.2, 0.0, 0.3], 0), vox(M.porcelain)  # repeated point
+        yield 0, lathe((0.2, 0.2, 0.9), [0.05, 0.0, 0.05, 0.0, 0.08, 0.25], vs * 2), vox(M.glassClear)
+        yield 0, prism((0.6, 0.1, 0.3), [0.0, 0.0, 0.1, 0.0, 0.2, 0.0, 0.1, 0.1], 0.1, 0.3), vox(M.oak)  # collinear
+        yield 0, torus((0.4, 0.5, 0.6), 0.15, 0.0, "x"), vox(M.chrome)          # radius clamped to the minimum
+        yield 0, cylinder((1.0, 0.3, 0.2), 0.0, 0.0, "z"), vox(M.steelDark)      # clamped radius and height
+        yield 0, rotateY(roundBox((0.9, 0.5, 0.5), (0.2, 0.1, 0.15), 0.05), 0.7, (0.9, 0.5, 0.5)), vox(M.velvet)
+        yield 0, subtract(sphere((0.5, 0.5, 0.5), 0.3), box((0.5, 0.5, 0.5), (0.1, 0.4, 0.1))), vox(M.felt)
+    o, _ = run_both(program(vpm, ops), vpm, (48, 32, 48))
+    assert o.pool_used > 0
+
+
+@pytest.mark.gpu
+def test_paints_on_air_paints_returning_air_and_pool_reuse(built_lib):
+    vpm = 40.0
+
+    def ops():
+        yield 2, box((0.4, 0.4, 0.4), (0.3, 0.3, 0.3)), vox(M.gold)             # paint on air: nothing
+        yield 0, boxMinMax(0.1, 0.1, 0.1, 0.9, 0.6, 0.9), vox(M.wall)
+        yield 0, boxMinMax(0.2, 0.2, 0.2, 0.7, 0.5, 0.7), black_keys(0.2, M.lacquer)  # returns 0 between keys
+        yield 1, sphere((0.5, 0.35, 0.5), 0.25), 0                                # carve: frees bricks
+        yield 2, boxMinMax(0.0, 0.0, 0.0, 1.0, 0.7, 1.0), tufted(0.1, 0.1, M.leather)
+        yield 0, sphere((0.45, 0.4, 0.45), 0.12), vox(M.bulb)                     # re-add: pops freed bricks
+        yield 1, boxMinMax(0.0, 0.0, 0.0, 1.0, 1.0, 0.35), 0                      # frees more
+        yield 0, capsule((0.1, 0.2, 0.1), (0.9, 0.5, 0.3), 0.08), vox(M.chrome)
+    o, stats = run_both(program(vpm, ops), vpm, (48, 32, 48))
+    assert o.free_holes.size > 0 or o.stats["frees"] > 0
+    assert all(s["free_events"] > 0 for s in stats)
+
+
+@pytest.mark.gpu
+def test_world_wider_than_the_float32_range(built_lib):
+    """1,104 m along z at 1 voxel per metre: every op runs in float64 in the mixed form."""
+    vpm = 1.0
+
+    def ops():
+        yield 0, boxMinMax(0.0, 0.0, 1000.0, 8.0, 8.0, 1100.0), vox(M.concrete)
+        yield 0, sphere((4.0, 4.0, 1050.0), 3.5), vox(M.marble)
+        yield 1, capsule((1.0, 1.0, 1010.0), (7.0, 7.0, 1090.0), 1.2), 0
+    o, stats = run_both(program(vpm, ops), vpm, (8, 8, 1104))
+    assert o.pool_used > 0
+    assert stats[1]["rescued"] == 0  # nothing to rescue: no float32 evaluation at all
