@@ -560,11 +560,10 @@ int convert_ops(const px_world* w, const IrOp* iops, size_t i0, size_t i1, const
       }
     }
     d.code_len = o.code_len;
-    {  // voxel work class: the primitive of a one-primitive shape (an offset may follow)
-      const uint32_t op0 = code[2 * (size_t)o.code_begin] & 0xffu;
-      const bool lone = o.code_len == 1 ||
-                        (o.code_len == 2 && (code[2 * ((size_t)o.code_begin + 1)] & 0xffu) == OP_OFFSET);
-      d.vclass = lone && op0 < (uint32_t)VCLASSES ? op0 : 0u;
+    uint32_t first_prim = 0;  // work class: the shape's first primitive (+16 if y-extruded, below)
+    for (uint32_t k = 0; k < o.code_len && !first_prim; k++) {
+      const uint32_t opk = code[2 * ((size_t)o.code_begin + k)] & 0xffu;
+      if (opk >= OP_BOX && opk < OP_ROT_X) first_prim = opk;
     }
     d.paint_off = (uint32_t)(param_base + o.paint_param);
     for (int k = 0; k < 3; k++) { d.mn[k] = o.mn[k]; d.mx[k] = o.mx[k]; }
@@ -667,6 +666,7 @@ int convert_ops(const px_world* w, const IrOp* iops, size_t i0, size_t i1, const
         for (uint32_t k = 0; k < o.code_len; k++)
           ysep = ysep && op_is_y_separable(code[2 * ((size_t)o.code_begin + k)] & 0xffu);
         if (ysep) d.flags |= OPF_Y_SEPARABLE;
+        d.vclass = (first_prim & 15u) | (ysep && !(d.flags & OPF_FP64_ONLY) ? 16u : 0u);
       }
       d.paint_slot = NO_SLOT;
       d.paint32_off = NO_SLOT;
@@ -905,7 +905,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
       (rc = ensure(w, w->touched, 8 * touched_bound)) ||
       (rc = ensure(w, w->work_counter, 16)) || (rc = ensure(w, w->res, sizeof(BuildResult))) ||
       (rc = ensure(w, w->chunk_op, 4 * ((P + 31) / 32))) || (rc = ensure(w, w->pcode, P)) ||
-      (rc = ensure(w, w->psub, 2 * P)) || (rc = ensure(w, w->pmask, 64 * P)) || (rc = ensure(w, w->chunk_counter, 256)) || (rc = ensure(w, w->pitems, 8 * P)) ||
+      (rc = ensure(w, w->psub, 2 * P)) || (rc = ensure(w, w->pmask, 64 * P)) || (rc = ensure(w, w->chunk_counter, 512)) || (rc = ensure(w, w->pitems, 8 * P)) ||
       (rc = ensure(w, w->vitems, 8 * 8 * P)) || (rc = ensure(w, w->paint_items, 8 * 8 * n_slots + 8)) ||
       (rc = ensure(w, w->pvals, 2048 * n_slots + 4)) || (rc = ensure(w, w->bmark, 4 * ((w->ncells + 31) / 32))) ||
       (rc = ensure(w, w->work, 4 * touched_bound + 4)))
@@ -963,7 +963,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   }
   CU(cudaMemsetAsync(w->res.p, 0, sizeof(BuildResult), s));
   CU(cudaMemsetAsync(w->work_counter.p, 0, 16, s));
-  CU(cudaMemsetAsync(w->chunk_counter.p, 0, 256, s));
+  CU(cudaMemsetAsync(w->chunk_counter.p, 0, 512, s));
   if (upload) {  // op of the first pair of every 32-pair chunk
     const size_t n_chunks = (P + 31) / 32;
     w->h_chunk_op.resize(n_chunks);
@@ -995,7 +995,8 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   fa.chunk_counter = (uint32_t*)w->chunk_counter.p;
   fa.vitems = (uint2*)w->vitems.p;
   fa.vitems_cap = (uint32_t)(8 * P < 0xffffffffull ? 8 * P : 0xffffffffull);
-  fa.vitem_counter = (uint32_t*)w->chunk_counter.p + 2;
+  fa.vitem_counter = (uint32_t*)w->chunk_counter.p + 4;   // counters: [0] chunks, [1] paint taken,
+                                                          // [2] paint pushed, [4..36] voxel, [40..72] pairs
   {  // per-class regions: the class's pairs (sub-block pass), 8 sub-blocks per pair (voxel pass)
     uint64_t per[VCLASSES] = {0};
     for (int i = 0; i < n_ops; i++) {
@@ -1013,12 +1014,12 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
     }
   }
   fa.pitems = (uint2*)w->pitems.p;
-  fa.pitem_counter = (uint32_t*)w->chunk_counter.p + 20;
+  fa.pitem_counter = (uint32_t*)w->chunk_counter.p + 40;
   fa.paint_counter = (uint32_t*)w->chunk_counter.p + 1;
   fa.n_paint_slots = (uint32_t)n_slots;
   fa.paint_items = (uint2*)w->paint_items.p;
   fa.paint_items_cap = (uint32_t)std::min<uint64_t>(8 * n_slots, 0xffffffffull);
-  fa.paint_item_counter = (uint32_t*)w->chunk_counter.p + 38;
+  fa.paint_item_counter = (uint32_t*)w->chunk_counter.p + 2;
   fa.pvals = (uint32_t*)w->pvals.p;
   fa.inline_paints = inline_paints ? 1 : 0;
   fa.bmark = (uint32_t*)w->bmark.p;

@@ -127,10 +127,10 @@ struct BuildResult {
 // sub-block classes of partial pairs, and voxel inside-masks of partial sub-blocks.
 enum : uint8_t { PC_SKIP = 0, PC_PARTIAL = 1, PC_FULL = 2 };
 
-// Voxel work items are grouped by the op's shape (its primitive when the code
-// is one primitive, optionally followed by an offset; class 0 otherwise), so
-// that warps draining the queue at the same time run the same code.
-constexpr int VCLASSES = 16;
+// Work items of the sub-block and voxel passes are grouped by the op's shape
+// (its first primitive, and whether it runs the y-extruded evaluation), so
+// that warps draining a queue at the same time run the same code.
+constexpr int VCLASSES = 32;
 
 struct FoldArgs {
   const uint32_t* chunk_op;   // op containing pair 32 * chunk
