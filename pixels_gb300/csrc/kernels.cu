@@ -731,199 +731,221 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
   uint32_t st_local = 0;
   const uint32_t n_work = __ldg(&a.res->n_work);
 
-  WorkBatch wb;
+  // bricks are taken four at a time; the grid entry and tile list of the next
+  // brick are loaded while the current one is applied
   for (;;) {
-    const uint32_t item = wb.next(a.work_counter, 4, lane);
-    if (item >= n_work) break;
-    const size_t ci = __ldg(a.work + item);
-    const int bx = (int)(ci % (size_t)a.BX), byz = (int)(ci / (size_t)a.BX), by = byz % a.BY, bz = byz / a.BY;
-    const uint32_t tile = (uint32_t)((bx >> 2) + a.TX * ((by >> 2) + a.TY * (bz >> 2)));
-    const int ox = bx * 8, oy = by * 8, oz = bz * 8;
-
-    // current brick contents (VoxelWorld.ts:55-61); every listed brick has an op
-    // that applies, so they are loaded up front, overlapping the op lookups
-    int state = ST_EMPTY;
-    uint32_t uval = 0;
-    uint32_t vox[8];
-    long long src = -1;  // pool identity: >= 0 pair of the last alloc, < 0 -(old index + 1)
-    bool dirty = false;
+    uint32_t wbase = 0;
+    if (lane == 0) wbase = atomicAdd(a.work_counter, 4u);
+    wbase = __shfl_sync(FULLMASK, wbase, 0);
+    if (wbase >= n_work) break;
+    const uint32_t n_here = min(4u, n_work - wbase);
+    const uint32_t my_ci = lane < (int)n_here ? __ldg(a.work + wbase + lane) : 0u;
+    uint32_t nci = __shfl_sync(FULLMASK, my_ci, 0);
+    uint32_t ng = a.grid[nci];
+    uint32_t ntile = 0, ntoff = 0, ntcnt = 0;
     {
-      const uint32_t g = a.grid[ci];
-      if (g == 0) {
-#pragma unroll
-        for (int j = 0; j < 8; j++) vox[j] = 0;
-      } else if (g & UNIFORM) {
-        state = ST_UNIF; uval = g & 0xffffu;
-#pragma unroll
-        for (int j = 0; j < 8; j++) vox[j] = uval | (uval << 16);
-      } else {
-        state = ST_MIXED; src = -(long long)(g - 1) - 1;
-        const uint32_t* pb = a.pool32 + (size_t)(g - 1) * 256;
-#pragma unroll
-        for (int j = 0; j < 8; j++) vox[j] = pb[32 * j + lane];
-      }
+      const int bx = (int)(nci % (uint32_t)a.BX), byz = (int)(nci / (uint32_t)a.BX), by = byz % a.BY, bz = byz / a.BY;
+      ntile = (uint32_t)((bx >> 2) + a.TX * ((by >> 2) + a.TY * (bz >> 2)));
+      ntoff = __ldg(a.tile_off + ntile);
+      ntcnt = __ldg(a.tile_cnt + ntile);
     }
+    for (uint32_t j = 0; j < n_here; j++) {
+      const size_t ci = nci;
+      const uint32_t g = ng, toff = ntoff, tcnt = ntcnt;
+      if (j + 1 < n_here) {  // prefetch the next brick
+        nci = __shfl_sync(FULLMASK, my_ci, j + 1);
+        ng = a.grid[nci];
+        const int bx = (int)(nci % (uint32_t)a.BX), byz = (int)(nci / (uint32_t)a.BX), by = byz % a.BY, bz = byz / a.BY;
+        ntile = (uint32_t)((bx >> 2) + a.TX * ((by >> 2) + a.TY * (bz >> 2)));
+        ntoff = __ldg(a.tile_off + ntile);
+        ntcnt = __ldg(a.tile_cnt + ntile);
+      }
+      const int bx = (int)(ci % (size_t)a.BX), byz = (int)(ci / (size_t)a.BX), by = byz % a.BY, bz = byz / a.BY;
+      const int ox = bx * 8, oy = by * 8, oz = bz * 8;
 
-    const uint32_t toff = __ldg(a.tile_off + tile), tcnt = __ldg(a.tile_cnt + tile);
-    for (uint32_t c0 = 0; c0 < tcnt; c0 += 32) {
-      // each lane looks up one op of the tile: does it cover the brick, the
-      // pair's classes, and the op fields the apply loop needs (all loads in parallel)
-      uint32_t oi = 0, meta = 0, pval = 0, pslot = NO_SLOT, sc = 0;
-      unsigned long long pr = 0;
-      int ocls = PC_SKIP;
-      if (c0 + lane < tcnt) {
-        oi = __ldg(a.tile_ops + toff + c0 + lane);
-        const OpDev* o = a.ops + oi;
-        if (bx >= o->bx0 && bx <= o->bx1 && by >= o->by0 && by <= o->by1 && bz >= o->bz0 && bz <= o->bz1) {
-          pr = o->pair_base + (unsigned long long)(((bz - o->bz0) * o->ny + (by - o->by0)) * o->nx + (bx - o->bx0));
-          ocls = __ldg(a.pcode + pr);
-          sc = __ldg(a.psub + pr);  // meaningful for partial pairs only
-          meta = (uint32_t)o->kind | ((uint32_t)o->flags << 8) | ((uint32_t)o->paint_kind << 16);
-          pval = o->paint_value;
-          pslot = o->paint_slot == NO_SLOT ? NO_SLOT : o->paint_slot + (uint32_t)(pr - o->pair_base);
+      // current brick contents (VoxelWorld.ts:55-61); every listed brick has an op
+      // that applies, so they are loaded up front, overlapping the op lookups
+      int state = ST_EMPTY;
+      uint32_t uval = 0;
+      uint32_t vox[8];
+      long long src = -1;  // pool identity: >= 0 pair of the last alloc, < 0 -(old index + 1)
+      bool dirty = false;
+      {
+        if (g == 0) {
+  #pragma unroll
+          for (int j = 0; j < 8; j++) vox[j] = 0;
+        } else if (g & UNIFORM) {
+          state = ST_UNIF; uval = g & 0xffffu;
+  #pragma unroll
+          for (int j = 0; j < 8; j++) vox[j] = uval | (uval << 16);
+        } else {
+          state = ST_MIXED; src = -(long long)(g - 1) - 1;
+          const uint32_t* pb = a.pool32 + (size_t)(g - 1) * 256;
+  #pragma unroll
+          for (int j = 0; j < 8; j++) vox[j] = pb[32 * j + lane];
         }
       }
-      uint32_t m = __ballot_sync(FULLMASK, ocls != PC_SKIP);  // shapes.ts:364 skips the rest
-      while (m) {
-        const int b = __ffs(m) - 1;
-        m &= m - 1;
-        const unsigned long long pair = __shfl_sync(FULLMASK, pr, b);
-        const int cls = __shfl_sync(FULLMASK, ocls, b);
-        const uint32_t mt = __shfl_sync(FULLMASK, meta, b);
-        const uint32_t pv = __shfl_sync(FULLMASK, pval, b);
-        const uint32_t slot = __shfl_sync(FULLMASK, pslot, b);
-        const uint32_t o_idx = __shfl_sync(FULLMASK, oi, b);
-        const bool full = cls == PC_FULL;
-        const int kind = (int)(mt & 0xffu);
-        const uint32_t pk = mt >> 16;
-        const bool constPaint = pk == PK_CONST;
-        // uniform shortcuts (shapes.ts:367-374)
-        int set_u = -1;
-        if (full) {
-          if (kind == KIND_ADD && constPaint) set_u = (int)pv;
-          else if (kind == KIND_CARVE) set_u = 0;
-          else if (kind == KIND_PAINT && state == ST_EMPTY) continue;
-          else if (kind == KIND_PAINT && constPaint && state == ST_UNIF) set_u = (int)pv;
-        }
-        if (set_u >= 0) {  // setBrickUniform (VoxelWorld.ts:89-97)
-          if (state == ST_MIXED) {
-            if (lane == 0) { a.evt[pair] = 2; a.fsrc[pair] = src; }
-            wc.free_++;
-          }
-          uint32_t v = (uint32_t)set_u;
-          state = v == 0 ? ST_EMPTY : ST_UNIF;
-          uval = v; src = -1;
-#pragma unroll
-          for (int j = 0; j < 8; j++) vox[j] = v | (v << 16);
-          dirty = true;
-          continue;
-        }
-        if (kind == KIND_PAINT && state == ST_EMPTY) continue;
 
-        // sub-block and voxel classes (shapes.ts:382-394), computed by classify_kernel
-        if (!full) {
-          const uint32_t psc = __shfl_sync(FULLMASK, sc, b);
-          if (lane < 8) {
-            const uint32_t c = (psc >> (2 * lane)) & 3u;
-            smask[wib][lane] = c == PC_FULL ? ~0ull : c == PC_PARTIAL ? __ldg(a.pmask + pair * 8 + lane) : 0ull;
+      for (uint32_t c0 = 0; c0 < tcnt; c0 += 32) {
+        // each lane looks up one op of the tile: does it cover the brick, the
+        // pair's classes, and the op fields the apply loop needs (all loads in parallel)
+        uint32_t oi = 0, meta = 0, pval = 0, pslot = NO_SLOT, sc = 0;
+        unsigned long long pr = 0;
+        int ocls = PC_SKIP;
+        if (c0 + lane < tcnt) {
+          oi = __ldg(a.tile_ops + toff + c0 + lane);
+          const OpDev* o = a.ops + oi;
+          if (bx >= o->bx0 && bx <= o->bx1 && by >= o->by0 && by <= o->by1 && bz >= o->bz0 && bz <= o->bz1) {
+            pr = o->pair_base + (unsigned long long)(((bz - o->bz0) * o->ny + (by - o->by0)) * o->nx + (bx - o->bx0));
+            ocls = __ldg(a.pcode + pr);
+            sc = __ldg(a.psub + pr);  // meaningful for partial pairs only
+            meta = (uint32_t)o->kind | ((uint32_t)o->flags << 8) | ((uint32_t)o->paint_kind << 16);
+            pval = o->paint_value;
+            pslot = o->paint_slot == NO_SLOT ? NO_SLOT : o->paint_slot + (uint32_t)(pr - o->pair_base);
           }
-          wc.sub += 8;
-          uint32_t np_ = 0;
-#pragma unroll
-          for (int s2 = 0; s2 < 8; s2++) np_ += ((psc >> (2 * s2)) & 3u) == PC_PARTIAL;
-          wc.vox += 64 * np_;
-        } else if (lane < 8) {
-          smask[wib][lane] = ~0ull;
         }
-        __syncwarp();
+        uint32_t m = __ballot_sync(FULLMASK, ocls != PC_SKIP);  // shapes.ts:364 skips the rest
+        while (m) {
+          const int b = __ffs(m) - 1;
+          m &= m - 1;
+          const unsigned long long pair = __shfl_sync(FULLMASK, pr, b);
+          const int cls = __shfl_sync(FULLMASK, ocls, b);
+          const uint32_t mt = __shfl_sync(FULLMASK, meta, b);
+          const uint32_t pv = __shfl_sync(FULLMASK, pval, b);
+          const uint32_t slot = __shfl_sync(FULLMASK, pslot, b);
+          const uint32_t o_idx = __shfl_sync(FULLMASK, oi, b);
+          const bool full = cls == PC_FULL;
+          const int kind = (int)(mt & 0xffu);
+          const uint32_t pk = mt >> 16;
+          const bool constPaint = pk == PK_CONST;
+          // uniform shortcuts (shapes.ts:367-374)
+          int set_u = -1;
+          if (full) {
+            if (kind == KIND_ADD && constPaint) set_u = (int)pv;
+            else if (kind == KIND_CARVE) set_u = 0;
+            else if (kind == KIND_PAINT && state == ST_EMPTY) continue;
+            else if (kind == KIND_PAINT && constPaint && state == ST_UNIF) set_u = (int)pv;
+          }
+          if (set_u >= 0) {  // setBrickUniform (VoxelWorld.ts:89-97)
+            if (state == ST_MIXED) {
+              if (lane == 0) { a.evt[pair] = 2; a.fsrc[pair] = src; }
+              wc.free_++;
+            }
+            uint32_t v = (uint32_t)set_u;
+            state = v == 0 ? ST_EMPTY : ST_UNIF;
+            uval = v; src = -1;
+  #pragma unroll
+            for (int j = 0; j < 8; j++) vox[j] = v | (v << 16);
+            dirty = true;
+            continue;
+          }
+          if (kind == KIND_PAINT && state == ST_EMPTY) continue;
 
-        // write voxels (shapes.ts:395-405)
-        bool changed = false;
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-          const int s = (lx0 >> 2) | ((ly >> 2) << 1) | ((j >> 2) << 2);
-          const int e0 = (lx0 & 3) | ((ly & 3) << 2) | ((j & 3) << 4);
-          const unsigned long long ms = smask[wib][s];
-#pragma unroll
-          for (int h = 0; h < 2; h++) {
-            if (!((ms >> (e0 + h)) & 1ull)) continue;
-            const uint32_t cur = (vox[j] >> (16 * h)) & 0xffffu;
-            uint32_t next;
-            if (kind == KIND_CARVE) next = 0;
-            else if (kind == KIND_PAINT && cur == 0) continue;
-            else if (!constPaint && slot != NO_SLOT) {  // evaluated by paint_kernel
-              const uint32_t pvv = __ldg(a.pvals + (size_t)slot * 512 + (uint32_t)((lx0 + h) | (ly << 3) | (j << 6)));
-              if (pvv & PV_RANGE) st_local |= ST_RANGE;
-              next = pvv & 0xffffu;
-              paint_calls++;
-            } else if (!constPaint) {
-              if constexpr (INLINE) {
-                const uint32_t pv2 = paint_at_voxel(a.params, a.vs, a.validate, a.ops + o_idx, ox + lx0 + h, oy + ly, oz + j);
-                if (pv2 & PV_RANGE) st_local |= ST_RANGE;
-                if (pv2 & PV_VIOL) paint_viol++;
-                next = pv2 & 0xffffu;
+          // sub-block and voxel classes (shapes.ts:382-394), computed by classify_kernel
+          if (!full) {
+            const uint32_t psc = __shfl_sync(FULLMASK, sc, b);
+            if (lane < 8) {
+              const uint32_t c = (psc >> (2 * lane)) & 3u;
+              smask[wib][lane] = c == PC_FULL ? ~0ull : c == PC_PARTIAL ? __ldg(a.pmask + pair * 8 + lane) : 0ull;
+            }
+            wc.sub += 8;
+            uint32_t np_ = 0;
+  #pragma unroll
+            for (int s2 = 0; s2 < 8; s2++) np_ += ((psc >> (2 * s2)) & 3u) == PC_PARTIAL;
+            wc.vox += 64 * np_;
+          } else if (lane < 8) {
+            smask[wib][lane] = ~0ull;
+          }
+          __syncwarp();
+
+          // write voxels (shapes.ts:395-405)
+          bool changed = false;
+  #pragma unroll
+          for (int j = 0; j < 8; j++) {
+            const int s = (lx0 >> 2) | ((ly >> 2) << 1) | ((j >> 2) << 2);
+            const int e0 = (lx0 & 3) | ((ly & 3) << 2) | ((j & 3) << 4);
+            const unsigned long long ms = smask[wib][s];
+  #pragma unroll
+            for (int h = 0; h < 2; h++) {
+              if (!((ms >> (e0 + h)) & 1ull)) continue;
+              const uint32_t cur = (vox[j] >> (16 * h)) & 0xffffu;
+              uint32_t next;
+              if (kind == KIND_CARVE) next = 0;
+              else if (kind == KIND_PAINT && cur == 0) continue;
+              else if (!constPaint && slot != NO_SLOT) {  // evaluated by paint_kernel
+                const uint32_t pvv = __ldg(a.pvals + (size_t)slot * 512 + (uint32_t)((lx0 + h) | (ly << 3) | (j << 6)));
+                if (pvv & PV_RANGE) st_local |= ST_RANGE;
+                next = pvv & 0xffffu;
                 paint_calls++;
-              } else {  // every painted op has a slot in this build
-                st_local |= ST_CHAIN;
-                next = cur;
+              } else if (!constPaint) {
+                if constexpr (INLINE) {
+                  const uint32_t pv2 = paint_at_voxel(a.params, a.vs, a.validate, a.ops + o_idx, ox + lx0 + h, oy + ly, oz + j);
+                  if (pv2 & PV_RANGE) st_local |= ST_RANGE;
+                  if (pv2 & PV_VIOL) paint_viol++;
+                  next = pv2 & 0xffffu;
+                  paint_calls++;
+                } else {  // every painted op has a slot in this build
+                  st_local |= ST_CHAIN;
+                  next = cur;
+                }
+              } else next = pv;
+              if (next != cur) {  // Uint16Array store; the comparison uses the unstored value
+                vox[j] = (vox[j] & ~(0xffffu << (16 * h))) | ((next & 0xffffu) << (16 * h));
+                changed = true;
               }
-            } else next = pv;
-            if (next != cur) {  // Uint16Array store; the comparison uses the unstored value
-              vox[j] = (vox[j] & ~(0xffffu << (16 * h))) | ((next & 0xffffu) << (16 * h));
-              changed = true;
             }
           }
+          __syncwarp();
+          if (!__any_sync(FULLMASK, changed)) continue;
+          dirty = true;
+          uint8_t ev = 0;
+          if (state != ST_MIXED) {  // editableBrick -> allocBrick (VoxelWorld.ts:103-122)
+            ev = 1; src = (long long)pair; state = ST_MIXED;
+            wc.alloc++;
+          }
+          // compactCell (VoxelWorld.ts:147-156)
+          const uint32_t v0 = __shfl_sync(FULLMASK, vox[0] & 0xffffu, 0);
+          const uint32_t vv = v0 | (v0 << 16);
+          bool eq = true;
+  #pragma unroll
+          for (int j = 0; j < 8; j++) eq = eq && vox[j] == vv;
+          if (__all_sync(FULLMASK, eq)) {
+            if (lane == 0) a.fsrc[pair] = src;
+            ev |= 2;
+            wc.free_++;
+            state = v0 == 0 ? ST_EMPTY : ST_UNIF;
+            uval = v0; src = -1;
+          }
+          if (lane == 0) a.evt[pair] = ev;
         }
-        __syncwarp();
-        if (!__any_sync(FULLMASK, changed)) continue;
-        dirty = true;
-        uint8_t ev = 0;
-        if (state != ST_MIXED) {  // editableBrick -> allocBrick (VoxelWorld.ts:103-122)
-          ev = 1; src = (long long)pair; state = ST_MIXED;
-          wc.alloc++;
-        }
-        // compactCell (VoxelWorld.ts:147-156)
-        const uint32_t v0 = __shfl_sync(FULLMASK, vox[0] & 0xffffu, 0);
-        const uint32_t vv = v0 | (v0 << 16);
-        bool eq = true;
-#pragma unroll
-        for (int j = 0; j < 8; j++) eq = eq && vox[j] == vv;
-        if (__all_sync(FULLMASK, eq)) {
-          if (lane == 0) a.fsrc[pair] = src;
-          ev |= 2;
-          wc.free_++;
-          state = v0 == 0 ? ST_EMPTY : ST_UNIF;
-          uval = v0; src = -1;
-        }
-        if (lane == 0) a.evt[pair] = ev;
       }
-    }
 
-    if (!dirty) continue;
-    // the grid entry is committed by finalize, so a failed build leaves the world intact
-    uint32_t tag;
-    if (state == ST_EMPTY) {
-      tag = 0;
-    } else if (state == ST_UNIF) {
-      tag = UNIFORM | uval;
-    } else {
-      uint32_t slot = 0;
-      if (lane == 0) slot = atomicAdd(&a.res->stage_count, 1u);
-      slot = __shfl_sync(FULLMASK, slot, 0);
-      if (slot >= a.stage_cap) {
-        st_local |= ST_STAGE_OVERFLOW;
+      if (!dirty) continue;
+      // the grid entry is committed by finalize, so a failed build leaves the world intact
+      uint32_t tag;
+      if (state == ST_EMPTY) {
+        tag = 0;
+      } else if (state == ST_UNIF) {
+        tag = UNIFORM | uval;
       } else {
-        uint32_t* dst = a.staging32 + (size_t)slot * 256;
-#pragma unroll
-        for (int j = 0; j < 8; j++) dst[32 * j + lane] = vox[j];
-        if (lane == 0) { a.stage_cell[slot] = (uint32_t)ci; a.stage_src[slot] = src; }
+        uint32_t slot = 0;
+        if (lane == 0) slot = atomicAdd(&a.res->stage_count, 1u);
+        slot = __shfl_sync(FULLMASK, slot, 0);
+        if (slot >= a.stage_cap) {
+          st_local |= ST_STAGE_OVERFLOW;
+        } else {
+          uint32_t* dst = a.staging32 + (size_t)slot * 256;
+  #pragma unroll
+          for (int j = 0; j < 8; j++) dst[32 * j + lane] = vox[j];
+          if (lane == 0) { a.stage_cell[slot] = (uint32_t)ci; a.stage_src[slot] = src; }
+        }
+        tag = TAG_STAGED | (slot & 0x3fffffffu);
       }
-      tag = TAG_STAGED | (slot & 0x3fffffffu);
-    }
-    if (lane == 0) {
-      const uint32_t t = atomicAdd(&a.res->touched_count, 1u);
-      if (t < a.touched_cap) a.touched[t] = make_uint2((uint32_t)ci, tag);
-      else st_local |= ST_STAGE_OVERFLOW;
+      if (lane == 0) {
+        const uint32_t t = atomicAdd(&a.res->touched_count, 1u);
+        if (t < a.touched_cap) a.touched[t] = make_uint2((uint32_t)ci, tag);
+        else st_local |= ST_STAGE_OVERFLOW;
+      }
     }
   }
   if (lane == 0) {
