@@ -87,7 +87,8 @@ __global__ void __launch_bounds__(256) cull_count_kernel(const uint2* __restrict
 }
 
 __global__ void __launch_bounds__(256) cull_fill_kernel(const uint2* __restrict__ boxes, int n_ops, int TX, int TY, int TZ,
-                                                        const uint32_t* __restrict__ tile_off, uint32_t* tile_ops) {
+                                                        const uint32_t* __restrict__ tile_off, uint32_t* tile_ops,
+                                                        uint2* tile_boxes) {
   const int lane = threadIdx.x & 31;
   const int n_tiles = TX * TY * TZ;
   const int n_groups = (n_ops + 31) / 32;
@@ -101,9 +102,14 @@ __global__ void __launch_bounds__(256) cull_fill_kernel(const uint2* __restrict_
       while (gm) {
         const int i = (g0 + __ffs(gm) - 1) * 32 + lane;
         gm &= gm - 1;
-        bool ov = i < n_ops && box_overlaps_tile(__ldg(boxes + i), tx, ty, tz);
+        const uint2 b = i < n_ops ? __ldg(boxes + i) : make_uint2(3u << 30, 0u);
+        bool ov = i < n_ops && box_overlaps_tile(b, tx, ty, tz);
         uint32_t m = __ballot_sync(FULLMASK, ov);
-        if (ov) tile_ops[pos + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
+        if (ov) {
+          const uint32_t at = pos + __popc(m & ((1u << lane) - 1u));
+          tile_ops[at] = (uint32_t)i;
+          tile_boxes[at] = b;  // the op's brick box beside it, for the apply pass
+        }
         pos += __popc(m);
       }
     }
@@ -117,10 +123,10 @@ void launch_cull_count(const uint2* boxes, int n_ops, int TX, int TY, int TZ, ui
   ++g_launches; cull_count_kernel<<<blocks, 256, 0, s>>>(boxes, n_ops, TX, TY, TZ, tile_cnt, tiles_nonempty, res);
 }
 void launch_cull_fill(const uint2* boxes, int n_ops, int TX, int TY, int TZ, const uint32_t* tile_off,
-                      uint32_t* tile_ops, cudaStream_t s) {
+                      uint32_t* tile_ops, uint2* tile_boxes, cudaStream_t s) {
   int n_tiles = TX * TY * TZ;
   int blocks = (n_tiles * 32 + 255) / 256;
-  ++g_launches; cull_fill_kernel<<<blocks, 256, 0, s>>>(boxes, n_ops, TX, TY, TZ, tile_off, tile_ops);
+  ++g_launches; cull_fill_kernel<<<blocks, 256, 0, s>>>(boxes, n_ops, TX, TY, TZ, tile_off, tile_ops, tile_boxes);
 }
 
 // ---------------------------------------------------------------------------
@@ -794,9 +800,12 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
         int ocls = PC_SKIP;
         if (c0 + lane < tcnt) {
           oi = __ldg(a.tile_ops + toff + c0 + lane);
-          const OpDev* o = a.ops + oi;
-          if (bx >= o->bx0 && bx <= o->bx1 && by >= o->by0 && by <= o->by1 && bz >= o->bz0 && bz <= o->bz1) {
-            pr = o->pair_base + (unsigned long long)(((bz - o->bz0) * o->ny + (by - o->by0)) * o->nx + (bx - o->bx0));
+          const uint2 bb = __ldg(a.tile_boxes + toff + c0 + lane);  // the op's brick box
+          const int x0 = bb.x & 1023, y0 = (bb.x >> 10) & 1023, z0 = (bb.x >> 20) & 1023;
+          const int x1 = bb.y & 1023, y1 = (bb.y >> 10) & 1023, z1 = (bb.y >> 20) & 1023;
+          if (bx >= x0 && bx <= x1 && by >= y0 && by <= y1 && bz >= z0 && bz <= z1) {
+            const OpDev* o = a.ops + oi;
+            pr = o->pair_base + (unsigned long long)(((bz - z0) * (y1 - y0 + 1) + (by - y0)) * (x1 - x0 + 1) + (bx - x0));
             ocls = __ldg(a.pcode + pr);
             sc = __ldg(a.psub + pr);  // meaningful for partial pairs only
             meta = (uint32_t)o->kind | ((uint32_t)o->flags << 8) | ((uint32_t)o->paint_kind << 16);

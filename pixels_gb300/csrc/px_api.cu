@@ -63,7 +63,7 @@ struct px_world {
 
   // per-build device scratch
   DevBuf d_ops, d_boxes, d_code, d_params, d_code32, d_p32, d_bases;
-  DevBuf tile_cnt, tile_off, tiles_nonempty, tile_ops;
+  DevBuf tile_cnt, tile_off, tiles_nonempty, tile_ops, tile_boxes;
   DevBuf evt, fsrc, cnt, pos, etype, ew, depth_fn, depth, tree, fresh, fresh_rank;
   DevBuf staging, stage_cell, stage_src, touched;
   uint64_t stage_hint = 0;      // staging slots the next build reserves (grown on overflow)
@@ -402,7 +402,7 @@ void px_world_destroy(px_world* w) {
                     &w->ew, &w->depth_fn, &w->depth, &w->tree, &w->fresh, &w->fresh_rank, &w->staging, &w->touched,
                     &w->stage_cell, &w->stage_src, &w->chunk_op, &w->pcode, &w->psub, &w->pmask,
                     &w->chunk_counter, &w->vitems, &w->scan_agg, &w->work_counter, &w->res, &w->opaque,
-                    &w->udens, &w->super_counts, &w->density, &w->paint_items, &w->pvals, &w->bmark, &w->work, &w->pitems};
+                    &w->udens, &w->super_counts, &w->density, &w->paint_items, &w->pvals, &w->tile_boxes, &w->bmark, &w->work, &w->pitems};
   for (DevBuf* b : bufs) release(*b);
   if (w->h_res) cudaFreeHost(w->h_res);
   if (w->ev0) cudaEventDestroy(w->ev0);
@@ -895,7 +895,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
       (rc = ensure(w, w->d_p32, sizeof(float2) * w->p32.size())) ||
       (rc = ensure(w, w->d_bases, sizeof(float2) * w->bases.size())) ||
       (rc = ensure(w, w->tile_cnt, 4 * w->ntiles)) || (rc = ensure(w, w->tile_off, 4 * w->ntiles)) ||
-      (rc = ensure(w, w->tiles_nonempty, 4 * w->ntiles)) || (rc = ensure(w, w->tile_ops, 4 * tile_pairs)) ||
+      (rc = ensure(w, w->tiles_nonempty, 4 * w->ntiles)) || (rc = ensure(w, w->tile_ops, 4 * tile_pairs)) || (rc = ensure(w, w->tile_boxes, 8 * tile_pairs)) ||
       (rc = ensure(w, w->evt, P)) || (rc = ensure(w, w->fsrc, 8 * P)) || (rc = ensure(w, w->cnt, 4 * P)) ||
       (rc = ensure(w, w->pos, 4 * P)) || (rc = ensure(w, w->etype, E_max)) || (rc = ensure(w, w->ew, 8 * E_max)) ||
       (rc = ensure(w, w->depth_fn, 8 * E_max)) || (rc = ensure(w, w->depth, 4 * E_max)) ||
@@ -984,7 +984,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
                     (uint32_t*)w->tiles_nonempty.p, res, s);
   launch_scan_u32((const uint32_t*)w->tile_cnt.p, (uint32_t*)w->tile_off.p, w->ntiles, nullptr, false, nullptr, st, s);
   launch_cull_fill((const uint2*)w->d_boxes.p, n_ops, w->TX, w->TY, w->TZ, (const uint32_t*)w->tile_off.p,
-                   (uint32_t*)w->tile_ops.p, s);
+                   (uint32_t*)w->tile_ops.p, (uint2*)w->tile_boxes.p, s);
   FoldArgs fa{};
   fa.chunk_op = (const uint32_t*)w->chunk_op.p;
   fa.n_ops = (uint32_t)n_ops;
@@ -1036,6 +1036,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   fa.tile_off = (const uint32_t*)w->tile_off.p;
   fa.tile_cnt = (const uint32_t*)w->tile_cnt.p;
   fa.tile_ops = (const uint32_t*)w->tile_ops.p;
+  fa.tile_boxes = (const uint2*)w->tile_boxes.p;
   fa.tiles_nonempty = (const uint32_t*)w->tiles_nonempty.p;
   fa.BX = w->BX; fa.BY = w->BY; fa.BZ = w->BZ; fa.TX = w->TX; fa.TY = w->TY;
   fa.vs = w->vs;

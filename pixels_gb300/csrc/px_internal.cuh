@@ -167,6 +167,7 @@ struct FoldArgs {
   const uint32_t* tile_off;
   const uint32_t* tile_cnt;
   const uint32_t* tile_ops;
+  const uint2* tile_boxes;    // the brick box of each tile_ops entry (packed like the op boxes)
   const uint32_t* tiles_nonempty;
   int BX, BY, BZ, TX, TY;
   double vs;
@@ -191,7 +192,7 @@ constexpr uint32_t TAG_STAGED = 0x40000000u;
 void launch_cull_count(const uint2* boxes, int n_ops, int TX, int TY, int TZ, uint32_t* tile_cnt,
                        uint32_t* tiles_nonempty, BuildResult* res, cudaStream_t s);
 void launch_cull_fill(const uint2* boxes, int n_ops, int TX, int TY, int TZ, const uint32_t* tile_off,
-                      uint32_t* tile_ops, cudaStream_t s);
+                      uint32_t* tile_ops, uint2* tile_boxes, cudaStream_t s);
 // max_blocks > 0 caps the persistent grids (builds sharing the GPU)
 void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEvent_t mid, int max_blocks);
 
