@@ -869,6 +869,32 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
 
           // write voxels (shapes.ts:395-405)
           bool changed = false;
+          if (constPaint || kind == KIND_CARVE) {
+            // one value for every covered voxel (carve: air; a const paint is a u16, so the
+            // unstored value equals the stored one): whole voxel pairs at a time.  Bit 2j + h
+            // of lb is voxel (x0 + h, y, j) of this lane.
+            const int base = (lx0 & 3) | ((ly & 3) << 2);
+            const int s0 = (lx0 >> 2) | ((ly >> 2) << 1);
+            const unsigned long long m0 = smask[wib][s0], m1 = smask[wib][s0 + 4];
+            uint32_t lb = 0;
+  #pragma unroll
+            for (int jj = 0; jj < 4; jj++) {
+              lb |= (uint32_t)((m0 >> (base + 16 * jj)) & 3ull) << (2 * jj);
+              lb |= (uint32_t)((m1 >> (base + 16 * jj)) & 3ull) << (2 * jj + 8);
+            }
+            const uint32_t v = kind == KIND_CARVE ? 0u : pv;
+            const uint32_t vv = v | (v << 16);
+  #pragma unroll
+            for (int j = 0; j < 8; j++) {
+              const uint32_t two = (lb >> (2 * j)) & 3u;
+              uint32_t keep = ((two & 1u) ? 0xffffu : 0u) | ((two & 2u) ? 0xffff0000u : 0u);
+              if (kind == KIND_PAINT)  // Paint recolours non-air voxels only
+                keep &= ((vox[j] & 0xffffu) ? 0xffffu : 0u) | ((vox[j] & 0xffff0000u) ? 0xffff0000u : 0u);
+              const uint32_t nv = (vox[j] & ~keep) | (vv & keep);
+              changed = changed || nv != vox[j];
+              vox[j] = nv;
+            }
+          } else {
   #pragma unroll
           for (int j = 0; j < 8; j++) {
             const int s = (lx0 >> 2) | ((ly >> 2) << 1) | ((j >> 2) << 2);
@@ -903,6 +929,7 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
                 changed = true;
               }
             }
+          }
           }
           __syncwarp();
           if (!__any_sync(FULLMASK, changed)) continue;
