@@ -389,17 +389,41 @@ def main():
         timed_builds.cls = statistics.mean(cls_ms)
         return ms, fold_ms
 
+    def graph_builds(mode, steps, warmup):
+        """The same build relaunched as the world's captured CUDA graph (px_batch of one
+        world): all of a build's launches submitted at once; device time per launch."""
+        b = _lib.batch_create([h], mode, 1, 0)
+        try:
+            for _ in range(warmup):
+                _lib.batch_run(b, s_ptr)
+            barrier()
+            torch.cuda.synchronize()
+            ms = []
+            for i in range(steps):
+                flush.fill_(i & 0xFF)                  # L2 flush between timed iterations
+                ms.append(_lib.batch_run(b, s_ptr))
+            torch.cuda.synchronize()
+            barrier()
+        finally:
+            _lib.batch_destroy(b)
+        return ms
+
     sampler = ClockSampler(local) if rank == 0 else None
     if sampler:
         sampler.start()
     ms64 = fold64 = ms_mx = fold_mx = None
     cls64 = cls_mx = None
+    stream_ms = {}
     if args.mode in ("both", "fp64"):
-        ms64, fold64 = timed_builds(MODE_FP64, args.steps, args.warmup)
+        s64, fold64 = timed_builds(MODE_FP64, args.steps, args.warmup)
         cls64 = timed_builds.cls
+        ms64 = graph_builds(MODE_FP64, args.steps, args.warmup)
+        stream_ms["fp64"] = statistics.mean(s64)
     if args.mode in ("both", "mixed"):
-        ms_mx, fold_mx = timed_builds(MODE_MIXED, args.steps, args.warmup)
+        smx, fold_mx = timed_builds(MODE_MIXED, args.steps, args.warmup)
         cls_mx = timed_builds.cls
+        ms_mx = graph_builds(MODE_MIXED, args.steps, args.warmup)
+        stream_ms["mixed"] = statistics.mean(smx)
     have64 = ms64 is not None
     if ms_mx is None:
         ms_mx, fold_mx = ms64, fold64
@@ -493,7 +517,11 @@ def main():
                    "cells": cells, "ops": len(prog), "l2": "flushed between timed steps (256 MB write)",
                    "parallelism": f"replicas x{world}"},
         "fp64_form": ({"value": round(value64, 4), "ms_per_step": round(t_64, 4),
+                       "stream_ms_per_step": round(stream_ms["fp64"], 4),
                        "fold_ms": round(fold64_s * 1e3, 4), "classify_ms": cls64} if have64 else None),
+        "stream_ms_per_step": round(stream_ms["mixed"], 4) if "mixed" in stream_ms else None,
+        "timing": "device time per build: the world's build graph relaunched (px_batch_run of one world); "
+                  "stream_ms_per_step: the same build launched kernel by kernel (px_build_enqueue)",
         "classify_ms": cls_mx,
         "speedup_mixed_vs_fp64": round(t_64 / t_mx, 3) if have64 else None,
         "mismatches": {"grid_cells": mism_grid, "pool_voxels": mism_vox, "pool_used": int(used) - int(o.pool_used)},
