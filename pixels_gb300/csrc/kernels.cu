@@ -194,7 +194,7 @@ __device__ __noinline__ double sdf64_at(const uint2* __restrict__ code, int clen
 template <int MODE>
 __device__ __forceinline__ int eval_decide(const FoldArgs& a, const OpDev* O, const uint2* code, int clen, bool use32,
                                            const Iv* bo, float kx, float ky, float kz, float tx, float ty, float tz,
-                                           int what, LaneStats& ls, bool count = true) {
+                                           int what, LaneStats& ls, bool count = true, Iv* dout = nullptr) {
   const int base = what == 1 ? T_BSK_HI : T_SSK_HI;
   if (MODE == 1 && use32) {
     bool amb = false;
@@ -204,8 +204,13 @@ __device__ __forceinline__ int eval_decide(const FoldArgs& a, const OpDev* O, co
     int r;
     if (what == 0) r = amb ? 3 : (d.lo > O->thr[T_V_HI] ? 0 : (d.hi <= O->thr[T_V_LO] ? 1 : 3));
     else r = amb ? 3 : classify32(d, O->thr, base);
+    if (dout) *dout = d;
     if (r != 3 && !a.validate) return r;
     double d64 = sdf64_at(code, clen, a.params, a.vs, tx, ty, tz);
+    if (dout && (amb || r == 3)) {  // the exact value lies within M of the float64 one
+      const double M64 = MIXED_MARGIN;
+      *dout = {__double2float_rd(d64 - M64), __double2float_ru(d64 + M64)};
+    }
     const double M = MIXED_MARGIN;
     if (a.validate && !amb && !((double)d.lo - M <= d64 && d64 <= (double)d.hi + M) && count) ls.viol++;
     if (r == 3 && count) {
@@ -425,6 +430,7 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
     unsigned long long pp = 0;
     int pbx = 0, pby = 0, pbz = 0, scls = PC_SKIP;
     bool boxr = false;
+    Iv dc = {-INFINITY, INFINITY};  // enclosure of the sub-block centre's value (mixed form)
     if (have) {
       const uint2 item = __ldg(a.pitems + a.pq_base[my_k] + (it - my_first));
       oo = item.x;
@@ -438,7 +444,8 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
       const int sxb = s & 1, syb = (s >> 1) & 1, szb = (s >> 2) & 1;
       scls = eval_decide<MODE>(a, Q, a.code + Q->code_off, (int)Q->code_len, use32, bo, 4.f * sxb + 1.5f,
                                4.f * syb + 1.5f, 4.f * szb + 1.5f, (float)(pbx * 8 + sxb * 4 + 2),
-                               (float)(pby * 8 + syb * 4 + 2), (float)(pbz * 8 + szb * 4 + 2), 2, ls);
+                               (float)(pby * 8 + syb * 4 + 2), (float)(pbz * 8 + szb * 4 + 2), 2, ls, true,
+                               MODE == 1 && use32 ? &dc : nullptr);
     }
     uint32_t code16 = (uint32_t)scls << (2 * s);
     code16 |= __shfl_xor_sync(FULLMASK, code16, 1);
@@ -458,7 +465,17 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
       const uint32_t at = pb + __popc(qm & ((1u << lane) - 1u));
       if (paint && at < a.paint_items_cap) a.paint_items[at] = make_uint2(oo, (uint32_t)(pp << 3) | (uint32_t)s);
     }
-    const bool push = have && scls == PC_PARTIAL && !boxr;
+    // mixed form: a partial sub-block whose centre value is farther from 0 than
+    // every voxel's distance bound (Lipschitz) has all its voxels decided
+    bool lipd = false;
+    if (MODE == 1 && have && scls == PC_PARTIAL && !boxr && !a.validate) {
+      const float l3 = a.ops[oo].lip[3];
+      if (dc.lo > l3 || dc.hi < -l3) {
+        a.pmask[pp * 8 + s] = dc.lo > l3 ? 0ull : ~0ull;
+        lipd = true;
+      }
+    }
+    const bool push = have && scls == PC_PARTIAL && !boxr && !lipd;
     const uint32_t vm = __ballot_sync(FULLMASK, push);
     if (push) {  // one append per shape class present among the pushing lanes
       const uint32_t k = a.ops[oo].vclass & (VCLASSES - 1);
@@ -468,7 +485,9 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
       if (lane == leader) vb = atomicAdd(&a.vitem_counter[1 + k], (uint32_t)__popc(grp));
       vb = __shfl_sync(grp, vb, leader);
       const uint32_t slot = vb + __popc(grp & ((1u << lane) - 1u));
-      if (slot < a.vq_cap[k]) a.vitems[a.vq_base[k] + slot] = make_uint2(oo, (uint32_t)(pp << 3) | (uint32_t)s);
+      if (slot < a.vq_cap[k])
+        a.vitems[a.vq_base[k] + slot] =
+            make_uint4(oo, (uint32_t)(pp << 3) | (uint32_t)s, __float_as_uint(dc.lo), __float_as_uint(dc.hi));
       else st_local |= ST_STAGE_OVERFLOW;
     }
   }
@@ -493,6 +512,15 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
   }
 }
 
+// Mixed form: a voxel's decision from its sub-block centre's value dc, when the
+// SDF's Lipschitz bound settles it (0 outside, 1 inside, 3 undecided); (ox, oy,
+// oz) is the voxel's offset in the sub-block, 0..3 per axis.
+__device__ __forceinline__ int lip_decide(const OpDev* O, Iv dc, int ox, int oy, int oz) {
+  const int k = (ox == 0 || ox == 3) + (oy == 0 || oy == 3) + (oz == 0 || oz == 3);  // axes at 1.5 voxels
+  const float t = O->lip[k];
+  return dc.lo > t ? 0 : (dc.hi < -t ? 1 : 3);
+}
+
 // Voxel inside-masks of the queued partial sub-blocks: one sub-block per warp
 // pass, 64 voxel SDFs on 32 lanes, two ballots (shapes.ts:390-394).
 template <int MODE>
@@ -514,7 +542,8 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_VOXEL_MINB : PX_CLASSIFY64
     if (it >= n_items) break;
     const int k = __popc(__ballot_sync(FULLMASK, lane < VCLASSES && incl <= it));  // class of item `it`
     const uint32_t first = __shfl_sync(FULLMASK, incl - own, k);
-    const uint2 item = __ldg(a.vitems + a.vq_base[k] + (it - first));
+    const uint4 item = __ldg(a.vitems + a.vq_base[k] + (it - first));
+    const Iv dcen = {__uint_as_float(item.z), __uint_as_float(item.w)};  // the sub-block centre's value
     const OpDev* V = a.ops + item.x;
     const unsigned long long vp = item.y >> 3;
     const int ss = item.y & 7;
@@ -534,25 +563,32 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_VOXEL_MINB : PX_CLASSIFY64
       bool amb = false;
       const Iv X = iadd(bo[0], koff((float)lx, a.vs_lo, a.vs_hi)), Z = iadd(bo[2], koff((float)lz, a.vs_lo, a.vs_hi));
       const Iv Y0 = iadd(bo[1], koff((float)ly0, a.vs_lo, a.vs_hi)), Y1 = iadd(bo[1], koff((float)(ly0 + 1), a.vs_lo, a.vs_hi));
-      const Iv2 d = sdf32i_y2(code, a.code32 + V->code_off, clen, reinterpret_cast<const Iv*>(a.p32), X, Y0, Y1, Z,
-                              V->thr[T_M], amb);
+      const int lip0 = lip_decide(V, dcen, col & 3, 2 * yh, col >> 2), lip1 = lip_decide(V, dcen, col & 3, 2 * yh + 1, col >> 2);
+      Iv2 d = {{0.f, 0.f}, {0.f, 0.f}};
+      if (lip0 == 3 || lip1 == 3 || a.validate)
+        d = sdf32i_y2(code, a.code32 + V->code_off, clen, reinterpret_cast<const Iv*>(a.p32), X, Y0, Y1, Z, V->thr[T_M], amb);
       uint32_t lo = 0, hi = 0;
 #pragma unroll
       for (int k = 0; k < 2; k++) {
         const Iv dk = k ? d.b : d.a;
-        int inside = amb ? 3 : (dk.lo > V->thr[T_V_HI] ? 0 : (dk.hi <= V->thr[T_V_LO] ? 1 : 3));
-        if (inside == 3 || a.validate) {
-          const VoxelF64 f = voxel_f64(a.params, a.vs, a.validate, code, clen, dk, amb, inside,
-                                       (float)(vbx * 8 + lx) + 0.5f, (float)(vby * 8 + ly0 + k) + 0.5f,
-                                       (float)(vbz * 8 + lz) + 0.5f);
-          ls.viol += f.viol;
-          if (inside == 3) {
-            ls.resc++;
-            ls.rv++;
-            if (amb) ls.rp++;
-            ls.max_err = fmaxf(ls.max_err, f.err);
+        const int lipk = k ? lip1 : lip0;
+        int inside = lipk;
+        if (lipk == 3 || a.validate) {
+          inside = amb ? 3 : (dk.lo > V->thr[T_V_HI] ? 0 : (dk.hi <= V->thr[T_V_LO] ? 1 : 3));
+          if (inside == 3 || a.validate) {
+            const VoxelF64 f = voxel_f64(a.params, a.vs, a.validate, code, clen, dk, amb, inside,
+                                         (float)(vbx * 8 + lx) + 0.5f, (float)(vby * 8 + ly0 + k) + 0.5f,
+                                         (float)(vbz * 8 + lz) + 0.5f);
+            ls.viol += f.viol;
+            if (inside == 3) {
+              ls.resc++;
+              ls.rv++;
+              if (amb) ls.rp++;
+              ls.max_err = fmaxf(ls.max_err, f.err);
+            }
+            inside = f.inside;
           }
-          inside = f.inside;
+          if (lipk != 3 && inside != lipk) ls.viol++;  // validation: the bound disagreed with the evaluation
         }
         const int bit = (col & 3) | ((2 * yh + k) << 2) | ((col >> 2) << 4);  // voxel index in the sub-block
         if (inside == 1) {
@@ -567,9 +603,14 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_VOXEL_MINB : PX_CLASSIFY64
       for (int r = 0; r < 2; r++) {
         const int e = r * 32 + lane;
         const int lx = sxo + (e & 3), lyv = syo + ((e >> 2) & 3), lz = szo + (e >> 4);
-        int inside = eval_decide<MODE>(a, V, code, clen, use32, bo, (float)lx, (float)lyv, (float)lz,
-                                       (float)(vbx * 8 + lx) + 0.5f, (float)(vby * 8 + lyv) + 0.5f,
-                                       (float)(vbz * 8 + lz) + 0.5f, 0, ls);
+        const int lipd = MODE == 1 && use32 ? lip_decide(V, dcen, e & 3, (e >> 2) & 3, e >> 4) : 3;
+        int inside = lipd;
+        if (lipd == 3 || a.validate) {
+          inside = eval_decide<MODE>(a, V, code, clen, use32, bo, (float)lx, (float)lyv, (float)lz,
+                                     (float)(vbx * 8 + lx) + 0.5f, (float)(vby * 8 + lyv) + 0.5f,
+                                     (float)(vbz * 8 + lz) + 0.5f, 0, ls);
+          if (lipd != 3 && inside != lipd) ls.viol++;  // validation: the bound disagreed with the evaluation
+        }
         bal[r] = __ballot_sync(FULLMASK, inside == 1);
       }
       m = (unsigned long long)bal[0] | ((unsigned long long)bal[1] << 32);

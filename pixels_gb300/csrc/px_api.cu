@@ -647,6 +647,14 @@ int convert_ops(const px_world* w, const IrOp* iops, size_t i0, size_t i1, const
       d.thr[T_SFU_HI] = rd32(-d.shd - M); d.thr[T_SFU_LO] = ru32(-d.shd + M);
       d.thr[T_V_HI] = ru32(M); d.thr[T_V_LO] = rd32(-M);
       d.thr[T_M] = ru32(M);
+      // Lipschitz decisions of voxels from their sub-block centre's value: a voxel
+      // centre lies sqrt(n1 + 9 n3) / 2 voxels from the centre (n3 axes at offset
+      // 1.5, the others at 0.5), plus the float64 rounding of both points
+      {
+        const double L = std::max(1.0, o.slack) * (1 + 0x1p-40);
+        const double dist[4] = {std::sqrt(3.0) / 2, std::sqrt(11.0) / 2, std::sqrt(19.0) / 2, std::sqrt(27.0) / 2};
+        for (int k = 0; k < 4; k++) d.lip[k] = ru32(L * (dist[k] * vs + 0x1p-40) + M);
+      }
       // (b*8 + 0.5)*vs - anchor per brick row, padded for the float64 rounding of the
       // reference's voxel centres ((x + 0.5)*vs, |x*vs| <= 2^10 m)
       d.base_off = (uint32_t)out.bases.size();  // + the chunk's base offset (merge)
@@ -906,7 +914,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
       (rc = ensure(w, w->work_counter, 16)) || (rc = ensure(w, w->res, sizeof(BuildResult))) ||
       (rc = ensure(w, w->chunk_op, 4 * ((P + 31) / 32))) || (rc = ensure(w, w->pcode, P)) ||
       (rc = ensure(w, w->psub, 2 * P)) || (rc = ensure(w, w->pmask, 64 * P)) || (rc = ensure(w, w->chunk_counter, 512)) || (rc = ensure(w, w->pitems, 8 * P)) ||
-      (rc = ensure(w, w->vitems, 8 * 8 * P)) || (rc = ensure(w, w->paint_items, 8 * 8 * n_slots + 8)) ||
+      (rc = ensure(w, w->vitems, 16 * 8 * P)) || (rc = ensure(w, w->paint_items, 8 * 8 * n_slots + 8)) ||
       (rc = ensure(w, w->pvals, 2048 * n_slots + 4)) || (rc = ensure(w, w->bmark, 4 * ((w->ncells + 31) / 32))) ||
       (rc = ensure(w, w->work, 4 * touched_bound + 4)))
     return rc;
@@ -993,7 +1001,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   fa.psub = (uint16_t*)w->psub.p;
   fa.pmask = (unsigned long long*)w->pmask.p;
   fa.chunk_counter = (uint32_t*)w->chunk_counter.p;
-  fa.vitems = (uint2*)w->vitems.p;
+  fa.vitems = (uint4*)w->vitems.p;
   fa.vitems_cap = (uint32_t)(8 * P < 0xffffffffull ? 8 * P : 0xffffffffull);
   fa.vitem_counter = (uint32_t*)w->chunk_counter.p + 4;   // counters: [0] chunks, [1] paint taken,
                                                           // [2] paint pushed, [4..36] voxel, [40..72] pairs

@@ -88,6 +88,10 @@ struct OpDev {
   uint32_t paint_slot;
   // mixed mode: float32 parameters of the certified paint evaluation (p32 index), or NO_SLOT
   uint32_t paint32_off;
+  // mixed mode: a voxel of a partial sub-block is outside if the sub-block centre's
+  // value exceeds lip[k], inside if it is below -lip[k] (k: the voxel's distance class
+  // from the centre; every shape's SDF is Lipschitz with constant <= its slack)
+  float lip[4];
 };
 constexpr uint32_t NO_SLOT = 0xffffffffu;
 // paint kinds whose calls are the most expensive (transcendentals, Math.hypot):
@@ -140,7 +144,8 @@ struct FoldArgs {
   uint16_t* psub;             // per partial pair: 2 bits per sub-block (PC_*)
   unsigned long long* pmask;  // per partial pair: 8 inside-masks (bit = x&3 | (y&3)<<2 | (z&3)<<4)
   uint32_t* chunk_counter;
-  uint2* vitems;              // partial sub-blocks to classify voxel by voxel: (op, pair << 3 | sub)
+  uint4* vitems;              // partial sub-blocks to classify voxel by voxel: (op, pair << 3 | sub,
+                              // bits of the centre value's enclosure lo, hi)
   uint32_t vitems_cap;
   uint32_t* vitem_counter;    // [0] items taken, [1 + k] items pushed to class k
   uint32_t vq_base[VCLASSES], vq_cap[VCLASSES];  // per-class regions of vitems
