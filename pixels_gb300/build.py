@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-fmad=false", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-Xptxas", "-warn-spills"]
 UNITS = ["kernels.cu", "px_api.cu", "px_serve.cu", "px_noalloc.cu", "px_lights.cu"]
-HEADERS = ["px_internal.cuh", "sdf64.cuh", "sdf32.cuh", "paint.cuh", "jsmath.cuh", "jsmath_tables.h"]
+HEADERS = ["px_internal.cuh", "sdf64.cuh", "sdf32.cuh", "paint.cuh", "paint32.cuh", "jsmath.cuh", "jsmath_tables.h"]
 
 
 def _nvcc() -> str:

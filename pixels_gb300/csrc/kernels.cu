@@ -737,9 +737,10 @@ __global__ void __launch_bounds__(256) paint_kernel(FoldArgs a) {
 // The warp applies its brick's ops in order, as apply() does (shapes.ts:367-412),
 // using the pair classifications.
 // The bricks the apply pass visits: those with a marked bit (one warp per 32
-// words of the bitmap, a warp-aggregated append).
+// words of the bitmap, a warp-aggregated append), listed as packed brick
+// coordinates bx | by << 10 | bz << 20.
 __global__ void __launch_bounds__(256) mark_compact_kernel(const uint32_t* __restrict__ bmark, uint32_t n_words,
-                                                           uint32_t* work, BuildResult* res) {
+                                                           uint32_t BX, uint32_t BY, uint32_t* work, BuildResult* res) {
   const int lane = threadIdx.x & 31;
   const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t w0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; w0 < n_words; w0 += warps * 32) {
@@ -760,202 +761,198 @@ __global__ void __launch_bounds__(256) mark_compact_kernel(const uint32_t* __res
     while (b) {
       const int k = __ffs(b) - 1;
       b &= b - 1;
-      work[base++] = wi * 32u + (uint32_t)k;
+      const uint32_t ci = wi * 32u + (uint32_t)k, byz = ci / BX;
+      work[base++] = (ci - byz * BX) | ((byz % BY) << 10) | ((byz / BY) << 20);
     }
   }
 }
 
+// One tile-list entry of a brick, looked up for the apply loop: the op, its
+// (op, brick) pair and that pair's classes, and the op fields the loop needs.
+struct FoldEntry {
+  unsigned long long pr;
+  uint32_t oi, meta, pval, pslot, sc;
+  int cls;
+};
+
+__device__ __forceinline__ FoldEntry fold_entry(const FoldArgs& a, uint32_t idx, int bx, int by, int bz) {
+  FoldEntry f = {0ull, 0u, 0u, 0u, NO_SLOT, 0u, PC_SKIP};
+  f.oi = __ldg(a.tile_ops + idx);
+  const uint2 bb = __ldg(a.tile_boxes + idx);  // the op's brick box
+  const int x0 = bb.x & 1023, y0 = (bb.x >> 10) & 1023, z0 = (bb.x >> 20) & 1023;
+  const int x1 = bb.y & 1023, y1 = (bb.y >> 10) & 1023, z1 = (bb.y >> 20) & 1023;
+  if (bx >= x0 && bx <= x1 && by >= y0 && by <= y1 && bz >= z0 && bz <= z1) {
+    const OpDev* o = a.ops + f.oi;
+    f.pr = o->pair_base + (unsigned long long)(((bz - z0) * (y1 - y0 + 1) + (by - y0)) * (x1 - x0 + 1) + (bx - x0));
+    f.cls = __ldg(a.pcode + f.pr);
+    f.sc = __ldg(a.psub + f.pr);  // meaningful for partial pairs only
+    f.meta = (uint32_t)o->kind | ((uint32_t)o->flags << 8) | ((uint32_t)o->paint_kind << 16);
+    f.pval = o->paint_value;
+    f.pslot = o->paint_slot == NO_SLOT ? NO_SLOT : o->paint_slot + (uint32_t)(f.pr - o->pair_base);
+  }
+  return f;
+}
+
 // INLINE: some painted op has no paint slot (paint values past the slot
 // budget), so paint calls happen here too; otherwise the apply loop calls nothing.
+// A warp takes four bricks at a time; lanes 8j..8j+7 look up the first eight
+// tile-list entries of brick j together (all four bricks' lookups in flight at
+// once), then the bricks are applied one after the other.
 template <bool INLINE>
 __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
   __shared__ unsigned long long smask[8][8];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const int lx0 = (lane & 3) * 2, ly = lane >> 2;
+  const uint32_t grp = (uint32_t)lane >> 3, ent = (uint32_t)lane & 7u;
   WarpCounters wc = {0, 0, 0, 0, 0};
   uint32_t paint_calls = 0, paint_viol = 0;
   uint32_t st_local = 0;
   const uint32_t n_work = __ldg(&a.res->n_work);
 
-  // bricks are taken four at a time; the grid entry and tile list of the next
-  // brick are loaded while the current one is applied
   for (;;) {
     uint32_t wbase = 0;
     if (lane == 0) wbase = atomicAdd(a.work_counter, 4u);
     wbase = __shfl_sync(FULLMASK, wbase, 0);
     if (wbase >= n_work) break;
     const uint32_t n_here = min(4u, n_work - wbase);
-    const uint32_t my_ci = lane < (int)n_here ? __ldg(a.work + wbase + lane) : 0u;
-    uint32_t nci = __shfl_sync(FULLMASK, my_ci, 0);
-    uint32_t ng = a.grid[nci];
-    uint32_t ntile = 0, ntoff = 0, ntcnt = 0;
-    {
-      const int bx = (int)(nci % (uint32_t)a.BX), byz = (int)(nci / (uint32_t)a.BX), by = byz % a.BY, bz = byz / a.BY;
-      ntile = (uint32_t)((bx >> 2) + a.TX * ((by >> 2) + a.TY * (bz >> 2)));
-      ntoff = __ldg(a.tile_off + ntile);
-      ntcnt = __ldg(a.tile_cnt + ntile);
+    uint32_t q_pk = 0, q_g = 0, q_toff = 0, q_tcnt = 0;
+    FoldEntry q = {0ull, 0u, 0u, 0u, NO_SLOT, 0u, PC_SKIP};
+    if (grp < n_here) {
+      q_pk = __ldg(a.work + wbase + grp);
+      const uint32_t bx = q_pk & 1023u, by = (q_pk >> 10) & 1023u, bz = q_pk >> 20;
+      q_g = a.grid[bx + (uint32_t)a.BX * (by + (uint32_t)a.BY * bz)];
+      const uint32_t tile = (bx >> 2) + (uint32_t)a.TX * ((by >> 2) + (uint32_t)a.TY * (bz >> 2));
+      q_toff = __ldg(a.tile_off + tile);
+      q_tcnt = __ldg(a.tile_cnt + tile);
+      if (ent < q_tcnt) q = fold_entry(a, q_toff + ent, (int)bx, (int)by, (int)bz);
     }
+    const uint32_t m_all = __ballot_sync(FULLMASK, q.cls != PC_SKIP);  // shapes.ts:364 skips the rest
+
     for (uint32_t j = 0; j < n_here; j++) {
-      const size_t ci = nci;
-      const uint32_t g = ng, toff = ntoff, tcnt = ntcnt;
-      if (j + 1 < n_here) {  // prefetch the next brick
-        nci = __shfl_sync(FULLMASK, my_ci, j + 1);
-        ng = a.grid[nci];
-        const int bx = (int)(nci % (uint32_t)a.BX), byz = (int)(nci / (uint32_t)a.BX), by = byz % a.BY, bz = byz / a.BY;
-        ntile = (uint32_t)((bx >> 2) + a.TX * ((by >> 2) + a.TY * (bz >> 2)));
-        ntoff = __ldg(a.tile_off + ntile);
-        ntcnt = __ldg(a.tile_cnt + ntile);
-      }
-      const int bx = (int)(ci % (size_t)a.BX), byz = (int)(ci / (size_t)a.BX), by = byz % a.BY, bz = byz / a.BY;
+      const uint32_t pk = __shfl_sync(FULLMASK, q_pk, 8 * j);
+      const uint32_t g = __shfl_sync(FULLMASK, q_g, 8 * j);
+      const uint32_t toff = __shfl_sync(FULLMASK, q_toff, 8 * j), tcnt = __shfl_sync(FULLMASK, q_tcnt, 8 * j);
+      const int bx = (int)(pk & 1023u), by = (int)((pk >> 10) & 1023u), bz = (int)(pk >> 20);
+      const uint32_t ci = (uint32_t)bx + (uint32_t)a.BX * ((uint32_t)by + (uint32_t)a.BY * (uint32_t)bz);
       const int ox = bx * 8, oy = by * 8, oz = bz * 8;
 
-      // current brick contents (VoxelWorld.ts:55-61); every listed brick has an op
-      // that applies, so they are loaded up front, overlapping the op lookups
+      // current brick contents (VoxelWorld.ts:55-61)
       int state = ST_EMPTY;
       uint32_t uval = 0;
       uint32_t vox[8];
       long long src = -1;  // pool identity: >= 0 pair of the last alloc, < 0 -(old index + 1)
       bool dirty = false;
-      {
-        if (g == 0) {
-  #pragma unroll
-          for (int j = 0; j < 8; j++) vox[j] = 0;
-        } else if (g & UNIFORM) {
-          state = ST_UNIF; uval = g & 0xffffu;
-  #pragma unroll
-          for (int j = 0; j < 8; j++) vox[j] = uval | (uval << 16);
-        } else {
-          state = ST_MIXED; src = -(long long)(g - 1) - 1;
-          const uint32_t* pb = a.pool32 + (size_t)(g - 1) * 256;
-  #pragma unroll
-          for (int j = 0; j < 8; j++) vox[j] = pb[32 * j + lane];
-        }
+      if (g == 0) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) vox[k] = 0;
+      } else if (g & UNIFORM) {
+        state = ST_UNIF; uval = g & 0xffffu;
+#pragma unroll
+        for (int k = 0; k < 8; k++) vox[k] = uval | (uval << 16);
+      } else {
+        state = ST_MIXED; src = -(long long)(g - 1) - 1;
+        const uint32_t* pb = a.pool32 + (size_t)(g - 1) * 256;
+#pragma unroll
+        for (int k = 0; k < 8; k++) vox[k] = pb[32 * k + lane];
       }
 
-      for (uint32_t c0 = 0; c0 < tcnt; c0 += 32) {
-        // each lane looks up one op of the tile: does it cover the brick, the
-        // pair's classes, and the op fields the apply loop needs (all loads in parallel)
-        uint32_t oi = 0, meta = 0, pval = 0, pslot = NO_SLOT, sc = 0;
-        unsigned long long pr = 0;
-        int ocls = PC_SKIP;
-        if (c0 + lane < tcnt) {
-          oi = __ldg(a.tile_ops + toff + c0 + lane);
-          const uint2 bb = __ldg(a.tile_boxes + toff + c0 + lane);  // the op's brick box
-          const int x0 = bb.x & 1023, y0 = (bb.x >> 10) & 1023, z0 = (bb.x >> 20) & 1023;
-          const int x1 = bb.y & 1023, y1 = (bb.y >> 10) & 1023, z1 = (bb.y >> 20) & 1023;
-          if (bx >= x0 && bx <= x1 && by >= y0 && by <= y1 && bz >= z0 && bz <= z1) {
-            const OpDev* o = a.ops + oi;
-            pr = o->pair_base + (unsigned long long)(((bz - z0) * (y1 - y0 + 1) + (by - y0)) * (x1 - x0 + 1) + (bx - x0));
-            ocls = __ldg(a.pcode + pr);
-            sc = __ldg(a.psub + pr);  // meaningful for partial pairs only
-            meta = (uint32_t)o->kind | ((uint32_t)o->flags << 8) | ((uint32_t)o->paint_kind << 16);
-            pval = o->paint_value;
-            pslot = o->paint_slot == NO_SLOT ? NO_SLOT : o->paint_slot + (uint32_t)(pr - o->pair_base);
-          }
+      // apply the op whose entry lane `b` holds
+      auto apply = [&](const FoldEntry& f, int b) {
+        const unsigned long long pair = __shfl_sync(FULLMASK, f.pr, b);
+        const int cls = __shfl_sync(FULLMASK, f.cls, b);
+        const uint32_t mt = __shfl_sync(FULLMASK, f.meta, b);
+        const uint32_t pv = __shfl_sync(FULLMASK, f.pval, b);
+        const uint32_t slot = __shfl_sync(FULLMASK, f.pslot, b);
+        const uint32_t o_idx = __shfl_sync(FULLMASK, f.oi, b);
+        const uint32_t psc = __shfl_sync(FULLMASK, f.sc, b);
+        const bool full = cls == PC_FULL;
+        const int kind = (int)(mt & 0xffu);
+        const uint32_t pk_ = mt >> 16;
+        const bool constPaint = pk_ == PK_CONST;
+        // uniform shortcuts (shapes.ts:367-374)
+        int set_u = -1;
+        if (full) {
+          if (kind == KIND_ADD && constPaint) set_u = (int)pv;
+          else if (kind == KIND_CARVE) set_u = 0;
+          else if (kind == KIND_PAINT && state == ST_EMPTY) return;
+          else if (kind == KIND_PAINT && constPaint && state == ST_UNIF) set_u = (int)pv;
         }
-        uint32_t m = __ballot_sync(FULLMASK, ocls != PC_SKIP);  // shapes.ts:364 skips the rest
-        while (m) {
-          const int b = __ffs(m) - 1;
-          m &= m - 1;
-          const unsigned long long pair = __shfl_sync(FULLMASK, pr, b);
-          const int cls = __shfl_sync(FULLMASK, ocls, b);
-          const uint32_t mt = __shfl_sync(FULLMASK, meta, b);
-          const uint32_t pv = __shfl_sync(FULLMASK, pval, b);
-          const uint32_t slot = __shfl_sync(FULLMASK, pslot, b);
-          const uint32_t o_idx = __shfl_sync(FULLMASK, oi, b);
-          const bool full = cls == PC_FULL;
-          const int kind = (int)(mt & 0xffu);
-          const uint32_t pk = mt >> 16;
-          const bool constPaint = pk == PK_CONST;
-          // uniform shortcuts (shapes.ts:367-374)
-          int set_u = -1;
-          if (full) {
-            if (kind == KIND_ADD && constPaint) set_u = (int)pv;
-            else if (kind == KIND_CARVE) set_u = 0;
-            else if (kind == KIND_PAINT && state == ST_EMPTY) continue;
-            else if (kind == KIND_PAINT && constPaint && state == ST_UNIF) set_u = (int)pv;
+        if (set_u >= 0) {  // setBrickUniform (VoxelWorld.ts:89-97)
+          if (state == ST_MIXED) {
+            if (lane == 0) { a.evt[pair] = 2; a.fsrc[pair] = src; }
+            wc.free_++;
           }
-          if (set_u >= 0) {  // setBrickUniform (VoxelWorld.ts:89-97)
-            if (state == ST_MIXED) {
-              if (lane == 0) { a.evt[pair] = 2; a.fsrc[pair] = src; }
-              wc.free_++;
-            }
-            uint32_t v = (uint32_t)set_u;
-            state = v == 0 ? ST_EMPTY : ST_UNIF;
-            uval = v; src = -1;
-  #pragma unroll
-            for (int j = 0; j < 8; j++) vox[j] = v | (v << 16);
-            dirty = true;
-            continue;
-          }
-          if (kind == KIND_PAINT && state == ST_EMPTY) continue;
+          const uint32_t v = (uint32_t)set_u;
+          state = v == 0 ? ST_EMPTY : ST_UNIF;
+          uval = v; src = -1;
+#pragma unroll
+          for (int k = 0; k < 8; k++) vox[k] = v | (v << 16);
+          dirty = true;
+          return;
+        }
+        if (kind == KIND_PAINT && state == ST_EMPTY) return;
 
-          // sub-block and voxel classes (shapes.ts:382-394), computed by classify_kernel
-          if (!full) {
-            const uint32_t psc = __shfl_sync(FULLMASK, sc, b);
-            if (lane < 8) {
-              const uint32_t c = (psc >> (2 * lane)) & 3u;
-              smask[wib][lane] = c == PC_FULL ? ~0ull : c == PC_PARTIAL ? __ldg(a.pmask + pair * 8 + lane) : 0ull;
-            }
-            wc.sub += 8;
-            uint32_t np_ = 0;
-  #pragma unroll
-            for (int s2 = 0; s2 < 8; s2++) np_ += ((psc >> (2 * s2)) & 3u) == PC_PARTIAL;
-            wc.vox += 64 * np_;
-          } else if (lane < 8) {
-            smask[wib][lane] = ~0ull;
+        // sub-block and voxel classes (shapes.ts:382-394), computed by classify_kernel
+        if (!full) {
+          if (lane < 8) {
+            const uint32_t c = (psc >> (2 * lane)) & 3u;
+            smask[wib][lane] = c == PC_FULL ? ~0ull : c == PC_PARTIAL ? __ldg(a.pmask + pair * 8 + lane) : 0ull;
           }
-          __syncwarp();
+          wc.sub += 8;
+          wc.vox += 64 * __popc(psc & ~(psc >> 1) & 0x5555u);  // sub-blocks of class PC_PARTIAL (01)
+        } else if (lane < 8) {
+          smask[wib][lane] = ~0ull;
+        }
+        __syncwarp();
 
-          // write voxels (shapes.ts:395-405)
-          bool changed = false;
-          if (constPaint || kind == KIND_CARVE) {
-            // one value for every covered voxel (carve: air; a const paint is a u16, so the
-            // unstored value equals the stored one): whole voxel pairs at a time.  Bit 2j + h
-            // of lb is voxel (x0 + h, y, j) of this lane.
-            const int base = (lx0 & 3) | ((ly & 3) << 2);
-            const int s0 = (lx0 >> 2) | ((ly >> 2) << 1);
-            const unsigned long long m0 = smask[wib][s0], m1 = smask[wib][s0 + 4];
-            uint32_t lb = 0;
-  #pragma unroll
-            for (int jj = 0; jj < 4; jj++) {
-              lb |= (uint32_t)((m0 >> (base + 16 * jj)) & 3ull) << (2 * jj);
-              lb |= (uint32_t)((m1 >> (base + 16 * jj)) & 3ull) << (2 * jj + 8);
-            }
-            const uint32_t v = kind == KIND_CARVE ? 0u : pv;
-            const uint32_t vv = v | (v << 16);
-  #pragma unroll
-            for (int j = 0; j < 8; j++) {
-              const uint32_t two = (lb >> (2 * j)) & 3u;
-              uint32_t keep = ((two & 1u) ? 0xffffu : 0u) | ((two & 2u) ? 0xffff0000u : 0u);
-              if (kind == KIND_PAINT)  // Paint recolours non-air voxels only
-                keep &= ((vox[j] & 0xffffu) ? 0xffffu : 0u) | ((vox[j] & 0xffff0000u) ? 0xffff0000u : 0u);
-              const uint32_t nv = (vox[j] & ~keep) | (vv & keep);
-              changed = changed || nv != vox[j];
-              vox[j] = nv;
-            }
-          } else {
-  #pragma unroll
-          for (int j = 0; j < 8; j++) {
-            const int s = (lx0 >> 2) | ((ly >> 2) << 1) | ((j >> 2) << 2);
-            const int e0 = (lx0 & 3) | ((ly & 3) << 2) | ((j & 3) << 4);
+        // write voxels (shapes.ts:395-405)
+        bool changed = false;
+        if (constPaint || kind == KIND_CARVE) {
+          // one value for every covered voxel (carve: air; a const paint is a u16, so the
+          // unstored value equals the stored one): whole voxel pairs at a time.  Bit 2j + h
+          // of lb is voxel (x0 + h, y, j) of this lane.
+          const int base = (lx0 & 3) | ((ly & 3) << 2);
+          const int s0 = (lx0 >> 2) | ((ly >> 2) << 1);
+          const unsigned long long m0 = smask[wib][s0], m1 = smask[wib][s0 + 4];
+          uint32_t lb = 0;
+#pragma unroll
+          for (int jj = 0; jj < 4; jj++) {
+            lb |= (uint32_t)((m0 >> (base + 16 * jj)) & 3ull) << (2 * jj);
+            lb |= (uint32_t)((m1 >> (base + 16 * jj)) & 3ull) << (2 * jj + 8);
+          }
+          const uint32_t v = kind == KIND_CARVE ? 0u : pv;
+          const uint32_t vv = v | (v << 16);
+#pragma unroll
+          for (int k = 0; k < 8; k++) {
+            const uint32_t two = (lb >> (2 * k)) & 3u;
+            uint32_t keep = ((two & 1u) ? 0xffffu : 0u) | ((two & 2u) ? 0xffff0000u : 0u);
+            if (kind == KIND_PAINT)  // Paint recolours non-air voxels only
+              keep &= ((vox[k] & 0xffffu) ? 0xffffu : 0u) | ((vox[k] & 0xffff0000u) ? 0xffff0000u : 0u);
+            const uint32_t nv = (vox[k] & ~keep) | (vv & keep);
+            changed = changed || nv != vox[k];
+            vox[k] = nv;
+          }
+        } else {
+#pragma unroll
+          for (int k = 0; k < 8; k++) {
+            const int s = (lx0 >> 2) | ((ly >> 2) << 1) | ((k >> 2) << 2);
+            const int e0 = (lx0 & 3) | ((ly & 3) << 2) | ((k & 3) << 4);
             const unsigned long long ms = smask[wib][s];
-  #pragma unroll
+#pragma unroll
             for (int h = 0; h < 2; h++) {
               if (!((ms >> (e0 + h)) & 1ull)) continue;
-              const uint32_t cur = (vox[j] >> (16 * h)) & 0xffffu;
+              const uint32_t cur = (vox[k] >> (16 * h)) & 0xffffu;
               uint32_t next;
-              if (kind == KIND_CARVE) next = 0;
-              else if (kind == KIND_PAINT && cur == 0) continue;
-              else if (!constPaint && slot != NO_SLOT) {  // evaluated by paint_kernel
-                const uint32_t pvv = __ldg(a.pvals + (size_t)slot * 512 + (uint32_t)((lx0 + h) | (ly << 3) | (j << 6)));
+              if (kind == KIND_PAINT && cur == 0) continue;
+              else if (slot != NO_SLOT) {  // evaluated by paint_kernel
+                const uint32_t pvv = __ldg(a.pvals + (size_t)slot * 512 + (uint32_t)((lx0 + h) | (ly << 3) | (k << 6)));
                 if (pvv & PV_RANGE) st_local |= ST_RANGE;
                 next = pvv & 0xffffu;
                 paint_calls++;
-              } else if (!constPaint) {
+              } else {
                 if constexpr (INLINE) {
-                  const uint32_t pv2 = paint_at_voxel(a.params, a.vs, a.validate, a.ops + o_idx, ox + lx0 + h, oy + ly, oz + j);
+                  const uint32_t pv2 = paint_at_voxel(a.params, a.vs, a.validate, a.ops + o_idx, ox + lx0 + h, oy + ly, oz + k);
                   if (pv2 & PV_RANGE) st_local |= ST_RANGE;
                   if (pv2 & PV_VIOL) paint_viol++;
                   next = pv2 & 0xffffu;
@@ -964,37 +961,45 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
                   st_local |= ST_CHAIN;
                   next = cur;
                 }
-              } else next = pv;
+              }
               if (next != cur) {  // Uint16Array store; the comparison uses the unstored value
-                vox[j] = (vox[j] & ~(0xffffu << (16 * h))) | ((next & 0xffffu) << (16 * h));
+                vox[k] = (vox[k] & ~(0xffffu << (16 * h))) | ((next & 0xffffu) << (16 * h));
                 changed = true;
               }
             }
           }
-          }
-          __syncwarp();
-          if (!__any_sync(FULLMASK, changed)) continue;
-          dirty = true;
-          uint8_t ev = 0;
-          if (state != ST_MIXED) {  // editableBrick -> allocBrick (VoxelWorld.ts:103-122)
-            ev = 1; src = (long long)pair; state = ST_MIXED;
-            wc.alloc++;
-          }
-          // compactCell (VoxelWorld.ts:147-156)
-          const uint32_t v0 = __shfl_sync(FULLMASK, vox[0] & 0xffffu, 0);
-          const uint32_t vv = v0 | (v0 << 16);
-          bool eq = true;
-  #pragma unroll
-          for (int j = 0; j < 8; j++) eq = eq && vox[j] == vv;
-          if (__all_sync(FULLMASK, eq)) {
-            if (lane == 0) a.fsrc[pair] = src;
-            ev |= 2;
-            wc.free_++;
-            state = v0 == 0 ? ST_EMPTY : ST_UNIF;
-            uval = v0; src = -1;
-          }
-          if (lane == 0) a.evt[pair] = ev;
         }
+        __syncwarp();
+        if (!__any_sync(FULLMASK, changed)) return;
+        dirty = true;
+        uint8_t ev = 0;
+        if (state != ST_MIXED) {  // editableBrick -> allocBrick (VoxelWorld.ts:103-122)
+          ev = 1; src = (long long)pair; state = ST_MIXED;
+          wc.alloc++;
+        }
+        // compactCell (VoxelWorld.ts:147-156)
+        const uint32_t v0 = __shfl_sync(FULLMASK, vox[0] & 0xffffu, 0);
+        const uint32_t vv = v0 | (v0 << 16);
+        bool eq = true;
+#pragma unroll
+        for (int k = 0; k < 8; k++) eq = eq && vox[k] == vv;
+        if (__all_sync(FULLMASK, eq)) {
+          if (lane == 0) a.fsrc[pair] = src;
+          ev |= 2;
+          wc.free_++;
+          state = v0 == 0 ? ST_EMPTY : ST_UNIF;
+          uval = v0; src = -1;
+        }
+        if (lane == 0) a.evt[pair] = ev;
+      };
+
+      // entries 0..7 of the tile list, looked up above by lanes 8j..8j+7
+      for (uint32_t m = (m_all >> (8 * j)) & 0xffu; m; m &= m - 1) apply(q, (int)(8 * j) + __ffs(m) - 1);
+      // the rest of a longer list, 32 entries per pass
+      for (uint32_t c0 = 8; c0 < tcnt; c0 += 32) {
+        FoldEntry f = {0ull, 0u, 0u, 0u, NO_SLOT, 0u, PC_SKIP};
+        if (c0 + lane < tcnt) f = fold_entry(a, toff + c0 + lane, bx, by, bz);
+        for (uint32_t m = __ballot_sync(FULLMASK, f.cls != PC_SKIP); m; m &= m - 1) apply(f, __ffs(m) - 1);
       }
 
       if (!dirty) continue;
@@ -1012,15 +1017,15 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
           st_local |= ST_STAGE_OVERFLOW;
         } else {
           uint32_t* dst = a.staging32 + (size_t)slot * 256;
-  #pragma unroll
-          for (int j = 0; j < 8; j++) dst[32 * j + lane] = vox[j];
-          if (lane == 0) { a.stage_cell[slot] = (uint32_t)ci; a.stage_src[slot] = src; }
+#pragma unroll
+          for (int k = 0; k < 8; k++) dst[32 * k + lane] = vox[k];
+          if (lane == 0) { a.stage_cell[slot] = ci; a.stage_src[slot] = src; }
         }
         tag = TAG_STAGED | (slot & 0x3fffffffu);
       }
       if (lane == 0) {
         const uint32_t t = atomicAdd(&a.res->touched_count, 1u);
-        if (t < a.touched_cap) a.touched[t] = make_uint2((uint32_t)ci, tag);
+        if (t < a.touched_cap) a.touched[t] = make_uint2(ci, tag);
         else st_local |= ST_STAGE_OVERFLOW;
       }
     }
@@ -1064,7 +1069,8 @@ void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEve
   {
     const uint32_t n_words = (uint32_t)(((size_t)a.BX * a.BY * a.BZ + 31) / 32);
     const uint32_t blocks = (n_words + 255) / 256;  // 8 warps per block, 32 words per warp
-    ++g_launches; mark_compact_kernel<<<blocks < 4096 ? blocks : 4096, 256, 0, s>>>(a.bmark, n_words, a.work, a.res);
+    ++g_launches; mark_compact_kernel<<<blocks < 4096 ? blocks : 4096, 256, 0, s>>>(a.bmark, n_words, (uint32_t)a.BX,
+                                                                              (uint32_t)a.BY, a.work, a.res);
   }
   if (a.inline_paints) { ++g_launches; fold_kernel<true><<<grid(PX_FOLD_MINB), 256, 0, s>>>(a); }
   else { ++g_launches; fold_kernel<false><<<grid(PX_FOLD_MINB), 256, 0, s>>>(a); }
