@@ -801,6 +801,7 @@ __device__ __forceinline__ FoldEntry fold_entry(const FoldArgs& a, uint32_t idx,
 template <bool INLINE>
 __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
   __shared__ unsigned long long smask[8][8];
+  __shared__ __align__(16) unsigned long long spm[8][32][8];  // voxel masks of the looked-up partial pairs
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const int lx0 = (lane & 3) * 2, ly = lane >> 2;
@@ -827,7 +828,19 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
       q_tcnt = __ldg(a.tile_cnt + tile);
       if (ent < q_tcnt) q = fold_entry(a, q_toff + ent, (int)bx, (int)by, (int)bz);
     }
+    if (q.cls == PC_PARTIAL) {  // its pair's voxel masks, copied to shared memory while the bricks load
+      const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&spm[wib][lane][0]);
+      const unsigned long long* srcp = a.pmask + q.pr * 8;
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst + 16 * k), "l"(srcp + 2 * k) : "memory");
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
     const uint32_t m_all = __ballot_sync(FULLMASK, q.cls != PC_SKIP);  // shapes.ts:364 skips the rest
+    uint32_t t_ci = 0, t_tag = 0;  // lane j: brick j's touched-list entry
+    bool t_dirty = false;
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+    __syncwarp();
 
     for (uint32_t j = 0; j < n_here; j++) {
       const uint32_t pk = __shfl_sync(FULLMASK, q_pk, 8 * j);
@@ -857,8 +870,8 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
         for (int k = 0; k < 8; k++) vox[k] = pb[32 * k + lane];
       }
 
-      // apply the op whose entry lane `b` holds
-      auto apply = [&](const FoldEntry& f, int b) {
+      // apply the op whose entry lane `b` holds (`pm`: its voxel masks are in spm[wib][b])
+      auto apply = [&](const FoldEntry& f, int b, bool pm) {
         const unsigned long long pair = __shfl_sync(FULLMASK, f.pr, b);
         const int cls = __shfl_sync(FULLMASK, f.cls, b);
         const uint32_t mt = __shfl_sync(FULLMASK, f.meta, b);
@@ -897,7 +910,10 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
         if (!full) {
           if (lane < 8) {
             const uint32_t c = (psc >> (2 * lane)) & 3u;
-            smask[wib][lane] = c == PC_FULL ? ~0ull : c == PC_PARTIAL ? __ldg(a.pmask + pair * 8 + lane) : 0ull;
+            smask[wib][lane] = c == PC_FULL      ? ~0ull
+                               : c != PC_PARTIAL ? 0ull
+                               : pm              ? spm[wib][b][lane]
+                                                 : __ldg(a.pmask + pair * 8 + lane);
           }
           wc.sub += 8;
           wc.vox += 64 * __popc(psc & ~(psc >> 1) & 0x5555u);  // sub-blocks of class PC_PARTIAL (01)
@@ -994,12 +1010,12 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
       };
 
       // entries 0..7 of the tile list, looked up above by lanes 8j..8j+7
-      for (uint32_t m = (m_all >> (8 * j)) & 0xffu; m; m &= m - 1) apply(q, (int)(8 * j) + __ffs(m) - 1);
+      for (uint32_t m = (m_all >> (8 * j)) & 0xffu; m; m &= m - 1) apply(q, (int)(8 * j) + __ffs(m) - 1, true);
       // the rest of a longer list, 32 entries per pass
       for (uint32_t c0 = 8; c0 < tcnt; c0 += 32) {
         FoldEntry f = {0ull, 0u, 0u, 0u, NO_SLOT, 0u, PC_SKIP};
         if (c0 + lane < tcnt) f = fold_entry(a, toff + c0 + lane, bx, by, bz);
-        for (uint32_t m = __ballot_sync(FULLMASK, f.cls != PC_SKIP); m; m &= m - 1) apply(f, __ffs(m) - 1);
+        for (uint32_t m = __ballot_sync(FULLMASK, f.cls != PC_SKIP); m; m &= m - 1) apply(f, __ffs(m) - 1, false);
       }
 
       if (!dirty) continue;
@@ -1023,9 +1039,17 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
         }
         tag = TAG_STAGED | (slot & 0x3fffffffu);
       }
-      if (lane == 0) {
-        const uint32_t t = atomicAdd(&a.res->touched_count, 1u);
-        if (t < a.touched_cap) a.touched[t] = make_uint2(ci, tag);
+      if (lane == (int)j) { t_ci = ci; t_tag = tag; t_dirty = true; }
+    }
+    // the group's touched-list entries, one append per group
+    const uint32_t dm = __ballot_sync(FULLMASK, t_dirty);
+    if (dm) {
+      uint32_t t0 = 0;
+      if (lane == 0) t0 = atomicAdd(&a.res->touched_count, (uint32_t)__popc(dm));
+      t0 = __shfl_sync(FULLMASK, t0, 0);
+      if (t_dirty) {
+        const uint32_t t = t0 + (uint32_t)__popc(dm & ((1u << lane) - 1u));
+        if (t < a.touched_cap) a.touched[t] = make_uint2(t_ci, t_tag);
         else st_local |= ST_STAGE_OVERFLOW;
       }
     }
