@@ -1325,15 +1325,34 @@ __device__ __forceinline__ size_t level_size(size_t E, int l) {
   return n;
 }
 
+// Level l of the min tree: entry k = the minimum of entries 32k .. 32k + 31 of
+// level l - 1 (one coalesced load per entry below, a warp minimum per entry).
 __global__ void tree_level_kernel(const int32_t* __restrict__ below, int32_t* level, int l, const BuildResult* res) {
   const size_t n_below = level_size(res->n_events, l - 1);
-  const size_t n = (n_below + 31) >> 5;
-  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
-    int32_t m = 0x7fffffff;
-    size_t c0 = k * 32, c1 = min(c0 + 32, n_below);
-    for (size_t c = c0; c < c1; c++) m = min(m, below[c]);
-    level[k] = m;
+  const size_t n32 = ((n_below + 31) >> 5) << 5;  // a whole warp per entry: the loop bound is warp-uniform
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n32; c += (size_t)gridDim.x * blockDim.x) {
+    const int32_t m = __reduce_min_sync(FULLMASK, c < n_below ? below[c] : 0x7fffffff);
+    if ((c & 31) == 0) level[c >> 5] = m;
   }
+}
+
+// Bit q of the result: entry 32 b + q of level L is below D, for q <= qmax
+// (the block's 32 entries as eight 16-byte loads; levels are 128-byte aligned
+// and padded to whole blocks).
+__device__ __forceinline__ uint32_t block_below(const int32_t* L, long long b, int D, int qmax) {
+  const int4* p = reinterpret_cast<const int4*>(L + b * 32);
+  int4 v[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) v[k] = p[k];
+  uint32_t m = 0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    m |= (uint32_t)(v[k].x < D) << (4 * k);
+    m |= (uint32_t)(v[k].y < D) << (4 * k + 1);
+    m |= (uint32_t)(v[k].z < D) << (4 * k + 2);
+    m |= (uint32_t)(v[k].w < D) << (4 * k + 3);
+  }
+  return qmax >= 31 ? m : m & ((2u << qmax) - 1u);
 }
 
 // Largest i < e with depth[i] < D (or -1): climb the min tree to the nearest
@@ -1344,10 +1363,9 @@ __device__ long long prev_less(const int32_t* depth, const int32_t* tree, const 
   long long found = -1;
   while (i >= 0) {
     const int32_t* L = lev == 0 ? depth : tree + tl.off[lev - 1];
-    long long start = i & ~31ll;
-    for (long long k = i; k >= start; k--)
-      if (L[k] < D) { found = k; break; }
-    if (found >= 0) break;
+    const long long start = i & ~31ll;
+    const uint32_t m = block_below(L, start >> 5, D, (int)(i - start));
+    if (m) { found = start + 31 - __clz(m); break; }
     if (start == 0 || lev == tl.n) return -1;
     i = (start >> 5) - 1;
     lev++;
@@ -1356,13 +1374,10 @@ __device__ long long prev_less(const int32_t* depth, const int32_t* tree, const 
   while (lev > 0) {
     lev--;
     const int32_t* L = lev == 0 ? depth : tree + tl.off[lev - 1];
-    const size_t n = level_size(E, lev);
-    long long c0 = found * 32, c1 = min((long long)n - 1, c0 + 31);
-    long long nf = -1;
-    for (long long c = c1; c >= c0; c--)
-      if (L[c] < D) { nf = c; break; }
-    found = nf;
-    if (found < 0) return -1;  // cannot happen: the parent's minimum is below D
+    const long long n = (long long)level_size(E, lev);
+    const uint32_t m = block_below(L, found, D, (int)min(31ll, n - 1 - found * 32));
+    if (!m) return -1;  // cannot happen: the parent's minimum is below D
+    found = found * 32 + 31 - __clz(m);
   }
   return found;
 }
@@ -1439,11 +1454,11 @@ void launch_replay(const ReplayArgs& a, cudaStream_t s) {
   while (n > 32 && tl.n < 8) {
     n = (n + 31) / 32;
     tl.off[tl.n++] = off;
-    off += n;
+    off += (n + 31) & ~(size_t)31;  // levels start on 128-byte boundaries (prev_less loads whole blocks)
   }
   for (int l = 1; l <= tl.n; l++) {
     const int32_t* below = l == 1 ? a.depth : a.tree + tl.off[l - 2];
-    ++g_launches; tree_level_kernel<<<blocks(level_size_host(a.E_max, l)), T, 0, s>>>(below, a.tree + tl.off[l - 1], l, a.res);
+    ++g_launches; tree_level_kernel<<<blocks(level_size_host(a.E_max, l - 1)), T, 0, s>>>(below, a.tree + tl.off[l - 1], l, a.res);
   }
   ++g_launches; match_kernel<<<blocks(a.E_max), T, 0, s>>>(a, tl);
   ++g_launches; resolve_kernel<<<blocks(a.E_max), T, 0, s>>>(a.ew, a.res);

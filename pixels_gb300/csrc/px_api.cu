@@ -906,8 +906,8 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
       (rc = ensure(w, w->tiles_nonempty, 4 * w->ntiles)) || (rc = ensure(w, w->tile_ops, 4 * tile_pairs)) || (rc = ensure(w, w->tile_boxes, 8 * tile_pairs)) ||
       (rc = ensure(w, w->evt, P)) || (rc = ensure(w, w->fsrc, 8 * P)) || (rc = ensure(w, w->cnt, 4 * P)) ||
       (rc = ensure(w, w->pos, 4 * P)) || (rc = ensure(w, w->etype, E_max)) || (rc = ensure(w, w->ew, 8 * E_max)) ||
-      (rc = ensure(w, w->depth_fn, 8 * E_max)) || (rc = ensure(w, w->depth, 4 * E_max)) ||
-      (rc = ensure(w, w->tree, 4 * (E_max / 16 + 64 + E_max))) || (rc = ensure(w, w->fresh, 4 * E_max)) ||
+      (rc = ensure(w, w->depth_fn, 8 * E_max)) || (rc = ensure(w, w->depth, 4 * (E_max + 32))) ||
+      (rc = ensure(w, w->tree, 4 * (E_max / 16 + 512 + E_max))) || (rc = ensure(w, w->fresh, 4 * E_max)) ||
       (rc = ensure(w, w->fresh_rank, 4 * E_max)) || (rc = ensure(w, w->staging, 1024 * stage_cap)) ||
       (rc = ensure(w, w->stage_cell, 4 * stage_cap)) || (rc = ensure(w, w->stage_src, 8 * stage_cap)) ||
       (rc = ensure(w, w->touched, 8 * touched_bound)) ||
