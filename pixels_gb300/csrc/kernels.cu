@@ -1101,7 +1101,7 @@ void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEve
 }
 
 // ---------------------------------------------------------------------------
-// scans (block-wise, three passes; sizes may live on the device)
+// scans (single pass; sizes may live on the device)
 
 constexpr int SCAN_THREADS = 512;
 constexpr int SCAN_ITEMS = 8;
@@ -1112,6 +1112,11 @@ __device__ __forceinline__ uint32_t shfl_up_any(uint32_t v, int o) { return __sh
 __device__ __forceinline__ int32_t shfl_up_any(int32_t v, int o) { return __shfl_up_sync(FULLMASK, v, o); }
 __device__ __forceinline__ int2 shfl_up_any(int2 v, int o) {
   return make_int2(__shfl_up_sync(FULLMASK, v.x, o), __shfl_up_sync(FULLMASK, v.y, o));
+}
+__device__ __forceinline__ uint32_t shfl_any(uint32_t v, int l) { return __shfl_sync(FULLMASK, v, l); }
+__device__ __forceinline__ int32_t shfl_any(int32_t v, int l) { return __shfl_sync(FULLMASK, v, l); }
+__device__ __forceinline__ int2 shfl_any(int2 v, int l) {
+  return make_int2(__shfl_sync(FULLMASK, v.x, l), __shfl_sync(FULLMASK, v.y, l));
 }
 
 struct SumOp {
@@ -1174,80 +1179,118 @@ __device__ __forceinline__ size_t scan_n(size_t n_max, const uint32_t* n_dev) {
 template <bool REV>
 __device__ __forceinline__ size_t scan_idx(size_t k, size_t n) { return REV ? n - 1 - k : k; }
 
-template <class Op, bool REV>
-__global__ void __launch_bounds__(SCAN_THREADS) scan_pass1(const typename Op::T* in, size_t n_max, const uint32_t* n_dev,
-                                                            typename Op::T* agg) {
-  typedef typename Op::T T;
-  __shared__ T sh[32];
-  const size_t n = scan_n(n_max, n_dev);
-  const size_t k0 = (size_t)blockIdx.x * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
-  T acc = Op::identity();
-#pragma unroll
-  for (int i = 0; i < SCAN_ITEMS; i++) {
-    size_t k = k0 + i;
-    if (k < n) acc = Op::combine(acc, in[scan_idx<REV>(k, n)]);
-  }
-  T total;
-  block_exclusive<Op>(acc, sh, total);
-  if (threadIdx.x == 0) agg[blockIdx.x] = total;
-}
+// Single-pass scan with decoupled look-back: each block takes the next tile
+// by ticket (so every earlier tile is already running or done), publishes its
+// aggregate, reads its predecessors' inclusive prefixes (or aggregates, while
+// those are pending) from nearest to farthest, publishes its own inclusive
+// prefix and writes its outputs.  Flags: 0 pending, 1 aggregate, 2 prefix.
+constexpr uint32_t SCAN_SPIN_LIMIT = 1u << 24;
 
-template <class Op>
-__global__ void __launch_bounds__(1024) scan_pass2(typename Op::T* agg, int nb) {
-  typedef typename Op::T T;
-  __shared__ T sh[32];
-  const int per = (nb + blockDim.x - 1) / blockDim.x;
-  const int b0 = threadIdx.x * per;
-  T acc = Op::identity();
-  for (int i = 0; i < per; i++)
-    if (b0 + i < nb) acc = Op::combine(acc, agg[b0 + i]);
-  T total;
-  T pre = block_exclusive<Op>(acc, sh, total);
-  for (int i = 0; i < per; i++)
-    if (b0 + i < nb) {
-      T v = agg[b0 + i];
-      agg[b0 + i] = pre;
-      pre = Op::combine(pre, v);
-    }
+template <class T>
+__device__ __forceinline__ void scan_publish(T* slot, uint32_t* flag, T v, uint32_t f) {
+  __stcg(slot, v);
+  __threadfence();
+  *(volatile uint32_t*)flag = f;
 }
+__device__ __forceinline__ int2 scan_peek(const int2* p) { return __ldcg(p); }
+__device__ __forceinline__ uint32_t scan_peek(const uint32_t* p) { return __ldcg(p); }
+__device__ __forceinline__ int32_t scan_peek(const int32_t* p) { return __ldcg(p); }
 
 template <class Op, bool REV>
-__global__ void __launch_bounds__(SCAN_THREADS) scan_pass3(const typename Op::T* in, typename Op::T* out, size_t n_max,
-                                                            const uint32_t* n_dev, const typename Op::T* agg,
-                                                            bool inclusive, typename Op::T* total_out) {
+__global__ void __launch_bounds__(SCAN_THREADS) scan_onepass(const typename Op::T* in, typename Op::T* out,
+                                                              size_t n_max, const uint32_t* n_dev, bool inclusive,
+                                                              typename Op::T* total_out, ScanTemp st,
+                                                              uint32_t* ticket) {
   typedef typename Op::T T;
   __shared__ T sh[32];
+  __shared__ T s_prefix;
+  __shared__ uint32_t s_tile;
+  uint32_t* flags = ticket + 4;
+  T* agg = (T*)st.block_agg;
+  T* incl = agg + st.max_blocks;
   const size_t n = scan_n(n_max, n_dev);
-  const size_t k0 = (size_t)blockIdx.x * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
+  if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  if ((size_t)tile * SCAN_TILE >= n) return;  // every later tile is past the end too
+  const size_t k0 = (size_t)tile * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
   T v[SCAN_ITEMS];
   T acc = Op::identity();
 #pragma unroll
   for (int i = 0; i < SCAN_ITEMS; i++) {
-    size_t k = k0 + i;
+    const size_t k = k0 + i;
     v[i] = k < n ? in[scan_idx<REV>(k, n)] : Op::identity();
     acc = Op::combine(acc, v[i]);
   }
   T total;
-  T pre = Op::combine(agg[blockIdx.x], block_exclusive<Op>(acc, sh, total));
+  const T pre_block = block_exclusive<Op>(acc, sh, total);
+  if (threadIdx.x < 32) {  // warp 0 publishes and looks back, 32 tiles per step
+    const int lane = threadIdx.x;
+    T prefix = Op::identity();
+    if (tile == 0) {
+      if (lane == 0) scan_publish(incl, flags, total, 2u);
+    } else {
+      if (lane == 0) scan_publish(agg + tile, flags + tile, total, 1u);
+      long long hi = (long long)tile - 1;
+      uint32_t spins = 0;
+      for (;;) {
+        const long long j = hi - 31 + lane;  // lane 31 reads the nearest tile of the window
+        const uint32_t f = j >= 0 ? *(volatile uint32_t*)(flags + j) : 2u;  // before tile 0: the identity
+        if (__any_sync(FULLMASK, f == 0)) {
+          if (++spins > SCAN_SPIN_LIMIT) {  // cannot happen: earlier tiles publish unconditionally
+            if (lane == 0) atomicOr(st.status, (uint32_t)ST_CHAIN);
+            break;
+          }
+          continue;
+        }
+        __threadfence();
+        T v = j >= 0 ? scan_peek(f == 2 ? incl + j : agg + j) : Op::identity();
+        const uint32_t im = __ballot_sync(FULLMASK, f == 2);
+        if (lane < (im ? 31 - __clz(im) : 0)) v = Op::identity();  // tiles before the nearest prefix
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {  // ordered combination of the window
+          const T y = shfl_up_any(v, o);
+          if (lane >= o) v = Op::combine(y, v);
+        }
+        prefix = Op::combine(shfl_any(v, 31), prefix);
+        if (im) break;
+        hi -= 32;
+      }
+      if (lane == 0) scan_publish(incl + tile, flags + tile, Op::combine(prefix, total), 2u);
+    }
+    if (lane == 0) s_prefix = prefix;
+  }
+  __syncthreads();
+  T pre = Op::combine(s_prefix, pre_block);
 #pragma unroll
   for (int i = 0; i < SCAN_ITEMS; i++) {
-    size_t k = k0 + i;
-    T nxt = Op::combine(pre, v[i]);
+    const size_t k = k0 + i;
+    const T nxt = Op::combine(pre, v[i]);
     if (k < n) out[scan_idx<REV>(k, n)] = inclusive ? nxt : pre;
     if (total_out && k + 1 == n) *total_out = nxt;
     pre = nxt;
   }
 }
 
+static size_t scan_region_bytes(size_t max_blocks) { return 16 + ((4 * max_blocks + 15) & ~(size_t)15); }
+size_t scan_regions_offset(size_t max_blocks) { return 16 * max_blocks; }
+size_t scan_regions_bytes(size_t max_blocks) { return SCAN_REGIONS * scan_region_bytes(max_blocks); }
+size_t scan_temp_bytes(size_t max_blocks) { return scan_regions_offset(max_blocks) + scan_regions_bytes(max_blocks); }
+
 template <class Op, bool REV>
 void scan_any(const typename Op::T* in, typename Op::T* out, size_t n_max, const uint32_t* n_dev, bool inclusive,
               typename Op::T* total_out, ScanTemp& t, cudaStream_t s) {
   if (n_max == 0) return;
-  int nb = (int)((n_max + SCAN_TILE - 1) / SCAN_TILE);
-  typename Op::T* agg = (typename Op::T*)t.block_agg;
-  ++g_launches; scan_pass1<Op, REV><<<nb, SCAN_THREADS, 0, s>>>(in, n_max, n_dev, agg);
-  ++g_launches; scan_pass2<Op><<<1, 1024, 0, s>>>(agg, nb);
-  ++g_launches; scan_pass3<Op, REV><<<nb, SCAN_THREADS, 0, s>>>(in, out, n_max, n_dev, agg, inclusive, total_out);
+  const size_t nb = (n_max + SCAN_TILE - 1) / SCAN_TILE;
+  int r = t.next_region++;
+  char* regions = (char*)t.block_agg + scan_regions_offset(t.max_blocks);
+  if (r >= SCAN_REGIONS) {  // more scans than cleared regions: clear the last one again
+    r = SCAN_REGIONS - 1;
+    cudaMemsetAsync(regions + r * scan_region_bytes(t.max_blocks), 0, scan_region_bytes(t.max_blocks), s);
+  }
+  uint32_t* ticket = (uint32_t*)(regions + r * scan_region_bytes(t.max_blocks));
+  ++g_launches;
+  scan_onepass<Op, REV><<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, out, n_max, n_dev, inclusive, total_out, t, ticket);
 }
 
 void launch_scan_u32(const uint32_t* in, uint32_t* out, size_t n, const uint32_t* n_dev, bool inclusive,

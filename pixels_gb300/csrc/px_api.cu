@@ -918,11 +918,12 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
       (rc = ensure(w, w->pvals, 2048 * n_slots + 4)) || (rc = ensure(w, w->bmark, 4 * ((w->ncells + 31) / 32))) ||
       (rc = ensure(w, w->work, 4 * touched_bound + 4)))
     return rc;
+  size_t scan_nb;
   {
     size_t items = w->ntiles > E_max ? w->ntiles : E_max;
     if (P > items) items = P;
-    size_t nb = items / scan_items_per_block() + 2;
-    if ((rc = ensure(w, w->scan_agg, 8 * nb))) return rc;
+    scan_nb = items / scan_items_per_block() + 2;
+    if ((rc = ensure(w, w->scan_agg, scan_temp_bytes(scan_nb)))) return rc;
   }
   {
     const void* after[9] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p,
@@ -987,7 +988,8 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   CU(cudaMemsetAsync(w->bmark.p, 0, 4 * ((w->ncells + 31) / 32), s));
 
   BuildResult* res = (BuildResult*)w->res.p;
-  ScanTemp st{w->scan_agg.p, w->scan_agg.bytes / 8};
+  ScanTemp st{w->scan_agg.p, scan_nb, &res->status, 0};
+  CU(cudaMemsetAsync((char*)w->scan_agg.p + scan_regions_offset(scan_nb), 0, scan_regions_bytes(scan_nb), s));
   launch_cull_count((const uint2*)w->d_boxes.p, n_ops, w->TX, w->TY, w->TZ, (uint32_t*)w->tile_cnt.p,
                     (uint32_t*)w->tiles_nonempty.p, res, s);
   launch_scan_u32((const uint32_t*)w->tile_cnt.p, (uint32_t*)w->tile_off.p, w->ntiles, nullptr, false, nullptr, st, s);

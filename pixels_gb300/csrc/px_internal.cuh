@@ -201,11 +201,21 @@ void launch_cull_fill(const uint2* boxes, int n_ops, int TX, int TY, int TZ, con
 // max_blocks > 0 caps the persistent grids (builds sharing the GPU)
 void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEvent_t mid, int max_blocks);
 
+// Scratch of the single-pass scans (scan_temp_bytes(max_blocks) bytes): the
+// tiles' aggregates and inclusive prefixes, then SCAN_REGIONS regions of a tile
+// ticket and per-tile flags.  A build clears the regions once
+// (scan_regions_bytes) and its scans take one region each, in launch order.
+constexpr int SCAN_REGIONS = 5;
 struct ScanTemp {
   void* block_agg;
   size_t max_blocks;
+  uint32_t* status;  // a look-back that waits too long sets ST_CHAIN here
+  int next_region;   // regions already used by this build's scans
 };
 size_t scan_items_per_block();
+size_t scan_temp_bytes(size_t max_blocks);
+size_t scan_regions_offset(size_t max_blocks);  // where the regions start
+size_t scan_regions_bytes(size_t max_blocks);
 void launch_scan_u32(const uint32_t* in, uint32_t* out, size_t n, const uint32_t* n_dev, bool inclusive,
                      uint32_t* total_out, ScanTemp& t, cudaStream_t s);
 
