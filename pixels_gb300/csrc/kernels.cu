@@ -138,11 +138,20 @@ struct WarpCounters {
   uint32_t brick, sub, vox, alloc, free_;
 };
 
-// Per-lane statistics of the float32 path.
+// The float32 path's rare events -- rescues and validation mismatches --
+// counted into the build's counters where they happen (no per-lane counters
+// held in registers through the work loops).
 struct LaneStats {
-  uint32_t paint, resc, viol;
-  float max_err;
-  uint32_t rb, rs, rv, rp;
+  BuildResult* res;
+  __device__ __forceinline__ void viol() { atomicAdd(&res->c.violations, 1ull); }
+  // a float64 rescue at level `what` (0 voxel, 1 brick, 2 sub-block); amb: an
+  // undecided polygon crossing test; err: |mid(d32) - d64| (negative: none)
+  __device__ __noinline__ void rescue(int what, bool amb, float err) {
+    atomicAdd(&res->c.rescued, 1ull);
+    atomicAdd(what == 1 ? &res->c.resc_brick : what == 2 ? &res->c.resc_sub : &res->c.resc_vox, 1ull);
+    if (amb) atomicAdd(&res->c.resc_poly, 1ull);
+    else if (err > 0.f) atomicMax(&res->max_err_bits, (unsigned long long)__double_as_longlong((double)err));
+  }
 };
 
 // Work items taken by a warp from a shared counter, several per atomic (one
@@ -212,14 +221,10 @@ __device__ __forceinline__ int eval_decide(const FoldArgs& a, const OpDev* O, co
       *dout = {__double2float_rd(d64 - M64), __double2float_ru(d64 + M64)};
     }
     const double M = MIXED_MARGIN;
-    if (a.validate && !amb && !((double)d.lo - M <= d64 && d64 <= (double)d.hi + M) && count) ls.viol++;
+    if (a.validate && !amb && !((double)d.lo - M <= d64 && d64 <= (double)d.hi + M) && count) ls.viol();
     if (r == 3 && count) {
-      ls.resc++;
-      if (what == 1) ls.rb++; else if (what == 2) ls.rs++; else ls.rv++;  // brick: counted by lane 0 only
-      if (amb) ls.rp++;
-      double mid = 0.5 * ((double)d.lo + (double)d.hi);
-      double e = fabs(mid - d64);
-      if (e == e && (float)e > ls.max_err && !amb) ls.max_err = (float)e;
+      const double e = fabs(0.5 * ((double)d.lo + (double)d.hi) - d64);
+      ls.rescue(what, amb, e == e ? (float)e : -1.f);
     }
     if (what == 0) return d64 > 0.0 ? 0 : 1;
     return classify64(d64, what == 1 ? O->bhd : O->shd);
@@ -300,7 +305,7 @@ __device__ __forceinline__ void brick_bases(const FoldArgs& a, const OpDev* O, i
 template <int MODE>
 __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIFY64_MINB) classify_kernel(FoldArgs a) {
   const int lane = threadIdx.x & 31;
-  LaneStats ls = {0, 0, 0, 0.f, 0, 0, 0, 0};
+  LaneStats ls = {a.res};
   uint32_t n_brick = 0;
   uint32_t st_local = 0;
   const unsigned long long P = a.n_pairs;
@@ -366,30 +371,15 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
       else st_local |= ST_STAGE_OVERFLOW;
     }
   }
-  uint32_t nb = n_brick, rc = ls.resc, vc = ls.viol, rb = ls.rb, rs = ls.rs, rv = ls.rv, rp = ls.rp, stw = st_local;
-  float me = ls.max_err;
+  uint32_t nb = n_brick, stw = st_local;
 #pragma unroll
   for (int o2 = 16; o2; o2 >>= 1) {
     nb += __shfl_xor_sync(FULLMASK, nb, o2);
-    rc += __shfl_xor_sync(FULLMASK, rc, o2);
-    vc += __shfl_xor_sync(FULLMASK, vc, o2);
-    rb += __shfl_xor_sync(FULLMASK, rb, o2);
-    rs += __shfl_xor_sync(FULLMASK, rs, o2);
-    rv += __shfl_xor_sync(FULLMASK, rv, o2);
-    rp += __shfl_xor_sync(FULLMASK, rp, o2);
     stw |= __shfl_xor_sync(FULLMASK, stw, o2);
-    me = fmaxf(me, __shfl_xor_sync(FULLMASK, me, o2));
   }
   if (lane == 0) {
     if (nb) atomicAdd(&a.res->c.brick_evals, (unsigned long long)nb);
-    if (rc) atomicAdd(&a.res->c.rescued, (unsigned long long)rc);
-    if (vc) atomicAdd(&a.res->c.violations, (unsigned long long)vc);
-    if (rb) atomicAdd(&a.res->c.resc_brick, (unsigned long long)rb);
-    if (rs) atomicAdd(&a.res->c.resc_sub, (unsigned long long)rs);
-    if (rv) atomicAdd(&a.res->c.resc_vox, (unsigned long long)rv);
-    if (rp) atomicAdd(&a.res->c.resc_poly, (unsigned long long)rp);
     if (stw) atomicOr(&a.res->status, stw);
-    if (me > 0.f) atomicMax(&a.res->max_err_bits, (unsigned long long)__double_as_longlong((double)me));
   }
 }
 
@@ -400,7 +390,7 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
 template <int MODE>
 __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIFY64_MINB) sub_kernel(FoldArgs a) {
   const int lane = threadIdx.x & 31;
-  LaneStats ls = {0, 0, 0, 0.f, 0, 0, 0, 0};
+  LaneStats ls = {a.res};
   uint32_t st_local = 0;
   uint32_t incl = lane < VCLASSES ? min(__ldg(&a.pitem_counter[1 + lane]), a.pq_cap[lane]) : 0u;
   const uint32_t own = incl;
@@ -491,25 +481,10 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
       else st_local |= ST_STAGE_OVERFLOW;
     }
   }
-  uint32_t rc = ls.resc, vc = ls.viol, rs = ls.rs, rp = ls.rp, stw = st_local;
-  float me = ls.max_err;
+  uint32_t stw = st_local;
 #pragma unroll
-  for (int o2 = 16; o2; o2 >>= 1) {
-    rc += __shfl_xor_sync(FULLMASK, rc, o2);
-    vc += __shfl_xor_sync(FULLMASK, vc, o2);
-    rs += __shfl_xor_sync(FULLMASK, rs, o2);
-    rp += __shfl_xor_sync(FULLMASK, rp, o2);
-    stw |= __shfl_xor_sync(FULLMASK, stw, o2);
-    me = fmaxf(me, __shfl_xor_sync(FULLMASK, me, o2));
-  }
-  if (lane == 0) {
-    if (rc) atomicAdd(&a.res->c.rescued, (unsigned long long)rc);
-    if (vc) atomicAdd(&a.res->c.violations, (unsigned long long)vc);
-    if (rs) atomicAdd(&a.res->c.resc_sub, (unsigned long long)rs);
-    if (rp) atomicAdd(&a.res->c.resc_poly, (unsigned long long)rp);
-    if (stw) atomicOr(&a.res->status, stw);
-    if (me > 0.f) atomicMax(&a.res->max_err_bits, (unsigned long long)__double_as_longlong((double)me));
-  }
+  for (int o2 = 16; o2; o2 >>= 1) stw |= __shfl_xor_sync(FULLMASK, stw, o2);
+  if (lane == 0 && stw) atomicOr(&a.res->status, stw);
 }
 
 // Mixed form: a voxel's decision from its sub-block centre's value dc, when the
@@ -526,7 +501,7 @@ __device__ __forceinline__ int lip_decide(const OpDev* O, Iv dc, int ox, int oy,
 template <int MODE>
 __global__ void __launch_bounds__(256, MODE == 1 ? PX_VOXEL_MINB : PX_CLASSIFY64_MINB) voxel_kernel(FoldArgs a) {
   const int lane = threadIdx.x & 31;
-  LaneStats ls = {0, 0, 0, 0.f, 0, 0, 0, 0};
+  LaneStats ls = {a.res};
   // the classes' item counts, as an inclusive prefix over lanes 0..VCLASSES-1
   uint32_t incl = lane < VCLASSES ? min(__ldg(&a.vitem_counter[1 + lane]), a.vq_cap[lane]) : 0u;
   const uint32_t own = incl;
@@ -579,16 +554,11 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_VOXEL_MINB : PX_CLASSIFY64
             const VoxelF64 f = voxel_f64(a.params, a.vs, a.validate, code, clen, dk, amb, inside,
                                          (float)(vbx * 8 + lx) + 0.5f, (float)(vby * 8 + ly0 + k) + 0.5f,
                                          (float)(vbz * 8 + lz) + 0.5f);
-            ls.viol += f.viol;
-            if (inside == 3) {
-              ls.resc++;
-              ls.rv++;
-              if (amb) ls.rp++;
-              ls.max_err = fmaxf(ls.max_err, f.err);
-            }
+            if (f.viol) ls.viol();
+            if (inside == 3) ls.rescue(0, amb, f.err);
             inside = f.inside;
           }
-          if (lipk != 3 && inside != lipk) ls.viol++;  // validation: the bound disagreed with the evaluation
+          if (lipk != 3 && inside != lipk) ls.viol();  // validation: the bound disagreed with the evaluation
         }
         const int bit = (col & 3) | ((2 * yh + k) << 2) | ((col >> 2) << 4);  // voxel index in the sub-block
         if (inside == 1) {
@@ -609,7 +579,7 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_VOXEL_MINB : PX_CLASSIFY64
           inside = eval_decide<MODE>(a, V, code, clen, use32, bo, (float)lx, (float)lyv, (float)lz,
                                      (float)(vbx * 8 + lx) + 0.5f, (float)(vby * 8 + lyv) + 0.5f,
                                      (float)(vbz * 8 + lz) + 0.5f, 0, ls);
-          if (lipd != 3 && inside != lipd) ls.viol++;  // validation: the bound disagreed with the evaluation
+          if (lipd != 3 && inside != lipd) ls.viol();  // validation: the bound disagreed with the evaluation
         }
         bal[r] = __ballot_sync(FULLMASK, inside == 1);
       }
@@ -617,25 +587,8 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_VOXEL_MINB : PX_CLASSIFY64
     }
     // a lone box's sub-block is queued only in validation mode: check its runs
     if ((V->flags & OPF_BOX_RANGES) && lane == 0 && box_mask(V, vbx * 8 + sxo, vby * 8 + syo, vbz * 8 + szo) != m)
-      ls.viol++;
+      ls.viol();
     if (lane == 0) a.pmask[vp * 8 + ss] = m;
-  }
-  uint32_t rc = ls.resc, vc = ls.viol, rv = ls.rv, rp = ls.rp;
-  float me = ls.max_err;
-#pragma unroll
-  for (int o2 = 16; o2; o2 >>= 1) {
-    rc += __shfl_xor_sync(FULLMASK, rc, o2);
-    vc += __shfl_xor_sync(FULLMASK, vc, o2);
-    rv += __shfl_xor_sync(FULLMASK, rv, o2);
-    rp += __shfl_xor_sync(FULLMASK, rp, o2);
-    me = fmaxf(me, __shfl_xor_sync(FULLMASK, me, o2));
-  }
-  if (lane == 0) {
-    if (rc) atomicAdd(&a.res->c.rescued, (unsigned long long)rc);
-    if (vc) atomicAdd(&a.res->c.violations, (unsigned long long)vc);
-    if (rv) atomicAdd(&a.res->c.resc_vox, (unsigned long long)rv);
-    if (rp) atomicAdd(&a.res->c.resc_poly, (unsigned long long)rp);
-    if (me > 0.f) atomicMax(&a.res->max_err_bits, (unsigned long long)__double_as_longlong((double)me));
   }
 }
 
