@@ -311,10 +311,11 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
   const unsigned long long P = a.n_pairs;
   const uint32_t n_chunks = (uint32_t)((P + 31) / 32);
   for (;;) {
-    uint32_t chunk = 0;
-    if (lane == 0) chunk = atomicAdd(a.chunk_counter, 1u);
-    chunk = __shfl_sync(FULLMASK, chunk, 0);
-    if (chunk >= n_chunks) break;
+    uint32_t take = 0;
+    if (lane == 0) take = atomicAdd(a.chunk_counter, 1u);
+    take = __shfl_sync(FULLMASK, take, 0);
+    if (take >= n_chunks) break;
+    const uint32_t chunk = __ldg(a.chunk_order + take);
     const unsigned long long p = (unsigned long long)chunk * 32 + lane;
     const bool valid = p < P;
     uint32_t o = __ldg(a.chunk_op + chunk);
@@ -345,15 +346,21 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
     }
     // a full pair of a painted op: its 8 sub-blocks go to the paint pass
     const bool fullp = valid && cls == PC_FULL && O->paint_slot != NO_SLOT;
-    const uint32_t fm = __ballot_sync(FULLMASK, fullp);
-    if (fm) {
-      uint32_t pb = 0;
-      if (lane == 0) pb = atomicAdd(a.paint_item_counter, 8u * __popc(fm));
-      pb = __shfl_sync(FULLMASK, pb, 0);
-      if (fullp) {
-        const uint32_t at = pb + 8u * __popc(fm & ((1u << lane) - 1u));
-        for (uint32_t q = 0; q < 8; q++)
-          if (at + q < a.paint_items_cap) a.paint_items[at + q] = make_uint2(o, (uint32_t)(p << 3) | q);
+    if (__any_sync(FULLMASK, fullp)) {
+      const bool back = MODE == 1 && O->paint32_off != NO_SLOT;
+#pragma unroll
+      for (int e = 0; e < 2; e++) {
+        const uint32_t fm = __ballot_sync(FULLMASK, fullp && back == (e == 1));
+        if (!fm) continue;
+        uint32_t pb = 0;
+        if (lane == 0) pb = atomicAdd(a.paint_item_counter + e, 8u * __popc(fm));
+        pb = __shfl_sync(FULLMASK, pb, 0);
+        if (fullp && back == (e == 1)) {
+          const uint32_t at = pb + 8u * __popc(fm & ((1u << lane) - 1u));
+          for (uint32_t q = 0; q < 8; q++)
+            if (at + q < a.paint_items_cap)
+              a.paint_items[e ? a.paint_items_cap - 1 - (at + q) : at + q] = make_uint2(o, (uint32_t)(p << 3) | q);
+        }
       }
     }
     // partial pairs go to the sub-block pass, one queue region per shape class
@@ -392,7 +399,9 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
   const int lane = threadIdx.x & 31;
   LaneStats ls = {a.res};
   uint32_t st_local = 0;
-  uint32_t incl = lane < VCLASSES ? min(__ldg(&a.pitem_counter[1 + lane]), a.pq_cap[lane]) : 0u;
+  // the classes' item counts in the order they are taken, as an inclusive prefix over lanes
+  const int my_cls = lane < VCLASSES ? a.class_order[lane] : 0;
+  uint32_t incl = lane < VCLASSES ? min(__ldg(&a.pitem_counter[1 + my_cls]), a.pq_cap[my_cls]) : 0u;
   const uint32_t own = incl;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -422,7 +431,7 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
     bool boxr = false;
     Iv dc = {-INFINITY, INFINITY};  // enclosure of the sub-block centre's value (mixed form)
     if (have) {
-      const uint2 item = __ldg(a.pitems + a.pq_base[my_k] + (it - my_first));
+      const uint2 item = __ldg(a.pitems + a.pq_base[a.class_order[my_k]] + (it - my_first));
       oo = item.x;
       pp = item.y;
       const OpDev* Q = a.ops + oo;
@@ -447,13 +456,19 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
       a.pmask[pp * 8 + s] = box_mask(a.ops + oo, pbx * 8 + (s & 1) * 4, pby * 8 + ((s >> 1) & 1) * 4,
                                      pbz * 8 + ((s >> 2) & 1) * 4);
     const bool paint = have && scls != PC_SKIP && a.ops[oo].paint_slot != NO_SLOT;
-    const uint32_t qm = __ballot_sync(FULLMASK, paint);
-    if (qm) {  // the covered sub-blocks of a painted op go to the paint pass
-      uint32_t pb = 0;
-      if (lane == 0) pb = atomicAdd(a.paint_item_counter, (uint32_t)__popc(qm));
-      pb = __shfl_sync(FULLMASK, pb, 0);
-      const uint32_t at = pb + __popc(qm & ((1u << lane) - 1u));
-      if (paint && at < a.paint_items_cap) a.paint_items[at] = make_uint2(oo, (uint32_t)(pp << 3) | (uint32_t)s);
+    if (__any_sync(FULLMASK, paint)) {  // the covered sub-blocks of a painted op go to the paint pass
+      const bool back = MODE == 1 && a.ops[oo].paint32_off != NO_SLOT;
+#pragma unroll
+      for (int e = 0; e < 2; e++) {
+        const uint32_t qm = __ballot_sync(FULLMASK, paint && back == (e == 1));
+        if (!qm) continue;
+        uint32_t pb = 0;
+        if (lane == 0) pb = atomicAdd(a.paint_item_counter + e, (uint32_t)__popc(qm));
+        pb = __shfl_sync(FULLMASK, pb, 0);
+        const uint32_t at = pb + __popc(qm & ((1u << lane) - 1u));
+        if (paint && back == (e == 1) && at < a.paint_items_cap)
+          a.paint_items[e ? a.paint_items_cap - 1 - at : at] = make_uint2(oo, (uint32_t)(pp << 3) | (uint32_t)s);
+      }
     }
     // mixed form: a partial sub-block whose centre value is farther from 0 than
     // every voxel's distance bound (Lipschitz) has all its voxels decided
@@ -502,8 +517,9 @@ template <int MODE>
 __global__ void __launch_bounds__(256, MODE == 1 ? PX_VOXEL_MINB : PX_CLASSIFY64_MINB) voxel_kernel(FoldArgs a) {
   const int lane = threadIdx.x & 31;
   LaneStats ls = {a.res};
-  // the classes' item counts, as an inclusive prefix over lanes 0..VCLASSES-1
-  uint32_t incl = lane < VCLASSES ? min(__ldg(&a.vitem_counter[1 + lane]), a.vq_cap[lane]) : 0u;
+  // the classes' item counts in the order they are taken, as an inclusive prefix over lanes
+  const int my_cls = lane < VCLASSES ? a.class_order[lane] : 0;
+  uint32_t incl = lane < VCLASSES ? min(__ldg(&a.vitem_counter[1 + my_cls]), a.vq_cap[my_cls]) : 0u;
   const uint32_t own = incl;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -517,7 +533,7 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_VOXEL_MINB : PX_CLASSIFY64
     if (it >= n_items) break;
     const int k = __popc(__ballot_sync(FULLMASK, lane < VCLASSES && incl <= it));  // class of item `it`
     const uint32_t first = __shfl_sync(FULLMASK, incl - own, k);
-    const uint4 item = __ldg(a.vitems + a.vq_base[k] + (it - first));
+    const uint4 item = __ldg(a.vitems + a.vq_base[a.class_order[k]] + (it - first));
     const Iv dcen = {__uint_as_float(item.z), __uint_as_float(item.w)};  // the sub-block centre's value
     const OpDev* V = a.ops + item.x;
     const unsigned long long vp = item.y >> 3;
@@ -623,13 +639,15 @@ __device__ __noinline__ uint32_t paint_at_voxel(const double* __restrict__ param
 template <int MODE>
 __global__ void __launch_bounds__(256) paint_kernel(FoldArgs a) {
   const int lane = threadIdx.x & 31;
-  const uint32_t n_items = min(__ldg(a.paint_item_counter), a.paint_items_cap);
+  // float64 paints (the front of the queue) first, then the certified float32 ones
+  const uint32_t n_front = min(__ldg(a.paint_item_counter), a.paint_items_cap);
+  const uint32_t n_items = n_front + min(__ldg(a.paint_item_counter + 1), a.paint_items_cap - n_front);
   uint32_t resc = 0, viol = 0;
   WorkBatch wb;
   for (;;) {
     const uint32_t it = wb.next(a.paint_counter, 2, lane);
     if (it >= n_items) break;
-    const uint2 item = __ldg(a.paint_items + it);
+    const uint2 item = __ldg(a.paint_items + (it < n_front ? it : a.paint_items_cap - 1 - (it - n_front)));
     const OpDev* O = a.ops + item.x;
     const unsigned long long pair = item.y >> 3;
     const int s = (int)(item.y & 7u);
@@ -693,29 +711,46 @@ __global__ void __launch_bounds__(256) paint_kernel(FoldArgs a) {
 // words of the bitmap, a warp-aggregated append), listed as packed brick
 // coordinates bx | by << 10 | bz << 20.
 __global__ void __launch_bounds__(256) mark_compact_kernel(const uint32_t* __restrict__ bmark, uint32_t n_words,
-                                                           uint32_t BX, uint32_t BY, uint32_t* work, BuildResult* res) {
+                                                           uint32_t BX, uint32_t BY, uint32_t TX, uint32_t TY,
+                                                           const uint32_t* __restrict__ tile_cnt, uint32_t* work,
+                                                           uint32_t last, uint32_t* counts, BuildResult* res) {
   const int lane = threadIdx.x & 31;
   const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t w0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; w0 < n_words; w0 += warps * 32) {
     const uint32_t wi = w0 + lane;
     const uint32_t bits = wi < n_words ? __ldg(bmark + wi) : 0u;
-    const uint32_t cnt = __popc(bits);
-    uint32_t incl = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t t = __shfl_up_sync(FULLMASK, incl, o);
-      if (lane >= o) incl += t;
-    }
-    const uint32_t total = __shfl_sync(FULLMASK, incl, 31);
-    uint32_t base = 0;
-    if (lane == 31 && total) base = atomicAdd(&res->n_work, total);
-    base = __shfl_sync(FULLMASK, base, 31) + incl - cnt;
-    uint32_t b = bits;
-    while (b) {
+    // split the word's bricks: those of tiles with more than 8 ops (the front) and the rest
+    uint32_t heavy = 0;
+    for (uint32_t b = bits; b;) {
       const int k = __ffs(b) - 1;
       b &= b - 1;
-      const uint32_t ci = wi * 32u + (uint32_t)k, byz = ci / BX;
-      work[base++] = (ci - byz * BX) | ((byz % BY) << 10) | ((byz / BY) << 20);
+      const uint32_t ci = wi * 32u + (uint32_t)k, byz = ci / BX, bx = ci - byz * BX, by = byz % BY, bz = byz / BY;
+      if (__ldg(tile_cnt + (bx >> 2) + TX * ((by >> 2) + TY * (bz >> 2))) > 8u) heavy |= 1u << k;
+    }
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+      const uint32_t mine = e ? bits & ~heavy : heavy;
+      const uint32_t cnt = __popc(mine);
+      uint32_t incl = cnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(FULLMASK, incl, o);
+        if (lane >= o) incl += t;
+      }
+      const uint32_t total = __shfl_sync(FULLMASK, incl, 31);
+      uint32_t base = 0;
+      if (lane == 31 && total) {
+        base = atomicAdd(counts + e, total);
+        atomicAdd(&res->n_work, total);
+      }
+      base = __shfl_sync(FULLMASK, base, 31) + incl - cnt;
+      for (uint32_t b = mine; b;) {
+        const int k = __ffs(b) - 1;
+        b &= b - 1;
+        const uint32_t ci = wi * 32u + (uint32_t)k, byz = ci / BX;
+        work[e ? last - base : base] = (ci - byz * BX) | ((byz % BY) << 10) | ((byz / BY) << 20);
+        base++;
+      }
     }
   }
 }
@@ -762,7 +797,7 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
   WarpCounters wc = {0, 0, 0, 0, 0};
   uint32_t paint_calls = 0, paint_viol = 0;
   uint32_t st_local = 0;
-  const uint32_t n_work = __ldg(&a.res->n_work);
+  const uint32_t n_front = __ldg(a.work_counter + 1), n_work = n_front + __ldg(a.work_counter + 2);
 
   for (;;) {
     uint32_t wbase = 0;
@@ -773,7 +808,8 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
     uint32_t q_pk = 0, q_g = 0, q_toff = 0, q_tcnt = 0;
     FoldEntry q = {0ull, 0u, 0u, 0u, NO_SLOT, 0u, PC_SKIP};
     if (grp < n_here) {
-      q_pk = __ldg(a.work + wbase + grp);
+      const uint32_t wi = wbase + grp;
+      q_pk = __ldg(a.work + (wi < n_front ? wi : a.touched_cap - (wi - n_front)));
       const uint32_t bx = q_pk & 1023u, by = (q_pk >> 10) & 1023u, bz = q_pk >> 20;
       q_g = a.grid[bx + (uint32_t)a.BX * (by + (uint32_t)a.BY * bz)];
       const uint32_t tile = (bx >> 2) + (uint32_t)a.TX * ((by >> 2) + (uint32_t)a.TY * (bz >> 2));
@@ -1046,8 +1082,10 @@ void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEve
   {
     const uint32_t n_words = (uint32_t)(((size_t)a.BX * a.BY * a.BZ + 31) / 32);
     const uint32_t blocks = (n_words + 255) / 256;  // 8 warps per block, 32 words per warp
-    ++g_launches; mark_compact_kernel<<<blocks < 4096 ? blocks : 4096, 256, 0, s>>>(a.bmark, n_words, (uint32_t)a.BX,
-                                                                              (uint32_t)a.BY, a.work, a.res);
+    ++g_launches;
+    mark_compact_kernel<<<blocks < 4096 ? blocks : 4096, 256, 0, s>>>(a.bmark, n_words, (uint32_t)a.BX, (uint32_t)a.BY,
+                                                                        (uint32_t)a.TX, (uint32_t)a.TY, a.tile_cnt, a.work,
+                                                                        a.touched_cap, a.work_counter + 1, a.res);
   }
   if (a.inline_paints) { ++g_launches; fold_kernel<true><<<grid(PX_FOLD_MINB), 256, 0, s>>>(a); }
   else { ++g_launches; fold_kernel<false><<<grid(PX_FOLD_MINB), 256, 0, s>>>(a); }

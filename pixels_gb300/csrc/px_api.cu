@@ -836,6 +836,25 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
   return PX_OK;
 }
 
+// Relative cost of one evaluation of an op's shape (ordering only: the
+// costliest work is taken first so that no long item starts last).
+static float op_cost(const px_world* w, const OpDev& o) {
+  float c = 0.f;
+  for (uint32_t i = 0; i < o.code_len; i++) {
+    const uint32_t x = w->code[o.code_off + i].x, op = x & 0xffu, cnt = x >> 8;
+    if (op == OP_LATHE_SOLID || op == OP_PRISM) c += 0.7f * (float)cnt;
+    else if (op == OP_LATHE_SHELL) c += 0.6f * (float)cnt;
+    else if (op == OP_ELLIPSOID || op == OP_CAPSULE || op == OP_STADIUM || (op >= OP_TORUS_X && op <= OP_TORUS_Z)) c += 1.5f;
+    else if (op < OP_ROT_X) c += 1.f;
+    else if (op <= OP_ROT_Z) c += 0.5f;
+    else c += 0.1f;
+  }
+  if (o.flags & OPF_FP64_ONLY) c *= 8.f;
+  if (o.flags & OPF_CONTAINS) c *= 0.5f;
+  return c;
+}
+static int cost_bucket(float c) { return c >= 15.75f ? 63 : (int)(c * 4.f); }
+
 int px_build_enqueue(px_world* w, int mode, void* stream) {
   if (!w) return PX_E_INVALID_ARG;
   if (w->batch_locked && !w->capturing) return fail(w, PX_E_INVALID_ARG, "the world belongs to a batch");
@@ -912,7 +931,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
       (rc = ensure(w, w->stage_cell, 4 * stage_cap)) || (rc = ensure(w, w->stage_src, 8 * stage_cap)) ||
       (rc = ensure(w, w->touched, 8 * touched_bound)) ||
       (rc = ensure(w, w->work_counter, 16)) || (rc = ensure(w, w->res, sizeof(BuildResult))) ||
-      (rc = ensure(w, w->chunk_op, 4 * ((P + 31) / 32))) || (rc = ensure(w, w->pcode, P)) ||
+      (rc = ensure(w, w->chunk_op, 8 * ((P + 31) / 32))) || (rc = ensure(w, w->pcode, P)) ||
       (rc = ensure(w, w->psub, 2 * P)) || (rc = ensure(w, w->pmask, 64 * P)) || (rc = ensure(w, w->chunk_counter, 512)) || (rc = ensure(w, w->pitems, 8 * P)) ||
       (rc = ensure(w, w->vitems, 16 * 8 * P)) || (rc = ensure(w, w->paint_items, 8 * 8 * n_slots + 8)) ||
       (rc = ensure(w, w->pvals, 2048 * n_slots + 4)) || (rc = ensure(w, w->bmark, 4 * ((w->ncells + 31) / 32))) ||
@@ -973,16 +992,28 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   CU(cudaMemsetAsync(w->res.p, 0, sizeof(BuildResult), s));
   CU(cudaMemsetAsync(w->work_counter.p, 0, 16, s));
   CU(cudaMemsetAsync(w->chunk_counter.p, 0, 512, s));
-  if (upload) {  // op of the first pair of every 32-pair chunk
-    const size_t n_chunks = (P + 31) / 32;
-    w->h_chunk_op.resize(n_chunks);
+  const size_t n_chunks = (P + 31) / 32;
+  if (upload) {
+    // op of the first pair of every 32-pair chunk, then the order classify_kernel
+    // takes the chunks in: costliest ops first (a bucket sort, stable within a bucket)
+    w->h_chunk_op.resize(2 * n_chunks);
     uint32_t o = 0;
+    std::vector<uint32_t> bucket_n(64, 0);
     for (size_t c = 0; c < n_chunks; c++) {
       const uint64_t p0 = (uint64_t)c * 32;
       while (o + 1 < (uint32_t)n_ops && w->ops[o + 1].pair_base <= p0) o++;
       w->h_chunk_op[c] = o;
+      bucket_n[cost_bucket(op_cost(w, w->ops[o]))]++;
     }
-    if (n_chunks) CU(cudaMemcpyAsync(w->chunk_op.p, w->h_chunk_op.data(), 4 * n_chunks, cudaMemcpyHostToDevice, s));
+    uint32_t at = 0;
+    for (int b = 63; b >= 0; b--) {
+      const uint32_t n = bucket_n[b];
+      bucket_n[b] = at;
+      at += n;
+    }
+    for (size_t c = 0; c < n_chunks; c++)
+      w->h_chunk_op[n_chunks + bucket_n[cost_bucket(op_cost(w, w->ops[w->h_chunk_op[c]]))]++] = (uint32_t)c;
+    if (n_chunks) CU(cudaMemcpyAsync(w->chunk_op.p, w->h_chunk_op.data(), 8 * n_chunks, cudaMemcpyHostToDevice, s));
   }
   if (P) CU(cudaMemsetAsync(w->evt.p, 0, P, s));
   CU(cudaMemsetAsync(w->bmark.p, 0, 4 * ((w->ncells + 31) / 32), s));
@@ -997,6 +1028,16 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
                    (uint32_t*)w->tile_ops.p, (uint2*)w->tile_boxes.p, s);
   FoldArgs fa{};
   fa.chunk_op = (const uint32_t*)w->chunk_op.p;
+  fa.chunk_order = fa.chunk_op + n_chunks;
+  {  // the sub-block and voxel passes take the classes costliest first
+    float cc[VCLASSES] = {0.f};
+    for (int i = 0; i < n_ops; i++)
+      if (w->ops[i].bx0 <= w->ops[i].bx1) cc[w->ops[i].vclass] = std::max(cc[w->ops[i].vclass], op_cost(w, w->ops[i]));
+    int order[VCLASSES];
+    for (int k = 0; k < VCLASSES; k++) order[k] = k;
+    std::stable_sort(order, order + VCLASSES, [&](int x, int y) { return cc[x] > cc[y]; });
+    for (int k = 0; k < VCLASSES; k++) fa.class_order[k] = (uint8_t)order[k];
+  }
   fa.n_ops = (uint32_t)n_ops;
   fa.n_pairs = P;
   fa.pcode = (uint8_t*)w->pcode.p;

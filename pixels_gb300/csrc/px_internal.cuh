@@ -138,6 +138,8 @@ constexpr int VCLASSES = 32;
 
 struct FoldArgs {
   const uint32_t* chunk_op;   // op containing pair 32 * chunk
+  const uint32_t* chunk_order;  // the order classify_kernel takes the chunks in (costliest ops first)
+  uint8_t class_order[VCLASSES];  // the order the sub-block and voxel passes take the classes in
   uint32_t n_ops;
   unsigned long long n_pairs;
   uint8_t* pcode;             // per pair: PC_*
@@ -154,13 +156,15 @@ struct FoldArgs {
   uint32_t pq_base[VCLASSES], pq_cap[VCLASSES];  // per-class regions of pitems
   uint32_t* paint_counter;    // paint_kernel items taken
   uint32_t n_paint_slots;     // (op, brick) pairs of painted ops with a slot
-  uint2* paint_items;         // sub-blocks to paint: (op, pair << 3 | sub-block), from classify and sub
+  uint2* paint_items;         // sub-blocks to paint: (op, pair << 3 | sub-block), from classify and sub;
+                              // float64 paints from the front, certified float32 ones from the back
   uint32_t paint_items_cap;
-  uint32_t* paint_item_counter;  // items pushed
+  uint32_t* paint_item_counter;  // items pushed: [0] at the front, [1] at the back
   uint32_t* pvals;            // 512 paint values per slot (voxel index order); PV_RANGE flags
   int inline_paints;          // some painted op has no slot: fold_kernel calls its paints itself
   uint32_t* bmark;            // one bit per brick: some pair of it is not skipped (classify_kernel)
-  uint32_t* work;             // those bricks (cell indices), listed by mark_compact_kernel
+  uint32_t* work;             // those bricks, listed by mark_compact_kernel: bricks of tiles with more
+                              // than 8 ops from the front, the others from the back (touched_cap down)
   const OpDev* ops;
   const uint2* code;
   const double* params;
@@ -186,7 +190,7 @@ struct FoldArgs {
   int64_t* stage_src;
   uint2* touched;             // (cell, final tag): 0, UNIFORM|v, or STAGED|slot
   uint32_t touched_cap;
-  uint32_t* work_counter;
+  uint32_t* work_counter;     // [0] apply-pass takes, [1] front bricks, [2] back bricks
   BuildResult* res;
 };
 
