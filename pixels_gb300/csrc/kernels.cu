@@ -349,17 +349,20 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
     if (__any_sync(FULLMASK, fullp)) {
       const bool back = MODE == 1 && O->paint32_off != NO_SLOT;
 #pragma unroll
-      for (int e = 0; e < 2; e++) {
+      for (int e = 0; e < 2; e++) {  // front: 16 half sub-blocks per pair; back: 8 sub-blocks
         const uint32_t fm = __ballot_sync(FULLMASK, fullp && back == (e == 1));
         if (!fm) continue;
+        const uint32_t per = e ? 8u : 16u;
         uint32_t pb = 0;
-        if (lane == 0) pb = atomicAdd(a.paint_item_counter + e, 8u * __popc(fm));
+        if (lane == 0) pb = atomicAdd(a.paint_item_counter + e, per * __popc(fm));
         pb = __shfl_sync(FULLMASK, pb, 0);
         if (fullp && back == (e == 1)) {
-          const uint32_t at = pb + 8u * __popc(fm & ((1u << lane) - 1u));
-          for (uint32_t q = 0; q < 8; q++)
-            if (at + q < a.paint_items_cap)
-              a.paint_items[e ? a.paint_items_cap - 1 - (at + q) : at + q] = make_uint2(o, (uint32_t)(p << 3) | q);
+          const uint32_t at = pb + per * __popc(fm & ((1u << lane) - 1u));
+          for (uint32_t q = 0; q < per; q++)
+            if (at + q < a.paint_items_cap) {
+              if (e) a.paint_items[a.paint_items_cap - 1 - (at + q)] = make_uint2(o, (uint32_t)(p << 3) | q);
+              else a.paint_items[at + q] = make_uint2(o | ((q & 1u) << 31), (uint32_t)(p << 3) | (q >> 1));
+            }
         }
       }
     }
@@ -459,15 +462,22 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
     if (__any_sync(FULLMASK, paint)) {  // the covered sub-blocks of a painted op go to the paint pass
       const bool back = MODE == 1 && a.ops[oo].paint32_off != NO_SLOT;
 #pragma unroll
-      for (int e = 0; e < 2; e++) {
+      for (int e = 0; e < 2; e++) {  // front: two half sub-blocks; back: the sub-block
         const uint32_t qm = __ballot_sync(FULLMASK, paint && back == (e == 1));
         if (!qm) continue;
+        const uint32_t per = e ? 1u : 2u;
         uint32_t pb = 0;
-        if (lane == 0) pb = atomicAdd(a.paint_item_counter + e, (uint32_t)__popc(qm));
+        if (lane == 0) pb = atomicAdd(a.paint_item_counter + e, per * __popc(qm));
         pb = __shfl_sync(FULLMASK, pb, 0);
-        const uint32_t at = pb + __popc(qm & ((1u << lane) - 1u));
-        if (paint && back == (e == 1) && at < a.paint_items_cap)
-          a.paint_items[e ? a.paint_items_cap - 1 - at : at] = make_uint2(oo, (uint32_t)(pp << 3) | (uint32_t)s);
+        const uint32_t at = pb + per * __popc(qm & ((1u << lane) - 1u));
+        if (paint && back == (e == 1)) {
+          if (e) {
+            if (at < a.paint_items_cap) a.paint_items[a.paint_items_cap - 1 - at] = make_uint2(oo, (uint32_t)(pp << 3) | (uint32_t)s);
+          } else {
+            for (uint32_t h = 0; h < 2; h++)
+              if (at + h < a.paint_items_cap) a.paint_items[at + h] = make_uint2(oo | (h << 31), (uint32_t)(pp << 3) | (uint32_t)s);
+          }
+        }
       }
     }
     // mixed form: a partial sub-block whose centre value is farther from 0 than
@@ -648,7 +658,9 @@ __global__ void __launch_bounds__(256) paint_kernel(FoldArgs a) {
     const uint32_t it = wb.next(a.paint_counter, 2, lane);
     if (it >= n_items) break;
     const uint2 item = __ldg(a.paint_items + (it < n_front ? it : a.paint_items_cap - 1 - (it - n_front)));
-    const OpDev* O = a.ops + item.x;
+    // a float64 item (the front) is half a sub-block: voxel rows r = bit 31 of its op field
+    const int r0 = it < n_front ? (int)(item.x >> 31) : 0, r1 = it < n_front ? r0 + 1 : 2;
+    const OpDev* O = a.ops + (item.x & 0x7fffffffu);
     const unsigned long long pair = item.y >> 3;
     const int s = (int)(item.y & 7u);
     const uint32_t slot = O->paint_slot + (uint32_t)(pair - O->pair_base);
@@ -666,7 +678,7 @@ __global__ void __launch_bounds__(256) paint_kernel(FoldArgs a) {
     Iv bo[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
     if (try32) brick_bases(a, O, bx, by, bz, bo);
 #pragma unroll 1
-    for (int r = 0; r < 2; r++) {
+    for (int r = r0; r < r1; r++) {
       const int e = r * 32 + lane;
       if (!((m >> e) & 1ull)) continue;
       const int lx = (s & 1) * 4 + (e & 3), ly = ((s >> 1) & 1) * 4 + ((e >> 2) & 3), lz = ((s >> 2) & 1) * 4 + (e >> 4);

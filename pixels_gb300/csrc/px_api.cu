@@ -68,7 +68,9 @@ struct px_world {
   DevBuf staging, stage_cell, stage_src, touched;
   uint64_t stage_hint = 0;      // staging slots the next build reserves (grown on overflow)
   DevBuf chunk_op, pcode, psub, pmask, chunk_counter, vitems, pitems;
-  std::vector<uint32_t> h_chunk_op;
+  std::vector<uint32_t> h_chunk_op;  // op of each 32-pair chunk, then the chunks' classify order
+  std::vector<uint8_t> h_op_bucket;  // per op: cost bucket (0..63) of one evaluation
+  uint8_t class_order[VCLASSES] = {0};  // sub-block / voxel class order of the resident ops
   DevBuf paint_items, pvals;    // sub-blocks to paint and the paint values
   DevBuf bmark, work;           // bricks the apply pass visits (bitmap, list)
   DevBuf scan_agg;
@@ -350,6 +352,7 @@ int px_world_create(int dx, int dy, int dz, double vpm, uint32_t initial_pool_br
   w->dx = dx; w->dy = dy; w->dz = dz;
   w->BX = dx / 8; w->BY = dy / 8; w->BZ = dz / 8;
   w->TX = (w->BX + 3) / 4; w->TY = (w->BY + 3) / 4; w->TZ = (w->BZ + 3) / 4;
+  for (int k = 0; k < VCLASSES; k++) w->class_order[k] = (uint8_t)k;
   w->vpm = vpm;
   w->vs = 1 / vpm;  // config.ts:13
   w->ncells = (size_t)w->BX * w->BY * w->BZ;
@@ -933,7 +936,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
       (rc = ensure(w, w->work_counter, 16)) || (rc = ensure(w, w->res, sizeof(BuildResult))) ||
       (rc = ensure(w, w->chunk_op, 8 * ((P + 31) / 32))) || (rc = ensure(w, w->pcode, P)) ||
       (rc = ensure(w, w->psub, 2 * P)) || (rc = ensure(w, w->pmask, 64 * P)) || (rc = ensure(w, w->chunk_counter, 512)) || (rc = ensure(w, w->pitems, 8 * P)) ||
-      (rc = ensure(w, w->vitems, 16 * 8 * P)) || (rc = ensure(w, w->paint_items, 8 * 8 * n_slots + 8)) ||
+      (rc = ensure(w, w->vitems, 16 * 8 * P)) || (rc = ensure(w, w->paint_items, 8 * 16 * n_slots + 8)) ||
       (rc = ensure(w, w->pvals, 2048 * n_slots + 4)) || (rc = ensure(w, w->bmark, 4 * ((w->ncells + 31) / 32))) ||
       (rc = ensure(w, w->work, 4 * touched_bound + 4)))
     return rc;
@@ -997,13 +1000,19 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
     // op of the first pair of every 32-pair chunk, then the order classify_kernel
     // takes the chunks in: costliest ops first (a bucket sort, stable within a bucket)
     w->h_chunk_op.resize(2 * n_chunks);
-    uint32_t o = 0;
-    std::vector<uint32_t> bucket_n(64, 0);
+    w->h_op_bucket.resize(n_ops);
+    float cc[VCLASSES] = {0.f};
+    for (int i = 0; i < n_ops; i++) {
+      const float c = op_cost(w, w->ops[i]);
+      w->h_op_bucket[i] = (uint8_t)cost_bucket(c);
+      if (w->ops[i].bx0 <= w->ops[i].bx1) cc[w->ops[i].vclass] = std::max(cc[w->ops[i].vclass], c);
+    }
+    uint32_t o = 0, bucket_n[64] = {0};
     for (size_t c = 0; c < n_chunks; c++) {
       const uint64_t p0 = (uint64_t)c * 32;
       while (o + 1 < (uint32_t)n_ops && w->ops[o + 1].pair_base <= p0) o++;
       w->h_chunk_op[c] = o;
-      bucket_n[cost_bucket(op_cost(w, w->ops[o]))]++;
+      bucket_n[w->h_op_bucket[o]]++;
     }
     uint32_t at = 0;
     for (int b = 63; b >= 0; b--) {
@@ -1012,8 +1021,13 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
       at += n;
     }
     for (size_t c = 0; c < n_chunks; c++)
-      w->h_chunk_op[n_chunks + bucket_n[cost_bucket(op_cost(w, w->ops[w->h_chunk_op[c]]))]++] = (uint32_t)c;
+      w->h_chunk_op[n_chunks + bucket_n[w->h_op_bucket[w->h_chunk_op[c]]]++] = (uint32_t)c;
     if (n_chunks) CU(cudaMemcpyAsync(w->chunk_op.p, w->h_chunk_op.data(), 8 * n_chunks, cudaMemcpyHostToDevice, s));
+    // the sub-block and voxel passes take the classes costliest first
+    int order[VCLASSES];
+    for (int k = 0; k < VCLASSES; k++) order[k] = k;
+    std::stable_sort(order, order + VCLASSES, [&](int x, int y) { return cc[x] > cc[y]; });
+    for (int k = 0; k < VCLASSES; k++) w->class_order[k] = (uint8_t)order[k];
   }
   if (P) CU(cudaMemsetAsync(w->evt.p, 0, P, s));
   CU(cudaMemsetAsync(w->bmark.p, 0, 4 * ((w->ncells + 31) / 32), s));
@@ -1029,15 +1043,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   FoldArgs fa{};
   fa.chunk_op = (const uint32_t*)w->chunk_op.p;
   fa.chunk_order = fa.chunk_op + n_chunks;
-  {  // the sub-block and voxel passes take the classes costliest first
-    float cc[VCLASSES] = {0.f};
-    for (int i = 0; i < n_ops; i++)
-      if (w->ops[i].bx0 <= w->ops[i].bx1) cc[w->ops[i].vclass] = std::max(cc[w->ops[i].vclass], op_cost(w, w->ops[i]));
-    int order[VCLASSES];
-    for (int k = 0; k < VCLASSES; k++) order[k] = k;
-    std::stable_sort(order, order + VCLASSES, [&](int x, int y) { return cc[x] > cc[y]; });
-    for (int k = 0; k < VCLASSES; k++) fa.class_order[k] = (uint8_t)order[k];
-  }
+  for (int k = 0; k < VCLASSES; k++) fa.class_order[k] = w->class_order[k];
   fa.n_ops = (uint32_t)n_ops;
   fa.n_pairs = P;
   fa.pcode = (uint8_t*)w->pcode.p;
@@ -1069,7 +1075,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   fa.paint_counter = (uint32_t*)w->chunk_counter.p + 1;
   fa.n_paint_slots = (uint32_t)n_slots;
   fa.paint_items = (uint2*)w->paint_items.p;
-  fa.paint_items_cap = (uint32_t)std::min<uint64_t>(8 * n_slots, 0xffffffffull);
+  fa.paint_items_cap = (uint32_t)std::min<uint64_t>(16 * n_slots, 0xffffffffull);  // float64 items come in halves
   fa.paint_item_counter = (uint32_t*)w->chunk_counter.p + 2;
   fa.pvals = (uint32_t*)w->pvals.p;
   fa.inline_paints = inline_paints ? 1 : 0;
