@@ -762,7 +762,79 @@ class HostPool {
   uint64_t gen_ = 0;
 };
 
+// Blocks of the single-pass scans of a build with P pairs and E_max events.
+size_t scan_blocks(const px_world* w, uint64_t P, size_t E_max) {
+  size_t items = w->ntiles > E_max ? w->ntiles : E_max;
+  if (P > items) items = P;
+  return items / scan_items_per_block() + 2;
+}
+
+// The build scratch that scales with the (op, brick) pairs P, the tile-list
+// entries, the paint slots, the touched bricks, the allocator events E_max and
+// the staging slots.
+int ensure_pair_scratch(px_world* w, uint64_t P, uint64_t tile_pairs, uint64_t n_slots,
+                               uint64_t touched_bound, size_t E_max, uint64_t stage_cap) {
+  int rc;
+  if ((rc = ensure(w, w->tile_cnt, 4 * w->ntiles)) || (rc = ensure(w, w->tile_off, 4 * w->ntiles)) ||
+      (rc = ensure(w, w->tiles_nonempty, 4 * w->ntiles)) || (rc = ensure(w, w->tile_ops, 4 * tile_pairs)) || (rc = ensure(w, w->tile_boxes, 8 * tile_pairs)) ||
+      (rc = ensure(w, w->evt, P)) || (rc = ensure(w, w->fsrc, 8 * P)) || (rc = ensure(w, w->cnt, 4 * P)) ||
+      (rc = ensure(w, w->pos, 4 * P)) || (rc = ensure(w, w->etype, E_max)) || (rc = ensure(w, w->ew, 8 * E_max)) ||
+      (rc = ensure(w, w->depth_fn, 8 * E_max)) || (rc = ensure(w, w->depth, 4 * (E_max + 32))) ||
+      (rc = ensure(w, w->tree, 4 * (E_max / 16 + 512 + E_max))) || (rc = ensure(w, w->fresh, 4 * E_max)) ||
+      (rc = ensure(w, w->fresh_rank, 4 * E_max)) || (rc = ensure(w, w->staging, 1024 * stage_cap)) ||
+      (rc = ensure(w, w->stage_cell, 4 * stage_cap)) || (rc = ensure(w, w->stage_src, 8 * stage_cap)) ||
+      (rc = ensure(w, w->touched, 8 * touched_bound)) ||
+      (rc = ensure(w, w->work_counter, 16)) || (rc = ensure(w, w->res, sizeof(BuildResult))) ||
+      (rc = ensure(w, w->chunk_op, 8 * ((P + 31) / 32))) || (rc = ensure(w, w->pcode, P)) ||
+      (rc = ensure(w, w->psub, 2 * P)) || (rc = ensure(w, w->pmask, 64 * P)) || (rc = ensure(w, w->chunk_counter, 512)) || (rc = ensure(w, w->pitems, 8 * P)) ||
+      (rc = ensure(w, w->vitems, 16 * 8 * P)) || (rc = ensure(w, w->paint_items, 8 * 16 * n_slots + 8)) ||
+      (rc = ensure(w, w->pvals, 2048 * n_slots + 4)) || (rc = ensure(w, w->bmark, 4 * ((w->ncells + 31) / 32))) ||
+      (rc = ensure(w, w->work, 4 * touched_bound + 4)))
+    return rc;
+  return ensure(w, w->scan_agg, scan_temp_bytes(scan_blocks(w, P, E_max)));
+}
+
+// Staging slots a build with P pairs reserves (a guess: a build that needs more
+// commits nothing and is retried with larger buffers).
+uint64_t stage_slots(const px_world* w, uint64_t P) {
+  const uint64_t touched_bound = P < w->ncells ? P : w->ncells;
+  uint64_t stage_cap = std::max(std::max((uint64_t)4096, w->stage_hint), (uint64_t)(P / 4));
+  if (stage_cap > touched_bound) stage_cap = touched_bound ? touched_bound : 1;
+  return stage_cap;
+}
+
 }  // namespace
+
+namespace px {
+// Serving: the scratch of any build of at most P pairs and no paint slots,
+// allocated ahead so that no serving step stops to allocate.  Also grows the
+// pool so that such a build's staging guess fits.
+int reserve_build_scratch(px_world* w, uint64_t P, uint32_t max_ops) {
+  if (w->in_flight || w->batch_locked) return fail(w, PX_E_INVALID_ARG, "the world is busy");
+  {  // op tables of up to max_ops one-instruction ops with up to 16 parameters and 64 bricks per axis
+    const size_t n = max_ops ? max_ops : 1;
+    const void* before[7] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p, w->d_p32.p, w->d_bases.p};
+    int rc0;
+    if ((rc0 = ensure(w, w->d_ops, sizeof(OpDev) * n)) || (rc0 = ensure(w, w->d_boxes, sizeof(uint2) * (n + (n + 31) / 32))) ||
+        (rc0 = ensure(w, w->d_code, sizeof(uint2) * n)) || (rc0 = ensure(w, w->d_params, sizeof(double) * 16 * n)) ||
+        (rc0 = ensure(w, w->d_code32, sizeof(uint32_t) * n)) || (rc0 = ensure(w, w->d_p32, sizeof(float2) * 16 * n)) ||
+        (rc0 = ensure(w, w->d_bases, sizeof(float2) * 192 * n)))
+      return rc0;
+    const void* after[7] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p, w->d_p32.p, w->d_bases.p};
+    for (int k = 0; k < 7; k++)
+      if (after[k] != before[k]) w->ops_resident = false;  // a reallocated table lost its resident copy
+  }
+  const uint64_t touched_bound = P < w->ncells ? P : w->ncells;
+  const size_t E_max = (size_t)w->pool_cap + 2 * P;  // the holes are pool bricks
+  const uint64_t stage_cap = stage_slots(w, P);
+  int rc = grow_pool(w, (uint64_t)w->pool_used + stage_cap, w->pool_used, nullptr);
+  if (rc) return rc;
+  if ((rc = ensure_pair_scratch(w, P, P, 0, touched_bound, E_max, stage_cap))) return rc;
+  if ((rc = ensure(w, w->holes_a, 4 * E_max + 4))) return rc;
+  return ensure(w, w->holes_b, 4 * E_max + 4);
+}
+uint64_t build_stage_slots(const px_world* w, uint64_t P) { return stage_slots(w, P); }
+}  // namespace px
 
 extern "C" {
 
@@ -858,6 +930,7 @@ static float op_cost(const px_world* w, const OpDev& o) {
 }
 static int cost_bucket(float c) { return c >= 15.75f ? 63 : (int)(c * 4.f); }
 
+
 int px_build_enqueue(px_world* w, int mode, void* stream) {
   if (!w) return PX_E_INVALID_ARG;
   if (w->batch_locked && !w->capturing) return fail(w, PX_E_INVALID_ARG, "the world belongs to a batch");
@@ -910,8 +983,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
 
   // staging slots and pool bricks are reserved from a guess; a build that needs
   // more commits nothing and is retried with larger buffers (px_build_finish)
-  uint64_t stage_cap = std::max(std::max((uint64_t)4096, w->stage_hint), (uint64_t)(P / 4));
-  if (stage_cap > touched_bound) stage_cap = touched_bound ? touched_bound : 1;
+  const uint64_t stage_cap = stage_slots(w, P);
   if ((rc = grow_pool(w, (uint64_t)U0 + stage_cap, U0, s))) return rc;
 
   // scratch (a reallocated op table loses its resident copy)
@@ -924,29 +996,9 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
       (rc = ensure(w, w->d_code32, sizeof(uint32_t) * w->code32.size())) ||
       (rc = ensure(w, w->d_p32, sizeof(float2) * w->p32.size())) ||
       (rc = ensure(w, w->d_bases, sizeof(float2) * w->bases.size())) ||
-      (rc = ensure(w, w->tile_cnt, 4 * w->ntiles)) || (rc = ensure(w, w->tile_off, 4 * w->ntiles)) ||
-      (rc = ensure(w, w->tiles_nonempty, 4 * w->ntiles)) || (rc = ensure(w, w->tile_ops, 4 * tile_pairs)) || (rc = ensure(w, w->tile_boxes, 8 * tile_pairs)) ||
-      (rc = ensure(w, w->evt, P)) || (rc = ensure(w, w->fsrc, 8 * P)) || (rc = ensure(w, w->cnt, 4 * P)) ||
-      (rc = ensure(w, w->pos, 4 * P)) || (rc = ensure(w, w->etype, E_max)) || (rc = ensure(w, w->ew, 8 * E_max)) ||
-      (rc = ensure(w, w->depth_fn, 8 * E_max)) || (rc = ensure(w, w->depth, 4 * (E_max + 32))) ||
-      (rc = ensure(w, w->tree, 4 * (E_max / 16 + 512 + E_max))) || (rc = ensure(w, w->fresh, 4 * E_max)) ||
-      (rc = ensure(w, w->fresh_rank, 4 * E_max)) || (rc = ensure(w, w->staging, 1024 * stage_cap)) ||
-      (rc = ensure(w, w->stage_cell, 4 * stage_cap)) || (rc = ensure(w, w->stage_src, 8 * stage_cap)) ||
-      (rc = ensure(w, w->touched, 8 * touched_bound)) ||
-      (rc = ensure(w, w->work_counter, 16)) || (rc = ensure(w, w->res, sizeof(BuildResult))) ||
-      (rc = ensure(w, w->chunk_op, 8 * ((P + 31) / 32))) || (rc = ensure(w, w->pcode, P)) ||
-      (rc = ensure(w, w->psub, 2 * P)) || (rc = ensure(w, w->pmask, 64 * P)) || (rc = ensure(w, w->chunk_counter, 512)) || (rc = ensure(w, w->pitems, 8 * P)) ||
-      (rc = ensure(w, w->vitems, 16 * 8 * P)) || (rc = ensure(w, w->paint_items, 8 * 16 * n_slots + 8)) ||
-      (rc = ensure(w, w->pvals, 2048 * n_slots + 4)) || (rc = ensure(w, w->bmark, 4 * ((w->ncells + 31) / 32))) ||
-      (rc = ensure(w, w->work, 4 * touched_bound + 4)))
+      (rc = ensure_pair_scratch(w, P, tile_pairs, n_slots, touched_bound, E_max, stage_cap)))
     return rc;
-  size_t scan_nb;
-  {
-    size_t items = w->ntiles > E_max ? w->ntiles : E_max;
-    if (P > items) items = P;
-    scan_nb = items / scan_items_per_block() + 2;
-    if ((rc = ensure(w, w->scan_agg, scan_temp_bytes(scan_nb)))) return rc;
-  }
+  const size_t scan_nb = scan_blocks(w, P, E_max);
   {
     const void* after[9] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p,
                             w->d_p32.p, w->d_bases.p, w->chunk_op.p, w->chunk_op.p};

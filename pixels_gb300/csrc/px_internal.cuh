@@ -270,3 +270,14 @@ float probe_fma_tflops(int fp64, int n_sms);
 unsigned long long launch_count();
 
 }  // namespace px
+
+struct px_world;
+namespace px {
+// Serving (px_api.cu): allocate ahead the scratch of any build of at most P
+// (op, brick) pairs and max_ops one-instruction ops without paint slots, and
+// the pool room its staging guess needs; the staging slots such a build
+// reserves.
+int reserve_build_scratch(px_world* w, uint64_t P, uint32_t max_ops);
+uint64_t build_stage_slots(const px_world* w, uint64_t P);
+
+}  // namespace px

@@ -14,6 +14,7 @@
 #include <cmath>
 #include <condition_variable>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -110,6 +111,24 @@ int px_serve_run(px_world* w, const px_edit* edits, const double* arrival_s, siz
     const int rc0 = px_reserve_pool(w, cap);
     if (rc0 != PX_OK) return rc0;
   }
+  // The build scratch of the largest batch the stream can form (the max_batch
+  // largest edits' pairs, at most kPairBudget), also allocated before the clock:
+  // a step that had to allocate device memory would stall the loop for a
+  // millisecond or more.  A batch is closed before its pairs pass that budget.
+  constexpr uint64_t kPairBudget = 1ull << 22;
+  uint64_t pair_budget = 0;
+  {
+    std::vector<uint64_t> nb(n);
+    for (size_t i = 0; i < n; i++) nb[i] = brick_bound(edits[i], vs, dims[0], dims[1], dims[2]);
+    const size_t top = std::min<size_t>(n, max_batch);
+    std::partial_sort(nb.begin(), nb.begin() + top, nb.end(), std::greater<uint64_t>());
+    for (size_t i = 0; i < top; i++) pair_budget += nb[i];
+    pair_budget = std::min(std::max<uint64_t>(pair_budget, 1), kPairBudget);
+    const int rc0 = reserve_build_scratch(w, pair_budget, max_batch);
+    if (rc0 != PX_OK) return rc0;
+    px_get_stats(w, &st);
+  }
+  uint64_t pool_cap = st.pool_capacity;
 
   // arrival order
   std::vector<size_t> order(n);
@@ -174,6 +193,11 @@ int px_serve_run(px_world* w, const px_edit* edits, const double* arrival_s, siz
         }
         break;  // wait for the next batch
       }
+      // the batch stays within the reserved scratch and pool room (an edit too
+      // large for them is built alone, growing the buffers)
+      if (!batch.empty() && (bound + b > pair_budget ||
+                             (uint64_t)st.pool_used + build_stage_slots(w, bound + b) > pool_cap))
+        break;
       bound += b;
       batch.push_back(i);
       encode_carve(edits[i], vs, ops, code, params);
@@ -193,6 +217,7 @@ int px_serve_run(px_world* w, const px_edit* edits, const double* arrival_s, siz
     const double done = secs(t0, clock_t_::now());
     px_get_stats(w, &st);
     live = (uint64_t)st.pool_used - st.n_holes;
+    pool_cap = st.pool_capacity;
     for (size_t i : batch) {
       results[i].start_s = start;
       results[i].done_s = done;
