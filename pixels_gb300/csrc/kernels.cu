@@ -169,6 +169,18 @@ struct WorkBatch {
   }
 };
 
+// The next work ticket of a warp, requested one item ahead: lane 0 issues the
+// atomic when the current item starts and the warp reads its result when the
+// item is done, so the atomic's latency (one counter for the whole grid) hides
+// behind the item's work.
+struct NextTicket {
+  uint32_t raw = 0;
+  __device__ __forceinline__ void issue(uint32_t* counter, uint32_t n, int lane) {
+    if (lane == 0) raw = atomicAdd(counter, n);
+  }
+  __device__ __forceinline__ uint32_t get() const { return __shfl_sync(FULLMASK, raw, 0); }
+};
+
 // Decisions of apply() from a float32 interval (thresholds certified on the host):
 // brick/sub-block: 0 = outside (skip), 1 = partial, 2 = full, 3 = undecided.
 __device__ __forceinline__ int classify32(Iv d, const float* thr, int base) {
@@ -413,11 +425,12 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
   }
   const uint32_t n_items = __shfl_sync(FULLMASK, incl, 31);
   const int g = lane >> 3, s = lane & 7;
+  NextTicket tk;
+  tk.issue(&a.pitem_counter[0], 4u, lane);
   for (;;) {
-    uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(&a.pitem_counter[0], 4u);
-    base = __shfl_sync(FULLMASK, base, 0);
+    const uint32_t base = tk.get();
     if (base >= n_items) break;
+    tk.issue(&a.pitem_counter[0], 4u, lane);
     // the class and queue position of each of the pass's four items
     uint32_t my_k = 0, my_first = 0;
 #pragma unroll
@@ -537,10 +550,12 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_VOXEL_MINB : PX_CLASSIFY64
     if (lane >= o) incl += t;
   }
   const uint32_t n_items = __shfl_sync(FULLMASK, incl, 31);
-  WorkBatch wb;
+  NextTicket tk;
+  tk.issue(&a.vitem_counter[0], 1, lane);
   for (;;) {
-    const uint32_t it = wb.next(&a.vitem_counter[0], 1, lane);
+    const uint32_t it = tk.get();
     if (it >= n_items) break;
+    tk.issue(&a.vitem_counter[0], 1, lane);
     const int k = __popc(__ballot_sync(FULLMASK, lane < VCLASSES && incl <= it));  // class of item `it`
     const uint32_t first = __shfl_sync(FULLMASK, incl - own, k);
     const uint4 item = __ldg(a.vitems + a.vq_base[a.class_order[k]] + (it - first));

@@ -57,13 +57,31 @@ __device__ __forceinline__ double stripe_index(double y, double x, uint32_t& st)
   return floor(((ac + PI) / (2 * PI)) * 8);
 }
 
+// Math.hypot(a, b) < r and Math.hypot(a, b) > r, decided from s = a*a + b*b
+// against r*r where that is certain, else from the engine's hypot itself.
+// The engine's result H is within 2^-50 (relative) of the exact E = sqrt(a^2 +
+// b^2), and s within 2^-52 of E^2 (plus underflow, absolute 2^-1073): s below
+// r*r (1 - 2^-40) gives E < r (1 - 2^-42), so H < r; s above r*r (1 + 2^-40)
+// gives E > r (1 + 2^-43), so H > r.  Inputs are finite (|a|, |b| <= 2^11 m)
+// and r > 2^-100 (checked), so nothing overflows and the underflow is far
+// below the margin.
+__device__ __forceinline__ int hypot_vs(double a, double b, double r) {  // -1: H < r, 1: H > r, 0: H == r
+  if (r > 0x1p-100 && r < 0x1p100 && fabs(a) < 0x1p11 && fabs(b) < 0x1p11) {
+    const double s = a * a + b * b, r2 = r * r;
+    if (s < r2 * (1.0 - 0x1p-40)) return -1;
+    if (s > r2 * (1.0 + 0x1p-40)) return 1;
+  }
+  const double h = px_hypot2(a, b);
+  return h < r ? -1 : (h > r ? 1 : 0);
+}
+
 // One paint call at a voxel centre (metres, after the optional frame).
 __device__ __noinline__ uint32_t paint_eval(uint32_t kind, const double* __restrict__ p, double x, double y, double z,
                                             uint32_t& st) {
   const double PI = 3.141592653589793;
   switch (kind) {
     case PK_CHIP: {  // penthouse.ts:371-377 (stripe only matters on the edge of even layers)
-      bool edge = px_hypot2(x - __ldg(p), z - __ldg(p + 2)) > __ldg(p + 3);
+      bool edge = hypot_vs(x - __ldg(p), z - __ldg(p + 2), __ldg(p + 3)) > 0;
       double layer = fmod(floor((y - __ldg(p + 1)) / 0.0045), 2.0);
       bool stripe = false;
       if (edge && layer == 0) stripe = fmod(stripe_index(z - __ldg(p + 2), x - __ldg(p), st), 2.0) == 0;
@@ -74,7 +92,7 @@ __device__ __noinline__ uint32_t paint_eval(uint32_t kind, const double* __restr
       double ru = px_round(u), rv = px_round(v);
       double du = u - ru, dv = v - rv;
       bool odd = fmod(ru + rv, 2.0) == 0;
-      return vox_of(__ldg(p + 2), odd && px_hypot2(du, dv) < 0.12 ? 200 : 0);
+      return vox_of(__ldg(p + 2), odd && hypot_vs(du, dv, 0.12) < 0 ? 200 : 0);
     }
     case PK_CARD: {  // penthouse.ts:597-600
       bool edge = fabs(x - __ldg(p) - __ldg(p + 2)) > 0.022 || fabs(z - __ldg(p + 1)) > 0.034;
@@ -118,7 +136,7 @@ __device__ __noinline__ uint32_t paint_eval(uint32_t kind, const double* __restr
       double shade = 0;
       for (int i = 0; i < 9; i++) {
         const double* b = p + 1 + 4 * i;
-        if (px_hypot2(x - __ldg(b), (y - __ldg(b + 1)) * 1.3) < __ldg(b + 2)) shade = __ldg(b + 3);
+        if (hypot_vs(x - __ldg(b), (y - __ldg(b + 1)) * 1.3, __ldg(b + 2)) < 0) shade = __ldg(b + 3);
       }
       double arg = x * 9 + y * 3;
       double s = fabs(sin(arg));
@@ -157,6 +175,12 @@ __device__ __noinline__ uint32_t paint_eval_cr(uint32_t kind, const double* __re
       bool stripe = fmod(floor(((a + PI) / (2 * PI)) * 8), 2.0) == 0;
       double layer = fmod(floor((y - __ldg(p + 1)) / 0.0045), 2.0);
       return vox_of(__ldg(p + 4), edge && stripe && layer == 0 ? 255 : 0);
+    }
+    case PK_TUFTED: {  // the engine's hypot itself
+      double u = (z - __ldg(p)) / 0.16, v = (y - __ldg(p + 1)) / 0.16;
+      double ru = px_round(u), rv = px_round(v);
+      bool odd = fmod(ru + rv, 2.0) == 0;
+      return vox_of(__ldg(p + 2), odd && px_hypot2(u - ru, v - rv) < 0.12 ? 200 : 0);
     }
     case PK_VASE: {
       double a = atan2_cr(z - __ldg(p + 2), x - __ldg(p));

@@ -420,7 +420,8 @@ void px_world_destroy(px_world* w) {
 // op, relative to its anchor A.  Returns false (float64 only) for a paint
 // frame or values outside the certified range.
 bool paint_params32(uint32_t kind, bool framed, const double* p, const double A[3], std::vector<float2>& out) {
-  if (framed || (kind != PK_TUFTED && kind != PK_PAINTING)) return false;
+  if (framed || (kind != PK_TUFTED && kind != PK_PAINTING && kind != PK_VASE)) return false;
+  if (kind == PK_VASE && !(p[3] > 0x1p-20 && p[3] < 0x1p20)) return false;
   bool ok = true;
   auto put = [&](float2 e, double v) {
     if (!std::isfinite(e.x) || !std::isfinite(e.y) || std::fabs(v) > MIXED_MAX_COORD) ok = false;
@@ -441,6 +442,14 @@ bool paint_params32(uint32_t kind, bool framed, const double* p, const double A[
     put(enc(r, r * 0x1p-52), r);
     thr(0.12);
     intv(p[2]);
+  } else if (kind == PK_VASE) {  // penthouse.ts:810-816
+    pos(p[0], 0);
+    pos(p[1], 1);
+    pos(p[2], 2);
+    const double r = 1.0 / p[3];  // the real 1/height lies within 2^-53 (relative) of r
+    put(enc(r, r * 0x1p-52), r);
+    for (double c : {0.04, 0.06, 0.36, 0.38, 0.47, 0.49, 0.08, 0.33, 0.55}) thr(c);
+    intv(p[4]);
   } else {  // penthouse.ts:840-845
     const long double K = 9.0L * (long double)A[0] + 3.0L * (long double)A[1];
     const long double k = std::floor(K / (2.0L * 3.14159265358979323846264338327950288L) + 0.5L);
