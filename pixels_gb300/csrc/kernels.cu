@@ -1328,12 +1328,9 @@ __global__ void evt_count_kernel(const uint8_t* __restrict__ evt, size_t P, uint
     cnt[p] = __popc(evt[p] & 3u);
 }
 
-__global__ void n_events_kernel(const uint32_t* pos, const uint32_t* cnt, size_t P, uint32_t H, BuildResult* res) {
-  res->n_events = H + (P ? pos[P - 1] + cnt[P - 1] : 0u);
-}
-
 __global__ void events_build_kernel(ReplayArgs a) {
   const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+  if (tid == 0) a.res->n_events = a.H + (a.P ? a.pos[a.P - 1] + a.cnt[a.P - 1] : 0u);
   for (size_t i = tid; i < a.H; i += stride) {
     a.etype[i] = EV_PUSH;
     a.depth_fn[i] = make_int2(1, -(1 << 30));
@@ -1358,19 +1355,19 @@ __global__ void events_build_kernel(ReplayArgs a) {
   }
 }
 
-__global__ void depth_apply_kernel(const int2* __restrict__ fn, int32_t* depth, const BuildResult* res) {
+// Stack depth after each event (the scanned maps applied to the empty stack)
+// and the pops that find the stack empty (they take poolUsed++).
+__global__ void depth_fresh_kernel(const int2* __restrict__ fn, const uint8_t* __restrict__ etype, int32_t* depth,
+                                   uint32_t* fresh, const BuildResult* res) {
   const size_t E = res->n_events;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (size_t)gridDim.x * blockDim.x) {
-    int2 f = fn[e];
+    const int2 f = __ldg(fn + e);
     depth[e] = max(f.y, f.x);  // applied to the empty stack (depth 0)
-  }
-}
-
-__global__ void fresh_flags_kernel(const uint8_t* __restrict__ etype, const int32_t* __restrict__ depth, uint32_t* fresh,
-                                   const BuildResult* res) {
-  const size_t E = res->n_events;
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (size_t)gridDim.x * blockDim.x) {
-    int dprev = e ? depth[e - 1] : 0;
+    int dprev = 0;
+    if (e) {
+      const int2 g = __ldg(fn + e - 1);
+      dprev = max(g.y, g.x);
+    }
     fresh[e] = (etype[e] == EV_POP && dprev == 0) ? 1u : 0u;
   }
 }
@@ -1498,15 +1495,18 @@ static size_t level_size_host(size_t E, int l) {
 
 void launch_replay(const ReplayArgs& a, cudaStream_t s) {
   const int T = 256;
-  auto blocks = [&](size_t n) { size_t b = (n + T - 1) / T; return (int)(b < 4096 ? (b ? b : 1) : 4096); };
+  // grid-stride kernels: at most one wave of 8 CTAs per SM (the event count is
+  // known on the device only, and is usually far below E_max)
+  int dev = 0, n_sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&n_sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t cap = (size_t)n_sms * 8;
+  auto blocks = [&](size_t n) { size_t b = (n + T - 1) / T; return (int)(b < cap ? (b ? b : 1) : cap); };
   ++g_launches; evt_count_kernel<<<blocks(a.P), T, 0, s>>>(a.evt, a.P, a.cnt);
   scan_any<SumOp, false>(a.cnt, a.pos, a.P, nullptr, false, nullptr, *a.scan, s);
-  ++g_launches; n_events_kernel<<<1, 1, 0, s>>>(a.pos, a.cnt, a.P, a.H, a.res);
-  ++g_launches; events_build_kernel<<<blocks(a.P > a.H ? a.P : a.H), T, 0, s>>>(a);
+  ++g_launches; events_build_kernel<<<blocks(a.P > a.H ? a.P : a.H), T, 0, s>>>(a);  // also the event count
   const uint32_t* nE = &a.res->n_events;
   scan_any<DepthOp, false>(a.depth_fn, a.depth_fn, a.E_max, nE, true, nullptr, *a.scan, s);
-  ++g_launches; depth_apply_kernel<<<blocks(a.E_max), T, 0, s>>>(a.depth_fn, a.depth, a.res);
-  ++g_launches; fresh_flags_kernel<<<blocks(a.E_max), T, 0, s>>>(a.etype, a.depth, a.fresh, a.res);
+  ++g_launches; depth_fresh_kernel<<<blocks(a.E_max), T, 0, s>>>(a.depth_fn, a.etype, a.depth, a.fresh, a.res);
   scan_any<SumOp, false>(a.fresh, a.fresh_rank, a.E_max, nE, false, &a.res->n_fresh, *a.scan, s);
   // min tree over the depths
   TreeLevels tl;
