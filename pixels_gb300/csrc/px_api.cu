@@ -30,6 +30,13 @@ struct DevBuf {
   size_t bytes = 0;
 };
 
+// one host-to-device copy of a build's op tables
+struct Upload {
+  void* dst;
+  const void* src;
+  size_t bytes;
+};
+
 }  // namespace
 
 struct px_world {
@@ -69,6 +76,7 @@ struct px_world {
   uint64_t stage_hint = 0;      // staging slots the next build reserves (grown on overflow)
   DevBuf chunk_op, pcode, psub, pmask, chunk_counter, vitems, pitems;
   std::vector<uint32_t> h_chunk_op;  // op of each 32-pair chunk, then the chunks' classify order
+  std::vector<Upload> h_uploads;     // the op-table copies of the build being enqueued
   std::vector<uint8_t> h_op_bucket;  // per op: cost bucket (0..63) of one evaluation
   uint8_t class_order[VCLASSES] = {0};  // sub-block / voxel class order of the resident ops
   DevBuf paint_items, pvals;    // sub-blocks to paint and the paint values
@@ -78,6 +86,10 @@ struct px_world {
   DevBuf res;
   DevBuf opaque, udens, super_counts, density;
   BuildResult* h_res = nullptr;   // pinned
+  // pinned staging of the op-table uploads: a copy from pageable memory would
+  // hold the host until the driver has staged it, one array at a time
+  unsigned char* h_stage = nullptr;
+  size_t h_stage_bytes = 0;
   std::vector<unsigned char> h_upload;
 
   // in-flight build
@@ -408,6 +420,7 @@ void px_world_destroy(px_world* w) {
                     &w->udens, &w->super_counts, &w->density, &w->paint_items, &w->pvals, &w->tile_boxes, &w->bmark, &w->work, &w->pitems};
   for (DevBuf* b : bufs) release(*b);
   if (w->h_res) cudaFreeHost(w->h_res);
+  if (w->h_stage) cudaFreeHost(w->h_stage);
   if (w->ev0) cudaEventDestroy(w->ev0);
   if (w->ev1) cudaEventDestroy(w->ev1);
   if (w->ev_fold0) cudaEventDestroy(w->ev_fold0);
@@ -939,6 +952,35 @@ static float op_cost(const px_world* w, const OpDev& o) {
 }
 static int cost_bucket(float c) { return c >= 15.75f ? 63 : (int)(c * 4.f); }
 
+// The host-to-device copies of one build's op tables, packed into the world's
+// pinned staging buffer and issued as asynchronous copies from it.  The
+// staging buffer is only rewritten by the next build, which starts after this
+// one has finished (px_build_finish synchronizes).
+static int flush_uploads(px_world* w, const std::vector<Upload>& ups, cudaStream_t s) {
+  size_t total = 0;
+  for (const Upload& u : ups) total += (u.bytes + 255) & ~(size_t)255;
+  if (total > w->h_stage_bytes) {
+    if (w->h_stage) cudaFreeHost(w->h_stage);
+    w->h_stage = nullptr;
+    w->h_stage_bytes = 0;
+    const size_t want = total + total / 4;
+    if (cudaMallocHost((void**)&w->h_stage, want) != cudaSuccess) {
+      cudaGetLastError();
+      w->h_stage = nullptr;
+      return fail(w, PX_E_OOM, "pinned staging of %zu bytes", want);
+    }
+    w->h_stage_bytes = want;
+  }
+  size_t at = 0;
+  for (const Upload& u : ups) {
+    if (!u.bytes) continue;
+    std::memcpy(w->h_stage + at, u.src, u.bytes);
+    CU(cudaMemcpyAsync(u.dst, w->h_stage + at, u.bytes, cudaMemcpyHostToDevice, s));
+    at += (u.bytes + 255) & ~(size_t)255;
+  }
+  return PX_OK;
+}
+
 
 int px_build_enqueue(px_world* w, int mode, void* stream) {
   if (!w) return PX_E_INVALID_ARG;
@@ -1022,8 +1064,10 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   const unsigned long long launches0 = launch_count();
   if (!w->capturing) CU(cudaEventRecord(w->ev0, s));
   const bool upload = !w->ops_resident;
+  std::vector<Upload>& ups = w->h_uploads;
+  ups.clear();
   if (upload) {
-    CU(cudaMemcpyAsync(w->d_ops.p, w->ops.data(), sizeof(OpDev) * (size_t)n_ops, cudaMemcpyHostToDevice, s));
+    ups.push_back({w->d_ops.p, w->ops.data(), sizeof(OpDev) * (size_t)n_ops});
     {  // op boxes, then the union box of every 32 consecutive ops (cull_count_kernel)
       const int n_groups = (n_ops + 31) / 32;
       w->h_boxes.assign(w->boxes.begin(), w->boxes.end());
@@ -1042,16 +1086,13 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
         w->h_boxes.push_back(any ? make_uint2(lo[0] | (lo[1] << 10) | (lo[2] << 20), hi[0] | (hi[1] << 10) | (hi[2] << 20))
                                  : make_uint2(3u << 30, 0u));
       }
-      CU(cudaMemcpyAsync(w->d_boxes.p, w->h_boxes.data(), sizeof(uint2) * w->h_boxes.size(), cudaMemcpyHostToDevice, s));
+      ups.push_back({w->d_boxes.p, w->h_boxes.data(), sizeof(uint2) * w->h_boxes.size()});
     }
-    CU(cudaMemcpyAsync(w->d_code.p, w->code.data(), sizeof(uint2) * w->code.size(), cudaMemcpyHostToDevice, s));
-    CU(cudaMemcpyAsync(w->d_params.p, w->params.data(), sizeof(double) * w->params.size(), cudaMemcpyHostToDevice, s));
-    if (!w->code32.empty()) {
-      CU(cudaMemcpyAsync(w->d_code32.p, w->code32.data(), sizeof(uint32_t) * w->code32.size(), cudaMemcpyHostToDevice, s));
-      CU(cudaMemcpyAsync(w->d_p32.p, w->p32.data(), sizeof(float2) * w->p32.size(), cudaMemcpyHostToDevice, s));
-    }
-    if (!w->bases.empty())
-      CU(cudaMemcpyAsync(w->d_bases.p, w->bases.data(), sizeof(float2) * w->bases.size(), cudaMemcpyHostToDevice, s));
+    ups.push_back({w->d_code.p, w->code.data(), sizeof(uint2) * w->code.size()});
+    ups.push_back({w->d_params.p, w->params.data(), sizeof(double) * w->params.size()});
+    ups.push_back({w->d_code32.p, w->code32.data(), sizeof(uint32_t) * w->code32.size()});
+    ups.push_back({w->d_p32.p, w->p32.data(), sizeof(float2) * w->p32.size()});
+    ups.push_back({w->d_bases.p, w->bases.data(), sizeof(float2) * w->bases.size()});
   }
   CU(cudaMemsetAsync(w->res.p, 0, sizeof(BuildResult), s));
   CU(cudaMemsetAsync(w->work_counter.p, 0, 16, s));
@@ -1083,12 +1124,18 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
     }
     for (size_t c = 0; c < n_chunks; c++)
       w->h_chunk_op[n_chunks + bucket_n[w->h_op_bucket[w->h_chunk_op[c]]]++] = (uint32_t)c;
-    if (n_chunks) CU(cudaMemcpyAsync(w->chunk_op.p, w->h_chunk_op.data(), 8 * n_chunks, cudaMemcpyHostToDevice, s));
+    ups.push_back({w->chunk_op.p, w->h_chunk_op.data(), 8 * n_chunks});
     // the sub-block and voxel passes take the classes costliest first
     int order[VCLASSES];
     for (int k = 0; k < VCLASSES; k++) order[k] = k;
     std::stable_sort(order, order + VCLASSES, [&](int x, int y) { return cc[x] > cc[y]; });
     for (int k = 0; k < VCLASSES; k++) w->class_order[k] = (uint8_t)order[k];
+  }
+  if (w->capturing) {  // a captured copy reads its host source at every replay: copy from the arrays themselves
+    for (const Upload& u : ups)
+      if (u.bytes) CU(cudaMemcpyAsync(u.dst, u.src, u.bytes, cudaMemcpyHostToDevice, s));
+  } else if ((rc = flush_uploads(w, ups, s))) {
+    return rc;
   }
   if (P) CU(cudaMemsetAsync(w->evt.p, 0, P, s));
   CU(cudaMemsetAsync(w->bmark.p, 0, 4 * ((w->ncells + 31) / 32), s));
