@@ -294,9 +294,10 @@ def serving_section(args, pyoracle):
     return out
 
 
-# DRAM bytes per build of the evaluation kernels, from one ncu capture of each
-# (profiles/build_kernels_penthouse_vpm80.md); the bench cannot run ncu itself
-EVAL_TRAFFIC_BYTES = 29_622_784
+# DRAM bytes per build of the evaluation kernels (classify, sub-block, voxel,
+# paint, apply), from one ncu capture of each (profiles/build_kernels_penthouse_vpm80.md);
+# the bench cannot run ncu itself
+EVAL_TRAFFIC_BYTES = 33_562_880
 
 
 def hbm_line(cfg, pool_used, ir_bytes, ms):
@@ -538,9 +539,11 @@ def main():
                              if e2e_parts else None)},
         "roofline": {"bound": "fp32-alu", "achieved": round(achieved, 4), "peak": round(peak32, 2),
                      "unit": "TFLOP/s", "frac": round(achieved / peak32, 5), "traffic": EVAL_TRAFFIC_BYTES,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the classify, voxel, "
-                                       "paint and apply kernels of one build (profiles/build_kernels_penthouse_vpm80.md)",
-                     "kernel": "classify_kernel + voxel_kernel + fold_kernel (every SDF and paint evaluation)",
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the classify, sub-block, "
+                                       "voxel, paint and apply kernels of one build "
+                                       "(profiles/build_kernels_penthouse_vpm80.md)",
+                     "kernel": "classify_kernel + sub_kernel + voxel_kernel + paint_kernel + fold_kernel "
+                               "(every SDF and paint evaluation)",
                      "alg_ops_per_launch": int(alg_ops),
                      "fold_ms": round(fold_s * 1e3, 4),
                      "peak_source": "measured here: dependent FFMA chains on all SMs (px_probe_peak)",

@@ -86,11 +86,10 @@ struct px_world {
   DevBuf res;
   DevBuf opaque, udens, super_counts, density;
   BuildResult* h_res = nullptr;   // pinned
-  // pinned staging of the op-table uploads: a copy from pageable memory would
-  // hold the host until the driver has staged it, one array at a time
+  // pinned staging of the op-table uploads: a copy from pageable memory holds
+  // the host until the driver has staged it, one array at a time
   unsigned char* h_stage = nullptr;
   size_t h_stage_bytes = 0;
-  std::vector<unsigned char> h_upload;
 
   // in-flight build
   bool in_flight = false;
@@ -487,6 +486,25 @@ bool paint_params32(uint32_t kind, bool framed, const double* p, const double A[
 
 namespace {
 
+// Relative cost of one evaluation of an op's shape (ordering only: the
+// costliest work is taken first so that no long item starts last); code: the
+// op's instructions (opcode | count << 8, parameter offset).
+float op_cost(const uint32_t* code, uint32_t code_len, uint32_t flags) {
+  float c = 0.f;
+  for (uint32_t i = 0; i < code_len; i++) {
+    const uint32_t x = code[2 * (size_t)i], op = x & 0xffu, cnt = x >> 8;
+    if (op == OP_LATHE_SOLID || op == OP_PRISM) c += 0.7f * (float)cnt;
+    else if (op == OP_LATHE_SHELL) c += 0.6f * (float)cnt;
+    else if (op == OP_ELLIPSOID || op == OP_CAPSULE || op == OP_STADIUM || (op >= OP_TORUS_X && op <= OP_TORUS_Z)) c += 1.5f;
+    else if (op < OP_ROT_X) c += 1.f;
+    else if (op <= OP_ROT_Z) c += 0.5f;
+    else c += 0.1f;
+  }
+  if (flags & OPF_FP64_ONLY) c *= 8.f;
+  if (flags & OPF_CONTAINS) c *= 0.5f;
+  return c;
+}
+
 // One contiguous range of a submitted op list, converted by one host thread:
 // offsets into its own arrays, rebased when the ranges are merged in order.
 struct SubmitChunk {
@@ -713,6 +731,7 @@ int convert_ops(const px_world* w, const IrOp* iops, size_t i0, size_t i1, const
       (void)c32_before;
       (void)p32_before;
     }
+    d.cost = op_cost(code + 2 * (size_t)o.code_begin, o.code_len, d.flags);
     out.ops.push_back(d);
     out.boxes.push_back(box);
   }
@@ -933,30 +952,13 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
   return PX_OK;
 }
 
-// Relative cost of one evaluation of an op's shape (ordering only: the
-// costliest work is taken first so that no long item starts last).
-static float op_cost(const px_world* w, const OpDev& o) {
-  float c = 0.f;
-  for (uint32_t i = 0; i < o.code_len; i++) {
-    const uint32_t x = w->code[o.code_off + i].x, op = x & 0xffu, cnt = x >> 8;
-    if (op == OP_LATHE_SOLID || op == OP_PRISM) c += 0.7f * (float)cnt;
-    else if (op == OP_LATHE_SHELL) c += 0.6f * (float)cnt;
-    else if (op == OP_ELLIPSOID || op == OP_CAPSULE || op == OP_STADIUM || (op >= OP_TORUS_X && op <= OP_TORUS_Z)) c += 1.5f;
-    else if (op < OP_ROT_X) c += 1.f;
-    else if (op <= OP_ROT_Z) c += 0.5f;
-    else c += 0.1f;
-  }
-  if (o.flags & OPF_FP64_ONLY) c *= 8.f;
-  if (o.flags & OPF_CONTAINS) c *= 0.5f;
-  return c;
-}
 static int cost_bucket(float c) { return c >= 15.75f ? 63 : (int)(c * 4.f); }
 
-// The host-to-device copies of one build's op tables, packed into the world's
-// pinned staging buffer and issued as asynchronous copies from it.  The
-// staging buffer is only rewritten by the next build, which starts after this
-// one has finished (px_build_finish synchronizes).
-static int flush_uploads(px_world* w, const std::vector<Upload>& ups, cudaStream_t s) {
+// The host-to-device copies of one build's op tables: packed into the world's
+// pinned staging buffer, then copied asynchronously.  The staging buffer is
+// only rewritten by the next build, which starts after this one has finished
+// (px_build_finish synchronizes).
+static int issue_uploads(px_world* w, const std::vector<Upload>& ups, cudaStream_t s) {
   size_t total = 0;
   for (const Upload& u : ups) total += (u.bytes + 255) & ~(size_t)255;
   if (total > w->h_stage_bytes) {
@@ -1105,16 +1107,17 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
     w->h_op_bucket.resize(n_ops);
     float cc[VCLASSES] = {0.f};
     for (int i = 0; i < n_ops; i++) {
-      const float c = op_cost(w, w->ops[i]);
+      const float c = w->ops[i].cost;
       w->h_op_bucket[i] = (uint8_t)cost_bucket(c);
       if (w->ops[i].bx0 <= w->ops[i].bx1) cc[w->ops[i].vclass] = std::max(cc[w->ops[i].vclass], c);
     }
-    uint32_t o = 0, bucket_n[64] = {0};
-    for (size_t c = 0; c < n_chunks; c++) {
-      const uint64_t p0 = (uint64_t)c * 32;
-      while (o + 1 < (uint32_t)n_ops && w->ops[o + 1].pair_base <= p0) o++;
-      w->h_chunk_op[c] = o;
-      bucket_n[w->h_op_bucket[o]]++;
+    // op o owns the chunks whose first pair it holds: [ceil(base_o / 32), ceil(base_o+1 / 32))
+    auto first_chunk = [&](int i) { return (uint32_t)((w->ops[i].pair_base + 31) / 32); };
+    uint32_t bucket_n[64] = {0};
+    for (int i = 0; i < n_ops; i++) {
+      const uint32_t c0 = first_chunk(i), c1 = i + 1 < n_ops ? first_chunk(i + 1) : (uint32_t)n_chunks;
+      for (uint32_t c = c0; c < c1; c++) w->h_chunk_op[c] = (uint32_t)i;
+      bucket_n[w->h_op_bucket[i]] += c1 - c0;
     }
     uint32_t at = 0;
     for (int b = 63; b >= 0; b--) {
@@ -1122,8 +1125,12 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
       bucket_n[b] = at;
       at += n;
     }
-    for (size_t c = 0; c < n_chunks; c++)
-      w->h_chunk_op[n_chunks + bucket_n[w->h_op_bucket[w->h_chunk_op[c]]]++] = (uint32_t)c;
+    for (int i = 0; i < n_ops; i++) {  // each op's chunks, in order, at its bucket's next place
+      const uint32_t c0 = first_chunk(i), c1 = i + 1 < n_ops ? first_chunk(i + 1) : (uint32_t)n_chunks;
+      uint32_t* dst = w->h_chunk_op.data() + n_chunks + bucket_n[w->h_op_bucket[i]];
+      for (uint32_t c = c0; c < c1; c++) *dst++ = c;
+      bucket_n[w->h_op_bucket[i]] += c1 - c0;
+    }
     ups.push_back({w->chunk_op.p, w->h_chunk_op.data(), 8 * n_chunks});
     // the sub-block and voxel passes take the classes costliest first
     int order[VCLASSES];
@@ -1134,7 +1141,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   if (w->capturing) {  // a captured copy reads its host source at every replay: copy from the arrays themselves
     for (const Upload& u : ups)
       if (u.bytes) CU(cudaMemcpyAsync(u.dst, u.src, u.bytes, cudaMemcpyHostToDevice, s));
-  } else if ((rc = flush_uploads(w, ups, s))) {
+  } else if ((rc = issue_uploads(w, ups, s))) {
     return rc;
   }
   if (P) CU(cudaMemsetAsync(w->evt.p, 0, P, s));

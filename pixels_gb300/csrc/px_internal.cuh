@@ -79,7 +79,7 @@ struct OpDev {
   float thr[12];                         // mixed mode thresholds (T_*)
   int32_t cbx0, cby0, cbz0, cbx1, cby1, cbz1;  // bricks the box fully contains (contains(), shapes.ts:47-48,360)
   uint32_t base_off;                     // mixed mode: float32 first-voxel-centre offsets per brick row
-  uint32_t pad2;
+  float cost;                            // relative cost of one evaluation (work order only)
   // OPF_BOX_RANGES (a lone axis-aligned box): per axis, the first and last voxel
   // whose centre the reference's float64 box SDF puts inside on that axis
   int32_t vr[6];                         // x lo, x hi, y lo, y hi, z lo, z hi (empty: lo > hi)
