@@ -322,16 +322,18 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
   uint32_t st_local = 0;
   const unsigned long long P = a.n_pairs;
   const uint32_t n_chunks = (uint32_t)((P + 31) / 32);
+  NextTicket tk;
+  tk.issue(a.chunk_counter, 1u, lane);
   for (;;) {
-    uint32_t take = 0;
-    if (lane == 0) take = atomicAdd(a.chunk_counter, 1u);
-    take = __shfl_sync(FULLMASK, take, 0);
+    const uint32_t take = tk.get();
     if (take >= n_chunks) break;
-    const uint32_t chunk = __ldg(a.chunk_order + take);
+    tk.issue(a.chunk_counter, 1u, lane);
+    const uint2 ce = __ldg(a.chunk_order + take);
+    const uint32_t chunk = ce.x;
     const unsigned long long p = (unsigned long long)chunk * 32 + lane;
     const bool valid = p < P;
-    uint32_t o = __ldg(a.chunk_op + chunk);
-    if (valid)
+    uint32_t o = ce.y & 0x7fffffffu;
+    if (valid && !(ce.y >> 31))  // the chunk spans several ops
       while (o + 1 < a.n_ops && a.ops[o + 1].pair_base <= p) o++;
     const OpDev* O = a.ops + o;
     int bx = 0, by = 0, bz = 0, cls = PC_SKIP;

@@ -75,7 +75,7 @@ struct px_world {
   DevBuf staging, stage_cell, stage_src, touched;
   uint64_t stage_hint = 0;      // staging slots the next build reserves (grown on overflow)
   DevBuf chunk_op, pcode, psub, pmask, chunk_counter, vitems, pitems;
-  std::vector<uint32_t> h_chunk_op;  // op of each 32-pair chunk, then the chunks' classify order
+  std::vector<uint32_t> h_chunk_op;  // the chunks in classify order: (chunk, op of its first pair | single-op bit)
   std::vector<Upload> h_uploads;     // the op-table copies of the build being enqueued
   std::vector<uint8_t> h_op_bucket;  // per op: cost bucket (0..63) of one evaluation
   uint8_t class_order[VCLASSES] = {0};  // sub-block / voxel class order of the resident ops
@@ -1111,12 +1111,12 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
       w->h_op_bucket[i] = (uint8_t)cost_bucket(c);
       if (w->ops[i].bx0 <= w->ops[i].bx1) cc[w->ops[i].vclass] = std::max(cc[w->ops[i].vclass], c);
     }
-    // op o owns the chunks whose first pair it holds: [ceil(base_o / 32), ceil(base_o+1 / 32))
+    // op o owns the chunks whose first pair it holds: [ceil(base_o / 32), ceil(base_o+1 / 32));
+    // a chunk entry is (chunk, its first pair's op | bit 31 when all its pairs are that op's)
     auto first_chunk = [&](int i) { return (uint32_t)((w->ops[i].pair_base + 31) / 32); };
     uint32_t bucket_n[64] = {0};
     for (int i = 0; i < n_ops; i++) {
       const uint32_t c0 = first_chunk(i), c1 = i + 1 < n_ops ? first_chunk(i + 1) : (uint32_t)n_chunks;
-      for (uint32_t c = c0; c < c1; c++) w->h_chunk_op[c] = (uint32_t)i;
       bucket_n[w->h_op_bucket[i]] += c1 - c0;
     }
     uint32_t at = 0;
@@ -1127,8 +1127,12 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
     }
     for (int i = 0; i < n_ops; i++) {  // each op's chunks, in order, at its bucket's next place
       const uint32_t c0 = first_chunk(i), c1 = i + 1 < n_ops ? first_chunk(i + 1) : (uint32_t)n_chunks;
-      uint32_t* dst = w->h_chunk_op.data() + n_chunks + bucket_n[w->h_op_bucket[i]];
-      for (uint32_t c = c0; c < c1; c++) *dst++ = c;
+      const uint64_t end = i + 1 < n_ops ? w->ops[i + 1].pair_base : P;  // the op's pairs end here
+      uint32_t* dst = w->h_chunk_op.data() + 2 * (size_t)bucket_n[w->h_op_bucket[i]];
+      for (uint32_t c = c0; c < c1; c++) {
+        *dst++ = c;
+        *dst++ = (uint32_t)i | ((uint64_t)c * 32 + 32 <= end || end >= P ? 0x80000000u : 0u);
+      }
       bucket_n[w->h_op_bucket[i]] += c1 - c0;
     }
     ups.push_back({w->chunk_op.p, w->h_chunk_op.data(), 8 * n_chunks});
@@ -1156,8 +1160,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   launch_cull_fill((const uint2*)w->d_boxes.p, n_ops, w->TX, w->TY, w->TZ, (const uint32_t*)w->tile_off.p,
                    (uint32_t*)w->tile_ops.p, (uint2*)w->tile_boxes.p, s);
   FoldArgs fa{};
-  fa.chunk_op = (const uint32_t*)w->chunk_op.p;
-  fa.chunk_order = fa.chunk_op + n_chunks;
+  fa.chunk_order = (const uint2*)w->chunk_op.p;
   for (int k = 0; k < VCLASSES; k++) fa.class_order[k] = w->class_order[k];
   fa.n_ops = (uint32_t)n_ops;
   fa.n_pairs = P;

@@ -137,8 +137,9 @@ enum : uint8_t { PC_SKIP = 0, PC_PARTIAL = 1, PC_FULL = 2 };
 constexpr int VCLASSES = 32;
 
 struct FoldArgs {
-  const uint32_t* chunk_op;   // op containing pair 32 * chunk
-  const uint32_t* chunk_order;  // the order classify_kernel takes the chunks in (costliest ops first)
+  const uint2* chunk_order;  // the 32-pair chunks in the order classify_kernel takes them (costliest ops
+                             // first): (chunk, op containing its first pair | 1 << 31 when that op holds
+                             // all of the chunk's pairs)
   uint8_t class_order[VCLASSES];  // the order the sub-block and voxel passes take the classes in
   uint32_t n_ops;
   unsigned long long n_pairs;
