@@ -1234,13 +1234,25 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_onepass(const typename Op::
   const uint32_t tile = s_tile;
   if ((size_t)tile * SCAN_TILE >= n) return;  // every later tile is past the end too
   const size_t k0 = (size_t)tile * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
+  // a forward scan reads a thread's whole run as 16-byte vectors (runs start on 32-byte boundaries)
+  constexpr int NV = (int)(sizeof(T) * SCAN_ITEMS / 16);
+  const bool vec = !REV && k0 + SCAN_ITEMS <= n;
   T v[SCAN_ITEMS];
   T acc = Op::identity();
+  if (vec) {
+    uint4 buf[NV];
 #pragma unroll
-  for (int i = 0; i < SCAN_ITEMS; i++) {
-    const size_t k = k0 + i;
-    v[i] = k < n ? in[scan_idx<REV>(k, n)] : Op::identity();
-    acc = Op::combine(acc, v[i]);
+    for (int j = 0; j < NV; j++) buf[j] = reinterpret_cast<const uint4*>(in + k0)[j];
+    memcpy(v, buf, sizeof v);
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; i++) acc = Op::combine(acc, v[i]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; i++) {
+      const size_t k = k0 + i;
+      v[i] = k < n ? in[scan_idx<REV>(k, n)] : Op::identity();
+      acc = Op::combine(acc, v[i]);
+    }
   }
   T total;
   const T pre_block = block_exclusive<Op>(acc, sh, total);
@@ -1282,13 +1294,27 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_onepass(const typename Op::
   }
   __syncthreads();
   T pre = Op::combine(s_prefix, pre_block);
+  if (vec) {
 #pragma unroll
-  for (int i = 0; i < SCAN_ITEMS; i++) {
-    const size_t k = k0 + i;
-    const T nxt = Op::combine(pre, v[i]);
-    if (k < n) out[scan_idx<REV>(k, n)] = inclusive ? nxt : pre;
-    if (total_out && k + 1 == n) *total_out = nxt;
-    pre = nxt;
+    for (int i = 0; i < SCAN_ITEMS; i++) {
+      const T nxt = Op::combine(pre, v[i]);
+      if (total_out && k0 + i + 1 == n) *total_out = nxt;
+      v[i] = inclusive ? nxt : pre;
+      pre = nxt;
+    }
+    uint4 buf[NV];
+    memcpy(buf, v, sizeof v);
+#pragma unroll
+    for (int j = 0; j < NV; j++) reinterpret_cast<uint4*>(out + k0)[j] = buf[j];
+  } else {
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; i++) {
+      const size_t k = k0 + i;
+      const T nxt = Op::combine(pre, v[i]);
+      if (k < n) out[scan_idx<REV>(k, n)] = inclusive ? nxt : pre;
+      if (total_out && k + 1 == n) *total_out = nxt;
+      pre = nxt;
+    }
   }
 }
 
