@@ -1694,6 +1694,25 @@ __global__ void __launch_bounds__(256) derive_kernel(const uint32_t* __restrict_
   }
 }
 
+// The op-table uploads of a build in one launch, read straight from the host
+// arrays (pageable memory the GPU reads through the host page tables): entry
+// blockIdx.y, 16-byte words, then the last bytes of an entry.
+__global__ void __launch_bounds__(256) upload_kernel(HostUploads u) {
+  const HostUploads::Entry& e = u.e[blockIdx.y];
+  const size_t n16 = e.bytes >> 4;
+  const uint4* src = reinterpret_cast<const uint4*>(e.src);
+  uint4* dst = reinterpret_cast<uint4*>(e.dst);
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+  if (blockIdx.x == 0 && threadIdx.x < (e.bytes & 15u))
+    static_cast<unsigned char*>(e.dst)[(n16 << 4) + threadIdx.x] = static_cast<const unsigned char*>(e.src)[(n16 << 4) + threadIdx.x];
+}
+void launch_uploads(const HostUploads& u, cudaStream_t s) {
+  if (u.n == 0) return;
+  ++g_launches;
+  upload_kernel<<<dim3(32, (unsigned)u.n), 256, 0, s>>>(u);
+}
+
 void launch_derive(const uint32_t* grid, const uint32_t* pool32, int BX, int BY, int BZ, const uint8_t* opaque,
                    const uint8_t* udens, uint32_t* super_counts, uint8_t* density, cudaStream_t s) {
   int n_super = ((BX + 3) / 4) * ((BY + 3) / 4) * ((BZ + 3) / 4);

@@ -4,6 +4,7 @@
 // (voxel ranges, classify thresholds) must round exactly as the reference's
 // JavaScript does (shapes.ts:341-350).
 #include <algorithm>
+#include <cstdlib>
 #include <atomic>
 #include <condition_variable>
 #include <functional>
@@ -86,10 +87,8 @@ struct px_world {
   DevBuf res;
   DevBuf opaque, udens, super_counts, density;
   BuildResult* h_res = nullptr;   // pinned
-  // pinned staging of the op-table uploads: a copy from pageable memory holds
-  // the host until the driver has staged it, one array at a time
-  unsigned char* h_stage = nullptr;
-  size_t h_stage_bytes = 0;
+  bool host_reads = false;        // the device reads pageable host memory (host page tables)
+  bool uploads_pending = false;   // an upload kernel may still read the host op tables
 
   // in-flight build
   bool in_flight = false;
@@ -371,6 +370,12 @@ int px_world_create(int dx, int dy, int dz, double vpm, uint32_t initial_pool_br
   int dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&w->n_sms, cudaDevAttrMultiProcessorCount, dev);
+  {
+    int pma = 0, hpt = 0;
+    cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev);
+    cudaDeviceGetAttribute(&hpt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);
+    w->host_reads = pma == 1 && hpt == 1 && getenv("PIXELS_GB300_NO_HOST_READS") == nullptr;
+  }
   int rc;
   DevBuf g;
   if ((rc = ensure(w, g, w->ncells * 4)) != PX_OK) { delete w; return rc; }
@@ -407,7 +412,7 @@ int px_set_material_tables(px_world* w, const uint8_t* opaque256, const uint8_t*
 
 void px_world_destroy(px_world* w) {
   if (!w || w->batch_locked) return;  // a batch's world outlives the batch
-  if (w->in_flight) cudaStreamSynchronize(w->stream);
+  if (w->in_flight || w->uploads_pending) cudaStreamSynchronize(w->stream);
   cudaFree(w->d_grid);
   cudaFree(w->d_pool32);
   DevBuf* bufs[] = {&w->holes_a, &w->holes_b, &w->d_ops, &w->d_boxes, &w->d_code, &w->d_params, &w->d_code32,
@@ -419,7 +424,6 @@ void px_world_destroy(px_world* w) {
                     &w->udens, &w->super_counts, &w->density, &w->paint_items, &w->pvals, &w->tile_boxes, &w->bmark, &w->work, &w->pitems};
   for (DevBuf* b : bufs) release(*b);
   if (w->h_res) cudaFreeHost(w->h_res);
-  if (w->h_stage) cudaFreeHost(w->h_stage);
   if (w->ev0) cudaEventDestroy(w->ev0);
   if (w->ev1) cudaEventDestroy(w->ev1);
   if (w->ev_fold0) cudaEventDestroy(w->ev_fold0);
@@ -883,6 +887,10 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
   if (!w || (!ir && bytes)) return PX_E_INVALID_ARG;
   if (w->batch_locked) return fail(w, PX_E_INVALID_ARG, "the world belongs to a batch");
   if (w->in_flight) return fail(w, PX_E_INVALID_ARG, "a build is in flight");
+  if (w->uploads_pending) {  // a build that failed after its upload kernel was launched
+    CU(cudaStreamSynchronize(w->stream));
+    w->uploads_pending = false;
+  }
   w->ops_resident = false;
   if (bytes < 32) return fail(w, PX_E_INVALID_IR, "IR shorter than its header");
   const uint32_t* h = (const uint32_t*)ir;
@@ -954,32 +962,27 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
 
 static int cost_bucket(float c) { return c >= 15.75f ? 63 : (int)(c * 4.f); }
 
-// The host-to-device copies of one build's op tables: packed into the world's
-// pinned staging buffer, then copied asynchronously.  The staging buffer is
-// only rewritten by the next build, which starts after this one has finished
-// (px_build_finish synchronizes).
+// The host-to-device copies of one build's op tables.  Where the GPU reads
+// pageable memory through the host page tables (Grace), one kernel copies them
+// all from the host arrays (a few microseconds of host time instead of ~10 per
+// cudaMemcpyAsync); the arrays then stay untouched until the build has
+// finished (px_submit_ops and px_world_reset wait for it).  Elsewhere, and
+// while a graph is captured, plain copies.
 static int issue_uploads(px_world* w, const std::vector<Upload>& ups, cudaStream_t s) {
-  size_t total = 0;
-  for (const Upload& u : ups) total += (u.bytes + 255) & ~(size_t)255;
-  if (total > w->h_stage_bytes) {
-    if (w->h_stage) cudaFreeHost(w->h_stage);
-    w->h_stage = nullptr;
-    w->h_stage_bytes = 0;
-    const size_t want = total + total / 4;
-    if (cudaMallocHost((void**)&w->h_stage, want) != cudaSuccess) {
-      cudaGetLastError();
-      w->h_stage = nullptr;
-      return fail(w, PX_E_OOM, "pinned staging of %zu bytes", want);
-    }
-    w->h_stage_bytes = want;
+  bool direct = w->host_reads && !w->capturing && ups.size() <= 8;
+  for (const Upload& u : ups)
+    if (u.bytes && (((uintptr_t)u.src | (uintptr_t)u.dst) & 15u)) direct = false;
+  if (direct) {
+    HostUploads hu{};
+    for (const Upload& u : ups)
+      if (u.bytes) hu.e[hu.n++] = {u.src, u.dst, u.bytes};
+    launch_uploads(hu, s);
+    CU(cudaGetLastError());
+    w->uploads_pending = hu.n > 0;
+    return PX_OK;
   }
-  size_t at = 0;
-  for (const Upload& u : ups) {
-    if (!u.bytes) continue;
-    std::memcpy(w->h_stage + at, u.src, u.bytes);
-    CU(cudaMemcpyAsync(u.dst, w->h_stage + at, u.bytes, cudaMemcpyHostToDevice, s));
-    at += (u.bytes + 255) & ~(size_t)255;
-  }
+  for (const Upload& u : ups)
+    if (u.bytes) CU(cudaMemcpyAsync(u.dst, u.src, u.bytes, cudaMemcpyHostToDevice, s));
   return PX_OK;
 }
 
@@ -1142,12 +1145,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
     std::stable_sort(order, order + VCLASSES, [&](int x, int y) { return cc[x] > cc[y]; });
     for (int k = 0; k < VCLASSES; k++) w->class_order[k] = (uint8_t)order[k];
   }
-  if (w->capturing) {  // a captured copy reads its host source at every replay: copy from the arrays themselves
-    for (const Upload& u : ups)
-      if (u.bytes) CU(cudaMemcpyAsync(u.dst, u.src, u.bytes, cudaMemcpyHostToDevice, s));
-  } else if ((rc = issue_uploads(w, ups, s))) {
-    return rc;
-  }
+  if ((rc = issue_uploads(w, ups, s))) return rc;
   if (P) CU(cudaMemsetAsync(w->evt.p, 0, P, s));
   CU(cudaMemsetAsync(w->bmark.p, 0, 4 * ((w->ncells + 31) / 32), s));
 
@@ -1317,6 +1315,7 @@ int px_build_finish(px_world* w) {
   if (!w->in_flight) return PX_OK;
   w->in_flight = false;
   CU(cudaStreamSynchronize(w->stream));
+  w->uploads_pending = false;
   const BuildResult& r = *w->h_res;
   float ms = 0.f, fold_ms = 0.f;
   cudaEventElapsedTime(&ms, w->ev0, w->ev1);
@@ -1402,6 +1401,10 @@ int px_world_reset(px_world* w, int requeue_last_ops, void* stream) {
   if (!w) return PX_E_INVALID_ARG;
   if (w->batch_locked && !w->capturing) return fail(w, PX_E_INVALID_ARG, "the world belongs to a batch");
   if (w->in_flight) return fail(w, PX_E_INVALID_ARG, "a build is in flight");
+  if (w->uploads_pending) {  // a build that failed after its upload kernel was launched
+    CU(cudaStreamSynchronize(w->stream));
+    w->uploads_pending = false;
+  }
   CU(cudaMemsetAsync(w->d_grid, 0, w->ncells * 4, (cudaStream_t)stream));
   w->pool_used = 0;
   w->n_holes = 0;

@@ -263,6 +263,19 @@ struct FinalizeArgs {
 };
 void launch_finalize(const FinalizeArgs& a, uint32_t touched_cap, cudaStream_t s);
 
+// Host-to-device copies done by one kernel that reads the host arrays directly
+// (only where the device reports pageable memory access through the host page
+// tables); sources and destinations 16-byte aligned.
+struct HostUploads {
+  struct Entry {
+    const void* src;
+    void* dst;
+    size_t bytes;
+  } e[8];
+  int n;
+};
+void launch_uploads(const HostUploads& u, cudaStream_t s);
+
 void launch_derive(const uint32_t* grid, const uint32_t* pool32, int BX, int BY, int BZ,
                    const uint8_t* opaque, const uint8_t* udens, uint32_t* super_counts,
                    uint8_t* density, cudaStream_t s);

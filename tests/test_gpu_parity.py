@@ -55,11 +55,13 @@ def test_penthouse_vpm20_bit_exact(built_lib, mode):
 
 
 @pytest.mark.gpu
-def test_mixed_enclosures_hold_everywhere(built_lib):
+@pytest.mark.parametrize("vpm", [20.0, 40.0])
+def test_mixed_enclosures_hold_everywhere(built_lib, vpm):
     """Validation mode: every float32 interval must enclose the float64 value
-    (within the certified margin); the build must still be bit-exact."""
+    (within the certified margin), every certified float32 paint decision and
+    every filtered Math.hypot decision must equal the correctly rounded float64
+    one; the build must still be bit-exact."""
     from pixels_gb300 import _lib
-    vpm = 20.0
     prog, _ = penthouse_program(vpm)
     o = pyoracle.OracleWorld(prog.to_bytes(), vpm, config.Config(vpm).dims)
     cfg = config.Config(vpm)
@@ -81,3 +83,17 @@ def test_penthouse_vpm40_mixed_bit_exact(built_lib, vpm):
     assert_same_world(w, o)
     s = w.stats()
     assert s["rescued"] < 0.01 * s["voxel_evals"]
+
+
+@pytest.mark.gpu
+def test_op_uploads_by_kernel_and_by_copy_agree(built_lib, monkeypatch):
+    """Where the GPU reads pageable host memory, a build's op tables are copied
+    by one kernel reading the host arrays; with that switched off they go by
+    cudaMemcpyAsync.  Both builds must give the same world."""
+    prog, _ = penthouse_program(20.0)
+    w_kernel = build_gpu(20.0, MODE_MIXED, program=prog)
+    monkeypatch.setenv("PIXELS_GB300_NO_HOST_READS", "1")
+    w_copy = build_gpu(20.0, MODE_MIXED, program=prog)
+    np.testing.assert_array_equal(w_kernel.grid, w_copy.grid)
+    assert w_kernel.poolUsed == w_copy.poolUsed
+    np.testing.assert_array_equal(w_kernel.pool, w_copy.pool)
