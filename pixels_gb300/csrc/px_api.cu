@@ -4,6 +4,7 @@
 // (voxel ranges, classify thresholds) must round exactly as the reference's
 // JavaScript does (shapes.ts:341-350).
 #include <algorithm>
+#include <chrono>
 #include <cstdlib>
 #include <atomic>
 #include <condition_variable>
@@ -31,6 +32,30 @@ struct DevBuf {
   size_t bytes = 0;
 };
 
+// The world's host op tables are filled by several host threads at once: a
+// resize must not first zero them on one thread, so their elements are
+// default-initialised (left as they are) instead of value-initialised.
+template <class T>
+struct DefaultInitAlloc : std::allocator<T> {
+  template <class U>
+  struct rebind {
+    using other = DefaultInitAlloc<U>;
+  };
+  DefaultInitAlloc() = default;
+  template <class U>
+  DefaultInitAlloc(const DefaultInitAlloc<U>&) noexcept {}
+  template <class U>
+  void construct(U* ptr) noexcept {
+    ::new (static_cast<void*>(ptr)) U;
+  }
+  template <class U, class... Args>
+  void construct(U* ptr, Args&&... args) {
+    ::new (static_cast<void*>(ptr)) U(std::forward<Args>(args)...);
+  }
+};
+template <class T>
+using hvec = std::vector<T, DefaultInitAlloc<T>>;
+
 // one host-to-device copy of a build's op tables
 struct Upload {
   void* dst;
@@ -56,16 +81,17 @@ struct px_world {
   bool holes_in_a = true;
 
   // ops queued by px_submit_ops (and the ops of the last committed build)
-  std::vector<OpDev> ops, last_ops;
-  std::vector<uint2> last_boxes, last_code;
-  std::vector<double> last_params;
+  hvec<OpDev> ops, last_ops;
+  hvec<uint2> last_boxes, last_code;
+  hvec<double> last_params;
   bool ops_resident = false;   // the device op tables already hold `ops`
-  std::vector<uint2> boxes, h_boxes;  // h_boxes: boxes + 32-op group boxes as uploaded
-  std::vector<uint2> code;
-  std::vector<double> params;
-  std::vector<uint32_t> code32, last_code32;   // per instruction: float32 parameter offset
-  std::vector<float2> p32, last_p32;           // float32 interval parameters
-  std::vector<float2> bases, last_bases;       // per-op brick-row offsets (mixed mode)
+  hvec<uint2> boxes;
+  std::vector<uint2> h_boxes;  // boxes + 32-op group boxes as uploaded
+  hvec<uint2> code;
+  hvec<double> params;
+  hvec<uint32_t> code32, last_code32;   // per instruction: float32 parameter offset
+  hvec<float2> p32, last_p32;           // float32 interval parameters
+  hvec<float2> bases, last_bases;       // per-op brick-row offsets (mixed mode)
   int validate = 0;
   uint64_t ops_applied = 0;
 
@@ -743,6 +769,9 @@ int convert_ops(const px_world* w, const IrOp* iops, size_t i0, size_t i1, const
 }
 
 // A small pool of host threads for op conversion (started on first use).
+// Between jobs a worker spins for a while before it sleeps, so that the jobs
+// of one submit (conversion, then the merge) and of back-to-back builds start
+// without a thread wake-up each.
 class HostPool {
  public:
   static HostPool& get() {
@@ -757,17 +786,26 @@ class HostPool {
       return;
     }
     std::lock_guard<std::mutex> one_job(run_mu_);  // callers on other threads wait their turn
-    std::unique_lock<std::mutex> g(mu_);
     job_ = &f;
     n_ = n;
     next_.store(0);
-    done_ = 0;
-    gen_++;
+    done_.store(0);
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      gen_.fetch_add(1, std::memory_order_release);
+    }
     cv_.notify_all();
-    g.unlock();
     work();
-    g.lock();
-    done_cv_.wait(g, [&] { return done_ == (int)workers_.size(); });
+    // the workers' part: spin briefly, then sleep until the last one reports
+    const int want = (int)workers_.size();
+    const auto t0 = std::chrono::steady_clock::now();
+    while (done_.load(std::memory_order_acquire) != want) {
+      if (std::chrono::steady_clock::now() - t0 > std::chrono::microseconds(200)) {
+        std::unique_lock<std::mutex> g(mu_);
+        done_cv_.wait(g, [&] { return done_.load(std::memory_order_acquire) == want; });
+        break;
+      }
+    }
     job_ = nullptr;
   }
 
@@ -788,23 +826,31 @@ class HostPool {
   void loop() {
     uint64_t seen = 0;
     for (;;) {
-      std::unique_lock<std::mutex> g(mu_);
-      cv_.wait(g, [&] { return gen_ != seen; });
-      seen = gen_;
-      g.unlock();
+      // spin up to 500 us for the next job, then sleep
+      const auto t0 = std::chrono::steady_clock::now();
+      uint32_t i = 0;
+      while (gen_.load(std::memory_order_acquire) == seen) {
+        if ((++i & 255u) == 0 && std::chrono::steady_clock::now() - t0 > std::chrono::microseconds(500)) {
+          std::unique_lock<std::mutex> g(mu_);
+          cv_.wait(g, [&] { return gen_.load(std::memory_order_acquire) != seen; });
+          break;
+        }
+      }
+      seen = gen_.load(std::memory_order_acquire);
       work();
-      g.lock();
-      done_++;
-      done_cv_.notify_one();
+      if (done_.fetch_add(1, std::memory_order_acq_rel) + 1 == (int)workers_.size()) {
+        std::lock_guard<std::mutex> g(mu_);
+        done_cv_.notify_one();
+      }
     }
   }
   std::vector<std::thread> workers_;
   std::mutex run_mu_, mu_;
   std::condition_variable cv_, done_cv_;
   const std::function<void(int)>* job_ = nullptr;
-  int n_ = 0, done_ = 0;
-  std::atomic<int> next_{0};
-  uint64_t gen_ = 0;
+  int n_ = 0;
+  std::atomic<int> next_{0}, done_{0};
+  std::atomic<uint64_t> gen_{0};
 };
 
 // Blocks of the single-pass scans of a build with P pairs and E_max events.
@@ -914,7 +960,7 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
   // convert the ops in contiguous ranges on the host pool, then append the
   // ranges in order (offsets rebased)
   HostPool& pool = HostPool::get();
-  const int n_chunks = n_ops < 512 ? 1 : (int)std::min<size_t>((size_t)pool.size() * 2, n_ops / 128);
+  const int n_chunks = n_ops < 512 ? 1 : (int)std::min<size_t>((size_t)pool.size() * 4, n_ops / 32);
   std::vector<SubmitChunk> chunks(n_chunks);
   pool.run(n_chunks, [&](int k) {
     const size_t i0 = n_ops * k / n_chunks, i1 = n_ops * (k + 1) / n_chunks;
@@ -922,41 +968,54 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
   });
   for (auto& c : chunks)
     if (c.rc != PX_OK) return fail(w, c.rc, "%s", c.err.c_str());
-  size_t n_code_new = 0, n_p32_new = 0, n_bases_new = 0, n_xp = 0;
-  for (const auto& c : chunks) {
-    n_code_new += c.code.size();
-    n_p32_new += c.p32.size();
-    n_bases_new += c.bases.size();
-    n_xp += c.xparams.size();
+  // every range's place in the world's arrays, then all ranges rebased and
+  // copied at once (the IR's own parameters as one more job)
+  struct Place {
+    size_t code, p32, bases, ops, xp;
+  };
+  std::vector<Place> at(n_chunks);
+  Place end = {w->code.size(), w->p32.size(), w->bases.size(), w->ops.size(), param_base + n_params};
+  for (int k = 0; k < n_chunks; k++) {
+    const SubmitChunk& c = chunks[k];
+    at[k] = end;
+    end.code += c.code.size();
+    end.p32 += c.p32.size();
+    end.bases += c.bases.size();
+    end.ops += c.ops.size();
+    end.xp += c.xparams.size();
   }
-  w->code.reserve(w->code.size() + n_code_new);
-  w->code32.reserve(w->code32.size() + n_code_new);
-  w->p32.reserve(w->p32.size() + n_p32_new);
-  w->bases.reserve(w->bases.size() + n_bases_new);
-  w->ops.reserve(w->ops.size() + n_ops);
-  w->boxes.reserve(w->boxes.size() + n_ops);
-  w->params.reserve(param_base + n_params + n_xp);
-  w->params.insert(w->params.end(), Pp, Pp + n_params);
-  size_t xbase = param_base + n_params;
-  for (auto& c : chunks) {  // in order: rebase each range's offsets, append it
-    const uint32_t code_at = (uint32_t)w->code.size(), p32_at = (uint32_t)w->p32.size(),
-                   bases_at = (uint32_t)w->bases.size();
-    for (uint32_t i : c.xfix) c.code[i].y += (uint32_t)xbase;
-    for (uint32_t& v : c.code32) v += p32_at;
-    for (OpDev& d : c.ops) {
-      d.code_off += code_at;
-      d.base_off += bases_at;
-      if (d.paint32_off != NO_SLOT) d.paint32_off += p32_at;
+  w->code.resize(end.code);
+  w->code32.resize(end.code);
+  w->p32.resize(end.p32);
+  w->bases.resize(end.bases);
+  w->ops.resize(end.ops);
+  w->boxes.resize(end.ops);
+  w->params.resize(end.xp);
+  pool.run(n_chunks + 1, [&](int k) {
+    if (k == n_chunks) {
+      if (n_params) std::memcpy(w->params.data() + param_base, Pp, n_params * sizeof(double));
+      return;
     }
-    w->code.insert(w->code.end(), c.code.begin(), c.code.end());
-    w->code32.insert(w->code32.end(), c.code32.begin(), c.code32.end());
-    w->p32.insert(w->p32.end(), c.p32.begin(), c.p32.end());
-    w->bases.insert(w->bases.end(), c.bases.begin(), c.bases.end());
-    w->ops.insert(w->ops.end(), c.ops.begin(), c.ops.end());
-    w->boxes.insert(w->boxes.end(), c.boxes.begin(), c.boxes.end());
-    xbase += c.xparams.size();
-  }
-  for (const auto& c : chunks) w->params.insert(w->params.end(), c.xparams.begin(), c.xparams.end());
+    SubmitChunk& c = chunks[k];
+    const Place& pl = at[k];
+    for (uint32_t i : c.xfix) c.code[i].y += (uint32_t)pl.xp;
+    for (uint32_t& v : c.code32) v += (uint32_t)pl.p32;
+    for (OpDev& d : c.ops) {
+      d.code_off += (uint32_t)pl.code;
+      d.base_off += (uint32_t)pl.bases;
+      if (d.paint32_off != NO_SLOT) d.paint32_off += (uint32_t)pl.p32;
+    }
+    auto put = [](auto& dst, size_t pos, const auto& src) {
+      if (!src.empty()) std::memcpy(dst.data() + pos, src.data(), src.size() * sizeof(src[0]));
+    };
+    put(w->code, pl.code, c.code);
+    put(w->code32, pl.code, c.code32);
+    put(w->p32, pl.p32, c.p32);
+    put(w->bases, pl.bases, c.bases);
+    put(w->ops, pl.ops, c.ops);
+    put(w->boxes, pl.ops, c.boxes);
+    put(w->params, pl.xp, c.xparams);
+  });
   return PX_OK;
 }
 
