@@ -1161,6 +1161,19 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   CU(cudaMemsetAsync(w->res.p, 0, sizeof(BuildResult), s));
   CU(cudaMemsetAsync(w->work_counter.p, 0, 16, s));
   CU(cudaMemsetAsync(w->chunk_counter.p, 0, 512, s));
+  if ((rc = issue_uploads(w, ups, s))) return rc;  // the op tables; the chunk order follows the cull launches
+  if (P) CU(cudaMemsetAsync(w->evt.p, 0, P, s));
+  CU(cudaMemsetAsync(w->bmark.p, 0, 4 * ((w->ncells + 31) / 32), s));
+
+  BuildResult* res = (BuildResult*)w->res.p;
+  ScanTemp st{w->scan_agg.p, scan_nb, &res->status, 0};
+  CU(cudaMemsetAsync((char*)w->scan_agg.p + scan_regions_offset(scan_nb), 0, scan_regions_bytes(scan_nb), s));
+  launch_cull_count((const uint2*)w->d_boxes.p, n_ops, w->TX, w->TY, w->TZ, (uint32_t*)w->tile_cnt.p,
+                    (uint32_t*)w->tiles_nonempty.p, res, s);
+  launch_scan_u32((const uint32_t*)w->tile_cnt.p, (uint32_t*)w->tile_off.p, w->ntiles, nullptr, false, nullptr, st, s);
+  launch_cull_fill((const uint2*)w->d_boxes.p, n_ops, w->TX, w->TY, w->TZ, (const uint32_t*)w->tile_off.p,
+                   (uint32_t*)w->tile_ops.p, (uint2*)w->tile_boxes.p, s);
+  // the classify pass's chunk order, computed while the cull kernels run
   const size_t n_chunks = (P + 31) / 32;
   if (upload) {
     // op of the first pair of every 32-pair chunk, then the order classify_kernel
@@ -1197,25 +1210,15 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
       }
       bucket_n[w->h_op_bucket[i]] += c1 - c0;
     }
+    ups.clear();
     ups.push_back({w->chunk_op.p, w->h_chunk_op.data(), 8 * n_chunks});
     // the sub-block and voxel passes take the classes costliest first
     int order[VCLASSES];
     for (int k = 0; k < VCLASSES; k++) order[k] = k;
     std::stable_sort(order, order + VCLASSES, [&](int x, int y) { return cc[x] > cc[y]; });
     for (int k = 0; k < VCLASSES; k++) w->class_order[k] = (uint8_t)order[k];
+    if ((rc = issue_uploads(w, ups, s))) return rc;
   }
-  if ((rc = issue_uploads(w, ups, s))) return rc;
-  if (P) CU(cudaMemsetAsync(w->evt.p, 0, P, s));
-  CU(cudaMemsetAsync(w->bmark.p, 0, 4 * ((w->ncells + 31) / 32), s));
-
-  BuildResult* res = (BuildResult*)w->res.p;
-  ScanTemp st{w->scan_agg.p, scan_nb, &res->status, 0};
-  CU(cudaMemsetAsync((char*)w->scan_agg.p + scan_regions_offset(scan_nb), 0, scan_regions_bytes(scan_nb), s));
-  launch_cull_count((const uint2*)w->d_boxes.p, n_ops, w->TX, w->TY, w->TZ, (uint32_t*)w->tile_cnt.p,
-                    (uint32_t*)w->tiles_nonempty.p, res, s);
-  launch_scan_u32((const uint32_t*)w->tile_cnt.p, (uint32_t*)w->tile_off.p, w->ntiles, nullptr, false, nullptr, st, s);
-  launch_cull_fill((const uint2*)w->d_boxes.p, n_ops, w->TX, w->TY, w->TZ, (const uint32_t*)w->tile_off.p,
-                   (uint32_t*)w->tile_ops.p, (uint2*)w->tile_boxes.p, s);
   FoldArgs fa{};
   fa.chunk_order = (const uint2*)w->chunk_op.p;
   for (int k = 0; k < VCLASSES; k++) fa.class_order[k] = w->class_order[k];
