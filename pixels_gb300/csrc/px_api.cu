@@ -104,6 +104,7 @@ struct px_world {
   DevBuf chunk_op, pcode, psub, pmask, chunk_counter, vitems, pitems;
   std::vector<uint32_t> h_chunk_op;  // the chunks in classify order: (chunk, op of its first pair | single-op bit)
   std::vector<Upload> h_uploads;     // the op-table copies of the build being enqueued
+  std::vector<uint32_t> h_painted, h_painted32;  // the build's painted ops, float64-only ones first
   std::vector<uint8_t> h_op_bucket;  // per op: cost bucket (0..63) of one evaluation
   uint8_t class_order[VCLASSES] = {0};  // sub-block / voxel class order of the resident ops
   DevBuf paint_items, pvals;    // sub-blocks to paint and the paint values
@@ -769,9 +770,8 @@ int convert_ops(const px_world* w, const IrOp* iops, size_t i0, size_t i1, const
 }
 
 // A small pool of host threads for op conversion (started on first use).
-// Between jobs a worker spins for a while before it sleeps, so that the jobs
-// of one submit (conversion, then the merge) and of back-to-back builds start
-// without a thread wake-up each.
+// Between jobs a worker spins briefly before it sleeps, so that the jobs of
+// one submit (conversion, then the merge) start without a thread wake-up each.
 class HostPool {
  public:
   static HostPool& get() {
@@ -826,11 +826,13 @@ class HostPool {
   void loop() {
     uint64_t seen = 0;
     for (;;) {
-      // spin up to 500 us for the next job, then sleep
+      // spin up to 50 us for the next job (the jobs of one submit follow each
+      // other within microseconds), then sleep: longer spinning would take the
+      // cores from the caller's other threads between submits
       const auto t0 = std::chrono::steady_clock::now();
       uint32_t i = 0;
       while (gen_.load(std::memory_order_acquire) == seen) {
-        if ((++i & 255u) == 0 && std::chrono::steady_clock::now() - t0 > std::chrono::microseconds(500)) {
+        if ((++i & 255u) == 0 && std::chrono::steady_clock::now() - t0 > std::chrono::microseconds(50)) {
           std::unique_lock<std::mutex> g(mu_);
           cv_.wait(g, [&] { return gen_.load(std::memory_order_acquire) != seen; });
           break;
@@ -991,7 +993,7 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
   w->ops.resize(end.ops);
   w->boxes.resize(end.ops);
   w->params.resize(end.xp);
-  pool.run(n_chunks + 1, [&](int k) {
+  auto merge = [&](int k) {
     if (k == n_chunks) {
       if (n_params) std::memcpy(w->params.data() + param_base, Pp, n_params * sizeof(double));
       return;
@@ -1015,7 +1017,13 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
     put(w->ops, pl.ops, c.ops);
     put(w->boxes, pl.ops, c.boxes);
     put(w->params, pl.xp, c.xparams);
-  });
+  };
+  if (n_chunks > 1) {
+    pool.run(n_chunks + 1, merge);
+  } else {  // a small list: no threads
+    merge(0);
+    merge(1);
+  }
   return PX_OK;
 }
 
@@ -1058,10 +1066,17 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
 
   // (op, brick) pair bases and the tile-list bound
   uint64_t P = 0, tile_pairs = 0;
+  // ops with paint calls: float64-only ones, then certified float32 ones
+  std::vector<uint32_t>& painted = w->h_painted;
+  std::vector<uint32_t>& painted32 = w->h_painted32;
+  painted.clear();
+  painted32.clear();
   for (int i = 0; i < n_ops; i++) {
     OpDev& o = w->ops[i];
     o.pair_base = P;
+    o.paint_slot = NO_SLOT;
     if (o.bx0 > o.bx1) continue;
+    if (o.kind != KIND_CARVE && o.paint_kind != PK_CONST) (o.paint32_off == NO_SLOT ? painted : painted32).push_back((uint32_t)i);
     uint64_t nz = (uint64_t)(o.bz1 - o.bz0 + 1);
     P += (uint64_t)o.nx * o.ny * nz;
     uint64_t tx = (uint64_t)(o.bx1 / 4 - o.bx0 / 4 + 1), ty = (uint64_t)(o.by1 / 4 - o.by0 / 4 + 1),
@@ -1069,6 +1084,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
     tile_pairs += tx * ty * tz;
   }
   if (P > 0x1fffffffull) return fail(w, PX_E_QUEUE_OVERFLOW, "too many (op, brick) pairs in one build: %llu", (unsigned long long)P);
+  painted.insert(painted.end(), painted32.begin(), painted32.end());
   // paint slots (one per (op, brick) pair of a painted op, 2 KiB each): every
   // painted op when they fit in 512 MiB, else the heavy kinds alone when they
   // fit, else none; ops without a slot have their paints called by the apply pass
@@ -1079,17 +1095,14 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
     inline_paints = false;
     // float64-only paints first: paint_kernel takes items in slot order, so the
     // slowest calls start earliest
-    for (int pass = 0; pass < 2; pass++)
-      for (int i = 0; i < n_ops; i++) {
-        OpDev& o = w->ops[i];
-        if (pass == 0) o.paint_slot = NO_SLOT;
-        if (o.bx0 > o.bx1 || o.kind == KIND_CARVE || o.paint_kind == PK_CONST) continue;
-        if ((o.paint32_off != NO_SLOT) != (pass == 1)) continue;
-        if (tier == 2 || (tier == 1 && !paint_is_heavy(o.paint_kind))) { inline_paints = true; continue; }
-        const uint64_t np = (uint64_t)o.nx * o.ny * (uint64_t)(o.bz1 - o.bz0 + 1);
-        o.paint_slot = (uint32_t)n_slots;
-        n_slots += np;
-      }
+    for (const uint32_t i : painted) {
+      OpDev& o = w->ops[i];
+      o.paint_slot = NO_SLOT;
+      if (tier == 2 || (tier == 1 && !paint_is_heavy(o.paint_kind))) { inline_paints = true; continue; }
+      const uint64_t np = (uint64_t)o.nx * o.ny * (uint64_t)(o.bz1 - o.bz0 + 1);
+      o.paint_slot = (uint32_t)n_slots;
+      n_slots += np;
+    }
     if (n_slots * 2048 <= (512ull << 20)) break;
   }
   const uint64_t touched_bound = P < w->ncells ? P : w->ncells;
