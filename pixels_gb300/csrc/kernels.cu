@@ -1694,18 +1694,20 @@ __global__ void __launch_bounds__(256) derive_kernel(const uint32_t* __restrict_
   }
 }
 
-// The op-table uploads of a build in one launch, read straight from the host
-// arrays (pageable memory the GPU reads through the host page tables): entry
-// blockIdx.y, 16-byte words, then the last bytes of an entry.
+// A build's op-table uploads (read straight from the host arrays: pageable
+// memory the GPU reads through the host page tables) and counter clears in one
+// launch: entry blockIdx.y, 16-byte words, then the last bytes of an entry.
 __global__ void __launch_bounds__(256) upload_kernel(HostUploads u) {
   const HostUploads::Entry& e = u.e[blockIdx.y];
   const size_t n16 = e.bytes >> 4;
   const uint4* src = reinterpret_cast<const uint4*>(e.src);
   uint4* dst = reinterpret_cast<uint4*>(e.dst);
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += (size_t)gridDim.x * blockDim.x)
-    dst[i] = src[i];
-  if (blockIdx.x == 0 && threadIdx.x < (e.bytes & 15u))
-    static_cast<unsigned char*>(e.dst)[(n16 << 4) + threadIdx.x] = static_cast<const unsigned char*>(e.src)[(n16 << 4) + threadIdx.x];
+    dst[i] = src ? src[i] : make_uint4(0u, 0u, 0u, 0u);
+  if (blockIdx.x == 0 && threadIdx.x < (e.bytes & 15u)) {
+    const size_t k = (n16 << 4) + threadIdx.x;
+    static_cast<unsigned char*>(e.dst)[k] = src ? static_cast<const unsigned char*>(e.src)[k] : (unsigned char)0;
+  }
 }
 void launch_uploads(const HostUploads& u, cudaStream_t s) {
   if (u.n == 0) return;

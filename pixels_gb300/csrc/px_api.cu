@@ -1029,27 +1029,35 @@ int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
 
 static int cost_bucket(float c) { return c >= 15.75f ? 63 : (int)(c * 4.f); }
 
-// The host-to-device copies of one build's op tables.  Where the GPU reads
-// pageable memory through the host page tables (Grace), one kernel copies them
-// all from the host arrays (a few microseconds of host time instead of ~10 per
-// cudaMemcpyAsync); the arrays then stay untouched until the build has
-// finished (px_submit_ops and px_world_reset wait for it).  Elsewhere, and
-// while a graph is captured, plain copies.
+// The host-to-device copies of one build's op tables and the clears of its
+// counters (entries without a source).  One kernel does the clears and, where
+// the GPU reads pageable memory through the host page tables (Grace), the
+// copies too, reading the host arrays directly (a few microseconds of host
+// time instead of ~10 per cudaMemcpyAsync or cudaMemsetAsync); the arrays then
+// stay untouched until the build has finished (px_submit_ops and
+// px_world_reset wait for it).  Elsewhere, and while a graph is captured, the
+// copies are cudaMemcpyAsync.
 static int issue_uploads(px_world* w, const std::vector<Upload>& ups, cudaStream_t s) {
-  bool direct = w->host_reads && !w->capturing && ups.size() <= 8;
-  for (const Upload& u : ups)
-    if (u.bytes && (((uintptr_t)u.src | (uintptr_t)u.dst) & 15u)) direct = false;
-  if (direct) {
-    HostUploads hu{};
-    for (const Upload& u : ups)
-      if (u.bytes) hu.e[hu.n++] = {u.src, u.dst, u.bytes};
+  HostUploads hu{};
+  bool reads_host = false;
+  for (const Upload& u : ups) {
+    if (!u.bytes) continue;
+    const bool aligned = !(((uintptr_t)u.src | (uintptr_t)u.dst) & 15u);
+    const bool by_kernel = aligned && hu.n < HostUploads::kMax && (!u.src || (w->host_reads && !w->capturing));
+    if (by_kernel) {
+      hu.e[hu.n++] = {u.src, u.dst, u.bytes};
+      reads_host = reads_host || u.src;
+    } else if (u.src) {
+      CU(cudaMemcpyAsync(u.dst, u.src, u.bytes, cudaMemcpyHostToDevice, s));
+    } else {
+      CU(cudaMemsetAsync(u.dst, 0, u.bytes, s));
+    }
+  }
+  if (hu.n) {
     launch_uploads(hu, s);
     CU(cudaGetLastError());
-    w->uploads_pending = hu.n > 0;
-    return PX_OK;
+    if (reads_host) w->uploads_pending = true;
   }
-  for (const Upload& u : ups)
-    if (u.bytes) CU(cudaMemcpyAsync(u.dst, u.src, u.bytes, cudaMemcpyHostToDevice, s));
   return PX_OK;
 }
 
@@ -1171,16 +1179,17 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
     ups.push_back({w->d_p32.p, w->p32.data(), sizeof(float2) * w->p32.size()});
     ups.push_back({w->d_bases.p, w->bases.data(), sizeof(float2) * w->bases.size()});
   }
-  CU(cudaMemsetAsync(w->res.p, 0, sizeof(BuildResult), s));
-  CU(cudaMemsetAsync(w->work_counter.p, 0, 16, s));
-  CU(cudaMemsetAsync(w->chunk_counter.p, 0, 512, s));
+  // the build's counters and flags start at zero
+  ups.push_back({w->res.p, nullptr, sizeof(BuildResult)});
+  ups.push_back({w->work_counter.p, nullptr, 16});
+  ups.push_back({w->chunk_counter.p, nullptr, 512});
+  ups.push_back({w->evt.p, nullptr, P});
+  ups.push_back({w->bmark.p, nullptr, 4 * ((w->ncells + 31) / 32)});
+  ups.push_back({(char*)w->scan_agg.p + scan_regions_offset(scan_nb), nullptr, scan_regions_bytes(scan_nb)});
   if ((rc = issue_uploads(w, ups, s))) return rc;  // the op tables; the chunk order follows the cull launches
-  if (P) CU(cudaMemsetAsync(w->evt.p, 0, P, s));
-  CU(cudaMemsetAsync(w->bmark.p, 0, 4 * ((w->ncells + 31) / 32), s));
 
   BuildResult* res = (BuildResult*)w->res.p;
   ScanTemp st{w->scan_agg.p, scan_nb, &res->status, 0};
-  CU(cudaMemsetAsync((char*)w->scan_agg.p + scan_regions_offset(scan_nb), 0, scan_regions_bytes(scan_nb), s));
   launch_cull_count((const uint2*)w->d_boxes.p, n_ops, w->TX, w->TY, w->TZ, (uint32_t*)w->tile_cnt.p,
                     (uint32_t*)w->tiles_nonempty.p, res, s);
   launch_scan_u32((const uint32_t*)w->tile_cnt.p, (uint32_t*)w->tile_off.p, w->ntiles, nullptr, false, nullptr, st, s);

@@ -263,15 +263,17 @@ struct FinalizeArgs {
 };
 void launch_finalize(const FinalizeArgs& a, uint32_t touched_cap, cudaStream_t s);
 
-// Host-to-device copies done by one kernel that reads the host arrays directly
-// (only where the device reports pageable memory access through the host page
-// tables); sources and destinations 16-byte aligned.
+// Host-to-device copies and device clears done by one kernel: an entry with a
+// source copies it (read straight from host memory: only where the device
+// reports pageable memory access through the host page tables), one without
+// zeroes its destination.  Sources and destinations 16-byte aligned.
 struct HostUploads {
+  static constexpr int kMax = 16;
   struct Entry {
     const void* src;
     void* dst;
     size_t bytes;
-  } e[8];
+  } e[kMax];
   int n;
 };
 void launch_uploads(const HostUploads& u, cudaStream_t s);
