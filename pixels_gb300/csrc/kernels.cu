@@ -32,6 +32,9 @@ namespace px {
 #ifndef PX_CLASSIFY_MINB
 #define PX_CLASSIFY_MINB 3
 #endif
+#ifndef PX_SUB_MINB
+#define PX_SUB_MINB PX_CLASSIFY_MINB
+#endif
 #ifndef PX_VOXEL_MINB
 #define PX_VOXEL_MINB 3
 #endif
@@ -412,7 +415,7 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
 // order like the voxel work.  Writes the pair's 2-bit sub-block classes, the
 // voxel masks of lone boxes (per-axis runs), and queues the partial sub-blocks.
 template <int MODE>
-__global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIFY64_MINB) sub_kernel(FoldArgs a) {
+__global__ void __launch_bounds__(256, MODE == 1 ? PX_SUB_MINB : PX_CLASSIFY64_MINB) sub_kernel(FoldArgs a) {
   const int lane = threadIdx.x & 31;
   LaneStats ls = {a.res};
   uint32_t st_local = 0;
@@ -1096,7 +1099,7 @@ void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEve
   auto grid = [&](int per_sm) { return max_blocks > 0 && max_blocks < n_sms * per_sm ? max_blocks : n_sms * per_sm; };
   if (mode == 1) {
     ++g_launches; classify_kernel<1><<<grid(PX_CLASSIFY_MINB), 256, 0, s>>>(a);
-    ++g_launches; sub_kernel<1><<<grid(PX_CLASSIFY_MINB), 256, 0, s>>>(a);
+    ++g_launches; sub_kernel<1><<<grid(PX_SUB_MINB), 256, 0, s>>>(a);
     ++g_launches; voxel_kernel<1><<<grid(PX_VOXEL_MINB), 256, 0, s>>>(a);
   } else {
     ++g_launches; classify_kernel<0><<<grid(PX_CLASSIFY64_MINB), 256, 0, s>>>(a);
