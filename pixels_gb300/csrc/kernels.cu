@@ -751,13 +751,23 @@ __global__ void __launch_bounds__(256) mark_compact_kernel(const uint32_t* __res
   for (uint32_t w0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; w0 < n_words; w0 += warps * 32) {
     const uint32_t wi = w0 + lane;
     const uint32_t bits = wi < n_words ? __ldg(bmark + wi) : 0u;
-    // split the word's bricks: those of tiles with more than 8 ops (the front) and the rest
+    // split the word's bricks: those of tiles with more than 8 ops (the front) and the rest;
+    // the 32 bricks' coordinates stepped along x (no division per brick), their tile counts
+    // loaded together (an unrolled loop of independent loads)
     uint32_t heavy = 0;
-    for (uint32_t b = bits; b;) {
-      const int k = __ffs(b) - 1;
-      b &= b - 1;
-      const uint32_t ci = wi * 32u + (uint32_t)k, byz = ci / BX, bx = ci - byz * BX, by = byz % BY, bz = byz / BY;
-      if (__ldg(tile_cnt + (bx >> 2) + TX * ((by >> 2) + TY * (bz >> 2))) > 8u) heavy |= 1u << k;
+    if (bits) {
+      const uint32_t ci0 = wi * 32u, byz0 = ci0 / BX;
+      uint32_t bx = ci0 - byz0 * BX, by = byz0 % BY, bz = byz0 / BY;
+#pragma unroll
+      for (int k = 0; k < 32; k++) {
+        if (((bits >> k) & 1u) &&
+            __ldg(tile_cnt + (bx >> 2) + TX * ((by >> 2) + TY * (bz >> 2))) > 8u)
+          heavy |= 1u << k;
+        if (++bx == BX) {
+          bx = 0;
+          if (++by == BY) { by = 0; bz++; }
+        }
+      }
     }
 #pragma unroll
     for (int e = 0; e < 2; e++) {
@@ -776,12 +786,20 @@ __global__ void __launch_bounds__(256) mark_compact_kernel(const uint32_t* __res
         atomicAdd(&res->n_work, total);
       }
       base = __shfl_sync(FULLMASK, base, 31) + incl - cnt;
-      for (uint32_t b = mine; b;) {
-        const int k = __ffs(b) - 1;
-        b &= b - 1;
-        const uint32_t ci = wi * 32u + (uint32_t)k, byz = ci / BX;
-        work[e ? last - base : base] = (ci - byz * BX) | ((byz % BY) << 10) | ((byz / BY) << 20);
-        base++;
+      if (mine) {
+        const uint32_t ci0 = wi * 32u, byz0 = ci0 / BX;
+        const uint32_t bx0 = ci0 - byz0 * BX, by0 = byz0 % BY, bz0 = byz0 / BY;
+        for (uint32_t b = mine; b;) {
+          const int k = __ffs(b) - 1;
+          b &= b - 1;
+          uint32_t bx = bx0 + (uint32_t)k, by = by0, bz = bz0;
+          while (bx >= BX) {  // the word's bricks run on along x into the next rows
+            bx -= BX;
+            if (++by == BY) { by = 0; bz++; }
+          }
+          work[e ? last - base : base] = bx | (by << 10) | (bz << 20);
+          base++;
+        }
       }
     }
   }
