@@ -64,7 +64,7 @@ __device__ __forceinline__ bool box_overlaps_tile(uint2 b, int tx, int ty, int t
 // tile (a two-level culling hierarchy; scene ops come object by object, so
 // groups are compact).
 __global__ void __launch_bounds__(256) cull_count_kernel(const uint2* __restrict__ boxes, int n_ops, int TX, int TY, int TZ,
-                                                         uint32_t* tile_cnt, uint32_t* tiles_nonempty, BuildResult* res) {
+                                                         uint32_t* tile_cnt) {
   const int lane = threadIdx.x & 31;
   const int n_tiles = TX * TY * TZ;
   const int n_groups = (n_ops + 31) / 32;
@@ -82,10 +82,7 @@ __global__ void __launch_bounds__(256) cull_count_kernel(const uint2* __restrict
         cnt += __popc(__ballot_sync(FULLMASK, ov));
       }
     }
-    if (lane == 0) {
-      tile_cnt[tile] = cnt;
-      if (cnt) tiles_nonempty[atomicAdd(&res->n_nonempty, 1u)] = (uint32_t)tile;
-    }
+    if (lane == 0) tile_cnt[tile] = cnt;
   }
 }
 
@@ -119,11 +116,10 @@ __global__ void __launch_bounds__(256) cull_fill_kernel(const uint2* __restrict_
   }
 }
 
-void launch_cull_count(const uint2* boxes, int n_ops, int TX, int TY, int TZ, uint32_t* tile_cnt,
-                       uint32_t* tiles_nonempty, BuildResult* res, cudaStream_t s) {
+void launch_cull_count(const uint2* boxes, int n_ops, int TX, int TY, int TZ, uint32_t* tile_cnt, cudaStream_t s) {
   int n_tiles = TX * TY * TZ;
   int blocks = (n_tiles * 32 + 255) / 256;
-  ++g_launches; cull_count_kernel<<<blocks, 256, 0, s>>>(boxes, n_ops, TX, TY, TZ, tile_cnt, tiles_nonempty, res);
+  ++g_launches; cull_count_kernel<<<blocks, 256, 0, s>>>(boxes, n_ops, TX, TY, TZ, tile_cnt);
 }
 void launch_cull_fill(const uint2* boxes, int n_ops, int TX, int TY, int TZ, const uint32_t* tile_off,
                       uint32_t* tile_ops, uint2* tile_boxes, cudaStream_t s) {

@@ -97,7 +97,7 @@ struct px_world {
 
   // per-build device scratch
   DevBuf d_ops, d_boxes, d_code, d_params, d_code32, d_p32, d_bases;
-  DevBuf tile_cnt, tile_off, tiles_nonempty, tile_ops, tile_boxes;
+  DevBuf tile_cnt, tile_off, tile_ops, tile_boxes;
   DevBuf evt, fsrc, cnt, pos, etype, ew, depth_fn, depth, tree, fresh, fresh_rank;
   DevBuf staging, stage_cell, stage_src, touched;
   uint64_t stage_hint = 0;      // staging slots the next build reserves (grown on overflow)
@@ -444,7 +444,7 @@ void px_world_destroy(px_world* w) {
   cudaFree(w->d_pool32);
   DevBuf* bufs[] = {&w->holes_a, &w->holes_b, &w->d_ops, &w->d_boxes, &w->d_code, &w->d_params, &w->d_code32,
                     &w->d_p32, &w->d_bases, &w->tile_cnt,
-                    &w->tile_off, &w->tiles_nonempty, &w->tile_ops, &w->evt, &w->fsrc, &w->cnt, &w->pos, &w->etype,
+                    &w->tile_off, &w->tile_ops, &w->evt, &w->fsrc, &w->cnt, &w->pos, &w->etype,
                     &w->ew, &w->depth_fn, &w->depth, &w->tree, &w->fresh, &w->fresh_rank, &w->staging, &w->touched,
                     &w->stage_cell, &w->stage_src, &w->chunk_op, &w->pcode, &w->psub, &w->pmask,
                     &w->chunk_counter, &w->vitems, &w->scan_agg, &w->work_counter, &w->res, &w->opaque,
@@ -869,7 +869,7 @@ int ensure_pair_scratch(px_world* w, uint64_t P, uint64_t tile_pairs, uint64_t n
                                uint64_t touched_bound, size_t E_max, uint64_t stage_cap) {
   int rc;
   if ((rc = ensure(w, w->tile_cnt, 4 * w->ntiles)) || (rc = ensure(w, w->tile_off, 4 * w->ntiles)) ||
-      (rc = ensure(w, w->tiles_nonempty, 4 * w->ntiles)) || (rc = ensure(w, w->tile_ops, 4 * tile_pairs)) || (rc = ensure(w, w->tile_boxes, 8 * tile_pairs)) ||
+      (rc = ensure(w, w->tile_ops, 4 * tile_pairs)) || (rc = ensure(w, w->tile_boxes, 8 * tile_pairs)) ||
       (rc = ensure(w, w->evt, P)) || (rc = ensure(w, w->fsrc, 8 * P)) || (rc = ensure(w, w->cnt, 4 * P)) ||
       (rc = ensure(w, w->pos, 4 * P)) || (rc = ensure(w, w->etype, E_max)) || (rc = ensure(w, w->ew, 8 * E_max)) ||
       (rc = ensure(w, w->depth_fn, 8 * E_max)) || (rc = ensure(w, w->depth, 4 * (E_max + 32))) ||
@@ -1190,8 +1190,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
 
   BuildResult* res = (BuildResult*)w->res.p;
   ScanTemp st{w->scan_agg.p, scan_nb, &res->status, 0};
-  launch_cull_count((const uint2*)w->d_boxes.p, n_ops, w->TX, w->TY, w->TZ, (uint32_t*)w->tile_cnt.p,
-                    (uint32_t*)w->tiles_nonempty.p, res, s);
+  launch_cull_count((const uint2*)w->d_boxes.p, n_ops, w->TX, w->TY, w->TZ, (uint32_t*)w->tile_cnt.p, s);
   launch_scan_u32((const uint32_t*)w->tile_cnt.p, (uint32_t*)w->tile_off.p, w->ntiles, nullptr, false, nullptr, st, s);
   launch_cull_fill((const uint2*)w->d_boxes.p, n_ops, w->TX, w->TY, w->TZ, (const uint32_t*)w->tile_off.p,
                    (uint32_t*)w->tile_ops.p, (uint2*)w->tile_boxes.p, s);
@@ -1294,7 +1293,6 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   fa.tile_cnt = (const uint32_t*)w->tile_cnt.p;
   fa.tile_ops = (const uint32_t*)w->tile_ops.p;
   fa.tile_boxes = (const uint2*)w->tile_boxes.p;
-  fa.tiles_nonempty = (const uint32_t*)w->tiles_nonempty.p;
   fa.BX = w->BX; fa.BY = w->BY; fa.BZ = w->BZ; fa.TX = w->TX; fa.TY = w->TY;
   fa.vs = w->vs;
   fa.grid = w->d_grid;

@@ -119,7 +119,6 @@ struct BuildResult {
   uint32_t n_holes;      // after the build
   uint32_t stage_count;  // bricks that end as pool bricks and were touched (staging slots wanted)
   uint32_t touched_count;  // bricks whose grid entry the build rewrites
-  uint32_t n_nonempty;   // tiles with at least one op
   uint32_t n_work;       // bricks with at least one (op, brick) pair that is not skipped
   uint32_t n_fresh;
   uint32_t max_pool_index;
@@ -178,7 +177,6 @@ struct FoldArgs {
   const uint32_t* tile_cnt;
   const uint32_t* tile_ops;
   const uint2* tile_boxes;    // the brick box of each tile_ops entry (packed like the op boxes)
-  const uint32_t* tiles_nonempty;
   int BX, BY, BZ, TX, TY;
   double vs;
   uint32_t* grid;
@@ -199,8 +197,7 @@ struct FoldArgs {
 constexpr uint32_t TAG_STAGED = 0x40000000u;
 
 // Host-side launch wrappers (kernels.cu)
-void launch_cull_count(const uint2* boxes, int n_ops, int TX, int TY, int TZ, uint32_t* tile_cnt,
-                       uint32_t* tiles_nonempty, BuildResult* res, cudaStream_t s);
+void launch_cull_count(const uint2* boxes, int n_ops, int TX, int TY, int TZ, uint32_t* tile_cnt, cudaStream_t s);
 void launch_cull_fill(const uint2* boxes, int n_ops, int TX, int TY, int TZ, const uint32_t* tile_off,
                       uint32_t* tile_ops, uint2* tile_boxes, cudaStream_t s);
 // max_blocks > 0 caps the persistent grids (builds sharing the GPU)
