@@ -928,7 +928,7 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
         }
         if (set_u >= 0) {  // setBrickUniform (VoxelWorld.ts:89-97)
           if (state == ST_MIXED) {
-            if (lane == 0) { a.evt[pair] = 2; a.fsrc[pair] = src; }
+            if (lane == 0) { a.evt[pair] = 2; a.evt_cnt[pair] = 1; a.fsrc[pair] = src; }
             wc.free_++;
           }
           const uint32_t v = (uint32_t)set_u;
@@ -1041,7 +1041,7 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
           state = v0 == 0 ? ST_EMPTY : ST_UNIF;
           uval = v0; src = -1;
         }
-        if (lane == 0) a.evt[pair] = ev;
+        if (lane == 0) { a.evt[pair] = ev; a.evt_cnt[pair] = (uint32_t)__popc(ev & 3u); }
       };
 
       // entries 0..7 of the tile list, looked up above by lanes 8j..8j+7
@@ -1368,10 +1368,6 @@ void launch_scan_u32(const uint32_t* in, uint32_t* out, size_t n, const uint32_t
 constexpr unsigned long long KNOWN = 1ull << 63;
 enum : uint8_t { EV_PUSH = 0, EV_POP = 1 };
 
-__global__ void evt_count_kernel(const uint8_t* __restrict__ evt, size_t P, uint32_t* cnt) {
-  for (size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x; p < P; p += (size_t)gridDim.x * blockDim.x)
-    cnt[p] = __popc(evt[p] & 3u);
-}
 
 __global__ void events_build_kernel(ReplayArgs a) {
   const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
@@ -1546,7 +1542,6 @@ void launch_replay(const ReplayArgs& a, cudaStream_t s) {
   if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&n_sms, cudaDevAttrMultiProcessorCount, dev);
   const size_t cap = (size_t)n_sms * 8;
   auto blocks = [&](size_t n) { size_t b = (n + T - 1) / T; return (int)(b < cap ? (b ? b : 1) : cap); };
-  ++g_launches; evt_count_kernel<<<blocks(a.P), T, 0, s>>>(a.evt, a.P, a.cnt);
   scan_any<SumOp, false>(a.cnt, a.pos, a.P, nullptr, false, nullptr, *a.scan, s);
   ++g_launches; events_build_kernel<<<blocks(a.P > a.H ? a.P : a.H), T, 0, s>>>(a);  // also the event count
   const uint32_t* nE = &a.res->n_events;

@@ -1184,6 +1184,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   ups.push_back({w->work_counter.p, nullptr, 16});
   ups.push_back({w->chunk_counter.p, nullptr, 512});
   ups.push_back({w->evt.p, nullptr, P});
+  ups.push_back({w->cnt.p, nullptr, 4 * P});  // events per pair, written by the apply pass
   ups.push_back({w->bmark.p, nullptr, 4 * ((w->ncells + 31) / 32)});
   ups.push_back({(char*)w->scan_agg.p + scan_regions_offset(scan_nb), nullptr, scan_regions_bytes(scan_nb)});
   if ((rc = issue_uploads(w, ups, s))) return rc;  // the op tables; the chunk order follows the cull launches
@@ -1298,6 +1299,7 @@ int px_build_enqueue(px_world* w, int mode, void* stream) {
   fa.grid = w->d_grid;
   fa.pool32 = w->d_pool32;
   fa.evt = (uint8_t*)w->evt.p;
+  fa.evt_cnt = (uint32_t*)w->cnt.p;
   fa.fsrc = (int64_t*)w->fsrc.p;
   fa.staging32 = (uint32_t*)w->staging.p;
   fa.stage_cap = (uint32_t)stage_cap;

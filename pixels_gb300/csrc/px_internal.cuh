@@ -182,6 +182,7 @@ struct FoldArgs {
   uint32_t* grid;
   const uint32_t* pool32;     // pool viewed as voxel pairs
   uint8_t* evt;               // per pair: 1 = alloc, 2 = free
+  uint32_t* evt_cnt;          // per pair: its number of events (the allocator replay scans these)
   int64_t* fsrc;              // per pair with a free: pair of the brick's last alloc, or -(old index + 1)
   uint32_t* staging32;
   uint32_t stage_cap;
