@@ -295,8 +295,8 @@ def serving_section(args, pyoracle):
 
 
 # DRAM bytes per build of the evaluation kernels (classify, sub-block, voxel,
-# paint, apply), from one ncu capture of each (profiles/build_kernels_penthouse_vpm80.md);
-# the bench cannot run ncu itself
+# paint, apply): dram__bytes_read.sum + dram__bytes_write.sum from one ncu
+# capture of each on the penthouse at vpm=80; the bench cannot run ncu itself
 EVAL_TRAFFIC_BYTES = 33_562_880
 
 

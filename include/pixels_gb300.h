@@ -7,7 +7,7 @@
  *   - the rasteriser and its Builder  src/world/shapes.ts:334-414, :417-431
  *   - the derived upload buffers      src/gpu/GpuWorld.ts:52-113
  * A host binding (Python ctypes in this repository; an N-API addon for the
- * TypeScript host, see INTEGRATION.md) records Builder.add/carve/paint calls as
+ * TypeScript host) records Builder.add/carve/paint calls as
  * a PXIR op list, submits it, and builds on the GPU.  All device memory is
  * owned by the world handle.  Functions return a PX_* status; no C++ exception
  * crosses this boundary; px_last_error() describes the last failure.
