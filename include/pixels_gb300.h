@@ -27,7 +27,7 @@ extern "C" {
 #define PX_OK 0
 #define PX_E_INVALID_ARG 1    /* bad handle, size or mode */
 #define PX_E_INVALID_IR 2     /* malformed op list (bounds, bytecode, NaN/inf parameters) */
-#define PX_E_OOM 3            /* device allocation failed */
+#define PX_E_OOM 3            /* device or host allocation failed */
 #define PX_E_QUEUE_OVERFLOW 4 /* a device work list ran out of room */
 #define PX_E_TIMEOUT 5        /* a bounded device wait gave up */
 #define PX_E_CUDA 6           /* CUDA runtime error */

@@ -4,6 +4,7 @@
 // (voxel ranges, classify thresholds) must round exactly as the reference's
 // JavaScript does (shapes.ts:341-350).
 #include <algorithm>
+#include <new>
 #include <chrono>
 #include <cstdlib>
 #include <atomic>
@@ -372,9 +373,24 @@ int grow_pool(px_world* w, uint64_t need, uint32_t keep, cudaStream_t s) {
 
 }  // namespace
 
+// Host exceptions never cross the C ABI: an entry point that allocates host
+// memory (op tables, worlds) turns a failed allocation into PX_E_OOM.
+template <class F>
+int guarded(px_world* w, F&& f) {
+  try {
+    return f();
+  } catch (const std::bad_alloc&) {
+    if (w) try { w->err = "host allocation failed"; } catch (...) {}
+    return PX_E_OOM;
+  } catch (...) {
+    if (w) try { w->err = "unexpected host exception"; } catch (...) {}
+    return PX_E_CUDA;
+  }
+}
+
 extern "C" {
 
-int px_world_create(int dx, int dy, int dz, double vpm, uint32_t initial_pool_bricks, px_world** out) {
+static int world_create_impl(int dx, int dy, int dz, double vpm, uint32_t initial_pool_bricks, px_world** out) {
   if (!out) return PX_E_INVALID_ARG;
   *out = nullptr;
   if (dx <= 0 || dy <= 0 || dz <= 0 || dx % 8 || dy % 8 || dz % 8) return PX_E_INVALID_ARG;
@@ -931,7 +947,7 @@ uint64_t build_stage_slots(const px_world* w, uint64_t P) { return stage_slots(w
 
 extern "C" {
 
-int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
+static int submit_ops_impl(px_world* w, const void* ir, size_t bytes) {
   if (!w || (!ir && bytes)) return PX_E_INVALID_ARG;
   if (w->batch_locked) return fail(w, PX_E_INVALID_ARG, "the world belongs to a batch");
   if (w->in_flight) return fail(w, PX_E_INVALID_ARG, "a build is in flight");
@@ -1062,7 +1078,7 @@ static int issue_uploads(px_world* w, const std::vector<Upload>& ups, cudaStream
 }
 
 
-int px_build_enqueue(px_world* w, int mode, void* stream) {
+static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   if (!w) return PX_E_INVALID_ARG;
   if (w->batch_locked && !w->capturing) return fail(w, PX_E_INVALID_ARG, "the world belongs to a batch");
   if (w->in_flight) return fail(w, PX_E_INVALID_ARG, "a build is already in flight");
@@ -1394,7 +1410,7 @@ void fill_stats(px_world* w, const BuildResult& r) {
 
 extern "C" {
 
-int px_build_finish(px_world* w) {
+static int build_finish_impl(px_world* w) {
   if (!w) return PX_E_INVALID_ARG;
   if (!w->in_flight) return PX_OK;
   w->in_flight = false;
@@ -1481,7 +1497,7 @@ int px_set_validation(px_world* w, int on) {
   return PX_OK;
 }
 
-int px_world_reset(px_world* w, int requeue_last_ops, void* stream) {
+static int world_reset_impl(px_world* w, int requeue_last_ops, void* stream) {
   if (!w) return PX_E_INVALID_ARG;
   if (w->batch_locked && !w->capturing) return fail(w, PX_E_INVALID_ARG, "the world belongs to a batch");
   if (w->in_flight) return fail(w, PX_E_INVALID_ARG, "a build is in flight");
@@ -1662,7 +1678,7 @@ struct WorldSaved {
 
 }  // namespace
 
-int px_batch_create(px_world* const* worlds, size_t n, int mode, uint32_t n_streams, uint32_t pairs_per_block,
+static int batch_create_impl(px_world* const* worlds, size_t n, int mode, uint32_t n_streams, uint32_t pairs_per_block,
                     px_batch** out) {
   if (!out) return PX_E_INVALID_ARG;
   *out = nullptr;
@@ -1803,5 +1819,34 @@ void px_batch_destroy(px_batch* b) {
 }
 
 const char* px_batch_last_error(px_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+}  // extern "C"
+
+extern "C" {
+
+int px_world_create(int dx, int dy, int dz, double vpm, uint32_t initial_pool_bricks, px_world** out) {
+  return guarded(nullptr, [&] { return world_create_impl(dx, dy, dz, vpm, initial_pool_bricks, out); });
+}
+
+int px_submit_ops(px_world* w, const void* ir, size_t bytes) {
+  return guarded(w, [&] { return submit_ops_impl(w, ir, bytes); });
+}
+
+int px_build_enqueue(px_world* w, int mode, void* stream) {
+  return guarded(w, [&] { return build_enqueue_impl(w, mode, stream); });
+}
+
+int px_build_finish(px_world* w) {
+  return guarded(w, [&] { return build_finish_impl(w); });
+}
+
+int px_world_reset(px_world* w, int requeue_last_ops, void* stream) {
+  return guarded(w, [&] { return world_reset_impl(w, requeue_last_ops, stream); });
+}
+
+int px_batch_create(px_world* const* worlds, size_t n, int mode, uint32_t n_streams, uint32_t pairs_per_block,
+                    px_batch** out) {
+  return guarded(nullptr, [&] { return batch_create_impl(worlds, n, mode, n_streams, pairs_per_block, out); });
+}
 
 }  // extern "C"

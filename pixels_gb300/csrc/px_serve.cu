@@ -16,6 +16,7 @@
 #include <cstring>
 #include <functional>
 #include <mutex>
+#include <new>
 #include <thread>
 #include <vector>
 
@@ -93,7 +94,7 @@ uint64_t brick_bound(const px_edit& e, double vs, int dx, int dy, int dz) {
 
 extern "C" {
 
-int px_serve_run(px_world* w, const px_edit* edits, const double* arrival_s, size_t n, uint32_t max_batch,
+static int serve_run_impl(px_world* w, const px_edit* edits, const double* arrival_s, size_t n, uint32_t max_batch,
                  uint64_t pool_budget_bricks, int mode, void* stream, px_edit_result* results, uint64_t* applied_order,
                  size_t* n_applied) {
   if (!w || (!edits && n) || (!arrival_s && n) || (!results && n) || max_batch == 0) return PX_E_INVALID_ARG;
@@ -235,6 +236,19 @@ int px_serve_run(px_world* w, const px_edit* edits, const double* arrival_s, siz
   producer.join();
   if (n_applied) *n_applied = applied;
   return rc;
+}
+
+// host exceptions (thread or allocation failures) never cross the C ABI
+int px_serve_run(px_world* w, const px_edit* edits, const double* arrival_s, size_t n, uint32_t max_batch,
+                 uint64_t pool_budget_bricks, int mode, void* stream, px_edit_result* results, uint64_t* applied_order,
+                 size_t* n_applied) {
+  try {
+    return serve_run_impl(w, edits, arrival_s, n, max_batch, pool_budget_bricks, mode, stream, results, applied_order, n_applied);
+  } catch (const std::bad_alloc&) {
+    return PX_E_OOM;
+  } catch (...) {
+    return PX_E_CUDA;
+  }
 }
 
 }  // extern "C"
