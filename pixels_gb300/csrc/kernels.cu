@@ -49,6 +49,36 @@ namespace px {
 static unsigned long long g_launches = 0;
 unsigned long long launch_count() { return g_launches; }
 
+// Programmatic dependent launch: the kernels of a build are launched so that
+// each may be scheduled while its predecessor drains.  Every such kernel starts
+// with pdl_prologue(): it waits until the preceding grid has completed and its
+// memory is visible (griddepcontrol.wait), then lets its own successor launch
+// once all of its CTAs have started (griddepcontrol.launch_dependents).
+__device__ __forceinline__ void pdl_prologue() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+// Launched from the host one by one, the overlap hides most of each launch's
+// latency; inside a captured graph (whose launches are already back to back)
+// it measured slower, so captures launch plainly (set_programmatic_launch).
+static thread_local bool g_pdl = true;
+void set_programmatic_launch(bool on) { g_pdl = on; }
+template <typename... KArgs, typename... Args>
+static void launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = g_pdl ? 1 : 0;
+  ++g_launches;
+  cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // ---------------------------------------------------------------------------
 // cull
 
@@ -65,6 +95,7 @@ __device__ __forceinline__ bool box_overlaps_tile(uint2 b, int tx, int ty, int t
 // groups are compact).
 __global__ void __launch_bounds__(256) cull_count_kernel(const uint2* __restrict__ boxes, int n_ops, int TX, int TY, int TZ,
                                                          uint32_t* tile_cnt) {
+  pdl_prologue();
   const int lane = threadIdx.x & 31;
   const int n_tiles = TX * TY * TZ;
   const int n_groups = (n_ops + 31) / 32;
@@ -89,6 +120,7 @@ __global__ void __launch_bounds__(256) cull_count_kernel(const uint2* __restrict
 __global__ void __launch_bounds__(256) cull_fill_kernel(const uint2* __restrict__ boxes, int n_ops, int TX, int TY, int TZ,
                                                         const uint32_t* __restrict__ tile_off, uint32_t* tile_ops,
                                                         uint2* tile_boxes) {
+  pdl_prologue();
   const int lane = threadIdx.x & 31;
   const int n_tiles = TX * TY * TZ;
   const int n_groups = (n_ops + 31) / 32;
@@ -119,13 +151,13 @@ __global__ void __launch_bounds__(256) cull_fill_kernel(const uint2* __restrict_
 void launch_cull_count(const uint2* boxes, int n_ops, int TX, int TY, int TZ, uint32_t* tile_cnt, cudaStream_t s) {
   int n_tiles = TX * TY * TZ;
   int blocks = (n_tiles * 32 + 255) / 256;
-  ++g_launches; cull_count_kernel<<<blocks, 256, 0, s>>>(boxes, n_ops, TX, TY, TZ, tile_cnt);
+  launch_pdl(cull_count_kernel, dim3(blocks), dim3(256), 0, s, boxes, n_ops, TX, TY, TZ, tile_cnt);
 }
 void launch_cull_fill(const uint2* boxes, int n_ops, int TX, int TY, int TZ, const uint32_t* tile_off,
                       uint32_t* tile_ops, uint2* tile_boxes, cudaStream_t s) {
   int n_tiles = TX * TY * TZ;
   int blocks = (n_tiles * 32 + 255) / 256;
-  ++g_launches; cull_fill_kernel<<<blocks, 256, 0, s>>>(boxes, n_ops, TX, TY, TZ, tile_off, tile_ops, tile_boxes);
+  launch_pdl(cull_fill_kernel, dim3(blocks), dim3(256), 0, s, boxes, n_ops, TX, TY, TZ, tile_off, tile_ops, tile_boxes);
 }
 
 // ---------------------------------------------------------------------------
@@ -315,6 +347,7 @@ __device__ __forceinline__ void brick_bases(const FoldArgs& a, const OpDev* O, i
 // (64 voxels on 32 lanes), which keeps the heavy voxel work evenly spread.
 template <int MODE>
 __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIFY64_MINB) classify_kernel(FoldArgs a) {
+  pdl_prologue();
   const int lane = threadIdx.x & 31;
   LaneStats ls = {a.res};
   uint32_t n_brick = 0;
@@ -412,6 +445,7 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
 // voxel masks of lone boxes (per-axis runs), and queues the partial sub-blocks.
 template <int MODE>
 __global__ void __launch_bounds__(256, MODE == 1 ? PX_SUB_MINB : PX_CLASSIFY64_MINB) sub_kernel(FoldArgs a) {
+  pdl_prologue();
   const int lane = threadIdx.x & 31;
   LaneStats ls = {a.res};
   uint32_t st_local = 0;
@@ -539,6 +573,7 @@ __device__ __forceinline__ int lip_decide(const OpDev* O, Iv dc, int ox, int oy,
 // pass, 64 voxel SDFs on 32 lanes, two ballots (shapes.ts:390-394).
 template <int MODE>
 __global__ void __launch_bounds__(256, MODE == 1 ? PX_VOXEL_MINB : PX_CLASSIFY64_MINB) voxel_kernel(FoldArgs a) {
+  pdl_prologue();
   const int lane = threadIdx.x & 31;
   LaneStats ls = {a.res};
   // the classes' item counts in the order they are taken, as an inclusive prefix over lanes
@@ -664,6 +699,7 @@ __device__ __noinline__ uint32_t paint_at_voxel(const double* __restrict__ param
 // certified float32 evaluation first (paint32.cuh).
 template <int MODE>
 __global__ void __launch_bounds__(256) paint_kernel(FoldArgs a) {
+  pdl_prologue();
   const int lane = threadIdx.x & 31;
   // float64 paints (the front of the queue) first, then the certified float32 ones
   const uint32_t n_front = min(__ldg(a.paint_item_counter), a.paint_items_cap);
@@ -742,6 +778,7 @@ __global__ void __launch_bounds__(256) mark_compact_kernel(const uint32_t* __res
                                                            uint32_t BX, uint32_t BY, uint32_t TX, uint32_t TY,
                                                            const uint32_t* __restrict__ tile_cnt, uint32_t* work,
                                                            uint32_t last, uint32_t* counts, BuildResult* res) {
+  pdl_prologue();
   const int lane = threadIdx.x & 31;
   const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t w0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; w0 < n_words; w0 += warps * 32) {
@@ -834,6 +871,7 @@ __device__ __forceinline__ FoldEntry fold_entry(const FoldArgs& a, uint32_t idx,
 // once), then the bricks are applied one after the other.
 template <bool INLINE>
 __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
+  pdl_prologue();
   __shared__ unsigned long long smask[8][8];
   __shared__ __align__(16) unsigned long long spm[8][32][8];  // voxel masks of the looked-up partial pairs
   const int lane = threadIdx.x & 31;
@@ -1112,29 +1150,28 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
 void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEvent_t mid, int max_blocks) {
   auto grid = [&](int per_sm) { return max_blocks > 0 && max_blocks < n_sms * per_sm ? max_blocks : n_sms * per_sm; };
   if (mode == 1) {
-    ++g_launches; classify_kernel<1><<<grid(PX_CLASSIFY_MINB), 256, 0, s>>>(a);
-    ++g_launches; sub_kernel<1><<<grid(PX_SUB_MINB), 256, 0, s>>>(a);
-    ++g_launches; voxel_kernel<1><<<grid(PX_VOXEL_MINB), 256, 0, s>>>(a);
+    launch_pdl(classify_kernel<1>, dim3(grid(PX_CLASSIFY_MINB)), dim3(256), 0, s, a);
+    launch_pdl(sub_kernel<1>, dim3(grid(PX_SUB_MINB)), dim3(256), 0, s, a);
+    launch_pdl(voxel_kernel<1>, dim3(grid(PX_VOXEL_MINB)), dim3(256), 0, s, a);
   } else {
-    ++g_launches; classify_kernel<0><<<grid(PX_CLASSIFY64_MINB), 256, 0, s>>>(a);
-    ++g_launches; sub_kernel<0><<<grid(PX_CLASSIFY64_MINB), 256, 0, s>>>(a);
-    ++g_launches; voxel_kernel<0><<<grid(PX_CLASSIFY64_MINB), 256, 0, s>>>(a);
+    launch_pdl(classify_kernel<0>, dim3(grid(PX_CLASSIFY64_MINB)), dim3(256), 0, s, a);
+    launch_pdl(sub_kernel<0>, dim3(grid(PX_CLASSIFY64_MINB)), dim3(256), 0, s, a);
+    launch_pdl(voxel_kernel<0>, dim3(grid(PX_CLASSIFY64_MINB)), dim3(256), 0, s, a);
   }
   if (a.n_paint_slots) {
-    if (mode == 1) { ++g_launches; paint_kernel<1><<<grid(4), 256, 0, s>>>(a); }
-    else { ++g_launches; paint_kernel<0><<<grid(4), 256, 0, s>>>(a); }
+    if (mode == 1) launch_pdl(paint_kernel<1>, dim3(grid(4)), dim3(256), 0, s, a);
+    else launch_pdl(paint_kernel<0>, dim3(grid(4)), dim3(256), 0, s, a);
   }
   if (mid) cudaEventRecord(mid, s);
   {
     const uint32_t n_words = (uint32_t)(((size_t)a.BX * a.BY * a.BZ + 31) / 32);
     const uint32_t blocks = (n_words + 255) / 256;  // 8 warps per block, 32 words per warp
-    ++g_launches;
-    mark_compact_kernel<<<blocks < 4096 ? blocks : 4096, 256, 0, s>>>(a.bmark, n_words, (uint32_t)a.BX, (uint32_t)a.BY,
-                                                                        (uint32_t)a.TX, (uint32_t)a.TY, a.tile_cnt, a.work,
-                                                                        a.touched_cap, a.work_counter + 1, a.res);
+    launch_pdl(mark_compact_kernel, dim3(blocks < 4096 ? blocks : 4096), dim3(256), 0, s, (const uint32_t*)a.bmark, n_words,
+               (uint32_t)a.BX, (uint32_t)a.BY, (uint32_t)a.TX, (uint32_t)a.TY, (const uint32_t*)a.tile_cnt, a.work,
+               (uint32_t)a.touched_cap, a.work_counter + 1, a.res);
   }
-  if (a.inline_paints) { ++g_launches; fold_kernel<true><<<grid(PX_FOLD_MINB), 256, 0, s>>>(a); }
-  else { ++g_launches; fold_kernel<false><<<grid(PX_FOLD_MINB), 256, 0, s>>>(a); }
+  if (a.inline_paints) launch_pdl(fold_kernel<true>, dim3(grid(PX_FOLD_MINB)), dim3(256), 0, s, a);
+  else launch_pdl(fold_kernel<false>, dim3(grid(PX_FOLD_MINB)), dim3(256), 0, s, a);
 }
 
 // ---------------------------------------------------------------------------
@@ -1238,6 +1275,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_onepass(const typename Op::
                                                               size_t n_max, const uint32_t* n_dev, bool inclusive,
                                                               typename Op::T* total_out, ScanTemp st,
                                                               uint32_t* ticket) {
+  pdl_prologue();
   typedef typename Op::T T;
   __shared__ T sh[32];
   __shared__ T s_prefix;
@@ -1352,8 +1390,8 @@ void scan_any(const typename Op::T* in, typename Op::T* out, size_t n_max, const
     cudaMemsetAsync(regions + r * scan_region_bytes(t.max_blocks), 0, scan_region_bytes(t.max_blocks), s);
   }
   uint32_t* ticket = (uint32_t*)(regions + r * scan_region_bytes(t.max_blocks));
-  ++g_launches;
-  scan_onepass<Op, REV><<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, out, n_max, n_dev, inclusive, total_out, t, ticket);
+  launch_pdl(scan_onepass<Op, REV>, dim3((unsigned)nb), dim3(SCAN_THREADS), 0, s, in, out, n_max, n_dev, inclusive, total_out, t,
+             ticket);
 }
 
 void launch_scan_u32(const uint32_t* in, uint32_t* out, size_t n, const uint32_t* n_dev, bool inclusive,
@@ -1370,6 +1408,7 @@ enum : uint8_t { EV_PUSH = 0, EV_POP = 1 };
 
 
 __global__ void events_build_kernel(ReplayArgs a) {
+  pdl_prologue();
   const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
   if (tid == 0) a.res->n_events = a.H + (a.P ? a.pos[a.P - 1] + a.cnt[a.P - 1] : 0u);
   for (size_t i = tid; i < a.H; i += stride) {
@@ -1400,6 +1439,7 @@ __global__ void events_build_kernel(ReplayArgs a) {
 // and the pops that find the stack empty (they take poolUsed++).
 __global__ void depth_fresh_kernel(const int2* __restrict__ fn, const uint8_t* __restrict__ etype, int32_t* depth,
                                    uint32_t* fresh, const BuildResult* res) {
+  pdl_prologue();
   const size_t E = res->n_events;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (size_t)gridDim.x * blockDim.x) {
     const int2 f = __ldg(fn + e);
@@ -1427,6 +1467,7 @@ __device__ __forceinline__ size_t level_size(size_t E, int l) {
 // Level l of the min tree: entry k = the minimum of entries 32k .. 32k + 31 of
 // level l - 1 (one coalesced load per entry below, a warp minimum per entry).
 __global__ void tree_level_kernel(const int32_t* __restrict__ below, int32_t* level, int l, const BuildResult* res) {
+  pdl_prologue();
   const size_t n_below = level_size(res->n_events, l - 1);
   const size_t n32 = ((n_below + 31) >> 5) << 5;  // a whole warp per entry: the loop bound is warp-uniform
   for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n32; c += (size_t)gridDim.x * blockDim.x) {
@@ -1482,6 +1523,7 @@ __device__ long long prev_less(const int32_t* depth, const int32_t* tree, const 
 }
 
 __global__ void match_kernel(ReplayArgs a, TreeLevels tl) {
+  pdl_prologue();
   const size_t E = a.res->n_events;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (size_t)gridDim.x * blockDim.x) {
     if (a.etype[e] != EV_POP) continue;
@@ -1496,6 +1538,7 @@ __global__ void match_kernel(ReplayArgs a, TreeLevels tl) {
 }
 
 __global__ void resolve_kernel(unsigned long long* ew, BuildResult* res) {
+  pdl_prologue();
   const size_t E = res->n_events;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (size_t)gridDim.x * blockDim.x) {
     unsigned long long w = ew[e];
@@ -1516,6 +1559,7 @@ __global__ void resolve_kernel(unsigned long long* ew, BuildResult* res) {
 __global__ void holes_out_kernel(const uint8_t* __restrict__ etype, const int32_t* __restrict__ depth,
                                  const int32_t* __restrict__ sufmin, const unsigned long long* __restrict__ ew,
                                  uint32_t* holes_out, BuildResult* res, uint32_t U0) {
+  pdl_prologue();
   const size_t E = res->n_events;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (size_t)gridDim.x * blockDim.x) {
     if (etype[e] != EV_PUSH) continue;
@@ -1543,10 +1587,10 @@ void launch_replay(const ReplayArgs& a, cudaStream_t s) {
   const size_t cap = (size_t)n_sms * 8;
   auto blocks = [&](size_t n) { size_t b = (n + T - 1) / T; return (int)(b < cap ? (b ? b : 1) : cap); };
   scan_any<SumOp, false>(a.cnt, a.pos, a.P, nullptr, false, nullptr, *a.scan, s);
-  ++g_launches; events_build_kernel<<<blocks(a.P > a.H ? a.P : a.H), T, 0, s>>>(a);  // also the event count
+  launch_pdl(events_build_kernel, dim3(blocks(a.P > a.H ? a.P : a.H)), dim3(T), 0, s, a);  // also the event count
   const uint32_t* nE = &a.res->n_events;
   scan_any<DepthOp, false>(a.depth_fn, a.depth_fn, a.E_max, nE, true, nullptr, *a.scan, s);
-  ++g_launches; depth_fresh_kernel<<<blocks(a.E_max), T, 0, s>>>(a.depth_fn, a.etype, a.depth, a.fresh, a.res);
+  launch_pdl(depth_fresh_kernel, dim3(blocks(a.E_max)), dim3(T), 0, s, (const int2*)a.depth_fn, (const uint8_t*)a.etype, a.depth, a.fresh, (const BuildResult*)a.res);
   scan_any<SumOp, false>(a.fresh, a.fresh_rank, a.E_max, nE, false, &a.res->n_fresh, *a.scan, s);
   // min tree over the depths
   TreeLevels tl;
@@ -1559,20 +1603,21 @@ void launch_replay(const ReplayArgs& a, cudaStream_t s) {
   }
   for (int l = 1; l <= tl.n; l++) {
     const int32_t* below = l == 1 ? a.depth : a.tree + tl.off[l - 2];
-    ++g_launches; tree_level_kernel<<<blocks(level_size_host(a.E_max, l - 1)), T, 0, s>>>(below, a.tree + tl.off[l - 1], l, a.res);
+    launch_pdl(tree_level_kernel, dim3(blocks(level_size_host(a.E_max, l - 1))), dim3(T), 0, s, below, a.tree + tl.off[l - 1], l, (const BuildResult*)a.res);
   }
-  ++g_launches; match_kernel<<<blocks(a.E_max), T, 0, s>>>(a, tl);
-  ++g_launches; resolve_kernel<<<blocks(a.E_max), T, 0, s>>>(a.ew, a.res);
+  launch_pdl(match_kernel, dim3(blocks(a.E_max)), dim3(T), 0, s, a, tl);
+  launch_pdl(resolve_kernel, dim3(blocks(a.E_max)), dim3(T), 0, s, a.ew, a.res);
   // suffix minimum of the depths (stored after the tree levels)
   int32_t* sufmin = a.tree + off;
   scan_any<MinOp, true>(a.depth, sufmin, a.E_max, nE, true, nullptr, *a.scan, s);
-  ++g_launches; holes_out_kernel<<<blocks(a.E_max), T, 0, s>>>(a.etype, a.depth, sufmin, a.ew, a.holes_out, a.res, a.U0);
+  launch_pdl(holes_out_kernel, dim3(blocks(a.E_max)), dim3(T), 0, s, (const uint8_t*)a.etype, (const int32_t*)a.depth, (const int32_t*)sufmin, (const unsigned long long*)a.ew, a.holes_out, a.res, a.U0);
 }
 
 // ---------------------------------------------------------------------------
 // finalize: staging -> pool at the replayed indices, grid entries
 
 __global__ void __launch_bounds__(256) finalize_kernel(FinalizeArgs a) {
+  pdl_prologue();
   // commit only a complete build: every staging slot written, every pool index within the pool
   if (a.res->status & (ST_STAGE_OVERFLOW | ST_CHAIN)) return;
   if (a.res->pool_used > a.pool_cap) {
@@ -1645,7 +1690,7 @@ void launch_finalize(const FinalizeArgs& a, uint32_t touched_cap, cudaStream_t s
   size_t warps = touched_cap ? (touched_cap + 31) / 32 : 1;
   size_t b = (warps * 32 + 255) / 256;
   int blocks = (int)(b < 8192 ? b : 8192);
-  ++g_launches; finalize_kernel<<<blocks, 256, 0, s>>>(a);
+  launch_pdl(finalize_kernel, dim3(blocks), dim3(256), 0, s, a);
 }
 
 // ---------------------------------------------------------------------------
@@ -1710,6 +1755,7 @@ __global__ void __launch_bounds__(256) derive_kernel(const uint32_t* __restrict_
 // memory the GPU reads through the host page tables) and counter clears in one
 // launch: entry blockIdx.y, 16-byte words, then the last bytes of an entry.
 __global__ void __launch_bounds__(256) upload_kernel(HostUploads u) {
+  pdl_prologue();
   const HostUploads::Entry& e = u.e[blockIdx.y];
   const size_t n16 = e.bytes >> 4;
   const uint4* src = reinterpret_cast<const uint4*>(e.src);
@@ -1723,8 +1769,7 @@ __global__ void __launch_bounds__(256) upload_kernel(HostUploads u) {
 }
 void launch_uploads(const HostUploads& u, cudaStream_t s) {
   if (u.n == 0) return;
-  ++g_launches;
-  upload_kernel<<<dim3(32, (unsigned)u.n), 256, 0, s>>>(u);
+  launch_pdl(upload_kernel, dim3(32, (unsigned)u.n), dim3(256), 0, s, u);
 }
 
 void launch_derive(const uint32_t* grid, const uint32_t* pool32, int BX, int BY, int BZ, const uint8_t* opaque,

@@ -1079,6 +1079,7 @@ static int issue_uploads(px_world* w, const std::vector<Upload>& ups, cudaStream
 
 
 static int build_enqueue_impl(px_world* w, int mode, void* stream) {
+  set_programmatic_launch(!w->capturing);
   if (!w) return PX_E_INVALID_ARG;
   if (w->batch_locked && !w->capturing) return fail(w, PX_E_INVALID_ARG, "the world belongs to a batch");
   if (w->in_flight) return fail(w, PX_E_INVALID_ARG, "a build is already in flight");

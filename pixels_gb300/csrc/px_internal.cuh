@@ -280,6 +280,9 @@ void launch_derive(const uint32_t* grid, const uint32_t* pool32, int BX, int BY,
                    const uint8_t* opaque, const uint8_t* udens, uint32_t* super_counts,
                    uint8_t* density, cudaStream_t s);
 
+// Build kernels launched by this thread overlap their predecessors' tails
+// (programmatic dependent launch) unless switched off (graph captures).
+void set_programmatic_launch(bool on);
 float probe_fma_tflops(int fp64, int n_sms);
 unsigned long long launch_count();
 
