@@ -105,7 +105,14 @@ struct px_world {
   DevBuf chunk_op, pcode, psub, pmask, chunk_counter, vitems, pitems;
   std::vector<uint32_t> h_chunk_op;  // the chunks in classify order: (chunk, op of its first pair | single-op bit)
   std::vector<Upload> h_uploads;     // the op-table copies of the build being enqueued
-  std::vector<uint32_t> h_painted, h_painted32;  // the build's painted ops, float64-only ones first
+  std::vector<uint32_t> h_painted;  // the build's painted ops, float64-only ones first
+  // totals of the queued op list, summed as it is converted: (op, brick) pairs,
+  // tile-list entries, painted ops (float64-only and certified float32 ones)
+  struct QueueTotals {
+    uint64_t pairs = 0, tile_pairs = 0;
+    std::vector<uint32_t> painted64, painted32;
+    void clear() { pairs = tile_pairs = 0; painted64.clear(); painted32.clear(); }
+  } q, last_q;
   std::vector<uint8_t> h_op_bucket;  // per op: cost bucket (0..63) of one evaluation
   uint8_t class_order[VCLASSES] = {0};  // sub-block / voxel class order of the resident ops
   DevBuf paint_items, pvals;    // sub-blocks to paint and the paint values
@@ -561,6 +568,8 @@ struct SubmitChunk {
   std::vector<uint32_t> code32;    // float32 parameter offset per instruction
   std::vector<float2> bases, p32;
   std::vector<uint32_t> xfix;      // instructions whose parameter offset is a polygon record
+  uint64_t n_pairs = 0, n_tile_pairs = 0;        // the range's (op, brick) pairs and tile-list entries
+  std::vector<uint32_t> painted64, painted32;    // its painted ops (range-local indices)
   int rc = PX_OK;
   std::string err;
 };
@@ -779,6 +788,17 @@ int convert_ops(const px_world* w, const IrOp* iops, size_t i0, size_t i1, const
       (void)p32_before;
     }
     d.cost = op_cost(code + 2 * (size_t)o.code_begin, o.code_len, d.flags);
+    // the op's first (op, brick) pair (range-local; rebased when the ranges merge), its
+    // tile-list entries, and whether its paint is called per voxel
+    d.pair_base = out.n_pairs;
+    d.paint_slot = NO_SLOT;
+    if (d.bx0 <= d.bx1) {
+      out.n_pairs += (uint64_t)d.nx * d.ny * (uint64_t)(d.bz1 - d.bz0 + 1);
+      out.n_tile_pairs += (uint64_t)(d.bx1 / 4 - d.bx0 / 4 + 1) * (uint64_t)(d.by1 / 4 - d.by0 / 4 + 1) *
+                          (uint64_t)(d.bz1 / 4 - d.bz0 / 4 + 1);
+      if (d.kind != KIND_CARVE && d.paint_kind != PK_CONST)
+        (d.paint32_off == NO_SLOT ? out.painted64 : out.painted32).push_back((uint32_t)out.ops.size());
+    }
     out.ops.push_back(d);
     out.boxes.push_back(box);
   }
@@ -990,9 +1010,10 @@ static int submit_ops_impl(px_world* w, const void* ir, size_t bytes) {
   // copied at once (the IR's own parameters as one more job)
   struct Place {
     size_t code, p32, bases, ops, xp;
+    uint64_t pairs;
   };
   std::vector<Place> at(n_chunks);
-  Place end = {w->code.size(), w->p32.size(), w->bases.size(), w->ops.size(), param_base + n_params};
+  Place end = {w->code.size(), w->p32.size(), w->bases.size(), w->ops.size(), param_base + n_params, w->q.pairs};
   for (int k = 0; k < n_chunks; k++) {
     const SubmitChunk& c = chunks[k];
     at[k] = end;
@@ -1001,7 +1022,12 @@ static int submit_ops_impl(px_world* w, const void* ir, size_t bytes) {
     end.bases += c.bases.size();
     end.ops += c.ops.size();
     end.xp += c.xparams.size();
+    end.pairs += c.n_pairs;
+    w->q.tile_pairs += c.n_tile_pairs;
+    for (uint32_t i : c.painted64) w->q.painted64.push_back((uint32_t)at[k].ops + i);
+    for (uint32_t i : c.painted32) w->q.painted32.push_back((uint32_t)at[k].ops + i);
   }
+  w->q.pairs = end.pairs;
   w->code.resize(end.code);
   w->code32.resize(end.code);
   w->p32.resize(end.p32);
@@ -1021,6 +1047,7 @@ static int submit_ops_impl(px_world* w, const void* ir, size_t bytes) {
     for (OpDev& d : c.ops) {
       d.code_off += (uint32_t)pl.code;
       d.base_off += (uint32_t)pl.bases;
+      d.pair_base += pl.pairs;
       if (d.paint32_off != NO_SLOT) d.paint32_off += (uint32_t)pl.p32;
     }
     auto put = [](auto& dst, size_t pos, const auto& src) {
@@ -1089,27 +1116,12 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   const int n_ops = (int)w->ops.size();
   int rc;
 
-  // (op, brick) pair bases and the tile-list bound
-  uint64_t P = 0, tile_pairs = 0;
-  // ops with paint calls: float64-only ones, then certified float32 ones
-  std::vector<uint32_t>& painted = w->h_painted;
-  std::vector<uint32_t>& painted32 = w->h_painted32;
-  painted.clear();
-  painted32.clear();
-  for (int i = 0; i < n_ops; i++) {
-    OpDev& o = w->ops[i];
-    o.pair_base = P;
-    o.paint_slot = NO_SLOT;
-    if (o.bx0 > o.bx1) continue;
-    if (o.kind != KIND_CARVE && o.paint_kind != PK_CONST) (o.paint32_off == NO_SLOT ? painted : painted32).push_back((uint32_t)i);
-    uint64_t nz = (uint64_t)(o.bz1 - o.bz0 + 1);
-    P += (uint64_t)o.nx * o.ny * nz;
-    uint64_t tx = (uint64_t)(o.bx1 / 4 - o.bx0 / 4 + 1), ty = (uint64_t)(o.by1 / 4 - o.by0 / 4 + 1),
-             tz = (uint64_t)(o.bz1 / 4 - o.bz0 / 4 + 1);
-    tile_pairs += tx * ty * tz;
-  }
+  // (op, brick) pair bases (set as the ops were converted) and the tile-list bound
+  const uint64_t P = w->q.pairs, tile_pairs = w->q.tile_pairs;
+  std::vector<uint32_t>& painted = w->h_painted;  // float64-only paints first
+  painted.assign(w->q.painted64.begin(), w->q.painted64.end());
   if (P > 0x1fffffffull) return fail(w, PX_E_QUEUE_OVERFLOW, "too many (op, brick) pairs in one build: %llu", (unsigned long long)P);
-  painted.insert(painted.end(), painted32.begin(), painted32.end());
+  painted.insert(painted.end(), w->q.painted32.begin(), w->q.painted32.end());
   // paint slots (one per (op, brick) pair of a painted op, 2 KiB each): every
   // painted op when they fit in 512 MiB, else the heavy kinds alone when they
   // fit, else none; ops without a slot have their paints called by the apply pass
@@ -1470,6 +1482,8 @@ static int build_finish_impl(px_world* w) {
   w->last_code32.swap(w->code32);
   w->last_p32.swap(w->p32);
   w->last_bases.swap(w->bases);
+  std::swap(w->last_q, w->q);
+  w->q.clear();
   w->code32.clear();
   w->p32.clear();
   w->bases.clear();
@@ -1519,6 +1533,7 @@ static int world_reset_impl(px_world* w, int requeue_last_ops, void* stream) {
     w->code32 = w->last_code32;
     w->p32 = w->last_p32;
     w->bases = w->last_bases;
+    w->q = w->last_q;
     w->ops_resident = true;  // the device tables of the last build still hold them
   }
   return PX_OK;
@@ -1766,6 +1781,7 @@ static int batch_create_impl(px_world* const* worlds, size_t n, int mode, uint32
     w->pairs_per_block = saved[i].ppb;
     w->ops.clear(); w->boxes.clear(); w->code.clear(); w->params.clear();
     w->code32.clear(); w->p32.clear(); w->bases.clear();
+    w->q.clear();
   }
   if (rc == PX_OK && ce != cudaSuccess) rc = batch_fail(b, PX_E_CUDA, "capture: %s", cudaGetErrorString(ce));
   if (rc == PX_OK && cudaGraphInstantiate(&b->exec, b->graph, 0) != cudaSuccess)
