@@ -2,10 +2,13 @@
 
 A step is one complete build of the penthouse scene (2,429 ops) into an empty
 1280x352x960 world (432,537,600 cells): brick / sub-block / voxel
-classification, paint, pool allocation replay and the pool / grid write-out.
+classification, paint, pool allocation replay, the pool / grid write-out and
+the derived upload buffers (super-grid counts, density, the GPU free list).
 ``value`` is Gvoxels/s (grid cells per second of device time, ops already
 resident in HBM); ``e2e`` is the same metric through the public C ABI with the
-op list uploaded from host memory and the grid and pool read back every step.
+op list uploaded from host memory and grid, pool, super counts, density and
+free list read back every step (``e2e.with_host_flatten`` also runs the scene
+program and flattens it to PXIR on the host every step).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -31,6 +34,49 @@ sys.path.insert(0, ROOT)
 METRIC = "Gvoxels/s at vpm=80 (mixed vs all-FP64 GPU, 0 mismatches); edit p50/p99 ms"
 UNIT = "Gvoxels/s"
 VPM = 80.0
+
+
+def node_runtime() -> dict:
+    """The JavaScript runtime the reference would run under on this host, if any."""
+    import shutil
+    path = shutil.which("node")
+    if not path:
+        return {"node": "absent"}
+    try:
+        v = subprocess.run([path, "--version"], capture_output=True, text=True, timeout=10).stdout.strip()
+    except (OSError, subprocess.SubprocessError):
+        v = "unknown"
+    return {"node": v, "node_path": path}
+
+
+def world_mismatches(h, o, cfg, max_bricks=1 << 31) -> dict:
+    """Every output of a built world against the oracle's: grid entries, live pool
+    voxels, poolUsed, holes, super counts, density bytes and the GPU free list."""
+    import numpy as np
+    from pixels_gb300 import _lib
+    n = cfg.bricks[0] * cfg.bricks[1] * cfg.bricks[2]
+    grid = _lib.read_grid(h, n)
+    pool = _lib.read_pool(h)
+    st = _lib.stats(h)
+    n_super = ((cfg.bricks[0] + 3) // 4) * ((cfg.bricks[1] + 3) // 4) * ((cfg.bricks[2] + 3) // 4)
+    d = _lib.read_derived(h, max_bricks, n, n_super)
+    holes = _lib.read_holes(h)
+    out = {"grid_cells": int(np.count_nonzero(grid != o.grid)),
+           "pool_used": int(st["pool_used"]) - int(o.pool_used),
+           "holes": 0 if np.array_equal(holes, o.free_holes) else max(1, len(holes) ^ len(o.free_holes)),
+           "super": int(np.count_nonzero(d["super"] != o.super)),
+           "density": int(np.count_nonzero(d["density"] != o.density))}
+    fl = o.free_list(max_bricks)
+    out["free_list"] = (int(np.count_nonzero(d["free_list"] != fl)) if len(fl) == len(d["free_list"])
+                        else abs(len(fl) - len(d["free_list"])))
+    if out["grid_cells"] == 0 and out["pool_used"] == 0:
+        live = np.nonzero((o.grid != 0) & ((o.grid & 0x80000000) == 0))[0]
+        idx = o.grid[live].astype(np.int64) - 1
+        out["pool_voxels"] = int(np.count_nonzero(pool.reshape(-1, 512)[idx] != o.pool.reshape(-1, 512)[idx]))
+    else:
+        out["pool_voxels"] = -1
+    out["total"] = sum(abs(v) for v in out.values())
+    return out
 
 
 def _env_int(k, d):
@@ -126,7 +172,8 @@ def reference_arm(args):
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        pyoracle.OracleWorld(ir, VPM, cfg.dims, threads=threads)
+        o = pyoracle.OracleWorld(ir, VPM, cfg.dims, threads=threads)  # build + super counts + density
+        o.free_list()                                                  # GpuWorld.ts:103-109
         times.append(time.perf_counter() - t0)
     t = statistics.mean(times)
     v = cfg.cells / t / 1e9
@@ -138,7 +185,8 @@ def reference_arm(args):
                    "cells": cfg.cells, "ops": len(prog)},
         "cpu_baseline": {"value": round(v, 6), "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{args.steps} full penthouse builds at vpm=80 (float64 restatement of "
-                                   f"shapes.ts apply + VoxelWorld + GpuWorld derived buffers)"},
+                                   f"shapes.ts apply + VoxelWorld + GpuWorld derived buffers and free list)",
+                         **node_runtime()},
         "e2e": {"value": round(v, 6), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
 
@@ -162,8 +210,8 @@ def _device_ms(build_fn, steps, warmup):
 def synthetic_section(args, pyoracle):
     """Seeded synthetic scene: 4,096 primitives (box, rounded box, cylinder, capsule,
     torus, 8-point lathe, extruded hexagon; 30% subtract, 10% intersect; 25% noise
-    paint) in the 16 x 4.4 x 12 m volume at vpm=80, both forms, checked against the oracle."""
-    import numpy as np
+    paint) in the 16 x 4.4 x 12 m volume at vpm=80, both forms, each checked
+    against the oracle right after it is timed (every output of the world)."""
     from pixels_gb300 import _lib, config
     from pixels_gb300.scenes.synthetic import synthetic_program
     from pixels_gb300.world import MODE_FP64, MODE_MIXED
@@ -171,7 +219,9 @@ def synthetic_section(args, pyoracle):
     cfg = config.Config(vpm)
     prog = synthetic_program(1, 4096, vpm)
     ir = prog.to_bytes()
+    o = pyoracle.OracleWorld(ir, vpm, cfg.dims, threads=os.cpu_count() or 1)
     h = _lib.world_create(*cfg.dims, vpm, 1 << 15)
+    _lib.set_derive_on_build(h, 1 << 31)
     _lib.submit_ops(h, ir)
     _lib.build(h, MODE_MIXED)
     res = {"workload": "synthetic seed 1, 4096 primitives, vpm=80", "ops": len(prog), "cells": cfg.cells}
@@ -180,19 +230,14 @@ def synthetic_section(args, pyoracle):
             _lib.world_reset(h, True)
             _lib.build(h, mode)
         t = _device_ms(one, max(2, args.steps // 2), 2)
-        res[name] = {"ms_per_step": round(t, 4), "value": round(cfg.cells / (t * 1e-3) / 1e9, 3)}
-    st = _lib.stats(h)
-    grid = _lib.read_grid(h, cfg.bricks[0] * cfg.bricks[1] * cfg.bricks[2])
-    pool = _lib.read_pool(h)
-    o = pyoracle.OracleWorld(ir, vpm, cfg.dims, threads=os.cpu_count() or 1)
-    live = np.nonzero((o.grid != 0) & ((o.grid & 0x80000000) == 0))[0]
-    idx = o.grid[live].astype(np.int64) - 1
-    res["mismatches"] = {"grid_cells": int(np.count_nonzero(grid != o.grid)),
-                         "pool_voxels": int(np.count_nonzero(pool.reshape(-1, 512)[idx] != o.pool.reshape(-1, 512)[idx]))
-                         if st["pool_used"] == o.pool_used else -1,
-                         "pool_used": int(st["pool_used"]) - int(o.pool_used)}
-    res["rescued_voxels"] = st["rescued_voxel"]
-    res["voxel_evals"] = st["voxel_evals"]
+        st = _lib.stats(h)
+        res[name] = {"ms_per_step": round(t, 4), "value": round(cfg.cells / (t * 1e-3) / 1e9, 3),
+                     "mismatches": world_mismatches(h, o, cfg), "voxel_evals": st["voxel_evals"]}
+        if mode == MODE_MIXED:
+            res[name]["rescued_voxels"] = st["rescued_voxel"]
+            res[name]["rescued"] = st["rescued"]
+            res[name]["max_abs_d32_minus_d64"] = st["max_abs_err32"]
+    res["speedup_mixed_vs_fp64"] = round(res["fp64"]["ms_per_step"] / res["mixed"]["ms_per_step"], 3)
     _lib.world_destroy(h)
     return res
 
@@ -300,16 +345,17 @@ def serving_section(args, pyoracle):
 EVAL_TRAFFIC_BYTES = 33_562_880
 
 
-def hbm_line(cfg, pool_used, ir_bytes, ms):
-    """Algorithmic HBM bytes of one build (outputs written + the op list read
-    once) over the build time, against the measured copy bandwidth."""
+def hbm_line(cfg, pool_used, ir_bytes, ms, derived_bytes=0):
+    """Algorithmic HBM bytes of one build (outputs written -- grid, pool, and the
+    derived super counts, density and free list -- plus the op list read once)
+    over the build time, against the measured copy bandwidth."""
     peak = None
     try:
         peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]
     except (OSError, KeyError, ValueError):
         pass
     n_bricks = cfg.bricks[0] * cfg.bricks[1] * cfg.bricks[2]
-    alg = 4 * n_bricks + 1024 * int(pool_used) + int(ir_bytes)
+    alg = 4 * n_bricks + 1024 * int(pool_used) + int(ir_bytes) + int(derived_bytes)
     gbs = alg / (ms * 1e-3) / 1e9
     return {"alg_bytes_per_build": alg, "achieved_gbs": round(gbs, 2), "peak_gbs": peak,
             "frac": round(gbs / peak, 5) if peak else None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
@@ -358,6 +404,8 @@ def main():
     stream = torch.cuda.current_stream(dev)
     s_ptr = stream.cuda_stream
     h = _lib.world_create(*cfg.dims, vpm, 1 << 15)
+    MAX_BRICKS = 1 << 31
+    _lib.set_derive_on_build(h, MAX_BRICKS)  # every build ends with super counts, density and free list
     _lib.submit_ops(h, ir)
     _lib.build(h, MODE_FP64 if args.mode == "fp64" else MODE_MIXED, s_ptr)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)   # 256 MB > L2 (129 MB)
@@ -439,55 +487,79 @@ def main():
     value = job_value(world, cells, t_mx * 1e-3)
     value64 = job_value(world, cells, t_64 * 1e-3)
 
-    # end to end through the C ABI: op list from host memory, grid + pool back to pinned host memory
-    grid_h = torch.empty(cfg.bricks[0] * cfg.bricks[1] * cfg.bricks[2], dtype=torch.int32, pin_memory=True)
+    # end to end through the C ABI: op list from host memory; grid, pool, super counts,
+    # density and free list back to pinned host memory
+    import ctypes
+    n_bricks = cfg.bricks[0] * cfg.bricks[1] * cfg.bricks[2]
+    n_super = ((cfg.bricks[0] + 3) // 4) * ((cfg.bricks[1] + 3) // 4) * ((cfg.bricks[2] + 3) // 4)
+    grid_h = torch.empty(n_bricks, dtype=torch.int32, pin_memory=True)
     pool_h = torch.empty(max(st["pool_used"], 1) * 512, dtype=torch.int16, pin_memory=True)
-    ir_buf = __import__("ctypes").create_string_buffer(ir, len(ir))
-    e2e = []
-    e2e_parts = []
-    for i in range(0 if args.no_e2e else args.warmup + args.steps):
-        torch.cuda.synchronize()
-        barrier()
+    super_h = torch.empty(n_super, dtype=torch.int32, pin_memory=True)
+    dens_h = torch.empty(n_bricks, dtype=torch.uint8, pin_memory=True)
+    free_len = ctypes.c_uint32()
+    assert L.px_read_free_list(h, MAX_BRICKS, None, 0, ctypes.byref(free_len)) == 0
+    free_h = torch.empty(free_len.value + 4096, dtype=torch.int32, pin_memory=True)
+    ir_buf = ctypes.create_string_buffer(ir, len(ir))
+
+    def e2e_step(flatten: bool):
         t0 = time.perf_counter()
+        if flatten:  # the scene program and its flattening to PXIR on the host
+            p_, _ = penthouse_program(vpm)
+            ir_ = p_.to_bytes()
+            buf = ctypes.create_string_buffer(ir_, len(ir_))
+        else:
+            buf, ir_ = ir_buf, ir
+        tf = time.perf_counter()
         _lib.world_reset(h, False, s_ptr)
-        rc = L.px_submit_ops(h, ir_buf, len(ir))
-        assert rc == 0
+        assert L.px_submit_ops(h, buf, len(ir_)) == 0
         ta = time.perf_counter()
         _lib.build(h, MODE_MIXED, s_ptr)
-        used = _lib.stats(h)["pool_used"]
+        used_ = _lib.stats(h)["pool_used"]
         tb = time.perf_counter()
         assert L.px_read_grid(h, grid_h.data_ptr(), grid_h.numel()) == 0
         assert L.px_read_pool(h, pool_h.data_ptr(), pool_h.numel()) == 0
+        assert L.px_read_super(h, super_h.data_ptr(), super_h.numel()) == 0
+        assert L.px_read_density(h, dens_h.data_ptr(), dens_h.numel()) == 0
+        assert L.px_read_free_list(h, MAX_BRICKS, free_h.data_ptr(), free_h.numel(), ctypes.byref(free_len)) == 0
         t1 = time.perf_counter()
-        if i >= args.warmup:
-            e2e.append(t1 - t0)
-            e2e_parts.append((ta - t0, tb - ta, t1 - tb))
+        return used_, (tf - t0, ta - tf, tb - ta, t1 - tb)
+
+    e2e, e2e_parts, e2e_fl = [], [], []
+    used = st["pool_used"]
+    for flatten in (False, True):
+        for i in range(0 if args.no_e2e else args.warmup + args.steps):
+            torch.cuda.synchronize()
+            barrier()
+            used, parts = e2e_step(flatten)
+            if i >= args.warmup:
+                (e2e_fl if flatten else e2e).append(sum(parts))
+                if not flatten:
+                    e2e_parts.append(parts[1:])
     if not e2e:  # profiling run: one readback for the mismatch check
-        assert L.px_read_grid(h, grid_h.data_ptr(), grid_h.numel()) == 0
-        used = _lib.stats(h)["pool_used"]
-        pool_h = torch.empty(max(used, 1) * 512, dtype=torch.int16, pin_memory=True)
-        assert L.px_read_pool(h, pool_h.data_ptr(), pool_h.numel()) == 0
-        e2e = [float("nan")]
-    t_e2e = max_over_ranks([statistics.mean(e2e)], dist, dev)[0]
+        used, _ = e2e_step(False)
+        e2e = e2e_fl = [float("nan")]
+    t_e2e, t_e2e_fl = max_over_ranks([statistics.mean(e2e), statistics.mean(e2e_fl)], dist, dev)
     e2e_value = job_value(world, cells, t_e2e)
+    d2h = int(grid_h.numel() * 4 + used * 1024 + super_h.numel() * 4 + dens_h.numel() + free_len.value * 4)
 
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
         return
 
-    # mismatches against the float64 oracle at the full size (outside the timed region)
+    # mismatches against the float64 oracle at the full size (outside the timed region):
+    # the world the last e2e step built (mixed form), every output
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
     t0 = time.perf_counter()
     o = pyoracle.OracleWorld(ir, vpm, cfg.dims, count_flops=True)
     t_cpu1 = time.perf_counter() - t0
-    grid = grid_h.numpy().view(np.uint32)
-    mism_grid = int(np.count_nonzero(grid != o.grid))
-    pool = pool_h.numpy().view(np.uint16)[: used * 512]
-    live = np.nonzero((o.grid != 0) & ((o.grid & 0x80000000) == 0))[0]
-    idx = o.grid[live].astype(np.int64) - 1
-    mism_vox = int(np.count_nonzero(pool.reshape(-1, 512)[idx] != o.pool.reshape(-1, 512)[idx])) if used == o.pool_used else -1
+    mism = world_mismatches(h, o, cfg, MAX_BRICKS)
+    mism64 = None
+    if have64:  # the float64 form's world, rebuilt once
+        _lib.world_reset(h, True, s_ptr)
+        _lib.build(h, MODE_FP64, s_ptr)
+        mism64 = world_mismatches(h, o, cfg, MAX_BRICKS)
 
     # CPU baseline: the oracle, one thread, a bounded sample
     cpu = None
@@ -500,7 +572,7 @@ def main():
             times.append(time.perf_counter() - t0)
         tc = statistics.mean(times[1:] or times)
         cpu = {"value": round(cells / tc / 1e9, 6), "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"{len(times)} full penthouse builds at vpm=80, single thread"}
+               "sample": f"{len(times)} full penthouse builds at vpm=80, single thread", **node_runtime()}
 
     # roofline of the dominant kernel (fold): algorithmic float ops from the oracle ledger
     alg_ops = o.stats["flops"] + o.stats["divs"] + o.stats["sqrts"]
@@ -525,23 +597,29 @@ def main():
                   "stream_ms_per_step: the same build launched kernel by kernel (px_build_enqueue)",
         "classify_ms": cls_mx,
         "speedup_mixed_vs_fp64": round(t_64 / t_mx, 3) if have64 else None,
-        "mismatches": {"grid_cells": mism_grid, "pool_voxels": mism_vox, "pool_used": int(used) - int(o.pool_used)},
+        "mismatches": mism,
+        "mismatches_fp64_form": mism64,
         "rescued": {"total": st["rescued"], "brick": st["rescued_brick"], "sub": st["rescued_sub"],
                     "voxel": st["rescued_voxel"], "polygon_test": st["rescued_polygon"],
                     "paint": st["rescued_paint"],
                     "fraction_of_voxel_evals": round(st["rescued_voxel"] / max(st["voxel_evals"], 1), 6)},
         "max_abs_d32_minus_d64": st["max_abs_err32"],
         "e2e": {"value": round(e2e_value, 4), "unit": UNIT, "h2d_bytes_per_step": len(ir),
-                "d2h_bytes_per_step": int(grid_h.numel() * 4 + used * 1024),
+                "d2h_bytes_per_step": d2h,
                 "ms_per_step": round(t_e2e * 1e3, 3),
+                "reads": "grid, pool, super counts, density, free list",
                 "split_ms": ({k: round(statistics.mean(p[j] for p in e2e_parts) * 1e3, 3)
-                              for j, k in enumerate(("reset_and_submit", "build", "read_grid_and_pool"))}
-                             if e2e_parts else None)},
+                              for j, k in enumerate(("reset_and_submit", "build_and_derive", "read_outputs"))}
+                             if e2e_parts else None),
+                "with_host_flatten": {"value": round(job_value(world, cells, t_e2e_fl), 4),
+                                      "ms_per_step": round(t_e2e_fl * 1e3, 3),
+                                      "what": "the scene program run and flattened to PXIR on the host "
+                                              "(Python) every step, then the same C ABI calls"}},
         "roofline": {"bound": "fp32-alu", "achieved": round(achieved, 4), "peak": round(peak32, 2),
                      "unit": "TFLOP/s", "frac": round(achieved / peak32, 5), "traffic": EVAL_TRAFFIC_BYTES,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the classify, sub-block, "
-                                       "voxel, paint and apply kernels of one build "
-                                       "(profiles/build_kernels_penthouse_vpm80.md)",
+                                       "voxel, paint and apply kernels of one build of this workload "
+                                       "(one capture, --clock-control none)",
                      "kernel": "classify_kernel + sub_kernel + voxel_kernel + paint_kernel + fold_kernel "
                                "(every SDF and paint evaluation)",
                      "alg_ops_per_launch": int(alg_ops),
@@ -549,7 +627,7 @@ def main():
                      "peak_source": "measured here: dependent FFMA chains on all SMs (px_probe_peak)",
                      "fp64": ({"achieved": round(alg_ops / fold64_s / 1e12, 5), "peak": round(peak64, 3),
                                "frac": round(alg_ops / fold64_s / 1e12 / peak64, 5)} if have64 else None)},
-        "hbm": hbm_line(cfg, used, len(ir), t_mx),
+        "hbm": hbm_line(cfg, used, len(ir), t_mx, super_h.numel() * 4 + dens_h.numel() + free_len.value * 4),
         "host_flatten_ms": round(t_flat * 1e3, 2),
         "cpu_baseline": cpu,
         "clocks": clocks,

@@ -76,6 +76,9 @@ typedef struct px_device_view {
   const uint32_t* holes;     /* n_holes, push order */
   const uint32_t* super_counts; /* ceil(bx/4)*ceil(by/4)*ceil(bz/4), after px_derive */
   const uint8_t* density;    /* bx*by*bz, after px_derive */
+  const uint32_t* free_list; /* free_len entries: the GPU free list of the last build (derive on build), else NULL */
+  uint32_t free_len;
+  uint32_t pad;
 } px_device_view;
 
 /* new VoxelWorld(dx, dy, dz, initialPoolBricks) at a voxel density (VoxelWorld.ts:35-45;
@@ -112,6 +115,17 @@ int px_read_super(px_world* w, uint32_t* dst, size_t n);
 int px_read_density(px_world* w, uint8_t* dst, size_t n);
 int px_read_free_list(px_world* w, uint32_t max_bricks, uint32_t* dst, size_t n, uint32_t* out_len);
 
+/* Derive on build: with max_bricks > 0 every later build ends, on the device and
+   on its stream, with the super-grid counts, the density bytes and the GPU free
+   list for a device limit of max_bricks pool bricks (GpuWorld.ts:55-60,90-111:
+   the free list is the holes in push order, then cap - 1 down to poolUsed), so
+   a build leaves every upload buffer in HBM with no host step.  px_read_super /
+   px_read_density / px_read_free_list (with the same max_bricks) then copy them
+   out.  A world whose poolUsed exceeds the capacity gets no free list
+   (px_read_free_list returns PX_E_OOM, as GpuWorld.ts:59 throws).  0 turns it
+   off (the derived buffers are then computed when first read). */
+int px_set_derive_on_build(px_world* w, uint32_t max_bricks);
+
 /* The same super-grid counts and density bytes as px_derive, from a grid (bx*by*bz
    entries, bricks) and a pool (n_pool_bricks * 512 voxels) that the caller holds
    on the current device, written into caller-held device buffers super_counts
@@ -123,10 +137,13 @@ int px_read_free_list(px_world* w, uint32_t max_bricks, uint32_t* dst, size_t n,
    scratch area of 2 MiB + 256 bytes inside the library, which limits
    n_pool_bricks to PX_NOALLOC_MAX_POOL_BRICKS (larger: PX_E_TOO_LARGE, no GPU
    work).  The first call on each device looks up that area, with the device
-   current; make it before any stream capture on that device.  All calls share
-   the area, so calls that overlap in time race: serialise them.  Returns after
-   the work on `stream` has finished; PX_E_INVALID_ARG also when the grid names
-   a pool brick >= n_pool_bricks (that cell's density is written as 0). */
+   current; make it before any stream capture on that device, and do not call
+   it on a device reset (cudaDeviceReset) since that first call.  grid, pool
+   and super_counts must be 4-byte aligned (else PX_E_INVALID_ARG, no GPU
+   work).  All calls share the area, so calls that overlap in time race:
+   serialise them.  Returns after the work on `stream` has finished;
+   PX_E_INVALID_ARG also when the grid names a pool brick >= n_pool_bricks
+   (that cell's density is written as 0). */
 #define PX_NOALLOC_MAX_POOL_BRICKS 1048576u
 int px_derive_noalloc(const uint32_t* grid, const uint16_t* pool, int bx, int by, int bz, uint32_t n_pool_bricks,
                       const uint8_t* opaque256, const uint8_t* uniform_density256, uint32_t* super_counts,

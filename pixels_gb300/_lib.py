@@ -26,7 +26,7 @@ EXPORTS = [
     "px_read_density", "px_read_free_list", "px_set_material_tables", "px_set_validation", "px_get_stats",
     "px_device_view_get", "px_last_error", "px_probe_peak", "px_world_info", "px_serve_run", "px_derive_noalloc",
     "px_batch_create", "px_batch_run", "px_batch_destroy", "px_batch_last_error", "px_snap_anchors",
-    "px_reserve_pool",
+    "px_reserve_pool", "px_set_derive_on_build",
 ]
 
 
@@ -38,7 +38,8 @@ class PxError(RuntimeError):
 
 class DeviceView(ctypes.Structure):
     _fields_ = [("grid", ctypes.c_void_p), ("pool", ctypes.c_void_p), ("holes", ctypes.c_void_p),
-                ("super_counts", ctypes.c_void_p), ("density", ctypes.c_void_p)]
+                ("super_counts", ctypes.c_void_p), ("density", ctypes.c_void_p), ("free_list", ctypes.c_void_p),
+                ("free_len", ctypes.c_uint32), ("pad", ctypes.c_uint32)]
 
 
 class Edit(ctypes.Structure):
@@ -109,6 +110,7 @@ def load(path: str = LIB_PATH):
     L.px_snap_anchors.argtypes = [vp, vp, sz, vp, vp]
     L.px_reserve_pool.argtypes = [vp, ctypes.c_uint64]
     L.px_derive_noalloc.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, u32, vp, vp, vp, vp, vp]
+    L.px_set_derive_on_build.argtypes = [vp, u32]
     _L = L
     return L
 
@@ -128,6 +130,12 @@ def world_create(dx, dy, dz, vpm, initial_pool_bricks):
     ud = np.array(uniform_density_table(), np.uint8)
     _check(h, L.px_set_material_tables(h, op.ctypes.data, ud.ctypes.data))
     return h
+
+
+def set_derive_on_build(h, max_bricks: int):
+    """Every later build ends with super counts, density and the GPU free list
+    on the device (0: off)."""
+    _check(h, load().px_set_derive_on_build(h, int(max_bricks)))
 
 
 def set_validation(h, on: bool):

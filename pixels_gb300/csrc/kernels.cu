@@ -273,7 +273,8 @@ __device__ __forceinline__ int eval_decide(const FoldArgs& a, const OpDev* O, co
     return classify64(d64, what == 1 ? O->bhd : O->shd);
   }
   const double vs = a.vs;
-  double d = sdf64(code, clen, a.params, (double)tx * vs, (double)ty * vs, (double)tz * vs);
+  const double X = (double)tx * vs, Y = (double)ty * vs, Z = (double)tz * vs;
+  const double d = (O->flags & OPF_DEEP) ? sdf64_deep(code, clen, a.params, X, Y, Z) : sdf64(code, clen, a.params, X, Y, Z);
   if (what == 0) return d > 0.0 ? 0 : 1;
   return classify64(d, what == 1 ? O->bhd : O->shd);
 }
@@ -1696,9 +1697,17 @@ void launch_finalize(const FinalizeArgs& a, uint32_t touched_cap, cudaStream_t s
 // ---------------------------------------------------------------------------
 // derive: super-grid counts and density (GpuWorld.ts:90-101, VoxelWorld.ts:159-170)
 
-__global__ void __launch_bounds__(256) derive_kernel(const uint32_t* __restrict__ grid, const uint32_t* __restrict__ pool32,
-                                                     int BX, int BY, int BZ, const uint8_t* __restrict__ opaque,
-                                                     const uint8_t* __restrict__ udens, uint32_t* super_counts, uint8_t* density) {
+__global__ void __launch_bounds__(256) derive_kernel(DeriveArgs a) {
+  pdl_prologue();
+  // a build that committed nothing leaves the world (and its derived buffers) as they were
+  if (a.res && (a.res->status & (ST_STAGE_OVERFLOW | ST_POOL_OVERFLOW | ST_CHAIN))) return;
+  const uint32_t* __restrict__ grid = a.grid;
+  const uint32_t* __restrict__ pool32 = a.pool32;
+  const int BX = a.BX, BY = a.BY, BZ = a.BZ;
+  const uint8_t* __restrict__ opaque = a.opaque;
+  const uint8_t* __restrict__ udens = a.udens;
+  uint32_t* super_counts = a.super_counts;
+  uint8_t* density = a.density;
   __shared__ uint8_t op_s[256];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) op_s[i] = opaque[i];
   __syncthreads();
@@ -1749,6 +1758,19 @@ __global__ void __launch_bounds__(256) derive_kernel(const uint32_t* __restrict_
     for (int o = 16; o; o >>= 1) nz += __shfl_xor_sync(FULLMASK, nz, o);
     if (lane == 0) super_counts[sc] = nz;
   }
+  // the GPU free list (GpuWorld.ts:103-109): holes inside the used range in
+  // push order, then every index above it, from the top of the pool down
+  if (!a.free_list) return;
+  const uint32_t used = a.res ? a.res->pool_used : 0u, n_holes = a.res ? a.res->n_holes : 0u;
+  const uint64_t cap = free_list_bound(used, a.max_bricks);
+  const uint64_t len = used <= cap ? (uint64_t)n_holes + (cap - used) : 0ull;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (used > cap || len > a.free_cap) atomicOr(&a.res->status, (uint32_t)ST_FREE_CAP);
+    a.res->free_len = used > cap || len > a.free_cap ? 0u : (uint32_t)len;
+  }
+  if (used > cap || len > a.free_cap) return;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (uint64_t)gridDim.x * blockDim.x)
+    a.free_list[i] = i < n_holes ? __ldg(a.holes + i) : (uint32_t)(cap - 1 - (i - n_holes));
 }
 
 // A build's op-table uploads (read straight from the host arrays: pageable
@@ -1772,11 +1794,10 @@ void launch_uploads(const HostUploads& u, cudaStream_t s) {
   launch_pdl(upload_kernel, dim3(32, (unsigned)u.n), dim3(256), 0, s, u);
 }
 
-void launch_derive(const uint32_t* grid, const uint32_t* pool32, int BX, int BY, int BZ, const uint8_t* opaque,
-                   const uint8_t* udens, uint32_t* super_counts, uint8_t* density, cudaStream_t s) {
-  int n_super = ((BX + 3) / 4) * ((BY + 3) / 4) * ((BZ + 3) / 4);
-  size_t b = ((size_t)n_super * 32 + 255) / 256;
-  ++g_launches; derive_kernel<<<(int)(b < 65535 ? b : 65535), 256, 0, s>>>(grid, pool32, BX, BY, BZ, opaque, udens, super_counts, density);
+void launch_derive(const DeriveArgs& a, cudaStream_t s) {
+  const int n_super = ((a.BX + 3) / 4) * ((a.BY + 3) / 4) * ((a.BZ + 3) / 4);
+  const size_t b = ((size_t)n_super * 32 + 255) / 256;
+  launch_pdl(derive_kernel, dim3((unsigned)(b < 65535 ? b : 65535)), dim3(256), 0, s, a);
 }
 
 // ---------------------------------------------------------------------------

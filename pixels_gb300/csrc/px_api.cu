@@ -121,6 +121,13 @@ struct px_world {
   DevBuf work_counter;
   DevBuf res;
   DevBuf opaque, udens, super_counts, density;
+  // derive on build (px_set_derive_on_build): every build ends with the derived
+  // upload buffers and the GPU free list for a device limit of derive_max bricks
+  uint32_t derive_max = 0;
+  DevBuf free_list;
+  uint32_t free_len = 0;
+  bool free_valid = false;      // free_list holds the current world's GPU free list
+  bool free_over = false;       // ... or poolUsed exceeded the capacity (GpuWorld.ts:59)
   BuildResult* h_res = nullptr;   // pinned
   bool host_reads = false;        // the device reads pageable host memory (host page tables)
   bool uploads_pending = false;   // an upload kernel may still read the host op tables
@@ -307,9 +314,10 @@ bool convert32(const uint32_t* code, uint32_t n, const double* P, const double A
 }
 
 // Validate one op's SDF bytecode: opcodes, parameter ranges, finite values,
-// stack and rotation depths the device evaluator holds.
-bool check_code(const uint32_t* code, uint32_t n, const double* P, size_t np, std::string& why) {
-  int depth = 0, rot = 0;
+// stack and rotation depths.  `deep` is set when the program needs more than
+// the register evaluators hold (it then runs on the deep float64 evaluator).
+bool check_code(const uint32_t* code, uint32_t n, const double* P, size_t np, std::string& why, bool& deep) {
+  int depth = 0, rot = 0, max_depth = 0, max_rot = 0;
   for (uint32_t i = 0; i < n; i++) {
     uint32_t w0 = code[2 * i], off = code[2 * i + 1];
     uint32_t op = w0 & 0xffu, cnt = w0 >> 8;
@@ -334,7 +342,8 @@ bool check_code(const uint32_t* code, uint32_t n, const double* P, size_t np, st
         need = 4 + 2 * (size_t)cnt; break;
       case OP_ROT_X: case OP_ROT_Y: case OP_ROT_Z:
         need = 4;
-        if (++rot > MAX_ROT) { why = "rotations nested deeper than 3"; return false; }
+        if (++rot > DEEP_MAX_ROT) { why = "rotations nested deeper than 16"; return false; }
+        max_rot = std::max(max_rot, rot);
         break;
       case OP_ROT_END:
         if (--rot < 0) { why = "unmatched rotation end"; return false; }
@@ -351,10 +360,12 @@ bool check_code(const uint32_t* code, uint32_t n, const double* P, size_t np, st
         if (!std::isfinite(P[off + k])) { why = "non-finite parameter"; return false; }
     }
     if (op < OP_ROT_X) {
-      if (++depth > MAX_STACK) { why = "SDF stack deeper than 4"; return false; }
+      if (++depth > DEEP_MAX_STACK) { why = "SDF stack deeper than 32"; return false; }
+      max_depth = std::max(max_depth, depth);
     }
   }
   if (depth != 1 || rot != 0) { why = "bytecode does not leave exactly one distance"; return false; }
+  deep = max_depth > MAX_STACK || max_rot > MAX_ROT;
   return true;
 }
 
@@ -618,12 +629,14 @@ int convert_ops(const px_world* w, const IrOp* iops, size_t i0, size_t i1, const
     for (int k = 0; k < 4; k++)
       if (!std::isfinite(o.frame[k])) return chunk_fail(out, PX_E_INVALID_IR, "op %zu: non-finite paint frame", i);
     if (o.code_len == 0 || (size_t)o.code_begin + o.code_len > n_code) return chunk_fail(out, PX_E_INVALID_IR, "op %zu: code range", i);
-    if (!check_code(code + 2 * (size_t)o.code_begin, o.code_len, P, n_params, why))
+    bool deep = false;
+    if (!check_code(code + 2 * (size_t)o.code_begin, o.code_len, P, n_params, why, deep))
       return chunk_fail(out, PX_E_INVALID_IR, "op %zu: %s", i, why.c_str());
 
     OpDev d{};
     d.kind = o.kind;
     d.flags = o.flags & OPF_FROM_IR;
+    if (deep) d.flags |= OPF_DEEP | OPF_FP64_ONLY;  // beyond the register evaluators: float64, stack in local memory
     d.paint_kind = o.paint_kind;
     d.paint_value = o.paint_value;
     d.code_off = (uint32_t)out.code.size();  // + the chunk's code base (merge)
@@ -1105,6 +1118,30 @@ static int issue_uploads(px_world* w, const std::vector<Upload>& ups, cudaStream
 }
 
 
+// The derived upload buffers as the last kernel of a build (derive on build).
+static int enqueue_build_derive(px_world* w, cudaStream_t s, const uint32_t* holes_after) {
+  int rc;
+  const uint64_t fcap = free_list_bound(w->pool_cap, w->derive_max);
+  if ((rc = ensure(w, w->super_counts, 4 * w->ntiles)) || (rc = ensure(w, w->density, w->ncells)) ||
+      (rc = ensure(w, w->free_list, 4 * fcap + 4)))
+    return rc;
+  DeriveArgs da{};
+  da.grid = w->d_grid;
+  da.pool32 = w->d_pool32;
+  da.BX = w->BX; da.BY = w->BY; da.BZ = w->BZ;
+  da.opaque = (const uint8_t*)w->opaque.p;
+  da.udens = (const uint8_t*)w->udens.p;
+  da.super_counts = (uint32_t*)w->super_counts.p;
+  da.density = (uint8_t*)w->density.p;
+  da.holes = holes_after;
+  da.free_list = (uint32_t*)w->free_list.p;
+  da.free_cap = (uint32_t)fcap;
+  da.max_bricks = w->derive_max;
+  da.res = (BuildResult*)w->res.p;
+  launch_derive(da, s);
+  return PX_OK;
+}
+
 static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   set_programmatic_launch(!w->capturing);
   if (!w) return PX_E_INVALID_ARG;
@@ -1377,6 +1414,7 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   fn.pool_cap = w->pool_cap;
   fn.res = res;
   launch_finalize(fn, (uint32_t)touched_bound, s);
+  if (w->derive_max && (rc = enqueue_build_derive(w, s, (const uint32_t*)holes_out.p))) return rc;
   CU(cudaGetLastError());
   w->stats.kernel_launches = (uint32_t)(launch_count() - launches0);
   if (!w->capturing) CU(cudaEventRecord(w->ev1, s));
@@ -1459,6 +1497,10 @@ static int build_finish_impl(px_world* w) {
     w->fin.pool32 = w->d_pool32;
     w->fin.pool_cap = w->pool_cap;
     launch_finalize(w->fin, w->last_touched_cap, w->stream);
+    if (w->derive_max) {  // the holes the replay wrote are the other buffer of the pair
+      DevBuf& holes_after = w->holes_in_a ? w->holes_b : w->holes_a;
+      if ((rc = enqueue_build_derive(w, w->stream, (const uint32_t*)holes_after.p))) { w->retries = 0; return rc; }
+    }
     CU(cudaGetLastError());
     CU(cudaMemcpyAsync(w->h_res, dres, sizeof(BuildResult), cudaMemcpyDeviceToHost, w->stream));
     w->in_flight = true;
@@ -1491,7 +1533,10 @@ static int build_finish_impl(px_world* w) {
   w->boxes.clear();
   w->code.clear();
   w->params.clear();
-  w->derived_valid = false;
+  w->derived_valid = w->derive_max != 0;  // derive on build: super, density and free list are current
+  w->free_valid = w->derive_max != 0;
+  w->free_over = (r.status & ST_FREE_CAP) != 0;
+  w->free_len = r.free_len;
   w->stats.ops_applied = w->ops_applied;
   w->stats.pool_used = w->pool_used;
   w->stats.n_holes = w->n_holes;
@@ -1524,6 +1569,7 @@ static int world_reset_impl(px_world* w, int requeue_last_ops, void* stream) {
   w->pool_used = 0;
   w->n_holes = 0;
   w->derived_valid = false;
+  w->free_valid = false;
   if (requeue_last_ops) {
     if (!w->ops.empty()) return fail(w, PX_E_INVALID_ARG, "ops are already queued");
     w->ops = w->last_ops;
@@ -1561,8 +1607,15 @@ int px_derive(px_world* w) {
   int rc;
   size_t nsup = w->ntiles;
   if ((rc = ensure(w, w->super_counts, 4 * nsup)) || (rc = ensure(w, w->density, w->ncells))) return rc;
-  launch_derive(w->d_grid, w->d_pool32, w->BX, w->BY, w->BZ, (const uint8_t*)w->opaque.p, (const uint8_t*)w->udens.p,
-                (uint32_t*)w->super_counts.p, (uint8_t*)w->density.p, 0);
+  DeriveArgs da{};
+  da.grid = w->d_grid;
+  da.pool32 = w->d_pool32;
+  da.BX = w->BX; da.BY = w->BY; da.BZ = w->BZ;
+  da.opaque = (const uint8_t*)w->opaque.p;
+  da.udens = (const uint8_t*)w->udens.p;
+  da.super_counts = (uint32_t*)w->super_counts.p;
+  da.density = (uint8_t*)w->density.p;
+  launch_derive(da, 0);
   CU(cudaGetLastError());
   CU(cudaDeviceSynchronize());
   w->derived_valid = true;
@@ -1583,6 +1636,15 @@ int px_read_density(px_world* w, uint8_t* dst, size_t n) {
 // GpuWorld.ts:55-60, 103-109
 int px_read_free_list(px_world* w, uint32_t max_bricks, uint32_t* dst, size_t n, uint32_t* out_len) {
   if (!w) return PX_E_INVALID_ARG;
+  if (w->free_valid && max_bricks == w->derive_max) {  // built on the device by the last build
+    if (w->free_over)
+      return fail(w, PX_E_OOM, "the scene needs %u bricks but the pool holds fewer", (unsigned)w->pool_used);
+    if (out_len) *out_len = w->free_len;
+    if (!dst) return PX_OK;
+    if (n < w->free_len) return PX_E_INVALID_ARG;
+    if (w->free_len) CU(cudaMemcpy(dst, w->free_list.p, (size_t)w->free_len * 4, cudaMemcpyDeviceToHost));
+    return PX_OK;
+  }
   uint64_t used = w->pool_used;
   uint64_t cap = used + 98304 > used * 2 ? used + 98304 : used * 2;
   if (cap > max_bricks) cap = max_bricks;
@@ -1622,6 +1684,17 @@ int px_device_view_get(px_world* w, px_device_view* out) {
   out->holes = (const uint32_t*)cur.p;
   out->super_counts = w->derived_valid ? (const uint32_t*)w->super_counts.p : nullptr;
   out->density = w->derived_valid ? (const uint8_t*)w->density.p : nullptr;
+  out->free_list = w->free_valid && !w->free_over ? (const uint32_t*)w->free_list.p : nullptr;
+  out->free_len = w->free_valid && !w->free_over ? w->free_len : 0u;
+  out->pad = 0;
+  return PX_OK;
+}
+
+int px_set_derive_on_build(px_world* w, uint32_t max_bricks) {
+  if (!w) return PX_E_INVALID_ARG;
+  if (w->in_flight || w->batch_locked) return fail(w, PX_E_INVALID_ARG, "the world is busy");
+  w->derive_max = max_bricks;
+  w->free_valid = false;
   return PX_OK;
 }
 
@@ -1688,7 +1761,7 @@ void batch_free(px_batch* b) {
 // Host state of a world across the capture (capture runs nothing).
 struct WorldSaved {
   uint32_t pool_used, n_holes;
-  bool holes_in_a, derived_valid;
+  bool holes_in_a, derived_valid, free_valid;
   uint32_t ppb;
 };
 
@@ -1746,7 +1819,7 @@ static int batch_create_impl(px_world* const* worlds, size_t n, int mode, uint32
   std::vector<WorldSaved> saved(n);
   for (size_t i = 0; i < n; i++) {
     px_world* w = b->worlds[i];
-    saved[i] = {w->pool_used, w->n_holes, w->holes_in_a, w->derived_valid, w->pairs_per_block};
+    saved[i] = {w->pool_used, w->n_holes, w->holes_in_a, w->derived_valid, w->free_valid, w->pairs_per_block};
   }
   cudaStream_t origin = b->streams[0];
   int rc = PX_OK;
@@ -1778,6 +1851,7 @@ static int batch_create_impl(px_world* const* worlds, size_t n, int mode, uint32
     w->n_holes = saved[i].n_holes;
     w->holes_in_a = saved[i].holes_in_a;
     w->derived_valid = saved[i].derived_valid;
+    w->free_valid = saved[i].free_valid;
     w->pairs_per_block = saved[i].ppb;
     w->ops.clear(); w->boxes.clear(); w->code.clear(); w->params.clear();
     w->code32.clear(); w->p32.clear(); w->bases.clear();
@@ -1817,7 +1891,10 @@ int px_batch_run(px_batch* b, void* stream, float* device_ms) {
     w->pool_used = r.pool_used;
     w->n_holes = r.n_holes;
     w->holes_in_a = !w->batch_holes_in_a;  // the captured build wrote the other holes buffer
-    w->derived_valid = false;
+    w->derived_valid = w->derive_max != 0;
+    w->free_valid = w->derive_max != 0;
+    w->free_over = (r.status & ST_FREE_CAP) != 0;
+    w->free_len = r.free_len;
     w->ops_applied += w->last_ops.size();
     w->stats.ops_applied = w->ops_applied;
     w->stats.pool_used = w->pool_used;

@@ -9,8 +9,12 @@ constexpr uint32_t UNIFORM = 0x80000000u;  // VoxelWorld.ts:13
 constexpr int BRICK = 8;
 constexpr int BRICK_VOXELS = 512;
 constexpr int TILE = 4;                    // tiles are the 4^3-brick super cells (GpuWorld.ts:52)
-constexpr int MAX_STACK = 4;               // SDF value-stack depth the device evaluator holds
-constexpr int MAX_ROT = 3;                 // nested rotation frames
+constexpr int MAX_STACK = 4;               // SDF value-stack depth the register evaluators hold
+constexpr int MAX_ROT = 3;                 // nested rotation frames they hold
+// Deeper programs (nested CSG / rotation trees) run on the float64 evaluator
+// with a stack in local memory (sdf64_deep), up to these depths.
+constexpr int DEEP_MAX_STACK = 32;
+constexpr int DEEP_MAX_ROT = 16;
 constexpr int MAX_AXIS_BRICKS = 1023;      // op brick boxes pack 10 bits per axis
 
 // op kinds (shapes.ts:325-330)
@@ -33,8 +37,8 @@ enum : uint16_t {
 };
 constexpr int PAINT_NPARAMS[PK_COUNT] = {0, 5, 3, 4, 2, 2, 5, 37, 8};
 
-enum : uint8_t { OPF_CONTAINS = 1, OPF_HAS_SLACK = 2, OPF_PAINT_FRAME = 4, OPF_Y_SEPARABLE = 0x20, OPF_BOX_RANGES = 0x40,
-                 OPF_FP64_ONLY = 0x80 };
+enum : uint8_t { OPF_CONTAINS = 1, OPF_HAS_SLACK = 2, OPF_PAINT_FRAME = 4, OPF_DEEP = 0x10, OPF_Y_SEPARABLE = 0x20,
+                 OPF_BOX_RANGES = 0x40, OPF_FP64_ONLY = 0x80 };
 constexpr uint8_t OPF_FROM_IR = OPF_CONTAINS | OPF_HAS_SLACK | OPF_PAINT_FRAME;  // flags an op list may set
 
 // Mixed mode: margin between the exact value of an expression on the float64
@@ -48,6 +52,7 @@ enum { T_BSK_HI, T_BSK_LO, T_BFU_HI, T_BFU_LO, T_SSK_HI, T_SSK_LO, T_SFU_HI, T_S
 // device status bits (first error wins for the reported code)
 enum : uint32_t {
   ST_OK = 0, ST_STAGE_OVERFLOW = 1, ST_POOL_OVERFLOW = 2, ST_RANGE = 4, ST_CHAIN = 8,
+  ST_FREE_CAP = 16,  // derive: poolUsed exceeds the GPU pool capacity (GpuWorld.ts:59 throws)
 };
 
 // PXIR op record (128 bytes, pixels_gb300/ir.py OP_DTYPE)
@@ -124,6 +129,8 @@ struct BuildResult {
   uint32_t max_pool_index;
   BuildCounters c;
   unsigned long long max_err_bits;  // max |mid(d32) - d64| over rescued evaluations (double bits, >= 0)
+  uint32_t free_len;     // derive: length of the GPU free list (GpuWorld.ts:103-111, C_FREE_TOP)
+  uint32_t pad_;
 };
 
 // Pair classification (state independent): class per (op, brick) pair, the 8
@@ -276,9 +283,32 @@ struct HostUploads {
 };
 void launch_uploads(const HostUploads& u, cudaStream_t s);
 
-void launch_derive(const uint32_t* grid, const uint32_t* pool32, int BX, int BY, int BZ,
-                   const uint8_t* opaque, const uint8_t* udens, uint32_t* super_counts,
-                   uint8_t* density, cudaStream_t s);
+// Derived upload buffers of a world (GpuWorld.ts:52-109): super-grid counts,
+// density bytes and, when free_list is set, the GPU free list -- the holes in
+// push order, then cap - 1 down to poolUsed, cap = min(max_bricks,
+// max(used + 98304, 2 used)).  With res set the kernel is the last step of a
+// build: poolUsed and the hole count come from the build's result, and a
+// build that committed nothing derives nothing.
+struct DeriveArgs {
+  const uint32_t* grid;
+  const uint32_t* pool32;
+  int BX, BY, BZ;
+  const uint8_t* opaque;
+  const uint8_t* udens;
+  uint32_t* super_counts;
+  uint8_t* density;
+  const uint32_t* holes;  // the world's holes after the build
+  uint32_t* free_list;    // nullptr: no free list
+  uint32_t free_cap;      // entries free_list holds
+  uint32_t max_bricks;
+  BuildResult* res;
+};
+void launch_derive(const DeriveArgs& a, cudaStream_t s);
+// entries the GPU free list of a pool of `pool_cap` bricks can need
+__host__ __device__ inline uint64_t free_list_bound(uint64_t pool_cap, uint64_t max_bricks) {
+  const uint64_t c = pool_cap + 98304 > 2 * pool_cap ? pool_cap + 98304 : 2 * pool_cap;
+  return c < max_bricks ? c : max_bricks;
+}
 
 // Build kernels launched by this thread overlap their predecessors' tails
 // (programmatic dependent launch) unless switched off (graph captures).

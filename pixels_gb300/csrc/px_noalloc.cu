@@ -20,7 +20,15 @@
 // Set-up: the first call on each device, with that device current, looks up
 // the array's device address (cudaGetSymbolAddress) and keeps it for later
 // calls on that device.  Make the first call on a device before any stream
-// capture is begun on it.
+// capture is begun on it.  The kept address belongs to the device's current
+// context: after cudaDeviceReset (which unloads the library's device code) the
+// array may live elsewhere, so this entry point is not to be called on a
+// device that has been reset since its first call.
+//
+// Alignment: the pool is read as 32-bit voxel pairs and the grid and super
+// counts as 32-bit words, so those three addresses must be multiples of 4
+// bytes (a uint16 pool that starts at an odd element is refused with
+// PX_E_INVALID_ARG before any GPU work).
 //
 // Every call shares the one array: calls that overlap in time (from several
 // host threads, or on several streams) race on it and may return wrong
@@ -166,6 +174,7 @@ extern "C" int px_derive_noalloc(const uint32_t* grid, const uint16_t* pool, int
       bx <= 0 || by <= 0 || bz <= 0)
     return PX_E_INVALID_ARG;
   if (n_pool_bricks > MAX_POOL_BRICKS) return PX_E_TOO_LARGE;
+  if (((uintptr_t)grid & 3u) || ((uintptr_t)pool & 3u) || ((uintptr_t)super_counts & 3u)) return PX_E_INVALID_ARG;
   void* scratch = nullptr;
   int rc = scratch_for_current_device(&scratch);
   if (rc != PX_OK) return rc;

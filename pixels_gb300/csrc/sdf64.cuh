@@ -152,4 +152,54 @@ __device__ __noinline__ double sdf64(const uint2* __restrict__ code, int n, cons
   return s0;
 }
 
+// sdf64 for programs deeper than its registers hold (nested CSG and rotation
+// trees): the value stack and the saved points live in local memory.  Same
+// operations in the same order as sdf64.
+__device__ __noinline__ double sdf64_deep(const uint2* __restrict__ code, int n, const double* __restrict__ P,
+                                          double x, double y, double z) {
+  double st[DEEP_MAX_STACK];
+  double saved[DEEP_MAX_ROT][3];
+  int sp = 0, rp = 0;  // the validator bounds both depths
+  for (int i = 0; i < n; i++) {
+    uint2 ins = __ldg(code + i);
+    uint32_t op = ins.x & 0xffu;
+    int cnt = (int)(ins.x >> 8);
+    const double* p = P + ins.y;
+    if (op < OP_ROT_X) {
+      st[sp++] = prim64(op, cnt, p, x, y, z);
+      continue;
+    }
+    switch (op) {
+      case OP_ROT_X: case OP_ROT_Y: case OP_ROT_Z: {
+        saved[rp][0] = x; saved[rp][1] = y; saved[rp][2] = z;
+        rp++;
+        double p0 = __ldg(p), p1 = __ldg(p + 1), c = __ldg(p + 2), sn = __ldg(p + 3);
+        if (op == OP_ROT_Y) {  // shapes.ts:273-274
+          double dx = x - p0, dz = z - p1;
+          x = p0 + c * dx + sn * dz;
+          z = p1 - sn * dx + c * dz;
+        } else if (op == OP_ROT_X) {  // shapes.ts:293-294
+          double dy = y - p0, dz = z - p1;
+          y = p0 + c * dy + sn * dz;
+          z = p1 - sn * dy + c * dz;
+        } else {  // shapes.ts:313-314
+          double dx = x - p0, dy = y - p1;
+          x = p0 + c * dx + sn * dy;
+          y = p1 - sn * dx + c * dy;
+        }
+        break;
+      }
+      case OP_ROT_END:
+        rp--;
+        x = saved[rp][0]; y = saved[rp][1]; z = saved[rp][2];
+        break;
+      case OP_OFFSET: st[sp - 1] = st[sp - 1] + __ldg(p); break;                          // penthouse.ts:250
+      case OP_NEGMAX: sp--; st[sp - 1] = fmax(st[sp - 1], -st[sp]); break;                // shapes.ts:244
+      case OP_MAX: sp--; st[sp - 1] = fmax(st[sp - 1], st[sp]); break;                    // shapes.ts:255
+      case OP_MIN: sp--; st[sp - 1] = fmin(st[sp - 1], st[sp]); break;                    // shapes.ts:231
+    }
+  }
+  return st[0];
+}
+
 }  // namespace px

@@ -43,7 +43,8 @@ class VoxelWorld:
     """A world handle owned by the CUDA library (one GPU)."""
 
     def __init__(self, dx: int, dy: int, dz: int, initialPoolBricks: int = 1 << 14,
-                 vpm: float | None = None, mode: int = MODE_MIXED, max_bricks: int = 1 << 31):
+                 vpm: float | None = None, mode: int = MODE_MIXED, max_bricks: int = 1 << 31,
+                 derive_on_build: bool = False):
         from . import _lib
         if vpm is None:
             vpm = _config.current().vpm
@@ -54,6 +55,8 @@ class VoxelWorld:
         self.max_bricks = int(max_bricks)
         self._lib = _lib
         self._h = _lib.world_create(self.dx, self.dy, self.dz, self.vpm, int(initialPoolBricks))
+        if derive_on_build:  # every build also leaves the upload buffers of GpuWorld.ts:90-111 on the device
+            _lib.set_derive_on_build(self._h, self.max_bricks)
         self._pending = Program()
 
     # -- op submission (shapes.apply) ---------------------------------------

@@ -3,8 +3,10 @@
 Empty op lists, ops wholly outside the world, degenerate shapes (zero-size
 boxes, capsules with equal ends, lathe profiles with repeated points,
 collinear prisms), paints on air and paints that return air, carve/re-add
-sequences that reuse freed pool bricks in LIFO order, and a world wider than
-the float32 path certifies (every op then runs in float64).
+sequences that reuse freed pool bricks in LIFO order, a world wider than
+the float32 path certifies (every op then runs in float64), unions, and CSG /
+rotation trees deeper than the register evaluators hold (shapes.ts:227-320
+put no limit on nesting).
 """
 import numpy as np
 import pytest
@@ -13,8 +15,8 @@ from pixels_gb300 import config
 from pixels_gb300.ir import Program
 from pixels_gb300.materials import M, vox
 from pixels_gb300.paints import black_keys, tufted
-from pixels_gb300.shapes import (box, boxMinMax, capsule, cylinder, lathe, prism, rotateY, roundBox, sphere,
-                                 subtract, torus)
+from pixels_gb300.shapes import (box, boxMinMax, capsule, cylinder, ellipsoid, intersect, lathe, prism, rotateX,
+                                 rotateY, rotateZ, roundBox, sphere, subtract, torus, union)
 from pixels_gb300.world import MODE_FP64, MODE_MIXED, VoxelWorld
 
 import pyoracle
@@ -112,3 +114,44 @@ def test_world_wider_than_the_float32_range(built_lib):
     o, stats = run_both(program(vpm, ops), vpm, (8, 8, 1104))
     assert o.pool_used > 0
     assert stats[1]["rescued"] == 0  # nothing to rescue: no float32 evaluation at all
+
+
+@pytest.mark.gpu
+def test_union_and_deep_csg_and_rotation_trees(built_lib):
+    """union (shapes.ts:227-238) of six overlapping shapes; a subtract chain six
+    deep, subtract(a, subtract(b, subtract(c, ...))); rotations nested five deep
+    (rotateY(rotateX(rotateZ(rotateY(rotateX(...)))))); and a union of
+    intersections of rotated subtracts.  Programs deeper than four stack values
+    or three rotation frames run on the deep float64 evaluator in both forms."""
+    vpm = 40.0
+
+    def chain(depth, c):
+        s = sphere(c, 0.05 + 0.03 * depth)
+        for k in range(depth):
+            r = 0.08 + 0.03 * (depth - k)
+            outer = box(c, (r, r * 0.8, r * 0.9)) if k % 2 else sphere(c, r)
+            s = subtract(outer, s)
+        return s
+
+    def nested_rot(shape, c, depth):
+        for k in range(depth):
+            rot = (rotateY, rotateX, rotateZ)[k % 3]
+            shape = rot(shape, 0.3 + 0.41 * k, c)
+        return shape
+
+    def ops():
+        u = union(sphere((0.3, 0.3, 0.3), 0.12), box((0.4, 0.3, 0.3), (0.1, 0.05, 0.08)),
+                  capsule((0.2, 0.2, 0.4), (0.5, 0.4, 0.4), 0.04), torus((0.35, 0.35, 0.25), 0.1, 0.03, "z"),
+                  cylinder((0.3, 0.45, 0.3), 0.05, 0.1, "y"), ellipsoid((0.45, 0.3, 0.45), (0.08, 0.05, 0.12)))
+        yield 0, u, vox(M.marble)
+        yield 0, chain(6, (0.9, 0.4, 0.4)), vox(M.gold)                        # stack depth 7
+        c = (0.6, 0.45, 0.9)
+        yield 0, nested_rot(roundBox(c, (0.15, 0.05, 0.1), 0.02), c, 5), vox(M.oak)   # 5 rotation frames
+        d = (1.0, 0.3, 1.0)
+        deep = union(*[intersect(nested_rot(subtract(box(d, (0.2, 0.2, 0.2)), sphere(d, 0.1 + 0.02 * k)), d, 4),
+                                 sphere(d, 0.22 + 0.01 * k)) for k in range(3)])
+        yield 0, deep, vox(M.velvet)
+        yield 1, union(sphere((0.3, 0.3, 0.3), 0.06), chain(5, (0.35, 0.32, 0.3))), 0   # carve with a deep union
+        yield 2, nested_rot(chain(4, (0.9, 0.4, 0.4)), (0.9, 0.4, 0.4), 4), tufted(0.05, 0.05, M.leather)
+    o, stats = run_both(program(vpm, ops), vpm, (64, 32, 64))
+    assert o.pool_used > 0

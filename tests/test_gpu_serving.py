@@ -61,6 +61,32 @@ def _concat_ir(a, b):
 
 
 @pytest.mark.gpu
+def test_resident_synthetic_vpm160_after_served_stream_matches_oracle(built_lib):
+    """The serving benchmark's world: the seeded 4,096-primitive synthetic map at
+    160 voxels per metre (2560 x 704 x 1920 = 3.46 G cells), then a Poisson
+    stream of 2,000 sphere/capsule subtract-edits served in batches of up to 512.
+    The result must equal the oracle's build of the scene followed by the
+    carves in the order they were applied (shapes.ts:423-426)."""
+    import os
+    from pixels_gb300.scenes.synthetic import synthetic_program
+    vpm = 160.0
+    cfg = config.Config(vpm)
+    prog = synthetic_program(1, 4096, vpm)
+    w = VoxelWorld(*cfg.dims, initialPoolBricks=1 << 20, vpm=vpm, mode=MODE_MIXED)
+    w._pending = prog
+    w.build()
+    edits, arrivals = serving.edit_stream(w.grid, cfg.bricks, vpm, 2000, rate=100000.0, seed=100000)
+    res, order = serving.serve(w, edits, arrivals, max_batch=512)
+    assert (res["status"] == 0).all() and len(order) == len(edits)
+    assert len(np.unique(res["batch"])) > 1
+    carves = serving.carve_program(edits, order, vpm)
+    o = pyoracle.OracleWorld(_concat_ir(synthetic_program(1, 4096, vpm), carves), vpm, cfg.dims,
+                             threads=os.cpu_count() or 1)
+    assert_same_world(w, o)
+    w.close()
+
+
+@pytest.mark.gpu
 def test_poisson_stream_latency(built_lib):
     vpm = 40.0
     prog, _ = penthouse_program(vpm)
