@@ -231,6 +231,13 @@ const char* px_batch_last_error(px_batch* b);
    float32 (fp64 = 0) — the denominators of the voxeliser's ALU roofline. */
 int px_probe_peak(int fp64, float* tflops);
 
+/* Self-check of the mixed form's float32 square-root bounds (no counterpart in
+   the reference): for every float whose bit pattern lies in [lo_bits, hi_bits]
+   (positive, finite), the lower and upper bounds the interval evaluator uses
+   must enclose the IEEE directed square roots of this GPU; n_bad receives the
+   failures (must be 0) and first_bad the smallest failing bit pattern. */
+int px_check_sqrt_bounds(uint32_t lo_bits, uint32_t hi_bits, uint64_t* n_bad, uint32_t* first_bad);
+
 #ifdef __cplusplus
 }
 #endif

@@ -26,7 +26,7 @@ EXPORTS = [
     "px_read_density", "px_read_free_list", "px_set_material_tables", "px_set_validation", "px_get_stats",
     "px_device_view_get", "px_last_error", "px_probe_peak", "px_world_info", "px_serve_run", "px_derive_noalloc",
     "px_batch_create", "px_batch_run", "px_batch_destroy", "px_batch_last_error", "px_snap_anchors",
-    "px_reserve_pool", "px_set_derive_on_build",
+    "px_reserve_pool", "px_set_derive_on_build", "px_check_sqrt_bounds",
 ]
 
 
@@ -111,6 +111,7 @@ def load(path: str = LIB_PATH):
     L.px_reserve_pool.argtypes = [vp, ctypes.c_uint64]
     L.px_derive_noalloc.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, u32, vp, vp, vp, vp, vp]
     L.px_set_derive_on_build.argtypes = [vp, u32]
+    L.px_check_sqrt_bounds.argtypes = [u32, u32, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(u32)]
     _L = L
     return L
 
@@ -211,6 +212,15 @@ def probe_peak(fp64: bool) -> float:
     v = ctypes.c_float()
     _check(None, load().px_probe_peak(int(fp64), ctypes.byref(v)))
     return float(v.value)
+
+
+def check_sqrt_bounds(lo_bits: int, hi_bits: int):
+    """(failures, smallest failing bit pattern) of the float32 evaluator's
+    square-root bounds against the IEEE directed square roots."""
+    n = ctypes.c_uint64()
+    first = ctypes.c_uint32()
+    _check(None, load().px_check_sqrt_bounds(int(lo_bits), int(hi_bits), ctypes.byref(n), ctypes.byref(first)))
+    return int(n.value), int(first.value)
 
 
 def serve_run(h, edits, arrivals, max_batch: int, pool_budget: int, mode: int, stream: int = 0):

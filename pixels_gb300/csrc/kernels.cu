@@ -44,6 +44,9 @@ namespace px {
 #ifndef PX_FOLD_MINB
 #define PX_FOLD_MINB 3
 #endif
+#ifndef PX_VSIMPLE_MINB
+#define PX_VSIMPLE_MINB 4
+#endif
 
 // kernel launches issued by the host wrappers (reported per build)
 static unsigned long long g_launches = 0;
@@ -542,7 +545,7 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_SUB_MINB : PX_CLASSIFY64_M
     const bool push = have && scls == PC_PARTIAL && !boxr && !lipd;
     const uint32_t vm = __ballot_sync(FULLMASK, push);
     if (push) {  // one append per shape class present among the pushing lanes
-      const uint32_t k = a.ops[oo].vclass & (VCLASSES - 1);
+      const uint32_t k = a.ops[oo].vq_class & (VQ_CLASSES - 1);
       const uint32_t grp = __match_any_sync(vm, k);
       const int leader = __ffs(grp) - 1;
       uint32_t vb = 0;
@@ -571,15 +574,19 @@ __device__ __forceinline__ int lip_decide(const OpDev* O, Iv dc, int ox, int oy,
 }
 
 // Voxel inside-masks of the queued partial sub-blocks: one sub-block per warp
-// pass, 64 voxel SDFs on 32 lanes, two ballots (shapes.ts:390-394).
-template <int MODE>
+// pass, 64 voxel SDFs on 32 lanes, two ballots (shapes.ts:390-394), any
+// program (the bytecode interpreters).  HALF: the voxel classes it drains,
+// [32 HALF, 32 HALF + 32) in vclass_order (the mixed form sends the first half,
+// the single-primitive programs, to voxel_simple_kernel).
+template <int MODE, int HALF>
 __global__ void __launch_bounds__(256, MODE == 1 ? PX_VOXEL_MINB : PX_CLASSIFY64_MINB) voxel_kernel(FoldArgs a) {
   pdl_prologue();
   const int lane = threadIdx.x & 31;
   LaneStats ls = {a.res};
+  uint32_t* const taken = HALF ? &a.vitem_counter[0] : &a.vitem_counter[VQ_SIMPLE_TAKEN];
   // the classes' item counts in the order they are taken, as an inclusive prefix over lanes
-  const int my_cls = lane < VCLASSES ? a.class_order[lane] : 0;
-  uint32_t incl = lane < VCLASSES ? min(__ldg(&a.vitem_counter[1 + my_cls]), a.vq_cap[my_cls]) : 0u;
+  const int my_cls = a.vclass_order[32 * HALF + lane];
+  uint32_t incl = min(__ldg(&a.vitem_counter[1 + my_cls]), a.vq_cap[my_cls]);
   const uint32_t own = incl;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -588,14 +595,14 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_VOXEL_MINB : PX_CLASSIFY64
   }
   const uint32_t n_items = __shfl_sync(FULLMASK, incl, 31);
   NextTicket tk;
-  tk.issue(&a.vitem_counter[0], 1, lane);
+  tk.issue(taken, 1, lane);
   for (;;) {
     const uint32_t it = tk.get();
     if (it >= n_items) break;
-    tk.issue(&a.vitem_counter[0], 1, lane);
-    const int k = __popc(__ballot_sync(FULLMASK, lane < VCLASSES && incl <= it));  // class of item `it`
+    tk.issue(taken, 1, lane);
+    const int k = __popc(__ballot_sync(FULLMASK, incl <= it));  // class of item `it`
     const uint32_t first = __shfl_sync(FULLMASK, incl - own, k);
-    const uint4 item = __ldg(a.vitems + a.vq_base[a.class_order[k]] + (it - first));
+    const uint4 item = __ldg(a.vitems + a.vq_base[a.vclass_order[32 * HALF + k]] + (it - first));
     const Iv dcen = {__uint_as_float(item.z), __uint_as_float(item.w)};  // the sub-block centre's value
     const OpDev* V = a.ops + item.x;
     const unsigned long long vp = item.y >> 3;
@@ -663,6 +670,135 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_VOXEL_MINB : PX_CLASSIFY64
       }
       m = (unsigned long long)bal[0] | ((unsigned long long)bal[1] << 32);
     }
+    // a lone box's sub-block is queued only in validation mode: check its runs
+    if ((V->flags & OPF_BOX_RANGES) && lane == 0 && box_mask(V, vbx * 8 + sxo, vby * 8 + syo, vbz * 8 + szo) != m)
+      ls.viol();
+    if (lane == 0) a.pmask[vp * 8 + ss] = m;
+  }
+}
+
+// The point through a rotation of the shape's frame (shapes.ts:263-320 on
+// intervals): p holds the pivot's two coordinates, cos and sin.
+__device__ __forceinline__ void rot32(uint32_t op, const Iv* __restrict__ p, Iv& x, Iv& y, Iv& z) {
+  const Iv p0 = ldp(p, 0), p1 = ldp(p, 1), c = ldp(p, 2), sn = ldp(p, 3);
+  if (op == OP_ROT_Y) {
+    const Iv dx = isub(x, p0), dz = isub(z, p1);
+    x = iadd(iadd(p0, icmul(dx, c)), icmul(dz, sn));
+    z = iadd(isub(p1, icmul(dx, sn)), icmul(dz, c));
+  } else if (op == OP_ROT_X) {
+    const Iv dy = isub(y, p0), dz = isub(z, p1);
+    y = iadd(iadd(p0, icmul(dy, c)), icmul(dz, sn));
+    z = iadd(isub(p1, icmul(dy, sn)), icmul(dz, c));
+  } else {
+    const Iv dx = isub(x, p0), dy = isub(y, p1);
+    x = iadd(iadd(p0, icmul(dx, c)), icmul(dy, sn));
+    y = iadd(isub(p1, icmul(dx, sn)), icmul(dy, c));
+  }
+}
+
+// Voxel inside-masks of the queued partial sub-blocks of single-primitive
+// programs -- [rotation] primitive [rotation end] [offset], 88% of the
+// penthouse's non-box voxel work -- in the mixed form: the same decisions as
+// voxel_kernel (shapes.ts:390-394), without the interpreters' value stack and
+// rotation frames.  Lane = voxel column (x, z) of the sub-block and a pair of
+// y rows; a primitive extruded along y (unrotated, or rotated about y) shares
+// its x/z work between the two voxels.
+__global__ void __launch_bounds__(256, PX_VSIMPLE_MINB) voxel_simple_kernel(FoldArgs a) {
+  pdl_prologue();
+  const int lane = threadIdx.x & 31;
+  LaneStats ls = {a.res};
+  uint32_t* const taken = &a.vitem_counter[VQ_SIMPLE_TAKEN];
+  const int my_cls = a.vclass_order[lane];
+  uint32_t incl = min(__ldg(&a.vitem_counter[1 + my_cls]), a.vq_cap[my_cls]);
+  const uint32_t own = incl;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(FULLMASK, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const uint32_t n_items = __shfl_sync(FULLMASK, incl, 31);
+  const int col = lane & 15, yh = lane >> 4;
+  const Iv* __restrict__ P = reinterpret_cast<const Iv*>(a.p32);
+  NextTicket tk;
+  tk.issue(taken, 1, lane);
+  for (;;) {
+    const uint32_t it = tk.get();
+    if (it >= n_items) break;
+    tk.issue(taken, 1, lane);
+    const int k = __popc(__ballot_sync(FULLMASK, incl <= it));  // class of item `it`
+    const uint32_t first = __shfl_sync(FULLMASK, incl - own, k);
+    const uint4 item = __ldg(a.vitems + a.vq_base[a.vclass_order[k]] + (it - first));
+    const Iv dcen = {__uint_as_float(item.z), __uint_as_float(item.w)};  // the sub-block centre's value
+    const OpDev* V = a.ops + item.x;
+    const unsigned long long vp = item.y >> 3;
+    const int ss = item.y & 7;
+    int vbx, vby, vbz;
+    brick_of_pair(V, vp, vbx, vby, vbz);
+    Iv bo[3];
+    brick_bases(a, V, vbx, vby, vbz, bo);
+    const int sxo = (ss & 1) * 4, syo = ((ss >> 1) & 1) * 4, szo = ((ss >> 2) & 1) * 4;
+    const int lx = sxo + (col & 3), lz = szo + (col >> 2), ly0 = syo + 2 * yh;
+    const int lip0 = lip_decide(V, dcen, col & 3, 2 * yh, col >> 2), lip1 = lip_decide(V, dcen, col & 3, 2 * yh + 1, col >> 2);
+    const uint32_t sp = V->simple;
+    const uint32_t prim = sp & 0xffu, rot = (sp >> 8) & 0xffu;
+    const float M = V->thr[T_M];
+    bool amb = false;
+    Iv2 d = {{0.f, 0.f}, {0.f, 0.f}};
+    if (lip0 == 3 || lip1 == 3 || a.validate) {
+      const uint32_t* c32 = a.code32 + V->code_off;
+      const uint32_t ip = rot ? 1u : 0u;  // the primitive's instruction
+      const Iv* pr = P + __ldg(c32 + ip);
+      const int cnt = (int)(__ldg(&a.code[V->code_off + ip].x) >> 8);
+      Iv x = iadd(bo[0], koff((float)lx, a.vs_lo, a.vs_hi)), z = iadd(bo[2], koff((float)lz, a.vs_lo, a.vs_hi));
+      const Iv y0 = iadd(bo[1], koff((float)ly0, a.vs_lo, a.vs_hi)), y1 = iadd(bo[1], koff((float)(ly0 + 1), a.vs_lo, a.vs_hi));
+      if ((rot == 0 || rot == OP_ROT_Y) && op_is_y_separable(prim)) {
+        if (rot) {  // x and z only: shared by both voxels
+          Iv yd = y0;
+          rot32(rot, P + __ldg(c32), x, yd, z);
+        }
+        d = prim32_y2(prim, cnt, pr, x, y0, y1, z, M, amb);
+      } else {
+#pragma unroll 1
+        for (int q = 0; q < 2; q++) {
+          Iv xx = x, yy = q ? y1 : y0, zz = z;
+          if (rot) rot32(rot, P + __ldg(c32), xx, yy, zz);
+          const Iv v = prim32(prim, cnt, pr, xx, yy, zz, M, amb);
+          if (q) d.b = v; else d.a = v;
+        }
+      }
+      if (sp >> 16) {  // offset (penthouse.ts:250)
+        const Iv o = ldp(P + __ldg(c32 + (rot ? 3u : 1u)), 0);
+        d = {iadd(d.a, o), iadd(d.b, o)};
+      }
+    }
+    const uint2* code = a.code + V->code_off;
+    const int clen = (int)V->code_len;
+    uint32_t lo = 0, hi = 0;
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      const Iv dk = q ? d.b : d.a;
+      const int lipk = q ? lip1 : lip0;
+      int inside = lipk;
+      if (lipk == 3 || a.validate) {
+        inside = amb ? 3 : (dk.lo > V->thr[T_V_HI] ? 0 : (dk.hi <= V->thr[T_V_LO] ? 1 : 3));
+        if (inside == 3 || a.validate) {
+          const VoxelF64 f = voxel_f64(a.params, a.vs, a.validate, code, clen, dk, amb, inside,
+                                       (float)(vbx * 8 + lx) + 0.5f, (float)(vby * 8 + ly0 + q) + 0.5f,
+                                       (float)(vbz * 8 + lz) + 0.5f);
+          if (f.viol) ls.viol();
+          if (inside == 3) ls.rescue(0, amb, f.err);
+          inside = f.inside;
+        }
+        if (lipk != 3 && inside != lipk) ls.viol();  // validation: the bound disagreed with the evaluation
+      }
+      const int bit = (col & 3) | ((2 * yh + q) << 2) | ((col >> 2) << 4);  // voxel index in the sub-block
+      if (inside == 1) {
+        if (bit < 32) lo |= 1u << bit;
+        else hi |= 1u << (bit - 32);
+      }
+    }
+    const unsigned long long m =
+        (unsigned long long)__reduce_or_sync(FULLMASK, lo) | ((unsigned long long)__reduce_or_sync(FULLMASK, hi) << 32);
     // a lone box's sub-block is queued only in validation mode: check its runs
     if ((V->flags & OPF_BOX_RANGES) && lane == 0 && box_mask(V, vbx * 8 + sxo, vby * 8 + syo, vbz * 8 + szo) != m)
       ls.viol();
@@ -1153,11 +1289,13 @@ void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEve
   if (mode == 1) {
     launch_pdl(classify_kernel<1>, dim3(grid(PX_CLASSIFY_MINB)), dim3(256), 0, s, a);
     launch_pdl(sub_kernel<1>, dim3(grid(PX_SUB_MINB)), dim3(256), 0, s, a);
-    launch_pdl(voxel_kernel<1>, dim3(grid(PX_VOXEL_MINB)), dim3(256), 0, s, a);
+    launch_pdl(voxel_simple_kernel, dim3(grid(PX_VSIMPLE_MINB)), dim3(256), 0, s, a);
+    launch_pdl(voxel_kernel<1, 1>, dim3(grid(PX_VOXEL_MINB)), dim3(256), 0, s, a);
   } else {
     launch_pdl(classify_kernel<0>, dim3(grid(PX_CLASSIFY64_MINB)), dim3(256), 0, s, a);
     launch_pdl(sub_kernel<0>, dim3(grid(PX_CLASSIFY64_MINB)), dim3(256), 0, s, a);
-    launch_pdl(voxel_kernel<0>, dim3(grid(PX_CLASSIFY64_MINB)), dim3(256), 0, s, a);
+    launch_pdl(voxel_kernel<0, 0>, dim3(grid(PX_CLASSIFY64_MINB)), dim3(256), 0, s, a);
+    launch_pdl(voxel_kernel<0, 1>, dim3(grid(PX_CLASSIFY64_MINB)), dim3(256), 0, s, a);
   }
   if (a.n_paint_slots) {
     if (mode == 1) launch_pdl(paint_kernel<1>, dim3(grid(4)), dim3(256), 0, s, a);
@@ -1618,7 +1756,10 @@ void launch_replay(const ReplayArgs& a, cudaStream_t s) {
 // finalize: staging -> pool at the replayed indices, grid entries
 
 __global__ void __launch_bounds__(256) finalize_kernel(FinalizeArgs a) {
+  __shared__ uint8_t op_s[256];
+  op_s[threadIdx.x] = a.opaque[threadIdx.x];  // 256 threads
   pdl_prologue();
+  __syncthreads();
   // commit only a complete build: every staging slot written, every pool index within the pool
   if (a.res->status & (ST_STAGE_OVERFLOW | ST_CHAIN)) return;
   if (a.res->pool_used > a.pool_cap) {
@@ -1675,6 +1816,25 @@ __global__ void __launch_bounds__(256) finalize_kernel(FinalizeArgs a) {
         v[q][0] = s4[lane];
         v[q][1] = s4[lane + 32];
       }
+      // each brick's opaque, non-air voxels (16 per lane), two bricks per 32-bit word
+      uint32_t cnt2[2] = {0u, 0u};
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        if (src_l[q] < 0) continue;
+        const uint32_t w8[8] = {v[q][0].x, v[q][0].y, v[q][0].z, v[q][0].w, v[q][1].x, v[q][1].y, v[q][1].z, v[q][1].w};
+        uint32_t c = 0;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+          const uint32_t lo = w8[k] & 0xffffu, hi = w8[k] >> 16;
+          c += (lo != 0 && op_s[lo & 0xffu]) + (hi != 0 && op_s[hi & 0xffu]);
+        }
+        cnt2[q >> 1] += c << (16 * (q & 1));
+      }
+#pragma unroll
+      for (int o = 16; o; o >>= 1) {
+        cnt2[0] += __shfl_xor_sync(FULLMASK, cnt2[0], o);
+        cnt2[1] += __shfl_xor_sync(FULLMASK, cnt2[1], o);
+      }
 #pragma unroll
       for (int q = 0; q < 4; q++) {
         if (src_l[q] < 0) continue;
@@ -1682,6 +1842,7 @@ __global__ void __launch_bounds__(256) finalize_kernel(FinalizeArgs a) {
         uint4* d4 = reinterpret_cast<uint4*>(a.pool32 + (size_t)di * 256);
         d4[lane] = v[q][0];
         d4[lane + 32] = v[q][1];
+        if (lane == 0) a.pcount[di] = (uint16_t)((cnt2[q >> 1] >> (16 * (q & 1))) & 0xffffu);
       }
     }
   }
@@ -1730,6 +1891,7 @@ __global__ void __launch_bounds__(256) derive_kernel(DeriveArgs a) {
         nz += g != 0;
         if (g == 0) density[ci] = 0;
         else if (g & UNIFORM) density[ci] = udens[g & 0xffu];
+        else if (a.pcount) density[ci] = (uint8_t)px_round(((double)__ldg(a.pcount + (g - 1)) / 512.0) * 255.0);
         else { is_mixed[h] = true; mixed_g[h] = g; mixed_ci[h] = ci; }
       }
     }
@@ -1751,7 +1913,10 @@ __global__ void __launch_bounds__(256) derive_kernel(DeriveArgs a) {
         }
 #pragma unroll
         for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(FULLMASK, cnt, o);
-        if (lane == 0) density[ci] = (uint8_t)px_round(((double)cnt / 512.0) * 255.0);
+        if (lane == 0) {
+          density[ci] = (uint8_t)px_round(((double)cnt / 512.0) * 255.0);
+          if (a.pcount_out) a.pcount_out[g - 1] = (uint16_t)cnt;
+        }
       }
     }
 #pragma unroll
@@ -1798,6 +1963,43 @@ void launch_derive(const DeriveArgs& a, cudaStream_t s) {
   const int n_super = ((a.BX + 3) / 4) * ((a.BY + 3) / 4) * ((a.BZ + 3) / 4);
   const size_t b = ((size_t)n_super * 32 + 255) / 256;
   launch_pdl(derive_kernel, dim3((unsigned)(b < 65535 ? b : 65535)), dim3(256), 0, s, a);
+}
+
+// ---------------------------------------------------------------------------
+// check of the square-root bounds of the float32 interval evaluator: every
+// float v in [lo_bits, hi_bits] against the IEEE directed square roots
+// (sqrt_lo(v) <= sqrt_rd(v) and sqrt_hi(v) >= sqrt_ru(v)); counts failures and
+// keeps the smallest failing bit pattern.
+
+__global__ void __launch_bounds__(256) sqrt_bounds_kernel(uint32_t lo_bits, uint32_t hi_bits,
+                                                          unsigned long long* bad, uint32_t* first_bad) {
+  uint32_t n_bad = 0;
+  for (uint64_t b = (uint64_t)lo_bits + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; b <= hi_bits;
+       b += (uint64_t)gridDim.x * blockDim.x) {
+    const float v = __uint_as_float((uint32_t)b);
+    if (sqrt_lo(v) > __fsqrt_rd(v) || sqrt_hi(v) < __fsqrt_ru(v)) {
+      n_bad++;
+      atomicMin(first_bad, (uint32_t)b);
+    }
+  }
+  if (n_bad) atomicAdd(bad, (unsigned long long)n_bad);
+}
+
+int check_sqrt_bounds(uint32_t lo_bits, uint32_t hi_bits, unsigned long long* n_bad, uint32_t* first_bad) {
+  unsigned long long* d_bad = nullptr;
+  if (cudaMalloc((void**)&d_bad, 16) != cudaSuccess) return 1;
+  uint32_t* d_first = (uint32_t*)(d_bad + 1);
+  cudaMemset(d_bad, 0, 8);
+  cudaMemset(d_first, 0xff, 4);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  sqrt_bounds_kernel<<<sms * 8, 256>>>(lo_bits, hi_bits, d_bad, d_first);
+  cudaMemcpy(n_bad, d_bad, 8, cudaMemcpyDeviceToHost);
+  cudaMemcpy(first_bad, d_first, 4, cudaMemcpyDeviceToHost);
+  const cudaError_t e = cudaGetLastError();
+  cudaFree(d_bad);
+  return e == cudaSuccess ? 0 : 1;
 }
 
 // ---------------------------------------------------------------------------

@@ -58,7 +58,7 @@ __device__ __forceinline__ Iv isin32(Iv t) {
 __device__ __forceinline__ Iv iatan2_32(Iv Y, Iv X, bool& ok) {
   ok = !(X.lo < 0.f && Y.lo <= 0.f && Y.hi >= 0.f);
   const float cx = X.lo > 0.f ? X.lo : (X.hi < 0.f ? -X.hi : 0.f), cy = Y.lo > 0.f ? Y.lo : (Y.hi < 0.f ? -Y.hi : 0.f);
-  const float r_lo = __fsqrt_rd(__fadd_rd(__fmul_rd(cx, cx), __fmul_rd(cy, cy)));
+  const float r_lo = sqrt_lo(__fadd_rd(__fmul_rd(cx, cx), __fmul_rd(cy, cy)));
   ok = ok && r_lo > 0x1p-60f;
   const float mx = fminf(fmaxf(0.5f * (X.lo + X.hi), X.lo), X.hi), my = fminf(fmaxf(0.5f * (Y.lo + Y.hi), Y.lo), Y.hi);
   const float d = __fadd_ru(fmaxf(__fsub_ru(mx, X.lo), __fsub_ru(X.hi, mx)), fmaxf(__fsub_ru(my, Y.lo), __fsub_ru(Y.hi, my)));

@@ -75,6 +75,9 @@ struct px_world {
   // world state on the device
   uint32_t* d_grid = nullptr;
   uint32_t* d_pool32 = nullptr;   // pool as voxel pairs (capacity * 256 words)
+  uint16_t* d_pcount = nullptr;   // per pool brick: opaque, non-air voxels (written as bricks are written)
+  bool pcount_valid = true;       // d_pcount holds every referenced brick's count (tables unchanged since)
+  bool pcount_refresh = false;    // the build in flight recounts them from the pool
   uint32_t pool_cap = 0;
   uint32_t pool_used = 0;
   uint32_t n_holes = 0;
@@ -114,7 +117,8 @@ struct px_world {
     void clear() { pairs = tile_pairs = 0; painted64.clear(); painted32.clear(); }
   } q, last_q;
   std::vector<uint8_t> h_op_bucket;  // per op: cost bucket (0..63) of one evaluation
-  uint8_t class_order[VCLASSES] = {0};  // sub-block / voxel class order of the resident ops
+  uint8_t class_order[VCLASSES] = {0};  // sub-block class order of the resident ops
+  uint8_t vclass_order[VQ_CLASSES] = {0};  // voxel class order (each half on its own)
   DevBuf paint_items, pvals;    // sub-blocks to paint and the paint values
   DevBuf bmark, work;           // bricks the apply pass visits (bitmap, list)
   DevBuf scan_agg;
@@ -377,14 +381,25 @@ int grow_pool(px_world* w, uint64_t need, uint32_t keep, cudaStream_t s) {
   while (cap < need) cap = (uint64_t)std::ceil(cap * 1.5) + 1;
   if (cap > 0x3fffffffull) return fail(w, PX_E_OOM, "pool of %llu bricks exceeds the index range", (unsigned long long)cap);
   uint32_t* np_ = nullptr;
+  uint16_t* nc_ = nullptr;
   if (cudaMalloc((void**)&np_, (size_t)cap * 1024) != cudaSuccess) {
     cudaGetLastError();
     return fail(w, PX_E_OOM, "pool of %llu bricks", (unsigned long long)cap);
   }
-  if (keep) CU(cudaMemcpyAsync(np_, w->d_pool32, (size_t)keep * 1024, cudaMemcpyDeviceToDevice, s));
+  if (cudaMalloc((void**)&nc_, (size_t)cap * 2) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(np_);
+    return fail(w, PX_E_OOM, "pool of %llu bricks", (unsigned long long)cap);
+  }
+  if (keep) {
+    CU(cudaMemcpyAsync(np_, w->d_pool32, (size_t)keep * 1024, cudaMemcpyDeviceToDevice, s));
+    CU(cudaMemcpyAsync(nc_, w->d_pcount, (size_t)keep * 2, cudaMemcpyDeviceToDevice, s));
+  }
   CU(cudaStreamSynchronize(s));
   cudaFree(w->d_pool32);
+  cudaFree(w->d_pcount);
   w->d_pool32 = np_;
+  w->d_pcount = nc_;
   w->pool_cap = (uint32_t)cap;
   return PX_OK;
 }
@@ -424,6 +439,7 @@ static int world_create_impl(int dx, int dy, int dz, double vpm, uint32_t initia
   w->BX = dx / 8; w->BY = dy / 8; w->BZ = dz / 8;
   w->TX = (w->BX + 3) / 4; w->TY = (w->BY + 3) / 4; w->TZ = (w->BZ + 3) / 4;
   for (int k = 0; k < VCLASSES; k++) w->class_order[k] = (uint8_t)k;
+  for (int k = 0; k < VQ_CLASSES; k++) w->vclass_order[k] = (uint8_t)k;
   w->vpm = vpm;
   w->vs = 1 / vpm;  // config.ts:13
   w->ncells = (size_t)w->BX * w->BY * w->BZ;
@@ -444,6 +460,9 @@ static int world_create_impl(int dx, int dy, int dz, double vpm, uint32_t initia
   if (cudaMemset(w->d_grid, 0, w->ncells * 4) != cudaSuccess) { delete w; return PX_E_CUDA; }
   uint32_t cap = initial_pool_bricks ? initial_pool_bricks : 1;
   if (cudaMalloc((void**)&w->d_pool32, (size_t)cap * 1024) != cudaSuccess) { cudaFree(w->d_grid); delete w; return PX_E_OOM; }
+  if (cudaMalloc((void**)&w->d_pcount, (size_t)cap * 2) != cudaSuccess) {
+    cudaFree(w->d_grid); cudaFree(w->d_pool32); delete w; return PX_E_OOM;
+  }
   w->pool_cap = cap;
   if (cudaMallocHost((void**)&w->h_res, sizeof(BuildResult)) != cudaSuccess) { delete w; return PX_E_OOM; }
   cudaEventCreate(&w->ev0);
@@ -468,6 +487,7 @@ int px_set_material_tables(px_world* w, const uint8_t* opaque256, const uint8_t*
   CU(cudaMemcpy(w->opaque.p, opaque256, 256, cudaMemcpyHostToDevice));
   CU(cudaMemcpy(w->udens.p, uniform_density256, 256, cudaMemcpyHostToDevice));
   w->derived_valid = false;
+  w->pcount_valid = false;  // the pool bricks' opaque counts follow the old table
   return PX_OK;
 }
 
@@ -476,13 +496,15 @@ void px_world_destroy(px_world* w) {
   if (w->in_flight || w->uploads_pending) cudaStreamSynchronize(w->stream);
   cudaFree(w->d_grid);
   cudaFree(w->d_pool32);
+  cudaFree(w->d_pcount);
   DevBuf* bufs[] = {&w->holes_a, &w->holes_b, &w->d_ops, &w->d_boxes, &w->d_code, &w->d_params, &w->d_code32,
                     &w->d_p32, &w->d_bases, &w->tile_cnt,
                     &w->tile_off, &w->tile_ops, &w->evt, &w->fsrc, &w->cnt, &w->pos, &w->etype,
                     &w->ew, &w->depth_fn, &w->depth, &w->tree, &w->fresh, &w->fresh_rank, &w->staging, &w->touched,
                     &w->stage_cell, &w->stage_src, &w->chunk_op, &w->pcode, &w->psub, &w->pmask,
                     &w->chunk_counter, &w->vitems, &w->scan_agg, &w->work_counter, &w->res, &w->opaque,
-                    &w->udens, &w->super_counts, &w->density, &w->paint_items, &w->pvals, &w->tile_boxes, &w->bmark, &w->work, &w->pitems};
+                    &w->udens, &w->super_counts, &w->density, &w->paint_items, &w->pvals, &w->tile_boxes, &w->bmark, &w->work, &w->pitems,
+                    &w->free_list};
   for (DevBuf* b : bufs) release(*b);
   if (w->h_res) cudaFreeHost(w->h_res);
   if (w->ev0) cudaEventDestroy(w->ev0);
@@ -787,6 +809,20 @@ int convert_ops(const px_world* w, const IrOp* iops, size_t i0, size_t i1, const
           ysep = ysep && op_is_y_separable(code[2 * ((size_t)o.code_begin + k)] & 0xffu);
         if (ysep) d.flags |= OPF_Y_SEPARABLE;
         d.vclass = (first_prim & 15u) | (ysep && !(d.flags & OPF_FP64_ONLY) ? 16u : 0u);
+        // a single-primitive program: [rotation] primitive [rotation end] [offset]
+        d.simple = 0;
+        if (!(d.flags & (OPF_FP64_ONLY | OPF_DEEP))) {
+          uint32_t ops_[4] = {0, 0, 0, 0};
+          const uint32_t nc = o.code_len < 5 ? o.code_len : 0;
+          for (uint32_t k = 0; k < nc; k++) ops_[k] = code[2 * ((size_t)o.code_begin + k)] & 0xffu;
+          const bool rot = nc >= 3 && (ops_[0] == OP_ROT_X || ops_[0] == OP_ROT_Y || ops_[0] == OP_ROT_Z) &&
+                           ops_[1] < OP_ROT_X && ops_[1] >= OP_BOX && ops_[2] == OP_ROT_END;
+          const uint32_t np = rot ? 3 : 1;  // instructions before an offset
+          const bool prim_ok = rot || (nc >= 1 && ops_[0] >= OP_BOX && ops_[0] < OP_ROT_X);
+          if (prim_ok && (nc == np || (nc == np + 1 && ops_[np] == OP_OFFSET)))
+            d.simple = (rot ? ops_[1] : ops_[0]) | (rot ? ops_[0] << 8 : 0u) | (nc == np + 1 ? 1u << 16 : 0u);
+        }
+        d.vq_class = d.simple ? ((d.simple & 15u) | ((d.simple >> 8) ? 16u : 0u)) : 32u + d.vclass;
       }
       d.paint_slot = NO_SLOT;
       d.paint32_off = NO_SLOT;
@@ -928,7 +964,7 @@ int ensure_pair_scratch(px_world* w, uint64_t P, uint64_t tile_pairs, uint64_t n
       (rc = ensure(w, w->touched, 8 * touched_bound)) ||
       (rc = ensure(w, w->work_counter, 16)) || (rc = ensure(w, w->res, sizeof(BuildResult))) ||
       (rc = ensure(w, w->chunk_op, 8 * ((P + 31) / 32))) || (rc = ensure(w, w->pcode, P)) ||
-      (rc = ensure(w, w->psub, 2 * P)) || (rc = ensure(w, w->pmask, 64 * P)) || (rc = ensure(w, w->chunk_counter, 512)) || (rc = ensure(w, w->pitems, 8 * P)) ||
+      (rc = ensure(w, w->psub, 2 * P)) || (rc = ensure(w, w->pmask, 64 * P)) || (rc = ensure(w, w->chunk_counter, 1024)) || (rc = ensure(w, w->pitems, 8 * P)) ||
       (rc = ensure(w, w->vitems, 16 * 8 * P)) || (rc = ensure(w, w->paint_items, 8 * 16 * n_slots + 8)) ||
       (rc = ensure(w, w->pvals, 2048 * n_slots + 4)) || (rc = ensure(w, w->bmark, 4 * ((w->ncells + 31) / 32))) ||
       (rc = ensure(w, w->work, 4 * touched_bound + 4)))
@@ -1138,6 +1174,10 @@ static int enqueue_build_derive(px_world* w, cudaStream_t s, const uint32_t* hol
   da.free_cap = (uint32_t)fcap;
   da.max_bricks = w->derive_max;
   da.res = (BuildResult*)w->res.p;
+  // counts kept by finalize, unless the material tables changed since: then recount
+  da.pcount = w->pcount_valid ? w->d_pcount : nullptr;
+  da.pcount_out = w->pcount_valid ? nullptr : w->d_pcount;
+  w->pcount_refresh = !w->pcount_valid;
   launch_derive(da, s);
   return PX_OK;
 }
@@ -1248,7 +1288,7 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   // the build's counters and flags start at zero
   ups.push_back({w->res.p, nullptr, sizeof(BuildResult)});
   ups.push_back({w->work_counter.p, nullptr, 16});
-  ups.push_back({w->chunk_counter.p, nullptr, 512});
+  ups.push_back({w->chunk_counter.p, nullptr, 1024});
   ups.push_back({w->evt.p, nullptr, P});
   ups.push_back({w->cnt.p, nullptr, 4 * P});  // events per pair, written by the apply pass
   ups.push_back({w->bmark.p, nullptr, 4 * ((w->ncells + 31) / 32)});
@@ -1268,11 +1308,14 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
     // takes the chunks in: costliest ops first (a bucket sort, stable within a bucket)
     w->h_chunk_op.resize(2 * n_chunks);
     w->h_op_bucket.resize(n_ops);
-    float cc[VCLASSES] = {0.f};
+    float cc[VCLASSES] = {0.f}, cv[VQ_CLASSES] = {0.f};
     for (int i = 0; i < n_ops; i++) {
       const float c = w->ops[i].cost;
       w->h_op_bucket[i] = (uint8_t)cost_bucket(c);
-      if (w->ops[i].bx0 <= w->ops[i].bx1) cc[w->ops[i].vclass] = std::max(cc[w->ops[i].vclass], c);
+      if (w->ops[i].bx0 <= w->ops[i].bx1) {
+        cc[w->ops[i].vclass] = std::max(cc[w->ops[i].vclass], c);
+        cv[w->ops[i].vq_class] = std::max(cv[w->ops[i].vq_class], c);
+      }
     }
     // op o owns the chunks whose first pair it holds: [ceil(base_o / 32), ceil(base_o+1 / 32));
     // a chunk entry is (chunk, its first pair's op | bit 31 when all its pairs are that op's)
@@ -1305,11 +1348,17 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
     for (int k = 0; k < VCLASSES; k++) order[k] = k;
     std::stable_sort(order, order + VCLASSES, [&](int x, int y) { return cc[x] > cc[y]; });
     for (int k = 0; k < VCLASSES; k++) w->class_order[k] = (uint8_t)order[k];
+    int vorder[VQ_CLASSES];  // each half of the voxel classes costliest first
+    for (int k = 0; k < VQ_CLASSES; k++) vorder[k] = k;
+    for (int h = 0; h < 2; h++)
+      std::stable_sort(vorder + 32 * h, vorder + 32 * h + 32, [&](int x, int y) { return cv[x] > cv[y]; });
+    for (int k = 0; k < VQ_CLASSES; k++) w->vclass_order[k] = (uint8_t)vorder[k];
     if ((rc = issue_uploads(w, ups, s))) return rc;
   }
   FoldArgs fa{};
   fa.chunk_order = (const uint2*)w->chunk_op.p;
   for (int k = 0; k < VCLASSES; k++) fa.class_order[k] = w->class_order[k];
+  for (int k = 0; k < VQ_CLASSES; k++) fa.vclass_order[k] = w->vclass_order[k];
   fa.n_ops = (uint32_t)n_ops;
   fa.n_pairs = P;
   fa.pcode = (uint8_t*)w->pcode.p;
@@ -1319,25 +1368,31 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   fa.vitems = (uint4*)w->vitems.p;
   fa.vitems_cap = (uint32_t)(8 * P < 0xffffffffull ? 8 * P : 0xffffffffull);
   fa.vitem_counter = (uint32_t*)w->chunk_counter.p + 4;   // counters: [0] chunks, [1] paint taken,
-                                                          // [2] paint pushed, [4..36] voxel, [40..72] pairs
+                                                          // [2] paint pushed, [4..70] voxel, [80..113] pairs
   {  // per-class regions: the class's pairs (sub-block pass), 8 sub-blocks per pair (voxel pass)
-    uint64_t per[VCLASSES] = {0};
+    uint64_t per[VCLASSES] = {0}, vper[VQ_CLASSES] = {0};
     for (int i = 0; i < n_ops; i++) {
       const OpDev& o = w->ops[i];
       if (o.bx0 > o.bx1) continue;
-      per[o.vclass & (VCLASSES - 1)] += (uint64_t)o.nx * o.ny * (uint64_t)(o.bz1 - o.bz0 + 1);
+      const uint64_t np = (uint64_t)o.nx * o.ny * (uint64_t)(o.bz1 - o.bz0 + 1);
+      per[o.vclass & (VCLASSES - 1)] += np;
+      vper[o.vq_class & (VQ_CLASSES - 1)] += np;
     }
     uint64_t at = 0;
     for (int k = 0; k < VCLASSES; k++) {
       fa.pq_base[k] = (uint32_t)at;
       fa.pq_cap[k] = (uint32_t)per[k];
-      fa.vq_base[k] = (uint32_t)std::min<uint64_t>(8 * at, 0xffffffffull);
-      fa.vq_cap[k] = (uint32_t)std::min<uint64_t>(8 * per[k], 0xffffffffull - fa.vq_base[k]);
       at += per[k];
+    }
+    at = 0;
+    for (int k = 0; k < VQ_CLASSES; k++) {
+      fa.vq_base[k] = (uint32_t)std::min<uint64_t>(8 * at, 0xffffffffull);
+      fa.vq_cap[k] = (uint32_t)std::min<uint64_t>(8 * vper[k], 0xffffffffull - fa.vq_base[k]);
+      at += vper[k];
     }
   }
   fa.pitems = (uint2*)w->pitems.p;
-  fa.pitem_counter = (uint32_t*)w->chunk_counter.p + 40;
+  fa.pitem_counter = (uint32_t*)w->chunk_counter.p + 80;
   fa.paint_counter = (uint32_t*)w->chunk_counter.p + 1;
   fa.n_paint_slots = (uint32_t)n_slots;
   fa.paint_items = (uint2*)w->paint_items.p;
@@ -1413,6 +1468,8 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   fn.pool32 = w->d_pool32;
   fn.pool_cap = w->pool_cap;
   fn.res = res;
+  fn.opaque = (const uint8_t*)w->opaque.p;
+  fn.pcount = w->d_pcount;
   launch_finalize(fn, (uint32_t)touched_bound, s);
   if (w->derive_max && (rc = enqueue_build_derive(w, s, (const uint32_t*)holes_out.p))) return rc;
   CU(cudaGetLastError());
@@ -1495,6 +1552,7 @@ static int build_finish_impl(px_world* w) {
     const uint32_t st2 = r.status & ~(uint32_t)ST_POOL_OVERFLOW;
     CU(cudaMemcpyAsync(&dres->status, &st2, 4, cudaMemcpyHostToDevice, w->stream));
     w->fin.pool32 = w->d_pool32;
+    w->fin.pcount = w->d_pcount;
     w->fin.pool_cap = w->pool_cap;
     launch_finalize(w->fin, w->last_touched_cap, w->stream);
     if (w->derive_max) {  // the holes the replay wrote are the other buffer of the pair
@@ -1509,9 +1567,11 @@ static int build_finish_impl(px_world* w) {
     return rc;
   }
   w->retries = 0;
-  if (r.status & (ST_STAGE_OVERFLOW | ST_POOL_OVERFLOW | ST_CHAIN))
+  if (r.status & (ST_STAGE_OVERFLOW | ST_POOL_OVERFLOW | ST_CHAIN)) {
+    w->pcount_refresh = false;
     return fail(w, PX_E_QUEUE_OVERFLOW, "device status 0x%x (stage %u of %u, max pool index %u of %u)", r.status,
                 r.stage_count, w->last_stage_cap, r.max_pool_index, w->pool_cap);
+  }
   // the build is committed: holes/pool counters move to the new state
   w->pool_used = r.pool_used;
   w->n_holes = r.n_holes;
@@ -1535,6 +1595,8 @@ static int build_finish_impl(px_world* w) {
   w->params.clear();
   w->derived_valid = w->derive_max != 0;  // derive on build: super, density and free list are current
   w->free_valid = w->derive_max != 0;
+  if (w->pcount_refresh) w->pcount_valid = true;  // that derive recounted every referenced brick
+  w->pcount_refresh = false;
   w->free_over = (r.status & ST_FREE_CAP) != 0;
   w->free_len = r.free_len;
   w->stats.ops_applied = w->ops_applied;
@@ -1615,10 +1677,13 @@ int px_derive(px_world* w) {
   da.udens = (const uint8_t*)w->udens.p;
   da.super_counts = (uint32_t*)w->super_counts.p;
   da.density = (uint8_t*)w->density.p;
+  da.pcount = w->pcount_valid ? w->d_pcount : nullptr;
+  da.pcount_out = w->pcount_valid ? nullptr : w->d_pcount;
   launch_derive(da, 0);
   CU(cudaGetLastError());
   CU(cudaDeviceSynchronize());
   w->derived_valid = true;
+  w->pcount_valid = true;
   return PX_OK;
 }
 int px_read_super(px_world* w, uint32_t* dst, size_t n) {
@@ -1715,6 +1780,16 @@ int px_probe_peak(int fp64, float* tflops) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   *tflops = probe_fma_tflops(fp64, sms);
   return cudaGetLastError() == cudaSuccess ? PX_OK : PX_E_CUDA;
+}
+
+int px_check_sqrt_bounds(uint32_t lo_bits, uint32_t hi_bits, uint64_t* n_bad, uint32_t* first_bad) {
+  if (!n_bad || !first_bad || lo_bits > hi_bits || hi_bits >= 0x7f800000u) return PX_E_INVALID_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { cudaGetLastError(); return PX_E_NO_DEVICE; }
+  unsigned long long nb = 0;
+  if (check_sqrt_bounds(lo_bits, hi_bits, &nb, first_bad)) return PX_E_CUDA;
+  *n_bad = nb;
+  return PX_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -1895,6 +1970,7 @@ int px_batch_run(px_batch* b, void* stream, float* device_ms) {
     w->free_valid = w->derive_max != 0;
     w->free_over = (r.status & ST_FREE_CAP) != 0;
     w->free_len = r.free_len;
+    if (w->pcount_refresh) w->pcount_valid = true;  // the captured derive recounts every referenced brick
     w->ops_applied += w->last_ops.size();
     w->stats.ops_applied = w->ops_applied;
     w->stats.pool_used = w->pool_used;

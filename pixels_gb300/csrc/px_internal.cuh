@@ -76,7 +76,11 @@ struct OpDev {
   uint8_t kind, flags;
   uint16_t paint_kind;
   uint32_t paint_value;
-  uint32_t vclass;                       // voxel work class (VCLASSES)
+  uint32_t vclass;                       // sub-block work class (VCLASSES): first primitive, y-extruded
+  uint32_t vq_class;                     // voxel work class (VQ_CLASSES): [0, 32) single-primitive programs
+                                         // (voxel_simple_kernel), [32, 64) the others
+  uint32_t simple;                       // single-primitive program: primitive opcode | rotation opcode << 8
+                                         // (0: none) | 1 << 16 with an offset (0: not one)
   double bhd, shd;                       // brickHalfDiag, subHalfDiag (shapes.ts:349-350)
   double mn[3], mx[3];                   // contains box (boxes only)
   double frame[4];                       // paint frame px, pz, cos, sin
@@ -141,12 +145,20 @@ enum : uint8_t { PC_SKIP = 0, PC_PARTIAL = 1, PC_FULL = 2 };
 // (its first primitive, and whether it runs the y-extruded evaluation), so
 // that warps draining a queue at the same time run the same code.
 constexpr int VCLASSES = 32;
+// The voxel queue has twice as many classes: single-primitive programs --
+// [rotation] primitive [rotation end] [offset] -- by primitive and rotation in
+// classes [0, 32), drained by a kernel without a value stack or rotation
+// frames; every other program by its sub-block class + 32.
+constexpr int VQ_CLASSES = 64;
+constexpr int VQ_SIMPLE_TAKEN = 1 + VQ_CLASSES;  // vitem_counter slot of the single-primitive kernel's tickets
 
 struct FoldArgs {
   const uint2* chunk_order;  // the 32-pair chunks in the order classify_kernel takes them (costliest ops
                              // first): (chunk, op containing its first pair | 1 << 31 when that op holds
                              // all of the chunk's pairs)
-  uint8_t class_order[VCLASSES];  // the order the sub-block and voxel passes take the classes in
+  uint8_t class_order[VCLASSES];  // the order the sub-block pass takes its classes in
+  uint8_t vclass_order[VQ_CLASSES];  // the order the voxel passes take theirs: [0, 32) the single-primitive
+                                     // classes, [32, 64) the others
   uint32_t n_ops;
   unsigned long long n_pairs;
   uint8_t* pcode;             // per pair: PC_*
@@ -156,8 +168,9 @@ struct FoldArgs {
   uint4* vitems;              // partial sub-blocks to classify voxel by voxel: (op, pair << 3 | sub,
                               // bits of the centre value's enclosure lo, hi)
   uint32_t vitems_cap;
-  uint32_t* vitem_counter;    // [0] items taken, [1 + k] items pushed to class k
-  uint32_t vq_base[VCLASSES], vq_cap[VCLASSES];  // per-class regions of vitems
+  uint32_t* vitem_counter;    // [0] items taken by voxel_kernel's second half, [1 + k] items pushed to class k,
+                              // [VQ_SIMPLE_TAKEN] items taken from the first half
+  uint32_t vq_base[VQ_CLASSES], vq_cap[VQ_CLASSES];  // per-class regions of vitems
   uint2* pitems;              // partial pairs for the sub-block pass: (op, pair)
   uint32_t* pitem_counter;    // [0] items taken, [1 + k] items pushed to class k
   uint32_t pq_base[VCLASSES], pq_cap[VCLASSES];  // per-class regions of pitems
@@ -265,6 +278,10 @@ struct FinalizeArgs {
   uint32_t* pool32;
   uint32_t pool_cap;
   BuildResult* res;
+  // per pool brick: its opaque, non-air voxels (cellDensity's count, VoxelWorld.ts:163-169),
+  // written for every brick the build writes to the pool
+  const uint8_t* opaque;
+  uint16_t* pcount;
 };
 void launch_finalize(const FinalizeArgs& a, uint32_t touched_cap, cudaStream_t s);
 
@@ -302,6 +319,11 @@ struct DeriveArgs {
   uint32_t free_cap;      // entries free_list holds
   uint32_t max_bricks;
   BuildResult* res;
+  // pool bricks' opaque counts: read from pcount when it holds every referenced
+  // brick's count (kept by the builds' finalize), else counted from the pool and
+  // written to pcount_out
+  const uint16_t* pcount;
+  uint16_t* pcount_out;
 };
 void launch_derive(const DeriveArgs& a, cudaStream_t s);
 // entries the GPU free list of a pool of `pool_cap` bricks can need
@@ -314,6 +336,8 @@ __host__ __device__ inline uint64_t free_list_bound(uint64_t pool_cap, uint64_t 
 // (programmatic dependent launch) unless switched off (graph captures).
 void set_programmatic_launch(bool on);
 float probe_fma_tflops(int fp64, int n_sms);
+// failures of the float32 evaluator's square-root bounds over float bit patterns [lo_bits, hi_bits]
+int check_sqrt_bounds(uint32_t lo_bits, uint32_t hi_bits, unsigned long long* n_bad, uint32_t* first_bad);
 unsigned long long launch_count();
 
 }  // namespace px

@@ -44,7 +44,26 @@ __device__ __forceinline__ Iv isqr(Iv a) {
   float mx = fmaxf(l, h);
   return {__fmul_rd(mn, mn), __fmul_ru(mx, mx)};
 }
-__device__ __forceinline__ Iv isqrt(Iv a) { return {__fsqrt_rd(fmaxf(a.lo, 0.f)), __fsqrt_ru(fmaxf(a.hi, 0.f))}; }
+// Bounds of sqrt(v), v >= 0, from the hardware reciprocal square root.  CUDA
+// documents rsqrtf's maximum error as 2 ulp: 1/sqrt(v) = r (1 + d) with
+// |d| <= 2^-22, so sqrt(v) = v r (1 + d).  v r rounded down and shrunk by
+// (1 - 2^-20), resp. rounded up and grown by (1 + 2^-20), lies below, resp.
+// above sqrt(v), with a factor-4 margin on the documented bound.  This costs a
+// few instructions where the IEEE directed square roots (__fsqrt_rd/_ru) run a
+// long sequence, longer still at zero.  Outside [2^-100, 2^100]: 0 and 2^-50
+// bound the square roots of smaller values; larger ones (and infinity) take
+// the IEEE directed square roots.
+__device__ __forceinline__ float sqrt_lo(float v) {
+  if (v < 0x1p-100f) return 0.f;
+  if (v > 0x1p100f) return __fsqrt_rd(v);
+  return __fmul_rd(__fmul_rd(v, rsqrtf(v)), 1.f - 0x1p-20f);
+}
+__device__ __forceinline__ float sqrt_hi(float v) {
+  if (v < 0x1p-100f) return v > 0.f ? 0x1p-50f : 0.f;
+  if (v > 0x1p100f) return __fsqrt_ru(v);
+  return __fmul_ru(__fmul_ru(v, rsqrtf(v)), 1.f + 0x1p-20f);
+}
+__device__ __forceinline__ Iv isqrt(Iv a) { return {sqrt_lo(fmaxf(a.lo, 0.f)), sqrt_hi(fmaxf(a.hi, 0.f))}; }
 // x * c for a constant interval c that does not straddle zero (or is [0, 0])
 __device__ __forceinline__ Iv icmul(Iv x, Iv c) {
   if (c.lo >= 0.f) return {__fmul_rd(x.lo, x.lo >= 0.f ? c.lo : c.hi), __fmul_ru(x.hi, x.hi >= 0.f ? c.hi : c.lo)};
