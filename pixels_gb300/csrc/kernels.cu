@@ -594,6 +594,28 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_VOXEL_MINB : PX_CLASSIFY64
     if (lane >= o) incl += t;
   }
   const uint32_t n_items = __shfl_sync(FULLMASK, incl, 31);
+  if (MODE == 1 && HALF == 1) {
+    // first the voxels voxel_simple_kernel left undecided: one per thread, in float64
+    // (shapes.ts:393); their sub-block masks hold them as outside until here
+    const uint32_t n_resc = min(__ldcg(&a.res->n_rescue), a.rescue_cap);
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n_resc; r += gridDim.x * blockDim.x) {
+      const uint4 ri = __ldcg(a.rescue + r);
+      const OpDev* R = a.ops + (ri.x & 0xffffffu);
+      const int bit = (int)((ri.x >> 24) & 63u);
+      const bool ramb = (ri.x >> 30) & 1u;
+      const unsigned long long rp = ri.y >> 3;
+      const int rs = ri.y & 7;
+      int rbx, rby, rbz;
+      brick_of_pair(R, rp, rbx, rby, rbz);
+      const int vx = rbx * 8 + (rs & 1) * 4 + (bit & 3), vy = rby * 8 + ((rs >> 1) & 1) * 4 + ((bit >> 2) & 3),
+                vz = rbz * 8 + ((rs >> 2) & 1) * 4 + (bit >> 4);
+      const Iv dk = {__uint_as_float(ri.z), __uint_as_float(ri.w)};
+      const VoxelF64 f = voxel_f64(a.params, a.vs, 0, a.code + R->code_off, (int)R->code_len, dk, ramb, 3,
+                                   (float)vx + 0.5f, (float)vy + 0.5f, (float)vz + 0.5f);
+      ls.rescue(0, ramb, f.err);
+      if (f.inside) atomicOr(a.pmask + rp * 8 + rs, 1ull << bit);
+    }
+  }
   NextTicket tk;
   tk.issue(taken, 1, lane);
   for (;;) {
@@ -703,6 +725,11 @@ __device__ __forceinline__ void rot32(uint32_t op, const Iv* __restrict__ p, Iv&
 // rotation frames.  Lane = voxel column (x, z) of the sub-block and a pair of
 // y rows; a primitive extruded along y (unrotated, or rotated about y) shares
 // its x/z work between the two voxels.
+// VALIDATE (validation mode) evaluates every voxel in float64 too, in line;
+// otherwise a voxel the interval cannot decide goes to the rescue list (no
+// call in the kernel: the float64 evaluator's calls would make every register
+// live across them spill).
+template <bool VALIDATE>
 __global__ void __launch_bounds__(256, PX_VSIMPLE_MINB) voxel_simple_kernel(FoldArgs a) {
   pdl_prologue();
   const int lane = threadIdx.x & 31;
@@ -744,7 +771,7 @@ __global__ void __launch_bounds__(256, PX_VSIMPLE_MINB) voxel_simple_kernel(Fold
     const float M = V->thr[T_M];
     bool amb = false;
     Iv2 d = {{0.f, 0.f}, {0.f, 0.f}};
-    if (lip0 == 3 || lip1 == 3 || a.validate) {
+    if (lip0 == 3 || lip1 == 3 || VALIDATE) {
       const uint32_t* c32 = a.code32 + V->code_off;
       const uint32_t ip = rot ? 1u : 0u;  // the primitive's instruction
       const Iv* pr = P + __ldg(c32 + ip);
@@ -778,20 +805,28 @@ __global__ void __launch_bounds__(256, PX_VSIMPLE_MINB) voxel_simple_kernel(Fold
     for (int q = 0; q < 2; q++) {
       const Iv dk = q ? d.b : d.a;
       const int lipk = q ? lip1 : lip0;
+      const int bit = (col & 3) | ((2 * yh + q) << 2) | ((col >> 2) << 4);  // voxel index in the sub-block
       int inside = lipk;
-      if (lipk == 3 || a.validate) {
+      if (lipk == 3 || VALIDATE) {
         inside = amb ? 3 : (dk.lo > V->thr[T_V_HI] ? 0 : (dk.hi <= V->thr[T_V_LO] ? 1 : 3));
-        if (inside == 3 || a.validate) {
-          const VoxelF64 f = voxel_f64(a.params, a.vs, a.validate, code, clen, dk, amb, inside,
+        if constexpr (VALIDATE) {
+          const VoxelF64 f = voxel_f64(a.params, a.vs, 1, code, clen, dk, amb, inside,
                                        (float)(vbx * 8 + lx) + 0.5f, (float)(vby * 8 + ly0 + q) + 0.5f,
                                        (float)(vbz * 8 + lz) + 0.5f);
           if (f.viol) ls.viol();
           if (inside == 3) ls.rescue(0, amb, f.err);
           inside = f.inside;
+          if (lipk != 3 && inside != lipk) ls.viol();  // the bound disagreed with the evaluation
+        } else if (inside == 3) {  // decided in float64 by voxel_kernel<1, 1>; outside until then
+          const uint32_t r = atomicAdd(&a.res->n_rescue, 1u);
+          if (r < a.rescue_cap)
+            a.rescue[r] = make_uint4(item.x | ((uint32_t)bit << 24) | (amb ? 1u << 30 : 0u), item.y,
+                                     __float_as_uint(dk.lo), __float_as_uint(dk.hi));
+          else
+            atomicOr(&a.res->status, (uint32_t)ST_RESCUE_OVERFLOW);
+          inside = 0;
         }
-        if (lipk != 3 && inside != lipk) ls.viol();  // validation: the bound disagreed with the evaluation
       }
-      const int bit = (col & 3) | ((2 * yh + q) << 2) | ((col >> 2) << 4);  // voxel index in the sub-block
       if (inside == 1) {
         if (bit < 32) lo |= 1u << bit;
         else hi |= 1u << (bit - 32);
@@ -800,7 +835,8 @@ __global__ void __launch_bounds__(256, PX_VSIMPLE_MINB) voxel_simple_kernel(Fold
     const unsigned long long m =
         (unsigned long long)__reduce_or_sync(FULLMASK, lo) | ((unsigned long long)__reduce_or_sync(FULLMASK, hi) << 32);
     // a lone box's sub-block is queued only in validation mode: check its runs
-    if ((V->flags & OPF_BOX_RANGES) && lane == 0 && box_mask(V, vbx * 8 + sxo, vby * 8 + syo, vbz * 8 + szo) != m)
+    if (VALIDATE && (V->flags & OPF_BOX_RANGES) && lane == 0 &&
+        box_mask(V, vbx * 8 + sxo, vby * 8 + syo, vbz * 8 + szo) != m)
       ls.viol();
     if (lane == 0) a.pmask[vp * 8 + ss] = m;
   }
@@ -1289,7 +1325,8 @@ void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEve
   if (mode == 1) {
     launch_pdl(classify_kernel<1>, dim3(grid(PX_CLASSIFY_MINB)), dim3(256), 0, s, a);
     launch_pdl(sub_kernel<1>, dim3(grid(PX_SUB_MINB)), dim3(256), 0, s, a);
-    launch_pdl(voxel_simple_kernel, dim3(grid(PX_VSIMPLE_MINB)), dim3(256), 0, s, a);
+    if (a.validate) launch_pdl(voxel_simple_kernel<true>, dim3(grid(PX_VSIMPLE_MINB)), dim3(256), 0, s, a);
+    else launch_pdl(voxel_simple_kernel<false>, dim3(grid(PX_VSIMPLE_MINB)), dim3(256), 0, s, a);
     launch_pdl(voxel_kernel<1, 1>, dim3(grid(PX_VOXEL_MINB)), dim3(256), 0, s, a);
   } else {
     launch_pdl(classify_kernel<0>, dim3(grid(PX_CLASSIFY64_MINB)), dim3(256), 0, s, a);
@@ -1761,7 +1798,7 @@ __global__ void __launch_bounds__(256) finalize_kernel(FinalizeArgs a) {
   pdl_prologue();
   __syncthreads();
   // commit only a complete build: every staging slot written, every pool index within the pool
-  if (a.res->status & (ST_STAGE_OVERFLOW | ST_CHAIN)) return;
+  if (a.res->status & ST_NO_COMMIT) return;
   if (a.res->pool_used > a.pool_cap) {
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.res->status, (uint32_t)ST_POOL_OVERFLOW);
     return;
@@ -1861,7 +1898,7 @@ void launch_finalize(const FinalizeArgs& a, uint32_t touched_cap, cudaStream_t s
 __global__ void __launch_bounds__(256) derive_kernel(DeriveArgs a) {
   pdl_prologue();
   // a build that committed nothing leaves the world (and its derived buffers) as they were
-  if (a.res && (a.res->status & (ST_STAGE_OVERFLOW | ST_POOL_OVERFLOW | ST_CHAIN))) return;
+  if (a.res && (a.res->status & (ST_NO_COMMIT | ST_POOL_OVERFLOW))) return;
   const uint32_t* __restrict__ grid = a.grid;
   const uint32_t* __restrict__ pool32 = a.pool32;
   const int BX = a.BX, BY = a.BY, BZ = a.BZ;

@@ -105,6 +105,8 @@ struct px_world {
   DevBuf evt, fsrc, cnt, pos, etype, ew, depth_fn, depth, tree, fresh, fresh_rank;
   DevBuf staging, stage_cell, stage_src, touched;
   uint64_t stage_hint = 0;      // staging slots the next build reserves (grown on overflow)
+  uint32_t rescue_cap = 1u << 16;  // voxels a build may leave to float64 (grown on overflow)
+  DevBuf rescue;
   DevBuf chunk_op, pcode, psub, pmask, chunk_counter, vitems, pitems;
   std::vector<uint32_t> h_chunk_op;  // the chunks in classify order: (chunk, op of its first pair | single-op bit)
   std::vector<Upload> h_uploads;     // the op-table copies of the build being enqueued
@@ -504,7 +506,7 @@ void px_world_destroy(px_world* w) {
                     &w->stage_cell, &w->stage_src, &w->chunk_op, &w->pcode, &w->psub, &w->pmask,
                     &w->chunk_counter, &w->vitems, &w->scan_agg, &w->work_counter, &w->res, &w->opaque,
                     &w->udens, &w->super_counts, &w->density, &w->paint_items, &w->pvals, &w->tile_boxes, &w->bmark, &w->work, &w->pitems,
-                    &w->free_list};
+                    &w->free_list, &w->rescue};
   for (DevBuf* b : bufs) release(*b);
   if (w->h_res) cudaFreeHost(w->h_res);
   if (w->ev0) cudaEventDestroy(w->ev0);
@@ -967,7 +969,7 @@ int ensure_pair_scratch(px_world* w, uint64_t P, uint64_t tile_pairs, uint64_t n
       (rc = ensure(w, w->psub, 2 * P)) || (rc = ensure(w, w->pmask, 64 * P)) || (rc = ensure(w, w->chunk_counter, 1024)) || (rc = ensure(w, w->pitems, 8 * P)) ||
       (rc = ensure(w, w->vitems, 16 * 8 * P)) || (rc = ensure(w, w->paint_items, 8 * 16 * n_slots + 8)) ||
       (rc = ensure(w, w->pvals, 2048 * n_slots + 4)) || (rc = ensure(w, w->bmark, 4 * ((w->ncells + 31) / 32))) ||
-      (rc = ensure(w, w->work, 4 * touched_bound + 4)))
+      (rc = ensure(w, w->work, 4 * touched_bound + 4)) || (rc = ensure(w, w->rescue, 16 * (size_t)w->rescue_cap)))
     return rc;
   return ensure(w, w->scan_agg, scan_temp_bytes(scan_blocks(w, P, E_max)));
 }
@@ -1198,6 +1200,7 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   std::vector<uint32_t>& painted = w->h_painted;  // float64-only paints first
   painted.assign(w->q.painted64.begin(), w->q.painted64.end());
   if (P > 0x1fffffffull) return fail(w, PX_E_QUEUE_OVERFLOW, "too many (op, brick) pairs in one build: %llu", (unsigned long long)P);
+  if (n_ops >= (1 << 24)) return fail(w, PX_E_QUEUE_OVERFLOW, "too many ops in one build: %d", n_ops);
   painted.insert(painted.end(), w->q.painted32.begin(), w->q.painted32.end());
   // paint slots (one per (op, brick) pair of a painted op, 2 KiB each): every
   // painted op when they fit in 512 MiB, else the heavy kinds alone when they
@@ -1393,6 +1396,8 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   }
   fa.pitems = (uint2*)w->pitems.p;
   fa.pitem_counter = (uint32_t*)w->chunk_counter.p + 80;
+  fa.rescue = (uint4*)w->rescue.p;
+  fa.rescue_cap = w->rescue_cap;
   fa.paint_counter = (uint32_t*)w->chunk_counter.p + 1;
   fa.n_paint_slots = (uint32_t)n_slots;
   fa.paint_items = (uint2*)w->paint_items.p;
@@ -1535,6 +1540,15 @@ static int build_finish_impl(px_world* w) {
   w->stats.build_ms = ms;
   fill_stats(w, r);
   // transactional retries: nothing was committed
+  if ((r.status & ST_RESCUE_OVERFLOW) && w->retries < 2) {  // more voxels left to float64 than the list holds
+    w->rescue_cap = std::max(w->rescue_cap, r.n_rescue + r.n_rescue / 4 + 1024);
+    w->retries++;
+    w->ops_resident = true;
+    int rc = px_build_enqueue(w, w->last_mode, w->stream);
+    if (rc == PX_OK) rc = px_build_finish(w);
+    w->retries = 0;
+    return rc;
+  }
   if ((r.status & ST_STAGE_OVERFLOW) && r.stage_count > w->last_stage_cap && w->retries < 2) {
     w->stage_hint = (uint64_t)r.stage_count + r.stage_count / 4 + 64;
     w->retries++;
@@ -1544,7 +1558,7 @@ static int build_finish_impl(px_world* w) {
     w->retries = 0;
     return rc;
   }
-  if ((r.status & ST_POOL_OVERFLOW) && !(r.status & (ST_STAGE_OVERFLOW | ST_CHAIN)) && w->retries < 2) {
+  if ((r.status & ST_POOL_OVERFLOW) && !(r.status & ST_NO_COMMIT) && w->retries < 2) {
     w->retries++;
     int rc = grow_pool(w, (uint64_t)r.pool_used + r.pool_used / 4 + 64, w->last_U0, w->stream);
     if (rc) { w->retries = 0; return rc; }
@@ -1567,7 +1581,7 @@ static int build_finish_impl(px_world* w) {
     return rc;
   }
   w->retries = 0;
-  if (r.status & (ST_STAGE_OVERFLOW | ST_POOL_OVERFLOW | ST_CHAIN)) {
+  if (r.status & (ST_NO_COMMIT | ST_POOL_OVERFLOW)) {
     w->pcount_refresh = false;
     return fail(w, PX_E_QUEUE_OVERFLOW, "device status 0x%x (stage %u of %u, max pool index %u of %u)", r.status,
                 r.stage_count, w->last_stage_cap, r.max_pool_index, w->pool_cap);
@@ -1959,7 +1973,7 @@ int px_batch_run(px_batch* b, void* stream, float* device_ms) {
     const BuildResult& r = *w->h_res;
     fill_stats(w, r);
     w->stats.build_ms = 0.f;
-    if (r.status & (ST_STAGE_OVERFLOW | ST_POOL_OVERFLOW | ST_CHAIN)) {
+    if (r.status & (ST_NO_COMMIT | ST_POOL_OVERFLOW)) {
       if (first == PX_OK) first = batch_fail(b, PX_E_QUEUE_OVERFLOW, "world %zu: device status 0x%x", i, r.status);
       continue;
     }

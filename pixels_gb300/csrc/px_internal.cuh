@@ -53,7 +53,10 @@ enum { T_BSK_HI, T_BSK_LO, T_BFU_HI, T_BFU_LO, T_SSK_HI, T_SSK_LO, T_SFU_HI, T_S
 enum : uint32_t {
   ST_OK = 0, ST_STAGE_OVERFLOW = 1, ST_POOL_OVERFLOW = 2, ST_RANGE = 4, ST_CHAIN = 8,
   ST_FREE_CAP = 16,  // derive: poolUsed exceeds the GPU pool capacity (GpuWorld.ts:59 throws)
+  ST_RESCUE_OVERFLOW = 32,  // the list of voxels left to float64 ran out of room (the build commits nothing)
 };
+// a build's failures: it commits nothing and the host retries with larger buffers or reports
+constexpr uint32_t ST_NO_COMMIT = ST_STAGE_OVERFLOW | ST_CHAIN | ST_RESCUE_OVERFLOW;
 
 // PXIR op record (128 bytes, pixels_gb300/ir.py OP_DTYPE)
 struct IrOp {
@@ -134,7 +137,7 @@ struct BuildResult {
   BuildCounters c;
   unsigned long long max_err_bits;  // max |mid(d32) - d64| over rescued evaluations (double bits, >= 0)
   uint32_t free_len;     // derive: length of the GPU free list (GpuWorld.ts:103-111, C_FREE_TOP)
-  uint32_t pad_;
+  uint32_t n_rescue;     // voxels the float32 pass left to float64 (voxel_simple_kernel), pushed
 };
 
 // Pair classification (state independent): class per (op, brick) pair, the 8
@@ -165,6 +168,11 @@ struct FoldArgs {
   uint16_t* psub;             // per partial pair: 2 bits per sub-block (PC_*)
   unsigned long long* pmask;  // per partial pair: 8 inside-masks (bit = x&3 | (y&3)<<2 | (z&3)<<4)
   uint32_t* chunk_counter;
+  // voxels whose float32 interval cannot decide them, left by voxel_simple_kernel
+  // to voxel_kernel<1, 1> (which carries the float64 evaluator): (op | voxel bit << 24 |
+  // undecided-crossing-test << 30, pair << 3 | sub-block, interval lo, hi bits)
+  uint4* rescue;
+  uint32_t rescue_cap;
   uint4* vitems;              // partial sub-blocks to classify voxel by voxel: (op, pair << 3 | sub,
                               // bits of the centre value's enclosure lo, hi)
   uint32_t vitems_cap;
