@@ -1586,8 +1586,13 @@ enum : uint8_t { EV_PUSH = 0, EV_POP = 1 };
 __global__ void events_build_kernel(ReplayArgs a) {
   pdl_prologue();
   const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
-  if (tid == 0) a.res->n_events = a.H + (a.P ? a.pos[a.P - 1] + a.cnt[a.P - 1] : 0u);
-  for (size_t i = tid; i < a.H; i += stride) {
+  const uint32_t H = __ldcg(&a.state->n_holes);  // the committed state: no build writes it until this one commits
+  if (tid == 0) {
+    a.res->n_events = H + (a.P ? a.pos[a.P - 1] + a.cnt[a.P - 1] : 0u);
+    a.res->h_before = H;
+    a.res->u_before = __ldcg(&a.state->pool_used);
+  }
+  for (size_t i = tid; i < H; i += stride) {
     a.etype[i] = EV_PUSH;
     a.depth_fn[i] = make_int2(1, -(1 << 30));
     a.ew[i] = KNOWN | a.holes_in[i];
@@ -1595,7 +1600,7 @@ __global__ void events_build_kernel(ReplayArgs a) {
   for (size_t p = tid; p < a.P; p += stride) {
     const uint32_t e = a.evt[p];
     if (!e) continue;
-    const size_t base = a.H + a.pos[p];
+    const size_t base = H + a.pos[p];
     if (e & 1u) {
       a.etype[base] = EV_POP;
       a.depth_fn[base] = make_int2(-1, 0);
@@ -1606,7 +1611,7 @@ __global__ void events_build_kernel(ReplayArgs a) {
       a.etype[k] = EV_PUSH;
       a.depth_fn[k] = make_int2(1, -(1 << 30));
       const long long src = a.fsrc[p];
-      a.ew[k] = src >= 0 ? (unsigned long long)(a.H + a.pos[src]) : (KNOWN | (unsigned long long)(-(src + 1)));
+      a.ew[k] = src >= 0 ? (unsigned long long)(H + a.pos[src]) : (KNOWN | (unsigned long long)(-(src + 1)));
     }
   }
 }
@@ -1701,11 +1706,12 @@ __device__ long long prev_less(const int32_t* depth, const int32_t* tree, const 
 __global__ void match_kernel(ReplayArgs a, TreeLevels tl) {
   pdl_prologue();
   const size_t E = a.res->n_events;
+  const uint32_t U0 = a.res->u_before;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (size_t)gridDim.x * blockDim.x) {
     if (a.etype[e] != EV_POP) continue;
     const int dprev = e ? a.depth[e - 1] : 0;
     if (dprev == 0) {
-      a.ew[e] = KNOWN | (unsigned long long)(a.U0 + a.fresh_rank[e]);
+      a.ew[e] = KNOWN | (unsigned long long)(U0 + a.fresh_rank[e]);
     } else {
       long long i = prev_less(a.depth, a.tree, tl, E, e, dprev);
       a.ew[e] = (unsigned long long)(i + 1);  // the push that filled slot dprev
@@ -1734,7 +1740,7 @@ __global__ void resolve_kernel(unsigned long long* ew, BuildResult* res) {
 
 __global__ void holes_out_kernel(const uint8_t* __restrict__ etype, const int32_t* __restrict__ depth,
                                  const int32_t* __restrict__ sufmin, const unsigned long long* __restrict__ ew,
-                                 uint32_t* holes_out, BuildResult* res, uint32_t U0) {
+                                 uint32_t* holes_out, BuildResult* res) {
   pdl_prologue();
   const size_t E = res->n_events;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (size_t)gridDim.x * blockDim.x) {
@@ -1744,7 +1750,7 @@ __global__ void holes_out_kernel(const uint8_t* __restrict__ etype, const int32_
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     res->n_holes = E ? (uint32_t)depth[E - 1] : 0u;
-    res->pool_used = U0 + res->n_fresh;
+    res->pool_used = res->u_before + res->n_fresh;
   }
 }
 
@@ -1763,7 +1769,7 @@ void launch_replay(const ReplayArgs& a, cudaStream_t s) {
   const size_t cap = (size_t)n_sms * 8;
   auto blocks = [&](size_t n) { size_t b = (n + T - 1) / T; return (int)(b < cap ? (b ? b : 1) : cap); };
   scan_any<SumOp, false>(a.cnt, a.pos, a.P, nullptr, false, nullptr, *a.scan, s);
-  launch_pdl(events_build_kernel, dim3(blocks(a.P > a.H ? a.P : a.H)), dim3(T), 0, s, a);  // also the event count
+  launch_pdl(events_build_kernel, dim3(blocks(a.P > a.H_max ? a.P : a.H_max)), dim3(T), 0, s, a);  // also the event count
   const uint32_t* nE = &a.res->n_events;
   scan_any<DepthOp, false>(a.depth_fn, a.depth_fn, a.E_max, nE, true, nullptr, *a.scan, s);
   launch_pdl(depth_fresh_kernel, dim3(blocks(a.E_max)), dim3(T), 0, s, (const int2*)a.depth_fn, (const uint8_t*)a.etype, a.depth, a.fresh, (const BuildResult*)a.res);
@@ -1786,7 +1792,7 @@ void launch_replay(const ReplayArgs& a, cudaStream_t s) {
   // suffix minimum of the depths (stored after the tree levels)
   int32_t* sufmin = a.tree + off;
   scan_any<MinOp, true>(a.depth, sufmin, a.E_max, nE, true, nullptr, *a.scan, s);
-  launch_pdl(holes_out_kernel, dim3(blocks(a.E_max)), dim3(T), 0, s, (const uint8_t*)a.etype, (const int32_t*)a.depth, (const int32_t*)sufmin, (const unsigned long long*)a.ew, a.holes_out, a.res, a.U0);
+  launch_pdl(holes_out_kernel, dim3(blocks(a.E_max)), dim3(T), 0, s, (const uint8_t*)a.etype, (const int32_t*)a.depth, (const int32_t*)sufmin, (const unsigned long long*)a.ew, a.holes_out, a.res);
 }
 
 // ---------------------------------------------------------------------------
@@ -1797,12 +1803,22 @@ __global__ void __launch_bounds__(256) finalize_kernel(FinalizeArgs a) {
   op_s[threadIdx.x] = a.opaque[threadIdx.x];  // 256 threads
   pdl_prologue();
   __syncthreads();
-  // commit only a complete build: every staging slot written, every pool index within the pool
-  if (a.res->status & ST_NO_COMMIT) return;
-  if (a.res->pool_used > a.pool_cap) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.res->status, (uint32_t)ST_POOL_OVERFLOW);
+  // commit only a complete build (every staging slot written, every pool index within
+  // the pool) that follows committed builds; the first thread records the outcome
+  const bool after_failure = __ldcg(&a.state->poisoned) != 0;
+  if (after_failure || (a.res->status & ST_NO_COMMIT) || a.res->pool_used > a.pool_cap) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      if (after_failure) atomicOr(&a.res->status, (uint32_t)ST_CHAIN);
+      else if (!(a.res->status & ST_NO_COMMIT)) atomicOr(&a.res->status, (uint32_t)ST_POOL_OVERFLOW);
+      a.state->poisoned = 1u;
+    }
     return;
   }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {  // nothing below reads the state
+    a.state->pool_used = a.res->pool_used;
+    a.state->n_holes = a.res->n_holes;
+  }
+  const uint32_t H = a.res->h_before;
   const int lane = threadIdx.x & 31;
   const uint32_t n = a.res->touched_count;
   // 32 touched bricks per warp pass: each lane resolves one brick's pool index
@@ -1822,7 +1838,7 @@ __global__ void __launch_bounds__(256) finalize_kernel(FinalizeArgs a) {
         slot = e.y & 0x3fffffffu;
         const long long src = a.stage_src[slot];
         if (src >= 0) {
-          const unsigned long long w = a.ew[a.H + a.pos[src]];
+          const unsigned long long w = a.ew[H + a.pos[src]];
           if (!(w & KNOWN)) atomicOr(&a.res->status, (uint32_t)ST_CHAIN);
           else { idx = (uint32_t)(w & 0xffffffffull); staged = true; }
         } else {

@@ -31,6 +31,7 @@ namespace {
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
+  bool borrowed = false;  // another world's buffer (pipelined serving): never reallocated or freed here
 };
 
 // The world's host op tables are filled by several host threads at once: a
@@ -75,6 +76,8 @@ struct px_world {
   // world state on the device
   uint32_t* d_grid = nullptr;
   uint32_t* d_pool32 = nullptr;   // pool as voxel pairs (capacity * 256 words)
+  WorldState* d_state = nullptr;  // poolUsed and hole count as the builds commit them (device)
+  bool shares_state = false;      // grid, pool, counts, holes and state belong to another world
   uint16_t* d_pcount = nullptr;   // per pool brick: opaque, non-air voxels (written as bricks are written)
   bool pcount_valid = true;       // d_pcount holds every referenced brick's count (tables unchanged since)
   bool pcount_refresh = false;    // the build in flight recounts them from the pool
@@ -183,6 +186,7 @@ int fail(px_world* w, int code, const char* fmt, ...) {
 int ensure(px_world* w, DevBuf& b, size_t bytes) {
   if (bytes == 0) bytes = 16;
   if (b.bytes >= bytes) return PX_OK;
+  if (b.borrowed) return fail(w, PX_E_OOM, "a shared buffer of %zu bytes is too small (%zu needed)", b.bytes, bytes);
   if (b.p) cudaFree(b.p);
   b.p = nullptr;
   b.bytes = 0;
@@ -195,6 +199,7 @@ int ensure(px_world* w, DevBuf& b, size_t bytes) {
   return PX_OK;
 }
 void release(DevBuf& b) {
+  if (b.borrowed) { b = DevBuf{}; return; }
   if (b.p) cudaFree(b.p);
   b.p = nullptr;
   b.bytes = 0;
@@ -379,6 +384,7 @@ bool check_code(const uint32_t* code, uint32_t n, const double* P, size_t np, st
 // bricks (growPool, VoxelWorld.ts:129-136, grows by 1.5x).
 int grow_pool(px_world* w, uint64_t need, uint32_t keep, cudaStream_t s) {
   if (need <= w->pool_cap) return PX_OK;
+  if (w->shares_state) return fail(w, PX_E_OOM, "the shared pool of %u bricks cannot grow here", w->pool_cap);
   uint64_t cap = w->pool_cap ? w->pool_cap : 1;
   while (cap < need) cap = (uint64_t)std::ceil(cap * 1.5) + 1;
   if (cap > 0x3fffffffull) return fail(w, PX_E_OOM, "pool of %llu bricks exceeds the index range", (unsigned long long)cap);
@@ -467,6 +473,12 @@ static int world_create_impl(int dx, int dy, int dz, double vpm, uint32_t initia
   }
   w->pool_cap = cap;
   if (cudaMallocHost((void**)&w->h_res, sizeof(BuildResult)) != cudaSuccess) { delete w; return PX_E_OOM; }
+  if (cudaMalloc((void**)&w->d_state, sizeof(WorldState)) != cudaSuccess ||
+      cudaMemset(w->d_state, 0, sizeof(WorldState)) != cudaSuccess) {
+    cudaGetLastError();
+    delete w;
+    return PX_E_OOM;
+  }
   cudaEventCreate(&w->ev0);
   cudaEventCreate(&w->ev1);
   cudaEventCreate(&w->ev_fold0);
@@ -496,9 +508,12 @@ int px_set_material_tables(px_world* w, const uint8_t* opaque256, const uint8_t*
 void px_world_destroy(px_world* w) {
   if (!w || w->batch_locked) return;  // a batch's world outlives the batch
   if (w->in_flight || w->uploads_pending) cudaStreamSynchronize(w->stream);
-  cudaFree(w->d_grid);
-  cudaFree(w->d_pool32);
-  cudaFree(w->d_pcount);
+  if (!w->shares_state) {
+    cudaFree(w->d_grid);
+    cudaFree(w->d_pool32);
+    cudaFree(w->d_pcount);
+    cudaFree(w->d_state);
+  }
   DevBuf* bufs[] = {&w->holes_a, &w->holes_b, &w->d_ops, &w->d_boxes, &w->d_code, &w->d_params, &w->d_code32,
                     &w->d_p32, &w->d_bases, &w->tile_cnt,
                     &w->tile_off, &w->tile_ops, &w->evt, &w->fsrc, &w->cnt, &w->pos, &w->etype,
@@ -1223,13 +1238,16 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
     if (n_slots * 2048 <= (512ull << 20)) break;
   }
   const uint64_t touched_bound = P < w->ncells ? P : w->ncells;
+  // the host's view of the allocator state (exact unless builds are pipelined,
+  // where the replay reads it from the device and these only bound sizes)
   const uint32_t H = w->n_holes, U0 = w->pool_used;
-  const size_t E_max = (size_t)H + 2 * P;
+  size_t E_max = (size_t)std::max(H, w->pool_cap) + 2 * P;
 
   // staging slots and pool bricks are reserved from a guess; a build that needs
   // more commits nothing and is retried with larger buffers (px_build_finish)
   const uint64_t stage_cap = stage_slots(w, P);
   if ((rc = grow_pool(w, (uint64_t)U0 + stage_cap, U0, s))) return rc;
+  E_max = (size_t)std::max(H, w->pool_cap) + 2 * P;
 
   // scratch (a reallocated op table loses its resident copy)
   const void* op_bufs_before[9] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p,
@@ -1244,6 +1262,7 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
       (rc = ensure_pair_scratch(w, P, tile_pairs, n_slots, touched_bound, E_max, stage_cap)))
     return rc;
   const size_t scan_nb = scan_blocks(w, P, E_max);
+  const uint32_t H_max = std::max(H, w->pool_cap);  // holes are pool bricks
   {
     const void* after[9] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p,
                             w->d_p32.p, w->d_bases.p, w->chunk_op.p, w->chunk_op.p};
@@ -1442,7 +1461,7 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   if (!w->capturing) CU(cudaEventRecord(w->ev_fold1, s));
 
   ReplayArgs ra{};
-  ra.P = P; ra.E_max = E_max; ra.H = H; ra.U0 = U0;
+  ra.P = P; ra.E_max = E_max; ra.H_max = H_max; ra.state = w->d_state;
   ra.evt = (const uint8_t*)w->evt.p;
   ra.fsrc = (const int64_t*)w->fsrc.p;
   ra.holes_in = (const uint32_t*)holes_in.p;
@@ -1468,7 +1487,7 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   fn.stage_src = (const int64_t*)w->stage_src.p;
   fn.pos = (const uint32_t*)w->pos.p;
   fn.ew = (const unsigned long long*)w->ew.p;
-  fn.H = H;
+  fn.state = w->d_state;
   fn.grid = w->d_grid;
   fn.pool32 = w->d_pool32;
   fn.pool_cap = w->pool_cap;
@@ -1540,7 +1559,10 @@ static int build_finish_impl(px_world* w) {
   w->stats.build_ms = ms;
   fill_stats(w, r);
   // transactional retries: nothing was committed
+  // a build that commits nothing poisons the device state (WorldState); retries clear it
+  auto clear_poison = [&] { return cudaMemsetAsync(&w->d_state->poisoned, 0, 4, w->stream); };
   if ((r.status & ST_RESCUE_OVERFLOW) && w->retries < 2) {  // more voxels left to float64 than the list holds
+    CU(clear_poison());
     w->rescue_cap = std::max(w->rescue_cap, r.n_rescue + r.n_rescue / 4 + 1024);
     w->retries++;
     w->ops_resident = true;
@@ -1550,6 +1572,7 @@ static int build_finish_impl(px_world* w) {
     return rc;
   }
   if ((r.status & ST_STAGE_OVERFLOW) && r.stage_count > w->last_stage_cap && w->retries < 2) {
+    CU(clear_poison());
     w->stage_hint = (uint64_t)r.stage_count + r.stage_count / 4 + 64;
     w->retries++;
     w->ops_resident = true;  // the op tables uploaded by this attempt are still on the device
@@ -1563,6 +1586,7 @@ static int build_finish_impl(px_world* w) {
     int rc = grow_pool(w, (uint64_t)r.pool_used + r.pool_used / 4 + 64, w->last_U0, w->stream);
     if (rc) { w->retries = 0; return rc; }
     BuildResult* dres = (BuildResult*)w->res.p;
+    CU(clear_poison());
     const uint32_t st2 = r.status & ~(uint32_t)ST_POOL_OVERFLOW;
     CU(cudaMemcpyAsync(&dres->status, &st2, 4, cudaMemcpyHostToDevice, w->stream));
     w->fin.pool32 = w->d_pool32;
@@ -1583,6 +1607,10 @@ static int build_finish_impl(px_world* w) {
   w->retries = 0;
   if (r.status & (ST_NO_COMMIT | ST_POOL_OVERFLOW)) {
     w->pcount_refresh = false;
+    if (!w->shares_state) {  // nothing was committed: the world stays as it was, ready for the next build
+      CU(clear_poison());
+      CU(cudaStreamSynchronize(w->stream));
+    }
     return fail(w, PX_E_QUEUE_OVERFLOW, "device status 0x%x (stage %u of %u, max pool index %u of %u)", r.status,
                 r.stage_count, w->last_stage_cap, r.max_pool_index, w->pool_cap);
   }
@@ -1642,6 +1670,7 @@ static int world_reset_impl(px_world* w, int requeue_last_ops, void* stream) {
     w->uploads_pending = false;
   }
   CU(cudaMemsetAsync(w->d_grid, 0, w->ncells * 4, (cudaStream_t)stream));
+  CU(cudaMemsetAsync(w->d_state, 0, sizeof(WorldState), (cudaStream_t)stream));
   w->pool_used = 0;
   w->n_holes = 0;
   w->derived_valid = false;
@@ -1975,6 +2004,7 @@ int px_batch_run(px_batch* b, void* stream, float* device_ms) {
     w->stats.build_ms = 0.f;
     if (r.status & (ST_NO_COMMIT | ST_POOL_OVERFLOW)) {
       if (first == PX_OK) first = batch_fail(b, PX_E_QUEUE_OVERFLOW, "world %zu: device status 0x%x", i, r.status);
+      cudaMemset(&w->d_state->poisoned, 0, 4);  // the world stays as it was
       continue;
     }
     w->pool_used = r.pool_used;

@@ -123,6 +123,16 @@ struct BuildCounters {
   unsigned long long resc_paint;  // mixed mode: paint calls the float32 path could not decide
 };
 
+// The world's allocator state on the device (VoxelWorld.poolUsed and the
+// free-list length), written by the finalize kernel of each build that commits
+// and read by the next build's allocator replay, so that builds can be queued
+// before the previous one has returned to the host.  A build that commits
+// nothing sets `poisoned`; every later build then commits nothing either,
+// until the host clears it.
+struct WorldState {
+  uint32_t pool_used, n_holes, poisoned, pad;
+};
+
 // Small device block read back after every build.
 struct BuildResult {
   uint32_t status;
@@ -138,6 +148,9 @@ struct BuildResult {
   unsigned long long max_err_bits;  // max |mid(d32) - d64| over rescued evaluations (double bits, >= 0)
   uint32_t free_len;     // derive: length of the GPU free list (GpuWorld.ts:103-111, C_FREE_TOP)
   uint32_t n_rescue;     // voxels the float32 pass left to float64 (voxel_simple_kernel), pushed
+  uint32_t h_before;     // holes before the build (from the WorldState)
+  uint32_t u_before;     // poolUsed before the build
+  uint32_t pad2;
 };
 
 // Pair classification (state independent): class per (op, brick) pair, the 8
@@ -252,9 +265,9 @@ void launch_scan_u32(const uint32_t* in, uint32_t* out, size_t n, const uint32_t
 
 struct ReplayArgs {
   size_t P;                 // pairs
-  size_t E_max;             // H + 2P
-  uint32_t H;               // holes before the build
-  uint32_t U0;              // poolUsed before the build
+  size_t E_max;             // bound of H + 2P (H: holes before the build)
+  uint32_t H_max;           // bound of H (launch sizes only)
+  const WorldState* state;  // H and poolUsed before the build, copied to res->h_before / u_before
   const uint8_t* evt;
   const int64_t* fsrc;
   const uint32_t* holes_in;
@@ -281,7 +294,7 @@ struct FinalizeArgs {
   const int64_t* stage_src;
   const uint32_t* pos;
   const unsigned long long* ew;
-  uint32_t H;
+  WorldState* state;        // committed: the build's poolUsed and hole count
   uint32_t* grid;
   uint32_t* pool32;
   uint32_t pool_cap;
