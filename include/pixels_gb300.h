@@ -193,15 +193,23 @@ typedef struct px_edit_result {
   uint32_t status;     /* PX_OK, or PX_E_OOM when the edit cannot fit the pool budget */
   uint32_t batch;      /* build step that applied it */
   double arrival_s, start_s, done_s;  /* seconds since the run started */
+  double dev_start_ms, dev_end_ms;    /* its build step's first and last kernel on the device,
+                                         ms since the run started on the device */
 } px_edit_result;
 /* Serve `n` edits arriving at arrival_s[i] (seconds from now): a producer
    releases them in real time; each build step takes every released edit, in
    arrival order, up to max_batch, whose worst-case pool growth (bricks in its
-   box) fits pool_budget_bricks minus the live bricks, and builds them together
-   on the resident world.  Before the first edit the pool is reserved to
-   min(pool_budget_bricks, max(used + 98304, 2 used)) bricks (GpuWorld.ts:57).  applied_order (n entries, may be NULL) receives the
-   edit indices in the order applied.  Blocks until every edit is applied or
-   rejected. */
+   box) fits pool_budget_bricks minus the live bricks (and the steps still in
+   flight), and builds them together on the resident world.  Steps overlap on
+   the device: a step's evaluation passes (classify, sub-block, voxel, paint:
+   independent of the world's state) run on `stream` while the previous step's
+   apply pass, allocator replay and commit run on a second stream; steps commit
+   in admission order, so the world equals the edits applied one after another
+   (shapes.ts:423-426).  Before the first edit the pool is reserved to
+   min(pool_budget_bricks, max(used + 98304, 2 used)) bricks (GpuWorld.ts:57).
+   applied_order (n entries, may be NULL) receives the edit indices in the
+   order applied.  Blocks until every edit is applied or rejected; a step that
+   fails (PX_E_QUEUE_OVERFLOW) ends the run with the world as it was before it. */
 int px_serve_run(px_world* w, const px_edit* edits, const double* arrival_s, size_t n, uint32_t max_batch,
                  uint64_t pool_budget_bricks, int mode, void* stream, px_edit_result* results,
                  uint64_t* applied_order, size_t* n_applied);

@@ -49,7 +49,8 @@ class Edit(ctypes.Structure):
 
 class EditResult(ctypes.Structure):
     _fields_ = [("id", ctypes.c_uint64), ("status", ctypes.c_uint32), ("batch", ctypes.c_uint32),
-                ("arrival_s", ctypes.c_double), ("start_s", ctypes.c_double), ("done_s", ctypes.c_double)]
+                ("arrival_s", ctypes.c_double), ("start_s", ctypes.c_double), ("done_s", ctypes.c_double),
+                ("dev_start_ms", ctypes.c_double), ("dev_end_ms", ctypes.c_double)]
 
 
 class Stats(ctypes.Structure):
@@ -241,9 +242,10 @@ def serve_run(h, edits, arrivals, max_batch: int, pool_budget: int, mode: int, s
     n_app = ctypes.c_size_t()
     _check(h, load().px_serve_run(h, arr, t, n, max_batch, pool_budget, mode, ctypes.c_void_p(stream), res, order,
                                   ctypes.byref(n_app)))
-    out = np.array([(r.id, r.status, r.batch, r.arrival_s, r.start_s, r.done_s) for r in res[:n]],
+    out = np.array([(r.id, r.status, r.batch, r.arrival_s, r.start_s, r.done_s, r.dev_start_ms, r.dev_end_ms)
+                    for r in res[:n]],
                    dtype=[("id", "u8"), ("status", "u4"), ("batch", "u4"), ("arrival_s", "f8"), ("start_s", "f8"),
-                          ("done_s", "f8")])
+                          ("done_s", "f8"), ("dev_start_ms", "f8"), ("dev_end_ms", "f8")])
     return out, np.array(order[:n_app.value], dtype=np.int64)
 
 

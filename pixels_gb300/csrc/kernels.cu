@@ -1320,7 +1320,8 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
   }
 }
 
-void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEvent_t mid, int max_blocks) {
+void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEvent_t mid, int max_blocks,
+                 cudaStream_t s_apply, cudaEvent_t eval_done) {
   auto grid = [&](int per_sm) { return max_blocks > 0 && max_blocks < n_sms * per_sm ? max_blocks : n_sms * per_sm; };
   if (mode == 1) {
     launch_pdl(classify_kernel<1>, dim3(grid(PX_CLASSIFY_MINB)), dim3(256), 0, s, a);
@@ -1339,6 +1340,11 @@ void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEve
     else launch_pdl(paint_kernel<0>, dim3(grid(4)), dim3(256), 0, s, a);
   }
   if (mid) cudaEventRecord(mid, s);
+  if (s_apply != s) {  // the apply pass waits for these passes on its own stream
+    cudaEventRecord(eval_done, s);
+    cudaStreamWaitEvent(s_apply, eval_done, 0);
+    s = s_apply;
+  }
   {
     const uint32_t n_words = (uint32_t)(((size_t)a.BX * a.BY * a.BZ + 31) / 32);
     const uint32_t blocks = (n_words + 255) / 256;  // 8 warps per block, 32 words per warp

@@ -145,6 +145,10 @@ struct px_world {
   bool in_flight = false;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev_fold0 = nullptr, ev_fold1 = nullptr, ev_mid = nullptr;
+  cudaEvent_t ev_eval = nullptr;   // evaluation passes done (the apply stream waits for it)
+  cudaEvent_t ev_done = nullptr;   // the build's result block is on the host
+  cudaStream_t apply_stream = nullptr;  // pipelined builds: the apply pass's stream (nullptr: the build's)
+  bool no_retry = false;           // pipelined builds: a failed build is reported, not retried
   size_t last_P = 0;
   uint32_t last_stage_cap = 0, last_touched_cap = 0;
   int last_mode = 0;
@@ -484,6 +488,8 @@ static int world_create_impl(int dx, int dy, int dz, double vpm, uint32_t initia
   cudaEventCreate(&w->ev_fold0);
   cudaEventCreate(&w->ev_fold1);
   cudaEventCreate(&w->ev_mid);
+  cudaEventCreateWithFlags(&w->ev_eval, cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&w->ev_done, cudaEventDisableTiming);
   // material tables (VoxelWorld.ts:159-170,190-196): filled by px_set_tables or the defaults
   uint8_t op_tab[256], ud_tab[256];
   for (int i = 0; i < 256; i++) { op_tab[i] = i ? 1 : 0; ud_tab[i] = 255; }
@@ -529,6 +535,8 @@ void px_world_destroy(px_world* w) {
   if (w->ev_fold0) cudaEventDestroy(w->ev_fold0);
   if (w->ev_fold1) cudaEventDestroy(w->ev_fold1);
   if (w->ev_mid) cudaEventDestroy(w->ev_mid);
+  if (w->ev_eval) cudaEventDestroy(w->ev_eval);
+  if (w->ev_done) cudaEventDestroy(w->ev_done);
   delete w;
 }
 
@@ -1029,6 +1037,103 @@ int reserve_build_scratch(px_world* w, uint64_t P, uint32_t max_ops) {
   return ensure(w, w->holes_b, 4 * E_max + 4);
 }
 uint64_t build_stage_slots(const px_world* w, uint64_t P) { return stage_slots(w, P); }
+
+#ifndef PIPELINE_PAIRS_PER_BLOCK
+#define PIPELINE_PAIRS_PER_BLOCK 64
+#endif
+
+px_world* twin_create(px_world* w, uint64_t P, uint32_t max_ops, int* rc) {
+  *rc = PX_OK;
+  px_world* t = new px_world();
+  t->dx = w->dx; t->dy = w->dy; t->dz = w->dz;
+  t->BX = w->BX; t->BY = w->BY; t->BZ = w->BZ; t->TX = w->TX; t->TY = w->TY; t->TZ = w->TZ;
+  t->vpm = w->vpm; t->vs = w->vs; t->ncells = w->ncells; t->ntiles = w->ntiles; t->n_sms = w->n_sms;
+  for (int k = 0; k < VCLASSES; k++) t->class_order[k] = w->class_order[k];
+  for (int k = 0; k < VQ_CLASSES; k++) t->vclass_order[k] = w->vclass_order[k];
+  t->host_reads = w->host_reads;
+  t->validate = w->validate;
+  t->rescue_cap = w->rescue_cap;
+  t->stage_hint = w->stage_hint;
+  t->pairs_per_block = PIPELINE_PAIRS_PER_BLOCK;
+  // the shared world: grid, pool, opaque counts, device state, free lists, material tables
+  t->shares_state = true;
+  t->d_grid = w->d_grid; t->d_pool32 = w->d_pool32; t->d_pcount = w->d_pcount; t->d_state = w->d_state;
+  t->pool_cap = w->pool_cap;
+  t->pool_used = w->pool_used; t->n_holes = w->n_holes; t->holes_in_a = w->holes_in_a;
+  t->pcount_valid = w->pcount_valid;
+  auto borrow = [](DevBuf& dst, const DevBuf& src) { dst = src; dst.borrowed = true; };
+  borrow(t->holes_a, w->holes_a);
+  borrow(t->holes_b, w->holes_b);
+  borrow(t->opaque, w->opaque);
+  borrow(t->udens, w->udens);
+  if (cudaMallocHost((void**)&t->h_res, sizeof(BuildResult)) != cudaSuccess) {
+    cudaGetLastError();
+    delete t;
+    *rc = PX_E_OOM;
+    return nullptr;
+  }
+  cudaEventCreate(&t->ev0);
+  cudaEventCreate(&t->ev1);
+  cudaEventCreate(&t->ev_fold0);
+  cudaEventCreate(&t->ev_fold1);
+  cudaEventCreate(&t->ev_mid);
+  cudaEventCreateWithFlags(&t->ev_eval, cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&t->ev_done, cudaEventDisableTiming);
+  *rc = reserve_build_scratch(t, P, max_ops);  // its own scratch; the shared buffers are already sized
+  if (*rc != PX_OK) {
+    twin_destroy(t);
+    return nullptr;
+  }
+  return t;
+}
+
+void twin_destroy(px_world* t) { px_world_destroy(t); }
+
+void pipeline_set(px_world* w, cudaStream_t apply, bool holes_in_a, uint32_t pool_used_bound, uint32_t n_holes_bound) {
+  w->apply_stream = apply;
+  w->no_retry = apply != nullptr;
+  w->holes_in_a = holes_in_a;
+  w->pool_used = pool_used_bound;
+  w->n_holes = n_holes_bound;
+}
+
+PipelineState pipeline_begin(px_world* w) {
+  PipelineState st{w->pool_used, w->n_holes, w->holes_in_a, w->derive_max, w->pairs_per_block};
+  w->derive_max = 0;
+  // two builds share the GPU: persistent grids sized to each build's pairs
+  // (a few edits need a few blocks, not the whole GPU)
+  w->pairs_per_block = PIPELINE_PAIRS_PER_BLOCK;
+  return st;
+}
+
+void pipeline_end(px_world* w, const PipelineState& st, uint64_t ops, cudaStream_t s) {
+  w->apply_stream = nullptr;
+  w->stream = s;
+  w->no_retry = false;
+  w->pool_used = st.pool_used;
+  w->n_holes = st.n_holes;
+  w->holes_in_a = st.holes_in_a;
+  w->derive_max = st.derive_max;
+  w->pairs_per_block = st.pairs_per_block;
+  w->ops_applied += ops;
+  w->stats.ops_applied = w->ops_applied;
+  w->stats.pool_used = st.pool_used;
+  w->stats.n_holes = st.n_holes;
+  w->derived_valid = false;
+  w->free_valid = false;
+  cudaMemsetAsync(&w->d_state->poisoned, 0, 4, s);  // a failed build left the world as it was
+  cudaStreamSynchronize(s);
+}
+
+bool build_done(px_world* w) { return !w->in_flight || cudaEventQuery(w->ev_done) == cudaSuccess; }
+
+void build_times(px_world* w, cudaEvent_t base, double* start_ms, double* end_ms) {
+  float a = 0.f, b = 0.f;
+  cudaEventElapsedTime(&a, base, w->ev0);
+  cudaEventElapsedTime(&b, base, w->ev1);
+  *start_ms = a;
+  *end_ms = b;
+}
 }  // namespace px
 
 extern "C" {
@@ -1206,7 +1311,9 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   if (w->in_flight) return fail(w, PX_E_INVALID_ARG, "a build is already in flight");
   if (mode != PX_MODE_FP64 && mode != PX_MODE_MIXED) return fail(w, PX_E_INVALID_ARG, "unknown mode %d", mode);
   cudaStream_t s = (cudaStream_t)stream;
-  w->stream = s;
+  // the apply pass and everything after it: on the apply stream when pipelined
+  cudaStream_t sa = w->apply_stream && !w->capturing ? w->apply_stream : s;
+  w->stream = sa;
   const int n_ops = (int)w->ops.size();
   int rc;
 
@@ -1238,16 +1345,15 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
     if (n_slots * 2048 <= (512ull << 20)) break;
   }
   const uint64_t touched_bound = P < w->ncells ? P : w->ncells;
-  // the host's view of the allocator state (exact unless builds are pipelined,
-  // where the replay reads it from the device and these only bound sizes)
+  // the host's view of the allocator state: exact, or for pipelined builds
+  // (whose replay reads it from the device) upper bounds that size the buffers
   const uint32_t H = w->n_holes, U0 = w->pool_used;
-  size_t E_max = (size_t)std::max(H, w->pool_cap) + 2 * P;
+  const size_t E_max = (size_t)H + 2 * P;
 
   // staging slots and pool bricks are reserved from a guess; a build that needs
   // more commits nothing and is retried with larger buffers (px_build_finish)
   const uint64_t stage_cap = stage_slots(w, P);
   if ((rc = grow_pool(w, (uint64_t)U0 + stage_cap, U0, s))) return rc;
-  E_max = (size_t)std::max(H, w->pool_cap) + 2 * P;
 
   // scratch (a reallocated op table loses its resident copy)
   const void* op_bufs_before[9] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p,
@@ -1262,7 +1368,7 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
       (rc = ensure_pair_scratch(w, P, tile_pairs, n_slots, touched_bound, E_max, stage_cap)))
     return rc;
   const size_t scan_nb = scan_blocks(w, P, E_max);
-  const uint32_t H_max = std::max(H, w->pool_cap);  // holes are pool bricks
+  const uint32_t H_max = H;
   {
     const void* after[9] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p,
                             w->d_p32.p, w->d_bases.p, w->chunk_op.p, w->chunk_op.p};
@@ -1457,7 +1563,8 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   int max_blocks = 0;  // persistent grids sized to the build (batched builds share the GPU)
   if (w->pairs_per_block) max_blocks = (int)std::max<uint64_t>(1, (P + w->pairs_per_block - 1) / w->pairs_per_block);
   if (!w->capturing) CU(cudaEventRecord(w->ev_fold0, s));
-  launch_fold(fa, mode, w->n_sms, s, w->capturing ? nullptr : w->ev_mid, max_blocks);
+  launch_fold(fa, mode, w->n_sms, s, w->capturing ? nullptr : w->ev_mid, max_blocks, sa, w->ev_eval);
+  s = sa;  // the rest of the build follows the apply pass
   if (!w->capturing) CU(cudaEventRecord(w->ev_fold1, s));
 
   ReplayArgs ra{};
@@ -1500,6 +1607,7 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   w->stats.kernel_launches = (uint32_t)(launch_count() - launches0);
   if (!w->capturing) CU(cudaEventRecord(w->ev1, s));
   CU(cudaMemcpyAsync(w->h_res, res, sizeof(BuildResult), cudaMemcpyDeviceToHost, s));
+  if (!w->capturing) CU(cudaEventRecord(w->ev_done, s));
   w->in_flight = true;
   w->last_P = P;
   w->last_stage_cap = (uint32_t)stage_cap;
@@ -1546,7 +1654,7 @@ static int build_finish_impl(px_world* w) {
   if (!w) return PX_E_INVALID_ARG;
   if (!w->in_flight) return PX_OK;
   w->in_flight = false;
-  CU(cudaStreamSynchronize(w->stream));
+  CU(cudaEventSynchronize(w->ev_done));  // the result block (later work on the stream may still run)
   w->uploads_pending = false;
   const BuildResult& r = *w->h_res;
   float ms = 0.f, fold_ms = 0.f;
@@ -1561,6 +1669,10 @@ static int build_finish_impl(px_world* w) {
   // transactional retries: nothing was committed
   // a build that commits nothing poisons the device state (WorldState); retries clear it
   auto clear_poison = [&] { return cudaMemsetAsync(&w->d_state->poisoned, 0, 4, w->stream); };
+  if (w->no_retry && (r.status & (ST_NO_COMMIT | ST_POOL_OVERFLOW))) {  // pipelined: later builds are queued
+    w->retries = 0;
+    return fail(w, PX_E_QUEUE_OVERFLOW, "pipelined build failed: device status 0x%x", r.status);
+  }
   if ((r.status & ST_RESCUE_OVERFLOW) && w->retries < 2) {  // more voxels left to float64 than the list holds
     CU(clear_poison());
     w->rescue_cap = std::max(w->rescue_cap, r.n_rescue + r.n_rescue / 4 + 1024);
@@ -1599,6 +1711,7 @@ static int build_finish_impl(px_world* w) {
     }
     CU(cudaGetLastError());
     CU(cudaMemcpyAsync(w->h_res, dres, sizeof(BuildResult), cudaMemcpyDeviceToHost, w->stream));
+    CU(cudaEventRecord(w->ev_done, w->stream));
     w->in_flight = true;
     rc = px_build_finish(w);
     w->retries = 0;

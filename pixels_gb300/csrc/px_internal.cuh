@@ -243,7 +243,10 @@ void launch_cull_count(const uint2* boxes, int n_ops, int TX, int TY, int TZ, ui
 void launch_cull_fill(const uint2* boxes, int n_ops, int TX, int TY, int TZ, const uint32_t* tile_off,
                       uint32_t* tile_ops, uint2* tile_boxes, cudaStream_t s);
 // max_blocks > 0 caps the persistent grids (builds sharing the GPU)
-void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEvent_t mid, int max_blocks);
+// The evaluation passes (classify .. paint) go on s; the apply pass on s_apply,
+// after eval_done is recorded on s (s_apply == s: one stream, no event).
+void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEvent_t mid, int max_blocks,
+                 cudaStream_t s_apply, cudaEvent_t eval_done);
 
 // Scratch of the single-pass scans (scan_temp_bytes(max_blocks) bytes): the
 // tiles' aggregates and inclusive prefixes, then SCAN_REGIONS regions of a tile
@@ -371,5 +374,32 @@ namespace px {
 // reserves.
 int reserve_build_scratch(px_world* w, uint64_t P, uint32_t max_ops);
 uint64_t build_stage_slots(const px_world* w, uint64_t P);
+// Pipelined builds (serving): a twin of a world over the same grid, pool,
+// opaque counts, free list and device state, with build scratch of its own,
+// so that one build's evaluation passes can run on the device while the
+// other's apply pass does.  Builds on either commit to the shared world in the
+// order their apply passes are queued on the apply stream.
+px_world* twin_create(px_world* w, uint64_t P, uint32_t max_ops, int* rc);
+void twin_destroy(px_world* t);
+// Queue settings of a pipelined world: the apply pass on `apply` (NULL: the
+// build's stream), no retries, and the host's view of the shared allocator
+// state before the build (holes parity, bounds of poolUsed and the hole count).
+void pipeline_set(px_world* w, cudaStream_t apply, bool holes_in_a, uint32_t pool_used_bound, uint32_t n_holes_bound);
+// The committed allocator state a pipeline starts from (and ends with).
+struct PipelineState {
+  uint32_t pool_used, n_holes;
+  bool holes_in_a;
+  uint32_t derive_max;  // the world's derive-on-build setting, off while pipelined
+  uint32_t pairs_per_block;  // the world's persistent-grid sizing, restored after the pipeline
+};
+PipelineState pipeline_begin(px_world* w);
+// After the last pipelined build: the world takes over the committed state,
+// counts `ops` more ops applied, clears a poisoned device state and restores
+// derive on build.
+void pipeline_end(px_world* w, const PipelineState& st, uint64_t ops, cudaStream_t s);
+// The build's result block is on the host (px_build_finish would not wait).
+bool build_done(px_world* w);
+// Device times (ms since `base`) of the last finished build's first and last kernels.
+void build_times(px_world* w, cudaEvent_t base, double* start_ms, double* end_ms);
 
 }  // namespace px

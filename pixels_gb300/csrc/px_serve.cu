@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <atomic>
 #include <condition_variable>
 #include <cstring>
 #include <functional>
@@ -104,7 +105,6 @@ static int serve_run_impl(px_world* w, const px_edit* edits, const double* arriv
   const double vs = 1 / vpm;
   px_stats st;
   px_get_stats(w, &st);
-  uint64_t live = (uint64_t)st.pool_used - st.n_holes;
   {  // the pool the serving loop works in, allocated before the clock starts (GpuWorld.ts:57)
     const uint64_t used = st.pool_used;
     uint64_t cap = std::max<uint64_t>(used + 98304, 2 * used);
@@ -141,43 +141,124 @@ static int serve_run_impl(px_world* w, const px_edit* edits, const double* arriv
     results[i].batch = 0;
     results[i].arrival_s = arrival_s[i];
     results[i].start_s = results[i].done_s = -1;
+    results[i].dev_start_ms = results[i].dev_end_ms = -1;
   }
+
+  // Two world objects over the one resident world (the twin has build scratch
+  // of its own), builds alternating between them: a step's evaluation passes
+  // run on s_eval while the previous step's apply pass runs on s_apply.
+  int trc = PX_OK;
+  px_world* twin = twin_create(w, pair_budget, max_batch, &trc);
+  if (!twin) return trc;
+  cudaStream_t s_eval = (cudaStream_t)stream, s_apply = nullptr;
+  cudaEvent_t base = nullptr;
+  if (cudaStreamCreateWithFlags(&s_apply, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&base) != cudaSuccess) {
+    cudaGetLastError();
+    if (s_apply) cudaStreamDestroy(s_apply);
+    twin_destroy(twin);
+    return PX_E_CUDA;
+  }
+  cudaEventRecord(base, s_eval);
+  px_world* W[2] = {w, twin};
+  PipelineState committed = pipeline_begin(w);  // the allocator state of the last finished step
 
   // producer: releases requests at their arrival times
   std::mutex mu;
   std::condition_variable cv;
-  size_t released = 0;
-  bool stop = false;
+  std::atomic<size_t> released{0};
+  std::atomic<bool> stop{false};
   const auto t0 = clock_t_::now();
   std::thread producer([&] {
     for (size_t k = 0; k < n; k++) {
       const double t = arrival_s[order[k]];
       std::this_thread::sleep_until(t0 + std::chrono::duration_cast<clock_t_::duration>(std::chrono::duration<double>(t)));
+      if (stop.load()) return;
       {
         std::lock_guard<std::mutex> g(mu);
-        released = k + 1;
-        if (stop) return;
+        released.store(k + 1);
       }
       cv.notify_one();
     }
   });
 
+  struct Step {
+    std::vector<size_t> edits;
+    uint64_t bound;       // the most pool bricks it can add
+    int world;            // W index
+    double start;
+    uint32_t id;
+    size_t n_ops;
+  };
+  std::vector<Step> flight;  // at most two steps in flight, oldest first
   size_t next = 0, applied = 0;
   uint32_t batch_id = 0;
+  uint64_t ops_done = 0;
+  bool parity = committed.holes_in_a;  // holes buffer the next queued step reads
   int rc = PX_OK;
   std::vector<IrOp> ops;
   std::vector<uint32_t> code;
   std::vector<double> params;
-  std::vector<size_t> batch;
-  while (next < n && rc == PX_OK) {
-    size_t avail;
-    {
-      std::unique_lock<std::mutex> g(mu);
-      cv.wait(g, [&] { return released > next; });
-      avail = released;
+  std::vector<unsigned char> ir;
+
+  auto finish_oldest = [&]() {
+    Step stp = std::move(flight.front());
+    flight.erase(flight.begin());
+    px_world* x = W[stp.world];
+    const int brc = px_build_finish(x);
+    const double done = secs(t0, clock_t_::now());
+    double d0 = -1, d1 = -1;
+    build_times(x, base, &d0, &d1);
+    if (brc == PX_OK && rc == PX_OK) {
+      px_stats xs;
+      px_get_stats(x, &xs);
+      committed.pool_used = xs.pool_used;
+      committed.n_holes = xs.n_holes;
+      committed.holes_in_a = !committed.holes_in_a;  // the step wrote the other holes buffer
+      ops_done += stp.n_ops;
+    } else if (rc == PX_OK) {
+      rc = brc;  // later queued steps commit nothing (the device state is poisoned)
     }
-    // admit in arrival order while the free pool holds the worst case
-    batch.clear();
+    for (size_t i : stp.edits) {
+      results[i].start_s = stp.start;
+      results[i].done_s = done;
+      results[i].dev_start_ms = d0;
+      results[i].dev_end_ms = d1;
+      results[i].batch = stp.id;
+      results[i].status = (uint32_t)(rc == PX_OK ? PX_OK : PX_E_QUEUE_OVERFLOW);
+      if (rc == PX_OK) {
+        if (applied_order) applied_order[applied] = i;
+        applied++;
+      }
+    }
+  };
+
+  while ((next < n && rc == PX_OK) || !flight.empty()) {
+    if (flight.size() == 2 || rc != PX_OK) {  // both world objects busy (or draining after a failure)
+      finish_oldest();
+      continue;
+    }
+    if (flight.empty() && released.load() <= next && next < n) {  // idle: sleep until a request arrives
+      std::unique_lock<std::mutex> g(mu);
+      cv.wait(g, [&] { return released.load() > next; });
+    }
+    const size_t avail = released.load();
+    if (next >= n) {
+      finish_oldest();
+      continue;
+    }
+    if (avail <= next) {  // nothing new: the step in flight finishes unless a request arrives first
+      if (build_done(W[flight.front().world])) finish_oldest();
+      else std::this_thread::yield();
+      continue;
+    }
+    // admit in arrival order while the free pool holds the worst case of this
+    // step and of the step still in flight
+    uint64_t in_flight = 0;
+    for (const Step& f : flight) in_flight += f.bound;
+    const uint64_t live = (uint64_t)committed.pool_used - committed.n_holes;
+    const uint64_t used_bound = (uint64_t)committed.pool_used + in_flight;
+    std::vector<size_t> batch;
     ops.clear();
     code.clear();
     params.clear();
@@ -185,55 +266,58 @@ static int serve_run_impl(px_world* w, const px_edit* edits, const double* arriv
     while (next < avail && batch.size() < max_batch) {
       const size_t i = order[next];
       const uint64_t b = brick_bound(edits[i], vs, dims[0], dims[1], dims[2]);
-      if (live + bound + b > pool_budget_bricks) {
-        if (batch.empty()) {  // cannot fit even alone: reject
+      const bool fits = live + in_flight + bound + b <= pool_budget_bricks &&
+                        used_bound + build_stage_slots(w, bound + b) <= pool_cap && bound + b <= pair_budget;
+      if (!fits) {
+        if (batch.empty() && flight.empty()) {  // cannot fit even alone on an idle world: reject
           results[i].status = PX_E_OOM;
           results[i].done_s = secs(t0, clock_t_::now());
           next++;
           continue;
         }
-        break;  // wait for the next batch
+        break;  // wait for the next step (or for the step in flight to commit)
       }
-      // the batch stays within the reserved scratch and pool room (an edit too
-      // large for them is built alone, growing the buffers)
-      if (!batch.empty() && (bound + b > pair_budget ||
-                             (uint64_t)st.pool_used + build_stage_slots(w, bound + b) > pool_cap))
-        break;
       bound += b;
       batch.push_back(i);
       encode_carve(edits[i], vs, ops, code, params);
       next++;
     }
-    if (batch.empty()) continue;
+    if (batch.empty()) {
+      if (!flight.empty()) finish_oldest();
+      continue;
+    }
     const double start = secs(t0, clock_t_::now());
-    // PXIR buffer
-    std::vector<unsigned char> ir(32 + ops.size() * sizeof(IrOp) + code.size() * 4 + params.size() * 8);
+    ir.assign(32 + ops.size() * sizeof(IrOp) + code.size() * 4 + params.size() * 8, 0);
     uint32_t hdr[8] = {0x52495850u, 1u, (uint32_t)ops.size(), (uint32_t)(code.size() / 2), (uint32_t)params.size(), 0, 0, 0};
     std::memcpy(ir.data(), hdr, 32);
     std::memcpy(ir.data() + 32, ops.data(), ops.size() * sizeof(IrOp));
     std::memcpy(ir.data() + 32 + ops.size() * sizeof(IrOp), code.data(), code.size() * 4);
     std::memcpy(ir.data() + 32 + ops.size() * sizeof(IrOp) + code.size() * 4, params.data(), params.size() * 8);
-    rc = px_submit_ops(w, ir.data(), ir.size());
-    if (rc == PX_OK) rc = px_build(w, mode, stream);
-    const double done = secs(t0, clock_t_::now());
-    px_get_stats(w, &st);
-    live = (uint64_t)st.pool_used - st.n_holes;
-    pool_cap = st.pool_capacity;
-    for (size_t i : batch) {
-      results[i].start_s = start;
-      results[i].done_s = done;
-      results[i].batch = batch_id;
-      results[i].status = (uint32_t)rc;
-      if (applied_order && rc == PX_OK) applied_order[applied] = i;
-      if (rc == PX_OK) applied++;
+    const int wi = (int)(batch_id & 1u);
+    px_world* x = W[wi];
+    pipeline_set(x, s_apply, parity, (uint32_t)std::min<uint64_t>(used_bound, pool_cap),
+                 (uint32_t)std::min<uint64_t>((uint64_t)committed.n_holes + in_flight, pool_cap));
+    int erc = px_submit_ops(x, ir.data(), ir.size());
+    if (erc == PX_OK) erc = px_build_enqueue(x, mode, s_eval);
+    if (erc != PX_OK) {
+      rc = erc;
+      for (size_t i : batch) {
+        results[i].status = (uint32_t)erc;
+        results[i].done_s = secs(t0, clock_t_::now());
+      }
+      continue;
     }
+    parity = !parity;
+    flight.push_back(Step{std::move(batch), bound, wi, start, batch_id, ops.size()});
     batch_id++;
   }
-  {
-    std::lock_guard<std::mutex> g(mu);
-    stop = true;
-  }
+  stop.store(true);
   producer.join();
+  cudaStreamSynchronize(s_apply);
+  pipeline_end(w, committed, ops_done, s_eval);
+  twin_destroy(twin);
+  cudaStreamDestroy(s_apply);
+  cudaEventDestroy(base);
   if (n_applied) *n_applied = applied;
   return rc;
 }

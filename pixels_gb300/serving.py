@@ -68,6 +68,22 @@ def serve(world, edits, arrivals, max_batch: int = 256, pool_budget: int | None 
     return _lib.serve_run(world._h, edits, arrivals, max_batch, pool_budget, world.mode, stream)
 
 
+def step_overlap(results) -> float | None:
+    """Fraction of consecutive build steps whose device work overlapped: the
+    next step's first kernel started before the previous step's last ended."""
+    ok = results[results["status"] == 0]
+    if len(ok) == 0:
+        return None
+    steps = {}
+    for b, s0, s1 in zip(ok["batch"], ok["dev_start_ms"], ok["dev_end_ms"]):
+        steps[int(b)] = (float(s0), float(s1))
+    ids = sorted(steps)
+    pairs = list(zip(ids, ids[1:]))
+    if not pairs:
+        return None
+    return sum(steps[b][0] < steps[a][1] for a, b in pairs) / len(pairs)
+
+
 def latency_stats(results) -> dict:
     ok = results[results["status"] == 0]
     lat = (ok["done_s"] - ok["arrival_s"]) * 1e3
@@ -81,4 +97,5 @@ def latency_stats(results) -> dict:
         "batches": int(len(np.unique(ok["batch"]))) if len(ok) else 0,
         "max_step_ms": float(((ok["done_s"] - ok["start_s"]) * 1e3).max()) if len(ok) else None,
         "mean_batch": float(len(ok) / max(len(np.unique(ok["batch"])), 1)) if len(ok) else 0.0,
+        "steps_overlapping_on_device": step_overlap(results),
     }

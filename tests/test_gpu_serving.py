@@ -87,6 +87,28 @@ def test_resident_synthetic_vpm160_after_served_stream_matches_oracle(built_lib)
 
 
 @pytest.mark.gpu
+def test_steps_overlap_on_the_device_and_commit_in_order(built_lib):
+    """256 edits arriving together, at most 16 per step: while one step's apply
+    pass runs, the next step's evaluation passes run on another stream.  The
+    device timestamps of consecutive steps overlap, and the world still equals
+    the oracle's build followed by the carves in the order applied."""
+    vpm = 40.0
+    cfg = config.Config(vpm)
+    prog, _ = penthouse_program(vpm)
+    w = resident(vpm, prog)
+    edits, _ = serving.edit_stream(w.grid, cfg.bricks, vpm, 256, rate=0, seed=11)
+    res, order = serving.serve(w, edits, np.zeros(len(edits)), max_batch=16)
+    assert (res["status"] == 0).all() and len(order) == len(edits)
+    assert len(np.unique(res["batch"])) >= 16
+    assert (res["dev_end_ms"] > res["dev_start_ms"]).all()
+    frac = serving.step_overlap(res)
+    assert frac is not None and frac > 0.5, frac
+    prog2, _ = penthouse_program(vpm)
+    o = pyoracle.OracleWorld(_concat_ir(prog2, serving.carve_program(edits, order, vpm)), vpm, cfg.dims)
+    assert_same_world(w, o)
+
+
+@pytest.mark.gpu
 def test_poisson_stream_latency(built_lib):
     vpm = 40.0
     prog, _ = penthouse_program(vpm)
