@@ -769,7 +769,7 @@ __global__ void __launch_bounds__(256, PX_VSIMPLE_MINB) voxel_simple_kernel(Fold
     const uint32_t sp = V->simple;
     const uint32_t prim = sp & 0xffu, rot = (sp >> 8) & 0xffu;
     const float M = V->thr[T_M];
-    bool amb = false;
+    bool amb0 = false, amb1 = false;  // a polygon crossing test the interval could not settle, per voxel
     Iv2 d = {{0.f, 0.f}, {0.f, 0.f}};
     if (lip0 == 3 || lip1 == 3 || VALIDATE) {
       const uint32_t* c32 = a.code32 + V->code_off;
@@ -783,14 +783,17 @@ __global__ void __launch_bounds__(256, PX_VSIMPLE_MINB) voxel_simple_kernel(Fold
           Iv yd = y0;
           rot32(rot, P + __ldg(c32), x, yd, z);
         }
+        bool amb = false;  // the column's polygon work is shared by both voxels
         d = prim32_y2(prim, cnt, pr, x, y0, y1, z, M, amb);
+        amb0 = amb1 = amb;
       } else {
 #pragma unroll 1
         for (int q = 0; q < 2; q++) {
           Iv xx = x, yy = q ? y1 : y0, zz = z;
           if (rot) rot32(rot, P + __ldg(c32), xx, yy, zz);
-          const Iv v = prim32(prim, cnt, pr, xx, yy, zz, M, amb);
-          if (q) d.b = v; else d.a = v;
+          bool ambq = false;  // each voxel's own crossing tests
+          const Iv v = prim32(prim, cnt, pr, xx, yy, zz, M, ambq);
+          if (q) { d.b = v; amb1 = ambq; } else { d.a = v; amb0 = ambq; }
         }
       }
       if (sp >> 16) {  // offset (penthouse.ts:250)
@@ -804,6 +807,7 @@ __global__ void __launch_bounds__(256, PX_VSIMPLE_MINB) voxel_simple_kernel(Fold
 #pragma unroll
     for (int q = 0; q < 2; q++) {
       const Iv dk = q ? d.b : d.a;
+      const bool amb = q ? amb1 : amb0;
       const int lipk = q ? lip1 : lip0;
       const int bit = (col & 3) | ((2 * yh + q) << 2) | ((col >> 2) << 4);  // voxel index in the sub-block
       int inside = lipk;
