@@ -17,6 +17,7 @@
 //   finalize  staging -> pool at the replayed indices (16-byte vector copies),
 //             grid entries.
 //   derive    super-grid counts and density bytes (GpuWorld.ts:90-101).
+#include <algorithm>
 #include <cstdio>
 #include "px_internal.cuh"
 #include "sdf64.cuh"
@@ -1392,11 +1393,6 @@ struct DepthOp {
   __device__ static T identity() { return make_int2(0, -(1 << 30)); }
   __device__ static T combine(T x, T y) { return make_int2(x.x + y.x, max(y.y, x.y + y.x)); }
 };
-struct MinOp {
-  typedef int32_t T;
-  __device__ static T identity() { return 0x7fffffff; }
-  __device__ static T combine(T a, T b) { return min(a, b); }
-};
 
 // Exclusive scan of one value per thread across the block; returns the
 // thread's exclusive prefix and the block total.
@@ -1587,67 +1583,138 @@ void launch_scan_u32(const uint32_t* in, uint32_t* out, size_t n, const uint32_t
 
 // ---------------------------------------------------------------------------
 // replay of the LIFO pool allocator (VoxelWorld.ts:112-127) over the build's
-// alloc/free events in (op, cell) order.
+// alloc/free events in (op, cell) order -- the order of the reference's loop --
+// in three kernels:
+//   scan_events   the event positions of the (op, brick) pairs (a single-pass
+//                 scan of their event counts) and the events themselves: a pop
+//                 per allocation, a push per free, the H holes before the build
+//                 as the first pushes;
+//   depth_scan    the stack depth after each event (a clamped prefix scan: a
+//                 pop that finds the stack empty takes poolUsed++ instead), the
+//                 rank of those fresh allocations (a second look-back, chained
+//                 after the first) and the min tree over the depths;
+//   match         each event's link towards its pool index: a pop at depth D
+//                 takes the push that last filled slot D (the event after the
+//                 last earlier event of depth < D, found in the min tree); a
+//                 push frees its brick's index, the index of that brick's last
+//                 allocation.  The pushes no later event undercuts are the holes
+//                 after the build;
+//   resolve       the links followed to pool indices (finalize turns the holes'
+//                 event indices into their pool indices).
 
-constexpr unsigned long long KNOWN = 1ull << 63;
-enum : uint8_t { EV_PUSH = 0, EV_POP = 1 };
+constexpr unsigned long long KNOWN = 1ull << 63;    // ew: a resolved pool index
+constexpr unsigned long long PAIRREF = 1ull << 62;  // ew of a push: the pair of its brick's last allocation
+enum : uint8_t { EV_PUSH = 0, EV_POP = 1, EV_NONE = 0xff };
+constexpr int RP_THREADS = 512, RP_ITEMS = 8;
+static_assert(RP_THREADS * RP_ITEMS == REPLAY_TILE, "a tile is one block pass");
 
+// Decoupled look-back of tile `tile`, by warp 0: publishes the tile's
+// aggregate, combines its predecessors' (inclusive prefixes where published,
+// aggregates while those are pending, 32 tiles per step, nearest first) and
+// publishes the tile's inclusive prefix.  Returns the exclusive prefix.
+template <class Op>
+__device__ typename Op::T lookback(uint32_t tile, typename Op::T total, typename Op::T* agg, typename Op::T* incl,
+                                   uint32_t* flags, uint32_t* status) {
+  typedef typename Op::T T;
+  const int lane = threadIdx.x & 31;
+  T prefix = Op::identity();
+  if (tile == 0) {
+    if (lane == 0) scan_publish(incl, flags, total, 2u);
+    return prefix;
+  }
+  if (lane == 0) scan_publish(agg + tile, flags + tile, total, 1u);
+  long long hi = (long long)tile - 1;
+  uint32_t spins = 0;
+  for (;;) {
+    const long long j = hi - 31 + lane;  // lane 31 reads the nearest tile of the window
+    const uint32_t f = j >= 0 ? *(volatile uint32_t*)(flags + j) : 2u;  // before tile 0: the identity
+    if (__any_sync(FULLMASK, f == 0)) {
+      if (++spins > SCAN_SPIN_LIMIT) {  // cannot happen: earlier tiles publish unconditionally
+        if (lane == 0) atomicOr(status, (uint32_t)ST_CHAIN);
+        break;
+      }
+      continue;
+    }
+    __threadfence();
+    T v = j >= 0 ? scan_peek(f == 2 ? incl + j : agg + j) : Op::identity();
+    const uint32_t im = __ballot_sync(FULLMASK, f == 2);
+    if (lane < (im ? 31 - __clz(im) : 0)) v = Op::identity();  // tiles before the nearest prefix
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {  // ordered combination of the window
+      const T y = shfl_up_any(v, o);
+      if (lane >= o) v = Op::combine(y, v);
+    }
+    prefix = Op::combine(shfl_any(v, 31), prefix);
+    if (im) break;
+    hi -= 32;
+  }
+  if (lane == 0) scan_publish(incl + tile, flags + tile, Op::combine(prefix, total), 2u);
+  return prefix;
+}
 
-__global__ void events_build_kernel(ReplayArgs a) {
+__global__ void __launch_bounds__(RP_THREADS) scan_events_kernel(ReplayArgs a) {
   pdl_prologue();
-  const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+  __shared__ uint32_t sh[32];
+  __shared__ uint32_t s_prefix, s_tile;
   const uint32_t H = __ldcg(&a.state->n_holes);  // the committed state: no build writes it until this one commits
-  if (tid == 0) {
-    a.res->n_events = H + (a.P ? a.pos[a.P - 1] + a.cnt[a.P - 1] : 0u);
+  if (threadIdx.x == 0) s_tile = atomicAdd(&a.t.counters[0], 1u);
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  const size_t P = a.P, n_tiles = (P + REPLAY_TILE - 1) / REPLAY_TILE;
+  if (tile == 0 && threadIdx.x == 0) {
     a.res->h_before = H;
     a.res->u_before = __ldcg(&a.state->pool_used);
+    if (P == 0) a.res->n_events = H;
   }
-  for (size_t i = tid; i < H; i += stride) {
+  if (tile < n_tiles) {
+    const size_t k0 = (size_t)tile * REPLAY_TILE + (size_t)threadIdx.x * RP_ITEMS;
+    uint32_t c[RP_ITEMS], acc = 0;
+    if (k0 + RP_ITEMS <= P) {  // 32-byte aligned runs
+      const uint4 u0 = reinterpret_cast<const uint4*>(a.cnt + k0)[0], u1 = reinterpret_cast<const uint4*>(a.cnt + k0)[1];
+      c[0] = u0.x; c[1] = u0.y; c[2] = u0.z; c[3] = u0.w; c[4] = u1.x; c[5] = u1.y; c[6] = u1.z; c[7] = u1.w;
+    } else {
+#pragma unroll
+      for (int j = 0; j < RP_ITEMS; j++) c[j] = k0 + j < P ? a.cnt[k0 + j] : 0u;
+    }
+#pragma unroll
+    for (int j = 0; j < RP_ITEMS; j++) acc += c[j];
+    uint32_t total;
+    const uint32_t pre_block = block_exclusive<SumOp>(acc, sh, total);
+    if (threadIdx.x < 32) {
+      const uint32_t pf = lookback<SumOp>(tile, total, a.t.p_agg, a.t.p_incl, a.t.p_flag, &a.res->status);
+      if (threadIdx.x == 0) s_prefix = pf;
+    }
+    __syncthreads();
+    uint32_t pos = s_prefix + pre_block;
+#pragma unroll
+    for (int j = 0; j < RP_ITEMS; j++) {
+      const size_t k = k0 + j;
+      if (k >= P) break;
+      a.pos[k] = pos;
+      if (c[j]) {
+        const uint32_t ev = a.evt[k];
+        const size_t e0 = (size_t)H + pos;
+        if (ev & 1u) {  // editableBrick -> allocBrick: a pop
+          a.etype[e0] = EV_POP;
+          a.ew[e0] = 0;
+        }
+        if (ev & 2u) {  // setBrickUniform / compactCell: a push of the brick's index
+          const size_t e1 = e0 + (ev & 1u);
+          const long long src = a.fsrc[k];
+          a.etype[e1] = EV_PUSH;
+          a.ew[e1] = src >= 0 ? PAIRREF | (unsigned long long)src : KNOWN | (unsigned long long)(-(src + 1));
+        }
+      }
+      pos += c[j];
+      if (k == P - 1) a.res->n_events = H + pos;
+    }
+  }
+  // the holes before the build: the first H pushes, known indices (every block takes a share)
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < H; i += (size_t)gridDim.x * blockDim.x) {
     a.etype[i] = EV_PUSH;
-    a.depth_fn[i] = make_int2(1, -(1 << 30));
     a.ew[i] = KNOWN | a.holes_in[i];
   }
-  for (size_t p = tid; p < a.P; p += stride) {
-    const uint32_t e = a.evt[p];
-    if (!e) continue;
-    const size_t base = H + a.pos[p];
-    if (e & 1u) {
-      a.etype[base] = EV_POP;
-      a.depth_fn[base] = make_int2(-1, 0);
-      a.ew[base] = 0;
-    }
-    if (e & 2u) {
-      const size_t k = base + (e & 1u);
-      a.etype[k] = EV_PUSH;
-      a.depth_fn[k] = make_int2(1, -(1 << 30));
-      const long long src = a.fsrc[p];
-      a.ew[k] = src >= 0 ? (unsigned long long)(H + a.pos[src]) : (KNOWN | (unsigned long long)(-(src + 1)));
-    }
-  }
 }
-
-// Stack depth after each event (the scanned maps applied to the empty stack)
-// and the pops that find the stack empty (they take poolUsed++).
-__global__ void depth_fresh_kernel(const int2* __restrict__ fn, const uint8_t* __restrict__ etype, int32_t* depth,
-                                   uint32_t* fresh, const BuildResult* res) {
-  pdl_prologue();
-  const size_t E = res->n_events;
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (size_t)gridDim.x * blockDim.x) {
-    const int2 f = __ldg(fn + e);
-    depth[e] = max(f.y, f.x);  // applied to the empty stack (depth 0)
-    int dprev = 0;
-    if (e) {
-      const int2 g = __ldg(fn + e - 1);
-      dprev = max(g.y, g.x);
-    }
-    fresh[e] = (etype[e] == EV_POP && dprev == 0) ? 1u : 0u;
-  }
-}
-
-struct TreeLevels {
-  size_t off[8];  // offsets (in int32) of levels 1.. in the tree buffer
-  int n;          // levels above the depth array
-};
 
 __device__ __forceinline__ size_t level_size(size_t E, int l) {
   size_t n = E;
@@ -1655,15 +1722,121 @@ __device__ __forceinline__ size_t level_size(size_t E, int l) {
   return n;
 }
 
-// Level l of the min tree: entry k = the minimum of entries 32k .. 32k + 31 of
-// level l - 1 (one coalesced load per entry below, a warp minimum per entry).
-__global__ void tree_level_kernel(const int32_t* __restrict__ below, int32_t* level, int l, const BuildResult* res) {
+__global__ void __launch_bounds__(RP_THREADS) depth_scan_kernel(ReplayArgs a) {
   pdl_prologue();
-  const size_t n_below = level_size(res->n_events, l - 1);
-  const size_t n32 = ((n_below + 31) >> 5) << 5;  // a whole warp per entry: the loop bound is warp-uniform
-  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n32; c += (size_t)gridDim.x * blockDim.x) {
-    const int32_t m = __reduce_min_sync(FULLMASK, c < n_below ? below[c] : 0x7fffffff);
-    if ((c & 31) == 0) level[c >> 5] = m;
+  __shared__ int2 shd[32];
+  __shared__ uint32_t shf[32];
+  __shared__ int32_t s_wmin[RP_THREADS / 32];
+  __shared__ int2 s_dpre;
+  __shared__ uint32_t s_fpre, s_tile;
+  __shared__ bool s_last;
+  const size_t E = a.res->n_events;
+  const uint32_t U0 = a.res->u_before;
+  if (threadIdx.x == 0) s_tile = atomicAdd(&a.t.counters[1], 1u);
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  const size_t n_tiles = (E + REPLAY_TILE - 1) / REPLAY_TILE;
+  if (tile >= n_tiles) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const size_t k0 = (size_t)tile * REPLAY_TILE + (size_t)threadIdx.x * RP_ITEMS;
+  uint8_t ty[RP_ITEMS];
+  if (k0 + RP_ITEMS <= E) {
+    const uint2 u = *reinterpret_cast<const uint2*>(a.etype + k0);
+#pragma unroll
+    for (int j = 0; j < RP_ITEMS; j++) ty[j] = (uint8_t)(((j < 4 ? u.x : u.y) >> (8 * (j & 3))) & 0xffu);
+  } else {
+#pragma unroll
+    for (int j = 0; j < RP_ITEMS; j++) ty[j] = k0 + j < E ? a.etype[k0 + j] : EV_NONE;
+  }
+  // a push is (1, -inf); a pop (-1, 0): on an empty stack it takes a fresh brick
+  auto depth_map = [](uint8_t t) {
+    return t == EV_PUSH ? make_int2(1, -(1 << 30)) : t == EV_POP ? make_int2(-1, 0) : DepthOp::identity();
+  };
+  int2 acc = DepthOp::identity();
+#pragma unroll
+  for (int j = 0; j < RP_ITEMS; j++) acc = DepthOp::combine(acc, depth_map(ty[j]));
+  int2 total;
+  const int2 pre_block = block_exclusive<DepthOp>(acc, shd, total);
+  if (threadIdx.x < 32) {
+    const int2 pf = lookback<DepthOp>(tile, total, a.t.d_agg, a.t.d_incl, a.t.d_flag, &a.res->status);
+    if (threadIdx.x == 0) s_dpre = pf;
+  }
+  __syncthreads();
+  int2 run = DepthOp::combine(s_dpre, pre_block);  // the events before this thread's first
+  int dprev = max(run.y, run.x);                     // applied to the empty stack
+  int32_t dep[RP_ITEMS];
+  uint32_t fresh = 0;
+#pragma unroll
+  for (int j = 0; j < RP_ITEMS; j++) {
+    run = DepthOp::combine(run, depth_map(ty[j]));
+    dep[j] = max(run.y, run.x);
+    if (ty[j] == EV_POP && dprev == 0) fresh |= 1u << j;
+    dprev = dep[j];
+  }
+  // the fresh allocations' ranks: a second look-back, after this tile's depths
+  const uint32_t nfr = __popc(fresh);
+  uint32_t ftotal;
+  const uint32_t fpre_block = block_exclusive<SumOp>(nfr, shf, ftotal);
+  if (threadIdx.x < 32) {
+    const uint32_t pf = lookback<SumOp>(tile, ftotal, a.t.f_agg, a.t.f_incl, a.t.f_flag, &a.res->status);
+    if (threadIdx.x == 0) s_fpre = pf;
+  }
+  __syncthreads();
+  uint32_t rank = s_fpre + fpre_block;
+  if (tile == n_tiles - 1 && threadIdx.x == RP_THREADS - 1) a.res->n_fresh = rank + nfr;
+#pragma unroll
+  for (int j = 0; j < RP_ITEMS; j++)
+    if ((fresh >> j) & 1u) a.ew[k0 + j] = KNOWN | (unsigned long long)(U0 + rank++);
+  if (k0 + RP_ITEMS <= E) {
+    reinterpret_cast<int4*>(a.depth + k0)[0] = make_int4(dep[0], dep[1], dep[2], dep[3]);
+    reinterpret_cast<int4*>(a.depth + k0)[1] = make_int4(dep[4], dep[5], dep[6], dep[7]);
+  } else {
+#pragma unroll
+    for (int j = 0; j < RP_ITEMS; j++)
+      if (k0 + j < E) a.depth[k0 + j] = dep[j];
+  }
+  // the min tree: levels 1 (32 events, four threads) and 2 (1,024 events) of this tile
+  if (a.tl.n >= 1) {
+    int32_t m = 0x7fffffff;
+#pragma unroll
+    for (int j = 0; j < RP_ITEMS; j++)
+      if (k0 + j < E) m = min(m, dep[j]);
+    m = min(m, __shfl_xor_sync(FULLMASK, m, 1));
+    m = min(m, __shfl_xor_sync(FULLMASK, m, 2));
+    if ((threadIdx.x & 3) == 0 && k0 < E) a.tree[a.tl.off[0] + k0 / 32] = m;
+    if (a.tl.n >= 2) {
+      const int32_t wm = __reduce_min_sync(FULLMASK, m);  // 256 events
+      if (lane == 0) s_wmin[warp] = wm;
+      __syncthreads();
+      if (threadIdx.x < REPLAY_TILE / 1024) {
+        const size_t l2 = (size_t)tile * (REPLAY_TILE / 1024) + threadIdx.x;
+        if (l2 * 1024 < E) {
+          const int w0 = threadIdx.x * 4;
+          a.tree[a.tl.off[1] + l2] = min(min(s_wmin[w0], s_wmin[w0 + 1]), min(s_wmin[w0 + 2], s_wmin[w0 + 3]));
+        }
+      }
+    }
+  }
+  // the levels above: by the tile that finishes last
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(&a.t.counters[2], 1u) == (uint32_t)(n_tiles - 1);
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  for (int l = 3; l <= a.tl.n; l++) {
+    const size_t nb = level_size(E, l - 1), n = level_size(E, l);
+    const int32_t* below = a.tree + a.tl.off[l - 2];
+    int32_t* lev = a.tree + a.tl.off[l - 1];
+    for (size_t c = warp; c < n; c += RP_THREADS / 32) {
+      const size_t i = c * 32 + lane;
+      const int32_t m = __reduce_min_sync(FULLMASK, i < nb ? __ldcg(below + i) : 0x7fffffff);
+      if (lane == 0) lev[c] = m;
+    }
+    __threadfence();
+    __syncthreads();
   }
 }
 
@@ -1674,7 +1847,7 @@ __device__ __forceinline__ uint32_t block_below(const int32_t* L, long long b, i
   const int4* p = reinterpret_cast<const int4*>(L + b * 32);
   int4 v[8];
 #pragma unroll
-  for (int k = 0; k < 8; k++) v[k] = p[k];
+  for (int k = 0; k < 8; k++) v[k] = __ldcg(p + k);
   uint32_t m = 0;
 #pragma unroll
   for (int k = 0; k < 8; k++) {
@@ -1713,96 +1886,131 @@ __device__ long long prev_less(const int32_t* depth, const int32_t* tree, const 
   return found;
 }
 
-__global__ void match_kernel(ReplayArgs a, TreeLevels tl) {
+// Whether some i > e (i < E) has depth[i] < D: the rest of e's block at each
+// level, climbing; at the top level, every entry to the right.
+__device__ bool next_less_exists(const int32_t* depth, const int32_t* tree, const TreeLevels& tl, size_t E, size_t e,
+                                 int D) {
+  size_t i = e + 1;  // the first entry to check at level lev
+  for (int lev = 0;; lev++) {
+    const size_t n = level_size(E, lev);
+    if (i >= n) return false;
+    const int32_t* L = lev == 0 ? depth : tree + tl.off[lev - 1];
+    for (size_t b = i >> 5;; b++) {
+      uint32_t m = block_below(L, (long long)b, D, 31);
+      if (b == (i >> 5)) m &= ~((1u << (i & 31)) - 1u);  // entries from i on
+      if (b * 32 + 32 > n) m &= (1u << (n - b * 32)) - 1u;  // entries below n
+      if (m) return true;
+      if (lev < tl.n || b * 32 + 32 >= n) break;  // below the top level: one block, then climb
+    }
+    if (lev == tl.n) return false;
+    i = (i >> 5) + 1;  // the blocks wholly to the right, one level up
+  }
+}
+
+// Each event's link towards its pool index: a pop (not fresh) points to the push
+// that last filled its slot, a push of a brick allocated in this build to that
+// allocation's pop; fresh pops, old indices and the holes before the build are
+// known already.  Links always lead to earlier events; finalize follows them.
+// A push that no later event undercuts is the hole of its slot after the build:
+// holes_out[slot] receives the push's event index (finalize turns it into the
+// pool index).
+__global__ void __launch_bounds__(256) match_events_kernel(ReplayArgs a) {
   pdl_prologue();
   const size_t E = a.res->n_events;
-  const uint32_t U0 = a.res->u_before;
+  const uint32_t H = a.res->h_before;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.res->n_holes = E ? (uint32_t)a.depth[E - 1] : 0u;
+    a.res->pool_used = a.res->u_before + a.res->n_fresh;
+  }
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (size_t)gridDim.x * blockDim.x) {
-    if (a.etype[e] != EV_POP) continue;
-    const int dprev = e ? a.depth[e - 1] : 0;
-    if (dprev == 0) {
-      a.ew[e] = KNOWN | (unsigned long long)(U0 + a.fresh_rank[e]);
-    } else {
-      long long i = prev_less(a.depth, a.tree, tl, E, e, dprev);
-      a.ew[e] = (unsigned long long)(i + 1);  // the push that filled slot dprev
+    const unsigned long long w = __ldcg(a.ew + e);
+    if (a.etype[e] == EV_PUSH) {
+      if (!(w & KNOWN)) a.ew[e] = (unsigned long long)H + a.pos[w & ~PAIRREF];  // the brick's allocation
+      const int d = a.depth[e];
+      if (!next_less_exists(a.depth, a.tree, a.tl, E, e, d)) a.holes_out[d - 1] = (uint32_t)e;
+    } else if (!(w & KNOWN)) {
+      const int D = e ? a.depth[e - 1] : 0;  // >= 1: a pop at depth 0 is fresh, known already
+      a.ew[e] = (unsigned long long)(prev_less(a.depth, a.tree, a.tl, E, e, D) + 1);  // the push that filled slot D
     }
   }
 }
 
-__global__ void resolve_kernel(unsigned long long* ew, BuildResult* res) {
+// Each event's pool index: follow the links (each to an earlier event) to a
+// known index, storing it back, so that walks running at the same time cut
+// each other's chains short (a pool slot reused many times in one build makes
+// a long chain).
+__global__ void __launch_bounds__(256) resolve_events_kernel(ReplayArgs a) {
   pdl_prologue();
-  const size_t E = res->n_events;
+  const size_t E = a.res->n_events;
   for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (size_t)gridDim.x * blockDim.x) {
-    unsigned long long w = ew[e];
+    unsigned long long w = *((volatile unsigned long long*)a.ew + e);
     if (w & KNOWN) continue;
     size_t p = (size_t)w;
-    size_t steps = 0;
-    // pointers always lead to an earlier event, so the walk ends within E steps
-    for (;;) {
-      unsigned long long q = *((volatile unsigned long long*)ew + p);
+    for (size_t steps = 0;; steps++) {
+      const unsigned long long q = *((volatile unsigned long long*)a.ew + p);
       if (q & KNOWN) { w = q; break; }
-      if ((size_t)q >= p || ++steps > E) { atomicOr(&res->status, (uint32_t)ST_CHAIN); w = KNOWN; break; }
+      if ((size_t)q >= p || steps > E) {  // cannot happen: links lead to earlier events
+        atomicOr(&a.res->status, (uint32_t)ST_CHAIN);
+        w = KNOWN;
+        break;
+      }
       p = (size_t)q;
     }
-    ew[e] = w;
+    a.ew[e] = w;
   }
 }
 
-__global__ void holes_out_kernel(const uint8_t* __restrict__ etype, const int32_t* __restrict__ depth,
-                                 const int32_t* __restrict__ sufmin, const unsigned long long* __restrict__ ew,
-                                 uint32_t* holes_out, BuildResult* res) {
-  pdl_prologue();
-  const size_t E = res->n_events;
-  for (size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += (size_t)gridDim.x * blockDim.x) {
-    if (etype[e] != EV_PUSH) continue;
-    const int d = depth[e];
-    if (sufmin[e] >= d) holes_out[d - 1] = (uint32_t)(ew[e] & 0xffffffffull);
-  }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    res->n_holes = E ? (uint32_t)depth[E - 1] : 0u;
-    res->pool_used = res->u_before + res->n_fresh;
-  }
-}
-
-static size_t level_size_host(size_t E, int l) {
-  size_t n = E;
-  for (int i = 0; i < l; i++) n = (n + 31) / 32;
-  return n;
-}
-
-void launch_replay(const ReplayArgs& a, cudaStream_t s) {
-  const int T = 256;
-  // grid-stride kernels: at most one wave of 8 CTAs per SM (the event count is
-  // known on the device only, and is usually far below E_max)
-  int dev = 0, n_sms = 152;
-  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&n_sms, cudaDevAttrMultiProcessorCount, dev);
-  const size_t cap = (size_t)n_sms * 8;
-  auto blocks = [&](size_t n) { size_t b = (n + T - 1) / T; return (int)(b < cap ? (b ? b : 1) : cap); };
-  scan_any<SumOp, false>(a.cnt, a.pos, a.P, nullptr, false, nullptr, *a.scan, s);
-  launch_pdl(events_build_kernel, dim3(blocks(a.P > a.H_max ? a.P : a.H_max)), dim3(T), 0, s, a);  // also the event count
-  const uint32_t* nE = &a.res->n_events;
-  scan_any<DepthOp, false>(a.depth_fn, a.depth_fn, a.E_max, nE, true, nullptr, *a.scan, s);
-  launch_pdl(depth_fresh_kernel, dim3(blocks(a.E_max)), dim3(T), 0, s, (const int2*)a.depth_fn, (const uint8_t*)a.etype, a.depth, a.fresh, (const BuildResult*)a.res);
-  scan_any<SumOp, false>(a.fresh, a.fresh_rank, a.E_max, nE, false, &a.res->n_fresh, *a.scan, s);
-  // min tree over the depths
+TreeLevels tree_levels(size_t E_max) {
   TreeLevels tl;
   tl.n = 0;
-  size_t n = a.E_max, off = 0;
+  size_t n = E_max, off = 0;
   while (n > 32 && tl.n < 8) {
     n = (n + 31) / 32;
     tl.off[tl.n++] = off;
-    off += (n + 31) & ~(size_t)31;  // levels start on 128-byte boundaries (prev_less loads whole blocks)
+    off += (n + 31) & ~(size_t)31;  // levels start on 128-byte boundaries (whole blocks are loaded)
   }
-  for (int l = 1; l <= tl.n; l++) {
-    const int32_t* below = l == 1 ? a.depth : a.tree + tl.off[l - 2];
-    launch_pdl(tree_level_kernel, dim3(blocks(level_size_host(a.E_max, l - 1))), dim3(T), 0, s, below, a.tree + tl.off[l - 1], l, (const BuildResult*)a.res);
-  }
-  launch_pdl(match_kernel, dim3(blocks(a.E_max)), dim3(T), 0, s, a, tl);
-  launch_pdl(resolve_kernel, dim3(blocks(a.E_max)), dim3(T), 0, s, a.ew, a.res);
-  // suffix minimum of the depths (stored after the tree levels)
-  int32_t* sufmin = a.tree + off;
-  scan_any<MinOp, true>(a.depth, sufmin, a.E_max, nE, true, nullptr, *a.scan, s);
-  launch_pdl(holes_out_kernel, dim3(blocks(a.E_max)), dim3(T), 0, s, (const uint8_t*)a.etype, (const int32_t*)a.depth, (const int32_t*)sufmin, (const unsigned long long*)a.ew, a.holes_out, a.res);
+  return tl;
+}
+
+static size_t al16(size_t b) { return (b + 15) & ~(size_t)15; }
+// layout: counters[8], p_flag, d_flag, f_flag (cleared); p_agg, p_incl, d_agg, d_incl, f_agg, f_incl
+ReplayTemp replay_temp(void* base, uint64_t P, size_t E_max) {
+  const size_t tp = P / REPLAY_TILE + 2, te = E_max / REPLAY_TILE + 2;
+  char* c = (char*)base;
+  ReplayTemp t;
+  t.counters = (uint32_t*)c; c += 32;
+  t.p_flag = (uint32_t*)c; c += al16(4 * tp);
+  t.d_flag = (uint32_t*)c; c += al16(4 * te);
+  t.f_flag = (uint32_t*)c; c += al16(4 * te);
+  t.p_agg = (uint32_t*)c; c += al16(4 * tp);
+  t.p_incl = (uint32_t*)c; c += al16(4 * tp);
+  t.d_agg = (int2*)c; c += al16(8 * te);
+  t.d_incl = (int2*)c; c += al16(8 * te);
+  t.f_agg = (uint32_t*)c; c += al16(4 * te);
+  t.f_incl = (uint32_t*)c; c += al16(4 * te);
+  return t;
+}
+size_t replay_clear_bytes(uint64_t P, size_t E_max) {
+  const size_t tp = P / REPLAY_TILE + 2, te = E_max / REPLAY_TILE + 2;
+  return 32 + al16(4 * tp) + 2 * al16(4 * te);
+}
+size_t replay_temp_bytes(uint64_t P, size_t E_max) {
+  const size_t tp = P / REPLAY_TILE + 2, te = E_max / REPLAY_TILE + 2;
+  return replay_clear_bytes(P, E_max) + 2 * al16(4 * tp) + 2 * al16(8 * te) + 2 * al16(4 * te);
+}
+
+void launch_replay(const ReplayArgs& a, cudaStream_t s) {
+  int dev = 0, n_sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&n_sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t p_tiles = (a.P + REPLAY_TILE - 1) / REPLAY_TILE;
+  const size_t h_blocks = std::min<size_t>(((size_t)a.H_max + RP_THREADS - 1) / RP_THREADS, (size_t)n_sms * 4);
+  launch_pdl(scan_events_kernel, dim3((unsigned)std::max<size_t>(1, std::max(p_tiles, h_blocks))), dim3(RP_THREADS), 0,
+             s, a);
+  const size_t e_tiles = (a.E_max + REPLAY_TILE - 1) / REPLAY_TILE;
+  launch_pdl(depth_scan_kernel, dim3((unsigned)std::max<size_t>(1, e_tiles)), dim3(RP_THREADS), 0, s, a);
+  const size_t rb = std::min<size_t>((a.E_max + 255) / 256, (size_t)n_sms * 8);
+  launch_pdl(match_events_kernel, dim3((unsigned)std::max<size_t>(1, rb)), dim3(256), 0, s, a);
+  launch_pdl(resolve_events_kernel, dim3((unsigned)std::max<size_t>(1, rb)), dim3(256), 0, s, a);
 }
 
 // ---------------------------------------------------------------------------
@@ -1829,6 +2037,9 @@ __global__ void __launch_bounds__(256) finalize_kernel(FinalizeArgs a) {
     a.state->n_holes = a.res->n_holes;
   }
   const uint32_t H = a.res->h_before;
+  // the holes after the build: their pushes' event indices become pool indices
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x, nh = a.res->n_holes; k < nh; k += gridDim.x * blockDim.x)
+    a.holes_out[k] = (uint32_t)(__ldcg(a.ew + a.holes_out[k]) & 0xffffffffull);
   const int lane = threadIdx.x & 31;
   const uint32_t n = a.res->touched_count;
   // 32 touched bricks per warp pass: each lane resolves one brick's pool index

@@ -105,7 +105,7 @@ struct px_world {
   // per-build device scratch
   DevBuf d_ops, d_boxes, d_code, d_params, d_code32, d_p32, d_bases;
   DevBuf tile_cnt, tile_off, tile_ops, tile_boxes;
-  DevBuf evt, fsrc, cnt, pos, etype, ew, depth_fn, depth, tree, fresh, fresh_rank;
+  DevBuf evt, fsrc, cnt, pos, etype, ew, depth, tree, replay_tmp;
   DevBuf staging, stage_cell, stage_src, touched;
   uint64_t stage_hint = 0;      // staging slots the next build reserves (grown on overflow)
   uint32_t rescue_cap = 1u << 16;  // voxels a build may leave to float64 (grown on overflow)
@@ -523,7 +523,7 @@ void px_world_destroy(px_world* w) {
   DevBuf* bufs[] = {&w->holes_a, &w->holes_b, &w->d_ops, &w->d_boxes, &w->d_code, &w->d_params, &w->d_code32,
                     &w->d_p32, &w->d_bases, &w->tile_cnt,
                     &w->tile_off, &w->tile_ops, &w->evt, &w->fsrc, &w->cnt, &w->pos, &w->etype,
-                    &w->ew, &w->depth_fn, &w->depth, &w->tree, &w->fresh, &w->fresh_rank, &w->staging, &w->touched,
+                    &w->ew, &w->replay_tmp, &w->depth, &w->tree, &w->staging, &w->touched,
                     &w->stage_cell, &w->stage_src, &w->chunk_op, &w->pcode, &w->psub, &w->pmask,
                     &w->chunk_counter, &w->vitems, &w->scan_agg, &w->work_counter, &w->res, &w->opaque,
                     &w->udens, &w->super_counts, &w->density, &w->paint_items, &w->pvals, &w->tile_boxes, &w->bmark, &w->work, &w->pitems,
@@ -982,9 +982,8 @@ int ensure_pair_scratch(px_world* w, uint64_t P, uint64_t tile_pairs, uint64_t n
       (rc = ensure(w, w->tile_ops, 4 * tile_pairs)) || (rc = ensure(w, w->tile_boxes, 8 * tile_pairs)) ||
       (rc = ensure(w, w->evt, P)) || (rc = ensure(w, w->fsrc, 8 * P)) || (rc = ensure(w, w->cnt, 4 * P)) ||
       (rc = ensure(w, w->pos, 4 * P)) || (rc = ensure(w, w->etype, E_max)) || (rc = ensure(w, w->ew, 8 * E_max)) ||
-      (rc = ensure(w, w->depth_fn, 8 * E_max)) || (rc = ensure(w, w->depth, 4 * (E_max + 32))) ||
-      (rc = ensure(w, w->tree, 4 * (E_max / 16 + 512 + E_max))) || (rc = ensure(w, w->fresh, 4 * E_max)) ||
-      (rc = ensure(w, w->fresh_rank, 4 * E_max)) || (rc = ensure(w, w->staging, 1024 * stage_cap)) ||
+      (rc = ensure(w, w->replay_tmp, replay_temp_bytes(P, E_max))) || (rc = ensure(w, w->depth, 4 * (E_max + 32))) ||
+      (rc = ensure(w, w->tree, 4 * (E_max / 16 + 512))) || (rc = ensure(w, w->staging, 1024 * stage_cap)) ||
       (rc = ensure(w, w->stage_cell, 4 * stage_cap)) || (rc = ensure(w, w->stage_src, 8 * stage_cap)) ||
       (rc = ensure(w, w->touched, 8 * touched_bound)) ||
       (rc = ensure(w, w->work_counter, 16)) || (rc = ensure(w, w->res, sizeof(BuildResult))) ||
@@ -1421,6 +1420,7 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   ups.push_back({w->cnt.p, nullptr, 4 * P});  // events per pair, written by the apply pass
   ups.push_back({w->bmark.p, nullptr, 4 * ((w->ncells + 31) / 32)});
   ups.push_back({(char*)w->scan_agg.p + scan_regions_offset(scan_nb), nullptr, scan_regions_bytes(scan_nb)});
+  ups.push_back({w->replay_tmp.p, nullptr, replay_clear_bytes(P, E_max)});  // the replay's tickets and look-back flags
   if ((rc = issue_uploads(w, ups, s))) return rc;  // the op tables; the chunk order follows the cull launches
 
   BuildResult* res = (BuildResult*)w->res.p;
@@ -1572,19 +1572,16 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   ra.evt = (const uint8_t*)w->evt.p;
   ra.fsrc = (const int64_t*)w->fsrc.p;
   ra.holes_in = (const uint32_t*)holes_in.p;
-  ra.cnt = (uint32_t*)w->cnt.p;
+  ra.cnt = (const uint32_t*)w->cnt.p;
   ra.pos = (uint32_t*)w->pos.p;
   ra.etype = (uint8_t*)w->etype.p;
   ra.ew = (unsigned long long*)w->ew.p;
-  ra.depth_fn = (int2*)w->depth_fn.p;
   ra.depth = (int32_t*)w->depth.p;
   ra.tree = (int32_t*)w->tree.p;
-  ra.tree_words = w->tree.bytes / 4;
-  ra.fresh = (uint32_t*)w->fresh.p;
-  ra.fresh_rank = (uint32_t*)w->fresh_rank.p;
+  ra.tl = tree_levels(E_max);
   ra.holes_out = (uint32_t*)holes_out.p;
   ra.res = res;
-  ra.scan = &st;
+  ra.t = replay_temp(w->replay_tmp.p, P, E_max);
   launch_replay(ra, s);
 
   FinalizeArgs& fn = w->fin;
@@ -1595,6 +1592,7 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   fn.pos = (const uint32_t*)w->pos.p;
   fn.ew = (const unsigned long long*)w->ew.p;
   fn.state = w->d_state;
+  fn.holes_out = (uint32_t*)holes_out.p;
   fn.grid = w->d_grid;
   fn.pool32 = w->d_pool32;
   fn.pool_cap = w->pool_cap;

@@ -266,6 +266,32 @@ size_t scan_regions_bytes(size_t max_blocks);
 void launch_scan_u32(const uint32_t* in, uint32_t* out, size_t n, const uint32_t* n_dev, bool inclusive,
                      uint32_t* total_out, ScanTemp& t, cudaStream_t s);
 
+// The allocator replay's look-back scratch: flags and counters (cleared by
+// every build: replay_clear_bytes from `flags`) and the published aggregates.
+struct ReplayTemp {
+  uint32_t* counters;  // [0] pair-tile tickets, [1] event-tile tickets, [2] event tiles done
+  uint32_t* p_flag;    // per pair tile (0 pending, 1 aggregate, 2 prefix)
+  uint32_t* d_flag;    // per event tile, depth maps
+  uint32_t* f_flag;    // per event tile, fresh-allocation counts
+  uint32_t* p_agg;
+  uint32_t* p_incl;
+  int2* d_agg;
+  int2* d_incl;
+  uint32_t* f_agg;
+  uint32_t* f_incl;
+};
+constexpr int REPLAY_TILE = 4096;  // pairs or events per look-back tile (512 threads x 8)
+// bytes of the replay scratch for P pairs and E_max events, and of its cleared part
+size_t replay_temp_bytes(uint64_t P, size_t E_max);
+size_t replay_clear_bytes(uint64_t P, size_t E_max);
+ReplayTemp replay_temp(void* base, uint64_t P, size_t E_max);
+
+struct TreeLevels {
+  size_t off[8];  // offsets (in int32) of levels 1.. in the tree buffer
+  int n;          // levels above the depth array
+};
+TreeLevels tree_levels(size_t E_max);
+
 struct ReplayArgs {
   size_t P;                 // pairs
   size_t E_max;             // bound of H + 2P (H: holes before the build)
@@ -274,19 +300,16 @@ struct ReplayArgs {
   const uint8_t* evt;
   const int64_t* fsrc;
   const uint32_t* holes_in;
-  uint32_t* cnt;            // P
-  uint32_t* pos;            // P
+  const uint32_t* cnt;      // P: events per pair
+  uint32_t* pos;            // P: first event of each pair (after the H initial holes)
   uint8_t* etype;           // E_max
-  unsigned long long* ew;   // E_max
-  int2* depth_fn;           // E_max
-  int32_t* depth;           // E_max (+ tree levels)
-  int32_t* tree;            // levels above depth
-  size_t tree_words;
-  uint32_t* fresh;          // E_max
-  uint32_t* fresh_rank;     // E_max
+  unsigned long long* ew;   // E_max: the pool index of each event once resolved (KNOWN | index)
+  int32_t* depth;           // E_max (+ 32): stack depth after each event
+  int32_t* tree;            // levels of the min tree above depth
+  TreeLevels tl;
   uint32_t* holes_out;      // >= E_max
   BuildResult* res;
-  ScanTemp* scan;
+  ReplayTemp t;
 };
 void launch_replay(const ReplayArgs& a, cudaStream_t s);
 
@@ -297,6 +320,7 @@ struct FinalizeArgs {
   const int64_t* stage_src;
   const uint32_t* pos;
   const unsigned long long* ew;
+  uint32_t* holes_out;      // the holes after the build: event indices in, pool indices out
   WorldState* state;        // committed: the build's poolUsed and hole count
   uint32_t* grid;
   uint32_t* pool32;
