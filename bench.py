@@ -27,6 +27,7 @@ import subprocess
 import sys
 import threading
 import time
+import types
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
@@ -242,12 +243,12 @@ def synthetic_section(args, pyoracle):
     return res
 
 
-def batched_section(args, pyoracle, n_scenes: int = 256, check: int = 8):
+def batched_section(args, pyoracle, n_scenes: int = 256, check: int = 32):
     """256 independent seeded scenes of uneven size (volumes log-uniform 0.5-64 m^3,
     aspect up to 4:1, 16-2048 primitives, vpm 40/80/160) rebuilt by one CUDA graph
     launch; the autotuner picks the launch shape; `check` scenes (every n/check-th)
-    are compared with the oracle bit for bit."""
-    import numpy as np
+    are compared with the oracle bit for bit: grid, pool, poolUsed, holes, super
+    counts, density and the GPU free list."""
     from pixels_gb300.batch import Batch, tune
     from pixels_gb300.scenes.synthetic import batch_specs, synthetic_program
     from pixels_gb300.world import MODE_FP64, MODE_MIXED, VoxelWorld
@@ -285,18 +286,14 @@ def batched_section(args, pyoracle, n_scenes: int = 256, check: int = 8):
         _lib.world_reset(w._h, True)
         _lib.build(w._h, MODE_MIXED)
     out["sequential_ms"] = round((time.perf_counter() - t0) * 1e3, 3)
-    mism = 0
+    mism = {}
     checked = []
     for i in range(0, n_scenes, max(1, n_scenes // check)):
         s, w = specs[i], worlds[i]
         o = pyoracle.OracleWorld(progs[i].to_bytes(), s["vpm"], s["dims"], threads=os.cpu_count() or 1)
-        grid = w.grid
-        bad = int(np.count_nonzero(grid != o.grid)) + abs(w.poolUsed - o.pool_used)
-        if not bad:
-            live = np.nonzero((o.grid != 0) & ((o.grid & 0x80000000) == 0))[0]
-            idx = o.grid[live].astype(np.int64) - 1
-            bad = int(np.count_nonzero(w.pool.reshape(-1, 512)[idx] != o.pool.reshape(-1, 512)[idx]))
-        mism += bad
+        cfg = types.SimpleNamespace(bricks=tuple(d // 8 for d in s["dims"]))
+        for k, v in world_mismatches(w._h, o, cfg).items():
+            mism[k] = mism.get(k, 0) + abs(v)
         checked.append(i)
     out["oracle_checked_scenes"] = checked
     out["mismatches"] = mism

@@ -48,6 +48,12 @@ namespace px {
 #ifndef PX_VSIMPLE_MINB
 #define PX_VSIMPLE_MINB 4
 #endif
+#ifndef PX_VWIDE_MINB
+#define PX_VWIDE_MINB 3
+#endif
+#ifndef PX_VAFF_MINB
+#define PX_VAFF_MINB 3
+#endif
 
 // kernel launches issued by the host wrappers (reported per build)
 static unsigned long long g_launches = 0;
@@ -61,6 +67,23 @@ unsigned long long launch_count() { return g_launches; }
 __device__ __forceinline__ void pdl_prologue() {
   asm volatile("griddepcontrol.wait;" ::: "memory");
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// The staging area lives between the apply pass and finalize only: its stores
+// ask L2 to keep the lines (evict_last), and finalize, once it has read a staged
+// brick, drops its lines from L2 without writing them back (discard.global.L2),
+// so that the bricks need not travel through DRAM twice.
+__device__ __forceinline__ unsigned long long l2_keep_policy() {
+  unsigned long long p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ void st_keep(uint32_t* p, uint32_t v, unsigned long long pol) {
+  asm volatile("st.global.L2::cache_hint.b32 [%0], %1, %2;" ::"l"(p), "r"(v), "l"(pol) : "memory");
+}
+// p: a 128-byte aligned line whose data is no longer wanted
+__device__ __forceinline__ void l2_discard_line(const void* p) {
+  asm volatile("discard.global.L2 [%0], 128;" ::"l"(p) : "memory");
 }
 // Launched from the host one by one, the overlap hides most of each launch's
 // latency; inside a captured graph (whose launches are already back to back)
@@ -344,6 +367,59 @@ __device__ __forceinline__ void brick_bases(const FoldArgs& a, const OpDev* O, i
   bo[2] = {b2.x, b2.y};
 }
 
+// The rest of the brick pass for one pair per lane (`valid`), its class cls
+// known: the pair's class byte, the apply pass's brick bit, the paint items of
+// a full pair of a painted op, the sub-block work item of a partial pair.
+// Warp-collective.
+template <int MODE>
+__device__ __forceinline__ void classify_finish(const FoldArgs& a, bool valid, uint32_t o, const OpDev* O,
+                                                unsigned long long p, int bx, int by, int bz, int cls, int lane,
+                                                uint32_t& st_local) {
+  if (valid) {
+    a.pcode[p] = (uint8_t)cls;
+    if (cls != PC_SKIP) {  // the apply pass visits this brick
+      const size_t ci = (size_t)bx + (size_t)a.BX * ((size_t)by + (size_t)a.BY * (size_t)bz);
+      atomicOr(a.bmark + (ci >> 5), 1u << (ci & 31));
+    }
+  }
+  // a full pair of a painted op: its 8 sub-blocks go to the paint pass
+  const bool fullp = valid && cls == PC_FULL && O->paint_slot != NO_SLOT;
+  if (__any_sync(FULLMASK, fullp)) {
+    const bool back = MODE == 1 && O->paint32_off != NO_SLOT;
+#pragma unroll
+    for (int e = 0; e < 2; e++) {  // front: 16 half sub-blocks per pair; back: 8 sub-blocks
+      const uint32_t fm = __ballot_sync(FULLMASK, fullp && back == (e == 1));
+      if (!fm) continue;
+      const uint32_t per = e ? 8u : 16u;
+      uint32_t pb = 0;
+      if (lane == 0) pb = atomicAdd(a.paint_item_counter + e, per * __popc(fm));
+      pb = __shfl_sync(FULLMASK, pb, 0);
+      if (fullp && back == (e == 1)) {
+        const uint32_t at = pb + per * __popc(fm & ((1u << lane) - 1u));
+        for (uint32_t q = 0; q < per; q++)
+          if (at + q < a.paint_items_cap) {
+            if (e) a.paint_items[a.paint_items_cap - 1 - (at + q)] = make_uint2(o, (uint32_t)(p << 3) | q);
+            else a.paint_items[at + q] = make_uint2(o | ((q & 1u) << 31), (uint32_t)(p << 3) | (q >> 1));
+          }
+      }
+    }
+  }
+  // partial pairs go to the sub-block pass, one queue region per shape class
+  const bool part = valid && cls == PC_PARTIAL;
+  const uint32_t pm = __ballot_sync(FULLMASK, part);
+  if (part) {
+    const uint32_t k = O->vclass & (VCLASSES - 1);
+    const uint32_t grp = __match_any_sync(pm, k);
+    const int leader = __ffs(grp) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(&a.pitem_counter[1 + k], (uint32_t)__popc(grp));
+    base = __shfl_sync(grp, base, leader);
+    const uint32_t slot = base + __popc(grp & ((1u << lane) - 1u));
+    if (slot < a.pq_cap[k]) a.pitems[a.pq_base[k] + slot] = make_uint2(o, (uint32_t)p);
+    else st_local |= ST_STAGE_OVERFLOW;
+  }
+}
+
 // Classification of every (op, brick) pair — apply()'s SDF tests, which do not
 // depend on the world's state (shapes.ts:358-366, 382-394):
 //   bricks: one pair per lane (32 consecutive pairs, mostly one op);
@@ -389,48 +465,8 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
                                 (float)(bx * 8 + 4), (float)(by * 8 + 4), (float)(bz * 8 + 4), 1, ls);
         n_brick++;
       }
-      a.pcode[p] = (uint8_t)cls;
-      if (cls != PC_SKIP) {  // the apply pass visits this brick
-        const size_t ci = (size_t)bx + (size_t)a.BX * ((size_t)by + (size_t)a.BY * (size_t)bz);
-        atomicOr(a.bmark + (ci >> 5), 1u << (ci & 31));
-      }
     }
-    // a full pair of a painted op: its 8 sub-blocks go to the paint pass
-    const bool fullp = valid && cls == PC_FULL && O->paint_slot != NO_SLOT;
-    if (__any_sync(FULLMASK, fullp)) {
-      const bool back = MODE == 1 && O->paint32_off != NO_SLOT;
-#pragma unroll
-      for (int e = 0; e < 2; e++) {  // front: 16 half sub-blocks per pair; back: 8 sub-blocks
-        const uint32_t fm = __ballot_sync(FULLMASK, fullp && back == (e == 1));
-        if (!fm) continue;
-        const uint32_t per = e ? 8u : 16u;
-        uint32_t pb = 0;
-        if (lane == 0) pb = atomicAdd(a.paint_item_counter + e, per * __popc(fm));
-        pb = __shfl_sync(FULLMASK, pb, 0);
-        if (fullp && back == (e == 1)) {
-          const uint32_t at = pb + per * __popc(fm & ((1u << lane) - 1u));
-          for (uint32_t q = 0; q < per; q++)
-            if (at + q < a.paint_items_cap) {
-              if (e) a.paint_items[a.paint_items_cap - 1 - (at + q)] = make_uint2(o, (uint32_t)(p << 3) | q);
-              else a.paint_items[at + q] = make_uint2(o | ((q & 1u) << 31), (uint32_t)(p << 3) | (q >> 1));
-            }
-        }
-      }
-    }
-    // partial pairs go to the sub-block pass, one queue region per shape class
-    const bool part = valid && cls == PC_PARTIAL;
-    const uint32_t pm = __ballot_sync(FULLMASK, part);
-    if (part) {
-      const uint32_t k = O->vclass & (VCLASSES - 1);
-      const uint32_t grp = __match_any_sync(pm, k);
-      const int leader = __ffs(grp) - 1;
-      uint32_t base = 0;
-      if (lane == leader) base = atomicAdd(&a.pitem_counter[1 + k], (uint32_t)__popc(grp));
-      base = __shfl_sync(grp, base, leader);
-      const uint32_t slot = base + __popc(grp & ((1u << lane) - 1u));
-      if (slot < a.pq_cap[k]) a.pitems[a.pq_base[k] + slot] = make_uint2(o, (uint32_t)p);
-      else st_local |= ST_STAGE_OVERFLOW;
-    }
+    classify_finish<MODE>(a, valid, o, O, p, bx, by, bz, cls, lane, st_local);
   }
   uint32_t nb = n_brick, stw = st_local;
 #pragma unroll
@@ -441,6 +477,66 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
   if (lane == 0) {
     if (nb) atomicAdd(&a.res->c.brick_evals, (unsigned long long)nb);
     if (stw) atomicOr(&a.res->status, stw);
+  }
+}
+
+// The rest of the sub-block pass for one sub-block per lane (`have`), its class
+// scls known: the voxel mask of a lone box's partial sub-block (per-axis runs),
+// the paint items of a covered sub-block of a painted op, the Lipschitz decision
+// of a partial sub-block (mixed form) and its voxel work item.  Warp-collective.
+template <int MODE>
+__device__ __forceinline__ void sub_finish(const FoldArgs& a, bool have, uint32_t oo, unsigned long long pp, int pbx,
+                                           int pby, int pbz, int s, int scls, Iv dc, bool boxr, int lane,
+                                           uint32_t& st_local) {
+  if (boxr && scls == PC_PARTIAL)
+    a.pmask[pp * 8 + s] = box_mask(a.ops + oo, pbx * 8 + (s & 1) * 4, pby * 8 + ((s >> 1) & 1) * 4,
+                                   pbz * 8 + ((s >> 2) & 1) * 4);
+  const bool paint = have && scls != PC_SKIP && a.ops[oo].paint_slot != NO_SLOT;
+  if (__any_sync(FULLMASK, paint)) {  // the covered sub-blocks of a painted op go to the paint pass
+    const bool back = MODE == 1 && a.ops[oo].paint32_off != NO_SLOT;
+#pragma unroll
+    for (int e = 0; e < 2; e++) {  // front: two half sub-blocks; back: the sub-block
+      const uint32_t qm = __ballot_sync(FULLMASK, paint && back == (e == 1));
+      if (!qm) continue;
+      const uint32_t per = e ? 1u : 2u;
+      uint32_t pb = 0;
+      if (lane == 0) pb = atomicAdd(a.paint_item_counter + e, per * __popc(qm));
+      pb = __shfl_sync(FULLMASK, pb, 0);
+      const uint32_t at = pb + per * __popc(qm & ((1u << lane) - 1u));
+      if (paint && back == (e == 1)) {
+        if (e) {
+          if (at < a.paint_items_cap) a.paint_items[a.paint_items_cap - 1 - at] = make_uint2(oo, (uint32_t)(pp << 3) | (uint32_t)s);
+        } else {
+          for (uint32_t h = 0; h < 2; h++)
+            if (at + h < a.paint_items_cap) a.paint_items[at + h] = make_uint2(oo | (h << 31), (uint32_t)(pp << 3) | (uint32_t)s);
+        }
+      }
+    }
+  }
+  // mixed form: a partial sub-block whose centre value is farther from 0 than
+  // every voxel's distance bound (Lipschitz) has all its voxels decided
+  bool lipd = false;
+  if (MODE == 1 && have && scls == PC_PARTIAL && !boxr && !a.validate) {
+    const float l3 = a.ops[oo].lip[3];
+    if (dc.lo > l3 || dc.hi < -l3) {
+      a.pmask[pp * 8 + s] = dc.lo > l3 ? 0ull : ~0ull;
+      lipd = true;
+    }
+  }
+  const bool push = have && scls == PC_PARTIAL && !boxr && !lipd;
+  const uint32_t vm = __ballot_sync(FULLMASK, push);
+  if (push) {  // one append per shape class present among the pushing lanes
+    const uint32_t k = a.ops[oo].vq_class;
+    const uint32_t grp = __match_any_sync(vm, k);
+    const int leader = __ffs(grp) - 1;
+    uint32_t vb = 0;
+    if (lane == leader) vb = atomicAdd(&a.vitem_counter[1 + k], (uint32_t)__popc(grp));
+    vb = __shfl_sync(grp, vb, leader);
+    const uint32_t slot = vb + __popc(grp & ((1u << lane) - 1u));
+    if (slot < a.vq_cap[k])
+      a.vitems[a.vq_base[k] + slot] =
+          make_uint4(oo, (uint32_t)(pp << 3) | (uint32_t)s, __float_as_uint(dc.lo), __float_as_uint(dc.hi));
+    else st_local |= ST_STAGE_OVERFLOW;
   }
 }
 
@@ -507,57 +603,7 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_SUB_MINB : PX_CLASSIFY64_M
     code16 |= __shfl_xor_sync(FULLMASK, code16, 2);
     code16 |= __shfl_xor_sync(FULLMASK, code16, 4);
     if (s == 0 && have) a.psub[pp] = (uint16_t)code16;
-    // a lone box's voxel mask comes from its per-axis runs; other partial sub-blocks are queued
-    if (boxr && scls == PC_PARTIAL)
-      a.pmask[pp * 8 + s] = box_mask(a.ops + oo, pbx * 8 + (s & 1) * 4, pby * 8 + ((s >> 1) & 1) * 4,
-                                     pbz * 8 + ((s >> 2) & 1) * 4);
-    const bool paint = have && scls != PC_SKIP && a.ops[oo].paint_slot != NO_SLOT;
-    if (__any_sync(FULLMASK, paint)) {  // the covered sub-blocks of a painted op go to the paint pass
-      const bool back = MODE == 1 && a.ops[oo].paint32_off != NO_SLOT;
-#pragma unroll
-      for (int e = 0; e < 2; e++) {  // front: two half sub-blocks; back: the sub-block
-        const uint32_t qm = __ballot_sync(FULLMASK, paint && back == (e == 1));
-        if (!qm) continue;
-        const uint32_t per = e ? 1u : 2u;
-        uint32_t pb = 0;
-        if (lane == 0) pb = atomicAdd(a.paint_item_counter + e, per * __popc(qm));
-        pb = __shfl_sync(FULLMASK, pb, 0);
-        const uint32_t at = pb + per * __popc(qm & ((1u << lane) - 1u));
-        if (paint && back == (e == 1)) {
-          if (e) {
-            if (at < a.paint_items_cap) a.paint_items[a.paint_items_cap - 1 - at] = make_uint2(oo, (uint32_t)(pp << 3) | (uint32_t)s);
-          } else {
-            for (uint32_t h = 0; h < 2; h++)
-              if (at + h < a.paint_items_cap) a.paint_items[at + h] = make_uint2(oo | (h << 31), (uint32_t)(pp << 3) | (uint32_t)s);
-          }
-        }
-      }
-    }
-    // mixed form: a partial sub-block whose centre value is farther from 0 than
-    // every voxel's distance bound (Lipschitz) has all its voxels decided
-    bool lipd = false;
-    if (MODE == 1 && have && scls == PC_PARTIAL && !boxr && !a.validate) {
-      const float l3 = a.ops[oo].lip[3];
-      if (dc.lo > l3 || dc.hi < -l3) {
-        a.pmask[pp * 8 + s] = dc.lo > l3 ? 0ull : ~0ull;
-        lipd = true;
-      }
-    }
-    const bool push = have && scls == PC_PARTIAL && !boxr && !lipd;
-    const uint32_t vm = __ballot_sync(FULLMASK, push);
-    if (push) {  // one append per shape class present among the pushing lanes
-      const uint32_t k = a.ops[oo].vq_class & (VQ_CLASSES - 1);
-      const uint32_t grp = __match_any_sync(vm, k);
-      const int leader = __ffs(grp) - 1;
-      uint32_t vb = 0;
-      if (lane == leader) vb = atomicAdd(&a.vitem_counter[1 + k], (uint32_t)__popc(grp));
-      vb = __shfl_sync(grp, vb, leader);
-      const uint32_t slot = vb + __popc(grp & ((1u << lane) - 1u));
-      if (slot < a.vq_cap[k])
-        a.vitems[a.vq_base[k] + slot] =
-            make_uint4(oo, (uint32_t)(pp << 3) | (uint32_t)s, __float_as_uint(dc.lo), __float_as_uint(dc.hi));
-      else st_local |= ST_STAGE_OVERFLOW;
-    }
+    sub_finish<MODE>(a, have, oo, pp, pbx, pby, pbz, s, scls, dc, boxr, lane, st_local);
   }
   uint32_t stw = st_local;
 #pragma unroll
@@ -576,17 +622,20 @@ __device__ __forceinline__ int lip_decide(const OpDev* O, Iv dc, int ox, int oy,
 
 // Voxel inside-masks of the queued partial sub-blocks: one sub-block per warp
 // pass, 64 voxel SDFs on 32 lanes, two ballots (shapes.ts:390-394), any
-// program (the bytecode interpreters).  HALF: the voxel classes it drains,
-// [32 HALF, 32 HALF + 32) in vclass_order (the mixed form sends the first half,
-// the single-primitive programs, to voxel_simple_kernel).
-template <int MODE, int HALF>
+// program (the bytecode interpreters); a voxel its float32 interval cannot
+// decide is evaluated in float64 in line.  Groups G0 .. G1 of the voxel queue, one
+// after the other (the mixed form sends the lean programs' groups to
+// voxel_lean_kernel and this kernel the rest; the float64 form every group here).
+template <int MODE, int G0, int G1>
 __global__ void __launch_bounds__(256, MODE == 1 ? PX_VOXEL_MINB : PX_CLASSIFY64_MINB) voxel_kernel(FoldArgs a) {
   pdl_prologue();
   const int lane = threadIdx.x & 31;
   LaneStats ls = {a.res};
-  uint32_t* const taken = HALF ? &a.vitem_counter[0] : &a.vitem_counter[VQ_SIMPLE_TAKEN];
-  // the classes' item counts in the order they are taken, as an inclusive prefix over lanes
-  const int my_cls = a.vclass_order[32 * HALF + lane];
+#pragma unroll 1
+  for (int g = G0; g <= G1; g++) {
+  uint32_t* const taken = &a.vitem_counter[VQ_TAKEN + g];
+  // the group's classes' item counts in the order they are taken, as an inclusive prefix over lanes
+  const int my_cls = a.vclass_order[32 * g + lane];
   uint32_t incl = min(__ldg(&a.vitem_counter[1 + my_cls]), a.vq_cap[my_cls]);
   const uint32_t own = incl;
 #pragma unroll
@@ -595,28 +644,6 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_VOXEL_MINB : PX_CLASSIFY64
     if (lane >= o) incl += t;
   }
   const uint32_t n_items = __shfl_sync(FULLMASK, incl, 31);
-  if (MODE == 1 && HALF == 1) {
-    // first the voxels voxel_simple_kernel left undecided: one per thread, in float64
-    // (shapes.ts:393); their sub-block masks hold them as outside until here
-    const uint32_t n_resc = min(__ldcg(&a.res->n_rescue), a.rescue_cap);
-    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n_resc; r += gridDim.x * blockDim.x) {
-      const uint4 ri = __ldcg(a.rescue + r);
-      const OpDev* R = a.ops + (ri.x & 0xffffffu);
-      const int bit = (int)((ri.x >> 24) & 63u);
-      const bool ramb = (ri.x >> 30) & 1u;
-      const unsigned long long rp = ri.y >> 3;
-      const int rs = ri.y & 7;
-      int rbx, rby, rbz;
-      brick_of_pair(R, rp, rbx, rby, rbz);
-      const int vx = rbx * 8 + (rs & 1) * 4 + (bit & 3), vy = rby * 8 + ((rs >> 1) & 1) * 4 + ((bit >> 2) & 3),
-                vz = rbz * 8 + ((rs >> 2) & 1) * 4 + (bit >> 4);
-      const Iv dk = {__uint_as_float(ri.z), __uint_as_float(ri.w)};
-      const VoxelF64 f = voxel_f64(a.params, a.vs, 0, a.code + R->code_off, (int)R->code_len, dk, ramb, 3,
-                                   (float)vx + 0.5f, (float)vy + 0.5f, (float)vz + 0.5f);
-      ls.rescue(0, ramb, f.err);
-      if (f.inside) atomicOr(a.pmask + rp * 8 + rs, 1ull << bit);
-    }
-  }
   NextTicket tk;
   tk.issue(taken, 1, lane);
   for (;;) {
@@ -625,7 +652,7 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_VOXEL_MINB : PX_CLASSIFY64
     tk.issue(taken, 1, lane);
     const int k = __popc(__ballot_sync(FULLMASK, incl <= it));  // class of item `it`
     const uint32_t first = __shfl_sync(FULLMASK, incl - own, k);
-    const uint4 item = __ldg(a.vitems + a.vq_base[a.vclass_order[32 * HALF + k]] + (it - first));
+    const uint4 item = __ldg(a.vitems + a.vq_base[a.vclass_order[32 * g + k]] + (it - first));
     const Iv dcen = {__uint_as_float(item.z), __uint_as_float(item.w)};  // the sub-block centre's value
     const OpDev* V = a.ops + item.x;
     const unsigned long long vp = item.y >> 3;
@@ -698,6 +725,7 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_VOXEL_MINB : PX_CLASSIFY64
       ls.viol();
     if (lane == 0) a.pmask[vp * 8 + ss] = m;
   }
+  }
 }
 
 // The point through a rotation of the shape's frame (shapes.ts:263-320 on
@@ -719,24 +747,37 @@ __device__ __forceinline__ void rot32(uint32_t op, const Iv* __restrict__ p, Iv&
   }
 }
 
-// Voxel inside-masks of the queued partial sub-blocks of single-primitive
-// programs -- [rotation] primitive [rotation end] [offset], 88% of the
-// penthouse's non-box voxel work -- in the mixed form: the same decisions as
+// Apply a lean program's stage (LP_* kinds): one rotation, or (AFF) a composed run.
+template <bool AFF>
+__device__ __forceinline__ void stage32(uint32_t kind, const Iv* __restrict__ p, Iv& x, Iv& y, Iv& z) {
+  if (AFF && kind == LP_AFFINE) aff32(p, x, y, z);
+  else if (kind) rot32(OP_ROT_X - 1 + kind, p, x, y, z);
+}
+
+// Voxel inside-masks of the queued partial sub-blocks of the lean programs --
+// one or two primitives under a rotation, a composed run of rotations or none
+// (LP_* forms): 88% of the penthouse's non-box voxel work, all of the
+// rotated synthetic scenes' -- in the mixed form: the same decisions as
 // voxel_kernel (shapes.ts:390-394), without the interpreters' value stack and
 // rotation frames.  Lane = voxel column (x, z) of the sub-block and a pair of
-// y rows; a primitive extruded along y (unrotated, or rotated about y) shares
-// its x/z work between the two voxels.
-// VALIDATE (validation mode) evaluates every voxel in float64 too, in line;
-// otherwise a voxel the interval cannot decide goes to the rescue list (no
-// call in the kernel: the float64 evaluator's calls would make every register
-// live across them spill).
-template <bool VALIDATE>
-__global__ void __launch_bounds__(256, PX_VSIMPLE_MINB) voxel_simple_kernel(FoldArgs a) {
+// y rows; unrotated primitives extruded along y (or rotated about y) share
+// their x/z work between the two voxels.
+// VALIDATE (validation mode) evaluates every voxel in float64 too, in line.
+// Otherwise a voxel the interval cannot decide goes to the rescue list, which
+// voxel_kernel<1, ...> resolves in float64 first, and counts as outside until
+// then (no call in this kernel: every value live across one would be saved to
+// local memory).
+// G: the group of the voxel queue (VQ_NARROW, VQ_AFFINE or VQ_WIDE), each
+// compiled with only its forms' live values.
+template <bool VALIDATE, int G>
+__global__ void __launch_bounds__(256, G == VQ_WIDE ? PX_VWIDE_MINB : G == VQ_AFFINE ? PX_VAFF_MINB : PX_VSIMPLE_MINB)
+    voxel_lean_kernel(FoldArgs a) {
+  constexpr bool WIDE = G == VQ_WIDE, AFF = G != VQ_NARROW;
   pdl_prologue();
   const int lane = threadIdx.x & 31;
   LaneStats ls = {a.res};
-  uint32_t* const taken = &a.vitem_counter[VQ_SIMPLE_TAKEN];
-  const int my_cls = a.vclass_order[lane];
+  uint32_t* const taken = &a.vitem_counter[VQ_TAKEN + G];
+  const int my_cls = a.vclass_order[32 * G + lane];
   uint32_t incl = min(__ldg(&a.vitem_counter[1 + my_cls]), a.vq_cap[my_cls]);
   const uint32_t own = incl;
 #pragma unroll
@@ -755,7 +796,7 @@ __global__ void __launch_bounds__(256, PX_VSIMPLE_MINB) voxel_simple_kernel(Fold
     tk.issue(taken, 1, lane);
     const int k = __popc(__ballot_sync(FULLMASK, incl <= it));  // class of item `it`
     const uint32_t first = __shfl_sync(FULLMASK, incl - own, k);
-    const uint4 item = __ldg(a.vitems + a.vq_base[a.vclass_order[k]] + (it - first));
+    const uint4 item = __ldg(a.vitems + a.vq_base[a.vclass_order[32 * G + k]] + (it - first));
     const Iv dcen = {__uint_as_float(item.z), __uint_as_float(item.w)};  // the sub-block centre's value
     const OpDev* V = a.ops + item.x;
     const unsigned long long vp = item.y >> 3;
@@ -767,50 +808,76 @@ __global__ void __launch_bounds__(256, PX_VSIMPLE_MINB) voxel_simple_kernel(Fold
     const int sxo = (ss & 1) * 4, syo = ((ss >> 1) & 1) * 4, szo = ((ss >> 2) & 1) * 4;
     const int lx = sxo + (col & 3), lz = szo + (col >> 2), ly0 = syo + 2 * yh;
     const int lip0 = lip_decide(V, dcen, col & 3, 2 * yh, col >> 2), lip1 = lip_decide(V, dcen, col & 3, 2 * yh + 1, col >> 2);
-    const uint32_t sp = V->simple;
-    const uint32_t prim = sp & 0xffu, rot = (sp >> 8) & 0xffu;
     const float M = V->thr[T_M];
     bool amb0 = false, amb1 = false;  // a polygon crossing test the interval could not settle, per voxel
     Iv2 d = {{0.f, 0.f}, {0.f, 0.f}};
     if (lip0 == 3 || lip1 == 3 || VALIDATE) {
+      const uint2 lpw = make_uint2(*reinterpret_cast<const uint32_t*>(V->lp), *reinterpret_cast<const uint32_t*>(V->lp + 4));
+      const uint32_t form = WIDE ? lpw.x & 0xffu : 1u, comb = (lpw.x >> 8) & 0xffu, ip1 = (lpw.x >> 16) & 0xffu,
+                     ip2 = lpw.x >> 24, is2 = (lpw.y >> 8) & 0xffu, kinds = (lpw.y >> 16) & 0xffu,
+                     ioff = lpw.y >> 24;
+      const uint32_t k1 = kinds & 15u, k2 = WIDE ? kinds >> 4 : 0u;
       const uint32_t* c32 = a.code32 + V->code_off;
-      const uint32_t ip = rot ? 1u : 0u;  // the primitive's instruction
-      const Iv* pr = P + __ldg(c32 + ip);
-      const int cnt = (int)(__ldg(&a.code[V->code_off + ip].x) >> 8);
-      Iv x = iadd(bo[0], koff((float)lx, a.vs_lo, a.vs_hi)), z = iadd(bo[2], koff((float)lz, a.vs_lo, a.vs_hi));
+      const uint2* cw = a.code + V->code_off;
+      const uint32_t w1 = __ldg(&cw[ip1].x), w2 = form > 1 ? __ldg(&cw[ip2].x) : 0u;
+      const uint32_t p1 = w1 & 0xffu, p2 = w2 & 0xffu;
+      const Iv* pr1 = P + (__ldg(c32 + ip1) & C32_OFF);
+      const Iv* pr2 = P + (__ldg(c32 + (form > 1 ? ip2 : ip1)) & C32_OFF);
+      const Iv* ps1 = P + (__ldg(c32) & C32_OFF);  // the first stage is instruction 0
+      const Iv* ps2 = P + (__ldg(c32 + (k2 ? is2 : 0u)) & C32_OFF);
+      const Iv x = iadd(bo[0], koff((float)lx, a.vs_lo, a.vs_hi)), z = iadd(bo[2], koff((float)lz, a.vs_lo, a.vs_hi));
       const Iv y0 = iadd(bo[1], koff((float)ly0, a.vs_lo, a.vs_hi)), y1 = iadd(bo[1], koff((float)(ly0 + 1), a.vs_lo, a.vs_hi));
-      if ((rot == 0 || rot == OP_ROT_Y) && op_is_y_separable(prim)) {
-        if (rot) {  // x and z only: shared by both voxels
-          Iv yd = y0;
-          rot32(rot, P + __ldg(c32), x, yd, z);
-        }
+      auto combine = [&](Iv u, Iv v) -> Iv {
+        return comb == LP_NEGMAX ? imax(u, ineg(v)) : comb == LP_MAX ? imax(u, v) : imin(u, v);
+      };
+      // y-extruded primitives, unrotated or rotated about y: x and z are shared by both voxels
+      const bool ysep = (k1 == 0 || k1 == 2) && (k2 == 0 || k2 == 2) && op_is_y_separable(p1) &&
+                        (form == 1 || op_is_y_separable(p2));
+      if (ysep) {
         bool amb = false;  // the column's polygon work is shared by both voxels
-        d = prim32_y2(prim, cnt, pr, x, y0, y1, z, M, amb);
+        Iv x1 = x, z1 = z, yd = y0;
+        if (k1) rot32(OP_ROT_Y, ps1, x1, yd, z1);
+        d = prim32_y2(p1, (int)(w1 >> 8), pr1, x1, y0, y1, z1, M, amb);
+        if (form > 1) {
+          Iv x2 = x1, z2 = z1;
+          if (form == 3) {
+            x2 = x; z2 = z;
+            if (k2) rot32(OP_ROT_Y, ps2, x2, yd, z2);
+          }
+          const Iv2 e = prim32_y2(p2, (int)(w2 >> 8), pr2, x2, y0, y1, z2, M, amb);
+          d = {combine(d.a, e.a), combine(d.b, e.b)};
+        }
         amb0 = amb1 = amb;
       } else {
 #pragma unroll 1
         for (int q = 0; q < 2; q++) {
-          Iv xx = x, yy = q ? y1 : y0, zz = z;
-          if (rot) rot32(rot, P + __ldg(c32), xx, yy, zz);
           bool ambq = false;  // each voxel's own crossing tests
-          const Iv v = prim32(prim, cnt, pr, xx, yy, zz, M, ambq);
+          Iv x1 = x, y1q = q ? y1 : y0, z1 = z;
+          stage32<AFF>(k1, ps1, x1, y1q, z1);
+          Iv v = prim32(p1, (int)(w1 >> 8), pr1, x1, y1q, z1, M, ambq);
+          if (form == 2) {
+            v = combine(v, prim32(p2, (int)(w2 >> 8), pr2, x1, y1q, z1, M, ambq));
+          } else if (form == 3) {
+            Iv x2 = x, y2q = q ? y1 : y0, z2 = z;
+            stage32<AFF>(k2, ps2, x2, y2q, z2);
+            v = combine(v, prim32(p2, (int)(w2 >> 8), pr2, x2, y2q, z2, M, ambq));
+          }
           if (q) { d.b = v; amb1 = ambq; } else { d.a = v; amb0 = ambq; }
         }
       }
-      if (sp >> 16) {  // offset (penthouse.ts:250)
-        const Iv o = ldp(P + __ldg(c32 + (rot ? 3u : 1u)), 0);
+      if (ioff != LP_NONE) {  // offset (penthouse.ts:250)
+        const Iv o = ldp(P + (__ldg(c32 + ioff) & C32_OFF), 0);
         d = {iadd(d.a, o), iadd(d.b, o)};
       }
     }
     const uint2* code = a.code + V->code_off;
     const int clen = (int)V->code_len;
-    uint32_t lo = 0, hi = 0;
+    uint32_t lo = 0, hi = 0, resc = 0;  // resc: bit q, voxel q of this lane left to float64
 #pragma unroll
     for (int q = 0; q < 2; q++) {
       const Iv dk = q ? d.b : d.a;
       const bool amb = q ? amb1 : amb0;
       const int lipk = q ? lip1 : lip0;
-      const int bit = (col & 3) | ((2 * yh + q) << 2) | ((col >> 2) << 4);  // voxel index in the sub-block
       int inside = lipk;
       if (lipk == 3 || VALIDATE) {
         inside = amb ? 3 : (dk.lo > V->thr[T_V_HI] ? 0 : (dk.hi <= V->thr[T_V_LO] ? 1 : 3));
@@ -822,16 +889,12 @@ __global__ void __launch_bounds__(256, PX_VSIMPLE_MINB) voxel_simple_kernel(Fold
           if (inside == 3) ls.rescue(0, amb, f.err);
           inside = f.inside;
           if (lipk != 3 && inside != lipk) ls.viol();  // the bound disagreed with the evaluation
-        } else if (inside == 3) {  // decided in float64 by voxel_kernel<1, 1>; outside until then
-          const uint32_t r = atomicAdd(&a.res->n_rescue, 1u);
-          if (r < a.rescue_cap)
-            a.rescue[r] = make_uint4(item.x | ((uint32_t)bit << 24) | (amb ? 1u << 30 : 0u), item.y,
-                                     __float_as_uint(dk.lo), __float_as_uint(dk.hi));
-          else
-            atomicOr(&a.res->status, (uint32_t)ST_RESCUE_OVERFLOW);
+        } else if (inside == 3) {  // resolved in float64 after the work loop; outside until then
+          resc |= 1u << q;
           inside = 0;
         }
       }
+      const int bit = (col & 3) | ((2 * yh + q) << 2) | ((col >> 2) << 4);  // voxel index in the sub-block
       if (inside == 1) {
         if (bit < 32) lo |= 1u << bit;
         else hi |= 1u << (bit - 32);
@@ -844,6 +907,34 @@ __global__ void __launch_bounds__(256, PX_VSIMPLE_MINB) voxel_simple_kernel(Fold
         box_mask(V, vbx * 8 + sxo, vby * 8 + syo, vbz * 8 + szo) != m)
       ls.viol();
     if (lane == 0) a.pmask[vp * 8 + ss] = m;
+    if (!VALIDATE) {  // undecided voxels to the rescue list, one atomic per warp
+      const uint32_t nr = __popc(resc);
+      const uint32_t tot = __reduce_add_sync(FULLMASK, nr);
+      if (tot) {
+        uint32_t at = nr;  // this lane's first entry: an exclusive prefix over the lanes
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t t = __shfl_up_sync(FULLMASK, at, o);
+          if (lane >= o) at += t;
+        }
+        at -= nr;
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&a.res->n_rescue, tot);
+        base = __shfl_sync(FULLMASK, base, 0);
+#pragma unroll
+        for (int q = 0; q < 2; q++) {
+          if (!((resc >> q) & 1u)) continue;
+          const Iv dk = q ? d.b : d.a;
+          const bool amb = q ? amb1 : amb0;
+          const int bit = (col & 3) | ((2 * yh + q) << 2) | ((col >> 2) << 4);
+          const uint4 e = make_uint4(item.x | ((uint32_t)bit << 24) | (amb ? 1u << 30 : 0u), item.y,
+                                     __float_as_uint(dk.lo), __float_as_uint(dk.hi));
+          const uint32_t r = base + at++;
+          if (r < a.rescue_cap) a.rescue[r] = e;
+          else atomicOr(&a.res->status, (uint32_t)ST_RESCUE_OVERFLOW);
+        }
+      }
+    }
   }
 }
 
@@ -867,6 +958,38 @@ __device__ __noinline__ uint32_t paint_at_voxel(const double* __restrict__ param
   return (v & 0xffffu) | (st & ST_RANGE ? PV_RANGE : 0u) | (viol ? PV_VIOL : 0u);
 }
 
+// One paint call of op O at voxel (lx, ly, lz) of brick (bx, by, bz) as the paint
+// pass stores it (value | PV_RANGE): the certified float32 evaluation first in
+// the mixed form (bo: the brick's float32 bases, unused for the noise kind),
+// else float64; validation mode evaluates both and counts mismatches in viol.
+template <int MODE>
+__device__ __forceinline__ uint32_t paint_voxel(const FoldArgs& a, const OpDev* O, int bx, int by, int bz, const Iv* bo,
+                                                int lx, int ly, int lz, uint32_t& resc, uint32_t& viol) {
+  const uint32_t pk = O->paint_kind;
+  uint32_t v = 0, st = 0;
+  bool done = false;
+  if (MODE == 1 && O->paint32_off != NO_SLOT) {
+    if (pk == PK_NOISE)
+      done = noise32(a.p32 + O->paint32_off, __ldg(a.ax32 + bx * 8 + lx), __ldg(a.ay32 + by * 8 + ly),
+                     __ldg(a.az32 + bz * 8 + lz), v);
+    else
+      done = paint32(pk, a.p32 + O->paint32_off, iadd(bo[0], koff((float)lx, a.vs_lo, a.vs_hi)),
+                     iadd(bo[1], koff((float)ly, a.vs_lo, a.vs_hi)), iadd(bo[2], koff((float)lz, a.vs_lo, a.vs_hi)), v);
+    if (!done) resc++;
+  }
+  if (!done || a.validate) {  // float64 (validation: also the correctly rounded decision)
+    const uint32_t pr = paint_at_voxel(a.params, a.vs, a.validate, O, bx * 8 + lx, by * 8 + ly, bz * 8 + lz);
+    if (pr & PV_VIOL) viol++;
+    if (!done) {
+      v = pr & 0xffffu;
+      if (pr & PV_RANGE) st |= ST_RANGE;
+    } else if (v != (pr & 0xffffu)) {
+      viol++;
+    }
+  }
+  return (v & 0xffffu) | (st & ST_RANGE ? PV_RANGE : 0u);
+}
+
 // Paint calls ahead of the apply pass: the covered sub-blocks of the painted
 // ops' pairs (queued by the classify and sub-block passes), one 4^3 sub-block
 // per warp pass, two voxels per lane, every voxel the op's shape covers (whether
@@ -875,14 +998,48 @@ __device__ __noinline__ uint32_t paint_at_voxel(const double* __restrict__ param
 // voxel index order.  Spreading these calls over the whole GPU keeps one
 // warp from evaluating a painted brick's 512 calls alone.  Mixed mode tries the
 // certified float32 evaluation first (paint32.cuh).
+// Mixed form: first the voxels the lean voxel kernels left undecided (the rescue
+// list), one per thread, in float64 (shapes.ts:393): the inside ones are ORed
+// into their sub-block masks, and a painted op's paint value is stored for them
+// here.  Entry r goes to block r mod gridDim.x, so a warp holds few (an FP64
+// instruction of a sparse warp is far quicker than a full one: FP64 runs at 1/64
+// of the float32 rate) and the float64 chains overlap the paint work.  A paint
+// item of the same sub-block may read its mask before or after the OR: it then
+// paints the voxel too or leaves it out, and either way stores the same value.
 template <int MODE>
 __global__ void __launch_bounds__(256) paint_kernel(FoldArgs a) {
   pdl_prologue();
   const int lane = threadIdx.x & 31;
+  uint32_t resc = 0, viol = 0;
+  if (MODE == 1) {
+    LaneStats ls = {a.res};
+    const uint32_t n_resc = min(__ldcg(&a.res->n_rescue), a.rescue_cap);
+    for (uint32_t r = blockIdx.x + gridDim.x * threadIdx.x; r < n_resc; r += gridDim.x * blockDim.x) {
+      const uint4 ri = __ldcg(a.rescue + r);
+      const OpDev* R = a.ops + (ri.x & 0xffffffu);
+      const int bit = (int)((ri.x >> 24) & 63u);
+      const bool ramb = (ri.x >> 30) & 1u;
+      const unsigned long long rp = ri.y >> 3;
+      const int rs = ri.y & 7;
+      int rbx, rby, rbz;
+      brick_of_pair(R, rp, rbx, rby, rbz);
+      const int lx = (rs & 1) * 4 + (bit & 3), ly = ((rs >> 1) & 1) * 4 + ((bit >> 2) & 3), lz = ((rs >> 2) & 1) * 4 + (bit >> 4);
+      const Iv dk = {__uint_as_float(ri.z), __uint_as_float(ri.w)};
+      const VoxelF64 f = voxel_f64(a.params, a.vs, 0, a.code + R->code_off, (int)R->code_len, dk, ramb, 3,
+                                   (float)(rbx * 8 + lx) + 0.5f, (float)(rby * 8 + ly) + 0.5f, (float)(rbz * 8 + lz) + 0.5f);
+      ls.rescue(0, ramb, f.err);
+      if (!f.inside) continue;
+      atomicOr(a.pmask + rp * 8 + rs, 1ull << bit);
+      if (R->paint_slot == NO_SLOT) continue;
+      Iv bo[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+      if (R->paint32_off != NO_SLOT && R->paint_kind != PK_NOISE) brick_bases(a, R, rbx, rby, rbz, bo);
+      a.pvals[(size_t)(R->paint_slot + (uint32_t)(rp - R->pair_base)) * 512 + (uint32_t)(lx | (ly << 3) | (lz << 6))] =
+          paint_voxel<MODE>(a, R, rbx, rby, rbz, bo, lx, ly, lz, resc, viol);
+    }
+  }
   // float64 paints (the front of the queue) first, then the certified float32 ones
   const uint32_t n_front = min(__ldg(a.paint_item_counter), a.paint_items_cap);
   const uint32_t n_items = n_front + min(__ldg(a.paint_item_counter + 1), a.paint_items_cap - n_front);
-  uint32_t resc = 0, viol = 0;
   WorkBatch wb;
   for (;;) {
     const uint32_t it = wb.next(a.paint_counter, 2, lane);
@@ -898,7 +1055,7 @@ __global__ void __launch_bounds__(256) paint_kernel(FoldArgs a) {
     unsigned long long m = ~0ull;
     if (cls != PC_FULL) {
       const uint32_t c = (__ldg(a.psub + pair) >> (2 * s)) & 3u;
-      m = c == PC_FULL ? ~0ull : c == PC_PARTIAL ? __ldg(a.pmask + pair * 8 + s) : 0ull;
+      m = c == PC_FULL ? ~0ull : c == PC_PARTIAL ? __ldcg(a.pmask + pair * 8 + s) : 0ull;
     }
     if (!m) continue;
     int bx, by, bz;
@@ -906,30 +1063,14 @@ __global__ void __launch_bounds__(256) paint_kernel(FoldArgs a) {
     const uint32_t pk = O->paint_kind;
     const bool try32 = MODE == 1 && O->paint32_off != NO_SLOT;
     Iv bo[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    if (try32) brick_bases(a, O, bx, by, bz, bo);
+    if (try32 && pk != PK_NOISE) brick_bases(a, O, bx, by, bz, bo);
 #pragma unroll 1
     for (int r = r0; r < r1; r++) {
       const int e = r * 32 + lane;
       if (!((m >> e) & 1ull)) continue;
       const int lx = (s & 1) * 4 + (e & 3), ly = ((s >> 1) & 1) * 4 + ((e >> 2) & 3), lz = ((s >> 2) & 1) * 4 + (e >> 4);
-      uint32_t v = 0, st = 0;
-      bool done = false;
-      if (try32) {
-        done = paint32(pk, a.p32 + O->paint32_off, iadd(bo[0], koff((float)lx, a.vs_lo, a.vs_hi)),
-                       iadd(bo[1], koff((float)ly, a.vs_lo, a.vs_hi)), iadd(bo[2], koff((float)lz, a.vs_lo, a.vs_hi)), v);
-        if (!done) resc++;
-      }
-      if (!done || a.validate) {  // float64 (validation: also the correctly rounded decision)
-        const uint32_t pr = paint_at_voxel(a.params, a.vs, a.validate, O, bx * 8 + lx, by * 8 + ly, bz * 8 + lz);
-        if (pr & PV_VIOL) viol++;
-        if (!done) {
-          v = pr & 0xffffu;
-          if (pr & PV_RANGE) st |= ST_RANGE;
-        } else if (v != (pr & 0xffffu)) {
-          viol++;
-        }
-      }
-      a.pvals[(size_t)slot * 512 + (uint32_t)(lx | (ly << 3) | (lz << 6))] = (v & 0xffffu) | (st & ST_RANGE ? PV_RANGE : 0u);
+      a.pvals[(size_t)slot * 512 + (uint32_t)(lx | (ly << 3) | (lz << 6))] =
+          paint_voxel<MODE>(a, O, bx, by, bz, bo, lx, ly, lz, resc, viol);
     }
   }
 #pragma unroll
@@ -1284,8 +1425,9 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
           st_local |= ST_STAGE_OVERFLOW;
         } else {
           uint32_t* dst = a.staging32 + (size_t)slot * 256;
+          const unsigned long long keep = l2_keep_policy();
 #pragma unroll
-          for (int k = 0; k < 8; k++) dst[32 * k + lane] = vox[k];
+          for (int k = 0; k < 8; k++) st_keep(dst + 32 * k + lane, vox[k], keep);
           if (lane == 0) { a.stage_cell[slot] = ci; a.stage_src[slot] = src; }
         }
         tag = TAG_STAGED | (slot & 0x3fffffffu);
@@ -1331,19 +1473,27 @@ void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEve
   if (mode == 1) {
     launch_pdl(classify_kernel<1>, dim3(grid(PX_CLASSIFY_MINB)), dim3(256), 0, s, a);
     launch_pdl(sub_kernel<1>, dim3(grid(PX_SUB_MINB)), dim3(256), 0, s, a);
-    if (a.validate) launch_pdl(voxel_simple_kernel<true>, dim3(grid(PX_VSIMPLE_MINB)), dim3(256), 0, s, a);
-    else launch_pdl(voxel_simple_kernel<false>, dim3(grid(PX_VSIMPLE_MINB)), dim3(256), 0, s, a);
-    launch_pdl(voxel_kernel<1, 1>, dim3(grid(PX_VOXEL_MINB)), dim3(256), 0, s, a);
+    if (a.vq_nonempty & (1u << VQ_NARROW)) {
+      if (a.validate) launch_pdl(voxel_lean_kernel<true, VQ_NARROW>, dim3(grid(PX_VSIMPLE_MINB)), dim3(256), 0, s, a);
+      else launch_pdl(voxel_lean_kernel<false, VQ_NARROW>, dim3(grid(PX_VSIMPLE_MINB)), dim3(256), 0, s, a);
+    }
+    if (a.vq_nonempty & (1u << VQ_AFFINE)) {
+      if (a.validate) launch_pdl(voxel_lean_kernel<true, VQ_AFFINE>, dim3(grid(PX_VAFF_MINB)), dim3(256), 0, s, a);
+      else launch_pdl(voxel_lean_kernel<false, VQ_AFFINE>, dim3(grid(PX_VAFF_MINB)), dim3(256), 0, s, a);
+    }
+    if (a.vq_nonempty & (1u << VQ_WIDE)) {
+      if (a.validate) launch_pdl(voxel_lean_kernel<true, VQ_WIDE>, dim3(grid(PX_VWIDE_MINB)), dim3(256), 0, s, a);
+      else launch_pdl(voxel_lean_kernel<false, VQ_WIDE>, dim3(grid(PX_VWIDE_MINB)), dim3(256), 0, s, a);
+    }
+    launch_pdl(voxel_kernel<1, VQ_GENERIC, VQ_GENERIC>, dim3(grid(PX_VOXEL_MINB)), dim3(256), 0, s, a);
   } else {
     launch_pdl(classify_kernel<0>, dim3(grid(PX_CLASSIFY64_MINB)), dim3(256), 0, s, a);
     launch_pdl(sub_kernel<0>, dim3(grid(PX_CLASSIFY64_MINB)), dim3(256), 0, s, a);
-    launch_pdl(voxel_kernel<0, 0>, dim3(grid(PX_CLASSIFY64_MINB)), dim3(256), 0, s, a);
-    launch_pdl(voxel_kernel<0, 1>, dim3(grid(PX_CLASSIFY64_MINB)), dim3(256), 0, s, a);
+    launch_pdl(voxel_kernel<0, VQ_NARROW, VQ_GENERIC>, dim3(grid(PX_CLASSIFY64_MINB)), dim3(256), 0, s, a);
   }
-  if (a.n_paint_slots) {
-    if (mode == 1) launch_pdl(paint_kernel<1>, dim3(grid(4)), dim3(256), 0, s, a);
-    else launch_pdl(paint_kernel<0>, dim3(grid(4)), dim3(256), 0, s, a);
-  }
+  // the mixed form's paint pass also resolves the lean voxel kernels' rescue list
+  if (mode == 1) launch_pdl(paint_kernel<1>, dim3(grid(4)), dim3(256), 0, s, a);
+  else if (a.n_paint_slots) launch_pdl(paint_kernel<0>, dim3(grid(4)), dim3(256), 0, s, a);
   if (mid) cudaEventRecord(mid, s);
   if (s_apply != s) {  // the apply pass waits for these passes on its own stream
     cudaEventRecord(eval_done, s);
@@ -2117,6 +2267,15 @@ __global__ void __launch_bounds__(256) finalize_kernel(FinalizeArgs a) {
         d4[lane] = v[q][0];
         d4[lane + 32] = v[q][1];
         if (lane == 0) a.pcount[di] = (uint16_t)((cnt2[q >> 1] >> (16 * (q & 1))) & 0xffffu);
+      }
+      // every lane's loads of these staged bricks have returned (their values are
+      // stored): their eight 128-byte lines each leave L2 unwritten
+      __syncwarp();
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        if (src_l[q] < 0) continue;
+        const uint32_t sl = __shfl_sync(FULLMASK, slot, src_l[q]);
+        if (lane < 8) l2_discard_line(a.staging32 + (size_t)sl * 256 + 32 * lane);
       }
     }
   }

@@ -16,6 +16,7 @@
 // [-1, 1]) and sin is 1-Lipschitz, so |sin(t) - sinf(m)| <= |t - m| + 2^-22;
 // the enclosure uses the interval's full width plus 2^-21.
 #pragma once
+#include "paint.cuh"
 #include "px_internal.cuh"
 #include "sdf32.cuh"
 
@@ -76,6 +77,34 @@ __device__ __forceinline__ int or3(int a, int b) { return (a == 1 || b == 1) ? 1
 
 __device__ __forceinline__ uint32_t vox32(float mat, float shade) {
   return ((uint32_t)(int)mat & 0xffu) | (((uint32_t)(int)shade & 0xffu) << 8);
+}
+
+// The synthetic scenes' noise paint (PK_NOISE, paint.cuh) from the voxel's
+// indices, in float32 with the float64 path's results: the float32 roundings of
+// the voxel centre's float64 coordinates come from the world's axis tables, and
+// floor(x * scale) from a float32 enclosure of the float64 product when no
+// integer lies inside it (false: the float64 path decides).  q: seed bits,
+// [scale] enclosure, fx, fy, fz and the threshold as float32, the two values.
+__device__ __forceinline__ bool noise32(const float2* __restrict__ q, float fx, float fy, float fz, uint32_t& out) {
+  const float2 sc = __ldg(q + 1);
+  // the float64 coordinate lies in [pred(f), succ(f)] of its rounding f > 0; the
+  // product's float64 rounding lies in the directed float32 bounds of that box
+  auto cell = [&](float f, uint32_t& c) {
+    const float a = floorf(__fmul_rd(__int_as_float(__float_as_int(f) - 1), sc.x));
+    const float b = floorf(__fmul_ru(__int_as_float(__float_as_int(f) + 1), sc.y));
+    c = (uint32_t)(int)a;
+    return a == b && a < 16777216.f;
+  };
+  uint32_t ix, iy, iz;
+  const bool okx = cell(fx, ix), oky = cell(fy, iy), okz = cell(fz, iz);
+  if (!(okx && oky && okz)) return false;
+  const uint32_t h = noise_hash(ix, iy, iz, __float_as_uint(__ldg(q).x));
+  const float jitter = __fmul_rn((float)(h & 0xffffu), 1.0f / 65536.0f);
+  const float2 f01 = __ldg(q + 2), f23 = __ldg(q + 3);
+  const float t = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(fx, f01.x), __fmul_rn(fy, f01.y)), __fmul_rn(fz, f23.x)), jitter);
+  const float2 vals = __ldg(q + 4);
+  out = sin_poly_f32(t) > f23.y ? __float_as_uint(vals.x) : __float_as_uint(vals.y);
+  return true;
 }
 
 // Float32 parameter blocks (written by the host, paint_params32 in px_api.cu),

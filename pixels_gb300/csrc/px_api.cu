@@ -123,13 +123,15 @@ struct px_world {
   } q, last_q;
   std::vector<uint8_t> h_op_bucket;  // per op: cost bucket (0..63) of one evaluation
   uint8_t class_order[VCLASSES] = {0};  // sub-block class order of the resident ops
-  uint8_t vclass_order[VQ_CLASSES] = {0};  // voxel class order (each half on its own)
+  uint8_t vclass_order[VQ_CLASSES] = {0};  // voxel class order (each group on its own)
+  uint32_t vq_nonempty = 0;                // bit g: voxel group g has ops
   DevBuf paint_items, pvals;    // sub-blocks to paint and the paint values
   DevBuf bmark, work;           // bricks the apply pass visits (bitmap, list)
   DevBuf scan_agg;
   DevBuf work_counter;
   DevBuf res;
   DevBuf opaque, udens, super_counts, density;
+  DevBuf axis32;  // float32 roundings of the voxel centres' coordinates: x, then y, then z
   // derive on build (px_set_derive_on_build): every build ends with the derived
   // upload buffers and the GPU free list for a device limit of derive_max bricks
   uint32_t derive_max = 0;
@@ -243,6 +245,148 @@ inline float ru32(double v) {
 }
 inline float2 enc(double v, double pad = 0.0) { return make_float2(rd32(v - pad), ru32(v + pad)); }
 
+// Runs of k >= 2 rotations (not all about y: those stay y-extruded) whose k ends
+// are consecutive instructions -- rotateZ(rotateY(rotateZ(shape))) and the like:
+// flag[first rotation] = C32_AFFINE | k; the run's other rotations and its ends
+// but the first, C32_SKIP.
+void rotation_runs(const uint32_t* code, uint32_t n, std::vector<uint32_t>& flag) {
+  auto is_rot = [](uint32_t op) { return op == OP_ROT_X || op == OP_ROT_Y || op == OP_ROT_Z; };
+  std::vector<int> close(n, -1), stack;
+  for (uint32_t i = 0; i < n; i++) {
+    const uint32_t op = code[2 * i] & 0xffu;
+    if (is_rot(op)) stack.push_back((int)i);
+    else if (op == OP_ROT_END && !stack.empty()) { close[stack.back()] = (int)i; stack.pop_back(); }
+  }
+  for (uint32_t i = 0; i < n; i++) {
+    if (!is_rot(code[2 * i] & 0xffu) || (i && is_rot(code[2 * (i - 1)] & 0xffu))) continue;
+    uint32_t k = 0;
+    bool all_y = true;
+    while (i + k < n && is_rot(code[2 * (i + k)] & 0xffu)) { all_y = all_y && (code[2 * (i + k)] & 0xffu) == OP_ROT_Y; k++; }
+    if (k < 2 || all_y || k > 255) continue;
+    const int e0 = close[i + k - 1];
+    bool consecutive = e0 >= 0;
+    for (uint32_t j = 0; j < k && consecutive; j++) consecutive = close[i + k - 1 - j] == e0 + (int)j;
+    if (!consecutive) continue;
+    flag[i] = C32_AFFINE | k;
+    for (uint32_t j = 1; j < k; j++) flag[i + j] = C32_SKIP;
+    for (uint32_t j = 1; j < k; j++) flag[(uint32_t)e0 + j] = C32_SKIP;
+  }
+}
+
+// The k rotations from instruction i composed into x' = M x + t (shapes.ts:263-320:
+// each maps the point about its pivot with its float64 cos and sin), in the op's
+// anchor coordinates, as float32 intervals: M row by row, then t.  The exact map
+// is the composition of the exact rotations on those float64 constants; the
+// float64 arithmetic here errs by far less than the padding.
+bool compose_rotations(const uint32_t* code, uint32_t i, uint32_t k, const double* P, const double A[3],
+                       std::vector<float2>& p32) {
+  double M[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}}, t[3] = {0, 0, 0};
+  double mag = 0;  // a bound of the magnitudes summed into t
+  for (uint32_t j = 0; j < k; j++) {  // the outermost rotation acts first on the point
+    const uint32_t op = code[2 * (i + j)] & 0xffu;
+    const double* q = P + code[2 * (i + j) + 1];
+    const double p0 = q[0], p1 = q[1], c = q[2], sn = q[3];
+    double R[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}}, b[3] = {0, 0, 0};
+    int u = 0, v = 2;  // the rotated axes: x' about (u, v) = (p0, p1)
+    if (op == OP_ROT_X) { u = 1; v = 2; } else if (op == OP_ROT_Z) { u = 0; v = 1; }
+    R[u][u] = c; R[u][v] = sn; R[v][u] = -sn; R[v][v] = c;
+    b[u] = p0 - c * p0 - sn * p1;
+    b[v] = p1 + sn * p0 - c * p1;
+    mag += std::fabs(p0) + std::fabs(p1);
+    double M2[3][3], t2[3];
+    for (int r = 0; r < 3; r++) {
+      t2[r] = b[r];
+      for (int cc = 0; cc < 3; cc++) {
+        M2[r][cc] = 0;
+        for (int m = 0; m < 3; m++) M2[r][cc] += R[r][m] * M[m][cc];
+        t2[r] += R[r][cc] * t[cc];
+      }
+    }
+    std::memcpy(M, M2, sizeof M);
+    std::memcpy(t, t2, sizeof t);
+  }
+  bool ok = true;
+  const double padM = 0x1p-44 * (double)k, amag = std::fabs(A[0]) + std::fabs(A[1]) + std::fabs(A[2]);
+  const double padT = (mag * 3 + amag * 3 + 1.0) * 0x1p-44 * (double)k;
+  for (int r = 0; r < 3; r++)
+    for (int cc = 0; cc < 3; cc++) {
+      const float2 e = enc(M[r][cc], padM);
+      if (!std::isfinite(e.x) || !std::isfinite(e.y)) ok = false;
+      p32.push_back(e);
+    }
+  for (int r = 0; r < 3; r++) {  // x' - A = M (X + A) + t - A in anchor coordinates X = x - A
+    double tr = t[r] - A[r];
+    for (int cc = 0; cc < 3; cc++) tr += M[r][cc] * A[cc];
+    const float2 e = enc(tr, padT);
+    if (!std::isfinite(e.x) || !std::isfinite(e.y) || std::fabs(tr) > 4 * MIXED_MAX_COORD) ok = false;
+    p32.push_back(e);
+  }
+  return ok;
+}
+
+// The lean voxel kernel's reading of a program (LP_* forms in px_internal.cuh), or
+// lp[LP_FORM] = 0.  A stage is one rotation, or a run composed by rotation_runs.
+void lean_program(const uint32_t* code, uint32_t n, uint8_t lp[8]) {
+  if (n > 40) return;
+  std::vector<uint32_t> flag(n, 0u);
+  rotation_runs(code, n, flag);
+  auto op_at = [&](uint32_t i) { return code[2 * i] & 0xffu; };
+  auto is_prim = [&](uint32_t i) { return i < n && op_at(i) >= OP_BOX && op_at(i) < OP_ROT_X; };
+  auto is_rot = [&](uint32_t i) { return i < n && (op_at(i) == OP_ROT_X || op_at(i) == OP_ROT_Y || op_at(i) == OP_ROT_Z); };
+  // a stage at i: returns its kind and instruction count, and the ends it needs
+  auto stage = [&](uint32_t i, uint32_t& kind, uint32_t& len) {
+    kind = 0; len = 0;
+    if (!is_rot(i)) return true;
+    if (flag[i] & C32_AFFINE) { kind = LP_AFFINE; len = flag[i] & 0xffu; return true; }
+    if (is_rot(i + 1)) return false;  // an uncomposed run (all about y): not a lean program
+    kind = op_at(i) - OP_ROT_X + 1; len = 1;
+    return true;
+  };
+  auto ends = [&](uint32_t i, uint32_t len) {
+    for (uint32_t j = 0; j < len; j++) if (i + j >= n || op_at(i + j) != OP_ROT_END) return false;
+    return true;
+  };
+  auto comb_of = [&](uint32_t i) -> uint32_t {
+    if (i >= n) return 0;
+    const uint32_t o = op_at(i);
+    return o == OP_NEGMAX ? LP_NEGMAX : o == OP_MAX ? LP_MAX : o == OP_MIN ? LP_MIN : 0;
+  };
+  uint32_t k1, l1;
+  if (!stage(0, k1, l1)) return;
+  uint32_t i = l1;
+  if (!is_prim(i)) return;
+  const uint32_t p1 = i++;
+  uint32_t form = 1, p2 = LP_NONE, s2 = LP_NONE, k2 = 0, comb = 0;
+  if (is_prim(i) && comb_of(i + 1)) {  // form 2: both primitives in the one stage
+    form = 2; p2 = i; comb = comb_of(i + 1); i += 2;
+    if (!ends(i, l1)) return;
+    i += l1;
+  } else {
+    if (!ends(i, l1)) return;
+    i += l1;
+    uint32_t l2;
+    if (i < n && (is_rot(i) || is_prim(i))) {  // form 3: a second staged primitive, then comb
+      if (!stage(i, k2, l2)) return;
+      s2 = i; i += l2;
+      if (!is_prim(i)) return;
+      p2 = i++;
+      if (!ends(i, l2)) return;
+      i += l2;
+      comb = comb_of(i);
+      if (!comb) return;
+      i++;
+      form = 3;
+    }
+  }
+  uint32_t off = LP_NONE;
+  if (i < n && op_at(i) == OP_OFFSET) off = i++;
+  if (i != n) return;
+  lp[LP_FORM] = (uint8_t)form; lp[LP_COMB] = (uint8_t)comb;
+  lp[LP_P1] = (uint8_t)p1; lp[LP_P2] = (uint8_t)p2;
+  lp[LP_S1] = l1 ? 0 : LP_NONE; lp[LP_S2] = (uint8_t)(k2 ? s2 : LP_NONE);
+  lp[LP_KINDS] = (uint8_t)(k1 | (k2 << 4)); lp[LP_OFF] = (uint8_t)off;
+}
+
 // Convert one op's SDF parameters to float32 intervals relative to the op's
 // anchor.  Positions are shifted by the anchor; reciprocals (1/r, 1/|e|^2)
 // replace the divisions; polygon edges are expanded to per-vertex records.
@@ -280,9 +424,21 @@ bool convert32(const uint32_t* code, uint32_t n, const double* P, const double A
       p32.push_back(e);
     }
   };
+  // runs of rotations whose ends follow each other: composed into one affine map
+  std::vector<uint32_t> flag(n, 0u);
+  rotation_runs(code, n, flag);
   for (uint32_t i = 0; i < n; i++) {
     uint32_t op = code[2 * i] & 0xffu, cnt = code[2 * i] >> 8;
     const double* p = P + code[2 * i + 1];
+    if (flag[i] & C32_SKIP) {
+      code32.push_back(C32_SKIP);
+      continue;
+    }
+    if (flag[i] & C32_AFFINE) {
+      code32.push_back(C32_AFFINE | (uint32_t)p32.size());
+      if (!compose_rotations(code, i, flag[i] & 0xffu, P, A, p32)) ok = false;
+      continue;
+    }
     code32.push_back((uint32_t)p32.size());
     switch (op) {
       case OP_BOX: pos(p[0], 0); pos(p[1], 1); pos(p[2], 2); val(p[3]); val(p[4]); val(p[5]); break;
@@ -497,6 +653,18 @@ static int world_create_impl(int dx, int dy, int dz, double vpm, uint32_t initia
   ensure(w, w->udens, 256);
   cudaMemcpy(w->opaque.p, op_tab, 256, cudaMemcpyHostToDevice);
   cudaMemcpy(w->udens.p, ud_tab, 256, cudaMemcpyHostToDevice);
+  {  // the voxel centres' coordinates as the paint calls form them, (i + 0.5) * vs, rounded to float32
+    std::vector<float> ax((size_t)dx + dy + dz);
+    size_t at = 0;
+    for (int n : {dx, dy, dz})
+      for (int i = 0; i < n; i++) ax[at++] = (float)(((double)i + 0.5) * w->vs);
+    if ((rc = ensure(w, w->axis32, ax.size() * 4)) != PX_OK ||
+        cudaMemcpy(w->axis32.p, ax.data(), ax.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+      cudaGetLastError();
+      px_world_destroy(w);
+      return rc ? rc : PX_E_CUDA;
+    }
+  }
   *out = w;
   return PX_OK;
 }
@@ -544,6 +712,20 @@ void px_world_destroy(px_world* w) {
 // op, relative to its anchor A.  Returns false (float64 only) for a paint
 // frame or values outside the certified range.
 bool paint_params32(uint32_t kind, bool framed, const double* p, const double A[3], std::vector<float2>& out) {
+  if (kind == PK_NOISE && !framed) {  // noise32: the float32 values the float64 path converts to
+    const double sc = p[1];
+    const float sl = rd32(sc), sh = ru32(sc);
+    if (!(sl > 0.f) || !std::isfinite(sh)) return false;
+    for (int k : {6, 7})
+      if (!(p[k] >= 0 && p[k] <= 65535.0 && p[k] == std::floor(p[k]))) return false;
+    auto bits = [](uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; };
+    out.push_back(make_float2(bits((uint32_t)(long long)p[0]), 0.f));
+    out.push_back(make_float2(sl, sh));
+    out.push_back(make_float2((float)p[2], (float)p[3]));
+    out.push_back(make_float2((float)p[4], (float)p[5]));
+    out.push_back(make_float2(bits((uint32_t)p[6]), bits((uint32_t)p[7])));
+    return true;
+  }
   if (framed || (kind != PK_TUFTED && kind != PK_PAINTING && kind != PK_VASE)) return false;
   if (kind == PK_VASE && !(p[3] > 0x1p-20 && p[3] < 0x1p20)) return false;
   bool ok = true;
@@ -834,24 +1016,23 @@ int convert_ops(const px_world* w, const IrOp* iops, size_t i0, size_t i1, const
           ysep = ysep && op_is_y_separable(code[2 * ((size_t)o.code_begin + k)] & 0xffu);
         if (ysep) d.flags |= OPF_Y_SEPARABLE;
         d.vclass = (first_prim & 15u) | (ysep && !(d.flags & OPF_FP64_ONLY) ? 16u : 0u);
-        // a single-primitive program: [rotation] primitive [rotation end] [offset]
-        d.simple = 0;
-        if (!(d.flags & (OPF_FP64_ONLY | OPF_DEEP))) {
-          uint32_t ops_[4] = {0, 0, 0, 0};
-          const uint32_t nc = o.code_len < 5 ? o.code_len : 0;
-          for (uint32_t k = 0; k < nc; k++) ops_[k] = code[2 * ((size_t)o.code_begin + k)] & 0xffu;
-          const bool rot = nc >= 3 && (ops_[0] == OP_ROT_X || ops_[0] == OP_ROT_Y || ops_[0] == OP_ROT_Z) &&
-                           ops_[1] < OP_ROT_X && ops_[1] >= OP_BOX && ops_[2] == OP_ROT_END;
-          const uint32_t np = rot ? 3 : 1;  // instructions before an offset
-          const bool prim_ok = rot || (nc >= 1 && ops_[0] >= OP_BOX && ops_[0] < OP_ROT_X);
-          if (prim_ok && (nc == np || (nc == np + 1 && ops_[np] == OP_OFFSET)))
-            d.simple = (rot ? ops_[1] : ops_[0]) | (rot ? ops_[0] << 8 : 0u) | (nc == np + 1 ? 1u << 16 : 0u);
-        }
-        d.vq_class = d.simple ? ((d.simple & 15u) | ((d.simple >> 8) ? 16u : 0u)) : 32u + d.vclass;
+        // a program of the lean voxel kernel (LP_* forms)
+        for (int k = 0; k < 8; k++) d.lp[k] = 0;
+        if (!(d.flags & (OPF_FP64_ONLY | OPF_DEEP))) lean_program(code + 2 * (size_t)o.code_begin, o.code_len, d.lp);
+        // the voxel queue's group and class: one primitive under at most one rotation
+        // (by primitive and rotation), the other lean forms (by first primitive and
+        // form), the interpreter's programs (by sub-block class)
+        const uint32_t p1op = d.lp[LP_FORM] ? code[2 * ((size_t)o.code_begin + d.lp[LP_P1])] & 15u : 0u;
+        const uint32_t k1 = d.lp[LP_KINDS] & 15u;
+        if (d.lp[LP_FORM] == 1 && k1 != LP_AFFINE) d.vq_class = 32u * VQ_NARROW + (p1op | (k1 ? 16u : 0u));
+        else if (d.lp[LP_FORM] == 1) d.vq_class = 32u * VQ_AFFINE + p1op;
+        else if (d.lp[LP_FORM]) d.vq_class = 32u * VQ_WIDE + (p1op | (d.lp[LP_FORM] == 3 ? 16u : 0u));
+        else d.vq_class = 32u * VQ_GENERIC + d.vclass;
       }
       d.paint_slot = NO_SLOT;
       d.paint32_off = NO_SLOT;
-      if (!(d.flags & OPF_FP64_ONLY) && o.kind != KIND_CARVE && paint_is_heavy(o.paint_kind)) {
+      if (!(d.flags & OPF_FP64_ONLY) && o.kind != KIND_CARVE &&
+          (paint_is_heavy(o.paint_kind) || o.paint_kind == PK_NOISE)) {
         const size_t at = out.p32.size();
         if (paint_params32(o.paint_kind, (o.flags & OPF_PAINT_FRAME) != 0, P + o.paint_param, d.anchor, out.p32))
           d.paint32_off = (uint32_t)at;  // + the chunk's float32 base (merge)
@@ -1049,6 +1230,7 @@ px_world* twin_create(px_world* w, uint64_t P, uint32_t max_ops, int* rc) {
   t->vpm = w->vpm; t->vs = w->vs; t->ncells = w->ncells; t->ntiles = w->ntiles; t->n_sms = w->n_sms;
   for (int k = 0; k < VCLASSES; k++) t->class_order[k] = w->class_order[k];
   for (int k = 0; k < VQ_CLASSES; k++) t->vclass_order[k] = w->vclass_order[k];
+  t->vq_nonempty = w->vq_nonempty;
   t->host_reads = w->host_reads;
   t->validate = w->validate;
   t->rescue_cap = w->rescue_cap;
@@ -1064,6 +1246,7 @@ px_world* twin_create(px_world* w, uint64_t P, uint32_t max_ops, int* rc) {
   borrow(t->holes_a, w->holes_a);
   borrow(t->holes_b, w->holes_b);
   borrow(t->opaque, w->opaque);
+  borrow(t->axis32, w->axis32);
   borrow(t->udens, w->udens);
   if (cudaMallocHost((void**)&t->h_res, sizeof(BuildResult)) != cudaSuccess) {
     cudaGetLastError();
@@ -1476,17 +1659,21 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
     for (int k = 0; k < VCLASSES; k++) order[k] = k;
     std::stable_sort(order, order + VCLASSES, [&](int x, int y) { return cc[x] > cc[y]; });
     for (int k = 0; k < VCLASSES; k++) w->class_order[k] = (uint8_t)order[k];
-    int vorder[VQ_CLASSES];  // each half of the voxel classes costliest first
+    int vorder[VQ_CLASSES];  // each group of the voxel classes costliest first
     for (int k = 0; k < VQ_CLASSES; k++) vorder[k] = k;
-    for (int h = 0; h < 2; h++)
-      std::stable_sort(vorder + 32 * h, vorder + 32 * h + 32, [&](int x, int y) { return cv[x] > cv[y]; });
+    for (int g = 0; g < VQ_CLASSES / 32; g++)
+      std::stable_sort(vorder + 32 * g, vorder + 32 * g + 32, [&](int x, int y) { return cv[x] > cv[y]; });
     for (int k = 0; k < VQ_CLASSES; k++) w->vclass_order[k] = (uint8_t)vorder[k];
+    w->vq_nonempty = 0;
+    for (int i = 0; i < n_ops; i++)
+      if (w->ops[i].bx0 <= w->ops[i].bx1) w->vq_nonempty |= 1u << (w->ops[i].vq_class / 32);
     if ((rc = issue_uploads(w, ups, s))) return rc;
   }
   FoldArgs fa{};
   fa.chunk_order = (const uint2*)w->chunk_op.p;
   for (int k = 0; k < VCLASSES; k++) fa.class_order[k] = w->class_order[k];
   for (int k = 0; k < VQ_CLASSES; k++) fa.vclass_order[k] = w->vclass_order[k];
+  fa.vq_nonempty = w->vq_nonempty;
   fa.n_ops = (uint32_t)n_ops;
   fa.n_pairs = P;
   fa.pcode = (uint8_t*)w->pcode.p;
@@ -1496,7 +1683,7 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   fa.vitems = (uint4*)w->vitems.p;
   fa.vitems_cap = (uint32_t)(8 * P < 0xffffffffull ? 8 * P : 0xffffffffull);
   fa.vitem_counter = (uint32_t*)w->chunk_counter.p + 4;   // counters: [0] chunks, [1] paint taken,
-                                                          // [2] paint pushed, [4..70] voxel, [80..113] pairs
+                                                          // [2] paint pushed, [4..136] voxel, [160..193] pairs
   {  // per-class regions: the class's pairs (sub-block pass), 8 sub-blocks per pair (voxel pass)
     uint64_t per[VCLASSES] = {0}, vper[VQ_CLASSES] = {0};
     for (int i = 0; i < n_ops; i++) {
@@ -1504,7 +1691,7 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
       if (o.bx0 > o.bx1) continue;
       const uint64_t np = (uint64_t)o.nx * o.ny * (uint64_t)(o.bz1 - o.bz0 + 1);
       per[o.vclass & (VCLASSES - 1)] += np;
-      vper[o.vq_class & (VQ_CLASSES - 1)] += np;
+      vper[o.vq_class] += np;
     }
     uint64_t at = 0;
     for (int k = 0; k < VCLASSES; k++) {
@@ -1520,7 +1707,7 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
     }
   }
   fa.pitems = (uint2*)w->pitems.p;
-  fa.pitem_counter = (uint32_t*)w->chunk_counter.p + 80;
+  fa.pitem_counter = (uint32_t*)w->chunk_counter.p + 160;
   fa.rescue = (uint4*)w->rescue.p;
   fa.rescue_cap = w->rescue_cap;
   fa.paint_counter = (uint32_t*)w->chunk_counter.p + 1;
@@ -1547,6 +1734,9 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   fa.tile_boxes = (const uint2*)w->tile_boxes.p;
   fa.BX = w->BX; fa.BY = w->BY; fa.BZ = w->BZ; fa.TX = w->TX; fa.TY = w->TY;
   fa.vs = w->vs;
+  fa.ax32 = (const float*)w->axis32.p;
+  fa.ay32 = fa.ax32 + w->dx;
+  fa.az32 = fa.ay32 + w->dy;
   fa.grid = w->d_grid;
   fa.pool32 = w->d_pool32;
   fa.evt = (uint8_t*)w->evt.p;
@@ -1671,7 +1861,7 @@ static int build_finish_impl(px_world* w) {
     w->retries = 0;
     return fail(w, PX_E_QUEUE_OVERFLOW, "pipelined build failed: device status 0x%x", r.status);
   }
-  if ((r.status & ST_RESCUE_OVERFLOW) && w->retries < 2) {  // more voxels left to float64 than the list holds
+  if ((r.status & ST_RESCUE_OVERFLOW) && w->retries < 2) {  // more left to float64 than the rescue list holds
     CU(clear_poison());
     w->rescue_cap = std::max(w->rescue_cap, r.n_rescue + r.n_rescue / 4 + 1024);
     w->retries++;

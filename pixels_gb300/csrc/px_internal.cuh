@@ -80,10 +80,10 @@ struct OpDev {
   uint16_t paint_kind;
   uint32_t paint_value;
   uint32_t vclass;                       // sub-block work class (VCLASSES): first primitive, y-extruded
-  uint32_t vq_class;                     // voxel work class (VQ_CLASSES): [0, 32) single-primitive programs
-                                         // (voxel_simple_kernel), [32, 64) the others
-  uint32_t simple;                       // single-primitive program: primitive opcode | rotation opcode << 8
-                                         // (0: none) | 1 << 16 with an offset (0: not one)
+  uint32_t vq_class;                     // voxel work class (VQ_CLASSES): 32 per VQ_* group
+  // a program of the lean voxel kernel (LP_* forms; lp[LP_FORM] == 0: not one): instruction
+  // indices within the op of its primitives, stages and offset, and the stages' kinds
+  uint8_t lp[8];
   double bhd, shd;                       // brickHalfDiag, subHalfDiag (shapes.ts:349-350)
   double mn[3], mx[3];                   // contains box (boxes only)
   double frame[4];                       // paint frame px, pz, cos, sin
@@ -147,7 +147,7 @@ struct BuildResult {
   BuildCounters c;
   unsigned long long max_err_bits;  // max |mid(d32) - d64| over rescued evaluations (double bits, >= 0)
   uint32_t free_len;     // derive: length of the GPU free list (GpuWorld.ts:103-111, C_FREE_TOP)
-  uint32_t n_rescue;     // voxels the float32 pass left to float64 (voxel_simple_kernel), pushed
+  uint32_t n_rescue;     // voxels the float32 pass left to float64 (voxel_lean_kernel), pushed
   uint32_t h_before;     // holes before the build (from the WorldState)
   uint32_t u_before;     // poolUsed before the build
   uint32_t pad2;
@@ -161,27 +161,43 @@ enum : uint8_t { PC_SKIP = 0, PC_PARTIAL = 1, PC_FULL = 2 };
 // (its first primitive, and whether it runs the y-extruded evaluation), so
 // that warps draining a queue at the same time run the same code.
 constexpr int VCLASSES = 32;
-// The voxel queue has twice as many classes: single-primitive programs --
-// [rotation] primitive [rotation end] [offset] -- by primitive and rotation in
-// classes [0, 32), drained by a kernel without a value stack or rotation
-// frames; every other program by its sub-block class + 32.
-constexpr int VQ_CLASSES = 64;
-constexpr int VQ_SIMPLE_TAKEN = 1 + VQ_CLASSES;  // vitem_counter slot of the single-primitive kernel's tickets
+// The voxel queue has four groups of 32 classes, each drained by its own
+// kernel: VQ_NARROW, lean programs of one primitive under at most one rotation
+// (by primitive and rotation), VQ_AFFINE, one primitive under a composed run of
+// rotations (by primitive), VQ_WIDE, the two-primitive lean programs (by first
+// primitive and form), and VQ_GENERIC, every other program (by sub-block class),
+// drained by the interpreter kernel.
+enum { VQ_NARROW = 0, VQ_AFFINE = 1, VQ_WIDE = 2, VQ_GENERIC = 3 };
+constexpr int VQ_CLASSES = 128;
+constexpr int VQ_TAKEN = 1 + VQ_CLASSES;  // vitem_counter[VQ_TAKEN + group]: items the group's kernel took
+// Programs of the lean voxel kernel, by form:
+//   1  [stage] prim [stage end] [offset]
+//   2  [stage] prim prim comb [stage end] [offset]           (one stage for both)
+//   3  [stage] prim [stage end] [stage] prim [stage end] comb [offset]
+// A stage is one rotation (kind 1-3: about x, y, z) or a run of rotations the
+// float32 parameters hold composed into one affine map (kind 4); comb is a
+// subtract step, an intersection or a union.
+enum { LP_FORM, LP_COMB, LP_P1, LP_P2, LP_S1, LP_S2, LP_KINDS, LP_OFF };
+enum : uint8_t { LP_NEGMAX = 1, LP_MAX = 2, LP_MIN = 3, LP_NONE = 0xff, LP_AFFINE = 4 };
+// code32 flags of the float32 path: a run of rotations (not all about y) composed
+// into an affine map on its first rotation; its other rotations and all but the
+// first of its ends are skipped
+constexpr uint32_t C32_SKIP = 1u << 31, C32_AFFINE = 1u << 30, C32_OFF = (1u << 30) - 1;
 
 struct FoldArgs {
   const uint2* chunk_order;  // the 32-pair chunks in the order classify_kernel takes them (costliest ops
                              // first): (chunk, op containing its first pair | 1 << 31 when that op holds
                              // all of the chunk's pairs)
   uint8_t class_order[VCLASSES];  // the order the sub-block pass takes its classes in
-  uint8_t vclass_order[VQ_CLASSES];  // the order the voxel passes take theirs: [0, 32) the single-primitive
-                                     // classes, [32, 64) the others
+  uint8_t vclass_order[VQ_CLASSES];  // the order the voxel passes take theirs, group by group
+  uint32_t vq_nonempty;              // bit g: group g has work (its kernel is launched)
   uint32_t n_ops;
   unsigned long long n_pairs;
   uint8_t* pcode;             // per pair: PC_*
   uint16_t* psub;             // per partial pair: 2 bits per sub-block (PC_*)
   unsigned long long* pmask;  // per partial pair: 8 inside-masks (bit = x&3 | (y&3)<<2 | (z&3)<<4)
   uint32_t* chunk_counter;
-  // voxels whose float32 interval cannot decide them, left by voxel_simple_kernel
+  // voxels whose float32 interval cannot decide them, left by voxel_lean_kernel
   // to voxel_kernel<1, 1> (which carries the float64 evaluator): (op | voxel bit << 24 |
   // undecided-crossing-test << 30, pair << 3 | sub-block, interval lo, hi bits)
   uint4* rescue;
@@ -189,8 +205,7 @@ struct FoldArgs {
   uint4* vitems;              // partial sub-blocks to classify voxel by voxel: (op, pair << 3 | sub,
                               // bits of the centre value's enclosure lo, hi)
   uint32_t vitems_cap;
-  uint32_t* vitem_counter;    // [0] items taken by voxel_kernel's second half, [1 + k] items pushed to class k,
-                              // [VQ_SIMPLE_TAKEN] items taken from the first half
+  uint32_t* vitem_counter;    // [1 + k] items pushed to class k, [VQ_TAKEN + g] items taken from group g
   uint32_t vq_base[VQ_CLASSES], vq_cap[VQ_CLASSES];  // per-class regions of vitems
   uint2* pitems;              // partial pairs for the sub-block pass: (op, pair)
   uint32_t* pitem_counter;    // [0] items taken, [1 + k] items pushed to class k
@@ -213,6 +228,8 @@ struct FoldArgs {
   const float2* p32;          // float32 interval parameters (lo, hi)
   const float2* bases;        // per op and axis: (b*8 + 0.5)*vs - anchor as a float32 interval
   float vs_lo, vs_hi;         // float32 enclosure of the voxel size
+  // float32 roundings of the voxel centres' float64 coordinates ((i + 0.5) * vs), per axis
+  const float *ax32, *ay32, *az32;
   int validate;               // mixed mode: also evaluate float64 everywhere and count violations
   const uint32_t* tile_off;
   const uint32_t* tile_cnt;

@@ -69,6 +69,12 @@ __device__ __forceinline__ Iv icmul(Iv x, Iv c) {
   if (c.lo >= 0.f) return {__fmul_rd(x.lo, x.lo >= 0.f ? c.lo : c.hi), __fmul_ru(x.hi, x.hi >= 0.f ? c.hi : c.lo)};
   return {__fmul_rd(x.hi, x.hi >= 0.f ? c.lo : c.hi), __fmul_ru(x.lo, x.lo >= 0.f ? c.hi : c.lo)};
 }
+// x * c for any constant interval c (one that straddles zero is bounded by its magnitude)
+__device__ __forceinline__ Iv icmul_any(Iv x, Iv c) {
+  if (c.lo >= 0.f || c.hi <= 0.f) return icmul(x, c);
+  const float m = __fmul_ru(fmaxf(-c.lo, c.hi), fmaxf(fabsf(x.lo), fabsf(x.hi)));
+  return {-m, m};
+}
 __device__ __forceinline__ Iv ilen2(Iv a, Iv b) { return isqrt(iadd(isqr(a), isqr(b))); }
 __device__ __forceinline__ Iv ilen3(Iv a, Iv b, Iv c) { return isqrt(iadd(iadd(isqr(a), isqr(b)), isqr(c))); }
 __device__ __forceinline__ Iv ldp(const Iv* p, int k) {
@@ -171,7 +177,21 @@ __device__ __forceinline__ Iv prim32(uint32_t op, int cnt, const Iv* __restrict_
   return {-INFINITY, INFINITY};
 }
 
-// code32[i] is the offset of instruction i's float32 parameters.
+// A run of rotations composed into x' = M x + t (code32 flag C32_AFFINE): p holds
+// M row by row, then t, as constant intervals.
+__device__ __forceinline__ void aff32(const Iv* __restrict__ p, Iv& x, Iv& y, Iv& z) {
+  Iv o[3];
+#pragma unroll
+  for (int r = 0; r < 3; r++)
+    o[r] = iadd(iadd(iadd(ldp(p, 9 + r), icmul_any(x, ldp(p, 3 * r))), icmul_any(y, ldp(p, 3 * r + 1))),
+                icmul_any(z, ldp(p, 3 * r + 2)));
+  x = o[0];
+  y = o[1];
+  z = o[2];
+}
+
+// code32[i] is the offset of instruction i's float32 parameters (C32_OFF bits),
+// with the flags of a composed run of rotations (C32_AFFINE, C32_SKIP).
 __device__ PX_SDF32I_INLINE Iv sdf32i(const uint2* __restrict__ code, const uint32_t* __restrict__ code32, int n,
                                   const Iv* __restrict__ P, Iv x, Iv y, Iv z, float M, bool& amb) {
   Iv s0 = {0.f, 0.f}, s1 = s0, s2 = s0, s3 = s0;
@@ -180,7 +200,9 @@ __device__ PX_SDF32I_INLINE Iv sdf32i(const uint2* __restrict__ code, const uint
     const uint32_t w0 = __ldg(&code[i].x);
     const uint32_t op = w0 & 0xffu;
     const int cnt = (int)(w0 >> 8);
-    const Iv* p = P + __ldg(code32 + i);
+    const uint32_t c32 = __ldg(code32 + i);
+    if (c32 & C32_SKIP) continue;
+    const Iv* p = P + (c32 & C32_OFF);
     if (op < OP_ROT_X) {
       Iv v = prim32(op, cnt, p, x, y, z, M, amb);
       s3 = s2; s2 = s1; s1 = s0; s0 = v;
@@ -189,6 +211,10 @@ __device__ PX_SDF32I_INLINE Iv sdf32i(const uint2* __restrict__ code, const uint
     switch (op) {
       case OP_ROT_X: case OP_ROT_Y: case OP_ROT_Z: {
         ax2 = ax1; ay2 = ay1; az2 = az1; ax1 = ax0; ay1 = ay0; az1 = az0; ax0 = x; ay0 = y; az0 = z;
+        if (c32 & C32_AFFINE) {
+          aff32(p, x, y, z);
+          break;
+        }
         Iv p0 = ldp(p, 0), p1 = ldp(p, 1), c = ldp(p, 2), sn = ldp(p, 3);
         if (op == OP_ROT_Y) {
           Iv dx = isub(x, p0), dz = isub(z, p1);
@@ -308,7 +334,7 @@ __device__ __forceinline__ Iv2 sdf32i_y2(const uint2* __restrict__ code, const u
     const uint32_t w0 = __ldg(&code[i].x);
     const uint32_t op = w0 & 0xffu;
     const int cnt = (int)(w0 >> 8);
-    const Iv* p = P + __ldg(code32 + i);
+    const Iv* p = P + (__ldg(code32 + i) & C32_OFF);  // no composed runs in y-extruded programs
     switch (op) {
       case OP_ROT_Y: {  // rotations about y keep y: x and z only
         ax2 = ax1; az2 = az1; ax1 = ax0; az1 = az0; ax0 = x; az0 = z;

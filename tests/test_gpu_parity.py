@@ -124,6 +124,21 @@ def test_synthetic_4096_vpm80_bit_exact(built_lib, mode):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("seed,n,vpm", [(2, 1024, 40.0), (3, 256, 80.0)])
+def test_synthetic_validation_mode(built_lib, seed, n, vpm):
+    """Validation mode on synthetic scenes: every float32 enclosure of the rotated
+    and composed programs, and every float32 noise-paint value (cells from
+    enclosed products, coordinates from the axis tables), must agree with the
+    float64 evaluation; the build must be bit-exact."""
+    from pixels_gb300.scenes.synthetic import synthetic_program
+    prog = synthetic_program(seed, n, vpm)
+    o = pyoracle.OracleWorld(prog.to_bytes(), vpm, config.Config(vpm).dims, threads=THREADS)
+    w = build_gpu(vpm, MODE_MIXED, program=prog, validate=True)
+    assert w.stats()["violations"] == 0
+    assert_same_world(w, o)
+
+
+@pytest.mark.gpu
 def test_derive_on_build_matches_derive_on_read(built_lib):
     """The derived buffers the build leaves on the device equal those px_derive
     computes from the built world, and survive a rebuild."""
