@@ -120,71 +120,81 @@ __device__ __forceinline__ bool box_overlaps_tile(uint2 b, int tx, int ty, int t
 // tests the 32-op groups first and only the ops of groups that overlap its
 // tile (a two-level culling hierarchy; scene ops come object by object, so
 // groups are compact).
-__global__ void __launch_bounds__(256) cull_count_kernel(const uint2* __restrict__ boxes, int n_ops, int TX, int TY, int TZ,
-                                                         uint32_t* tile_cnt) {
+// One warp per tile, eight tiles per block: the tile's ops are counted, the
+// block reserves room for its eight lists with one atomic, and each warp writes
+// its list (op order) and the op boxes beside it.  The lists lie in reservation
+// order; tile_off / tile_cnt locate them.
+__global__ void __launch_bounds__(256) cull_kernel(const uint2* __restrict__ boxes, int n_ops, int TX, int TY, int TZ,
+                                                   uint32_t* tile_cnt, uint32_t* tile_off, uint32_t* tile_ops,
+                                                   uint2* tile_boxes, uint32_t* counter) {
   pdl_prologue();
-  const int lane = threadIdx.x & 31;
+  __shared__ uint32_t s_cnt[8], s_base;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int n_tiles = TX * TY * TZ;
   const int n_groups = (n_ops + 31) / 32;
   const uint2* __restrict__ gboxes = boxes + n_ops;
-  for (int tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; tile < n_tiles; tile += (gridDim.x * blockDim.x) >> 5) {
-    int tz = tile / (TX * TY), r = tile - tz * TX * TY, ty = r / TX, tx = r - ty * TX;
-    uint32_t cnt = 0;
+  const int tile = blockIdx.x * 8 + warp;
+  const bool valid = tile < n_tiles;
+  int tz = 0, ty = 0, tx = 0;
+  if (valid) {
+    tz = tile / (TX * TY);
+    const int r = tile - tz * TX * TY;
+    ty = r / TX;
+    tx = r - ty * TX;
+  }
+  uint32_t cnt = 0;
+  if (valid) {
     for (int g0 = 0; g0 < n_groups; g0 += 32) {
       const int gi = g0 + lane;
       uint32_t gm = __ballot_sync(FULLMASK, gi < n_groups && box_overlaps_tile(__ldg(gboxes + gi), tx, ty, tz));
       while (gm) {
         const int i = (g0 + __ffs(gm) - 1) * 32 + lane;
         gm &= gm - 1;
-        bool ov = i < n_ops && box_overlaps_tile(__ldg(boxes + i), tx, ty, tz);
+        const bool ov = i < n_ops && box_overlaps_tile(__ldg(boxes + i), tx, ty, tz);
         cnt += __popc(__ballot_sync(FULLMASK, ov));
       }
     }
-    if (lane == 0) tile_cnt[tile] = cnt;
   }
-}
-
-__global__ void __launch_bounds__(256) cull_fill_kernel(const uint2* __restrict__ boxes, int n_ops, int TX, int TY, int TZ,
-                                                        const uint32_t* __restrict__ tile_off, uint32_t* tile_ops,
-                                                        uint2* tile_boxes) {
-  pdl_prologue();
-  const int lane = threadIdx.x & 31;
-  const int n_tiles = TX * TY * TZ;
-  const int n_groups = (n_ops + 31) / 32;
-  const uint2* __restrict__ gboxes = boxes + n_ops;
-  for (int tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; tile < n_tiles; tile += (gridDim.x * blockDim.x) >> 5) {
-    int tz = tile / (TX * TY), r = tile - tz * TX * TY, ty = r / TX, tx = r - ty * TX;
-    uint32_t pos = tile_off[tile];
-    for (int g0 = 0; g0 < n_groups; g0 += 32) {
-      const int gi = g0 + lane;
-      uint32_t gm = __ballot_sync(FULLMASK, gi < n_groups && box_overlaps_tile(__ldg(gboxes + gi), tx, ty, tz));
-      while (gm) {
-        const int i = (g0 + __ffs(gm) - 1) * 32 + lane;
-        gm &= gm - 1;
-        const uint2 b = i < n_ops ? __ldg(boxes + i) : make_uint2(3u << 30, 0u);
-        bool ov = i < n_ops && box_overlaps_tile(b, tx, ty, tz);
-        uint32_t m = __ballot_sync(FULLMASK, ov);
-        if (ov) {
-          const uint32_t at = pos + __popc(m & ((1u << lane) - 1u));
-          tile_ops[at] = (uint32_t)i;
-          tile_boxes[at] = b;  // the op's brick box beside it, for the apply pass
-        }
-        pos += __popc(m);
+  if (lane == 0) s_cnt[warp] = cnt;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t sum = 0;
+    for (int k = 0; k < 8; k++) sum += s_cnt[k];
+    s_base = sum ? atomicAdd(counter, sum) : 0u;
+  }
+  __syncthreads();
+  if (!valid) return;
+  uint32_t pos = s_base;
+  for (int k = 0; k < warp; k++) pos += s_cnt[k];
+  if (lane == 0) {
+    tile_cnt[tile] = cnt;
+    tile_off[tile] = pos;
+  }
+  if (!cnt) return;
+  for (int g0 = 0; g0 < n_groups; g0 += 32) {
+    const int gi = g0 + lane;
+    uint32_t gm = __ballot_sync(FULLMASK, gi < n_groups && box_overlaps_tile(__ldg(gboxes + gi), tx, ty, tz));
+    while (gm) {
+      const int i = (g0 + __ffs(gm) - 1) * 32 + lane;
+      gm &= gm - 1;
+      const uint2 b = i < n_ops ? __ldg(boxes + i) : make_uint2(3u << 30, 0u);
+      const bool ov = i < n_ops && box_overlaps_tile(b, tx, ty, tz);
+      const uint32_t m = __ballot_sync(FULLMASK, ov);
+      if (ov) {
+        const uint32_t at = pos + __popc(m & ((1u << lane) - 1u));
+        tile_ops[at] = (uint32_t)i;
+        tile_boxes[at] = b;  // the op's brick box beside it, for the apply pass
       }
+      pos += __popc(m);
     }
   }
 }
 
-void launch_cull_count(const uint2* boxes, int n_ops, int TX, int TY, int TZ, uint32_t* tile_cnt, cudaStream_t s) {
-  int n_tiles = TX * TY * TZ;
-  int blocks = (n_tiles * 32 + 255) / 256;
-  launch_pdl(cull_count_kernel, dim3(blocks), dim3(256), 0, s, boxes, n_ops, TX, TY, TZ, tile_cnt);
-}
-void launch_cull_fill(const uint2* boxes, int n_ops, int TX, int TY, int TZ, const uint32_t* tile_off,
-                      uint32_t* tile_ops, uint2* tile_boxes, cudaStream_t s) {
-  int n_tiles = TX * TY * TZ;
-  int blocks = (n_tiles * 32 + 255) / 256;
-  launch_pdl(cull_fill_kernel, dim3(blocks), dim3(256), 0, s, boxes, n_ops, TX, TY, TZ, tile_off, tile_ops, tile_boxes);
+void launch_cull(const uint2* boxes, int n_ops, int TX, int TY, int TZ, uint32_t* tile_cnt, uint32_t* tile_off,
+                 uint32_t* tile_ops, uint2* tile_boxes, uint32_t* counter, cudaStream_t s) {
+  const int n_tiles = TX * TY * TZ;
+  launch_pdl(cull_kernel, dim3((n_tiles + 7) / 8), dim3(256), 0, s, boxes, n_ops, TX, TY, TZ, tile_cnt, tile_off,
+             tile_ops, tile_boxes, counter);
 }
 
 // ---------------------------------------------------------------------------
@@ -480,6 +490,73 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
   }
 }
 
+// The bricks the apply pass visits: those with a marked bit (one warp per 32
+// words of the bitmap, a warp-aggregated append), listed as packed brick
+// coordinates bx | by << 10 | bz << 20; bricks of tiles with more than 8 ops at
+// the front, the rest from the back.  Run by every warp of the sub-block pass
+// before its own work (the classify pass's bitmap is complete by then).
+__device__ __forceinline__ void mark_compact(const FoldArgs& a, uint32_t warp, uint32_t n_warps, int lane) {
+  const uint32_t BX = a.BX, BY = a.BY, TX = a.TX, TY = a.TY;
+  const uint32_t n_words = (uint32_t)(((size_t)a.BX * a.BY * a.BZ + 31) / 32);
+  const uint32_t last = (uint32_t)a.touched_cap;
+  uint32_t* const counts = a.work_counter + 1;
+  for (uint32_t w0 = warp * 32; w0 < n_words; w0 += n_warps * 32) {
+    const uint32_t wi = w0 + lane;
+    const uint32_t bits = wi < n_words ? __ldcg(a.bmark + wi) : 0u;
+    // split the word's bricks: those of tiles with more than 8 ops (the front) and the rest;
+    // the 32 bricks' coordinates stepped along x (no division per brick), their tile counts
+    // loaded together (an unrolled loop of independent loads)
+    uint32_t heavy = 0;
+    if (bits) {
+      const uint32_t ci0 = wi * 32u, byz0 = ci0 / BX;
+      uint32_t bx = ci0 - byz0 * BX, by = byz0 % BY, bz = byz0 / BY;
+#pragma unroll
+      for (int k = 0; k < 32; k++) {
+        if (((bits >> k) & 1u) &&
+            __ldg(a.tile_cnt + (bx >> 2) + TX * ((by >> 2) + TY * (bz >> 2))) > 8u)
+          heavy |= 1u << k;
+        if (++bx == BX) {
+          bx = 0;
+          if (++by == BY) { by = 0; bz++; }
+        }
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+      const uint32_t mine = e ? bits & ~heavy : heavy;
+      const uint32_t cnt = __popc(mine);
+      uint32_t incl = cnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(FULLMASK, incl, o);
+        if (lane >= o) incl += t;
+      }
+      const uint32_t total = __shfl_sync(FULLMASK, incl, 31);
+      uint32_t base = 0;
+      if (lane == 31 && total) {
+        base = atomicAdd(counts + e, total);
+        atomicAdd(&a.res->n_work, total);
+      }
+      base = __shfl_sync(FULLMASK, base, 31) + incl - cnt;
+      if (mine) {
+        const uint32_t ci0 = wi * 32u, byz0 = ci0 / BX;
+        const uint32_t bx0 = ci0 - byz0 * BX, by0 = byz0 % BY, bz0 = byz0 / BY;
+        for (uint32_t b = mine; b;) {
+          const int k = __ffs(b) - 1;
+          b &= b - 1;
+          uint32_t bx = bx0 + (uint32_t)k, by = by0, bz = bz0;
+          while (bx >= BX) {  // the word's bricks run on along x into the next rows
+            bx -= BX;
+            if (++by == BY) { by = 0; bz++; }
+          }
+          a.work[e ? last - base : base] = bx | (by << 10) | (bz << 20);
+          base++;
+        }
+      }
+    }
+  }
+}
+
 // The rest of the sub-block pass for one sub-block per lane (`have`), its class
 // scls known: the voxel mask of a lone box's partial sub-block (per-axis runs),
 // the paint items of a covered sub-block of a painted op, the Lipschitz decision
@@ -543,11 +620,13 @@ __device__ __forceinline__ void sub_finish(const FoldArgs& a, bool have, uint32_
 // Sub-block classes of the partial pairs (shapes.ts:382-389): four pairs per
 // warp pass (8 lanes each, one sub-block per lane), pairs taken in shape-class
 // order like the voxel work.  Writes the pair's 2-bit sub-block classes, the
-// voxel masks of lone boxes (per-axis runs), and queues the partial sub-blocks.
+// voxel masks of lone boxes (per-axis runs), and queues the partial sub-blocks;
+// first, the apply pass's brick list (mark_compact).
 template <int MODE>
 __global__ void __launch_bounds__(256, MODE == 1 ? PX_SUB_MINB : PX_CLASSIFY64_MINB) sub_kernel(FoldArgs a) {
   pdl_prologue();
   const int lane = threadIdx.x & 31;
+  mark_compact(a, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, (gridDim.x * blockDim.x) >> 5, lane);
   LaneStats ls = {a.res};
   uint32_t st_local = 0;
   // the classes' item counts in the order they are taken, as an inclusive prefix over lanes
@@ -1090,73 +1169,6 @@ __global__ void __launch_bounds__(256) paint_kernel(FoldArgs a) {
 // register j of the warp is the contiguous 128-byte slice pool[64 j .. 64 j + 63].
 // The warp applies its brick's ops in order, as apply() does (shapes.ts:367-412),
 // using the pair classifications.
-// The bricks the apply pass visits: those with a marked bit (one warp per 32
-// words of the bitmap, a warp-aggregated append), listed as packed brick
-// coordinates bx | by << 10 | bz << 20.
-__global__ void __launch_bounds__(256) mark_compact_kernel(const uint32_t* __restrict__ bmark, uint32_t n_words,
-                                                           uint32_t BX, uint32_t BY, uint32_t TX, uint32_t TY,
-                                                           const uint32_t* __restrict__ tile_cnt, uint32_t* work,
-                                                           uint32_t last, uint32_t* counts, BuildResult* res) {
-  pdl_prologue();
-  const int lane = threadIdx.x & 31;
-  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t w0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; w0 < n_words; w0 += warps * 32) {
-    const uint32_t wi = w0 + lane;
-    const uint32_t bits = wi < n_words ? __ldg(bmark + wi) : 0u;
-    // split the word's bricks: those of tiles with more than 8 ops (the front) and the rest;
-    // the 32 bricks' coordinates stepped along x (no division per brick), their tile counts
-    // loaded together (an unrolled loop of independent loads)
-    uint32_t heavy = 0;
-    if (bits) {
-      const uint32_t ci0 = wi * 32u, byz0 = ci0 / BX;
-      uint32_t bx = ci0 - byz0 * BX, by = byz0 % BY, bz = byz0 / BY;
-#pragma unroll
-      for (int k = 0; k < 32; k++) {
-        if (((bits >> k) & 1u) &&
-            __ldg(tile_cnt + (bx >> 2) + TX * ((by >> 2) + TY * (bz >> 2))) > 8u)
-          heavy |= 1u << k;
-        if (++bx == BX) {
-          bx = 0;
-          if (++by == BY) { by = 0; bz++; }
-        }
-      }
-    }
-#pragma unroll
-    for (int e = 0; e < 2; e++) {
-      const uint32_t mine = e ? bits & ~heavy : heavy;
-      const uint32_t cnt = __popc(mine);
-      uint32_t incl = cnt;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t t = __shfl_up_sync(FULLMASK, incl, o);
-        if (lane >= o) incl += t;
-      }
-      const uint32_t total = __shfl_sync(FULLMASK, incl, 31);
-      uint32_t base = 0;
-      if (lane == 31 && total) {
-        base = atomicAdd(counts + e, total);
-        atomicAdd(&res->n_work, total);
-      }
-      base = __shfl_sync(FULLMASK, base, 31) + incl - cnt;
-      if (mine) {
-        const uint32_t ci0 = wi * 32u, byz0 = ci0 / BX;
-        const uint32_t bx0 = ci0 - byz0 * BX, by0 = byz0 % BY, bz0 = byz0 / BY;
-        for (uint32_t b = mine; b;) {
-          const int k = __ffs(b) - 1;
-          b &= b - 1;
-          uint32_t bx = bx0 + (uint32_t)k, by = by0, bz = bz0;
-          while (bx >= BX) {  // the word's bricks run on along x into the next rows
-            bx -= BX;
-            if (++by == BY) { by = 0; bz++; }
-          }
-          work[e ? last - base : base] = bx | (by << 10) | (bz << 20);
-          base++;
-        }
-      }
-    }
-  }
-}
-
 // One tile-list entry of a brick, looked up for the apply loop: the op, its
 // (op, brick) pair and that pair's classes, and the op fields the loop needs.
 struct FoldEntry {
@@ -1500,24 +1512,12 @@ void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEve
     cudaStreamWaitEvent(s_apply, eval_done, 0);
     s = s_apply;
   }
-  {
-    const uint32_t n_words = (uint32_t)(((size_t)a.BX * a.BY * a.BZ + 31) / 32);
-    const uint32_t blocks = (n_words + 255) / 256;  // 8 warps per block, 32 words per warp
-    launch_pdl(mark_compact_kernel, dim3(blocks < 4096 ? blocks : 4096), dim3(256), 0, s, (const uint32_t*)a.bmark, n_words,
-               (uint32_t)a.BX, (uint32_t)a.BY, (uint32_t)a.TX, (uint32_t)a.TY, (const uint32_t*)a.tile_cnt, a.work,
-               (uint32_t)a.touched_cap, a.work_counter + 1, a.res);
-  }
   if (a.inline_paints) launch_pdl(fold_kernel<true>, dim3(grid(PX_FOLD_MINB)), dim3(256), 0, s, a);
   else launch_pdl(fold_kernel<false>, dim3(grid(PX_FOLD_MINB)), dim3(256), 0, s, a);
 }
 
 // ---------------------------------------------------------------------------
-// scans (single pass; sizes may live on the device)
-
-constexpr int SCAN_THREADS = 512;
-constexpr int SCAN_ITEMS = 8;
-constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
-size_t scan_items_per_block() { return SCAN_TILE; }
+// scan building blocks of the allocator replay's single-pass look-back scans
 
 __device__ __forceinline__ uint32_t shfl_up_any(uint32_t v, int o) { return __shfl_up_sync(FULLMASK, v, o); }
 __device__ __forceinline__ int32_t shfl_up_any(int32_t v, int o) { return __shfl_up_sync(FULLMASK, v, o); }
@@ -1576,20 +1576,12 @@ __device__ typename Op::T block_exclusive(typename Op::T v, typename Op::T* sh, 
   return Op::combine(wp, ex);
 }
 
-__device__ __forceinline__ size_t scan_n(size_t n_max, const uint32_t* n_dev) {
-  if (!n_dev) return n_max;
-  size_t n = *n_dev;
-  return n < n_max ? n : n_max;
-}
-// scan position k -> array index (reverse scans run from the end)
-template <bool REV>
-__device__ __forceinline__ size_t scan_idx(size_t k, size_t n) { return REV ? n - 1 - k : k; }
-
-// Single-pass scan with decoupled look-back: each block takes the next tile
-// by ticket (so every earlier tile is already running or done), publishes its
-// aggregate, reads its predecessors' inclusive prefixes (or aggregates, while
-// those are pending) from nearest to farthest, publishes its own inclusive
-// prefix and writes its outputs.  Flags: 0 pending, 1 aggregate, 2 prefix.
+// Decoupled look-back: each block takes the next tile by ticket (so every
+// earlier tile is already running or done), publishes its aggregate, reads its
+// predecessors' inclusive prefixes (or aggregates, while those are pending) from
+// nearest to farthest, publishes its own inclusive prefix and writes its
+// outputs.  Flags: 0 pending, 1 aggregate, 2 prefix.  Waits give up after
+// SCAN_SPIN_LIMIT polls (an error status, no hang).
 constexpr uint32_t SCAN_SPIN_LIMIT = 1u << 24;
 
 template <class T>
@@ -1602,139 +1594,10 @@ __device__ __forceinline__ int2 scan_peek(const int2* p) { return __ldcg(p); }
 __device__ __forceinline__ uint32_t scan_peek(const uint32_t* p) { return __ldcg(p); }
 __device__ __forceinline__ int32_t scan_peek(const int32_t* p) { return __ldcg(p); }
 
-template <class Op, bool REV>
-__global__ void __launch_bounds__(SCAN_THREADS) scan_onepass(const typename Op::T* in, typename Op::T* out,
-                                                              size_t n_max, const uint32_t* n_dev, bool inclusive,
-                                                              typename Op::T* total_out, ScanTemp st,
-                                                              uint32_t* ticket) {
-  pdl_prologue();
-  typedef typename Op::T T;
-  __shared__ T sh[32];
-  __shared__ T s_prefix;
-  __shared__ uint32_t s_tile;
-  uint32_t* flags = ticket + 4;
-  T* agg = (T*)st.block_agg;
-  T* incl = agg + st.max_blocks;
-  const size_t n = scan_n(n_max, n_dev);
-  if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
-  __syncthreads();
-  const uint32_t tile = s_tile;
-  if ((size_t)tile * SCAN_TILE >= n) return;  // every later tile is past the end too
-  const size_t k0 = (size_t)tile * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
-  // a forward scan reads a thread's whole run as 16-byte vectors (runs start on 32-byte boundaries)
-  constexpr int NV = (int)(sizeof(T) * SCAN_ITEMS / 16);
-  const bool vec = !REV && k0 + SCAN_ITEMS <= n;
-  T v[SCAN_ITEMS];
-  T acc = Op::identity();
-  if (vec) {
-    uint4 buf[NV];
-#pragma unroll
-    for (int j = 0; j < NV; j++) buf[j] = reinterpret_cast<const uint4*>(in + k0)[j];
-    memcpy(v, buf, sizeof v);
-#pragma unroll
-    for (int i = 0; i < SCAN_ITEMS; i++) acc = Op::combine(acc, v[i]);
-  } else {
-#pragma unroll
-    for (int i = 0; i < SCAN_ITEMS; i++) {
-      const size_t k = k0 + i;
-      v[i] = k < n ? in[scan_idx<REV>(k, n)] : Op::identity();
-      acc = Op::combine(acc, v[i]);
-    }
-  }
-  T total;
-  const T pre_block = block_exclusive<Op>(acc, sh, total);
-  if (threadIdx.x < 32) {  // warp 0 publishes and looks back, 32 tiles per step
-    const int lane = threadIdx.x;
-    T prefix = Op::identity();
-    if (tile == 0) {
-      if (lane == 0) scan_publish(incl, flags, total, 2u);
-    } else {
-      if (lane == 0) scan_publish(agg + tile, flags + tile, total, 1u);
-      long long hi = (long long)tile - 1;
-      uint32_t spins = 0;
-      for (;;) {
-        const long long j = hi - 31 + lane;  // lane 31 reads the nearest tile of the window
-        const uint32_t f = j >= 0 ? *(volatile uint32_t*)(flags + j) : 2u;  // before tile 0: the identity
-        if (__any_sync(FULLMASK, f == 0)) {
-          if (++spins > SCAN_SPIN_LIMIT) {  // cannot happen: earlier tiles publish unconditionally
-            if (lane == 0) atomicOr(st.status, (uint32_t)ST_CHAIN);
-            break;
-          }
-          continue;
-        }
-        __threadfence();
-        T v = j >= 0 ? scan_peek(f == 2 ? incl + j : agg + j) : Op::identity();
-        const uint32_t im = __ballot_sync(FULLMASK, f == 2);
-        if (lane < (im ? 31 - __clz(im) : 0)) v = Op::identity();  // tiles before the nearest prefix
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {  // ordered combination of the window
-          const T y = shfl_up_any(v, o);
-          if (lane >= o) v = Op::combine(y, v);
-        }
-        prefix = Op::combine(shfl_any(v, 31), prefix);
-        if (im) break;
-        hi -= 32;
-      }
-      if (lane == 0) scan_publish(incl + tile, flags + tile, Op::combine(prefix, total), 2u);
-    }
-    if (lane == 0) s_prefix = prefix;
-  }
-  __syncthreads();
-  T pre = Op::combine(s_prefix, pre_block);
-  if (vec) {
-#pragma unroll
-    for (int i = 0; i < SCAN_ITEMS; i++) {
-      const T nxt = Op::combine(pre, v[i]);
-      if (total_out && k0 + i + 1 == n) *total_out = nxt;
-      v[i] = inclusive ? nxt : pre;
-      pre = nxt;
-    }
-    uint4 buf[NV];
-    memcpy(buf, v, sizeof v);
-#pragma unroll
-    for (int j = 0; j < NV; j++) reinterpret_cast<uint4*>(out + k0)[j] = buf[j];
-  } else {
-#pragma unroll
-    for (int i = 0; i < SCAN_ITEMS; i++) {
-      const size_t k = k0 + i;
-      const T nxt = Op::combine(pre, v[i]);
-      if (k < n) out[scan_idx<REV>(k, n)] = inclusive ? nxt : pre;
-      if (total_out && k + 1 == n) *total_out = nxt;
-      pre = nxt;
-    }
-  }
-}
-
-static size_t scan_region_bytes(size_t max_blocks) { return 16 + ((4 * max_blocks + 15) & ~(size_t)15); }
-size_t scan_regions_offset(size_t max_blocks) { return 16 * max_blocks; }
-size_t scan_regions_bytes(size_t max_blocks) { return SCAN_REGIONS * scan_region_bytes(max_blocks); }
-size_t scan_temp_bytes(size_t max_blocks) { return scan_regions_offset(max_blocks) + scan_regions_bytes(max_blocks); }
-
-template <class Op, bool REV>
-void scan_any(const typename Op::T* in, typename Op::T* out, size_t n_max, const uint32_t* n_dev, bool inclusive,
-              typename Op::T* total_out, ScanTemp& t, cudaStream_t s) {
-  if (n_max == 0) return;
-  const size_t nb = (n_max + SCAN_TILE - 1) / SCAN_TILE;
-  int r = t.next_region++;
-  char* regions = (char*)t.block_agg + scan_regions_offset(t.max_blocks);
-  if (r >= SCAN_REGIONS) {  // more scans than cleared regions: clear the last one again
-    r = SCAN_REGIONS - 1;
-    cudaMemsetAsync(regions + r * scan_region_bytes(t.max_blocks), 0, scan_region_bytes(t.max_blocks), s);
-  }
-  uint32_t* ticket = (uint32_t*)(regions + r * scan_region_bytes(t.max_blocks));
-  launch_pdl(scan_onepass<Op, REV>, dim3((unsigned)nb), dim3(SCAN_THREADS), 0, s, in, out, n_max, n_dev, inclusive, total_out, t,
-             ticket);
-}
-
-void launch_scan_u32(const uint32_t* in, uint32_t* out, size_t n, const uint32_t* n_dev, bool inclusive,
-                     uint32_t* total_out, ScanTemp& t, cudaStream_t s) {
-  scan_any<SumOp, false>(in, out, n, n_dev, inclusive, total_out, t, s);
-}
-
 // ---------------------------------------------------------------------------
 // replay of the LIFO pool allocator (VoxelWorld.ts:112-127) over the build's
 // alloc/free events in (op, cell) order -- the order of the reference's loop --
-// in three kernels:
+// in four kernels:
 //   scan_events   the event positions of the (op, brick) pairs (a single-pass
 //                 scan of their event counts) and the events themselves: a pop
 //                 per allocation, a push per free, the H holes before the build

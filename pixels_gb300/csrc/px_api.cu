@@ -127,7 +127,6 @@ struct px_world {
   uint32_t vq_nonempty = 0;                // bit g: voxel group g has ops
   DevBuf paint_items, pvals;    // sub-blocks to paint and the paint values
   DevBuf bmark, work;           // bricks the apply pass visits (bitmap, list)
-  DevBuf scan_agg;
   DevBuf work_counter;
   DevBuf res;
   DevBuf opaque, udens, super_counts, density;
@@ -693,7 +692,7 @@ void px_world_destroy(px_world* w) {
                     &w->tile_off, &w->tile_ops, &w->evt, &w->fsrc, &w->cnt, &w->pos, &w->etype,
                     &w->ew, &w->replay_tmp, &w->depth, &w->tree, &w->staging, &w->touched,
                     &w->stage_cell, &w->stage_src, &w->chunk_op, &w->pcode, &w->psub, &w->pmask,
-                    &w->chunk_counter, &w->vitems, &w->scan_agg, &w->work_counter, &w->res, &w->opaque,
+                    &w->chunk_counter, &w->vitems, &w->work_counter, &w->res, &w->opaque,
                     &w->udens, &w->super_counts, &w->density, &w->paint_items, &w->pvals, &w->tile_boxes, &w->bmark, &w->work, &w->pitems,
                     &w->free_list, &w->rescue};
   for (DevBuf* b : bufs) release(*b);
@@ -1146,13 +1145,6 @@ class HostPool {
   std::atomic<uint64_t> gen_{0};
 };
 
-// Blocks of the single-pass scans of a build with P pairs and E_max events.
-size_t scan_blocks(const px_world* w, uint64_t P, size_t E_max) {
-  size_t items = w->ntiles > E_max ? w->ntiles : E_max;
-  if (P > items) items = P;
-  return items / scan_items_per_block() + 2;
-}
-
 // The build scratch that scales with the (op, brick) pairs P, the tile-list
 // entries, the paint slots, the touched bricks, the allocator events E_max and
 // the staging slots.
@@ -1174,7 +1166,7 @@ int ensure_pair_scratch(px_world* w, uint64_t P, uint64_t tile_pairs, uint64_t n
       (rc = ensure(w, w->pvals, 2048 * n_slots + 4)) || (rc = ensure(w, w->bmark, 4 * ((w->ncells + 31) / 32))) ||
       (rc = ensure(w, w->work, 4 * touched_bound + 4)) || (rc = ensure(w, w->rescue, 16 * (size_t)w->rescue_cap)))
     return rc;
-  return ensure(w, w->scan_agg, scan_temp_bytes(scan_blocks(w, P, E_max)));
+  return PX_OK;
 }
 
 // Staging slots a build with P pairs reserves (a guess: a build that needs more
@@ -1549,7 +1541,6 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
       (rc = ensure(w, w->d_bases, sizeof(float2) * w->bases.size())) ||
       (rc = ensure_pair_scratch(w, P, tile_pairs, n_slots, touched_bound, E_max, stage_cap)))
     return rc;
-  const size_t scan_nb = scan_blocks(w, P, E_max);
   const uint32_t H_max = H;
   {
     const void* after[9] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p,
@@ -1602,16 +1593,13 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   ups.push_back({w->evt.p, nullptr, P});
   ups.push_back({w->cnt.p, nullptr, 4 * P});  // events per pair, written by the apply pass
   ups.push_back({w->bmark.p, nullptr, 4 * ((w->ncells + 31) / 32)});
-  ups.push_back({(char*)w->scan_agg.p + scan_regions_offset(scan_nb), nullptr, scan_regions_bytes(scan_nb)});
   ups.push_back({w->replay_tmp.p, nullptr, replay_clear_bytes(P, E_max)});  // the replay's tickets and look-back flags
   if ((rc = issue_uploads(w, ups, s))) return rc;  // the op tables; the chunk order follows the cull launches
 
   BuildResult* res = (BuildResult*)w->res.p;
-  ScanTemp st{w->scan_agg.p, scan_nb, &res->status, 0};
-  launch_cull_count((const uint2*)w->d_boxes.p, n_ops, w->TX, w->TY, w->TZ, (uint32_t*)w->tile_cnt.p, s);
-  launch_scan_u32((const uint32_t*)w->tile_cnt.p, (uint32_t*)w->tile_off.p, w->ntiles, nullptr, false, nullptr, st, s);
-  launch_cull_fill((const uint2*)w->d_boxes.p, n_ops, w->TX, w->TY, w->TZ, (const uint32_t*)w->tile_off.p,
-                   (uint32_t*)w->tile_ops.p, (uint2*)w->tile_boxes.p, s);
+  launch_cull((const uint2*)w->d_boxes.p, n_ops, w->TX, w->TY, w->TZ, (uint32_t*)w->tile_cnt.p,
+              (uint32_t*)w->tile_off.p, (uint32_t*)w->tile_ops.p, (uint2*)w->tile_boxes.p,
+              (uint32_t*)w->chunk_counter.p + CULL_COUNTER, s);
   // the classify pass's chunk order, computed while the cull kernels run
   const size_t n_chunks = (P + 31) / 32;
   if (upload) {
@@ -1683,7 +1671,8 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   fa.vitems = (uint4*)w->vitems.p;
   fa.vitems_cap = (uint32_t)(8 * P < 0xffffffffull ? 8 * P : 0xffffffffull);
   fa.vitem_counter = (uint32_t*)w->chunk_counter.p + 4;   // counters: [0] chunks, [1] paint taken,
-                                                          // [2] paint pushed, [4..136] voxel, [160..193] pairs
+                                                          // [2] paint pushed, [4..136] voxel, [160..193] pairs,
+                                                          // [CULL_COUNTER] tile-list entries
   {  // per-class regions: the class's pairs (sub-block pass), 8 sub-blocks per pair (voxel pass)
     uint64_t per[VCLASSES] = {0}, vper[VQ_CLASSES] = {0};
     for (int i = 0; i < n_ops; i++) {

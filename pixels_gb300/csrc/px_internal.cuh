@@ -170,7 +170,9 @@ constexpr int VCLASSES = 32;
 enum { VQ_NARROW = 0, VQ_AFFINE = 1, VQ_WIDE = 2, VQ_GENERIC = 3 };
 constexpr int VQ_CLASSES = 128;
 constexpr int VQ_TAKEN = 1 + VQ_CLASSES;  // vitem_counter[VQ_TAKEN + group]: items the group's kernel took
-// Programs of the lean voxel kernel, by form:
+constexpr int CULL_COUNTER = 200;         // chunk_counter[CULL_COUNTER]: tile-list entries reserved by cull_kernel
+
+// Programs of the lean voxel kernels, by form:
 //   1  [stage] prim [stage end] [offset]
 //   2  [stage] prim prim comb [stage end] [offset]           (one stage for both)
 //   3  [stage] prim [stage end] [stage] prim [stage end] comb [offset]
@@ -219,7 +221,7 @@ struct FoldArgs {
   uint32_t* pvals;            // 512 paint values per slot (voxel index order); PV_RANGE flags
   int inline_paints;          // some painted op has no slot: fold_kernel calls its paints itself
   uint32_t* bmark;            // one bit per brick: some pair of it is not skipped (classify_kernel)
-  uint32_t* work;             // those bricks, listed by mark_compact_kernel: bricks of tiles with more
+  uint32_t* work;             // those bricks, listed by mark_compact (sub_kernel): bricks of tiles with more
                               // than 8 ops from the front, the others from the back (touched_cap down)
   const OpDev* ops;
   const uint2* code;
@@ -256,32 +258,16 @@ struct FoldArgs {
 constexpr uint32_t TAG_STAGED = 0x40000000u;
 
 // Host-side launch wrappers (kernels.cu)
-void launch_cull_count(const uint2* boxes, int n_ops, int TX, int TY, int TZ, uint32_t* tile_cnt, cudaStream_t s);
-void launch_cull_fill(const uint2* boxes, int n_ops, int TX, int TY, int TZ, const uint32_t* tile_off,
-                      uint32_t* tile_ops, uint2* tile_boxes, cudaStream_t s);
+// counter: a zeroed word (the tile lists' reservation count)
+void launch_cull(const uint2* boxes, int n_ops, int TX, int TY, int TZ, uint32_t* tile_cnt, uint32_t* tile_off,
+                 uint32_t* tile_ops, uint2* tile_boxes, uint32_t* counter, cudaStream_t s);
 // max_blocks > 0 caps the persistent grids (builds sharing the GPU)
 // The evaluation passes (classify .. paint) go on s; the apply pass on s_apply,
 // after eval_done is recorded on s (s_apply == s: one stream, no event).
 void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEvent_t mid, int max_blocks,
                  cudaStream_t s_apply, cudaEvent_t eval_done);
 
-// Scratch of the single-pass scans (scan_temp_bytes(max_blocks) bytes): the
-// tiles' aggregates and inclusive prefixes, then SCAN_REGIONS regions of a tile
-// ticket and per-tile flags.  A build clears the regions once
-// (scan_regions_bytes) and its scans take one region each, in launch order.
-constexpr int SCAN_REGIONS = 5;
-struct ScanTemp {
-  void* block_agg;
-  size_t max_blocks;
-  uint32_t* status;  // a look-back that waits too long sets ST_CHAIN here
-  int next_region;   // regions already used by this build's scans
-};
-size_t scan_items_per_block();
-size_t scan_temp_bytes(size_t max_blocks);
-size_t scan_regions_offset(size_t max_blocks);  // where the regions start
-size_t scan_regions_bytes(size_t max_blocks);
-void launch_scan_u32(const uint32_t* in, uint32_t* out, size_t n, const uint32_t* n_dev, bool inclusive,
-                     uint32_t* total_out, ScanTemp& t, cudaStream_t s);
+
 
 // The allocator replay's look-back scratch: flags and counters (cleared by
 // every build: replay_clear_bytes from `flags`) and the published aggregates.
