@@ -377,6 +377,59 @@ __device__ __forceinline__ void brick_bases(const FoldArgs& a, const OpDev* O, i
   bo[2] = {b2.x, b2.y};
 }
 
+// The point through a rotation of the shape's frame (shapes.ts:263-320 on
+// intervals): p holds the pivot's two coordinates, cos and sin.
+__device__ __forceinline__ void rot32(uint32_t op, const Iv* __restrict__ p, Iv& x, Iv& y, Iv& z) {
+  const Iv p0 = ldp(p, 0), p1 = ldp(p, 1), c = ldp(p, 2), sn = ldp(p, 3);
+  if (op == OP_ROT_Y) {
+    const Iv dx = isub(x, p0), dz = isub(z, p1);
+    x = iadd(iadd(p0, icmul(dx, c)), icmul(dz, sn));
+    z = iadd(isub(p1, icmul(dx, sn)), icmul(dz, c));
+  } else if (op == OP_ROT_X) {
+    const Iv dy = isub(y, p0), dz = isub(z, p1);
+    y = iadd(iadd(p0, icmul(dy, c)), icmul(dz, sn));
+    z = iadd(isub(p1, icmul(dy, sn)), icmul(dz, c));
+  } else {
+    const Iv dx = isub(x, p0), dy = isub(y, p1);
+    x = iadd(iadd(p0, icmul(dx, c)), icmul(dy, sn));
+    y = iadd(isub(p1, icmul(dx, sn)), icmul(dy, c));
+  }
+}
+
+// Apply a lean program's stage (LP_* kinds): one rotation, or (AFF) a composed run.
+template <bool AFF>
+__device__ __forceinline__ void stage32(uint32_t kind, const Iv* __restrict__ p, Iv& x, Iv& y, Iv& z) {
+  if (AFF && kind == LP_AFFINE) aff32(p, x, y, z);
+  else if (kind) rot32(OP_ROT_X - 1 + kind, p, x, y, z);
+}
+
+// A lean program (LP_* forms) at one point in float32 intervals, without the
+// interpreter's value stack and rotation frames; amb: a polygon crossing test
+// the intervals could not settle.  One copy of the primitive and stage code
+// serves both primitives of forms 2 and 3.
+__device__ __forceinline__ Iv lean_point(const FoldArgs& a, const OpDev* V, Iv x, Iv y, Iv z, float M, bool& amb) {
+  const Iv* __restrict__ P = reinterpret_cast<const Iv*>(a.p32);
+  const uint32_t l0 = *reinterpret_cast<const uint32_t*>(V->lp), l1 = *reinterpret_cast<const uint32_t*>(V->lp + 4);
+  const uint32_t form = l0 & 0xffu, comb = (l0 >> 8) & 0xffu, ioff = l1 >> 24, kinds = (l1 >> 16) & 0xffu;
+  const uint32_t* c32 = a.code32 + V->code_off;
+  const uint2* cw = a.code + V->code_off;
+  Iv v = {0.f, 0.f}, xs = x, ys = y, zs = z;
+#pragma unroll 1
+  for (uint32_t k = 0; k < (form > 1 ? 2u : 1u); k++) {
+    const uint32_t ip = k ? l0 >> 24 : (l0 >> 16) & 0xffu;
+    if (k == 0 || form == 3) {  // the stage: instruction 0, or the second primitive's own
+      xs = x; ys = y; zs = z;
+      const uint32_t ks = k ? kinds >> 4 : kinds & 15u, is = k ? (l1 >> 8) & 0xffu : 0u;
+      if (ks) stage32<true>(ks, P + (__ldg(c32 + is) & C32_OFF), xs, ys, zs);
+    }
+    const uint32_t w = __ldg(&cw[ip].x);
+    const Iv u = prim32(w & 0xffu, (int)(w >> 8), P + (__ldg(c32 + ip) & C32_OFF), xs, ys, zs, M, amb);
+    v = k == 0 ? u : comb == LP_NEGMAX ? imax(v, ineg(u)) : comb == LP_MAX ? imax(v, u) : imin(v, u);
+  }
+  if (ioff != LP_NONE) v = iadd(v, ldp(P + (__ldg(c32 + ioff) & C32_OFF), 0));  // offset (penthouse.ts:250)
+  return v;
+}
+
 // The rest of the brick pass for one pair per lane (`valid`), its class cls
 // known: the pair's class byte, the apply pass's brick bit, the paint items of
 // a full pair of a painted op, the sub-block work item of a partial pair.
@@ -471,8 +524,16 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
         const bool use32 = MODE == 1 && !(flags & OPF_FP64_ONLY);
         Iv bo[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
         if (use32) brick_bases(a, O, bx, by, bz, bo);
-        cls = eval_decide<MODE>(a, O, a.code + O->code_off, (int)O->code_len, use32, bo, 3.5f, 3.5f, 3.5f,
-                                (float)(bx * 8 + 4), (float)(by * 8 + 4), (float)(bz * 8 + 4), 1, ls);
+        cls = 3;
+        if (MODE == 1 && use32 && O->lp[LP_FORM] && !a.validate) {  // a lean program: no interpreter
+          bool amb = false;
+          const Iv k = koff(3.5f, a.vs_lo, a.vs_hi);
+          const Iv d = lean_point(a, O, iadd(bo[0], k), iadd(bo[1], k), iadd(bo[2], k), O->thr[T_M], amb);
+          if (!amb) cls = classify32(d, O->thr, T_BSK_HI);
+        }
+        if (cls == 3)  // the interpreter, with the float64 rescue
+          cls = eval_decide<MODE>(a, O, a.code + O->code_off, (int)O->code_len, use32, bo, 3.5f, 3.5f, 3.5f,
+                                  (float)(bx * 8 + 4), (float)(by * 8 + 4), (float)(bz * 8 + 4), 1, ls);
         n_brick++;
       }
     }
@@ -672,10 +733,19 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_SUB_MINB : PX_CLASSIFY64_M
       Iv bo[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
       if (use32) brick_bases(a, Q, pbx, pby, pbz, bo);
       const int sxb = s & 1, syb = (s >> 1) & 1, szb = (s >> 2) & 1;
-      scls = eval_decide<MODE>(a, Q, a.code + Q->code_off, (int)Q->code_len, use32, bo, 4.f * sxb + 1.5f,
-                               4.f * syb + 1.5f, 4.f * szb + 1.5f, (float)(pbx * 8 + sxb * 4 + 2),
-                               (float)(pby * 8 + syb * 4 + 2), (float)(pbz * 8 + szb * 4 + 2), 2, ls, true,
-                               MODE == 1 && use32 ? &dc : nullptr);
+      scls = 3;
+      if (MODE == 1 && use32 && Q->lp[LP_FORM] && !a.validate) {  // a lean program: no interpreter
+        bool amb = false;
+        dc = lean_point(a, Q, iadd(bo[0], koff(4.f * sxb + 1.5f, a.vs_lo, a.vs_hi)),
+                        iadd(bo[1], koff(4.f * syb + 1.5f, a.vs_lo, a.vs_hi)),
+                        iadd(bo[2], koff(4.f * szb + 1.5f, a.vs_lo, a.vs_hi)), Q->thr[T_M], amb);
+        if (!amb) scls = classify32(dc, Q->thr, T_SSK_HI);
+      }
+      if (scls == 3)  // the interpreter, with the float64 rescue
+        scls = eval_decide<MODE>(a, Q, a.code + Q->code_off, (int)Q->code_len, use32, bo, 4.f * sxb + 1.5f,
+                                 4.f * syb + 1.5f, 4.f * szb + 1.5f, (float)(pbx * 8 + sxb * 4 + 2),
+                                 (float)(pby * 8 + syb * 4 + 2), (float)(pbz * 8 + szb * 4 + 2), 2, ls, true,
+                                 MODE == 1 && use32 ? &dc : nullptr);
     }
     uint32_t code16 = (uint32_t)scls << (2 * s);
     code16 |= __shfl_xor_sync(FULLMASK, code16, 1);
@@ -805,32 +875,6 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_VOXEL_MINB : PX_CLASSIFY64
     if (lane == 0) a.pmask[vp * 8 + ss] = m;
   }
   }
-}
-
-// The point through a rotation of the shape's frame (shapes.ts:263-320 on
-// intervals): p holds the pivot's two coordinates, cos and sin.
-__device__ __forceinline__ void rot32(uint32_t op, const Iv* __restrict__ p, Iv& x, Iv& y, Iv& z) {
-  const Iv p0 = ldp(p, 0), p1 = ldp(p, 1), c = ldp(p, 2), sn = ldp(p, 3);
-  if (op == OP_ROT_Y) {
-    const Iv dx = isub(x, p0), dz = isub(z, p1);
-    x = iadd(iadd(p0, icmul(dx, c)), icmul(dz, sn));
-    z = iadd(isub(p1, icmul(dx, sn)), icmul(dz, c));
-  } else if (op == OP_ROT_X) {
-    const Iv dy = isub(y, p0), dz = isub(z, p1);
-    y = iadd(iadd(p0, icmul(dy, c)), icmul(dz, sn));
-    z = iadd(isub(p1, icmul(dy, sn)), icmul(dz, c));
-  } else {
-    const Iv dx = isub(x, p0), dy = isub(y, p1);
-    x = iadd(iadd(p0, icmul(dx, c)), icmul(dy, sn));
-    y = iadd(isub(p1, icmul(dx, sn)), icmul(dy, c));
-  }
-}
-
-// Apply a lean program's stage (LP_* kinds): one rotation, or (AFF) a composed run.
-template <bool AFF>
-__device__ __forceinline__ void stage32(uint32_t kind, const Iv* __restrict__ p, Iv& x, Iv& y, Iv& z) {
-  if (AFF && kind == LP_AFFINE) aff32(p, x, y, z);
-  else if (kind) rot32(OP_ROT_X - 1 + kind, p, x, y, z);
 }
 
 // Voxel inside-masks of the queued partial sub-blocks of the lean programs --
