@@ -336,10 +336,14 @@ def serving_section(args, pyoracle):
     return out
 
 
-# DRAM bytes per build of the evaluation kernels (classify, sub-block, voxel,
-# paint, apply): dram__bytes_read.sum + dram__bytes_write.sum from one ncu
-# capture of each on the penthouse at vpm=80; the bench cannot run ncu itself
-EVAL_TRAFFIC_BYTES = 33_562_880
+# DRAM bytes per build from one ncu capture on the penthouse at vpm=80 (the
+# bench cannot run ncu itself): dram__bytes_read.sum + dram__bytes_write.sum of
+# the evaluation kernels (classify, sub-block, the four voxel kernels, paint,
+# apply) with caches flushed before each kernel, and of all 16 kernels of the
+# build, flushed before each and left alone (the run's first build)
+EVAL_TRAFFIC_BYTES = 33_970_000
+BUILD_TRAFFIC_COLD_BYTES = 93_770_000
+BUILD_TRAFFIC_WARM_BYTES = 66_800_000
 
 
 def hbm_line(cfg, pool_used, ir_bytes, ms, derived_bytes=0):
@@ -521,6 +525,46 @@ def main():
         t1 = time.perf_counter()
         return used_, (tf - t0, ta - tf, tb - ta, t1 - tb)
 
+    # pipelined end to end: two worlds on two streams, so that step i's readback
+    # (host-blocking copies) overlaps step i+1's build on the GPU; every step still
+    # submits its op list from host memory and reads all of its outputs back
+    h2 = None
+    if not args.no_e2e:
+        h2 = _lib.world_create(*cfg.dims, vpm, 1 << 15)
+        _lib.set_derive_on_build(h2, MAX_BRICKS)
+        _lib.submit_ops(h2, ir)
+        _lib.build(h2, MODE_MIXED, s_ptr)
+    pipe_streams = [torch.cuda.Stream(dev), torch.cuda.Stream(dev)]
+
+    def read_outputs(hh):
+        assert L.px_read_grid(hh, grid_h.data_ptr(), grid_h.numel()) == 0
+        assert L.px_read_pool(hh, pool_h.data_ptr(), pool_h.numel()) == 0
+        assert L.px_read_super(hh, super_h.data_ptr(), super_h.numel()) == 0
+        assert L.px_read_density(hh, dens_h.data_ptr(), dens_h.numel()) == 0
+        assert L.px_read_free_list(hh, MAX_BRICKS, free_h.data_ptr(), free_h.numel(), ctypes.byref(free_len)) == 0
+
+    def e2e_pipelined(n: int) -> float:
+        hs = (h, h2)
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        for i in range(n + 1):
+            if i < n:
+                hh, st_ = hs[i % 2], pipe_streams[i % 2].cuda_stream
+                _lib.world_reset(hh, False, st_)
+                assert L.px_submit_ops(hh, ir_buf, len(ir)) == 0
+                _lib.build_enqueue(hh, MODE_MIXED, st_)
+            if i > 0:
+                hp = hs[(i - 1) % 2]
+                _lib.build_finish(hp)
+                read_outputs(hp)
+        return (time.perf_counter() - t0) / n
+
+    t_pipe = None
+    if not args.no_e2e:
+        e2e_pipelined(max(args.warmup, 1))
+        t_pipe = max_over_ranks([e2e_pipelined(max(args.steps, 2))], dist, dev)[0]
+
     e2e, e2e_parts, e2e_fl = [], [], []
     used = st["pool_used"]
     for flatten in (False, True):
@@ -535,8 +579,11 @@ def main():
     if not e2e:  # profiling run: one readback for the mismatch check
         used, _ = e2e_step(False)
         e2e = e2e_fl = [float("nan")]
-    t_e2e, t_e2e_fl = max_over_ranks([statistics.mean(e2e), statistics.mean(e2e_fl)], dist, dev)
+    t_e2e_serial, t_e2e_fl = max_over_ranks([statistics.mean(e2e), statistics.mean(e2e_fl)], dist, dev)
+    t_e2e = t_pipe if t_pipe is not None else t_e2e_serial
     e2e_value = job_value(world, cells, t_e2e)
+    if h2 is not None:
+        _lib.world_destroy(h2)
     d2h = int(grid_h.numel() * 4 + used * 1024 + super_h.numel() * 4 + dens_h.numel() + free_len.value * 4)
 
     if rank != 0:
@@ -605,6 +652,12 @@ def main():
                 "d2h_bytes_per_step": d2h,
                 "ms_per_step": round(t_e2e * 1e3, 3),
                 "reads": "grid, pool, super counts, density, free list",
+                "pipelined": t_pipe is not None,
+                "how": "two worlds built alternately on two CUDA streams: step i's readback (blocking copies "
+                       "to pinned host memory) overlaps step i+1's build; every step resets its world, submits "
+                       "the op list from host memory, builds and reads every output back",
+                "serial": {"value": round(job_value(world, cells, t_e2e_serial), 4),
+                           "ms_per_step": round(t_e2e_serial * 1e3, 3)},
                 "split_ms": ({k: round(statistics.mean(p[j] for p in e2e_parts) * 1e3, 3)
                               for j, k in enumerate(("reset_and_submit", "build_and_derive", "read_outputs"))}
                              if e2e_parts else None),
@@ -615,10 +668,13 @@ def main():
         "roofline": {"bound": "fp32-alu", "achieved": round(achieved, 4), "peak": round(peak32, 2),
                      "unit": "TFLOP/s", "frac": round(achieved / peak32, 5), "traffic": EVAL_TRAFFIC_BYTES,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the classify, sub-block, "
-                                       "voxel, paint and apply kernels of one build of this workload "
-                                       "(one capture, --clock-control none)",
-                     "kernel": "classify_kernel + sub_kernel + voxel_kernel + paint_kernel + fold_kernel "
-                               "(every SDF and paint evaluation)",
+                                       "voxel (4), paint and apply kernels of one build of this workload "
+                                       "(one capture, caches flushed before each kernel, --clock-control none)",
+                     "build_traffic": {"cold": BUILD_TRAFFIC_COLD_BYTES, "warm": BUILD_TRAFFIC_WARM_BYTES,
+                                       "what": "all 16 kernels of one build: caches flushed before each kernel "
+                                               "(cold), or left alone (warm, the run's first build)"},
+                     "kernel": "classify_kernel + sub_kernel + voxel_lean_kernel x3 + voxel_kernel + paint_kernel "
+                               "+ fold_kernel (every SDF and paint evaluation)",
                      "alg_ops_per_launch": int(alg_ops),
                      "fold_ms": round(fold_s * 1e3, 4),
                      "peak_source": "measured here: dependent FFMA chains on all SMs (px_probe_peak)",

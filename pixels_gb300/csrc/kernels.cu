@@ -438,12 +438,29 @@ template <int MODE>
 __device__ __forceinline__ void classify_finish(const FoldArgs& a, bool valid, uint32_t o, const OpDev* O,
                                                 unsigned long long p, int bx, int by, int bz, int cls, int lane,
                                                 uint32_t& st_local) {
+  bool first = false;  // the first pair to mark its brick: it lists the brick for the apply pass
   if (valid) {
     a.pcode[p] = (uint8_t)cls;
     if (cls != PC_SKIP) {  // the apply pass visits this brick
       const size_t ci = (size_t)bx + (size_t)a.BX * ((size_t)by + (size_t)a.BY * (size_t)bz);
-      atomicOr(a.bmark + (ci >> 5), 1u << (ci & 31));
+      first = !(atomicOr(a.bmark + (ci >> 5), 1u << (ci & 31)) & (1u << (ci & 31)));
     }
+  }
+  // the apply pass's brick list, packed coordinates bx | by << 10 | bz << 20: bricks
+  // of tiles with more than 8 ops from the front, the others from the back
+  const bool heavy = first && __ldg(a.tile_cnt + (bx >> 2) + a.TX * ((by >> 2) + a.TY * (bz >> 2))) > 8u;
+#pragma unroll
+  for (int e = 0; e < 2; e++) {
+    const uint32_t wm = __ballot_sync(FULLMASK, first && heavy == (e == 0));
+    if (!wm) continue;
+    uint32_t base = 0;
+    if (lane == 0) {
+      base = atomicAdd(a.work_counter + 1 + e, (uint32_t)__popc(wm));
+      atomicAdd(&a.res->n_work, (uint32_t)__popc(wm));
+    }
+    base = __shfl_sync(FULLMASK, base, 0) + __popc(wm & ((1u << lane) - 1u));
+    if (first && heavy == (e == 0))
+      a.work[e ? (uint32_t)a.touched_cap - base : base] = (uint32_t)bx | ((uint32_t)by << 10) | ((uint32_t)bz << 20);
   }
   // a full pair of a painted op: its 8 sub-blocks go to the paint pass
   const bool fullp = valid && cls == PC_FULL && O->paint_slot != NO_SLOT;
@@ -551,73 +568,6 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
   }
 }
 
-// The bricks the apply pass visits: those with a marked bit (one warp per 32
-// words of the bitmap, a warp-aggregated append), listed as packed brick
-// coordinates bx | by << 10 | bz << 20; bricks of tiles with more than 8 ops at
-// the front, the rest from the back.  Run by every warp of the sub-block pass
-// before its own work (the classify pass's bitmap is complete by then).
-__device__ __forceinline__ void mark_compact(const FoldArgs& a, uint32_t warp, uint32_t n_warps, int lane) {
-  const uint32_t BX = a.BX, BY = a.BY, TX = a.TX, TY = a.TY;
-  const uint32_t n_words = (uint32_t)(((size_t)a.BX * a.BY * a.BZ + 31) / 32);
-  const uint32_t last = (uint32_t)a.touched_cap;
-  uint32_t* const counts = a.work_counter + 1;
-  for (uint32_t w0 = warp * 32; w0 < n_words; w0 += n_warps * 32) {
-    const uint32_t wi = w0 + lane;
-    const uint32_t bits = wi < n_words ? __ldcg(a.bmark + wi) : 0u;
-    // split the word's bricks: those of tiles with more than 8 ops (the front) and the rest;
-    // the 32 bricks' coordinates stepped along x (no division per brick), their tile counts
-    // loaded together (an unrolled loop of independent loads)
-    uint32_t heavy = 0;
-    if (bits) {
-      const uint32_t ci0 = wi * 32u, byz0 = ci0 / BX;
-      uint32_t bx = ci0 - byz0 * BX, by = byz0 % BY, bz = byz0 / BY;
-#pragma unroll
-      for (int k = 0; k < 32; k++) {
-        if (((bits >> k) & 1u) &&
-            __ldg(a.tile_cnt + (bx >> 2) + TX * ((by >> 2) + TY * (bz >> 2))) > 8u)
-          heavy |= 1u << k;
-        if (++bx == BX) {
-          bx = 0;
-          if (++by == BY) { by = 0; bz++; }
-        }
-      }
-    }
-#pragma unroll
-    for (int e = 0; e < 2; e++) {
-      const uint32_t mine = e ? bits & ~heavy : heavy;
-      const uint32_t cnt = __popc(mine);
-      uint32_t incl = cnt;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t t = __shfl_up_sync(FULLMASK, incl, o);
-        if (lane >= o) incl += t;
-      }
-      const uint32_t total = __shfl_sync(FULLMASK, incl, 31);
-      uint32_t base = 0;
-      if (lane == 31 && total) {
-        base = atomicAdd(counts + e, total);
-        atomicAdd(&a.res->n_work, total);
-      }
-      base = __shfl_sync(FULLMASK, base, 31) + incl - cnt;
-      if (mine) {
-        const uint32_t ci0 = wi * 32u, byz0 = ci0 / BX;
-        const uint32_t bx0 = ci0 - byz0 * BX, by0 = byz0 % BY, bz0 = byz0 / BY;
-        for (uint32_t b = mine; b;) {
-          const int k = __ffs(b) - 1;
-          b &= b - 1;
-          uint32_t bx = bx0 + (uint32_t)k, by = by0, bz = bz0;
-          while (bx >= BX) {  // the word's bricks run on along x into the next rows
-            bx -= BX;
-            if (++by == BY) { by = 0; bz++; }
-          }
-          a.work[e ? last - base : base] = bx | (by << 10) | (bz << 20);
-          base++;
-        }
-      }
-    }
-  }
-}
-
 // The rest of the sub-block pass for one sub-block per lane (`have`), its class
 // scls known: the voxel mask of a lone box's partial sub-block (per-axis runs),
 // the paint items of a covered sub-block of a painted op, the Lipschitz decision
@@ -681,13 +631,11 @@ __device__ __forceinline__ void sub_finish(const FoldArgs& a, bool have, uint32_
 // Sub-block classes of the partial pairs (shapes.ts:382-389): four pairs per
 // warp pass (8 lanes each, one sub-block per lane), pairs taken in shape-class
 // order like the voxel work.  Writes the pair's 2-bit sub-block classes, the
-// voxel masks of lone boxes (per-axis runs), and queues the partial sub-blocks;
-// first, the apply pass's brick list (mark_compact).
+// voxel masks of lone boxes (per-axis runs), and queues the partial sub-blocks.
 template <int MODE>
 __global__ void __launch_bounds__(256, MODE == 1 ? PX_SUB_MINB : PX_CLASSIFY64_MINB) sub_kernel(FoldArgs a) {
   pdl_prologue();
   const int lane = threadIdx.x & 31;
-  mark_compact(a, (blockIdx.x * blockDim.x + threadIdx.x) >> 5, (gridDim.x * blockDim.x) >> 5, lane);
   LaneStats ls = {a.res};
   uint32_t st_local = 0;
   // the classes' item counts in the order they are taken, as an inclusive prefix over lanes

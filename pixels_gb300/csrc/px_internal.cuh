@@ -221,7 +221,7 @@ struct FoldArgs {
   uint32_t* pvals;            // 512 paint values per slot (voxel index order); PV_RANGE flags
   int inline_paints;          // some painted op has no slot: fold_kernel calls its paints itself
   uint32_t* bmark;            // one bit per brick: some pair of it is not skipped (classify_kernel)
-  uint32_t* work;             // those bricks, listed by mark_compact (sub_kernel): bricks of tiles with more
+  uint32_t* work;             // those bricks, listed by their first marking pair: bricks of tiles with more
                               // than 8 ops from the front, the others from the back (touched_cap down)
   const OpDev* ops;
   const uint2* code;
