@@ -361,8 +361,9 @@ __device__ __noinline__ VoxelF64 voxel_f64(const double* __restrict__ params, do
 __device__ __forceinline__ void brick_of_pair(const OpDev* O, unsigned long long p, int& bx, int& by, int& bz) {
   const uint32_t local = (uint32_t)(p - O->pair_base);
   const uint32_t nxy = (uint32_t)(O->nx * O->ny);
-  const uint32_t zq = local / nxy, r = local - zq * nxy;
-  const uint32_t yq = r / (uint32_t)O->nx;
+  const uint64_t ixy = O->inv_nxy, ix = O->inv_nx;  // 0: a divisor of 1
+  const uint32_t zq = ixy ? (uint32_t)__umul64hi(local, ixy) : local, r = local - zq * nxy;
+  const uint32_t yq = ix ? (uint32_t)__umul64hi(r, ix) : r;
   bz = O->bz0 + (int)zq;
   by = O->by0 + (int)yq;
   bx = O->bx0 + (int)(r - yq * (uint32_t)O->nx);

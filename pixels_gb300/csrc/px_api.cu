@@ -916,11 +916,17 @@ int convert_ops(const px_world* w, const IrOp* iops, size_t i0, size_t i1, const
     uint2 box;
     if (vx0 > vx1 || vy0 > vy1 || vz0 > vz1) {
       d.bx0 = d.by0 = d.bz0 = 1; d.bx1 = d.by1 = d.bz1 = 0; d.nx = d.ny = 0;
+      d.inv_nx = d.inv_nxy = 0;
       box = make_uint2(3u << 30, 0u);
     } else {
       d.bx0 = (int)vx0 >> 3; d.by0 = (int)vy0 >> 3; d.bz0 = (int)vz0 >> 3;
       d.bx1 = (int)vx1 >> 3; d.by1 = (int)vy1 >> 3; d.bz1 = (int)vz1 >> 3;
       d.nx = d.bx1 - d.bx0 + 1; d.ny = d.by1 - d.by0 + 1;
+      {  // n / d = the high 64 bits of n * ceil(2^64 / d), exactly, for n, d < 2^32
+        auto magic = [](uint64_t dv) { return dv > 1 ? ~0ull / dv + 1 : 0ull; };
+        d.inv_nx = magic((uint64_t)d.nx);
+        d.inv_nxy = magic((uint64_t)d.nx * (uint64_t)d.ny);
+      }
       box = make_uint2((uint32_t)d.bx0 | ((uint32_t)d.by0 << 10) | ((uint32_t)d.bz0 << 20),
                        (uint32_t)d.bx1 | ((uint32_t)d.by1 << 10) | ((uint32_t)d.bz1 << 20));
     }

@@ -74,6 +74,9 @@ struct OpDev {
   int32_t bx0, by0, bz0, bx1, by1, bz1;  // brick box (inclusive), from apply()'s voxel range
   int32_t nx, ny;                        // box extent in bricks (x, y)
   uint64_t pair_base;                    // index of the op's first (op, brick) pair
+  // ceil(2^64 / nx) and ceil(2^64 / (nx ny)) (0 for a divisor of 1): a pair's brick
+  // row and slab by one 64-bit high multiply instead of a division (brick_of_pair)
+  uint64_t inv_nx, inv_nxy;
   uint32_t code_off, code_len;           // SDF bytecode (uint2 records)
   uint32_t paint_off;                    // paint parameters (doubles)
   uint8_t kind, flags;
