@@ -132,3 +132,24 @@ def test_pool_budget_admission(built_lib):
     res, order = serving.serve(w, edits, np.zeros(len(edits)), max_batch=50, pool_budget=live + 8)
     # a 30-40 cm edit spans at least 3 x 3 x 3 bricks of 20 cm: none fits in 8
     assert (res["status"] == 3).all() and len(order) == 0
+
+
+@pytest.mark.gpu
+def test_derive_on_build_after_carves(built_lib):
+    """Derive on build over two builds: the penthouse, then 96 carves built on top
+    of it (no reset). The second build's super counts, density and GPU free list
+    come from the opaque counts finalize kept for the bricks the carves left
+    alone and recounted for the ones they rewrote; all must equal the oracle's
+    for the scene followed by the carves."""
+    vpm = 40.0
+    cfg = config.Config(vpm)
+    prog, _ = penthouse_program(vpm)
+    w = VoxelWorld(*cfg.dims, vpm=vpm, mode=MODE_MIXED, derive_on_build=True)
+    w._pending = prog
+    w.build()
+    edits, _ = serving.edit_stream(w.grid, cfg.bricks, vpm, 96, rate=0, seed=11)
+    carves = serving.carve_program(edits, range(len(edits)), vpm)
+    w._pending = carves
+    w.build()
+    o = pyoracle.OracleWorld(_concat_ir(prog, carves), vpm, cfg.dims)
+    assert_same_world(w, o)
