@@ -51,6 +51,9 @@ namespace px {
 #ifndef PX_VWIDE_MINB
 #define PX_VWIDE_MINB 3
 #endif
+#ifndef PX_PAINT_MINB
+#define PX_PAINT_MINB 3
+#endif
 #ifndef PX_VAFF_MINB
 #define PX_VAFF_MINB 3
 #endif
@@ -378,22 +381,35 @@ __device__ __forceinline__ void brick_bases(const FoldArgs& a, const OpDev* O, i
   bo[2] = {b2.x, b2.y};
 }
 
+// b + a0 u + a1 v for constant intervals b, a0, a1 and intervals u, v, in the
+// centre-radius form of aff32 (sdf32.cuh): [lower - R, upper + R + width(b)] with
+// R = sum |a.lo| width(w) + width(a) (|w.lo| + width(w)) over (a, w) = (a0, u), (a1, v).
+__device__ __forceinline__ Iv lin2(Iv b, Iv a0, Iv u, Iv a1, Iv v) {
+  const float du = __fsub_ru(u.hi, u.lo), dv = __fsub_ru(v.hi, v.lo);
+  const float lo = __fmaf_rd(a1.lo, v.lo, __fmaf_rd(a0.lo, u.lo, b.lo));
+  const float hi = __fmaf_ru(a1.lo, v.lo, __fmaf_ru(a0.lo, u.lo, b.lo));
+  float R = __fmaf_ru(fabsf(a0.lo), du, __fmul_ru(fabsf(a1.lo), dv));
+  R = __fmaf_ru(__fsub_ru(a0.hi, a0.lo), __fadd_ru(fabsf(u.lo), du), R);
+  R = __fmaf_ru(__fsub_ru(a1.hi, a1.lo), __fadd_ru(fabsf(v.lo), dv), R);
+  return {__fsub_rd(lo, R), __fadd_ru(__fadd_ru(hi, R), __fsub_ru(b.hi, b.lo))};
+}
+
 // The point through a rotation of the shape's frame (shapes.ts:263-320 on
 // intervals): p holds the pivot's two coordinates, cos and sin.
 __device__ __forceinline__ void rot32(uint32_t op, const Iv* __restrict__ p, Iv& x, Iv& y, Iv& z) {
-  const Iv p0 = ldp(p, 0), p1 = ldp(p, 1), c = ldp(p, 2), sn = ldp(p, 3);
+  const Iv p0 = ldp(p, 0), p1 = ldp(p, 1), c = ldp(p, 2), sn = ldp(p, 3), nsn = ineg(sn);
   if (op == OP_ROT_Y) {
     const Iv dx = isub(x, p0), dz = isub(z, p1);
-    x = iadd(iadd(p0, icmul(dx, c)), icmul(dz, sn));
-    z = iadd(isub(p1, icmul(dx, sn)), icmul(dz, c));
+    x = lin2(p0, c, dx, sn, dz);
+    z = lin2(p1, nsn, dx, c, dz);
   } else if (op == OP_ROT_X) {
     const Iv dy = isub(y, p0), dz = isub(z, p1);
-    y = iadd(iadd(p0, icmul(dy, c)), icmul(dz, sn));
-    z = iadd(isub(p1, icmul(dy, sn)), icmul(dz, c));
+    y = lin2(p0, c, dy, sn, dz);
+    z = lin2(p1, nsn, dy, c, dz);
   } else {
     const Iv dx = isub(x, p0), dy = isub(y, p1);
-    x = iadd(iadd(p0, icmul(dx, c)), icmul(dy, sn));
-    y = iadd(isub(p1, icmul(dx, sn)), icmul(dy, c));
+    x = lin2(p0, c, dx, sn, dy);
+    y = lin2(p1, nsn, dx, c, dy);
   }
 }
 
@@ -1079,7 +1095,7 @@ __device__ __forceinline__ uint32_t paint_voxel(const FoldArgs& a, const OpDev* 
 // item of the same sub-block may read its mask before or after the OR: it then
 // paints the voxel too or leaves it out, and either way stores the same value.
 template <int MODE>
-__global__ void __launch_bounds__(256) paint_kernel(FoldArgs a) {
+__global__ void __launch_bounds__(256, PX_PAINT_MINB) paint_kernel(FoldArgs a) {
   pdl_prologue();
   const int lane = threadIdx.x & 31;
   uint32_t resc = 0, viol = 0;

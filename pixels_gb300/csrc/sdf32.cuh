@@ -178,13 +178,32 @@ __device__ __forceinline__ Iv prim32(uint32_t op, int cnt, const Iv* __restrict_
 }
 
 // A run of rotations composed into x' = M x + t (code32 flag C32_AFFINE): p holds
-// M row by row, then t, as constant intervals.
+// M row by row, then t, as constant intervals.  In centre-radius form, with
+// directed fused multiply-adds and no sign selects: x_j lies in [c_j, c_j + d_j]
+// (c_j its lower bound, d_j its width rounded up) and M_rj in [m, m + e], so
+// M_rj x_j - m c_j = m (x_j - c_j) + (M_rj - m) x_j lies in [-R_rj, R_rj] with
+// R_rj = |m| d_j + e (|c_j| + d_j); sum_j m c_j + t.lo is bounded below and above
+// by chains of __fmaf_rd / __fmaf_ru (each rounds an exact a b + c), and the
+// row's interval is [lower - R, upper + R + (t.hi - t.lo)], every step outward.
 __device__ __forceinline__ void aff32(const Iv* __restrict__ p, Iv& x, Iv& y, Iv& z) {
+  const float c[3] = {x.lo, y.lo, z.lo};
+  const float d[3] = {__fsub_ru(x.hi, x.lo), __fsub_ru(y.hi, y.lo), __fsub_ru(z.hi, z.lo)};
+  const float g[3] = {__fadd_ru(fabsf(c[0]), d[0]), __fadd_ru(fabsf(c[1]), d[1]), __fadd_ru(fabsf(c[2]), d[2])};
   Iv o[3];
 #pragma unroll
-  for (int r = 0; r < 3; r++)
-    o[r] = iadd(iadd(iadd(ldp(p, 9 + r), icmul_any(x, ldp(p, 3 * r))), icmul_any(y, ldp(p, 3 * r + 1))),
-                icmul_any(z, ldp(p, 3 * r + 2)));
+  for (int r = 0; r < 3; r++) {
+    const Iv t = ldp(p, 9 + r);
+    float lo = t.lo, hi = t.lo, R = 0.f;
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      const Iv m = ldp(p, 3 * r + j);
+      lo = __fmaf_rd(m.lo, c[j], lo);
+      hi = __fmaf_ru(m.lo, c[j], hi);
+      R = __fmaf_ru(fabsf(m.lo), d[j], R);
+      R = __fmaf_ru(__fsub_ru(m.hi, m.lo), g[j], R);
+    }
+    o[r] = {__fsub_rd(lo, R), __fadd_ru(__fadd_ru(hi, R), __fsub_ru(t.hi, t.lo))};
+  }
   x = o[0];
   y = o[1];
   z = o[2];
