@@ -28,21 +28,17 @@ __device__ __forceinline__ Iv iv(float a) { return {a, a}; }
 __device__ __forceinline__ Iv iadd(Iv a, Iv b) { return {__fadd_rd(a.lo, b.lo), __fadd_ru(a.hi, b.hi)}; }
 __device__ __forceinline__ Iv isub(Iv a, Iv b) { return {__fsub_rd(a.lo, b.hi), __fsub_ru(a.hi, b.lo)}; }
 __device__ __forceinline__ Iv ineg(Iv a) { return {-a.hi, -a.lo}; }
-__device__ __forceinline__ Iv iabs(Iv a) {
-  if (a.lo >= 0.f) return a;
-  if (a.hi <= 0.f) return {-a.hi, -a.lo};
-  return {0.f, fmaxf(-a.lo, a.hi)};
-}
+// |a|: the least magnitude is max(lo, -hi, 0) and the largest max(-lo, hi), the
+// same bounds as the case split, in three min/max operations and no selects
+__device__ __forceinline__ Iv iabs(Iv a) { return {fmaxf(fmaxf(a.lo, -a.hi), 0.f), fmaxf(-a.lo, a.hi)}; }
 __device__ __forceinline__ Iv imax0(Iv a) { return {fmaxf(a.lo, 0.f), fmaxf(a.hi, 0.f)}; }
 __device__ __forceinline__ Iv imin0(Iv a) { return {fminf(a.lo, 0.f), fminf(a.hi, 0.f)}; }
 __device__ __forceinline__ Iv imax(Iv a, Iv b) { return {fmaxf(a.lo, b.lo), fmaxf(a.hi, b.hi)}; }
 __device__ __forceinline__ Iv imin(Iv a, Iv b) { return {fminf(a.lo, b.lo), fminf(a.hi, b.hi)}; }
 __device__ __forceinline__ Iv iclamp01(Iv a) { return {fminf(fmaxf(a.lo, 0.f), 1.f), fminf(fmaxf(a.hi, 0.f), 1.f)}; }
 __device__ __forceinline__ Iv isqr(Iv a) {
-  float l = fabsf(a.lo), h = fabsf(a.hi);
-  float mn = (a.lo <= 0.f && a.hi >= 0.f) ? 0.f : fminf(l, h);
-  float mx = fmaxf(l, h);
-  return {__fmul_rd(mn, mn), __fmul_ru(mx, mx)};
+  const Iv m = iabs(a);  // the least and largest magnitude
+  return {__fmul_rd(m.lo, m.lo), __fmul_ru(m.hi, m.hi)};
 }
 // Bounds of sqrt(v), v >= 0, from the hardware reciprocal square root.  CUDA
 // documents rsqrtf's maximum error as 2 ulp: 1/sqrt(v) = r (1 + d) with
@@ -64,10 +60,14 @@ __device__ __forceinline__ float sqrt_hi(float v) {
   return __fmul_ru(__fmul_ru(v, rsqrtf(v)), 1.f + 0x1p-20f);
 }
 __device__ __forceinline__ Iv isqrt(Iv a) { return {sqrt_lo(fmaxf(a.lo, 0.f)), sqrt_hi(fmaxf(a.hi, 0.f))}; }
-// x * c for a constant interval c that does not straddle zero (or is [0, 0])
+// x * c for a constant interval c that does not straddle zero (or is [0, 0]): the
+// sign of x picks which end of c bounds each product, so the bound is the lesser
+// (greater) of the two directed products -- two multiplies and a min/max in place
+// of a compare and a select
 __device__ __forceinline__ Iv icmul(Iv x, Iv c) {
-  if (c.lo >= 0.f) return {__fmul_rd(x.lo, x.lo >= 0.f ? c.lo : c.hi), __fmul_ru(x.hi, x.hi >= 0.f ? c.hi : c.lo)};
-  return {__fmul_rd(x.hi, x.hi >= 0.f ? c.lo : c.hi), __fmul_ru(x.lo, x.lo >= 0.f ? c.hi : c.lo)};
+  if (c.lo >= 0.f)
+    return {fminf(__fmul_rd(x.lo, c.lo), __fmul_rd(x.lo, c.hi)), fmaxf(__fmul_ru(x.hi, c.hi), __fmul_ru(x.hi, c.lo))};
+  return {fminf(__fmul_rd(x.hi, c.lo), __fmul_rd(x.hi, c.hi)), fmaxf(__fmul_ru(x.lo, c.hi), __fmul_ru(x.lo, c.lo))};
 }
 // x * c for any constant interval c (one that straddles zero is bounded by its magnitude)
 __device__ __forceinline__ Iv icmul_any(Iv x, Iv c) {
