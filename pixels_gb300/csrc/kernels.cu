@@ -543,11 +543,31 @@ __global__ void __launch_bounds__(256, MODE == 1 ? PX_CLASSIFY_MINB : PX_CLASSIF
     const unsigned long long p = (unsigned long long)chunk * 32 + lane;
     const bool valid = p < P;
     uint32_t o = ce.y & 0x7fffffffu;
-    if (valid && !(ce.y >> 31))  // the chunk spans several ops
-      while (o + 1 < a.n_ops && a.ops[o + 1].pair_base <= p) o++;
+    if (!(ce.y >> 31)) {  // the chunk spans several ops (at most 32 start in it; warp-uniform)
+      // lane j holds the first pair of op o + 1 + j; a lane's op is o plus the number of
+      // those at or below its pair (sorted: a binary search over the lanes, by shuffles)
+      const unsigned long long pb =
+          o + 1 + (uint32_t)lane < a.n_ops ? __ldg(&a.ops[o + 1 + lane].pair_base) : ~0ull;
+      // (33 possible counts: six halvings; every lane shuffles each time, from lane <= 31)
+      uint32_t lo = 0, hi = 32;
+#pragma unroll
+      for (int k = 0; k < 6; k++) {
+        const uint32_t mid = min((lo + hi) >> 1, 31u);
+        const unsigned long long v = __shfl_sync(FULLMASK, pb, (int)mid);
+        if (lo < hi) {
+          if (v <= p) lo = mid + 1;
+          else hi = mid;
+        }
+      }
+      o += lo;
+    }
     const OpDev* O = a.ops + o;
     int bx = 0, by = 0, bz = 0, cls = PC_SKIP;
-    if (valid) {
+    // a pair outside its op's bricks cannot happen; if it did, it would be reported, not used
+    const bool in_op = valid && p >= O->pair_base &&
+                       p - O->pair_base < (unsigned long long)O->nx * O->ny * (unsigned long long)(O->bz1 - O->bz0 + 1);
+    if (valid && !in_op) atomicOr(&a.res->status, (uint32_t)ST_CHAIN);
+    if (in_op) {
       brick_of_pair(O, p, bx, by, bz);
       const int flags = O->flags;
       const bool contained = (flags & OPF_CONTAINS) && bx >= O->cbx0 && bx <= O->cbx1 && by >= O->cby0 &&
