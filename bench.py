@@ -536,28 +536,55 @@ def main():
         _lib.build(h2, MODE_MIXED, s_ptr)
     pipe_streams = [torch.cuda.Stream(dev), torch.cuda.Stream(dev)]
 
-    def read_outputs(hh):
-        assert L.px_read_grid(hh, grid_h.data_ptr(), grid_h.numel()) == 0
-        assert L.px_read_pool(hh, pool_h.data_ptr(), pool_h.numel()) == 0
-        assert L.px_read_super(hh, super_h.data_ptr(), super_h.numel()) == 0
-        assert L.px_read_density(hh, dens_h.data_ptr(), dens_h.numel()) == 0
-        assert L.px_read_free_list(hh, MAX_BRICKS, free_h.data_ptr(), free_h.numel(), ctypes.byref(free_len)) == 0
+    class _DeviceArray:  # a world's device buffer seen through the CUDA array interface (no copy)
+        def __init__(self, ptr, n, typestr):
+            self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (ptr, False), "version": 3}
+
+    def dev_tensor(ptr, n, typestr):
+        return torch.as_tensor(_DeviceArray(ptr, n, typestr), device=dev)
+
+    # per world: pinned host copies of its outputs, and an event after their copies
+    outs = [{"grid": torch.empty_like(grid_h).pin_memory(), "pool": torch.empty_like(pool_h).pin_memory(),
+             "super": torch.empty_like(super_h).pin_memory(), "dens": torch.empty_like(dens_h).pin_memory(),
+             "free": torch.empty_like(free_h).pin_memory()} for _ in range(2)]
+    copy_stream = torch.cuda.Stream(dev)
+    copied = [torch.cuda.Event(), torch.cuda.Event()]
+
+    def copy_outputs(hh, k):
+        """Device-to-host copies of every output of world hh on the copy stream (the
+        device view of the public API), not waited for by the host."""
+        v = _lib.device_view(hh)
+        used_k = _lib.stats(hh)["pool_used"]
+        o = outs[k]
+        with torch.cuda.stream(copy_stream):
+            o["grid"].copy_(dev_tensor(v.grid, n_bricks, "<i4"), non_blocking=True)
+            o["pool"][:used_k * 512].copy_(dev_tensor(v.pool, used_k * 512, "<i2"), non_blocking=True)
+            o["super"].copy_(dev_tensor(v.super_counts, n_super, "<i4"), non_blocking=True)
+            o["dens"].copy_(dev_tensor(v.density, n_bricks, "|u1"), non_blocking=True)
+            o["free"][:v.free_len].copy_(dev_tensor(v.free_list, v.free_len, "<i4"), non_blocking=True)
+            copied[k].record(copy_stream)
 
     def e2e_pipelined(n: int) -> float:
         hs = (h, h2)
         torch.cuda.synchronize()
         barrier()
         t0 = time.perf_counter()
+        busy = [False, False]  # the world's outputs are still being copied out
         for i in range(n + 1):
             if i < n:
-                hh, st_ = hs[i % 2], pipe_streams[i % 2].cuda_stream
-                _lib.world_reset(hh, False, st_)
+                k = i % 2
+                hh, st = hs[k], pipe_streams[k]
+                if busy[k]:
+                    st.wait_event(copied[k])  # on the device: its readback first, then its reset
+                _lib.world_reset(hh, False, st.cuda_stream)
                 assert L.px_submit_ops(hh, ir_buf, len(ir)) == 0
-                _lib.build_enqueue(hh, MODE_MIXED, st_)
+                _lib.build_enqueue(hh, MODE_MIXED, st.cuda_stream)
             if i > 0:
-                hp = hs[(i - 1) % 2]
-                _lib.build_finish(hp)
-                read_outputs(hp)
+                k = (i - 1) % 2
+                _lib.build_finish(hs[k])
+                copy_outputs(hs[k], k)
+                busy[k] = True
+        copy_stream.synchronize()
         return (time.perf_counter() - t0) / n
 
     t_pipe = None
@@ -653,9 +680,10 @@ def main():
                 "ms_per_step": round(t_e2e * 1e3, 3),
                 "reads": "grid, pool, super counts, density, free list",
                 "pipelined": t_pipe is not None,
-                "how": "two worlds built alternately on two CUDA streams: step i's readback (blocking copies "
-                       "to pinned host memory) overlaps step i+1's build; every step resets its world, submits "
-                       "the op list from host memory, builds and reads every output back",
+                "how": "two worlds built alternately on two CUDA streams; every step resets its world, submits "
+                       "the op list from host memory, builds, and copies every output (the public device view) "
+                       "to pinned host memory on a third stream, overlapping the next step's build; the timed "
+                       "region ends when the last copy has landed",
                 "serial": {"value": round(job_value(world, cells, t_e2e_serial), 4),
                            "ms_per_step": round(t_e2e_serial * 1e3, 3)},
                 "split_ms": ({k: round(statistics.mean(p[j] for p in e2e_parts) * 1e3, 3)
