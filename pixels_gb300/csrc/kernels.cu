@@ -193,11 +193,100 @@ __global__ void __launch_bounds__(256) cull_kernel(const uint2* __restrict__ box
   }
 }
 
-void launch_cull(const uint2* boxes, int n_ops, int TX, int TY, int TZ, uint32_t* tile_cnt, uint32_t* tile_off,
-                 uint32_t* tile_ops, uint2* tile_boxes, uint32_t* counter, cudaStream_t s) {
+// The same lists with the ops grouped in space: the host orders the ops along a
+// Morton curve of their box centres and stores one union box per 32 of that order
+// (order[] after the group boxes), so that a group's box is compact even where
+// consecutive ops lie far apart (scattered primitives).  A warp marks its tile's
+// ops in a bit set in shared memory (one bit per op) and then writes them in op
+// order from it.  W: words of the bit set (ops / 32, rounded up).
+__global__ void __launch_bounds__(256) cull_sorted_kernel(const uint2* __restrict__ boxes, int n_ops, int TX, int TY,
+                                                          int TZ, int W, uint32_t* tile_cnt, uint32_t* tile_off,
+                                                          uint32_t* tile_ops, uint2* tile_boxes, uint32_t* counter) {
+  pdl_prologue();
+  extern __shared__ uint32_t s_bits[];  // [8][W]
+  __shared__ uint32_t s_cnt[8], s_base;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int n_tiles = TX * TY * TZ;
-  launch_pdl(cull_kernel, dim3((n_tiles + 7) / 8), dim3(256), 0, s, boxes, n_ops, TX, TY, TZ, tile_cnt, tile_off,
-             tile_ops, tile_boxes, counter);
+  const int n_groups = (n_ops + 31) / 32;
+  const uint2* __restrict__ gboxes = boxes + n_ops;
+  const uint32_t* __restrict__ order = reinterpret_cast<const uint32_t*>(boxes + n_ops + n_groups);
+  uint32_t* bits = s_bits + (size_t)warp * W;
+  const int tile = blockIdx.x * 8 + warp;
+  const bool valid = tile < n_tiles;
+  int tz = 0, ty = 0, tx = 0;
+  if (valid) {
+    tz = tile / (TX * TY);
+    const int r = tile - tz * TX * TY;
+    ty = r / TX;
+    tx = r - ty * TX;
+  }
+  for (int k = lane; k < W; k += 32) bits[k] = 0u;
+  __syncwarp();
+  if (valid) {
+    for (int g0 = 0; g0 < n_groups; g0 += 32) {
+      const int gi = g0 + lane;
+      uint32_t gm = __ballot_sync(FULLMASK, gi < n_groups && box_overlaps_tile(__ldg(gboxes + gi), tx, ty, tz));
+      while (gm) {
+        const int k = (g0 + __ffs(gm) - 1) * 32 + lane;
+        gm &= gm - 1;
+        if (k < n_ops) {
+          const uint32_t i = __ldg(order + k);
+          if (box_overlaps_tile(__ldg(boxes + i), tx, ty, tz)) atomicOr(bits + (i >> 5), 1u << (i & 31));
+        }
+      }
+    }
+  }
+  __syncwarp();
+  uint32_t cnt = 0;
+  for (int k = lane; k < W; k += 32) cnt += __popc(bits[k]);
+#pragma unroll
+  for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(FULLMASK, cnt, o);
+  if (lane == 0) s_cnt[warp] = valid ? cnt : 0u;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t sum = 0;
+    for (int k = 0; k < 8; k++) sum += s_cnt[k];
+    s_base = sum ? atomicAdd(counter, sum) : 0u;
+  }
+  __syncthreads();
+  if (!valid) return;
+  uint32_t pos = s_base;
+  for (int k = 0; k < warp; k++) pos += s_cnt[k];
+  if (lane == 0) {
+    tile_cnt[tile] = cnt;
+    tile_off[tile] = pos;
+  }
+  // the ops in order: lane l writes the ops of word w0 + l after those of the words before it
+  for (int w0 = 0; w0 < W && cnt; w0 += 32) {
+    const uint32_t word = w0 + lane < W ? bits[w0 + lane] : 0u;
+    const uint32_t c = __popc(word);
+    uint32_t incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(FULLMASK, incl, o);
+      if (lane >= o) incl += t;
+    }
+    uint32_t at = pos + incl - c;
+    for (uint32_t m = word; m; m &= m - 1) {
+      const uint32_t i = (uint32_t)(w0 + lane) * 32u + (uint32_t)(__ffs(m) - 1);
+      tile_ops[at] = i;
+      tile_boxes[at] = __ldg(boxes + i);  // the op's brick box beside it, for the apply pass
+      at++;
+    }
+    pos += __shfl_sync(FULLMASK, incl, 31);
+  }
+}
+
+void launch_cull(const uint2* boxes, int n_ops, int TX, int TY, int TZ, uint32_t* tile_cnt, uint32_t* tile_off,
+                 uint32_t* tile_ops, uint2* tile_boxes, uint32_t* counter, bool sorted, cudaStream_t s) {
+  const int n_tiles = TX * TY * TZ;
+  const int W = (n_ops + 31) / 32;
+  if (sorted)
+    launch_pdl(cull_sorted_kernel, dim3((n_tiles + 7) / 8), dim3(256), (size_t)8 * W * 4, s, boxes, n_ops, TX, TY, TZ,
+               W, tile_cnt, tile_off, tile_ops, tile_boxes, counter);
+  else
+    launch_pdl(cull_kernel, dim3((n_tiles + 7) / 8), dim3(256), 0, s, boxes, n_ops, TX, TY, TZ, tile_cnt, tile_off,
+               tile_ops, tile_boxes, counter);
 }
 
 // ---------------------------------------------------------------------------

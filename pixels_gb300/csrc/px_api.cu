@@ -104,6 +104,8 @@ struct px_world {
 
   // per-build device scratch
   DevBuf d_ops, d_boxes, d_code, d_params, d_code32, d_p32, d_bases;
+  std::vector<uint32_t> h_cull_order;  // the ops along a Morton curve of their boxes (cull_sorted_kernel)
+  bool cull_sorted = false;
   DevBuf tile_cnt, tile_off, tile_ops, tile_boxes;
   DevBuf evt, fsrc, cnt, pos, etype, ew, depth, tree, replay_tmp;
   DevBuf staging, stage_cell, stage_src, touched;
@@ -1196,7 +1198,7 @@ int reserve_build_scratch(px_world* w, uint64_t P, uint32_t max_ops) {
     const size_t n = max_ops ? max_ops : 1;
     const void* before[7] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p, w->d_p32.p, w->d_bases.p};
     int rc0;
-    if ((rc0 = ensure(w, w->d_ops, sizeof(OpDev) * n)) || (rc0 = ensure(w, w->d_boxes, sizeof(uint2) * (n + (n + 31) / 32))) ||
+    if ((rc0 = ensure(w, w->d_ops, sizeof(OpDev) * n)) || (rc0 = ensure(w, w->d_boxes, sizeof(uint2) * (n + (n + 31) / 32 + (n + 1) / 2))) ||
         (rc0 = ensure(w, w->d_code, sizeof(uint2) * n)) || (rc0 = ensure(w, w->d_params, sizeof(double) * 16 * n)) ||
         (rc0 = ensure(w, w->d_code32, sizeof(uint32_t) * n)) || (rc0 = ensure(w, w->d_p32, sizeof(float2) * 16 * n)) ||
         (rc0 = ensure(w, w->d_bases, sizeof(float2) * 192 * n)))
@@ -1539,7 +1541,7 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   const void* op_bufs_before[9] = {w->d_ops.p, w->d_boxes.p, w->d_code.p, w->d_params.p, w->d_code32.p,
                                    w->d_p32.p, w->d_bases.p, w->chunk_op.p, w->chunk_op.p};
   if ((rc = ensure(w, w->d_ops, sizeof(OpDev) * (size_t)n_ops)) ||
-      (rc = ensure(w, w->d_boxes, sizeof(uint2) * ((size_t)n_ops + (n_ops + 31) / 32))) ||
+      (rc = ensure(w, w->d_boxes, sizeof(uint2) * ((size_t)n_ops + (n_ops + 31) / 32 + (n_ops + 1) / 2))) ||
       (rc = ensure(w, w->d_code, sizeof(uint2) * w->code.size())) ||
       (rc = ensure(w, w->d_params, sizeof(double) * w->params.size())) ||
       (rc = ensure(w, w->d_code32, sizeof(uint32_t) * w->code32.size())) ||
@@ -1566,24 +1568,68 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   ups.clear();
   if (upload) {
     ups.push_back({w->d_ops.p, w->ops.data(), sizeof(OpDev) * (size_t)n_ops});
-    {  // op boxes, then the union box of every 32 consecutive ops (cull_count_kernel)
+    {  // op boxes, then the union box of every 32 ops of the culling order (cull_kernel /
+       // cull_sorted_kernel), then that order: along a Morton curve of the boxes' centres
+       // (in 4-brick tiles) when the sorted kernel is used, else the op order itself
       const int n_groups = (n_ops + 31) / 32;
-      w->h_boxes.assign(w->boxes.begin(), w->boxes.end());
-      for (int g = 0; g < n_groups; g++) {
-        uint32_t lo[3] = {1023, 1023, 1023}, hi[3] = {0, 0, 0};
-        bool any = false;
-        for (int i = g * 32; i < n_ops && i < g * 32 + 32; i++) {
-          const uint2 b = w->boxes[i];
-          if (b.x >> 30) continue;
-          any = true;
-          for (int k = 0; k < 3; k++) {
-            lo[k] = std::min(lo[k], (b.x >> (10 * k)) & 1023u);
-            hi[k] = std::max(hi[k], (b.y >> (10 * k)) & 1023u);
+      // the union boxes of 32 ops of an order, and the tiles they cover in all (the
+      // group tests a tile passes grow with it)
+      auto group_boxes = [&](const std::vector<uint32_t>& ord, std::vector<uint2>& gb) {
+        uint64_t vol = 0;
+        gb.clear();
+        for (int g = 0; g < n_groups; g++) {
+          uint32_t lo[3] = {1023, 1023, 1023}, hi[3] = {0, 0, 0};
+          bool any = false;
+          for (int k = g * 32; k < n_ops && k < g * 32 + 32; k++) {
+            const uint2 b = w->boxes[ord[k]];
+            if (b.x >> 30) continue;
+            any = true;
+            for (int a = 0; a < 3; a++) {
+              lo[a] = std::min(lo[a], (b.x >> (10 * a)) & 1023u);
+              hi[a] = std::max(hi[a], (b.y >> (10 * a)) & 1023u);
+            }
           }
+          gb.push_back(any ? make_uint2(lo[0] | (lo[1] << 10) | (lo[2] << 20), hi[0] | (hi[1] << 10) | (hi[2] << 20))
+                           : make_uint2(3u << 30, 0u));
+          if (any) vol += (uint64_t)(hi[0] / 4 - lo[0] / 4 + 1) * (hi[1] / 4 - lo[1] / 4 + 1) * (hi[2] / 4 - lo[2] / 4 + 1);
         }
-        w->h_boxes.push_back(any ? make_uint2(lo[0] | (lo[1] << 10) | (lo[2] << 20), hi[0] | (hi[1] << 10) | (hi[2] << 20))
-                                 : make_uint2(3u << 30, 0u));
+        return vol;
+      };
+      std::vector<uint32_t>& ord = w->h_cull_order;
+      ord.resize(n_ops);
+      for (int i = 0; i < n_ops; i++) ord[i] = (uint32_t)i;
+      std::vector<uint2> gb_seq, gb_mc;
+      const uint64_t vol_seq = group_boxes(ord, gb_seq);
+      bool sorted = false;
+      if (n_ops <= CULL_SORTED_MAX_OPS && n_groups > 1) {
+        auto spread = [](uint32_t v) {  // 8 bits -> every third bit
+          uint32_t r = 0;
+          for (int k = 0; k < 8; k++) r |= ((v >> k) & 1u) << (3 * k);
+          return r;
+        };
+        std::vector<uint32_t> key(n_ops), mc(ord);
+        for (int i = 0; i < n_ops; i++) {
+          const uint2 b = w->boxes[i];
+          if (b.x >> 30) { key[i] = 0xffffffffu; continue; }  // no bricks: last
+          uint32_t c[3];
+          for (int a = 0; a < 3; a++) c[a] = ((((b.x >> (10 * a)) & 1023u) + ((b.y >> (10 * a)) & 1023u)) >> 3) & 255u;
+          key[i] = spread(c[0]) | (spread(c[1]) << 1) | (spread(c[2]) << 2);
+        }
+        std::stable_sort(mc.begin(), mc.end(), [&](uint32_t x, uint32_t y) { return key[x] < key[y]; });
+        // the spatial order where its groups cover less than half the tiles the op order's
+        // do: scattered ops (the sorted kernel's bit set costs more on compact scenes)
+        if (2 * group_boxes(mc, gb_mc) < vol_seq) {
+          sorted = true;
+          ord.swap(mc);
+        }
       }
+      w->cull_sorted = sorted;
+      w->h_boxes.assign(w->boxes.begin(), w->boxes.end());
+      const std::vector<uint2>& gb = sorted ? gb_mc : gb_seq;
+      w->h_boxes.insert(w->h_boxes.end(), gb.begin(), gb.end());
+      if (sorted)  // the order, two per uint2
+        for (int k = 0; k < n_ops; k += 2)
+          w->h_boxes.push_back(make_uint2(ord[k], k + 1 < n_ops ? ord[k + 1] : 0u));
       ups.push_back({w->d_boxes.p, w->h_boxes.data(), sizeof(uint2) * w->h_boxes.size()});
     }
     ups.push_back({w->d_code.p, w->code.data(), sizeof(uint2) * w->code.size()});
@@ -1605,7 +1651,7 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   BuildResult* res = (BuildResult*)w->res.p;
   launch_cull((const uint2*)w->d_boxes.p, n_ops, w->TX, w->TY, w->TZ, (uint32_t*)w->tile_cnt.p,
               (uint32_t*)w->tile_off.p, (uint32_t*)w->tile_ops.p, (uint2*)w->tile_boxes.p,
-              (uint32_t*)w->chunk_counter.p + CULL_COUNTER, s);
+              (uint32_t*)w->chunk_counter.p + CULL_COUNTER, w->cull_sorted, s);
   // the classify pass's chunk order, computed while the cull kernels run
   const size_t n_chunks = (P + 31) / 32;
   if (upload) {

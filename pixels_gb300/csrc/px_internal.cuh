@@ -261,9 +261,13 @@ struct FoldArgs {
 constexpr uint32_t TAG_STAGED = 0x40000000u;
 
 // Host-side launch wrappers (kernels.cu)
-// counter: a zeroed word (the tile lists' reservation count)
+// counter: a zeroed word (the tile lists' reservation count).  sorted: boxes holds
+// the op boxes, the union boxes of 32 ops in the order after them, then that order
+// (cull_sorted_kernel, up to CULL_SORTED_MAX_OPS ops); else the union boxes of 32
+// consecutive ops
+constexpr int CULL_SORTED_MAX_OPS = 47 * 1024;  // 8 warps x ops / 8 bytes of shared memory: 47 KiB
 void launch_cull(const uint2* boxes, int n_ops, int TX, int TY, int TZ, uint32_t* tile_cnt, uint32_t* tile_off,
-                 uint32_t* tile_ops, uint2* tile_boxes, uint32_t* counter, cudaStream_t s);
+                 uint32_t* tile_ops, uint2* tile_boxes, uint32_t* counter, bool sorted, cudaStream_t s);
 // max_blocks > 0 caps the persistent grids (builds sharing the GPU)
 // The evaluation passes (classify .. paint) go on s; the apply pass on s_apply,
 // after eval_done is recorded on s (s_apply == s: one stream, no event).
