@@ -202,8 +202,8 @@ struct FoldArgs {
   uint16_t* psub;             // per partial pair: 2 bits per sub-block (PC_*)
   unsigned long long* pmask;  // per partial pair: 8 inside-masks (bit = x&3 | (y&3)<<2 | (z&3)<<4)
   uint32_t* chunk_counter;
-  // voxels whose float32 interval cannot decide them, left by voxel_lean_kernel
-  // to voxel_kernel<1, 1> (which carries the float64 evaluator): (op | voxel bit << 24 |
+  // voxels whose float32 interval cannot decide them, left by voxel_lean_kernel to
+  // paint_kernel<1> (which resolves them in float64 first): (op | voxel bit << 24 |
   // undecided-crossing-test << 30, pair << 3 | sub-block, interval lo, hi bits)
   uint4* rescue;
   uint32_t rescue_cap;
