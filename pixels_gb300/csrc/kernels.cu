@@ -470,21 +470,9 @@ __device__ __forceinline__ void brick_bases(const FoldArgs& a, const OpDev* O, i
   bo[2] = {b2.x, b2.y};
 }
 
-// b + a0 u + a1 v for constant intervals b, a0, a1 and intervals u, v, in the
-// centre-radius form of aff32 (sdf32.cuh): [lower - R, upper + R + width(b)] with
-// R = sum |a.lo| width(w) + width(a) (|w.lo| + width(w)) over (a, w) = (a0, u), (a1, v).
-__device__ __forceinline__ Iv lin2(Iv b, Iv a0, Iv u, Iv a1, Iv v) {
-  const float du = __fsub_ru(u.hi, u.lo), dv = __fsub_ru(v.hi, v.lo);
-  const float lo = __fmaf_rd(a1.lo, v.lo, __fmaf_rd(a0.lo, u.lo, b.lo));
-  const float hi = __fmaf_ru(a1.lo, v.lo, __fmaf_ru(a0.lo, u.lo, b.lo));
-  float R = __fmaf_ru(fabsf(a0.lo), du, __fmul_ru(fabsf(a1.lo), dv));
-  R = __fmaf_ru(__fsub_ru(a0.hi, a0.lo), __fadd_ru(fabsf(u.lo), du), R);
-  R = __fmaf_ru(__fsub_ru(a1.hi, a1.lo), __fadd_ru(fabsf(v.lo), dv), R);
-  return {__fsub_rd(lo, R), __fadd_ru(__fadd_ru(hi, R), __fsub_ru(b.hi, b.lo))};
-}
-
 // The point through a rotation of the shape's frame (shapes.ts:263-320 on
-// intervals): p holds the pivot's two coordinates, cos and sin.
+// intervals, in the centre-radius form of lin2): p holds the pivot's two
+// coordinates, cos and sin.
 __device__ __forceinline__ void rot32(uint32_t op, const Iv* __restrict__ p, Iv& x, Iv& y, Iv& z) {
   const Iv p0 = ldp(p, 0), p1 = ldp(p, 1), c = ldp(p, 2), sn = ldp(p, 3), nsn = ineg(sn);
   if (op == OP_ROT_Y) {
