@@ -221,7 +221,7 @@ const char* px_last_error(px_world* w);
    px_batch_create takes worlds that each hold a built scene (px_build done,
    no ops queued), rebuilds each once from its last op list to size every
    buffer, then captures the rebuild of all of them (reset + the same ops) into
-   one graph over n_streams streams, largest scenes first; pairs_per_block
+   one graph over n_streams streams (1-256), largest scenes first; pairs_per_block
    sizes each scene's persistent grids to its (op, brick) pairs (0: whole GPU
    per kernel).  px_batch_run launches the graph on `stream`, waits, and
    updates every world (reads work as after px_build); device_ms (may be NULL)

@@ -17,7 +17,7 @@ import statistics
 from . import _lib
 
 # launch shapes the autotuner tries: (streams, pairs per block)
-SHAPES = ((1, 0), (8, 0), (32, 0), (8, 256), (32, 256), (32, 2048), (64, 1024))
+SHAPES = ((1, 0), (8, 0), (32, 0), (8, 256), (32, 128), (32, 256), (32, 2048), (64, 256), (64, 1024), (128, 256))
 
 
 class Batch:

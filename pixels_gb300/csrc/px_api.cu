@@ -2231,7 +2231,7 @@ static int batch_create_impl(px_world* const* worlds, size_t n, int mode, uint32
                     px_batch** out) {
   if (!out) return PX_E_INVALID_ARG;
   *out = nullptr;
-  if (!worlds || n == 0 || n_streams == 0 || n_streams > 64 || (mode != PX_MODE_FP64 && mode != PX_MODE_MIXED))
+  if (!worlds || n == 0 || n_streams == 0 || n_streams > 256 || (mode != PX_MODE_FP64 && mode != PX_MODE_MIXED))
     return PX_E_INVALID_ARG;
   for (size_t i = 0; i < n; i++) {
     px_world* w = worlds[i];
