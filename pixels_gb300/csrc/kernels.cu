@@ -561,10 +561,10 @@ __device__ __forceinline__ void classify_finish(const FoldArgs& a, bool valid, u
   if (__any_sync(FULLMASK, fullp)) {
     const bool back = MODE == 1 && O->paint32_off != NO_SLOT;
 #pragma unroll
-    for (int e = 0; e < 2; e++) {  // front: 16 half sub-blocks per pair; back: 8 sub-blocks
+    for (int e = 0; e < 2; e++) {  // front: 16 half sub-blocks per pair; back: the pair (bit 30)
       const uint32_t fm = __ballot_sync(FULLMASK, fullp && back == (e == 1));
       if (!fm) continue;
-      const uint32_t per = e ? 8u : 16u;
+      const uint32_t per = e ? 1u : 16u;
       uint32_t pb = 0;
       if (lane == 0) pb = atomicAdd(a.paint_item_counter + e, per * __popc(fm));
       pb = __shfl_sync(FULLMASK, pb, 0);
@@ -572,7 +572,7 @@ __device__ __forceinline__ void classify_finish(const FoldArgs& a, bool valid, u
         const uint32_t at = pb + per * __popc(fm & ((1u << lane) - 1u));
         for (uint32_t q = 0; q < per; q++)
           if (at + q < a.paint_items_cap) {
-            if (e) a.paint_items[a.paint_items_cap - 1 - (at + q)] = make_uint2(o, (uint32_t)(p << 3) | q);
+            if (e) a.paint_items[a.paint_items_cap - 1 - (at + q)] = make_uint2(o | (1u << 30), (uint32_t)(p << 3));
             else a.paint_items[at + q] = make_uint2(o | ((q & 1u) << 31), (uint32_t)(p << 3) | (q >> 1));
           }
       }
@@ -1230,19 +1230,15 @@ __global__ void __launch_bounds__(256, PX_PAINT_MINB) paint_kernel(FoldArgs a) {
     const uint32_t it = wb.next(a.paint_counter, 2, lane);
     if (it >= n_items) break;
     const uint2 item = __ldg(a.paint_items + (it < n_front ? it : a.paint_items_cap - 1 - (it - n_front)));
-    // a float64 item (the front) is half a sub-block: voxel rows r = bit 31 of its op field
+    // a float64 item (the front) is half a sub-block: voxel rows r = bit 31 of its op field;
+    // a float32 item (the back) a sub-block, or with bit 30 a whole full pair (8 sub-blocks)
     const int r0 = it < n_front ? (int)(item.x >> 31) : 0, r1 = it < n_front ? r0 + 1 : 2;
-    const OpDev* O = a.ops + (item.x & 0x7fffffffu);
+    const bool whole = it >= n_front && ((item.x >> 30) & 1u);
+    const OpDev* O = a.ops + (item.x & 0xffffffu);
     const unsigned long long pair = item.y >> 3;
-    const int s = (int)(item.y & 7u);
+    const int s0 = (int)(item.y & 7u);
     const uint32_t slot = O->paint_slot + (uint32_t)(pair - O->pair_base);
-    const int cls = __ldg(a.pcode + pair);
-    unsigned long long m = ~0ull;
-    if (cls != PC_FULL) {
-      const uint32_t c = (__ldg(a.psub + pair) >> (2 * s)) & 3u;
-      m = c == PC_FULL ? ~0ull : c == PC_PARTIAL ? __ldcg(a.pmask + pair * 8 + s) : 0ull;
-    }
-    if (!m) continue;
+    const int cls = whole ? (int)PC_FULL : (int)__ldg(a.pcode + pair);
     int bx, by, bz;
     brick_of_pair(O, pair, bx, by, bz);
     const uint32_t pk = O->paint_kind;
@@ -1250,12 +1246,20 @@ __global__ void __launch_bounds__(256, PX_PAINT_MINB) paint_kernel(FoldArgs a) {
     Iv bo[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
     if (try32 && pk != PK_NOISE) brick_bases(a, O, bx, by, bz, bo);
 #pragma unroll 1
-    for (int r = r0; r < r1; r++) {
-      const int e = r * 32 + lane;
-      if (!((m >> e) & 1ull)) continue;
-      const int lx = (s & 1) * 4 + (e & 3), ly = ((s >> 1) & 1) * 4 + ((e >> 2) & 3), lz = ((s >> 2) & 1) * 4 + (e >> 4);
-      a.pvals[(size_t)slot * 512 + (uint32_t)(lx | (ly << 3) | (lz << 6))] =
-          paint_voxel<MODE>(a, O, bx, by, bz, bo, lx, ly, lz, resc, viol);
+    for (int s = whole ? 0 : s0; s <= (whole ? 7 : s0); s++) {
+      unsigned long long m = ~0ull;
+      if (cls != PC_FULL) {
+        const uint32_t c = (__ldg(a.psub + pair) >> (2 * s)) & 3u;
+        m = c == PC_FULL ? ~0ull : c == PC_PARTIAL ? __ldcg(a.pmask + pair * 8 + s) : 0ull;
+      }
+#pragma unroll 1
+      for (int r = r0; r < r1; r++) {
+        const int e = r * 32 + lane;
+        if (!((m >> e) & 1ull)) continue;
+        const int lx = (s & 1) * 4 + (e & 3), ly = ((s >> 1) & 1) * 4 + ((e >> 2) & 3), lz = ((s >> 2) & 1) * 4 + (e >> 4);
+        a.pvals[(size_t)slot * 512 + (uint32_t)(lx | (ly << 3) | (lz << 6))] =
+            paint_voxel<MODE>(a, O, bx, by, bz, bo, lx, ly, lz, resc, viol);
+      }
     }
   }
 #pragma unroll
