@@ -341,9 +341,9 @@ def serving_section(args, pyoracle):
 # the evaluation kernels (classify, sub-block, the four voxel kernels, paint,
 # apply) with caches flushed before each kernel, and of all 16 kernels of the
 # build, flushed before each and left alone (the run's first build)
-EVAL_TRAFFIC_BYTES = 33_970_000
-BUILD_TRAFFIC_COLD_BYTES = 93_770_000
-BUILD_TRAFFIC_WARM_BYTES = 66_800_000
+EVAL_TRAFFIC_BYTES = 33_108_992
+BUILD_TRAFFIC_COLD_BYTES = 93_007_616
+BUILD_TRAFFIC_WARM_BYTES = 74_451_968
 
 
 def hbm_line(cfg, pool_used, ir_bytes, ms, derived_bytes=0):
