@@ -1407,7 +1407,7 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
         }
         if (set_u >= 0) {  // setBrickUniform (VoxelWorld.ts:89-97)
           if (state == ST_MIXED) {
-            if (lane == 0) { a.evt[pair] = 2; a.evt_cnt[pair] = 1; a.fsrc[pair] = src; }
+            if (lane == 0) { a.evt[pair] = 2; a.fsrc[pair] = src; }
             wc.free_++;
           }
           const uint32_t v = (uint32_t)set_u;
@@ -1520,7 +1520,7 @@ __global__ void __launch_bounds__(256, PX_FOLD_MINB) fold_kernel(FoldArgs a) {
           state = v0 == 0 ? ST_EMPTY : ST_UNIF;
           uval = v0; src = -1;
         }
-        if (lane == 0) { a.evt[pair] = ev; a.evt_cnt[pair] = (uint32_t)__popc(ev & 3u); }
+        if (lane == 0) a.evt[pair] = ev;
       };
 
       // entries 0..7 of the tile list, looked up above by lanes 8j..8j+7
@@ -1629,30 +1629,28 @@ void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEve
 // ---------------------------------------------------------------------------
 // scan building blocks of the allocator replay's single-pass look-back scans
 
-__device__ __forceinline__ uint32_t shfl_up_any(uint32_t v, int o) { return __shfl_up_sync(FULLMASK, v, o); }
-__device__ __forceinline__ int32_t shfl_up_any(int32_t v, int o) { return __shfl_up_sync(FULLMASK, v, o); }
-__device__ __forceinline__ int2 shfl_up_any(int2 v, int o) {
-  return make_int2(__shfl_up_sync(FULLMASK, v.x, o), __shfl_up_sync(FULLMASK, v.y, o));
+__device__ __forceinline__ int4 shfl_up_any(int4 v, int o) {
+  return make_int4(__shfl_up_sync(FULLMASK, v.x, o), __shfl_up_sync(FULLMASK, v.y, o), __shfl_up_sync(FULLMASK, v.z, o),
+                   0);
 }
-__device__ __forceinline__ uint32_t shfl_any(uint32_t v, int l) { return __shfl_sync(FULLMASK, v, l); }
-__device__ __forceinline__ int32_t shfl_any(int32_t v, int l) { return __shfl_sync(FULLMASK, v, l); }
-__device__ __forceinline__ int2 shfl_any(int2 v, int l) {
-  return make_int2(__shfl_sync(FULLMASK, v.x, l), __shfl_sync(FULLMASK, v.y, l));
+__device__ __forceinline__ int4 shfl_any(int4 v, int l) {
+  return make_int4(__shfl_sync(FULLMASK, v.x, l), __shfl_sync(FULLMASK, v.y, l), __shfl_sync(FULLMASK, v.z, l), 0);
 }
 
-struct SumOp {
-  typedef uint32_t T;
-  __device__ static T identity() { return 0u; }
-  __device__ static T combine(T a, T b) { return a + b; }
+// A run of events: x its count, (y, z) = (a, c) its clamped stack-depth map:
+// after the run, a stack of depth d has depth max(c, d + a).  Applying x then y
+// gives (x.a + y.a, max(y.c, x.c + y.a)).  A push is (1, -inf); a pop is
+// (-1, 0): on an empty stack it allocates a fresh brick instead.
+struct EventOp {
+  typedef int4 T;
+  __device__ static T identity() { return make_int4(0, 0, -(1 << 30), 0); }
+  __device__ static T combine(T x, T y) { return make_int4(x.x + y.x, x.y + y.y, max(y.z, x.z + y.y), 0); }
+  __device__ static T push() { return make_int4(1, 1, -(1 << 30), 0); }
+  __device__ static T pop() { return make_int4(1, -1, 0, 0); }
 };
-// Clamped stack depth: after an event the depth is max(c, d + a).  Applying x
-// then y gives (x.a + y.a, max(y.c, x.c + y.a)).  A push is (1, -inf); a pop
-// that finds the stack empty allocates a fresh brick instead: (-1, 0).
-struct DepthOp {
-  typedef int2 T;
-  __device__ static T identity() { return make_int2(0, -(1 << 30)); }
-  __device__ static T combine(T x, T y) { return make_int2(x.x + y.x, max(y.y, x.y + y.x)); }
-};
+// Min-tree entries before any event (the byte value 0x7f of their clear),
+// above every depth.
+constexpr int32_t NO_DEPTH = 0x7f7f7f7f;
 
 // Exclusive scan of one value per thread across the block; returns the
 // thread's exclusive prefix and the block total.
@@ -1700,22 +1698,19 @@ __device__ __forceinline__ void scan_publish(T* slot, uint32_t* flag, T v, uint3
   __threadfence();
   *(volatile uint32_t*)flag = f;
 }
-__device__ __forceinline__ int2 scan_peek(const int2* p) { return __ldcg(p); }
-__device__ __forceinline__ uint32_t scan_peek(const uint32_t* p) { return __ldcg(p); }
-__device__ __forceinline__ int32_t scan_peek(const int32_t* p) { return __ldcg(p); }
+__device__ __forceinline__ int4 scan_peek(const int4* p) { return __ldcg(p); }
 
 // ---------------------------------------------------------------------------
 // replay of the LIFO pool allocator (VoxelWorld.ts:112-127) over the build's
 // alloc/free events in (op, cell) order -- the order of the reference's loop --
-// in four kernels:
-//   scan_events   the event positions of the (op, brick) pairs (a single-pass
-//                 scan of their event counts) and the events themselves: a pop
-//                 per allocation, a push per free, the H holes before the build
-//                 as the first pushes;
-//   depth_scan    the stack depth after each event (a clamped prefix scan: a
-//                 pop that finds the stack empty takes poolUsed++ instead), the
-//                 rank of those fresh allocations (a second look-back, chained
-//                 after the first) and the min tree over the depths;
+// in three kernels:
+//   event_scan    one look-back scan over the (op, brick) pairs: the position
+//                 of each pair's events, the events themselves (a pop per
+//                 allocation, a push per free, the H holes before the build as
+//                 the first pushes), the stack depth after each event (a
+//                 clamped prefix scan: a pop that finds the stack empty takes
+//                 poolUsed++ instead, its rank read off the same scan) and the
+//                 min tree over the depths;
 //   match         each event's link towards its pool index: a pop at depth D
 //                 takes the push that last filled slot D (the event after the
 //                 last earlier event of depth < D, found in the min tree); a
@@ -1775,180 +1770,138 @@ __device__ typename Op::T lookback(uint32_t tile, typename Op::T total, typename
   return prefix;
 }
 
-__global__ void __launch_bounds__(RP_THREADS) scan_events_kernel(ReplayArgs a) {
-  pdl_prologue();
-  __shared__ uint32_t sh[32];
-  __shared__ uint32_t s_prefix, s_tile;
-  const uint32_t H = __ldcg(&a.state->n_holes);  // the committed state: no build writes it until this one commits
-  if (threadIdx.x == 0) s_tile = atomicAdd(&a.t.counters[0], 1u);
-  __syncthreads();
-  const uint32_t tile = s_tile;
-  const size_t P = a.P, n_tiles = (P + REPLAY_TILE - 1) / REPLAY_TILE;
-  if (tile == 0 && threadIdx.x == 0) {
-    a.res->h_before = H;
-    a.res->u_before = __ldcg(&a.state->pool_used);
-    if (P == 0) a.res->n_events = H;
-  }
-  if (tile < n_tiles) {
-    const size_t k0 = (size_t)tile * REPLAY_TILE + (size_t)threadIdx.x * RP_ITEMS;
-    uint32_t c[RP_ITEMS], acc = 0;
-    if (k0 + RP_ITEMS <= P) {  // 32-byte aligned runs
-      const uint4 u0 = reinterpret_cast<const uint4*>(a.cnt + k0)[0], u1 = reinterpret_cast<const uint4*>(a.cnt + k0)[1];
-      c[0] = u0.x; c[1] = u0.y; c[2] = u0.z; c[3] = u0.w; c[4] = u1.x; c[5] = u1.y; c[6] = u1.z; c[7] = u1.w;
-    } else {
-#pragma unroll
-      for (int j = 0; j < RP_ITEMS; j++) c[j] = k0 + j < P ? a.cnt[k0 + j] : 0u;
-    }
-#pragma unroll
-    for (int j = 0; j < RP_ITEMS; j++) acc += c[j];
-    uint32_t total;
-    const uint32_t pre_block = block_exclusive<SumOp>(acc, sh, total);
-    if (threadIdx.x < 32) {
-      const uint32_t pf = lookback<SumOp>(tile, total, a.t.p_agg, a.t.p_incl, a.t.p_flag, &a.res->status);
-      if (threadIdx.x == 0) s_prefix = pf;
-    }
-    __syncthreads();
-    uint32_t pos = s_prefix + pre_block;
-#pragma unroll
-    for (int j = 0; j < RP_ITEMS; j++) {
-      const size_t k = k0 + j;
-      if (k >= P) break;
-      a.pos[k] = pos;
-      if (c[j]) {
-        const uint32_t ev = a.evt[k];
-        const size_t e0 = (size_t)H + pos;
-        if (ev & 1u) {  // editableBrick -> allocBrick: a pop
-          a.etype[e0] = EV_POP;
-          a.ew[e0] = 0;
-        }
-        if (ev & 2u) {  // setBrickUniform / compactCell: a push of the brick's index
-          const size_t e1 = e0 + (ev & 1u);
-          const long long src = a.fsrc[k];
-          a.etype[e1] = EV_PUSH;
-          a.ew[e1] = src >= 0 ? PAIRREF | (unsigned long long)src : KNOWN | (unsigned long long)(-(src + 1));
-        }
-      }
-      pos += c[j];
-      if (k == P - 1) a.res->n_events = H + pos;
-    }
-  }
-  // the holes before the build: the first H pushes, known indices (every block takes a share)
-  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < H; i += (size_t)gridDim.x * blockDim.x) {
-    a.etype[i] = EV_PUSH;
-    a.ew[i] = KNOWN | a.holes_in[i];
-  }
-}
-
 __device__ __forceinline__ size_t level_size(size_t E, int l) {
   size_t n = E;
   for (int i = 0; i < l; i++) n = (n + 31) >> 5;
   return n;
 }
 
-__global__ void __launch_bounds__(RP_THREADS) depth_scan_kernel(ReplayArgs a) {
+// The replay's first kernel: one single-pass look-back over the (op, brick)
+// pairs whose tile aggregate is an EventOp -- the tile's event count and the
+// depth map of its events -- so that each thread knows, for its pairs, the
+// position of their events and the stack as they find it.  It writes the
+// events (a pop per allocation, a push per free, the H holes before the build
+// as the first pushes), the depth after each event, the fresh allocations'
+// pool indices (a pop on the empty stack takes poolUsed + the number of fresh
+// allocations before it, which is max(c - a, 0) of the depth map of all events
+// before it) and the min tree: levels 1 and 2 by atomicMin on entries cleared
+// to NO_DEPTH (an entry's events may come from two tiles), the levels above by
+// the block that finishes last.
+__global__ void __launch_bounds__(RP_THREADS) event_scan_kernel(ReplayArgs a) {
   pdl_prologue();
-  __shared__ int2 shd[32];
-  __shared__ uint32_t shf[32];
-  __shared__ int32_t s_wmin[RP_THREADS / 32];
-  __shared__ int2 s_dpre;
-  __shared__ uint32_t s_fpre, s_tile;
+  __shared__ int4 sh[32];
+  __shared__ int4 s_prefix;
+  __shared__ uint32_t s_tile;
   __shared__ bool s_last;
-  const size_t E = a.res->n_events;
-  const uint32_t U0 = a.res->u_before;
-  if (threadIdx.x == 0) s_tile = atomicAdd(&a.t.counters[1], 1u);
+  // the committed state: no build writes it until this one commits
+  const uint32_t H = __ldcg(&a.state->n_holes), U0 = __ldcg(&a.state->pool_used);
+  if (threadIdx.x == 0) s_tile = atomicAdd(&a.t.counters[0], 1u);
   __syncthreads();
   const uint32_t tile = s_tile;
-  const size_t n_tiles = (E + REPLAY_TILE - 1) / REPLAY_TILE;
-  if (tile >= n_tiles) return;
+  const size_t P = a.P, n_tiles = (P + REPLAY_TILE - 1) / REPLAY_TILE;
+  int32_t* const L1 = a.tl.n >= 1 ? a.tree + a.tl.off[0] : nullptr;
+  int32_t* const L2 = a.tl.n >= 2 ? a.tree + a.tl.off[1] : nullptr;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const size_t k0 = (size_t)tile * REPLAY_TILE + (size_t)threadIdx.x * RP_ITEMS;
-  uint8_t ty[RP_ITEMS];
-  if (k0 + RP_ITEMS <= E) {
-    const uint2 u = *reinterpret_cast<const uint2*>(a.etype + k0);
-#pragma unroll
-    for (int j = 0; j < RP_ITEMS; j++) ty[j] = (uint8_t)(((j < 4 ? u.x : u.y) >> (8 * (j & 3))) & 0xffu);
-  } else {
-#pragma unroll
-    for (int j = 0; j < RP_ITEMS; j++) ty[j] = k0 + j < E ? a.etype[k0 + j] : EV_NONE;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    a.res->h_before = H;
+    a.res->u_before = U0;
+    if (P == 0) { a.res->n_events = H; a.res->n_fresh = 0; }
   }
-  // a push is (1, -inf); a pop (-1, 0): on an empty stack it takes a fresh brick
-  auto depth_map = [](uint8_t t) {
-    return t == EV_PUSH ? make_int2(1, -(1 << 30)) : t == EV_POP ? make_int2(-1, 0) : DepthOp::identity();
-  };
-  int2 acc = DepthOp::identity();
+  if (tile < n_tiles) {
+    const size_t k0 = (size_t)tile * REPLAY_TILE + (size_t)threadIdx.x * RP_ITEMS;
+    uint32_t ev8[2] = {0u, 0u};  // the event codes of the thread's 8 pairs, a byte each
+    if (k0 + RP_ITEMS <= P) {
+      const uint2 u = *reinterpret_cast<const uint2*>(a.evt + k0);
+      ev8[0] = u.x; ev8[1] = u.y;
+    } else {
 #pragma unroll
-  for (int j = 0; j < RP_ITEMS; j++) acc = DepthOp::combine(acc, depth_map(ty[j]));
-  int2 total;
-  const int2 pre_block = block_exclusive<DepthOp>(acc, shd, total);
-  if (threadIdx.x < 32) {
-    const int2 pf = lookback<DepthOp>(tile, total, a.t.d_agg, a.t.d_incl, a.t.d_flag, &a.res->status);
-    if (threadIdx.x == 0) s_dpre = pf;
-  }
-  __syncthreads();
-  int2 run = DepthOp::combine(s_dpre, pre_block);  // the events before this thread's first
-  int dprev = max(run.y, run.x);                     // applied to the empty stack
-  int32_t dep[RP_ITEMS];
-  uint32_t fresh = 0;
+      for (int j = 0; j < RP_ITEMS; j++)
+        if (k0 + j < P) ev8[j >> 2] |= (uint32_t)a.evt[k0 + j] << (8 * (j & 3));
+    }
+    int4 acc = EventOp::identity();
 #pragma unroll
-  for (int j = 0; j < RP_ITEMS; j++) {
-    run = DepthOp::combine(run, depth_map(ty[j]));
-    dep[j] = max(run.y, run.x);
-    if (ty[j] == EV_POP && dprev == 0) fresh |= 1u << j;
-    dprev = dep[j];
-  }
-  // the fresh allocations' ranks: a second look-back, after this tile's depths
-  const uint32_t nfr = __popc(fresh);
-  uint32_t ftotal;
-  const uint32_t fpre_block = block_exclusive<SumOp>(nfr, shf, ftotal);
-  if (threadIdx.x < 32) {
-    const uint32_t pf = lookback<SumOp>(tile, ftotal, a.t.f_agg, a.t.f_incl, a.t.f_flag, &a.res->status);
-    if (threadIdx.x == 0) s_fpre = pf;
-  }
-  __syncthreads();
-  uint32_t rank = s_fpre + fpre_block;
-  if (tile == n_tiles - 1 && threadIdx.x == RP_THREADS - 1) a.res->n_fresh = rank + nfr;
+    for (int j = 0; j < RP_ITEMS; j++) {
+      const uint32_t ev = (ev8[j >> 2] >> (8 * (j & 3))) & 3u;
+      if (ev & 1u) acc = EventOp::combine(acc, EventOp::pop());
+      if (ev & 2u) acc = EventOp::combine(acc, EventOp::push());
+    }
+    int4 total;
+    const int4 pre_block = block_exclusive<EventOp>(acc, sh, total);
+    if (threadIdx.x < 32) {
+      const int4 pf = lookback<EventOp>(tile, total, a.t.agg, a.t.incl, a.t.flag, &a.res->status);
+      if (threadIdx.x == 0) s_prefix = pf;
+    }
+    __syncthreads();
+    // the events before this thread's first: the H holes (pushes), then those of the earlier pairs
+    int4 run = EventOp::combine(make_int4(0, (int)H, -(1 << 30), 0), EventOp::combine(s_prefix, pre_block));
+    uint32_t pos = (uint32_t)run.x;  // events of the pairs before k0 (after the holes)
+    const uint32_t B0 = __shfl_sync(FULLMASK, H + pos, 0) >> 10;  // the warp's events lie in level-2 blocks B0, B0 + 1
+    int32_t m1 = NO_DEPTH, m2lo = NO_DEPTH, m2hi = NO_DEPTH;
+    long long b1 = -1;
 #pragma unroll
-  for (int j = 0; j < RP_ITEMS; j++)
-    if ((fresh >> j) & 1u) a.ew[k0 + j] = KNOWN | (unsigned long long)(U0 + rank++);
-  if (k0 + RP_ITEMS <= E) {
-    reinterpret_cast<int4*>(a.depth + k0)[0] = make_int4(dep[0], dep[1], dep[2], dep[3]);
-    reinterpret_cast<int4*>(a.depth + k0)[1] = make_int4(dep[4], dep[5], dep[6], dep[7]);
-  } else {
+    for (int j = 0; j < RP_ITEMS; j++) {
+      const size_t k = k0 + j;
+      if (k >= P) break;
+      a.pos[k] = pos;
+      const uint32_t ev = (ev8[j >> 2] >> (8 * (j & 3))) & 3u;
 #pragma unroll
-    for (int j = 0; j < RP_ITEMS; j++)
-      if (k0 + j < E) a.depth[k0 + j] = dep[j];
-  }
-  // the min tree: levels 1 (32 events, four threads) and 2 (1,024 events) of this tile
-  if (a.tl.n >= 1) {
-    int32_t m = 0x7fffffff;
-#pragma unroll
-    for (int j = 0; j < RP_ITEMS; j++)
-      if (k0 + j < E) m = min(m, dep[j]);
-    m = min(m, __shfl_xor_sync(FULLMASK, m, 1));
-    m = min(m, __shfl_xor_sync(FULLMASK, m, 2));
-    if ((threadIdx.x & 3) == 0 && k0 < E) a.tree[a.tl.off[0] + k0 / 32] = m;
-    if (a.tl.n >= 2) {
-      const int32_t wm = __reduce_min_sync(FULLMASK, m);  // 256 events
-      if (lane == 0) s_wmin[warp] = wm;
-      __syncthreads();
-      if (threadIdx.x < REPLAY_TILE / 1024) {
-        const size_t l2 = (size_t)tile * (REPLAY_TILE / 1024) + threadIdx.x;
-        if (l2 * 1024 < E) {
-          const int w0 = threadIdx.x * 4;
-          a.tree[a.tl.off[1] + l2] = min(min(s_wmin[w0], s_wmin[w0 + 1]), min(s_wmin[w0 + 2], s_wmin[w0 + 3]));
+      for (int t = 0; t < 2; t++) {
+        if (!((ev >> t) & 1u)) continue;
+        const size_t e = (size_t)H + pos;
+        if (t == 0) {  // editableBrick -> allocBrick: a pop; on the empty stack, a fresh brick
+          const bool fresh = max(run.z, run.y) == 0;
+          a.etype[e] = EV_POP;
+          a.ew[e] = fresh ? KNOWN | (unsigned long long)(U0 + (uint32_t)max(run.z - run.y, 0)) : 0ull;
+          run = EventOp::combine(run, EventOp::pop());
+        } else {  // setBrickUniform / compactCell: a push of the brick's index
+          const long long src = a.fsrc[k];
+          a.etype[e] = EV_PUSH;
+          a.ew[e] = src >= 0 ? PAIRREF | (unsigned long long)src : KNOWN | (unsigned long long)(-(src + 1));
+          run = EventOp::combine(run, EventOp::push());
         }
+        const int32_t d = max(run.z, run.y);
+        a.depth[e] = d;
+        if ((long long)(e >> 5) != b1) {
+          if (b1 >= 0 && L1) atomicMin(L1 + b1, m1);
+          b1 = (long long)(e >> 5);
+          m1 = d;
+        } else {
+          m1 = min(m1, d);
+        }
+        if ((uint32_t)(e >> 10) == B0) m2lo = min(m2lo, d);
+        else m2hi = min(m2hi, d);
+        pos++;
       }
     }
+    if (b1 >= 0 && L1) atomicMin(L1 + b1, m1);
+    if (L2) {
+      const int32_t lo = __reduce_min_sync(FULLMASK, m2lo), hi = __reduce_min_sync(FULLMASK, m2hi);
+      if (lane == 0 && lo != NO_DEPTH) atomicMin(L2 + B0, lo);
+      if (lane == 0 && hi != NO_DEPTH) atomicMin(L2 + B0 + 1, hi);
+    }
+    if (tile == n_tiles - 1 && threadIdx.x == RP_THREADS - 1) {
+      a.res->n_events = H + pos;
+      a.res->n_fresh = (uint32_t)max(run.z - run.y, 0);
+    }
   }
-  // the levels above: by the tile that finishes last
+  // the holes before the build: the first H pushes, known indices, depth i + 1 (every block takes a share)
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < H; i += (size_t)gridDim.x * blockDim.x) {
+    a.etype[i] = EV_PUSH;
+    a.ew[i] = KNOWN | a.holes_in[i];
+    a.depth[i] = (int32_t)(i + 1);
+    if (L1 && (i & 31) == 0) atomicMin(L1 + (i >> 5), (int32_t)(i + 1));  // a block's smallest hole depth
+    if (L2 && (i & 1023) == 0) atomicMin(L2 + (i >> 10), (int32_t)(i + 1));
+  }
+  // the levels above 2: by the block that finishes last
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
-    s_last = atomicAdd(&a.t.counters[2], 1u) == (uint32_t)(n_tiles - 1);
+    s_last = atomicAdd(&a.t.counters[2], 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (!s_last) return;
+  if (!s_last || a.tl.n < 3) return;
   __threadfence();
+  const size_t E = __ldcg(&a.res->n_events);
   for (int l = 3; l <= a.tl.n; l++) {
     const size_t nb = level_size(E, l - 1), n = level_size(E, l);
     const int32_t* below = a.tree + a.tl.off[l - 2];
@@ -2030,10 +1983,11 @@ __device__ bool next_less_exists(const int32_t* depth, const int32_t* tree, cons
   }
 }
 
-// Each event's link towards its pool index: a pop (not fresh) points to the push
-// that last filled its slot, a push of a brick allocated in this build to that
-// allocation's pop; fresh pops, old indices and the holes before the build are
-// known already.  Links always lead to earlier events; finalize follows them.
+// Each event's link towards its pool index: a pop (not fresh) takes the value of
+// the push that last filled its slot (it links past that push), a push of a brick
+// allocated in this build links to that allocation's pop; fresh pops, old indices
+// and the holes before the build are known already.  Links always lead to
+// earlier events; resolve follows them.
 // A push that no later event undercuts is the hole of its slot after the build:
 // holes_out[slot] receives the push's event index (finalize turns it into the
 // pool index).
@@ -2053,7 +2007,12 @@ __global__ void __launch_bounds__(256) match_events_kernel(ReplayArgs a) {
       if (!next_less_exists(a.depth, a.tree, a.tl, E, e, d)) a.holes_out[d - 1] = (uint32_t)e;
     } else if (!(w & KNOWN)) {
       const int D = e ? a.depth[e - 1] : 0;  // >= 1: a pop at depth 0 is fresh, known already
-      a.ew[e] = (unsigned long long)(prev_less(a.depth, a.tree, a.tl, E, e, D) + 1);  // the push that filled slot D
+      const size_t p = (size_t)(prev_less(a.depth, a.tree, a.tl, E, e, D) + 1);  // the push that filled slot D
+      // the pop takes that push's value: link past the push, to its known index or to its
+      // brick's allocation (an earlier pop).  The push's word is read while this kernel may
+      // be rewriting it, so it comes in either form.
+      const unsigned long long q = __ldcg(a.ew + p);
+      a.ew[e] = (q & KNOWN) ? q : (q & PAIRREF) ? (unsigned long long)H + a.pos[q & ~PAIRREF] : q;
     }
   }
 }
@@ -2095,42 +2054,37 @@ TreeLevels tree_levels(size_t E_max) {
   return tl;
 }
 
+size_t tree_clear_bytes(size_t E_max) {
+  size_t n = E_max, off = 0;
+  for (int l = 0; l < 2 && n > 32; l++) {  // levels 1 and 2, laid out as tree_levels lays them out
+    n = (n + 31) / 32;
+    off += (n + 31) & ~(size_t)31;
+  }
+  return 4 * off;
+}
+
 static size_t al16(size_t b) { return (b + 15) & ~(size_t)15; }
-// layout: counters[8], p_flag, d_flag, f_flag (cleared); p_agg, p_incl, d_agg, d_incl, f_agg, f_incl
-ReplayTemp replay_temp(void* base, uint64_t P, size_t E_max) {
-  const size_t tp = P / REPLAY_TILE + 2, te = E_max / REPLAY_TILE + 2;
+// layout: counters[8], flags (cleared); aggregates, inclusive prefixes
+ReplayTemp replay_temp(void* base, uint64_t P) {
+  const size_t tp = P / REPLAY_TILE + 2;
   char* c = (char*)base;
   ReplayTemp t;
   t.counters = (uint32_t*)c; c += 32;
-  t.p_flag = (uint32_t*)c; c += al16(4 * tp);
-  t.d_flag = (uint32_t*)c; c += al16(4 * te);
-  t.f_flag = (uint32_t*)c; c += al16(4 * te);
-  t.p_agg = (uint32_t*)c; c += al16(4 * tp);
-  t.p_incl = (uint32_t*)c; c += al16(4 * tp);
-  t.d_agg = (int2*)c; c += al16(8 * te);
-  t.d_incl = (int2*)c; c += al16(8 * te);
-  t.f_agg = (uint32_t*)c; c += al16(4 * te);
-  t.f_incl = (uint32_t*)c; c += al16(4 * te);
+  t.flag = (uint32_t*)c; c += al16(4 * tp);
+  t.agg = (int4*)c; c += 16 * tp;
+  t.incl = (int4*)c;
   return t;
 }
-size_t replay_clear_bytes(uint64_t P, size_t E_max) {
-  const size_t tp = P / REPLAY_TILE + 2, te = E_max / REPLAY_TILE + 2;
-  return 32 + al16(4 * tp) + 2 * al16(4 * te);
-}
-size_t replay_temp_bytes(uint64_t P, size_t E_max) {
-  const size_t tp = P / REPLAY_TILE + 2, te = E_max / REPLAY_TILE + 2;
-  return replay_clear_bytes(P, E_max) + 2 * al16(4 * tp) + 2 * al16(8 * te) + 2 * al16(4 * te);
-}
+size_t replay_clear_bytes(uint64_t P) { return 32 + al16(4 * (P / REPLAY_TILE + 2)); }
+size_t replay_temp_bytes(uint64_t P) { return replay_clear_bytes(P) + 32 * (P / REPLAY_TILE + 2); }
 
 void launch_replay(const ReplayArgs& a, cudaStream_t s) {
   int dev = 0, n_sms = 152;
   if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&n_sms, cudaDevAttrMultiProcessorCount, dev);
   const size_t p_tiles = (a.P + REPLAY_TILE - 1) / REPLAY_TILE;
   const size_t h_blocks = std::min<size_t>(((size_t)a.H_max + RP_THREADS - 1) / RP_THREADS, (size_t)n_sms * 4);
-  launch_pdl(scan_events_kernel, dim3((unsigned)std::max<size_t>(1, std::max(p_tiles, h_blocks))), dim3(RP_THREADS), 0,
+  launch_pdl(event_scan_kernel, dim3((unsigned)std::max<size_t>(1, std::max(p_tiles, h_blocks))), dim3(RP_THREADS), 0,
              s, a);
-  const size_t e_tiles = (a.E_max + REPLAY_TILE - 1) / REPLAY_TILE;
-  launch_pdl(depth_scan_kernel, dim3((unsigned)std::max<size_t>(1, e_tiles)), dim3(RP_THREADS), 0, s, a);
   const size_t rb = std::min<size_t>((a.E_max + 255) / 256, (size_t)n_sms * 8);
   launch_pdl(match_events_kernel, dim3((unsigned)std::max<size_t>(1, rb)), dim3(256), 0, s, a);
   launch_pdl(resolve_events_kernel, dim3((unsigned)std::max<size_t>(1, rb)), dim3(256), 0, s, a);
@@ -2354,10 +2308,10 @@ __global__ void __launch_bounds__(256) upload_kernel(HostUploads u) {
   const uint4* src = reinterpret_cast<const uint4*>(e.src);
   uint4* dst = reinterpret_cast<uint4*>(e.dst);
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += (size_t)gridDim.x * blockDim.x)
-    dst[i] = src ? src[i] : make_uint4(0u, 0u, 0u, 0u);
+    dst[i] = src ? src[i] : make_uint4(e.fill, e.fill, e.fill, e.fill);
   if (blockIdx.x == 0 && threadIdx.x < (e.bytes & 15u)) {
     const size_t k = (n16 << 4) + threadIdx.x;
-    static_cast<unsigned char*>(e.dst)[k] = src ? static_cast<const unsigned char*>(e.src)[k] : (unsigned char)0;
+    static_cast<unsigned char*>(e.dst)[k] = src ? static_cast<const unsigned char*>(e.src)[k] : (unsigned char)e.fill;
   }
 }
 void launch_uploads(const HostUploads& u, cudaStream_t s) {

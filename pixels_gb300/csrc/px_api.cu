@@ -63,6 +63,7 @@ struct Upload {
   void* dst;
   const void* src;
   size_t bytes;
+  uint8_t fill = 0;  // without a source: the byte value of the clear
 };
 
 }  // namespace
@@ -107,7 +108,7 @@ struct px_world {
   std::vector<uint32_t> h_cull_order;  // the ops along a Morton curve of their boxes (cull_sorted_kernel)
   bool cull_sorted = false;
   DevBuf tile_cnt, tile_off, tile_ops, tile_boxes;
-  DevBuf evt, fsrc, cnt, pos, etype, ew, depth, tree, replay_tmp;
+  DevBuf evt, fsrc, pos, etype, ew, depth, tree, replay_tmp;
   DevBuf staging, stage_cell, stage_src, touched;
   uint64_t stage_hint = 0;      // staging slots the next build reserves (grown on overflow)
   uint32_t rescue_cap = 1u << 16;  // voxels a build may leave to float64 (grown on overflow)
@@ -691,7 +692,7 @@ void px_world_destroy(px_world* w) {
   }
   DevBuf* bufs[] = {&w->holes_a, &w->holes_b, &w->d_ops, &w->d_boxes, &w->d_code, &w->d_params, &w->d_code32,
                     &w->d_p32, &w->d_bases, &w->tile_cnt,
-                    &w->tile_off, &w->tile_ops, &w->evt, &w->fsrc, &w->cnt, &w->pos, &w->etype,
+                    &w->tile_off, &w->tile_ops, &w->evt, &w->fsrc, &w->pos, &w->etype,
                     &w->ew, &w->replay_tmp, &w->depth, &w->tree, &w->staging, &w->touched,
                     &w->stage_cell, &w->stage_src, &w->chunk_op, &w->pcode, &w->psub, &w->pmask,
                     &w->chunk_counter, &w->vitems, &w->work_counter, &w->res, &w->opaque,
@@ -1161,9 +1162,9 @@ int ensure_pair_scratch(px_world* w, uint64_t P, uint64_t tile_pairs, uint64_t n
   int rc;
   if ((rc = ensure(w, w->tile_cnt, 4 * w->ntiles)) || (rc = ensure(w, w->tile_off, 4 * w->ntiles)) ||
       (rc = ensure(w, w->tile_ops, 4 * tile_pairs)) || (rc = ensure(w, w->tile_boxes, 8 * tile_pairs)) ||
-      (rc = ensure(w, w->evt, P)) || (rc = ensure(w, w->fsrc, 8 * P)) || (rc = ensure(w, w->cnt, 4 * P)) ||
+      (rc = ensure(w, w->evt, P)) || (rc = ensure(w, w->fsrc, 8 * P)) ||
       (rc = ensure(w, w->pos, 4 * P)) || (rc = ensure(w, w->etype, E_max)) || (rc = ensure(w, w->ew, 8 * E_max)) ||
-      (rc = ensure(w, w->replay_tmp, replay_temp_bytes(P, E_max))) || (rc = ensure(w, w->depth, 4 * (E_max + 32))) ||
+      (rc = ensure(w, w->replay_tmp, replay_temp_bytes(P))) || (rc = ensure(w, w->depth, 4 * (E_max + 32))) ||
       (rc = ensure(w, w->tree, 4 * (E_max / 16 + 512))) || (rc = ensure(w, w->staging, 1024 * stage_cap)) ||
       (rc = ensure(w, w->stage_cell, 4 * stage_cap)) || (rc = ensure(w, w->stage_src, 8 * stage_cap)) ||
       (rc = ensure(w, w->touched, 8 * touched_bound)) ||
@@ -1441,12 +1442,12 @@ static int issue_uploads(px_world* w, const std::vector<Upload>& ups, cudaStream
     const bool aligned = !(((uintptr_t)u.src | (uintptr_t)u.dst) & 15u);
     const bool by_kernel = aligned && hu.n < HostUploads::kMax && (!u.src || (w->host_reads && !w->capturing));
     if (by_kernel) {
-      hu.e[hu.n++] = {u.src, u.dst, u.bytes};
+      hu.e[hu.n++] = {u.src, u.dst, u.bytes, 0x01010101u * u.fill};
       reads_host = reads_host || u.src;
     } else if (u.src) {
       CU(cudaMemcpyAsync(u.dst, u.src, u.bytes, cudaMemcpyHostToDevice, s));
     } else {
-      CU(cudaMemsetAsync(u.dst, 0, u.bytes, s));
+      CU(cudaMemsetAsync(u.dst, u.fill, u.bytes, s));
     }
   }
   if (hu.n) {
@@ -1643,9 +1644,9 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   ups.push_back({w->work_counter.p, nullptr, 16});
   ups.push_back({w->chunk_counter.p, nullptr, 1024});
   ups.push_back({w->evt.p, nullptr, P});
-  ups.push_back({w->cnt.p, nullptr, 4 * P});  // events per pair, written by the apply pass
   ups.push_back({w->bmark.p, nullptr, 4 * ((w->ncells + 31) / 32)});
-  ups.push_back({w->replay_tmp.p, nullptr, replay_clear_bytes(P, E_max)});  // the replay's tickets and look-back flags
+  ups.push_back({w->replay_tmp.p, nullptr, replay_clear_bytes(P)});  // the replay's tickets and look-back flags
+  ups.push_back({w->tree.p, nullptr, tree_clear_bytes(E_max), 0x7f});  // min-tree levels 1 and 2, above every depth
   if ((rc = issue_uploads(w, ups, s))) return rc;  // the op tables; the chunk order follows the cull launches
 
   BuildResult* res = (BuildResult*)w->res.p;
@@ -1781,7 +1782,6 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   fa.grid = w->d_grid;
   fa.pool32 = w->d_pool32;
   fa.evt = (uint8_t*)w->evt.p;
-  fa.evt_cnt = (uint32_t*)w->cnt.p;
   fa.fsrc = (int64_t*)w->fsrc.p;
   fa.staging32 = (uint32_t*)w->staging.p;
   fa.stage_cap = (uint32_t)stage_cap;
@@ -1803,7 +1803,6 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   ra.evt = (const uint8_t*)w->evt.p;
   ra.fsrc = (const int64_t*)w->fsrc.p;
   ra.holes_in = (const uint32_t*)holes_in.p;
-  ra.cnt = (const uint32_t*)w->cnt.p;
   ra.pos = (uint32_t*)w->pos.p;
   ra.etype = (uint8_t*)w->etype.p;
   ra.ew = (unsigned long long*)w->ew.p;
@@ -1812,7 +1811,7 @@ static int build_enqueue_impl(px_world* w, int mode, void* stream) {
   ra.tl = tree_levels(E_max);
   ra.holes_out = (uint32_t*)holes_out.p;
   ra.res = res;
-  ra.t = replay_temp(w->replay_tmp.p, P, E_max);
+  ra.t = replay_temp(w->replay_tmp.p, P);
   launch_replay(ra, s);
 
   FinalizeArgs& fn = w->fin;

@@ -244,8 +244,7 @@ struct FoldArgs {
   double vs;
   uint32_t* grid;
   const uint32_t* pool32;     // pool viewed as voxel pairs
-  uint8_t* evt;               // per pair: 1 = alloc, 2 = free
-  uint32_t* evt_cnt;          // per pair: its number of events (the allocator replay scans these)
+  uint8_t* evt;               // per pair: 1 = alloc, 2 = free, 3 = both
   int64_t* fsrc;              // per pair with a free: pair of the brick's last alloc, or -(old index + 1)
   uint32_t* staging32;
   uint32_t stage_cap;
@@ -276,31 +275,29 @@ void launch_fold(const FoldArgs& a, int mode, int n_sms, cudaStream_t s, cudaEve
 
 
 
-// The allocator replay's look-back scratch: flags and counters (cleared by
-// every build: replay_clear_bytes from `flags`) and the published aggregates.
+// The allocator replay's look-back scratch: counters and flags (cleared by
+// every build: replay_clear_bytes from `counters`) and the published tile
+// aggregates and inclusive prefixes (event count and depth map, x/y/z).
 struct ReplayTemp {
-  uint32_t* counters;  // [0] pair-tile tickets, [1] event-tile tickets, [2] event tiles done
-  uint32_t* p_flag;    // per pair tile (0 pending, 1 aggregate, 2 prefix)
-  uint32_t* d_flag;    // per event tile, depth maps
-  uint32_t* f_flag;    // per event tile, fresh-allocation counts
-  uint32_t* p_agg;
-  uint32_t* p_incl;
-  int2* d_agg;
-  int2* d_incl;
-  uint32_t* f_agg;
-  uint32_t* f_incl;
+  uint32_t* counters;  // [0] pair-tile tickets, [2] blocks done
+  uint32_t* flag;      // per pair tile (0 pending, 1 aggregate, 2 prefix)
+  int4* agg;
+  int4* incl;
 };
-constexpr int REPLAY_TILE = 4096;  // pairs or events per look-back tile (512 threads x 8)
-// bytes of the replay scratch for P pairs and E_max events, and of its cleared part
-size_t replay_temp_bytes(uint64_t P, size_t E_max);
-size_t replay_clear_bytes(uint64_t P, size_t E_max);
-ReplayTemp replay_temp(void* base, uint64_t P, size_t E_max);
+constexpr int REPLAY_TILE = 4096;  // pairs per look-back tile (512 threads x 8)
+// bytes of the replay scratch for P pairs, and of its cleared part
+size_t replay_temp_bytes(uint64_t P);
+size_t replay_clear_bytes(uint64_t P);
+ReplayTemp replay_temp(void* base, uint64_t P);
 
 struct TreeLevels {
   size_t off[8];  // offsets (in int32) of levels 1.. in the tree buffer
   int n;          // levels above the depth array
 };
 TreeLevels tree_levels(size_t E_max);
+// bytes of levels 1 and 2 of the min tree, which every build clears to the
+// byte value 0x7f before the replay fills them by atomicMin
+size_t tree_clear_bytes(size_t E_max);
 
 struct ReplayArgs {
   size_t P;                 // pairs
@@ -310,7 +307,6 @@ struct ReplayArgs {
   const uint8_t* evt;
   const int64_t* fsrc;
   const uint32_t* holes_in;
-  const uint32_t* cnt;      // P: events per pair
   uint32_t* pos;            // P: first event of each pair (after the H initial holes)
   uint8_t* etype;           // E_max
   unsigned long long* ew;   // E_max: the pool index of each event once resolved (KNOWN | index)
@@ -353,6 +349,7 @@ struct HostUploads {
     const void* src;
     void* dst;
     size_t bytes;
+    uint32_t fill;  // without a source: the byte value of the clear, in all four bytes
   } e[kMax];
   int n;
 };
