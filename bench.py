@@ -339,11 +339,11 @@ def serving_section(args, pyoracle):
 # DRAM bytes per build from one ncu capture on the penthouse at vpm=80 (the
 # bench cannot run ncu itself): dram__bytes_read.sum + dram__bytes_write.sum of
 # the evaluation kernels (classify, sub-block, the four voxel kernels, paint,
-# apply) with caches flushed before each kernel, and of all 16 kernels of the
+# apply) with caches flushed before each kernel, and of all 15 kernels of the
 # build, flushed before each and left alone (the run's first build)
-EVAL_TRAFFIC_BYTES = 33_108_992
-BUILD_TRAFFIC_COLD_BYTES = 93_007_616
-BUILD_TRAFFIC_WARM_BYTES = 74_451_968
+EVAL_TRAFFIC_BYTES = 33_319_168
+BUILD_TRAFFIC_COLD_BYTES = 91_481_600
+BUILD_TRAFFIC_WARM_BYTES = 67_701_760
 
 
 def hbm_line(cfg, pool_used, ir_bytes, ms, derived_bytes=0):
@@ -699,7 +699,7 @@ def main():
                                        "voxel (4), paint and apply kernels of one build of this workload "
                                        "(one capture, caches flushed before each kernel, --clock-control none)",
                      "build_traffic": {"cold": BUILD_TRAFFIC_COLD_BYTES, "warm": BUILD_TRAFFIC_WARM_BYTES,
-                                       "what": "all 16 kernels of one build: caches flushed before each kernel "
+                                       "what": "all 15 kernels of one build: caches flushed before each kernel "
                                                "(cold), or left alone (warm, the run's first build)"},
                      "kernel": "classify_kernel + sub_kernel + voxel_lean_kernel x3 + voxel_kernel + paint_kernel "
                                "+ fold_kernel (every SDF and paint evaluation)",

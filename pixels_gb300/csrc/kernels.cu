@@ -1842,8 +1842,8 @@ __global__ void __launch_bounds__(RP_THREADS) event_scan_kernel(ReplayArgs a) {
     for (int j = 0; j < RP_ITEMS; j++) {
       const size_t k = k0 + j;
       if (k >= P) break;
-      a.pos[k] = pos;
       const uint32_t ev = (ev8[j >> 2] >> (8 * (j & 3))) & 3u;
+      if (ev & 1u) a.pos[k] = pos;  // read only for allocations (a push's brick, a staged brick)
 #pragma unroll
       for (int t = 0; t < 2; t++) {
         if (!((ev >> t) & 1u)) continue;

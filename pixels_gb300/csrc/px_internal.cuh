@@ -307,7 +307,7 @@ struct ReplayArgs {
   const uint8_t* evt;
   const int64_t* fsrc;
   const uint32_t* holes_in;
-  uint32_t* pos;            // P: first event of each pair (after the H initial holes)
+  uint32_t* pos;            // P: first event of each pair that allocates (after the H initial holes)
   uint8_t* etype;           // E_max
   unsigned long long* ew;   // E_max: the pool index of each event once resolved (KNOWN | index)
   int32_t* depth;           // E_max (+ 32): stack depth after each event
