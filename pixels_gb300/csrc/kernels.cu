@@ -2093,6 +2093,8 @@ void launch_replay(const ReplayArgs& a, cudaStream_t s) {
 // ---------------------------------------------------------------------------
 // finalize: staging -> pool at the replayed indices, grid entries
 
+constexpr int FIN_BRICKS = 8;  // touched bricks per warp pass of finalize (at most 32)
+
 __global__ void __launch_bounds__(256) finalize_kernel(FinalizeArgs a) {
   __shared__ uint8_t op_s[256];
   op_s[threadIdx.x] = a.opaque[threadIdx.x];  // 256 threads
@@ -2119,15 +2121,17 @@ __global__ void __launch_bounds__(256) finalize_kernel(FinalizeArgs a) {
     a.holes_out[k] = (uint32_t)(__ldcg(a.ew + a.holes_out[k]) & 0xffffffffull);
   const int lane = threadIdx.x & 31;
   const uint32_t n = a.res->touched_count;
-  // 32 touched bricks per warp pass: each lane resolves one brick's pool index
-  // (a chain of dependent loads, so 32 chains in flight), then the warp copies
-  // the staged bricks four at a time (eight 16-byte loads in flight per lane)
+  // FIN_BRICKS touched bricks per warp pass: each of the first lanes resolves one
+  // brick's pool index (a chain of dependent loads), then the warp copies the
+  // staged bricks four at a time (eight 16-byte loads in flight per lane).  Few
+  // bricks per pass keep many warps' chains and copies in flight at once.
   const uint32_t n_warps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; base < n; base += n_warps * 32) {
+  for (uint32_t base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * FIN_BRICKS; base < n;
+       base += n_warps * FIN_BRICKS) {
     const uint32_t t = base + lane;
     uint32_t cell = 0, slot = 0, idx = 0;
     bool staged = false;
-    if (t < n) {
+    if (lane < FIN_BRICKS && t < n) {
       const uint2 e = a.touched[t];
       cell = e.x;
       if (!(e.y & TAG_STAGED) || (e.y & UNIFORM)) {
@@ -2209,9 +2213,12 @@ __global__ void __launch_bounds__(256) finalize_kernel(FinalizeArgs a) {
 }
 
 void launch_finalize(const FinalizeArgs& a, uint32_t touched_cap, cudaStream_t s) {
-  size_t warps = touched_cap ? (touched_cap + 31) / 32 : 1;
-  size_t b = (warps * 32 + 255) / 256;
-  int blocks = (int)(b < 8192 ? b : 8192);
+  int dev = 0, n_sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&n_sms, cudaDevAttrMultiProcessorCount, dev);
+  // a grid-stride loop over the touched bricks (their count is known on the device
+  // only): at most four blocks per SM, fewer when the bound is small
+  const size_t b = ((size_t)touched_cap + 8 * FIN_BRICKS - 1) / (8 * FIN_BRICKS);
+  const int blocks = (int)std::max<size_t>(1, std::min<size_t>(b, (size_t)n_sms * 4));
   launch_pdl(finalize_kernel, dim3(blocks), dim3(256), 0, s, a);
 }
 
