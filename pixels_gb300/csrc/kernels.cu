@@ -1723,7 +1723,7 @@ __device__ __forceinline__ int4 scan_peek(const int4* p) { return __ldcg(p); }
 constexpr unsigned long long KNOWN = 1ull << 63;    // ew: a resolved pool index
 constexpr unsigned long long PAIRREF = 1ull << 62;  // ew of a push: the pair of its brick's last allocation
 enum : uint8_t { EV_PUSH = 0, EV_POP = 1, EV_NONE = 0xff };
-constexpr int RP_THREADS = 512, RP_ITEMS = 8;
+constexpr int RP_THREADS = PX_REPLAY_THREADS, RP_ITEMS = 8;
 static_assert(RP_THREADS * RP_ITEMS == REPLAY_TILE, "a tile is one block pass");
 
 // Decoupled look-back of tile `tile`, by warp 0: publishes the tile's
@@ -2093,7 +2093,11 @@ void launch_replay(const ReplayArgs& a, cudaStream_t s) {
 // ---------------------------------------------------------------------------
 // finalize: staging -> pool at the replayed indices, grid entries
 
-constexpr int FIN_BRICKS = 8;  // touched bricks per warp pass of finalize (at most 32)
+#ifndef PX_FIN_BRICKS
+#define PX_FIN_BRICKS 8
+#endif
+constexpr int FIN_BRICKS = PX_FIN_BRICKS;  // touched bricks per warp pass of finalize (at most 32)
+static_assert(FIN_BRICKS >= 1 && FIN_BRICKS <= 32, "one brick per lane");
 
 __global__ void __launch_bounds__(256) finalize_kernel(FinalizeArgs a) {
   __shared__ uint8_t op_s[256];
