@@ -341,9 +341,9 @@ def serving_section(args, pyoracle):
 # the evaluation kernels (classify, sub-block, the four voxel kernels, paint,
 # apply) with caches flushed before each kernel, and of all 15 kernels of the
 # build, flushed before each and left alone (the run's first build)
-EVAL_TRAFFIC_BYTES = 33_319_168
-BUILD_TRAFFIC_COLD_BYTES = 91_481_600
-BUILD_TRAFFIC_WARM_BYTES = 67_701_760
+EVAL_TRAFFIC_BYTES = 33_314_048
+BUILD_TRAFFIC_COLD_BYTES = 91_652_352
+BUILD_TRAFFIC_WARM_BYTES = 65_374_208
 
 
 def hbm_line(cfg, pool_used, ir_bytes, ms, derived_bytes=0):
