@@ -6,7 +6,8 @@ collinear prisms), paints on air and paints that return air, carve/re-add
 sequences that reuse freed pool bricks in LIFO order, a world wider than
 the float32 path certifies (every op then runs in float64), unions, and CSG /
 rotation trees deeper than the register evaluators hold (shapes.ts:227-320
-put no limit on nesting).
+put no limit on nesting), and allocator churn (bricks freed and reallocated
+many times in one build, then a build that starts with holes).
 """
 import numpy as np
 import pytest
@@ -155,3 +156,58 @@ def test_union_and_deep_csg_and_rotation_trees(built_lib):
         yield 2, nested_rot(chain(4, (0.9, 0.4, 0.4)), (0.9, 0.4, 0.4), 4), tufted(0.05, 0.05, M.leather)
     o, stats = run_both(program(vpm, ops), vpm, (64, 32, 64))
     assert o.pool_used > 0
+
+
+@pytest.mark.gpu
+def test_allocator_churn_across_scan_tiles_and_builds(built_lib):
+    """The pool allocator under churn (VoxelWorld.ts:112-127): the same bricks
+    allocated, freed and allocated again many times in one build, so that pool
+    indices pass along long chains of pushes and pops, over enough (op, brick)
+    pairs for many tiles of the replay's scan; then a second build that starts
+    with holes.  The world after both builds must equal the oracle's after the
+    concatenated op list, bit for bit, in both forms."""
+    vpm = 40.0
+    dims = (96, 48, 96)
+    rng = np.random.default_rng(7)
+    centres = [tuple(float(v) for v in (rng.uniform(0.5, 1.9), rng.uniform(0.4, 0.8), rng.uniform(0.5, 1.9)))
+               for _ in range(16)]
+
+    def first():
+        for k, c in enumerate(centres):
+            yield 0, sphere(c, 0.35), vox(M.marble)                                   # allocates mixed bricks
+            yield 0, capsule((c[0] - 0.3, c[1], c[2]), (c[0] + 0.3, c[1] + 0.1, c[2]), 0.12), vox(M.gold)
+            yield 1, box(c, (0.45, 0.45, 0.45)), 0                                    # frees them all again
+            yield 0, sphere((c[0] + 0.05, c[1], c[2] - 0.05), 0.3), vox(M.oak)       # pops the freed bricks
+            if k % 3 == 2:
+                yield 1, boxMinMax(c[0] - 0.2, 0.0, c[2] - 0.2, c[0] + 0.5, 1.2, c[2] + 0.5), 0
+        yield 1, boxMinMax(0.0, 0.0, 0.0, 2.4, 1.2, 1.2), 0                           # leaves holes behind
+
+    def second():
+        for c in centres[::2]:
+            yield 0, roundBox(c, (0.3, 0.2, 0.25), 0.05), vox(M.velvet)               # pops the holes first
+            yield 1, sphere(c, 0.15), 0
+        yield 2, boxMinMax(0.0, 0.0, 0.0, 2.4, 1.2, 2.4), tufted(0.1, 0.1, M.leather)
+
+    def both():
+        yield from first()
+        yield from second()
+
+    o = pyoracle.OracleWorld(program(vpm, both).to_bytes(), vpm, dims)
+    assert o.stats["frees"] > 1000
+    for mode in (MODE_FP64, MODE_MIXED):
+        w = VoxelWorld(*dims, initialPoolBricks=4, vpm=vpm, mode=mode)
+        w._pending = program(vpm, first)
+        w.build()
+        assert w.freeBricks().size > 0  # the second build starts with holes
+        w._pending = program(vpm, second)
+        w.build()
+        np.testing.assert_array_equal(w.grid, o.grid, err_msg=f"grid, mode {mode}")
+        assert w.poolUsed == o.pool_used
+        np.testing.assert_array_equal(w.freeBricks(), o.free_holes)
+        live = np.nonzero((o.grid != 0) & ((o.grid & 0x80000000) == 0))[0]
+        idx = o.grid[live].astype(np.int64) - 1
+        np.testing.assert_array_equal(w.pool.reshape(-1, 512)[idx], o.pool.reshape(-1, 512)[idx])
+        d = w.derived()
+        np.testing.assert_array_equal(d["super"], o.super)
+        np.testing.assert_array_equal(d["density"], o.density)
+        w.close()
